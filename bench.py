@@ -1,0 +1,376 @@
+#!/usr/bin/env python
+"""bench.py -- emulated (Ozaki split-product) vs native DGEMM on one GB300.
+
+Workload (the configuration the headline metric is quoted on): DGEMM
+C := A*B with m = n = k = 16384, column-major FP64, entries (1+u)*2^e with
+e uniform in [-20, 20] and random sign, generated on the device by the
+library's seeded generator.  A "step" is one full DGEMM.
+
+  value      Ozaki DGEMM (8 bf16 slices, tcgen05) in FP64-equivalent
+             TFLOP/s (2mnk per step), operands resident in HBM, CUDA events
+             on the launching stream, K steps after W warm-up steps.
+  e2e        the same DGEMM through the BLAS entry point dgemm_ (C ABI) on
+             pinned host buffers: H2D of A and B and D2H of C inside the
+             timed region of every step.
+  forms      native FP64 DGEMM (DMMA) on the same inputs, both results'
+             max componentwise error against a double-double evaluation of
+             4096 sampled entries, and the speed-up of the emulated form.
+  roofline   the dominant kernel (ozaki_slice_gemm): slice-product flops
+             (s(s+1)/2 * 2mnk) per launch over its event-timed duration,
+             against the measured bf16 tensor peak.
+  cpu_baseline  the CPU restatement of BLIS's five-loop DGEMM
+             (oracle/gb_oracle.c) on the host cores, on a column sample.
+
+`--impl reference` times that CPU implementation alone on the same
+workload (a column sample per step) and prints the reference line.
+Multi-GPU: the path is replicated (one independent DGEMM per rank, no
+collective); `value` sums the ranks' flops over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIZE = 16384
+SLICES = 8
+EMIN, EMAX = -20, 20
+SEED_A, SEED_B = 20261204, 20261205
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--size", type=int, default=SIZE)
+    p.add_argument("--slices", type=int, default=SLICES)
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    return p.parse_args()
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_dgemm_sample(n, seconds, threads, seed=SEED_A):
+    """Times the CPU five-loop DGEMM on an n x cols x n column sample sized
+    for about `seconds` of work; returns (TFLOP/s, description)."""
+    import numpy as np
+    from oracle import pyoracle as po
+    a = po.expspread((n, n), seed, EMIN, EMAX)
+    cols = 64
+    b = po.expspread((n, cols), seed + 1, EMIN, EMAX)
+    c = np.zeros((n, cols), order="F")
+    t0 = time.perf_counter()
+    po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+    dt = time.perf_counter() - t0
+    rate = 2.0 * n * n * cols / dt
+    cols2 = int(max(64, min(n, rate * seconds / (2.0 * n * n)))) // 64 * 64
+    b = po.expspread((n, cols2), seed + 1, EMIN, EMAX)
+    c = np.zeros((n, cols2), order="F")
+    t0 = time.perf_counter()
+    po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+    dt = time.perf_counter() - t0
+    tf = 2.0 * n * n * cols2 / dt / 1e12
+    return tf, "m=k=%d, n=%d column sample of the %d^3 DGEMM (%.1f s), five-loop C restatement, %d threads" % (
+        n, cols2, n, dt, threads), dt
+
+
+def run_reference(args):
+    ws, rank, local = dist_setup(args)
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = args.size
+    import numpy as np
+    from oracle import pyoracle as po
+    a = po.expspread((n, n), SEED_A, EMIN, EMAX)
+    cols = 64
+    b = po.expspread((n, cols), SEED_B, EMIN, EMAX)
+    c = np.zeros((n, cols), order="F")
+    # per-step sample sized so that warm-up + steps stay within a few minutes
+    t0 = time.perf_counter()
+    po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+    rate = 2.0 * n * n * cols / (time.perf_counter() - t0)
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    cols = int(max(64, min(n, rate * budget / (2.0 * n * n)))) // 64 * 64
+    b = po.expspread((n, cols), SEED_B, EMIN, EMAX)
+    c = np.zeros((n, cols), order="F")
+    for _ in range(args.warmup):
+        po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+    dt = (time.perf_counter() - t0) / max(1, args.steps)
+    tf = 2.0 * n * n * cols / dt / 1e12
+    sample = "m=k=%d, n=%d column sample per step of the %d^3 DGEMM, five-loop C restatement of bli_gemm" % (
+        n, cols, n)
+    line = {
+        "impl": "reference", "metric": "Emulated vs native DGEMM TFLOP/s on 1 GB300 at FP64-level error; % of roofline",
+        "value": tf, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "dgemm_%d_expspread" % n, "m": n, "n": n, "k": n, "e_range": [EMIN, EMAX],
+                   "sample_cols": cols},
+        "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    from blis_gb300 import _lib, blas, dev
+
+    ws, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    L = _lib.load()
+    _lib.check(L.gb_init(local), "gb_init")
+    n = args.size
+    s = args.slices
+    flops = 2.0 * n * n * n
+    peaks, peak_kind = load_peaks()
+
+    A = dev.colmajor(n, n)
+    B = dev.colmajor(n, n)
+    Cz = dev.colmajor(n, n)
+    dev.randm(A, dev.RAND_EXPSPREAD, SEED_A, EMIN, EMAX)
+    dev.randm(B, dev.RAND_EXPSPREAD, SEED_B, EMIN, EMAX)
+    Cz.zero_()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---------------- Ozaki form, device resident (value)
+    for _ in range(args.warmup):
+        dev.dgemm_ozaki(0, 0, 1.0, A, B, 0.0, Cz, s)
+    barrier()
+    stream = torch.cuda.current_stream()
+    dev.set_kernel_timing(True)
+    dev.kernel_time_ms("")  # drop earlier records
+    l0 = L.gb_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            dev.dgemm_ozaki(0, 0, 1.0, A, B, 0.0, Cz, s)
+        ev1.record(stream)
+        barrier()
+    launches = int(L.gb_launch_count() - l0)
+    dev.set_kernel_timing(False)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    gemm_ms, gemm_n = dev.kernel_time_ms("ozaki_slice_gemm")
+    split_ms, _ = dev.kernel_time_ms("oz_")
+    dev.kernel_time_ms("")
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = flops * ws / (ms * 1e-3) / 1e12
+    npairs = s * (s + 1) // 2
+    kern_ms = gemm_ms / max(1, gemm_n)
+    achieved = npairs * flops / (kern_ms * 1e-3) / 1e12
+    peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+
+    # ---------------- errors of both forms against double-double (sampled)
+    g = torch.Generator(device="cpu").manual_seed(7)
+    ii = torch.randint(0, n, (4096,), generator=g).cuda()
+    jj = torch.randint(0, n, (4096,), generator=g).cuda()
+    hi, lo = dev.dd_gemm_entries(0, 0, 1.0, A, B, 0.0, None, ii, jj)
+    err_oz = dev.componentwise_error(Cz[ii, jj], hi, lo)
+
+    # ---------------- native FP64 form on the same inputs (one timed call)
+    Cn = dev.colmajor(n, n)
+    w = 2048
+    dev.dgemm(0, 0, 1.0, A[:w, :w], B[:w, :w], 0.0, Cn[:w, :w])
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    dev.dgemm(0, 0, 1.0, A, B, 0.0, Cn)
+    e1.record(stream)
+    barrier()
+    native_ms = e0.elapsed_time(e1)
+    native_tf = flops / (native_ms * 1e-3) / 1e12
+    err_nat = dev.componentwise_error(Cn[ii, jj], hi, lo)
+    del Cn
+
+    # ---------------- end to end through dgemm_ with pinned host buffers
+    Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    Bh = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    Ch = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    Ah.copy_(A.t())  # Ah row-major storage of A^T == column-major A
+    Bh.copy_(B.t())
+    torch.cuda.synchronize()
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, s)
+    an, bn, cn = Ah.numpy(), Bh.numpy(), Ch.numpy()
+    blas.dgemm("N", "N", n, n, n, 1.0, an, n, bn, n, 0.0, cn, n)  # warm-up
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        blas.dgemm("N", "N", n, n, n, 1.0, an, n, bn, n, 0.0, cn, n)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+    blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_tf = flops * ws / (e2e_ms * 1e-3) / 1e12
+    # cn holds column-major C, i.e. cn[j, i] == C[i, j]
+    e2e_ok = bool(np.array_equal(cn[:64, :64], Cz[:64, :64].t().contiguous().cpu().numpy()))
+
+    # ---------------- traffic of the dominant kernel from the committed ncu summary
+    traffic = None
+    tf_path = os.path.join(ROOT, "profiles", "ozaki_slice_gemm_traffic.json")
+    if os.path.exists(tf_path):
+        with open(tf_path) as f:
+            tinfo = json.load(f)
+        traffic = tinfo.get("bytes_per_launch_scaled", {}).get(str(n))
+
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    threads = os.cpu_count() or 1
+    cpu_tf, cpu_sample, _ = cpu_dgemm_sample(min(n, 16384), args.cpu_seconds, threads)
+
+    line = {
+        "metric": "Emulated vs native DGEMM TFLOP/s on 1 GB300 at FP64-level error; % of roofline",
+        "value": value,
+        "unit": "TFLOP/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: (1+u)*2^e, e in [-20,20], random sign, seeded counter RNG on device",
+        "config": {"workload": "ozaki_dgemm_%d" % n, "m": n, "n": n, "k": n, "layout": "column-major",
+                   "alpha": 1.0, "beta": 0.0, "form": "ozaki bf16 slices=%d (triangular, %d products)" % (s, npairs),
+                   "l2": "inputs 2 GiB each, larger than the 126 MB L2", "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "forms": {
+            "ozaki": {"tflops": value / ws, "max_componentwise_err": err_oz, "slices": s},
+            "native_fp64": {"tflops": native_tf, "ms": native_ms, "max_componentwise_err": err_nat,
+                            "engine": os.environ.get("GB_DGEMM_ENGINE", "dmma")},
+            "speedup_vs_native": (value / ws) / native_tf,
+            "error_ratio_ozaki_over_native": err_oz / err_nat if err_nat > 0 else None,
+            "err_sample": "4096 random entries, double-double evaluation on the device",
+        },
+        "e2e": {"value": e2e_tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 2 * 8 * n * n,
+                "d2h_bytes_per_step": 8 * n * n, "ms_per_step": e2e_ms, "api": "dgemm_ (C ABI), pinned host buffers",
+                "matches_device_result": e2e_ok},
+        "roofline": {"bound": "tensor", "kernel": "ozaki_slice_gemm", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "%s bf16_tflops_sustained" % peak_kind,
+                     "kernel_ms": kern_ms, "algorithmic_flops_per_launch": npairs * flops,
+                     "split_recombine_ms_per_step": (split_ms / max(1, args.steps))},
+        "cpu_baseline": {"value": cpu_tf, "unit": "TFLOP/s", "cores": threads, "kind": "port", "sample": cpu_sample},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

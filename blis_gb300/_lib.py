@@ -1,0 +1,120 @@
+"""Loader for libblis_gb300.so with ctypes signatures for every exported entry.
+
+The shared library is the product; this module only binds it.  It raises
+immediately when the library is missing: there is no fallback path.
+"""
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libblis_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "blis_gb300.h")
+
+_lib = None
+
+_i32 = C.c_int32
+_i64 = C.c_int64
+_d = C.c_double
+_f = C.c_float
+_vp = C.c_void_p
+_ip = C.POINTER(C.c_int32)
+_dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
+_cp = C.c_char_p
+
+
+def _sig(L, name, res, args):
+    fn = getattr(L, name)
+    fn.restype = res
+    fn.argtypes = args
+
+
+def declared_functions():
+    """Names of the functions declared in include/blis_gb300.h."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\**\s+\**([a-z][A-Za-z0-9_]*)\s*\(",
+                                 text, flags=re.M)))
+
+
+def load(path=None):
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError("libblis_gb300.so is not built (%s); run __graft_entry__.build()" % path)
+    L = C.CDLL(path, mode=C.RTLD_GLOBAL)
+    gemm_blas = [_cp, _cp, _ip, _ip, _ip, _vp, _vp, _ip, _vp, _ip, _vp, _vp, _ip]
+    _sig(L, "dgemm_", None, gemm_blas)
+    _sig(L, "sgemm_", None, gemm_blas)
+    _sig(L, "dtrsm_", None, [_cp, _cp, _cp, _cp, _ip, _ip, _dp, _vp, _ip, _vp, _ip])
+    _sig(L, "dgemv_", None, [_cp, _ip, _ip, _dp, _vp, _ip, _vp, _ip, _dp, _vp, _ip])
+    _sig(L, "daxpy_", None, [_ip, _dp, _vp, _ip, _vp, _ip])
+    _sig(L, "ddot_", _d, [_ip, _vp, _ip, _vp, _ip])
+    batch = [_cp, _cp, _ip, _ip, _ip, _vp, _vp, _ip, _vp, _ip, _vp, _vp, _ip, _ip, _ip]
+    _sig(L, "dgemm_batch_", None, batch)
+    _sig(L, "sgemm_batch_", None, batch)
+    _sig(L, "xerbla_", C.c_int, [_cp, _ip, C.c_long])
+    _sig(L, "cblas_dgemm", None, [C.c_int] * 3 + [_i32] * 3 + [_d, _vp, _i32, _vp, _i32, _d, _vp, _i32])
+    _sig(L, "cblas_sgemm", None, [C.c_int] * 3 + [_i32] * 3 + [_f, _vp, _i32, _vp, _i32, _f, _vp, _i32])
+    _sig(L, "cblas_dtrsm", None, [C.c_int] * 5 + [_i32, _i32, _d, _vp, _i32, _vp, _i32])
+    _sig(L, "cblas_dgemv", None, [C.c_int, C.c_int, _i32, _i32, _d, _vp, _i32, _vp, _i32, _d, _vp, _i32])
+    _sig(L, "cblas_daxpy", None, [_i32, _d, _vp, _i32, _vp, _i32])
+    _sig(L, "cblas_ddot", _d, [_i32, _vp, _i32, _vp, _i32])
+    _sig(L, "cblas_dgemm_batch", None, [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                        _vp, _vp, _vp, _i32, _vp])
+    tg = [C.c_int, C.c_int, _i64, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _i64, _i64]
+    _sig(L, "bli_dgemm", None, tg)
+    _sig(L, "bli_sgemm", None, tg)
+    _sig(L, "bli_dgemm_ex", None, tg + [_vp, _vp])
+    tt = [C.c_int] * 4 + [_i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64]
+    _sig(L, "bli_dtrsm", None, tt)
+    _sig(L, "bli_dtrsm_ex", None, tt + [_vp, _vp])
+    tv = [C.c_int, C.c_int, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _vp, _i64]
+    _sig(L, "bli_dgemv", None, tv)
+    _sig(L, "bli_dgemv_ex", None, tv + [_vp, _vp])
+    _sig(L, "bli_daxpyv", None, [C.c_int, _i64, _vp, _vp, _i64, _vp, _i64])
+    _sig(L, "bli_daxpyv_ex", None, [C.c_int, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp])
+    _sig(L, "bli_ddotv", None, [C.c_int, C.c_int, _i64, _vp, _i64, _vp, _i64, _vp])
+    _sig(L, "bli_ddotv_ex", None, [C.c_int, C.c_int, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _vp])
+    dg = [C.c_int, C.c_int, _i64, _i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _d, _vp, _i64, _i64]
+    _sig(L, "gb_dgemm_dev", C.c_int, dg + [_vp])
+    _sig(L, "gb_dgemm_ozaki_dev", C.c_int, dg + [C.c_int, _vp])
+    sg = [C.c_int, C.c_int, _i64, _i64, _i64, _f, _vp, _i64, _i64, _vp, _i64, _i64, _f, _vp, _i64, _i64]
+    _sig(L, "gb_sgemm_dev", C.c_int, sg + [_vp])
+    _sig(L, "gb_dtrsm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_daxpyv_dev", C.c_int, [_i64, _d, _vp, _i64, _vp, _i64, _vp])
+    _sig(L, "gb_ddotv_dev", C.c_int, [_i64, _vp, _i64, _vp, _i64, _vp, _vp])
+    _sig(L, "gb_dgemv_dev", C.c_int, [C.c_int, _i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _d, _vp, _i64, _vp])
+    _sig(L, "gb_gemm_batch_dev", C.c_int, [_vp, _i64, C.c_int, C.c_int, _vp])
+    _sig(L, "gb_batch_plan_create", C.c_int, [_vp, _i64, C.c_int, C.POINTER(C.c_void_p)])
+    _sig(L, "gb_batch_plan_run", C.c_int, [_vp, C.c_int, _vp])
+    _sig(L, "gb_batch_plan_destroy", C.c_int, [_vp])
+    _sig(L, "gb_randm_dev", C.c_int, [C.c_int, C.c_int, _vp, _i64, _i64, _i64, _i64, C.c_uint64, _d, _d, _vp])
+    _sig(L, "gb_dd_gemm_entries_dev", C.c_int, [C.c_int, C.c_int, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64,
+                                                 _d, _vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp, _vp])
+    _sig(L, "gb_init", C.c_int, [C.c_int])
+    _sig(L, "gb_set_dgemm_mode", C.c_int, [C.c_int, C.c_int])
+    _sig(L, "gb_get_last_error", C.c_int, [C.c_char_p, C.c_size_t])
+    _sig(L, "gb_clear_last_error", None, [])
+    _sig(L, "gb_launch_count", _i64, [])
+    _sig(L, "gb_set_kernel_timing", C.c_int, [C.c_int])
+    _sig(L, "gb_kernel_time_ms", _d, [_cp, C.POINTER(_i64)])
+    _sig(L, "gb_synchronize", C.c_int, [])
+    _lib = L
+    return L
+
+
+def last_error():
+    buf = C.create_string_buffer(512)
+    code = load().gb_get_last_error(buf, 512)
+    return code, buf.value.decode(errors="replace")
+
+
+def check(rc, what="call"):
+    if rc != 0:
+        code, msg = last_error()
+        raise RuntimeError("%s failed (%d): %s" % (what, rc, msg))
+    return rc

@@ -1,0 +1,139 @@
+"""Python mirror of the reference's BLAS-compat and typed-API entry points.
+
+Each function calls the matching symbol of libblis_gb300.so through ctypes
+with host (numpy) buffers, so a test reads like a call into BLIS's own
+frame/compat layer: same names, same argument meaning (Fortran-style
+leading dimensions, netlib increment rules, xerbla on bad arguments).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+NO_TRANSPOSE, TRANSPOSE, CONJ_NO_TRANSPOSE, CONJ_TRANSPOSE = 0x00, 0x08, 0x10, 0x18
+NO_CONJUGATE, CONJUGATE = 0x00, 0x10
+LOWER, UPPER = 0xC0, 0x60
+LEFT, RIGHT = 0, 1
+NONUNIT_DIAG, UNIT_DIAG = 0x000, 0x100
+DGEMM_NATIVE, DGEMM_OZAKI = 0, 1
+
+
+def _i(v):
+    return C.byref(C.c_int32(int(v)))
+
+
+def _d(v):
+    return C.byref(C.c_double(float(v)))
+
+
+def _s(v):
+    return C.byref(C.c_float(float(v)))
+
+
+def _p(x):
+    return None if x is None else x.ctypes.data_as(C.c_void_p)
+
+
+def _c(ch):
+    return ch.encode() if isinstance(ch, str) else ch
+
+
+# ------------------------------------------------------------ Fortran BLAS
+def dgemm(transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+    _lib.load().dgemm_(_c(transa), _c(transb), _i(m), _i(n), _i(k), _d(alpha), _p(a), _i(lda),
+                       _p(b), _i(ldb), _d(beta), _p(c), _i(ldc))
+
+
+def sgemm(transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+    _lib.load().sgemm_(_c(transa), _c(transb), _i(m), _i(n), _i(k), _s(alpha), _p(a), _i(lda),
+                       _p(b), _i(ldb), _s(beta), _p(c), _i(ldc))
+
+
+def dtrsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
+    _lib.load().dtrsm_(_c(side), _c(uplo), _c(transa), _c(diag), _i(m), _i(n),
+                       C.byref(C.c_double(alpha)), _p(a), _i(lda), _p(b), _i(ldb))
+
+
+def dgemv(trans, m, n, alpha, a, lda, x, incx, beta, y, incy):
+    _lib.load().dgemv_(_c(trans), _i(m), _i(n), C.byref(C.c_double(alpha)), _p(a), _i(lda), _p(x),
+                       _i(incx), C.byref(C.c_double(beta)), _p(y), _i(incy))
+
+
+def daxpy(n, alpha, x, incx, y, incy):
+    _lib.load().daxpy_(_i(n), C.byref(C.c_double(alpha)), _p(x), _i(incx), _p(y), _i(incy))
+
+
+def ddot(n, x, incx, y, incy):
+    return _lib.load().ddot_(_i(n), _p(x), _i(incx), _p(y), _i(incy))
+
+
+def dgemm_batch(transa, transb, m, n, k, alpha, a_list, lda, b_list, ldb, beta, c_list, ldc,
+                group_size, dtype=np.float64):
+    """Grouped interface of frame/compat/extra/bla_gemm_batch.c: per-group
+    parameter arrays plus flat per-problem pointer arrays."""
+    g = len(group_size)
+    ta = (C.c_char * g)(*[_c(t) for t in transa])
+    tb = (C.c_char * g)(*[_c(t) for t in transb])
+    ia = lambda v: (C.c_int32 * g)(*[int(x) for x in v])
+    fty = C.c_double if dtype == np.float64 else C.c_float
+    fa = lambda v: (fty * g)(*[float(x) for x in v])
+    total = sum(group_size)
+    pa = (C.c_void_p * total)(*[x.ctypes.data for x in a_list])
+    pb = (C.c_void_p * total)(*[x.ctypes.data for x in b_list])
+    pc = (C.c_void_p * total)(*[x.ctypes.data for x in c_list])
+    fn = _lib.load().dgemm_batch_ if dtype == np.float64 else _lib.load().sgemm_batch_
+    fn(ta, tb, ia(m), ia(n), ia(k), fa(alpha), pa, ia(lda), pb, ia(ldb), fa(beta), pc, ia(ldc),
+       _i(g), ia(group_size))
+
+
+# ------------------------------------------------------------ typed BLIS API
+def _st(x):
+    it = x.itemsize
+    return x.strides[0] // it, x.strides[1] // it
+
+
+def bli_dgemm(transa, transb, alpha, a, b, beta, c):
+    m, n = c.shape
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    _lib.load().bli_dgemm(transa, transb, m, n, k, _d(alpha), _p(a), *_st(a), _p(b), *_st(b),
+                          _d(beta), _p(c), *_st(c))
+
+
+def bli_sgemm(transa, transb, alpha, a, b, beta, c):
+    m, n = c.shape
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    _lib.load().bli_sgemm(transa, transb, m, n, k, _s(alpha), _p(a), *_st(a), _p(b), *_st(b),
+                          _s(beta), _p(c), *_st(c))
+
+
+def bli_dtrsm(side, uplo, transa, diag, alpha, a, b):
+    m, n = b.shape
+    _lib.load().bli_dtrsm(side, uplo, transa, diag, m, n, _d(alpha), _p(a), *_st(a), _p(b), *_st(b))
+
+
+def bli_dgemv(transa, alpha, a, x, beta, y, incx=1, incy=1):
+    m, n = a.shape
+    _lib.load().bli_dgemv(transa, 0, m, n, _d(alpha), _p(a), *_st(a), _p(x), incx, _d(beta), _p(y),
+                          incy)
+
+
+def bli_daxpyv(alpha, x, y, n=None, incx=1, incy=1):
+    n = x.size if n is None else n
+    _lib.load().bli_daxpyv(0, n, _d(alpha), _p(x), incx, _p(y), incy)
+
+
+def bli_ddotv(x, y, n=None, incx=1, incy=1):
+    n = x.size if n is None else n
+    rho = np.zeros(1)
+    _lib.load().bli_ddotv(0, 0, n, _p(x), incx, _p(y), incy, _p(rho))
+    return float(rho[0])
+
+
+# ------------------------------------------------------------ controls
+def set_dgemm_mode(mode, slices=8):
+    return _lib.check(_lib.load().gb_set_dgemm_mode(mode, slices), "gb_set_dgemm_mode")
+
+
+def launch_count():
+    return int(_lib.load().gb_launch_count())

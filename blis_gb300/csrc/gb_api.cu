@@ -1,0 +1,703 @@
+// gb_api.cu -- the exported C ABI: BLAS compat layer, CBLAS, typed BLIS API
+// and the gb_ device-pointer addon.
+//
+// Host-pointer entry points follow the reference's argument handling line
+// for line in behaviour (checks and xerbla numbering from
+// frame/compat/check/bla_*_check.h, negative-increment conversion from
+// frame/include/bli_blas_macro_defs.h:50-75, the m==1/n==1 gemv redirect of
+// frame/compat/bla_gemm.c:180-218, the gemv n_x==0 quirk of
+// frame/compat/bla_gemv.c:88-106), then stage operands into HBM with
+// stream-ordered allocations, run the device kernels and copy results back
+// before returning, as a synchronous BLAS call must.
+#include <ctype.h>
+#include <string.h>
+
+#include "gb_internal.h"
+
+namespace gb {
+namespace {
+
+// ---------------------------------------------------------------- staging
+struct Staged {
+    char* alloc = nullptr;
+    char* origin = nullptr;
+    int64_t rs = 0, cs = 0;
+    int layout = 0;  // 0 packed column-major, 1 packed row-major, 2 span
+};
+
+int pick_layout(int64_t rows, int64_t cols, int64_t rs, int64_t cs)
+{
+    if (rs == 1 && (cols == 1 || cs >= rows)) return 0;
+    if (cs == 1 && (rows == 1 || rs >= cols)) return 1;
+    return 2;
+}
+
+void span_of(int64_t rows, int64_t cols, int64_t rs, int64_t cs, int64_t* lo, int64_t* hi)
+{
+    const int64_t o[4] = {0, (rows - 1) * rs, (cols - 1) * cs, (rows - 1) * rs + (cols - 1) * cs};
+    *lo = o[0];
+    *hi = o[0];
+    for (int i = 1; i < 4; ++i) {
+        if (o[i] < *lo) *lo = o[i];
+        if (o[i] > *hi) *hi = o[i];
+    }
+}
+
+// Copies a host (or any UVA) matrix into a fresh device buffer.  Packed
+// layouts drop the leading-dimension padding; general strides copy the
+// whole span and keep the strides.  `need_data` false skips the copy for
+// packed outputs that are fully overwritten (beta == 0).
+int stage_in(const void* host, int64_t rows, int64_t cols, int64_t rs, int64_t cs, size_t esz,
+             bool need_data, Staged* st, cudaStream_t s)
+{
+    *st = Staged();
+    if (rows <= 0 || cols <= 0) return GB_SUCCESS;
+    st->layout = pick_layout(rows, cols, rs, cs);
+    if (st->layout == 0) {
+        st->alloc = static_cast<char*>(dev_alloc((size_t)rows * cols * esz, s));
+        if (!st->alloc) return GB_ERR_NOMEM;
+        st->origin = st->alloc;
+        st->rs = 1;
+        st->cs = rows;
+        const size_t sp = (size_t)((cols == 1) ? rows : cs) * esz;
+        if (need_data)
+            GB_CUDA(cudaMemcpy2DAsync(st->alloc, rows * esz, host, sp, rows * esz, cols,
+                                      cudaMemcpyDefault, s));
+    } else if (st->layout == 1) {
+        st->alloc = static_cast<char*>(dev_alloc((size_t)rows * cols * esz, s));
+        if (!st->alloc) return GB_ERR_NOMEM;
+        st->origin = st->alloc;
+        st->rs = cols;
+        st->cs = 1;
+        const size_t sp = (size_t)((rows == 1) ? cols : rs) * esz;
+        if (need_data)
+            GB_CUDA(cudaMemcpy2DAsync(st->alloc, cols * esz, host, sp, cols * esz, rows,
+                                      cudaMemcpyDefault, s));
+    } else {
+        int64_t lo, hi;
+        span_of(rows, cols, rs, cs, &lo, &hi);
+        const size_t count = (size_t)(hi - lo + 1);
+        st->alloc = static_cast<char*>(dev_alloc(count * esz, s));
+        if (!st->alloc) return GB_ERR_NOMEM;
+        st->origin = st->alloc - lo * (int64_t)esz;
+        st->rs = rs;
+        st->cs = cs;
+        // always copied: the write-back below covers the whole span
+        GB_CUDA(cudaMemcpyAsync(st->alloc, static_cast<const char*>(host) + lo * (int64_t)esz,
+                                count * esz, cudaMemcpyDefault, s));
+    }
+    return GB_SUCCESS;
+}
+
+int stage_out(void* host, int64_t rows, int64_t cols, int64_t rs, int64_t cs, size_t esz,
+              const Staged& st, cudaStream_t s)
+{
+    if (rows <= 0 || cols <= 0 || !st.alloc) return GB_SUCCESS;
+    if (st.layout == 0) {
+        const size_t dp = (size_t)((cols == 1) ? rows : cs) * esz;
+        GB_CUDA(cudaMemcpy2DAsync(host, dp, st.alloc, rows * esz, rows * esz, cols, cudaMemcpyDefault, s));
+    } else if (st.layout == 1) {
+        const size_t dp = (size_t)((rows == 1) ? cols : rs) * esz;
+        GB_CUDA(cudaMemcpy2DAsync(host, dp, st.alloc, cols * esz, cols * esz, rows, cudaMemcpyDefault, s));
+    } else {
+        int64_t lo, hi;
+        span_of(rows, cols, rs, cs, &lo, &hi);
+        GB_CUDA(cudaMemcpyAsync(static_cast<char*>(host) + lo * (int64_t)esz, st.alloc,
+                                (size_t)(hi - lo + 1) * esz, cudaMemcpyDefault, s));
+    }
+    return GB_SUCCESS;
+}
+
+struct Bufs {
+    cudaStream_t s;
+    Staged b[4];
+    int n = 0;
+    explicit Bufs(cudaStream_t st) : s(st) {}
+    Staged& next() { return b[n++]; }
+    ~Bufs()
+    {
+        for (int i = 0; i < n; ++i) dev_free(b[i].alloc, s);
+    }
+};
+
+int finish(cudaStream_t s, const char* where)
+{
+    GB_CUDA(cudaStreamSynchronize(s));
+    return read_and_clear_device_status(s, where);
+}
+
+// ---------------------------------------------------------------- host ops
+template <typename T>
+int gemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, T alpha, const T* a,
+              int64_t rs_a, int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, T beta, T* c,
+              int64_t rs_c, int64_t cs_c, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const size_t esz = sizeof(T);
+    const bool trivial = (alpha == T(0) || k <= 0);
+    Staged& C = bufs.next();
+    if ((rc = stage_in(c, m, n, rs_c, cs_c, esz, beta != T(0), &C, s))) return rc;
+    T* cd = reinterpret_cast<T*>(C.origin);
+    if (trivial) {
+        if (sizeof(T) == 8) rc = scal_matrix(m, n, (double)beta, (double*)cd, C.rs, C.cs, s);
+        else rc = scal_matrix_f(m, n, (float)beta, (float*)cd, C.rs, C.cs, s);
+    } else {
+        const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+        Staged& A = bufs.next();
+        Staged& B = bufs.next();
+        if ((rc = stage_in(a, ta ? k : m, ta ? m : k, rs_a, cs_a, esz, true, &A, s))) return rc;
+        if ((rc = stage_in(b, tb ? n : k, tb ? k : n, rs_b, cs_b, esz, true, &B, s))) return rc;
+        const int64_t ars = ta ? A.cs : A.rs, acs = ta ? A.rs : A.cs;
+        const int64_t brs = tb ? B.cs : B.rs, bcs = tb ? B.rs : B.cs;
+        if (sizeof(T) == 8) {
+            const double* ad = reinterpret_cast<const double*>(A.origin);
+            const double* bd = reinterpret_cast<const double*>(B.origin);
+            if (dgemm_mode() == GB_DGEMM_OZAKI)
+                rc = dgemm_ozaki(m, n, k, (double)alpha, ad, ars, acs, bd, brs, bcs, (double)beta,
+                                 (double*)cd, C.rs, C.cs, ozaki_slices(), s);
+            else
+                rc = dgemm_native(m, n, k, (double)alpha, ad, ars, acs, bd, brs, bcs, (double)beta,
+                                  (double*)cd, C.rs, C.cs, s);
+        } else {
+            rc = sgemm_dev(m, n, k, (float)alpha, reinterpret_cast<const float*>(A.origin), ars, acs,
+                           reinterpret_cast<const float*>(B.origin), brs, bcs, (float)beta,
+                           (float*)cd, C.rs, C.cs, s);
+        }
+    }
+    if (rc) return rc;
+    if ((rc = stage_out(c, m, n, rs_c, cs_c, esz, C, s))) return rc;
+    return finish(s, where);
+}
+
+int gemv_host(int transa, int64_t m, int64_t n, double alpha, const double* a, int64_t rs_a,
+              int64_t cs_a, const double* x, int64_t incx, double beta, double* y, int64_t incy,
+              const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    const bool tr = GB_IS_TRANS(transa);
+    const int64_t my = tr ? n : m, nx = tr ? m : n;
+    if (my <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    Staged& Y = bufs.next();
+    if ((rc = stage_in(y, my, 1, incy, my, 8, beta != 0.0, &Y, s))) return rc;
+    const double* ad = nullptr;
+    const double* xd = nullptr;
+    int64_t ars = rs_a, acs = cs_a, xinc = incx;
+    if (nx > 0 && alpha != 0.0) {
+        Staged& A = bufs.next();
+        Staged& X = bufs.next();
+        if ((rc = stage_in(a, m, n, rs_a, cs_a, 8, true, &A, s))) return rc;
+        if ((rc = stage_in(x, nx, 1, incx, nx, 8, true, &X, s))) return rc;
+        ad = reinterpret_cast<const double*>(A.origin);
+        xd = reinterpret_cast<const double*>(X.origin);
+        ars = A.rs;
+        acs = A.cs;
+        xinc = X.rs;
+    }
+    if ((rc = dgemv_dev(tr ? 1 : 0, m, n, alpha, ad, ars, acs, xd, xinc, beta,
+                        reinterpret_cast<double*>(Y.origin), Y.rs, s)))
+        return rc;
+    if ((rc = stage_out(y, my, 1, incy, my, 8, Y, s))) return rc;
+    return finish(s, where);
+}
+
+int axpyv_host(int64_t n, double alpha, const double* x, int64_t incx, double* y, int64_t incy)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (n <= 0 || alpha == 0.0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    Staged& X = bufs.next();
+    Staged& Y = bufs.next();
+    if ((rc = stage_in(x, n, 1, incx, n, 8, true, &X, s))) return rc;
+    if ((rc = stage_in(y, n, 1, incy, n, 8, true, &Y, s))) return rc;
+    if ((rc = daxpyv_dev(n, alpha, reinterpret_cast<const double*>(X.origin), X.rs,
+                         reinterpret_cast<double*>(Y.origin), Y.rs, s)))
+        return rc;
+    if ((rc = stage_out(y, n, 1, incy, n, 8, Y, s))) return rc;
+    return finish(s, "axpyv");
+}
+
+int dotv_host(int64_t n, const double* x, int64_t incx, const double* y, int64_t incy, double* rho)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    Staged& X = bufs.next();
+    Staged& Y = bufs.next();
+    if (n > 0) {
+        if ((rc = stage_in(x, n, 1, incx, n, 8, true, &X, s))) return rc;
+        if ((rc = stage_in(y, n, 1, incy, n, 8, true, &Y, s))) return rc;
+    }
+    const int nparts = dotv_nparts(n > 0 ? n : 1);
+    double* scratch = static_cast<double*>(dev_alloc(sizeof(double) * (nparts + 1), s));
+    if (!scratch) return GB_ERR_NOMEM;
+    rc = ddotv_dev(n, reinterpret_cast<const double*>(X.origin), X.rs,
+                   reinterpret_cast<const double*>(Y.origin), Y.rs, scratch + nparts, scratch, nparts, s);
+    if (!rc) rc = check_cuda(cudaMemcpyAsync(rho, scratch + nparts, sizeof(double), cudaMemcpyDeviceToHost, s), "dotv");
+    dev_free(scratch, s);
+    if (rc) return rc;
+    return finish(s, "dotv");
+}
+
+int trsm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, double alpha,
+              const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const int64_t na = (side == GB_LEFT) ? m : n;
+    Staged& B = bufs.next();
+    if ((rc = stage_in(b, m, n, rs_b, cs_b, 8, alpha != 0.0, &B, s))) return rc;
+    Staged& A = bufs.next();
+    if (alpha != 0.0 && (rc = stage_in(a, na, na, rs_a, cs_a, 8, true, &A, s))) return rc;
+    const int slices = (dgemm_mode() == GB_DGEMM_OZAKI) ? ozaki_slices() : 0;
+    if ((rc = dtrsm_dev(side, uplo, transa, diag, m, n, alpha,
+                        reinterpret_cast<const double*>(A.origin), A.rs, A.cs,
+                        reinterpret_cast<double*>(B.origin), B.rs, B.cs, slices, s)))
+        return rc;
+    if ((rc = stage_out(b, m, n, rs_b, cs_b, 8, B, s))) return rc;
+    return finish(s, "trsm");
+}
+
+// ---------------------------------------------------------------- BLAS helpers
+bool lsame(char a, char b) { return toupper((unsigned char)a) == toupper((unsigned char)b); }
+
+void call_xerbla(const char* name, int info)
+{
+    gb_f77_int i = info;
+    xerbla_(name, &i, 6);
+}
+
+int map_trans(char t) { return lsame(t, 'N') ? GB_NO_TRANSPOSE : (lsame(t, 'T') ? GB_TRANSPOSE : GB_CONJ_TRANSPOSE); }
+
+// frame/compat/check/bla_gemm_check.h:37-86
+int gemm_check(char ta, char tb, int m, int n, int k, int lda, int ldb, int ldc)
+{
+    const bool nota = lsame(ta, 'N'), notb = lsame(tb, 'N');
+    const bool conja = lsame(ta, 'C'), conjb = lsame(tb, 'C');
+    const bool tta = lsame(ta, 'T'), ttb = lsame(tb, 'T');
+    const int nrowa = nota ? m : k, nrowb = notb ? k : n;
+    if (!nota && !conja && !tta) return 1;
+    if (!notb && !conjb && !ttb) return 2;
+    if (m < 0) return 3;
+    if (n < 0) return 4;
+    if (k < 0) return 5;
+    if (lda < (nrowa > 1 ? nrowa : 1)) return 8;
+    if (ldb < (nrowb > 1 ? nrowb : 1)) return 10;
+    if (ldc < (m > 1 ? m : 1)) return 13;
+    return 0;
+}
+
+// frame/include/bli_blas_macro_defs.h:50-75: BLAS passes element 0 of the
+// traversal; BLIS wants the pointer to element 0 with a signed stride.
+template <typename T>
+const T* blas_vec(const T* x, int64_t n, int64_t inc)
+{
+    return (inc < 0) ? x + (n - 1) * (-inc) : x;
+}
+
+template <typename T>
+void gemm_blas(const char* name, const char* transa, const char* transb, const gb_f77_int* m,
+               const gb_f77_int* n, const gb_f77_int* k, const T* alpha, const T* a,
+               const gb_f77_int* lda, const T* b, const gb_f77_int* ldb, const T* beta, T* c,
+               const gb_f77_int* ldc)
+{
+    const int info = gemm_check(*transa, *transb, *m, *n, *k, *lda, *ldb, *ldc);
+    if (info) {
+        call_xerbla(name, info);
+        return;
+    }
+    const int ta = map_trans(*transa), tb = map_trans(*transb);
+    const int64_t m0 = *m, n0 = *n, k0 = *k;
+    const int64_t rs_a = 1, cs_a = *lda, rs_b = 1, cs_b = *ldb, rs_c = 1, cs_c = *ldc;
+    if (sizeof(T) == 8) {
+        // m == 1 or n == 1 become gemv (frame/compat/bla_gemm.c:180-218)
+        if (n0 == 1) {
+            const int64_t m0t = GB_IS_TRANS(ta) ? k0 : m0, k0t = GB_IS_TRANS(ta) ? m0 : k0;
+            gemv_host(ta, m0t, k0t, (double)*alpha, (const double*)a, rs_a, cs_a, (const double*)b,
+                      GB_IS_TRANS(tb) ? cs_b : rs_b, (double)*beta, (double*)c, rs_c, name);
+            return;
+        }
+        if (m0 == 1) {
+            const int64_t n0t = GB_IS_TRANS(tb) ? k0 : n0, k0t = GB_IS_TRANS(tb) ? n0 : k0;
+            gemv_host(tb, n0t, k0t, (double)*alpha, (const double*)b, cs_b, rs_b, (const double*)a,
+                      GB_IS_TRANS(ta) ? rs_a : cs_a, (double)*beta, (double*)c, cs_c, name);
+            return;
+        }
+    }
+    gemm_host<T>(ta, tb, m0, n0, k0, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c, cs_c, name);
+}
+
+}  // namespace
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+// ==================================================================== BLAS
+int xerbla_(const gb_f77_char* srname, const gb_f77_int* info, long srname_len)
+{
+    char buf[16] = {0};
+    const long n = (srname_len > 0 && srname_len < 15) ? srname_len : 6;
+    for (long i = 0; i < n && srname[i]; ++i) buf[i] = srname[i];
+    printf("** On entry to %6s, parameter number %2i had an illegal value\n", buf, (int)*info);
+    fflush(stdout);
+    gb::set_error(GB_ERR_ARG, buf, "illegal BLAS argument");
+    return 0;
+}
+
+void dgemm_(const gb_f77_char* transa, const gb_f77_char* transb, const gb_f77_int* m,
+            const gb_f77_int* n, const gb_f77_int* k, const double* alpha, const double* a,
+            const gb_f77_int* lda, const double* b, const gb_f77_int* ldb, const double* beta,
+            double* c, const gb_f77_int* ldc)
+{
+    gemm_blas<double>("DGEMM ", transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc);
+}
+
+void sgemm_(const gb_f77_char* transa, const gb_f77_char* transb, const gb_f77_int* m,
+            const gb_f77_int* n, const gb_f77_int* k, const float* alpha, const float* a,
+            const gb_f77_int* lda, const float* b, const gb_f77_int* ldb, const float* beta,
+            float* c, const gb_f77_int* ldc)
+{
+    gemm_blas<float>("SGEMM ", transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc);
+}
+
+void dtrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const double* alpha,
+            const double* a, const gb_f77_int* lda, double* b, const gb_f77_int* ldb)
+{
+    // frame/compat/check/bla_trmm_check.h:37-86
+    const bool left = lsame(*side, 'L'), right = lsame(*side, 'R');
+    const bool lower = lsame(*uploa, 'L'), upper = lsame(*uploa, 'U');
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T'), conja = lsame(*transa, 'C');
+    const bool unita = lsame(*diaga, 'U'), nonua = lsame(*diaga, 'N');
+    const int nrowa = left ? *m : *n;
+    int info = 0;
+    if (!left && !right) info = 1;
+    else if (!lower && !upper) info = 2;
+    else if (!nota && !ta && !conja) info = 3;
+    else if (!unita && !nonua) info = 4;
+    else if (*m < 0) info = 5;
+    else if (*n < 0) info = 6;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 9;
+    else if (*ldb < (*m > 1 ? *m : 1)) info = 11;
+    if (info) {
+        call_xerbla("DTRSM ", info);
+        return;
+    }
+    trsm_host(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, map_trans(*transa),
+              unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, *n, *alpha, a, 1, *lda, b, 1, *ldb);
+}
+
+void dgemv_(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n, const double* alpha,
+            const double* a, const gb_f77_int* lda, const double* x, const gb_f77_int* incx,
+            const double* beta, double* y, const gb_f77_int* incy)
+{
+    // frame/compat/check/bla_gemv_check.h:37-75
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T'), conja = lsame(*transa, 'C');
+    int info = 0;
+    if (!nota && !ta && !conja) info = 1;
+    else if (*m < 0) info = 2;
+    else if (*n < 0) info = 3;
+    else if (*lda < (*m > 1 ? *m : 1)) info = 6;
+    else if (*incx == 0) info = 8;
+    else if (*incy == 0) info = 11;
+    if (info) {
+        call_xerbla("DGEMV ", info);
+        return;
+    }
+    const int t = map_trans(*transa);
+    const int64_t m0 = *m, n0 = *n;
+    const int64_t m_y = GB_IS_TRANS(t) ? n0 : m0, n_x = GB_IS_TRANS(t) ? m0 : n0;
+    if (m_y > 0 && n_x == 0) return;  // netlib quirk kept by frame/compat/bla_gemv.c:88-106
+    gemv_host(t, m0, n0, *alpha, a, 1, *lda, blas_vec(x, n_x, *incx), *incx, *beta,
+              const_cast<double*>(blas_vec<double>(y, m_y, *incy)), *incy, "DGEMV ");
+}
+
+void daxpy_(const gb_f77_int* n, const double* alpha, const double* x, const gb_f77_int* incx,
+            double* y, const gb_f77_int* incy)
+{
+    const int64_t n0 = (*n > 0) ? *n : 0;
+    axpyv_host(n0, *alpha, blas_vec(x, n0, *incx), *incx,
+               const_cast<double*>(blas_vec<double>(y, n0, *incy)), *incy);
+}
+
+double ddot_(const gb_f77_int* n, const double* x, const gb_f77_int* incx, const double* y,
+             const gb_f77_int* incy)
+{
+    const int64_t n0 = (*n > 0) ? *n : 0;
+    double rho = 0.0;
+    dotv_host(n0, blas_vec(x, n0, *incx), *incx, blas_vec(y, n0, *incy), *incy, &rho);
+    return rho;
+}
+
+// ==================================================================== CBLAS
+static char cblas_trans_char(int t)
+{
+    return t == GbCblasNoTrans ? 'N' : (t == GbCblasTrans ? 'T' : (t == GbCblasConjTrans ? 'C' : '?'));
+}
+
+void cblas_dgemm(int order, int transa, int transb, gb_f77_int m, gb_f77_int n, gb_f77_int k,
+                 double alpha, const double* a, gb_f77_int lda, const double* b, gb_f77_int ldb,
+                 double beta, double* c, gb_f77_int ldc)
+{
+    char ta = cblas_trans_char(transa), tb = cblas_trans_char(transb);
+    if (order == GbCblasColMajor) {
+        dgemm_(&ta, &tb, &m, &n, &k, &alpha, a, &lda, b, &ldb, &beta, c, &ldc);
+    } else if (order == GbCblasRowMajor) {
+        // row-major C = A B is column-major C^T = B^T A^T (cblas_dgemm.c:73-103)
+        dgemm_(&tb, &ta, &n, &m, &k, &alpha, b, &ldb, a, &lda, &beta, c, &ldc);
+    } else {
+        call_xerbla("cblas_dgemm", 1);
+    }
+}
+
+void cblas_sgemm(int order, int transa, int transb, gb_f77_int m, gb_f77_int n, gb_f77_int k,
+                 float alpha, const float* a, gb_f77_int lda, const float* b, gb_f77_int ldb,
+                 float beta, float* c, gb_f77_int ldc)
+{
+    char ta = cblas_trans_char(transa), tb = cblas_trans_char(transb);
+    if (order == GbCblasColMajor) sgemm_(&ta, &tb, &m, &n, &k, &alpha, a, &lda, b, &ldb, &beta, c, &ldc);
+    else if (order == GbCblasRowMajor) sgemm_(&tb, &ta, &n, &m, &k, &alpha, b, &ldb, a, &lda, &beta, c, &ldc);
+    else call_xerbla("cblas_sgemm", 1);
+}
+
+void cblas_dtrsm(int order, int side, int uplo, int transa, int diag, gb_f77_int m, gb_f77_int n,
+                 double alpha, const double* a, gb_f77_int lda, double* b, gb_f77_int ldb)
+{
+    char sd = side == GbCblasLeft ? 'L' : (side == GbCblasRight ? 'R' : '?');
+    char ul = uplo == GbCblasUpper ? 'U' : (uplo == GbCblasLower ? 'L' : '?');
+    char ta = cblas_trans_char(transa);
+    char dg = diag == GbCblasUnit ? 'U' : (diag == GbCblasNonUnit ? 'N' : '?');
+    if (order == GbCblasColMajor) {
+        dtrsm_(&sd, &ul, &ta, &dg, &m, &n, &alpha, a, &lda, b, &ldb);
+    } else if (order == GbCblasRowMajor) {
+        // row-major: swap side and uplo, swap m and n (cblas_dtrsm.c)
+        char sd2 = (sd == 'L') ? 'R' : (sd == 'R' ? 'L' : '?');
+        char ul2 = (ul == 'U') ? 'L' : (ul == 'L' ? 'U' : '?');
+        dtrsm_(&sd2, &ul2, &ta, &dg, &n, &m, &alpha, a, &lda, b, &ldb);
+    } else {
+        call_xerbla("cblas_dtrsm", 1);
+    }
+}
+
+void cblas_dgemv(int order, int transa, gb_f77_int m, gb_f77_int n, double alpha, const double* a,
+                 gb_f77_int lda, const double* x, gb_f77_int incx, double beta, double* y,
+                 gb_f77_int incy)
+{
+    char ta = cblas_trans_char(transa);
+    if (order == GbCblasColMajor) {
+        dgemv_(&ta, &m, &n, &alpha, a, &lda, x, &incx, &beta, y, &incy);
+    } else if (order == GbCblasRowMajor) {
+        char t2 = (ta == 'N') ? 'T' : 'N';
+        dgemv_(&t2, &n, &m, &alpha, a, &lda, x, &incx, &beta, y, &incy);
+    } else {
+        call_xerbla("cblas_dgemv", 1);
+    }
+}
+
+void cblas_daxpy(gb_f77_int n, double alpha, const double* x, gb_f77_int incx, double* y, gb_f77_int incy)
+{
+    daxpy_(&n, &alpha, x, &incx, y, &incy);
+}
+
+double cblas_ddot(gb_f77_int n, const double* x, gb_f77_int incx, const double* y, gb_f77_int incy)
+{
+    return ddot_(&n, x, &incx, y, &incy);
+}
+
+// ==================================================================== typed BLIS API
+void bli_dgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+               const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+               gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c, gb_inc_t rs_c,
+               gb_inc_t cs_c)
+{
+    gemm_host<double>(transa, transb, m, n, k, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c,
+                      cs_c, "bli_dgemm");
+}
+
+void bli_dgemm_ex(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                  const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                  const double* b, gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c,
+                  gb_inc_t rs_c, gb_inc_t cs_c, const void* cntx, const void* rntm)
+{
+    (void)cntx;
+    (void)rntm;
+    bli_dgemm(transa, transb, m, n, k, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c, cs_c);
+}
+
+void bli_sgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+               const float* alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a, const float* b,
+               gb_inc_t rs_b, gb_inc_t cs_b, const float* beta, float* c, gb_inc_t rs_c,
+               gb_inc_t cs_c)
+{
+    gemm_host<float>(transa, transb, m, n, k, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c,
+                     cs_c, "bli_sgemm");
+}
+
+void bli_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+               gb_dim_t n, const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               double* b, gb_inc_t rs_b, gb_inc_t cs_b)
+{
+    trsm_host(side, uploa, transa, diaga, m, n, *alpha, a, rs_a, cs_a, b, rs_b, cs_b);
+}
+
+void bli_dtrsm_ex(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+                  gb_dim_t n, const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                  double* b, gb_inc_t rs_b, gb_inc_t cs_b, const void* cntx, const void* rntm)
+{
+    (void)cntx;
+    (void)rntm;
+    bli_dtrsm(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b);
+}
+
+void bli_dgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, const double* alpha,
+               const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* x, gb_inc_t incx,
+               const double* beta, double* y, gb_inc_t incy)
+{
+    (void)conjx;
+    gemv_host(transa, m, n, *alpha, a, rs_a, cs_a, x, incx, *beta, y, incy, "bli_dgemv");
+}
+
+void bli_dgemv_ex(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, const double* alpha,
+                  const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* x, gb_inc_t incx,
+                  const double* beta, double* y, gb_inc_t incy, const void* cntx, const void* rntm)
+{
+    (void)cntx;
+    (void)rntm;
+    bli_dgemv(transa, conjx, m, n, alpha, a, rs_a, cs_a, x, incx, beta, y, incy);
+}
+
+void bli_daxpyv(gb_conj_t conjx, gb_dim_t n, const double* alpha, const double* x, gb_inc_t incx,
+                double* y, gb_inc_t incy)
+{
+    (void)conjx;
+    axpyv_host(n, *alpha, x, incx, y, incy);
+}
+
+void bli_daxpyv_ex(gb_conj_t conjx, gb_dim_t n, const double* alpha, const double* x, gb_inc_t incx,
+                   double* y, gb_inc_t incy, const void* cntx, const void* rntm)
+{
+    (void)cntx;
+    (void)rntm;
+    bli_daxpyv(conjx, n, alpha, x, incx, y, incy);
+}
+
+void bli_ddotv(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t n, const double* x, gb_inc_t incx,
+               const double* y, gb_inc_t incy, double* rho)
+{
+    (void)conjx;
+    (void)conjy;
+    dotv_host(n, x, incx, y, incy, rho);
+}
+
+void bli_ddotv_ex(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t n, const double* x, gb_inc_t incx,
+                  const double* y, gb_inc_t incy, double* rho, const void* cntx, const void* rntm)
+{
+    (void)cntx;
+    (void)rntm;
+    bli_ddotv(conjx, conjy, n, x, incx, y, incy, rho);
+}
+
+// ==================================================================== gb_ addon
+static cudaStream_t pick_stream(void* stream)
+{
+    return stream ? static_cast<cudaStream_t>(stream) : gb::thread_stream();
+}
+
+int gb_dgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                 double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c,
+                 gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_dgemm_dev", "negative dimension");
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    return gb::dgemm_native(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
+                            tb ? rs_b : cs_b, beta, c, rs_c, cs_c, pick_stream(stream));
+}
+
+int gb_dgemm_ozaki_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                       double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                       gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c,
+                       gb_inc_t cs_c, int slices, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_dgemm_ozaki_dev", "negative dimension");
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    return gb::dgemm_ozaki(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
+                           tb ? rs_b : cs_b, beta, c, rs_c, cs_c, slices, pick_stream(stream));
+}
+
+int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                 float alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a, const float* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, float beta, float* c, gb_inc_t rs_c, gb_inc_t cs_c,
+                 void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_sgemm_dev", "negative dimension");
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    return gb::sgemm_dev(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
+                         tb ? rs_b : cs_b, beta, c, rs_c, cs_c, pick_stream(stream));
+}
+
+int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+                 gb_dim_t n, double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, double* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_dtrsm_dev", "negative dimension");
+    const int slices = (gb::dgemm_mode() == GB_DGEMM_OZAKI) ? gb::ozaki_slices() : 0;
+    return gb::dtrsm_dev(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, slices,
+                         pick_stream(stream));
+}
+
+int gb_daxpyv_dev(gb_dim_t n, double alpha, const double* x, gb_inc_t incx, double* y, gb_inc_t incy,
+                  void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    return gb::daxpyv_dev(n, alpha, x, incx, y, incy, pick_stream(stream));
+}
+
+int gb_ddotv_dev(gb_dim_t n, const double* x, gb_inc_t incx, const double* y, gb_inc_t incy,
+                 double* rho, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    cudaStream_t s = pick_stream(stream);
+    const int nparts = gb::dotv_nparts(n > 0 ? n : 1);
+    double* scratch = static_cast<double*>(gb::dev_alloc(sizeof(double) * nparts, s));
+    if (!scratch) return GB_ERR_NOMEM;
+    rc = gb::ddotv_dev(n, x, incx, y, incy, rho, scratch, nparts, s);
+    gb::dev_free(scratch, s);
+    return rc;
+}
+
+int gb_dgemv_dev(gb_trans_t transa, gb_dim_t m, gb_dim_t n, double alpha, const double* a,
+                 gb_inc_t rs_a, gb_inc_t cs_a, const double* x, gb_inc_t incx, double beta, double* y,
+                 gb_inc_t incy, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    return gb::dgemv_dev(GB_IS_TRANS(transa) ? 1 : 0, m, n, alpha, a, rs_a, cs_a, x, incx, beta, y, incy,
+                         pick_stream(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+// gb_internal.h -- private declarations shared by the CUDA translation units
+// of libblis_gb300.so.  Nothing here is part of the exported C ABI (that is
+// include/blis_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/blis_gb300.h"
+
+// BLIS bit encodings (frame/include/bli_type_defs.h:395-427).
+#define GB_TRANS_BIT 0x08
+#define GB_CONJ_BIT 0x10
+#define GB_IS_TRANS(t) (((t) & GB_TRANS_BIT) != 0)
+
+namespace gb {
+
+// ---------------------------------------------------------------- status
+// Records a failure in the calling thread's status word and prints it once.
+int set_error(int code, const char* where, const char* what);
+int check_cuda(cudaError_t e, const char* where);
+#define GB_CUDA(call)                                                          \
+    do {                                                                       \
+        cudaError_t _e = (call);                                               \
+        if (_e != cudaSuccess) return ::gb::check_cuda(_e, #call);             \
+    } while (0)
+
+// ---------------------------------------------------------------- context
+// One CUDA stream per calling host thread (created lazily on the library's
+// device); device memory comes from a stream-ordered pool that keeps freed
+// blocks cached.
+cudaStream_t thread_stream();
+int ensure_init();
+int sm_count();
+
+// Stream-ordered device allocations (cudaMallocAsync on the pool).
+void* dev_alloc(size_t bytes, cudaStream_t s);
+void dev_free(void* p, cudaStream_t s);
+
+// Device-side status word shared by all kernels of the library: a kernel
+// that gives up on a bounded wait, or finds an impossible index, ORs a flag
+// into it and returns instead of trapping.
+unsigned int* device_status_word();
+int read_and_clear_device_status(cudaStream_t s, const char* where);
+
+enum : unsigned int {
+    DEV_WAIT_TIMEOUT = 1u,
+    DEV_BAD_INDEX = 2u,
+    DEV_INT_OVERFLOW = 4u,
+    DEV_NONFINITE = 8u,
+};
+
+// Wrap every kernel launch: counts it and, when per-kernel timing is on,
+// brackets it with CUDA events recorded on the launching stream.
+class LaunchScope {
+  public:
+    LaunchScope(const char* name, cudaStream_t s);
+    ~LaunchScope();
+
+  private:
+    const char* name_;
+    cudaStream_t s_;
+    bool timed_;
+    cudaEvent_t start_, stop_;
+};
+
+// Bounded-wait budget for spin loops in device code (nanoseconds of
+// %globaltimer); a wait that exceeds it reports DEV_WAIT_TIMEOUT.
+constexpr unsigned long long kWaitBudgetNs = 2000000000ull;
+
+// ---------------------------------------------------------------- kernels
+// All take device pointers and BLIS-style element strides (rs, cs).  op(A)
+// element (i, l) lives at a[i*ars + l*acs] after the caller folded the
+// transpose into the strides.
+int dgemm_native(int64_t m, int64_t n, int64_t k, double alpha,
+                 const double* a, int64_t ars, int64_t acs,
+                 const double* b, int64_t brs, int64_t bcs, double beta,
+                 double* c, int64_t rs_c, int64_t cs_c, cudaStream_t s);
+int sgemm_dev(int64_t m, int64_t n, int64_t k, float alpha,
+              const float* a, int64_t ars, int64_t acs,
+              const float* b, int64_t brs, int64_t bcs, float beta,
+              float* c, int64_t rs_c, int64_t cs_c, cudaStream_t s);
+int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
+                const double* a, int64_t ars, int64_t acs,
+                const double* b, int64_t brs, int64_t bcs, double beta,
+                double* c, int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s);
+int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, double alpha,
+              const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b,
+              int64_t cs_b, int slices, cudaStream_t s);
+int64_t ozaki_kpart_limit(int slices);
+int dotv_nparts(int64_t n);
+int scal_matrix(int64_t m, int64_t n, double beta, double* c, int64_t rs_c, int64_t cs_c,
+                cudaStream_t s);
+int scal_matrix_f(int64_t m, int64_t n, float beta, float* c, int64_t rs_c, int64_t cs_c,
+                  cudaStream_t s);
+int daxpyv_dev(int64_t n, double alpha, const double* x, int64_t incx, double* y,
+               int64_t incy, cudaStream_t s);
+int ddotv_dev(int64_t n, const double* x, int64_t incx, const double* y, int64_t incy,
+              double* rho_dev, double* scratch, int64_t scratch_len, cudaStream_t s);
+int dgemv_dev(int trans, int64_t m, int64_t n, double alpha, const double* a,
+              int64_t rs_a, int64_t cs_a, const double* x, int64_t incx, double beta,
+              double* y, int64_t incy, cudaStream_t s);
+
+// Default precision mode for dgemm entry points (GB_DGEMM_NATIVE or
+// GB_DGEMM_OZAKI) and slice count, set by gb_set_dgemm_mode().
+int dgemm_mode();
+int ozaki_slices();
+
+}  // namespace gb

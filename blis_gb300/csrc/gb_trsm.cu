@@ -1,0 +1,158 @@
+// gb_trsm.cu -- triangular solve with multiple right-hand sides for sm_103a
+// (bli_trsm_ex, frame/3/bli_l3_oapi_ex.c:692-801).
+//
+// The reference's blocked variant (frame/3/trsm/bli_trsm_blk_var1.c:37-189)
+// solves a KC x KC diagonal block, then updates the rest of B with gemm;
+// its macro-kernel walks MR-row panels serially (bli_trsm_ll_ker_var2.c).
+// On a GPU the serial part must stay small, so the solve is recursive:
+//     X1 = inv(L11) B1;  B2 -= L21 X1;  X2 = inv(L22) B2
+// down to diagonal blocks of at most 64 rows, which one kernel solves with
+// one thread per right-hand side (FP64, diagonal pre-inverted as with
+// BLIS_ENABLE_TRSM_PREINVERSION, ref_kernels/3/bli_trsm_ref.c:110-134).
+// Nearly all m^2 n flops land in the off-diagonal gemm updates, which run
+// on the native FP64 kernel or, in the precision form, on the Ozaki kernel.
+// Right-side solves are turned into left-side ones by swapping B's strides
+// and transposing A, the reduction of frame/3/bli_l3_oapi_ex.c:753-758.
+#include "gb_internal.h"
+
+namespace gb {
+namespace {
+
+constexpr int TRSM_NB = 64;
+
+// Solves op(A11) X = B1 in place for an nb x nb diagonal block.
+// op(A)(i, l) = a[i*ars + l*acs]; B(i, j) = b[i*brs + j*bcs].
+__global__ void trsm_diag_kernel(int nb, int lower, int unit, const double* __restrict__ a,
+                                 int64_t ars, int64_t acs, double* __restrict__ b, int64_t brs,
+                                 int64_t bcs, int64_t ncols)
+{
+    __shared__ double L[TRSM_NB][TRSM_NB + 1];
+    __shared__ double dinv[TRSM_NB];
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+        const int i = e % nb, l = e / nb;
+        const bool in_tri = lower ? (l <= i) : (l >= i);
+        L[i][l] = in_tri ? a[i * ars + l * acs] : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x < nb) dinv[threadIdx.x] = unit ? 1.0 : 1.0 / L[threadIdx.x][threadIdx.x];
+    __syncthreads();
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= ncols) return;
+    double x[TRSM_NB];
+    double* bj = b + j * bcs;
+#pragma unroll
+    for (int i = 0; i < TRSM_NB; ++i)
+        if (i < nb) x[i] = bj[i * brs];
+    if (lower) {
+#pragma unroll
+        for (int i = 0; i < TRSM_NB; ++i) {
+            if (i < nb) {
+                double t = x[i];
+#pragma unroll
+                for (int l = 0; l < TRSM_NB; ++l)
+                    if (l < i) t = fma(-L[i][l], x[l], t);
+                x[i] = t * dinv[i];
+            }
+        }
+    } else {
+#pragma unroll
+        for (int i = TRSM_NB - 1; i >= 0; --i) {
+            if (i < nb) {
+                double t = x[i];
+#pragma unroll
+                for (int l = 0; l < TRSM_NB; ++l)
+                    if (l > i && l < nb) t = fma(-L[i][l], x[l], t);
+                x[i] = t * dinv[i];
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < TRSM_NB; ++i)
+        if (i < nb) bj[i * brs] = x[i];
+}
+
+struct TrsmCtx {
+    int lower, unit, slices;
+    const double* a;
+    int64_t ars, acs;
+    double* b;
+    int64_t brs, bcs;
+    int64_t n;
+    cudaStream_t s;
+};
+
+int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t ccount)
+{
+    // B[r0:r0+rcount, :] -= op(A)[r0:.., c0:c0+ccount] * X[c0:c0+ccount, :]
+    const double* ap = t.a + r0 * t.ars + c0 * t.acs;
+    const double* xp = t.b + c0 * t.brs;
+    double* bp = t.b + r0 * t.brs;
+    if (t.slices > 0)
+        return dgemm_ozaki(rcount, t.n, ccount, -1.0, ap, t.ars, t.acs, xp, t.brs, t.bcs, 1.0, bp,
+                           t.brs, t.bcs, t.slices, t.s);
+    return dgemm_native(rcount, t.n, ccount, -1.0, ap, t.ars, t.acs, xp, t.brs, t.bcs, 1.0, bp,
+                        t.brs, t.bcs, t.s);
+}
+
+int solve(const TrsmCtx& t, int64_t r0, int64_t mm)
+{
+    if (mm <= TRSM_NB) {
+        const int blocks = (int)((t.n + 127) / 128);
+        LaunchScope ls("trsm_diag", t.s);
+        trsm_diag_kernel<<<blocks, 128, 0, t.s>>>((int)mm, t.lower, t.unit,
+                                                  t.a + r0 * t.ars + r0 * t.acs, t.ars, t.acs,
+                                                  t.b + r0 * t.brs, t.brs, t.bcs, t.n);
+        return check_cuda(cudaGetLastError(), "trsm_diag");
+    }
+    // split on a multiple of the diagonal block size
+    int64_t m1 = ((mm / 2 + TRSM_NB - 1) / TRSM_NB) * TRSM_NB;
+    if (m1 >= mm) m1 = mm - TRSM_NB;
+    const int64_t m2 = mm - m1;
+    int rc;
+    if (t.lower) {
+        if ((rc = solve(t, r0, m1))) return rc;
+        if ((rc = update(t, r0 + m1, m2, r0, m1))) return rc;
+        return solve(t, r0 + m1, m2);
+    }
+    if ((rc = solve(t, r0 + m1, m2))) return rc;
+    if ((rc = update(t, r0, m1, r0 + m1, m2))) return rc;
+    return solve(t, r0, m1);
+}
+
+}  // namespace
+
+int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, double alpha,
+              const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b,
+              int slices, cudaStream_t s)
+{
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    int64_t brs = rs_b, bcs = cs_b, mm = m, nn = n;
+    bool trans = GB_IS_TRANS(transa);
+    if (side == GB_RIGHT) {
+        brs = cs_b;
+        bcs = rs_b;
+        mm = n;
+        nn = m;
+        trans = !trans;
+    }
+    if (alpha == 0.0) return scal_matrix(mm, nn, 0.0, b, brs, bcs, s);
+    if (alpha != 1.0) {
+        int rc = scal_matrix(mm, nn, alpha, b, brs, bcs, s);
+        if (rc) return rc;
+    }
+    TrsmCtx t;
+    t.ars = trans ? cs_a : rs_a;
+    t.acs = trans ? rs_a : cs_a;
+    t.lower = ((uplo == GB_LOWER) != trans) ? 1 : 0;
+    t.unit = (diag == GB_UNIT_DIAG) ? 1 : 0;
+    t.slices = slices;
+    t.a = a;
+    t.b = b;
+    t.brs = brs;
+    t.bcs = bcs;
+    t.n = nn;
+    t.s = s;
+    return solve(t, 0, mm);
+}
+
+}  // namespace gb

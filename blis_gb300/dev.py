@@ -1,0 +1,123 @@
+"""Device-pointer bindings of the gb_ addon for torch tensors already in HBM.
+
+Strides are taken from the tensors (BLIS (rs, cs) convention, elements) and
+every call is issued on the tensor's current torch CUDA stream, so torch
+CUDA events recorded on that stream bracket exactly the library's kernels.
+"""
+import ctypes as C
+
+import torch
+
+from . import _lib
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _rc(t):
+    return t.stride(0), t.stride(1)
+
+
+def _k(trans, a):
+    return a.shape[0] if trans & 0x08 else a.shape[1]
+
+
+def dgemm(transa, transb, alpha, a, b, beta, c):
+    m, n = c.shape
+    rc = _lib.load().gb_dgemm_dev(transa, transb, m, n, _k(transa, a), alpha, a.data_ptr(), *_rc(a),
+                                  b.data_ptr(), *_rc(b), beta, c.data_ptr(), *_rc(c), _stream())
+    return _lib.check(rc, "gb_dgemm_dev")
+
+
+def dgemm_ozaki(transa, transb, alpha, a, b, beta, c, slices=8):
+    m, n = c.shape
+    rc = _lib.load().gb_dgemm_ozaki_dev(transa, transb, m, n, _k(transa, a), alpha, a.data_ptr(),
+                                        *_rc(a), b.data_ptr(), *_rc(b), beta, c.data_ptr(), *_rc(c),
+                                        slices, _stream())
+    return _lib.check(rc, "gb_dgemm_ozaki_dev")
+
+
+def sgemm(transa, transb, alpha, a, b, beta, c):
+    m, n = c.shape
+    rc = _lib.load().gb_sgemm_dev(transa, transb, m, n, _k(transa, a), alpha, a.data_ptr(), *_rc(a),
+                                  b.data_ptr(), *_rc(b), beta, c.data_ptr(), *_rc(c), _stream())
+    return _lib.check(rc, "gb_sgemm_dev")
+
+
+def dtrsm(side, uplo, transa, diag, alpha, a, b):
+    m, n = b.shape
+    rc = _lib.load().gb_dtrsm_dev(side, uplo, transa, diag, m, n, alpha, a.data_ptr(), *_rc(a),
+                                  b.data_ptr(), *_rc(b), _stream())
+    return _lib.check(rc, "gb_dtrsm_dev")
+
+
+def daxpyv(alpha, x, y, incx=1, incy=1, n=None):
+    n = x.numel() if n is None else n
+    rc = _lib.load().gb_daxpyv_dev(n, alpha, x.data_ptr(), incx, y.data_ptr(), incy, _stream())
+    return _lib.check(rc, "gb_daxpyv_dev")
+
+
+def ddotv(x, y, rho, incx=1, incy=1, n=None):
+    n = x.numel() if n is None else n
+    rc = _lib.load().gb_ddotv_dev(n, x.data_ptr(), incx, y.data_ptr(), incy, rho.data_ptr(), _stream())
+    return _lib.check(rc, "gb_ddotv_dev")
+
+
+def dgemv(transa, alpha, a, x, beta, y, incx=1, incy=1):
+    m, n = a.shape
+    rc = _lib.load().gb_dgemv_dev(transa, m, n, alpha, a.data_ptr(), *_rc(a), x.data_ptr(), incx, beta,
+                                  y.data_ptr(), incy, _stream())
+    return _lib.check(rc, "gb_dgemv_dev")
+
+
+RAND_UNIFORM, RAND_EXPSPREAD, RAND_NARROW_POW2 = 0, 1, 2
+
+
+def randm(x, kind, seed, p0=-1.0, p1=1.0):
+    """Fill a 2-D float64/float32 CUDA tensor in place with seeded values."""
+    m, n = x.shape
+    is_float = 1 if x.dtype == torch.float32 else 0
+    rc = _lib.load().gb_randm_dev(kind, is_float, x.data_ptr(), m, n, *_rc(x), seed, p0, p1, _stream())
+    return _lib.check(rc, "gb_randm_dev")
+
+
+def colmajor(m, n, dtype=torch.float64):
+    """An m x n CUDA tensor with column-major strides (1, m)."""
+    return torch.empty((n, m), dtype=dtype, device="cuda").t()
+
+
+def dd_gemm_entries(transa, transb, alpha, a, b, beta, c, ii, jj):
+    """Double-double (hi, lo) of selected entries of alpha*op(A)*op(B) + beta*C."""
+    k = _k(transa, a)
+    hi = torch.empty(ii.numel(), dtype=torch.float64, device="cuda")
+    lo = torch.empty_like(hi)
+    cp = c.data_ptr() if c is not None else None
+    crs, ccs = _rc(c) if c is not None else (1, 1)
+    rc = _lib.load().gb_dd_gemm_entries_dev(transa, transb, k, alpha, a.data_ptr(), *_rc(a), b.data_ptr(),
+                                            *_rc(b), beta, cp, crs, ccs, ii.numel(), ii.data_ptr(),
+                                            jj.data_ptr(), hi.data_ptr(), lo.data_ptr(), _stream())
+    _lib.check(rc, "gb_dd_gemm_entries_dev")
+    return hi, lo
+
+
+def componentwise_error(c_vals, hi, lo):
+    """max |c - (hi + lo)| / |hi + lo| over entries with a nonzero exact value."""
+    d = ((c_vals - hi) - lo).abs()
+    den = hi.abs()
+    mask = den > 0
+    return float((d[mask] / den[mask]).max()) if bool(mask.any()) else float(d.max())
+
+
+def set_kernel_timing(on):
+    _lib.load().gb_set_kernel_timing(1 if on else 0)
+
+
+def kernel_time_ms(prefix):
+    n = C.c_int64(0)
+    ms = _lib.load().gb_kernel_time_ms(prefix.encode(), C.byref(n))
+    return ms, int(n.value)
+
+
+def synchronize():
+    return _lib.check(_lib.load().gb_synchronize(), "gb_synchronize")

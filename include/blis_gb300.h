@@ -1,0 +1,343 @@
+/*
+ * blis_gb300.h -- C ABI of libblis_gb300.so, the GB300 (sm_103a) implementation
+ * of BLIS's dense hot path.
+ *
+ * Three groups of entry points:
+ *
+ *  1. Drop-ins with the exact signatures of the BLIS 1.0 entry points they
+ *     replace (BLAS compat layer, CBLAS, typed BLIS API).  They take HOST
+ *     pointers owned by the caller, move the operands through HBM, and
+ *     return with the result in place, like the CPU library.  Argument errors
+ *     go through xerbla_ exactly as frame/compat/check/bla_*_check.h does.
+ *  2. The "gb_" addon (device pointers, explicit CUDA stream) used by callers
+ *     that keep operands resident in HBM; the drop-ins are built on it.
+ *  3. Controls and introspection (precision mode, status, counters).
+ *
+ * Citations are to the BLIS 1.0 source tree (file:line).
+ * Integer widths follow BLIS: dim_t/inc_t are int64_t
+ * (frame/include/bli_type_defs.h:112-115); the BLAS integer is 32-bit
+ * (BLIS_BLAS_INT_TYPE_SIZE 32 default).  trans_t/conj_t/uplo_t/side_t/diag_t
+ * carry BLIS's bit encodings (frame/include/bli_type_defs.h:395-427).
+ */
+#ifndef BLIS_GB300_H
+#define BLIS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int64_t gb_dim_t;  /* dim_t */
+typedef int64_t gb_inc_t;  /* inc_t */
+typedef int32_t gb_f77_int;  /* f77_int (32-bit BLAS integer) */
+typedef char gb_f77_char;  /* f77_char */
+typedef int gb_trans_t;    /* trans_t: 0x00 N, 0x08 T, 0x10 conj-N, 0x18 conj-T */
+typedef int gb_conj_t;     /* conj_t:  0x00, 0x10 */
+typedef int gb_uplo_t;     /* uplo_t:  0xC0 lower, 0x60 upper */
+typedef int gb_side_t;     /* side_t:  0 left, 1 right */
+typedef int gb_diag_t;     /* diag_t:  0x000 non-unit, 0x100 unit */
+
+#define GB_NO_TRANSPOSE 0x00
+#define GB_TRANSPOSE 0x08
+#define GB_CONJ_NO_TRANSPOSE 0x10
+#define GB_CONJ_TRANSPOSE 0x18
+#define GB_NO_CONJUGATE 0x00
+#define GB_CONJUGATE 0x10
+#define GB_LOWER 0xC0
+#define GB_UPPER 0x60
+#define GB_LEFT 0
+#define GB_RIGHT 1
+#define GB_NONUNIT_DIAG 0x000
+#define GB_UNIT_DIAG 0x100
+
+/* Status codes of the gb_ addon (0 = success). */
+#define GB_SUCCESS 0
+#define GB_ERR_ARG (-1)
+#define GB_ERR_CUDA (-2)
+#define GB_ERR_DEVICE (-3)   /* a kernel reported a bounded-wait timeout or bad index */
+#define GB_ERR_NOMEM (-4)
+#define GB_ERR_UNSUPPORTED (-5)
+
+/* ===================================================================== */
+/* 1a. Fortran-77 BLAS compat layer                                        */
+/* ===================================================================== */
+
+/* replaces dgemm_/sgemm_, frame/compat/bla_gemm.c:122-262 (m==1 / n==1 go
+   to gemv as in :180-218; checks frame/compat/check/bla_gemm_check.h:37-86) */
+void dgemm_(const gb_f77_char* transa, const gb_f77_char* transb,
+            const gb_f77_int* m, const gb_f77_int* n, const gb_f77_int* k,
+            const double* alpha, const double* a, const gb_f77_int* lda,
+            const double* b, const gb_f77_int* ldb,
+            const double* beta, double* c, const gb_f77_int* ldc);
+void sgemm_(const gb_f77_char* transa, const gb_f77_char* transb,
+            const gb_f77_int* m, const gb_f77_int* n, const gb_f77_int* k,
+            const float* alpha, const float* a, const gb_f77_int* lda,
+            const float* b, const gb_f77_int* ldb,
+            const float* beta, float* c, const gb_f77_int* ldc);
+
+/* replaces dtrsm_, frame/compat/bla_trsm.c:121-219 (checks
+   frame/compat/check/bla_trmm_check.h:37-86) */
+void dtrsm_(const gb_f77_char* side, const gb_f77_char* uploa,
+            const gb_f77_char* transa, const gb_f77_char* diaga,
+            const gb_f77_int* m, const gb_f77_int* n, const double* alpha,
+            const double* a, const gb_f77_int* lda, double* b, const gb_f77_int* ldb);
+
+/* replaces dgemv_, frame/compat/bla_gemv.c:45-143 (checks
+   frame/compat/check/bla_gemv_check.h:37-75; n_x == 0 returns untouched, :95-106) */
+void dgemv_(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n,
+            const double* alpha, const double* a, const gb_f77_int* lda,
+            const double* x, const gb_f77_int* incx, const double* beta,
+            double* y, const gb_f77_int* incy);
+
+/* replaces daxpy_, frame/compat/bla_axpy.c:45-86 (negative increments:
+   frame/include/bli_blas_macro_defs.h:50-75) */
+void daxpy_(const gb_f77_int* n, const double* alpha, const double* x,
+            const gb_f77_int* incx, double* y, const gb_f77_int* incy);
+
+/* replaces ddot_, frame/compat/bla_dot.c:45-93 */
+double ddot_(const gb_f77_int* n, const double* x, const gb_f77_int* incx,
+             const double* y, const gb_f77_int* incy);
+
+/* replaces dgemm_batch_/sgemm_batch_, frame/compat/extra/bla_gemm_batch.c:135-249
+   (the reference loops over the problems serially, :227; here every group
+   member of every group runs in one grouped launch) */
+void dgemm_batch_(const gb_f77_char* transa_array, const gb_f77_char* transb_array,
+                  const gb_f77_int* m_array, const gb_f77_int* n_array,
+                  const gb_f77_int* k_array, const double* alpha_array,
+                  const double** a_array, const gb_f77_int* lda_array,
+                  const double** b_array, const gb_f77_int* ldb_array,
+                  const double* beta_array, double** c_array,
+                  const gb_f77_int* ldc_array, const gb_f77_int* group_count,
+                  const gb_f77_int* group_size);
+void sgemm_batch_(const gb_f77_char* transa_array, const gb_f77_char* transb_array,
+                  const gb_f77_int* m_array, const gb_f77_int* n_array,
+                  const gb_f77_int* k_array, const float* alpha_array,
+                  const float** a_array, const gb_f77_int* lda_array,
+                  const float** b_array, const gb_f77_int* ldb_array,
+                  const float* beta_array, float** c_array,
+                  const gb_f77_int* ldc_array, const gb_f77_int* group_count,
+                  const gb_f77_int* group_size);
+
+/* replaces xerbla_, frame/compat/f2c/bla_xerbla.c:45-88 (prints, returns) */
+int xerbla_(const gb_f77_char* srname, const gb_f77_int* info, long srname_len);
+
+/* ===================================================================== */
+/* 1b. CBLAS (frame/compat/cblas/src)                                     */
+/* ===================================================================== */
+enum GB_CBLAS_ORDER { GbCblasRowMajor = 101, GbCblasColMajor = 102 };
+enum GB_CBLAS_TRANSPOSE { GbCblasNoTrans = 111, GbCblasTrans = 112, GbCblasConjTrans = 113 };
+enum GB_CBLAS_UPLO { GbCblasUpper = 121, GbCblasLower = 122 };
+enum GB_CBLAS_DIAG { GbCblasNonUnit = 131, GbCblasUnit = 132 };
+enum GB_CBLAS_SIDE { GbCblasLeft = 141, GbCblasRight = 142 };
+
+/* replaces cblas_dgemm, frame/compat/cblas/src/cblas_dgemm.c:14-110 */
+void cblas_dgemm(int order, int transa, int transb, gb_f77_int m, gb_f77_int n,
+                 gb_f77_int k, double alpha, const double* a, gb_f77_int lda,
+                 const double* b, gb_f77_int ldb, double beta, double* c, gb_f77_int ldc);
+/* replaces cblas_sgemm, frame/compat/cblas/src/cblas_sgemm.c:14-110 */
+void cblas_sgemm(int order, int transa, int transb, gb_f77_int m, gb_f77_int n,
+                 gb_f77_int k, float alpha, const float* a, gb_f77_int lda,
+                 const float* b, gb_f77_int ldb, float beta, float* c, gb_f77_int ldc);
+/* replaces cblas_dtrsm, frame/compat/cblas/src/cblas_dtrsm.c:12-140 */
+void cblas_dtrsm(int order, int side, int uplo, int transa, int diag, gb_f77_int m,
+                 gb_f77_int n, double alpha, const double* a, gb_f77_int lda,
+                 double* b, gb_f77_int ldb);
+/* replaces cblas_dgemv, frame/compat/cblas/src/cblas_dgemv.c:11-80 */
+void cblas_dgemv(int order, int transa, gb_f77_int m, gb_f77_int n, double alpha,
+                 const double* a, gb_f77_int lda, const double* x, gb_f77_int incx,
+                 double beta, double* y, gb_f77_int incy);
+/* replaces cblas_daxpy / cblas_ddot, frame/compat/cblas/src/cblas_daxpy.c, cblas_ddot.c */
+void cblas_daxpy(gb_f77_int n, double alpha, const double* x, gb_f77_int incx, double* y,
+                 gb_f77_int incy);
+double cblas_ddot(gb_f77_int n, const double* x, gb_f77_int incx, const double* y,
+                  gb_f77_int incy);
+/* replaces cblas_dgemm_batch, frame/compat/cblas/src/extra/cblas_dgemm_batch.c:14-168 */
+void cblas_dgemm_batch(int order, const int* transa_array, const int* transb_array,
+                       const gb_f77_int* m_array, const gb_f77_int* n_array,
+                       const gb_f77_int* k_array, const double* alpha_array,
+                       const double** a_array, const gb_f77_int* lda_array,
+                       const double** b_array, const gb_f77_int* ldb_array,
+                       const double* beta_array, double** c_array,
+                       const gb_f77_int* ldc_array, gb_f77_int group_count,
+                       const gb_f77_int* group_size);
+
+/* ===================================================================== */
+/* 1c. Typed BLIS API (host pointers, general strides)                     */
+/* ===================================================================== */
+
+/* replaces bli_dgemm / bli_sgemm, frame/3/bli_l3_tapi.c (basic) and
+   bli_?gemm_ex, frame/3/bli_l3_tapi_ex.c:42-99 (cntx/rntm accepted and ignored) */
+void bli_dgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+               const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               const double* b, gb_inc_t rs_b, gb_inc_t cs_b, const double* beta,
+               double* c, gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_dgemm_ex(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                  const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                  const double* b, gb_inc_t rs_b, gb_inc_t cs_b, const double* beta,
+                  double* c, gb_inc_t rs_c, gb_inc_t cs_c, const void* cntx, const void* rntm);
+void bli_sgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+               const float* alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               const float* b, gb_inc_t rs_b, gb_inc_t cs_b, const float* beta,
+               float* c, gb_inc_t rs_c, gb_inc_t cs_c);
+
+/* replaces bli_dtrsm / bli_dtrsm_ex, frame/3/bli_l3_tapi_ex.c:533-586 */
+void bli_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
+               gb_dim_t m, gb_dim_t n, const double* alpha, const double* a,
+               gb_inc_t rs_a, gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b);
+void bli_dtrsm_ex(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
+                  gb_dim_t m, gb_dim_t n, const double* alpha, const double* a,
+                  gb_inc_t rs_a, gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b,
+                  const void* cntx, const void* rntm);
+
+/* replaces bli_dgemv / bli_dgemv_ex, frame/2/bli_l2_tapi.c:43-127 */
+void bli_dgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n,
+               const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               const double* x, gb_inc_t incx, const double* beta, double* y, gb_inc_t incy);
+void bli_dgemv_ex(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n,
+                  const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                  const double* x, gb_inc_t incx, const double* beta, double* y,
+                  gb_inc_t incy, const void* cntx, const void* rntm);
+
+/* replaces bli_daxpyv / bli_daxpyv_ex, frame/1/bli_l1v_tapi.c:155-191 */
+void bli_daxpyv(gb_conj_t conjx, gb_dim_t n, const double* alpha, const double* x,
+                gb_inc_t incx, double* y, gb_inc_t incy);
+void bli_daxpyv_ex(gb_conj_t conjx, gb_dim_t n, const double* alpha, const double* x,
+                   gb_inc_t incx, double* y, gb_inc_t incy, const void* cntx,
+                   const void* rntm);
+
+/* replaces bli_ddotv / bli_ddotv_ex, frame/1/bli_l1v_tapi.c:195-232 */
+void bli_ddotv(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t n, const double* x,
+               gb_inc_t incx, const double* y, gb_inc_t incy, double* rho);
+void bli_ddotv_ex(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t n, const double* x,
+                  gb_inc_t incx, const double* y, gb_inc_t incy, double* rho,
+                  const void* cntx, const void* rntm);
+
+/* ===================================================================== */
+/* 2. gb_ addon: device pointers, explicit stream (NULL = the calling      */
+/*    thread's library stream).  Return GB_SUCCESS or a negative code.     */
+/*    Device operands use the same (rs, cs) element-stride convention as   */
+/*    the typed BLIS API.  Calls are asynchronous on the given stream.     */
+/* ===================================================================== */
+
+/* Native FP64 GEMM on the FP64 pipe: C := beta*C + alpha*op(A)*op(B).
+   Counterpart of bli_gemm_ex, frame/3/bli_l3_oapi_ex.c:48-148. */
+int gb_dgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                 double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                 const double* b, gb_inc_t rs_b, gb_inc_t cs_b, double beta,
+                 double* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+
+/* Ozaki split-product DGEMM: FP64 operands cut into `slices` bf16 digit
+   slices, products on the tcgen05 tensor cores, exact integer level sums,
+   FP64 recombination.  No reference counterpart (precision form). */
+int gb_dgemm_ozaki_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+                       gb_dim_t k, double alpha, const double* a, gb_inc_t rs_a,
+                       gb_inc_t cs_a, const double* b, gb_inc_t rs_b, gb_inc_t cs_b,
+                       double beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c, int slices,
+                       void* stream);
+
+int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                 float alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                 const float* b, gb_inc_t rs_b, gb_inc_t cs_b, float beta,
+                 float* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+
+/* Counterpart of bli_trsm_ex, frame/3/bli_l3_oapi_ex.c:692-801. */
+int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
+                 gb_dim_t m, gb_dim_t n, double alpha, const double* a, gb_inc_t rs_a,
+                 gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
+
+/* Counterparts of the axpyv / dotv / gemv kernels (frame/1/bli_l1v_ker_params.h:61-83,
+   frame/2/bli_l2_tapi.c:43-127).  gb_ddotv_dev writes rho to DEVICE memory. */
+int gb_daxpyv_dev(gb_dim_t n, double alpha, const double* x, gb_inc_t incx, double* y,
+                  gb_inc_t incy, void* stream);
+int gb_ddotv_dev(gb_dim_t n, const double* x, gb_inc_t incx, const double* y,
+                 gb_inc_t incy, double* rho, void* stream);
+int gb_dgemv_dev(gb_trans_t transa, gb_dim_t m, gb_dim_t n, double alpha, const double* a,
+                 gb_inc_t rs_a, gb_inc_t cs_a, const double* x, gb_inc_t incx,
+                 double beta, double* y, gb_inc_t incy, void* stream);
+
+/* One problem of a grouped GEMM on device operands (column-major, BLAS
+   leading dimensions): C := beta*C + alpha*op(A)*op(B). */
+typedef struct {
+    gb_trans_t transa, transb;
+    gb_dim_t m, n, k;
+    double alpha, beta;
+    const void* a;
+    gb_inc_t lda;
+    const void* b;
+    gb_inc_t ldb;
+    void* c;
+    gb_inc_t ldc;
+} gb_gemm_problem_t;
+
+#define GB_BATCH_GROUPED 0  /* one persistent launch, device tile scheduler */
+#define GB_BATCH_LOOP 1     /* one launch per problem (comparison baseline) */
+
+/* Counterpart of dgemm_batch_/sgemm_batch_ (frame/compat/extra/bla_gemm_batch.c:
+   135-249) on device operands; dtype 0 = FP64, 1 = FP32. */
+int gb_gemm_batch_dev(const gb_gemm_problem_t* probs, gb_dim_t count, int dtype, int mode,
+                      void* stream);
+
+/* Resident plan for repeated grouped launches: the descriptor table stays in
+   HBM and gb_batch_plan_run(use_graph=1) replays the counter reset and the
+   grouped launch as one captured CUDA graph. */
+int gb_batch_plan_create(const gb_gemm_problem_t* probs, gb_dim_t count, int dtype, void** plan);
+int gb_batch_plan_run(void* plan, int use_graph, void* stream);
+int gb_batch_plan_destroy(void* plan);
+
+/* Seeded matrix fill on the device, the counterpart of bli_randm (frame/util,
+   value generators frame/include/bli_cast_macro_defs.h:465-525) with a
+   counter-based generator: element (i, j) of the logical m x n matrix takes
+   index i + j*m, so values do not depend on the storage strides.
+   GB_RAND_UNIFORM: uniform [p0, p1); GB_RAND_EXPSPREAD: (1+u) 2^e, e uniform
+   integer in [p0, p1], random sign; GB_RAND_NARROW_POW2: {0, +-2^0..+-2^-6}. */
+#define GB_RAND_UNIFORM 0
+#define GB_RAND_EXPSPREAD 1
+#define GB_RAND_NARROW_POW2 2
+int gb_randm_dev(int kind, int is_float, void* x, gb_dim_t m, gb_dim_t n, gb_inc_t rs,
+                 gb_inc_t cs, uint64_t seed, double p0, double p1, void* stream);
+
+/* Double-double value (hi + lo) of entries (ii[e], jj[e]) of
+   alpha*op(A)*op(B) + beta*C, for reporting the max componentwise error of a
+   GEMM result.  All pointers are device pointers.  No reference counterpart. */
+int gb_dd_gemm_entries_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t k, double alpha,
+                           const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                           gb_inc_t rs_b, gb_inc_t cs_b, double beta, const double* c,
+                           gb_inc_t rs_c, gb_inc_t cs_c, gb_dim_t nent, const int64_t* ii,
+                           const int64_t* jj, double* hi, double* lo, void* stream);
+
+/* ===================================================================== */
+/* 3. Controls and introspection                                           */
+/* ===================================================================== */
+
+/* Selects the device used by this library (default: the current device). */
+int gb_init(int device);
+
+/* Routes dgemm_ / cblas_dgemm / bli_dgemm through the native FP64 kernel
+   (GB_DGEMM_NATIVE) or the Ozaki split form with the given slice count. */
+#define GB_DGEMM_NATIVE 0
+#define GB_DGEMM_OZAKI 1
+int gb_set_dgemm_mode(int mode, int slices);
+
+/* Last error of the calling thread (GB_SUCCESS if none), with its message. */
+int gb_get_last_error(char* msg, size_t len);
+void gb_clear_last_error(void);
+
+/* Number of kernels this library has launched since load. */
+int64_t gb_launch_count(void);
+
+/* Per-kernel device time (CUDA events on the launching stream), enabled by
+   gb_set_kernel_timing(1).  gb_kernel_time_ms() synchronises the recorded
+   events and returns the summed time and launch count of kernels whose name
+   starts with `prefix`, then forgets them. */
+int gb_set_kernel_timing(int enable);
+double gb_kernel_time_ms(const char* prefix, int64_t* launches);
+
+/* Blocks until the calling thread's library stream is idle. */
+int gb_synchronize(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BLIS_GB300_H */

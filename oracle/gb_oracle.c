@@ -1,0 +1,557 @@
+/*
+ * gb_oracle.c -- CPU restatement of the BLIS dense hot path.  TEST
+ * INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference leg of bench.py, always as the checker or the
+ * timed CPU baseline, never as part of the product.
+ *
+ * Compiled with -ffp-contract=off: every fused multiply-add below is an
+ * explicit fma(), so the results are bit-identical on x86-64 and aarch64.
+ *
+ * Reference behaviour restated here (paths relative to the BLIS 1.0 tree):
+ *   gemm  early exits          frame/3/bli_l3_util.c:41-65
+ *         five-loop algorithm  frame/3/gemm/bli_gemm_blk_var{1,2,3}.c,
+ *                              bli_gemm_ker_var2.c:216-276 (JR/IR loops);
+ *                              beta applied at the first KC block only
+ *                              (bli_gemm_blk_var3.c:108-110)
+ *         micro-kernel math    ref_kernels/3/bli_gemm_ref.c:40-130
+ *                              (ab = sum_k a*b; ab *= alpha;
+ *                               beta == 0 ? c = ab : c = ab + beta*c)
+ *   trsm  left/right reduction frame/3/bli_l3_oapi_ex.c:753-758
+ *         blocked solve + gemm frame/3/trsm/bli_trsm_blk_var1.c:37-189
+ *         pre-inverted diagonal ref_kernels/3/bli_trsm_ref.c:40-125
+ *   gemv  var2 (axpyf), var1 (dotxf) frame/2/gemv/bli_gemv_unf_var2.c:37-129,
+ *                              bli_gemv_unf_var1.c:37-102; beta == 0 is setv
+ *   axpyv ref_kernels/1/bli_axpyv_ref.c:37-120 (alpha == 0 returns)
+ *   dotv  ref_kernels/1/bli_dotv_ref.c:37-121 (n == 0 gives rho = 0)
+ * Not in the reference: the double-double evaluator (error oracle) and the
+ * Ozaki split-product model (Ozaki, Ogita, Oishi & Rump 2012; integer-slice
+ * variant of Ootomo, Ozaki & Yokota 2024), restated from the papers.
+ */
+#include "gb_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ */
+/* RNG: SplitMix64 finaliser applied to seed and element index.        */
+/* ------------------------------------------------------------------ */
+#define GOLDEN 0x9E3779B97F4A7C15ull
+
+uint64_t orc_mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+uint64_t orc_hash(uint64_t seed, uint64_t idx)
+{
+    return orc_mix64(orc_mix64(seed + GOLDEN) + (idx + 1) * GOLDEN);
+}
+
+static inline double u01(uint64_t h) { return (double)(h >> 11) * 0x1.0p-53; }
+
+void orc_fill_uniform(double* x, int64_t n, uint64_t seed, double lo, double hi)
+{
+    const double w = hi - lo;
+    for (int64_t i = 0; i < n; ++i) x[i] = lo + w * u01(orc_hash(seed, (uint64_t)i));
+}
+
+void orc_fill_uniform_f(float* x, int64_t n, uint64_t seed, double lo, double hi)
+{
+    const double w = hi - lo;
+    for (int64_t i = 0; i < n; ++i) x[i] = (float)(lo + w * u01(orc_hash(seed, (uint64_t)i)));
+}
+
+/* (1 + u) * 2^e with random sign; e uniform integer in [emin, emax]. */
+void orc_fill_expspread(double* x, int64_t n, uint64_t seed, int emin, int emax)
+{
+    const uint64_t span = (uint64_t)(emax - emin + 1);
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t h = orc_hash(seed, (uint64_t)i);
+        double mant = 1.0 + (double)(h >> 12) * 0x1.0p-52;
+        int e = emin + (int)(((h >> 1) & 0x7FFull) % span);
+        double v = ldexp(mant, e);
+        x[i] = (h & 1ull) ? -v : v;
+    }
+}
+
+/* {0, +-2^0 .. +-2^-6}, the testsuite's "narrow power of two" values
+   (frame/include/bli_cast_macro_defs.h:477-525). */
+void orc_fill_narrow_pow2(double* x, int64_t n, uint64_t seed)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t h = orc_hash(seed, (uint64_t)i);
+        int t = (int)(h & 7ull);
+        double v = (t == 0) ? 0.0 : ldexp(1.0, -(t - 1));
+        x[i] = ((h >> 3) & 1ull) ? -v : v;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Tiny pthread parallel-for.                                          */
+/* ------------------------------------------------------------------ */
+typedef void (*orc_task_fn)(void* arg, int tid, int nt);
+typedef struct { orc_task_fn fn; void* arg; int tid; int nt; } orc_task_t;
+
+static void* orc_task_tramp(void* p)
+{
+    orc_task_t* t = (orc_task_t*)p;
+    t->fn(t->arg, t->tid, t->nt);
+    return NULL;
+}
+
+static void orc_parallel(orc_task_fn fn, void* arg, int nt)
+{
+    if (nt <= 1) { fn(arg, 0, 1); return; }
+    pthread_t th[256];
+    orc_task_t ts[256];
+    if (nt > 256) nt = 256;
+    for (int t = 0; t < nt; ++t) {
+        ts[t].fn = fn; ts[t].arg = arg; ts[t].tid = t; ts[t].nt = nt;
+        if (t > 0) pthread_create(&th[t], NULL, orc_task_tramp, &ts[t]);
+    }
+    fn(arg, 0, nt);
+    for (int t = 1; t < nt; ++t) pthread_join(th[t], NULL);
+}
+
+/* ------------------------------------------------------------------ */
+/* Five-loop GEMM (JC -> PC -> pack B -> IC -> pack A -> JR/IR -> ukr). */
+/* Instantiated for double and float by a macro.                        */
+/* ------------------------------------------------------------------ */
+#define ORC_TRANS(t) (((t) & ORC_TRANSPOSE) != 0)
+
+#define GEN_GEMM(T, CH, FMA, MR, NR, MC, KC, NC)                                         \
+static void CH##_ukr(int64_t kc, const T* restrict ap, const T* restrict bp,             \
+                     T* restrict ab)                                                      \
+{                                                                                        \
+    T acc[NR][MR];                                                                       \
+    for (int j = 0; j < NR; ++j) for (int i = 0; i < MR; ++i) acc[j][i] = (T)0;          \
+    for (int64_t l = 0; l < kc; ++l) {                                                   \
+        const T* a = ap + l * MR; const T* b = bp + l * NR;                              \
+        for (int j = 0; j < NR; ++j) {                                                   \
+            const T bj = b[j];                                                           \
+            for (int i = 0; i < MR; ++i) acc[j][i] = FMA(a[i], bj, acc[j][i]);           \
+        }                                                                                \
+    }                                                                                    \
+    for (int j = 0; j < NR; ++j) for (int i = 0; i < MR; ++i) ab[j * MR + i] = acc[j][i];\
+}                                                                                        \
+                                                                                         \
+/* C[0:m,0:n] := beta*C + alpha*A*B where A(i,l) = a[i*ars+l*acs], B(l,j)=b[l*brs+j*bcs] */\
+static void CH##_gemm_serial(int64_t m, int64_t n, int64_t k, T alpha,                   \
+                             const T* a, int64_t ars, int64_t acs,                        \
+                             const T* b, int64_t brs, int64_t bcs, T beta,                \
+                             T* c, int64_t rs_c, int64_t cs_c)                            \
+{                                                                                        \
+    T* apack = (T*)malloc(sizeof(T) * (size_t)(MC + MR) * KC);                           \
+    T* bpack = (T*)malloc(sizeof(T) * (size_t)KC * (NC + NR));                           \
+    T ab[MR * NR];                                                                       \
+    for (int64_t jc = 0; jc < n; jc += NC) {                                             \
+        const int64_t nc = (n - jc < NC) ? n - jc : NC;                                  \
+        for (int64_t pc = 0; pc < k; pc += KC) {                                         \
+            const int64_t kc = (k - pc < KC) ? k - pc : KC;                              \
+            const T beta_use = (pc == 0) ? beta : (T)1;                                  \
+            for (int64_t jp = 0; jp < nc; jp += NR)                                      \
+                for (int64_t l = 0; l < kc; ++l)                                         \
+                    for (int j = 0; j < NR; ++j) {                                       \
+                        int64_t jj = jc + jp + j;                                        \
+                        bpack[(jp / NR) * KC * NR + l * NR + j] = (jp + j < nc)          \
+                            ? b[(pc + l) * brs + jj * bcs] : (T)0;                       \
+                    }                                                                    \
+            for (int64_t ic = 0; ic < m; ic += MC) {                                     \
+                const int64_t mc = (m - ic < MC) ? m - ic : MC;                          \
+                for (int64_t ip = 0; ip < mc; ip += MR)                                  \
+                    for (int64_t l = 0; l < kc; ++l)                                     \
+                        for (int i = 0; i < MR; ++i) {                                   \
+                            int64_t ii = ic + ip + i;                                    \
+                            apack[(ip / MR) * KC * MR + l * MR + i] = (ip + i < mc)      \
+                                ? a[ii * ars + (pc + l) * acs] : (T)0;                   \
+                        }                                                                \
+                for (int64_t jr = 0; jr < nc; jr += NR) {                                \
+                    const int64_t nr = (nc - jr < NR) ? nc - jr : NR;                    \
+                    for (int64_t ir = 0; ir < mc; ir += MR) {                            \
+                        const int64_t mr = (mc - ir < MR) ? mc - ir : MR;                \
+                        CH##_ukr(kc, apack + (ir / MR) * KC * MR,                        \
+                                 bpack + (jr / NR) * KC * NR, ab);                       \
+                        for (int64_t j = 0; j < nr; ++j)                                 \
+                            for (int64_t i = 0; i < mr; ++i) {                           \
+                                T* cij = c + (ic + ir + i) * rs_c + (jc + jr + j) * cs_c;\
+                                T t = alpha * ab[j * MR + i];                            \
+                                *cij = (beta_use == (T)0) ? t : FMA(beta_use, *cij, t);  \
+                            }                                                            \
+                    }                                                                    \
+                }                                                                        \
+            }                                                                            \
+        }                                                                                \
+    }                                                                                    \
+    free(apack); free(bpack);                                                            \
+}                                                                                        \
+                                                                                         \
+typedef struct { int64_t m, n, k; T alpha, beta; const T* a; int64_t ars, acs;           \
+                 const T* b; int64_t brs, bcs; T* c; int64_t rs_c, cs_c; int tm, tn; }   \
+    CH##_gemm_args;                                                                      \
+                                                                                         \
+static void CH##_gemm_task(void* p, int tid, int nt)                                     \
+{                                                                                        \
+    CH##_gemm_args* g = (CH##_gemm_args*)p; (void)nt;                                    \
+    int ti = tid % g->tm, tj = tid / g->tm;                                              \
+    int64_t r0 = g->m * ti / g->tm, r1 = g->m * (ti + 1) / g->tm;                        \
+    int64_t c0 = g->n * tj / g->tn, c1 = g->n * (tj + 1) / g->tn;                        \
+    /* keep row splits on MR boundaries so the partition does not change results */    \
+    r0 = (r0 / MR) * MR; r1 = (ti + 1 == g->tm) ? g->m : (r1 / MR) * MR;                 \
+    if (r1 <= r0 || c1 <= c0) return;                                                    \
+    CH##_gemm_serial(r1 - r0, c1 - c0, g->k, g->alpha, g->a + r0 * g->ars, g->ars,       \
+                     g->acs, g->b + c0 * g->bcs, g->brs, g->bcs, g->beta,                \
+                     g->c + r0 * g->rs_c + c0 * g->cs_c, g->rs_c, g->cs_c);              \
+}                                                                                        \
+                                                                                         \
+static void CH##_scalm(int64_t m, int64_t n, T beta, T* c, int64_t rs_c, int64_t cs_c)  \
+{                                                                                        \
+    for (int64_t j = 0; j < n; ++j)                                                      \
+        for (int64_t i = 0; i < m; ++i) {                                                \
+            T* cij = c + i * rs_c + j * cs_c;                                            \
+            *cij = (beta == (T)0) ? (T)0 : beta * *cij;                                  \
+        }                                                                                \
+}                                                                                        \
+                                                                                         \
+void orc_##CH##gemm(int transa, int transb, int64_t m, int64_t n, int64_t k,            \
+                    T alpha, const T* a, int64_t rs_a, int64_t cs_a,                     \
+                    const T* b, int64_t rs_b, int64_t cs_b,                              \
+                    T beta, T* c, int64_t rs_c, int64_t cs_c, int nthreads)              \
+{                                                                                        \
+    if (m <= 0 || n <= 0) return;                                                        \
+    if (alpha == (T)0 || k <= 0) { CH##_scalm(m, n, beta, c, rs_c, cs_c); return; }      \
+    CH##_gemm_args g;                                                                    \
+    g.m = m; g.n = n; g.k = k; g.alpha = alpha; g.beta = beta;                           \
+    g.a = a; g.ars = ORC_TRANS(transa) ? cs_a : rs_a; g.acs = ORC_TRANS(transa) ? rs_a : cs_a; \
+    g.b = b; g.brs = ORC_TRANS(transb) ? cs_b : rs_b; g.bcs = ORC_TRANS(transb) ? rs_b : cs_b; \
+    g.c = c; g.rs_c = rs_c; g.cs_c = cs_c;                                               \
+    int nt = nthreads < 1 ? 1 : nthreads;                                                \
+    /* 2-D thread grid: tm x tn, rows get the larger share when m >= n */               \
+    int best_tm = 1; double best = 1e300;                                                \
+    for (int tm = 1; tm <= nt; ++tm) {                                                   \
+        if (nt % tm) continue;                                                           \
+        int tn = nt / tm;                                                                \
+        double cost = (double)m / tm * k + (double)n / tn * k; /* packing traffic */     \
+        if ((m + tm - 1) / tm < MR && tm > 1) continue;                                  \
+        if (cost < best) { best = cost; best_tm = tm; }                                  \
+    }                                                                                    \
+    g.tm = best_tm; g.tn = nt / best_tm;                                                 \
+    orc_parallel(CH##_gemm_task, &g, nt);                                                \
+}
+
+GEN_GEMM(double, d, fma, 8, 6, 128, 256, 3072)
+GEN_GEMM(float, s, fmaf, 16, 6, 128, 256, 3072)
+
+/* ------------------------------------------------------------------ */
+/* TRSM: left solves only; the right side is handled by transposing    */
+/* B and A (frame/3/bli_l3_oapi_ex.c:753-758).                         */
+/* ------------------------------------------------------------------ */
+#define TRSM_NB 128
+
+void orc_dtrsm(int side, int uplo, int transa, int diag, int64_t m, int64_t n,
+               double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+               double* b, int64_t rs_b, int64_t cs_b, int nthreads)
+{
+    if (m <= 0 || n <= 0) return;
+    int64_t brs = rs_b, bcs = cs_b, mm = m, nn = n;
+    int trans = ORC_TRANS(transa);
+    if (side == ORC_RIGHT) {
+        /* B*inv(op(A)) = (inv(op(A))^T * B^T)^T */
+        brs = cs_b; bcs = rs_b; mm = n; nn = m; trans = !trans;
+    }
+    /* effective op(A)(i,l) = a[i*ars + l*acs] */
+    const int64_t ars = trans ? cs_a : rs_a, acs = trans ? rs_a : cs_a;
+    const int lower = ((uplo == ORC_LOWER) != (trans != 0));
+    const int unit = (diag == ORC_UNIT_DIAG);
+
+    if (alpha == 0.0) {
+        for (int64_t j = 0; j < nn; ++j) for (int64_t i = 0; i < mm; ++i) b[i * brs + j * bcs] = 0.0;
+        return;
+    }
+    if (alpha != 1.0)
+        for (int64_t j = 0; j < nn; ++j) for (int64_t i = 0; i < mm; ++i) b[i * brs + j * bcs] *= alpha;
+
+    for (int64_t blk = 0; blk < mm; blk += TRSM_NB) {
+        const int64_t nb = (mm - blk < TRSM_NB) ? mm - blk : TRSM_NB;
+        /* block rows [i0, i0+nb) processed in forward (lower) or backward (upper) order */
+        const int64_t i0 = lower ? blk : mm - blk - nb;
+        for (int64_t j = 0; j < nn; ++j) {
+            double* bj = b + j * bcs;
+            if (lower) {
+                for (int64_t i = i0; i < i0 + nb; ++i) {
+                    double t = bj[i * brs];
+                    for (int64_t l = i0; l < i; ++l) t = fma(-a[i * ars + l * acs], bj[l * brs], t);
+                    bj[i * brs] = unit ? t : t * (1.0 / a[i * ars + i * acs]);
+                }
+            } else {
+                for (int64_t i = i0 + nb - 1; i >= i0; --i) {
+                    double t = bj[i * brs];
+                    for (int64_t l = i + 1; l < i0 + nb; ++l) t = fma(-a[i * ars + l * acs], bj[l * brs], t);
+                    bj[i * brs] = unit ? t : t * (1.0 / a[i * ars + i * acs]);
+                }
+            }
+        }
+        /* update the rows not yet solved: B2 -= A21 * X1 */
+        if (lower && i0 + nb < mm) {
+            const int64_t r0 = i0 + nb, rcount = mm - r0;
+            orc_dgemm(ORC_NO_TRANSPOSE, ORC_NO_TRANSPOSE, rcount, nn, nb, -1.0,
+                      a + r0 * ars + i0 * acs, ars, acs, b + i0 * brs, brs, bcs,
+                      1.0, b + r0 * brs, brs, bcs, nthreads);
+        } else if (!lower && i0 > 0) {
+            orc_dgemm(ORC_NO_TRANSPOSE, ORC_NO_TRANSPOSE, i0, nn, nb, -1.0,
+                      a + i0 * acs, ars, acs, b + i0 * brs, brs, bcs,
+                      1.0, b, brs, bcs, nthreads);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Level-2 / level-1v                                                  */
+/* ------------------------------------------------------------------ */
+void orc_dgemv(int transa, int conjx, int64_t m, int64_t n, double alpha,
+               const double* a, int64_t rs_a, int64_t cs_a,
+               const double* x, int64_t incx, double beta, double* y, int64_t incy)
+{
+    (void)conjx;
+    const int trans = ORC_TRANS(transa);
+    const int64_t my = trans ? n : m, nx = trans ? m : n;
+    if (my <= 0) return;
+    /* y := beta*y, with beta == 0 overwriting (setv) */
+    for (int64_t i = 0; i < my; ++i) y[i * incy] = (beta == 0.0) ? 0.0 : beta * y[i * incy];
+    if (nx <= 0 || alpha == 0.0) return;
+    if (!trans) {
+        /* var2: y += (alpha*x_j) * a_j, column by column */
+        for (int64_t j = 0; j < n; ++j) {
+            const double chi = alpha * x[j * incx];
+            for (int64_t i = 0; i < m; ++i) y[i * incy] = fma(chi, a[i * rs_a + j * cs_a], y[i * incy]);
+        }
+    } else {
+        /* var1: y_i += alpha * (a_i^T x) */
+        for (int64_t i = 0; i < n; ++i) {
+            double rho = 0.0;
+            for (int64_t l = 0; l < m; ++l) rho = fma(a[l * rs_a + i * cs_a], x[l * incx], rho);
+            y[i * incy] = fma(alpha, rho, y[i * incy]);
+        }
+    }
+}
+
+void orc_daxpyv(int conjx, int64_t n, double alpha, const double* x, int64_t incx,
+                double* y, int64_t incy)
+{
+    (void)conjx;
+    if (n <= 0 || alpha == 0.0) return;
+    for (int64_t i = 0; i < n; ++i) y[i * incy] = fma(alpha, x[i * incx], y[i * incy]);
+}
+
+void orc_ddotv(int conjx, int conjy, int64_t n, const double* x, int64_t incx,
+               const double* y, int64_t incy, double* rho)
+{
+    (void)conjx; (void)conjy;
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s = fma(x[i * incx], y[i * incy], s);
+    *rho = s;
+}
+
+/* ------------------------------------------------------------------ */
+/* Double-double evaluation (Dekker/Knuth error-free transformations). */
+/* ------------------------------------------------------------------ */
+typedef struct { double hi, lo; } dd_t;
+
+static inline dd_t two_sum(double a, double b)
+{
+    double s = a + b, bb = s - a;
+    dd_t r = { s, (a - (s - bb)) + (b - bb) };
+    return r;
+}
+
+static inline dd_t fast_two_sum(double a, double b)
+{
+    double s = a + b;
+    dd_t r = { s, b - (s - a) };
+    return r;
+}
+
+static inline dd_t dd_add(dd_t x, dd_t y)
+{
+    dd_t s = two_sum(x.hi, y.hi);
+    dd_t t = two_sum(x.lo, y.lo);
+    s.lo += t.hi;
+    s = fast_two_sum(s.hi, s.lo);
+    s.lo += t.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+
+static inline dd_t dd_mul_d(dd_t x, double b)
+{
+    double p = x.hi * b;
+    double e = fma(x.hi, b, -p);
+    e = fma(x.lo, b, e);
+    return fast_two_sum(p, e);
+}
+
+static inline dd_t two_prod(double a, double b)
+{
+    double p = a * b;
+    dd_t r = { p, fma(a, b, -p) };
+    return r;
+}
+
+typedef struct {
+    int64_t k; double alpha, beta; const double* a; int64_t ars, acs;
+    const double* b; int64_t brs, bcs; const double* c; int64_t rs_c, cs_c;
+    int64_t nent; const int64_t* ii; const int64_t* jj; double* hi; double* lo;
+} dd_args;
+
+static void dd_task(void* p, int tid, int nt)
+{
+    dd_args* g = (dd_args*)p;
+    for (int64_t e = tid; e < g->nent; e += nt) {
+        const int64_t i = g->ii[e], j = g->jj[e];
+        dd_t s = { 0.0, 0.0 };
+        for (int64_t l = 0; l < g->k; ++l)
+            s = dd_add(s, two_prod(g->a[i * g->ars + l * g->acs], g->b[l * g->brs + j * g->bcs]));
+        dd_t r = dd_mul_d(s, g->alpha);
+        if (g->beta != 0.0) r = dd_add(r, two_prod(g->beta, g->c[i * g->rs_c + j * g->cs_c]));
+        g->hi[e] = r.hi; g->lo[e] = r.lo;
+    }
+}
+
+void orc_dd_gemm_entries(int transa, int transb, int64_t m, int64_t n, int64_t k,
+                         double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+                         const double* b, int64_t rs_b, int64_t cs_b,
+                         double beta, const double* c, int64_t rs_c, int64_t cs_c,
+                         int64_t nent, const int64_t* ii, const int64_t* jj,
+                         double* hi, double* lo, int nthreads)
+{
+    (void)m; (void)n;
+    dd_args g;
+    g.k = k; g.alpha = alpha; g.beta = beta; g.a = a;
+    g.ars = ORC_TRANS(transa) ? cs_a : rs_a; g.acs = ORC_TRANS(transa) ? rs_a : cs_a;
+    g.b = b; g.brs = ORC_TRANS(transb) ? cs_b : rs_b; g.bcs = ORC_TRANS(transb) ? rs_b : cs_b;
+    g.c = c; g.rs_c = rs_c; g.cs_c = cs_c; g.nent = nent; g.ii = ii; g.jj = jj; g.hi = hi; g.lo = lo;
+    orc_parallel(dd_task, &g, nthreads < 1 ? 1 : nthreads);
+}
+
+void orc_dd_dotv(int64_t n, const double* x, int64_t incx, const double* y,
+                 int64_t incy, double* hi, double* lo)
+{
+    dd_t s = { 0.0, 0.0 };
+    for (int64_t i = 0; i < n; ++i) s = dd_add(s, two_prod(x[i * incx], y[i * incy]));
+    *hi = s.hi; *lo = s.lo;
+}
+
+/* ------------------------------------------------------------------ */
+/* Ozaki split-product model.                                          */
+/*                                                                     */
+/* Each row r of the row operand (op(A), or op(B)^T) is scaled by       */
+/* 2^-e_r with e_r = ilogb(max_k |r_k|) + 2, so |v| < 1/2, and then cut */
+/* into s balanced base-256 digits by rounding to nearest:              */
+/*     t = 256*v; d_p = rint(t); v = t - d_p         (all exact)        */
+/* so r = 2^e_r * (sum_p d_p 2^-8p + remainder), |d_p| <= 128, and the  */
+/* remainder is at most 2^-(8s+1) * 2^e_r.  Each digit is exact in      */
+/* bf16; a product of two digits is at most 2^14, so 1024 of them sum   */
+/* exactly in fp32 (the GPU's accumulation chunk).                       */
+/* Level sums S_l = sum_{p+q=l} D^A_p (D^B_q)^T for l = 2..s+1 (the     */
+/* triangular product set, s(s+1)/2 products) are exact integers; the   */
+/* GPU keeps them in int32, so K is cut into parts with                 */
+/* s * Kpart * 2^14 < 2^31.                                             */
+/* Recombination, least significant level first, in FP64:               */
+/*     acc = 0; for l = s+1 .. 2: acc += S_l * 2^-8l                    */
+/*     AB  = acc * 2^(e_i + e_j)                                        */
+/*     c   = beta == 0 ? alpha*AB : fma(beta, c, alpha*AB)               */
+/* ------------------------------------------------------------------ */
+int64_t orc_ozaki_kpart_limit(int slices)
+{
+    /* level sums must stay below 2^31 in int32: pairs * K * 128^2 < 2^31 */
+    int64_t lim = (int64_t)2147483647 / ((int64_t)slices * 128 * 128);
+    lim = (lim / 1024) * 1024;
+    return lim < 1024 ? 1024 : lim;
+}
+
+void orc_ozaki_split(int64_t rows, int64_t k, const double* r, int64_t rs, int64_t cs,
+                     int slices, int32_t* exps, int16_t* digits)
+{
+    for (int64_t i = 0; i < rows; ++i) {
+        double mx = 0.0;
+        for (int64_t l = 0; l < k; ++l) { double v = fabs(r[i * rs + l * cs]); if (v > mx) mx = v; }
+        const int e = (mx == 0.0) ? 0 : ilogb(mx) + 2;
+        exps[i] = e;
+        for (int64_t l = 0; l < k; ++l) {
+            double v = ldexp(r[i * rs + l * cs], -e);
+            for (int p = 0; p < slices; ++p) {
+                double t = v * 256.0;
+                double d = rint(t);
+                v = t - d;
+                digits[((int64_t)p * rows + i) * k + l] = (int16_t)d;
+            }
+        }
+    }
+}
+
+typedef struct {
+    int64_t m, n, k; int s; const int16_t* da; const int16_t* db;
+    const int32_t* ea; const int32_t* eb; double alpha, beta;
+    double* c; int64_t rs_c, cs_c;
+} oz_args;
+
+static void oz_task(void* p, int tid, int nt)
+{
+    oz_args* g = (oz_args*)p;
+    const int s = g->s;
+    int64_t lev[64];
+    for (int64_t i = tid; i < g->m; i += nt) {
+        for (int64_t j = 0; j < g->n; ++j) {
+            for (int l = 0; l <= s + 1; ++l) lev[l] = 0;
+            for (int pa = 1; pa <= s; ++pa)
+                for (int pb = 1; pa + pb <= s + 1; ++pb) {
+                    const int16_t* ra = g->da + ((int64_t)(pa - 1) * g->m + i) * g->k;
+                    const int16_t* rb = g->db + ((int64_t)(pb - 1) * g->n + j) * g->k;
+                    int64_t acc = 0;
+                    for (int64_t l = 0; l < g->k; ++l) acc += (int64_t)ra[l] * (int64_t)rb[l];
+                    lev[pa + pb] += acc;
+                }
+            double acc = 0.0;
+            for (int l = s + 1; l >= 2; --l) acc += ldexp((double)lev[l], -8 * l);
+            const double ab = ldexp(acc, g->ea[i] + g->eb[j]);
+            double* cij = g->c + i * g->rs_c + j * g->cs_c;
+            const double t = g->alpha * ab;
+            *cij = (g->beta == 0.0) ? t : fma(g->beta, *cij, t);
+        }
+    }
+}
+
+int orc_ozaki_dgemm(int transa, int transb, int64_t m, int64_t n, int64_t k,
+                    double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+                    const double* b, int64_t rs_b, int64_t cs_b,
+                    double beta, double* c, int64_t rs_c, int64_t cs_c,
+                    int slices, int nthreads)
+{
+    if (m <= 0 || n <= 0) return 0;
+    if (alpha == 0.0 || k <= 0) { d_scalm(m, n, beta, c, rs_c, cs_c); return 0; }
+    const int64_t ars = ORC_TRANS(transa) ? cs_a : rs_a, acs = ORC_TRANS(transa) ? rs_a : cs_a;
+    const int64_t brs = ORC_TRANS(transb) ? cs_b : rs_b, bcs = ORC_TRANS(transb) ? rs_b : cs_b;
+    /* non-finite operands cannot be sliced: the native FP64 path is used */
+    for (int64_t i = 0; i < m; ++i) for (int64_t l = 0; l < k; ++l)
+        if (!isfinite(a[i * ars + l * acs])) goto native;
+    for (int64_t l = 0; l < k; ++l) for (int64_t j = 0; j < n; ++j)
+        if (!isfinite(b[l * brs + j * bcs])) goto native;
+    {
+        int16_t* da = (int16_t*)malloc(sizeof(int16_t) * (size_t)slices * m * k);
+        int16_t* db = (int16_t*)malloc(sizeof(int16_t) * (size_t)slices * n * k);
+        int32_t* ea = (int32_t*)malloc(sizeof(int32_t) * m);
+        int32_t* eb = (int32_t*)malloc(sizeof(int32_t) * n);
+        orc_ozaki_split(m, k, a, ars, acs, slices, ea, da);
+        /* rows of op(B)^T are the columns of op(B): element (j, l) = B(l, j) */
+        orc_ozaki_split(n, k, b, bcs, brs, slices, eb, db);
+        oz_args g = { m, n, k, slices, da, db, ea, eb, alpha, beta, c, rs_c, cs_c };
+        orc_parallel(oz_task, &g, nthreads < 1 ? 1 : nthreads);
+        free(da); free(db); free(ea); free(eb);
+        return 0;
+    }
+native:
+    orc_dgemm(transa, transb, m, n, k, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c, cs_c, nthreads);
+    return 1;
+}

@@ -1,0 +1,135 @@
+"""Ozaki split-product DGEMM (tcgen05 slice products) against the CPU model.
+
+The model in oracle/gb_oracle.c performs the same digit split, exact integer
+level sums and FP64 recombination, so the GPU result must match it bit for
+bit; the double-double oracle then bounds the error against native FP64.
+"""
+import numpy as np
+import pytest
+
+from blis_gb300 import blas
+from oracle import pyoracle as po
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+N, T = blas.NO_TRANSPOSE, blas.TRANSPOSE
+
+
+@pytest.fixture(autouse=True)
+def reset_mode(gblib):
+    yield
+    blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+
+
+def _run_gpu(ta, tb, alpha, a, b, beta, c, slices):
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, slices)
+    blas.bli_dgemm(ta, tb, alpha, a, b, beta, c)
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 256, 64), (300, 200, 1000), (17, 33, 5), (129, 257, 1100)])
+@pytest.mark.parametrize("slices", [3, 8])
+def test_ozaki_bit_exact_vs_model(m, n, k, slices):
+    a = po.expspread((m, k), 1)
+    b = po.expspread((k, n), 2)
+    c0 = po.uniform((m, n), 3)
+    ref = np.asfortranarray(c0.copy())
+    po.ozaki_dgemm(N, N, 1.25, a, b, 0.5, ref, slices)
+    c = np.asfortranarray(c0.copy())
+    _run_gpu(N, N, 1.25, a, b, 0.5, c, slices)
+    assert np.array_equal(c, ref)
+
+
+@pytest.mark.parametrize("ta", [N, T])
+@pytest.mark.parametrize("tb", [N, T])
+@pytest.mark.parametrize("rowmajor", [False, True])
+def test_ozaki_transposes_and_layouts(ta, tb, rowmajor):
+    m, n, k = 150, 90, 333
+    order = "C" if rowmajor else "F"
+    a = po.uniform((k, m) if ta else (m, k), 4, order=order)
+    b = po.uniform((n, k) if tb else (k, n), 5, order=order)
+    c0 = po.uniform((m, n), 6, order=order)
+    ref = c0.copy(order=order)
+    po.ozaki_dgemm(ta, tb, -0.75, a, b, 0.0, ref, 6)
+    c = c0.copy(order=order)
+    _run_gpu(ta, tb, -0.75, a, b, 0.0, c, 6)
+    assert np.array_equal(c, ref)
+
+
+def test_ozaki_k_partitions_bit_exact():
+    # 16 slices: one k part holds at most 7168 -> k = 8000 uses two parts
+    assert po.ozaki_kpart_limit(16) < 8000
+    m, n, k = 64, 96, 8000
+    a = po.expspread((m, k), 7)
+    b = po.expspread((k, n), 8)
+    ref = np.zeros((m, n), order="F")
+    po.ozaki_dgemm(N, N, 1.0, a, b, 0.0, ref, 16)
+    c = np.zeros((m, n), order="F")
+    _run_gpu(N, N, 1.0, a, b, 0.0, c, 16)
+    assert np.array_equal(c, ref)
+
+
+def test_ozaki_error_not_worse_than_native():
+    n = 1024
+    a = po.expspread((n, n), 11)
+    b = po.expspread((n, n), 12)
+    c_oz = np.zeros((n, n), order="F")
+    c_nat = np.zeros((n, n), order="F")
+    _run_gpu(N, N, 1.0, a, b, 0.0, c_oz, 8)
+    blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+    blas.bli_dgemm(N, N, 1.0, a, b, 0.0, c_nat)
+    rng = np.random.default_rng(1)
+    ii = rng.integers(0, n, 4096)
+    jj = rng.integers(0, n, 4096)
+    hi, lo = po.dd_gemm_entries(0, 0, 1.0, a, b, 0.0, c_oz, ii, jj)
+    e_oz = po.componentwise_error(c_oz[ii, jj], hi, lo)
+    e_nat = po.componentwise_error(c_nat[ii, jj], hi, lo)
+    assert e_oz <= e_nat
+
+
+def test_ozaki_nonfinite_falls_back_to_ieee():
+    m, n, k = 40, 30, 20
+    a = po.uniform((m, k), 1)
+    b = po.uniform((k, n), 2)
+    a[5, 3] = np.inf
+    b[7, 9] = np.nan
+    c = np.zeros((m, n), order="F")
+    _run_gpu(N, N, 1.0, a, b, 0.0, c, 8)
+    ref = np.zeros((m, n), order="F")
+    po.dgemm(0, 0, 1.0, a, b, 0.0, ref)
+    assert np.array_equal(np.isnan(c), np.isnan(ref))
+    fin = np.isfinite(ref)
+    assert np.allclose(c[fin], ref[fin], rtol=1e-13, atol=1e-13)
+
+
+def test_ozaki_through_dgemm_blas_and_scalars():
+    m, n, k = 96, 80, 640
+    a = po.uniform((m, k), 21)
+    b = po.uniform((k, n), 22)
+    c = po.uniform((m, n), 23)
+    ref = np.asfortranarray(c.copy())
+    po.ozaki_dgemm(N, N, 2.0, a, b, 1.2, ref, 7)
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 7)
+    blas.dgemm("N", "N", m, n, k, 2.0, a, m, b, k, 1.2, c, m)
+    assert np.array_equal(c, ref)
+    # alpha == 0 and k == 0 keep the level-3 early exits
+    c2 = po.uniform((m, n), 24)
+    r2 = 3.0 * c2
+    blas.dgemm("N", "N", m, n, k, 0.0, a, m, b, k, 3.0, c2, m)
+    assert np.array_equal(c2, r2)
+
+
+def test_ozaki_device_api_matches_model():
+    torch = pytest.importorskip("torch")
+    from blis_gb300 import dev
+    m, n, k = 512, 384, 2048
+    a = po.expspread((m, k), 31)
+    b = po.expspread((k, n), 32)
+    ref = np.zeros((m, n), order="F")
+    po.ozaki_dgemm(N, N, 1.0, a, b, 0.0, ref, 8)
+    ta = torch.from_numpy(a.T.copy()).cuda().t()
+    tb = torch.from_numpy(b.T.copy()).cuda().t()
+    tc = torch.zeros((n, m), dtype=torch.float64, device="cuda").t()
+    dev.dgemm_ozaki(N, N, 1.0, ta, tb, 0.0, tc, 8)
+    torch.cuda.synchronize()
+    assert np.array_equal(tc.cpu().numpy(), ref)

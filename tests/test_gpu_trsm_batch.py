@@ -1,0 +1,147 @@
+"""DTRSM (recursive blocked solve on the GPU) and grouped gemm_batch."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from blis_gb300 import _lib, blas
+from oracle import pyoracle as po
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def native(gblib):
+    blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+    yield
+    blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+
+
+def _tri(a, uplo, diag):
+    t = np.tril(a) if uplo == "L" else np.triu(a)
+    if diag == "U":
+        t = t - np.diag(np.diag(t)) + np.eye(a.shape[0])
+    return t
+
+
+@pytest.mark.parametrize("side", ["L", "R"])
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("trans", ["N", "T"])
+@pytest.mark.parametrize("diag", ["N", "U"])
+@pytest.mark.parametrize("m,n", [(300, 200), (65, 1), (1, 7), (257, 129)])
+def test_dtrsm_testsuite_residual(side, uplo, trans, diag, m, n):
+    na = m if side == "L" else n
+    a = np.asfortranarray(H.normalize(po.uniform((na, na), 4)) + 2.0 * np.eye(na))
+    b0 = H.normalize(po.uniform((m, n), 5))
+    x = np.asfortranarray(b0.copy())
+    blas.dtrsm(side, uplo, trans, diag, m, n, 2.0, a, na, x, m)
+    tri = _tri(a, uplo, diag)
+    r = H.trsm_residual(0 if side == "L" else 1, 2.0, tri.T if trans == "T" else tri, b0, x)
+    assert r < 1e-13
+
+
+def test_dtrsm_config_shape_reduced_and_ozaki():
+    # config-2 style: L lower, non-unit, diagonal = m + |u|
+    m, n = 1536, 512
+    L = np.tril(po.uniform((m, m), 7))
+    L[np.diag_indices(m)] = m + np.abs(np.diag(L))
+    L = np.asfortranarray(L)
+    b0 = po.uniform((m, n), 8)
+    ref = np.asfortranarray(b0.copy())
+    po.dtrsm(po.LEFT, po.LOWER, 0, 0, 1.0, L, ref)
+    for mode, slices in ((blas.DGEMM_NATIVE, 8), (blas.DGEMM_OZAKI, 8)):
+        blas.set_dgemm_mode(mode, slices)
+        x = np.asfortranarray(b0.copy())
+        blas.dtrsm("L", "L", "N", "N", m, n, 1.0, L, m, x, m)
+        assert np.max(np.abs(x - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def test_dtrsm_alpha_zero():
+    a = np.eye(5)
+    b = np.full((5, 3), np.nan, order="F")
+    blas.dtrsm("L", "L", "N", "N", 5, 3, 0.0, a, 5, b, 5)
+    assert (b == 0).all()
+
+
+def _problems(seed, count, dtype):
+    rng = np.random.default_rng(seed)
+    probs = []
+    for _ in range(count):
+        m, n, k = (int(round(np.exp(rng.uniform(np.log(16), np.log(300))))) for _ in range(3))
+        ta, tb = rng.integers(0, 2, 2)
+        a = po.uniform((k, m) if ta else (m, k), int(rng.integers(1 << 30)), dtype=dtype)
+        b = po.uniform((n, k) if tb else (k, n), int(rng.integers(1 << 30)), dtype=dtype)
+        c = po.uniform((m, n), int(rng.integers(1 << 30)), dtype=dtype)
+        probs.append(("T" if ta else "N", "T" if tb else "N", m, n, k, a, b, c))
+    return probs
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_gemm_batch_blas_vs_oracle(dtype):
+    probs = _problems(3, 40, dtype)
+    # one group per problem, as the reference's batch test driver does
+    ref = []
+    for ta, tb, m, n, k, a, b, c in probs:
+        r = np.asfortranarray(c.copy())
+        po.dgemm(8 if ta == "T" else 0, 8 if tb == "T" else 0, 1.5, a, b, 0.5, r)
+        ref.append(r)
+    blas.dgemm_batch([p[0] for p in probs], [p[1] for p in probs], [p[2] for p in probs],
+                     [p[3] for p in probs], [p[4] for p in probs], [1.5] * len(probs),
+                     [p[5] for p in probs], [p[5].shape[0] for p in probs], [p[6] for p in probs],
+                     [p[6].shape[0] for p in probs], [0.5] * len(probs), [p[7] for p in probs],
+                     [p[2] for p in probs], [1] * len(probs), dtype=dtype)
+    tol = 1e-12 if dtype == np.float64 else 2e-4
+    for (ta, tb, m, n, k, a, b, c), r in zip(probs, ref):
+        assert np.allclose(c, r, rtol=tol, atol=tol)
+
+
+def test_grouped_equals_loop_and_graph_replay(gblib):
+    torch = pytest.importorskip("torch")
+    probs = _problems(5, 64, np.float64)
+    tens = []
+    descs = (_lib_problem * len(probs))()
+    outs = []
+    for i, (ta, tb, m, n, k, a, b, c) in enumerate(probs):
+        A = torch.from_numpy(np.asfortranarray(a).T.copy()).cuda()
+        B = torch.from_numpy(np.asfortranarray(b).T.copy()).cuda()
+        Cg = torch.from_numpy(np.asfortranarray(c).T.copy()).cuda()
+        tens += [A, B, Cg]
+        outs.append(Cg)
+        descs[i] = _lib_problem(8 if ta == "T" else 0, 8 if tb == "T" else 0, m, n, k, 1.0, 0.0,
+                                A.data_ptr(), a.shape[0], B.data_ptr(), b.shape[0], Cg.data_ptr(), m)
+    L = _lib.load()
+    L.gb_gemm_batch_dev.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_void_p]
+    assert L.gb_gemm_batch_dev(C.addressof(descs), len(probs), 0, 0, None) == 0
+    torch.cuda.synchronize()
+    grouped = [o.clone() for o in outs]
+    for o in outs:
+        o.zero_()
+    assert L.gb_gemm_batch_dev(C.addressof(descs), len(probs), 0, 1, None) == 0
+    torch.cuda.synchronize()
+    for g, o in zip(grouped, outs):
+        assert torch.equal(g, o)
+    plan = C.c_void_p()
+    L.gb_batch_plan_create.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]
+    L.gb_batch_plan_run.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    L.gb_batch_plan_destroy.argtypes = [C.c_void_p]
+    assert L.gb_batch_plan_create(C.addressof(descs), len(probs), 0, C.byref(plan)) == 0
+    for _ in range(3):
+        for o in outs:
+            o.zero_()
+        assert L.gb_batch_plan_run(plan, 1, None) == 0
+        assert L.gb_synchronize() == 0
+        for g, o in zip(grouped, outs):
+            assert torch.equal(g, o)
+    L.gb_batch_plan_destroy(plan)
+    for (ta, tb, m, n, k, a, b, c), g in zip(probs, grouped):
+        ref = np.zeros((m, n), order="F")
+        po.dgemm(8 if ta == "T" else 0, 8 if tb == "T" else 0, 1.0, a, b, 0.0, ref)
+        assert np.allclose(g.cpu().numpy().T, ref, rtol=1e-12, atol=1e-12)
+
+
+class _lib_problem(C.Structure):
+    _fields_ = [("transa", C.c_int), ("transb", C.c_int), ("m", C.c_int64), ("n", C.c_int64),
+                ("k", C.c_int64), ("alpha", C.c_double), ("beta", C.c_double), ("a", C.c_void_p),
+                ("lda", C.c_int64), ("b", C.c_void_p), ("ldb", C.c_int64), ("c", C.c_void_p),
+                ("ldc", C.c_int64)]
