@@ -611,6 +611,53 @@ void bli_ddotv_ex(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t n, const double* x,
     bli_ddotv(conjx, conjy, n, x, incx, y, incy, rho);
 }
 
+// ==================================================================== gb_ host aliases
+void gb_dgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+              const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+              gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    gemm_host<double>(transa, transb, m, n, k, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c,
+                      cs_c, "gb_dgemm");
+}
+
+void gb_sgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+              const float* alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a, const float* b,
+              gb_inc_t rs_b, gb_inc_t cs_b, const float* beta, float* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    gemm_host<float>(transa, transb, m, n, k, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c,
+                     cs_c, "gb_sgemm");
+}
+
+void gb_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+              gb_dim_t n, const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+              double* b, gb_inc_t rs_b, gb_inc_t cs_b)
+{
+    trsm_host(side, uploa, transa, diaga, m, n, *alpha, a, rs_a, cs_a, b, rs_b, cs_b);
+}
+
+void gb_dgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, const double* alpha,
+              const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* x, gb_inc_t incx,
+              const double* beta, double* y, gb_inc_t incy)
+{
+    (void)conjx;
+    gemv_host(transa, m, n, *alpha, a, rs_a, cs_a, x, incx, *beta, y, incy, "gb_dgemv");
+}
+
+void gb_daxpyv(gb_conj_t conjx, gb_dim_t n, const double* alpha, const double* x, gb_inc_t incx,
+               double* y, gb_inc_t incy)
+{
+    (void)conjx;
+    axpyv_host(n, *alpha, x, incx, y, incy);
+}
+
+void gb_ddotv(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t n, const double* x, gb_inc_t incx,
+              const double* y, gb_inc_t incy, double* rho)
+{
+    (void)conjx;
+    (void)conjy;
+    dotv_host(n, x, incx, y, incy, rho);
+}
+
 // ==================================================================== gb_ addon
 static cudaStream_t pick_stream(void* stream)
 {

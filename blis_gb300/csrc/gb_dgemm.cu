@@ -22,16 +22,20 @@ namespace {
 
 using namespace tiles;
 
-__global__ void __launch_bounds__(NT) dgemm_dmma_kernel(DArgs p)
+// gate != nullptr: the kernel only runs when *gate is nonzero (a device-side
+// condition raised by an earlier kernel on the same stream).
+__global__ void __launch_bounds__(NT) dgemm_dmma_kernel(DArgs p, const int* gate)
 {
+    if (gate && *gate == 0) return;
     __shared__ double As[BK * LDS];
     __shared__ double Bs[BK * LDS];
     dmma_tile(p, (int64_t)blockIdx.y * BM, (int64_t)blockIdx.x * BN, As, Bs);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NT) gemm_simt_kernel(GArgs<T> p)
+__global__ void __launch_bounds__(NT) gemm_simt_kernel(GArgs<T> p, const int* gate)
 {
+    if (gate && *gate == 0) return;
     __shared__ T As[BK * LDS];
     __shared__ T Bs[BK * LDS];
     simt_tile<T>(p, (int64_t)blockIdx.y * BM, (int64_t)blockIdx.x * BN, As, Bs);
@@ -86,26 +90,34 @@ int scal_matrix_f(int64_t m, int64_t n, float beta, float* c, int64_t rs_c, int6
     return check_cuda(cudaGetLastError(), "scal_matrix_f");
 }
 
-int dgemm_native(int64_t m, int64_t n, int64_t k, double alpha,
-                 const double* a, int64_t ars, int64_t acs,
-                 const double* b, int64_t brs, int64_t bcs, double beta,
-                 double* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
+int dgemm_native_gated(int64_t m, int64_t n, int64_t k, double alpha,
+                       const double* a, int64_t ars, int64_t acs,
+                       const double* b, int64_t brs, int64_t bcs, double beta,
+                       double* c, int64_t rs_c, int64_t cs_c, const int* gate, cudaStream_t s)
 {
     // Early exits of frame/3/bli_l3_util.c:41-65.
     if (m <= 0 || n <= 0) return GB_SUCCESS;
-    if (alpha == 0.0 || k <= 0) return scal_matrix(m, n, beta, c, rs_c, cs_c, s);
+    if (alpha == 0.0 || k <= 0) return gate ? GB_SUCCESS : scal_matrix(m, n, beta, c, rs_c, cs_c, s);
     const int64_t gx = (n + BN - 1) / BN, gy = (m + BM - 1) / BM;
     if (gy > 65535) return set_error(GB_ERR_ARG, "gb_dgemm", "m too large for one launch");
     DArgs p{m, n, k, alpha, beta, a, ars, acs, b, brs, bcs, c, rs_c, cs_c};
     dim3 grid((unsigned)gx, (unsigned)gy);
     if (use_dfma()) {
         LaunchScope ls("dgemm_dfma", s);
-        gemm_simt_kernel<double><<<grid, NT, 0, s>>>(p);
+        gemm_simt_kernel<double><<<grid, NT, 0, s>>>(p, gate);
     } else {
-        LaunchScope ls("dgemm_dmma", s);
-        dgemm_dmma_kernel<<<grid, NT, 0, s>>>(p);
+        LaunchScope ls(gate ? "dgemm_dmma_gated" : "dgemm_dmma", s);
+        dgemm_dmma_kernel<<<grid, NT, 0, s>>>(p, gate);
     }
     return check_cuda(cudaGetLastError(), "dgemm_native");
+}
+
+int dgemm_native(int64_t m, int64_t n, int64_t k, double alpha,
+                 const double* a, int64_t ars, int64_t acs,
+                 const double* b, int64_t brs, int64_t bcs, double beta,
+                 double* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
+{
+    return dgemm_native_gated(m, n, k, alpha, a, ars, acs, b, brs, bcs, beta, c, rs_c, cs_c, nullptr, s);
 }
 
 int sgemm_dev(int64_t m, int64_t n, int64_t k, float alpha,
@@ -119,7 +131,7 @@ int sgemm_dev(int64_t m, int64_t n, int64_t k, float alpha,
     if (gy > 65535) return set_error(GB_ERR_ARG, "gb_sgemm", "m too large for one launch");
     GArgs<float> p{m, n, k, alpha, beta, a, ars, acs, b, brs, bcs, c, rs_c, cs_c};
     LaunchScope ls("sgemm_ffma", s);
-    gemm_simt_kernel<float><<<dim3((unsigned)gx, (unsigned)gy), NT, 0, s>>>(p);
+    gemm_simt_kernel<float><<<dim3((unsigned)gx, (unsigned)gy), NT, 0, s>>>(p, nullptr);
     return check_cuda(cudaGetLastError(), "sgemm");
 }
 

@@ -77,6 +77,11 @@ int dgemm_native(int64_t m, int64_t n, int64_t k, double alpha,
                  const double* a, int64_t ars, int64_t acs,
                  const double* b, int64_t brs, int64_t bcs, double beta,
                  double* c, int64_t rs_c, int64_t cs_c, cudaStream_t s);
+int dgemm_native_gated(int64_t m, int64_t n, int64_t k, double alpha,
+                       const double* a, int64_t ars, int64_t acs,
+                       const double* b, int64_t brs, int64_t bcs, double beta,
+                       double* c, int64_t rs_c, int64_t cs_c, const int* gate, cudaStream_t s);
+double ozaki_t_bound_log2(int s, int64_t k);
 int sgemm_dev(int64_t m, int64_t n, int64_t k, float alpha,
               const float* a, int64_t ars, int64_t acs,
               const float* b, int64_t brs, int64_t bcs, float beta,

@@ -3,26 +3,33 @@
 // FP64 on GB300 runs on a narrow pipe; the bf16 tensor cores are three
 // orders of magnitude wider.  This form computes C := beta*C + alpha*A*B
 // from exact integer products of bf16 digit slices (Ozaki, Ogita, Oishi &
-// Rump 2012; integer-slice variant of Ootomo, Ozaki & Yokota 2024):
+// Rump 2012; integer-slice variant of Ootomo, Ozaki & Yokota 2024), and
+// keeps FP64 arithmetic out of every bulk step:
 //
-//  1. oz_rowmax / oz_split: every row of op(A) and of op(B)^T is scaled by
-//     2^-e (e = ilogb(row max) + 2, so |v| < 1/2) and cut into s balanced
-//     base-256 digits, t = 256 v; d = rint(t); v = t - d, |d| <= 128.  Each
-//     digit is exact in bf16.  Slices are stored K-major, s planes of
-//     [rows_pad][K_pad] bf16, zero padded.
+//  1. oz_rowmax / oz_split (integer only): every row of op(A) and of
+//     op(B)^T gets e = ilogb(row max) + 2, so U = |x| 2^-e < 1/2, and is cut
+//     into s balanced base-256 digits of the exact value U (greedy, rounding
+//     to nearest, ties to even), |d| <= 128, each exact in bf16.  The digits
+//     come from a 128-bit fixed-point image of the mantissa.  Slices are
+//     stored K-major: s planes of [rows_pad][K_pad] bf16, zero padded.
 //  2. ozaki_slice_gemm: a persistent tcgen05 kernel computes the integer
-//     level sums S_l = sum_{p+q=l} A_p B_q^T for l = 2..s+1 (triangular
-//     set, s(s+1)/2 slice products).  Operand tiles arrive by TMA (128B
-//     swizzle) into a 4-stage mbarrier ring; one thread issues
-//     tcgen05.mma kind::f16 (M=128, N=256, K=16) into one of two fp32 TMEM
-//     accumulators; every 1024 products (|sum| <= 2^24, exact in fp32) the
-//     accumulator is drained by 8 epilogue warps into int32 registers, so
-//     the level sums are exact.  K is cut into parts so s*Kpart*2^14 < 2^31.
-//  3. oz_recombine: FP64 only here: acc = sum_l S_l 2^-8l (least
-//     significant level first), AB = acc 2^(e_i+e_j), c = alpha AB + beta c.
+//     level sums S_l = sum_{p+q=l} A_p B_q^T, l = 2..s+1 (the triangular
+//     set, s(s+1)/2 slice products).  Tiles arrive by TMA (128B swizzle)
+//     into a 4-stage mbarrier ring; one thread issues tcgen05.mma kind::f16
+//     (M=128, N=256, K=16) into one of two fp32 TMEM accumulators; every
+//     1024 products (|sum| <= 2^24, exact in fp32) 8 epilogue warps drain
+//     the accumulator into int32 registers.  Each level's K range is cut
+//     into parts with npairs(l) * Kpart * 2^14 < 2^31, one int32 plane per
+//     (level, part).
+//  3. oz_recombine (integer + one rounding): T = sum_l S_l 2^(8(s+1-l))
+//     exactly in 128-bit, AB = RNE(T 2^(e_i+e_j-8(s+1))); FP64 only for
+//     c = alpha AB + beta c (skipped for alpha = 1, beta = 0).
 //
-// The same arithmetic, step for step, is the CPU model used by the tests,
-// which therefore check this path bit for bit.
+// Non-finite inputs cannot be cut into digits: the split kernels raise a
+// device flag, the later kernels of this form see it and return, and a
+// gated native FP64 kernel computes the IEEE result instead -- no host
+// round trip.  The same arithmetic is the CPU model in oracle/gb_oracle.c,
+// which the tests compare against bit for bit.
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <stdlib.h>
@@ -46,33 +53,38 @@ constexpr int OZ_THREADS = (OZ_EPI_WARPS + 2) * 32;
 constexpr uint32_t OZ_TMEM_COLS = 512;  // two 128x256 fp32 accumulators
 constexpr int OZ_SMEM_BYTES = OZ_STAGES * OZ_STAGE_BYTES + 1024 + 256;
 constexpr int OZ_CHUNK_KB = 16;  // 16 k-blocks of 64 = 1024 products per exact fp32 chunk
+constexpr int OZ_MAX_SLICES = 12;
+
+struct OzLevel {
+    int lev, npairs, pa_lo, nparts, kb_per_part, plane_base;
+    long long item_base;
+};
 
 struct OzGemmParams {
-    int slices;
-    int nparts;
-    int kb_per_part;
-    int kb_total;
-    int tiles_m, tiles_n;
-    int64_t items;
-    int chunk_kb;
-    int64_t mpad, npad;
-    int32_t* planes;  // [(part*slices + lev-2)][npad][mpad]
+    int slices, nlevels, kb_total, tiles_m, tiles_n, chunk_kb;
+    int64_t items, mpad, npad;
+    int32_t* planes;  // [plane][npad][mpad]
     unsigned int* status;
+    const int* skip;  // non-finite flag of the split kernels
+    OzLevel lv[OZ_MAX_SLICES];
 };
 
 struct OzItem {
-    int lev, part, tm, tn, pa_lo, npairs, kb0, kbn;
+    int lev, npairs, pa_lo, tm, tn, kb0, kbn, plane;
 };
 
 __device__ __forceinline__ OzItem oz_decode(const OzGemmParams& p, int64_t it)
 {
+    int L = 0;
+    while (L + 1 < p.nlevels && it >= p.lv[L + 1].item_base) ++L;
+    const OzLevel& lv = p.lv[L];
     OzItem w;
+    w.lev = lv.lev;
+    w.npairs = lv.npairs;
+    w.pa_lo = lv.pa_lo;
     const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
-    const int64_t per_lev = (int64_t)p.nparts * tiles;
-    const int q = (int)(it / per_lev);
-    w.lev = p.slices + 1 - q;  // heaviest (most pairs) level first
-    int64_t rem = it % per_lev;
-    w.part = (int)(rem / tiles);
+    const int64_t rem = it - lv.item_base;
+    const int part = (int)(rem / tiles);
     const int64_t t = rem % tiles;
     // grouped raster over tiles: 8 tile rows per group for L2 reuse
     const int64_t group = t / (8 * (int64_t)p.tiles_n);
@@ -81,12 +93,10 @@ __device__ __forceinline__ OzItem oz_decode(const OzGemmParams& p, int64_t it)
     const int64_t wi = t - group * 8 * (int64_t)p.tiles_n;
     w.tm = (int)(first_m + wi % gm);
     w.tn = (int)(wi / gm);
-    w.pa_lo = (w.lev - p.slices > 1) ? w.lev - p.slices : 1;
-    const int pa_hi = (w.lev - 1 < p.slices) ? w.lev - 1 : p.slices;
-    w.npairs = pa_hi - w.pa_lo + 1;
-    w.kb0 = w.part * p.kb_per_part;
-    const int kb_end = (w.kb0 + p.kb_per_part < p.kb_total) ? w.kb0 + p.kb_per_part : p.kb_total;
+    w.kb0 = part * lv.kb_per_part;
+    const int kb_end = (w.kb0 + lv.kb_per_part < p.kb_total) ? w.kb0 + lv.kb_per_part : p.kb_total;
     w.kbn = kb_end - w.kb0;
+    w.plane = lv.plane_base + part;
     return w;
 }
 
@@ -98,8 +108,9 @@ __device__ __forceinline__ void oz_fail(const OzGemmParams& p, volatile int* abo
 
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     ozaki_slice_gemm_kernel(const __grid_constant__ CUtensorMap map_a,
-                            const __grid_constant__ CUtensorMap map_b, OzGemmParams p)
+                            const __grid_constant__ CUtensorMap map_b, const __grid_constant__ OzGemmParams p)
 {
+    if (*p.skip) return;  // uniform across the CTA: the native kernel takes over
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                ~uintptr_t(1023));
@@ -270,10 +281,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 ++chunk_ctr;
             }
             if (!ok) break;
-            const int64_t q = (int64_t)w.part * p.slices + (w.lev - 2);
             const int64_t i = (int64_t)w.tm * OZ_BM + quad * 32 + lane;
             const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
-            int32_t* dst = p.planes + (q * p.npad + j0) * p.mpad + i;
+            int32_t* dst = p.planes + ((int64_t)w.plane * p.npad + j0) * p.mpad + i;
 #pragma unroll
             for (int c = 0; c < 128; ++c) dst[(int64_t)c * p.mpad] = acc[c];
         }
@@ -286,38 +296,115 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 }
 
 // ---------------------------------------------------------------- split
-// Row r of the row operand R: element (r, l) at R[r*sr + l*sl].
-__global__ void oz_rowmax_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
-                                 int64_t sr, int64_t sl, unsigned long long* __restrict__ maxbits)
+// Row r of the row operand R: element (r, l) at R[r*sr + l*sl].  |x| as its
+// IEEE bit pattern is monotone in |x|, so the row maximum is an integer max.
+__device__ __forceinline__ unsigned long long abs_bits(double x)
 {
-    __shared__ unsigned long long tmax[64];
-    if (threadIdx.x < 64) tmax[threadIdx.x] = 0ull;
-    __syncthreads();
-    const int64_t r0 = (int64_t)blockIdx.x * 64;
-    const bool rows_fast = (sr == 1);
-    for (int64_t lt = blockIdx.y; lt * 64 < k; lt += gridDim.y) {
-        const int64_t l0 = lt * 64;
-        unsigned long long local[16];
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const int e = threadIdx.x + 256 * q;
-            const int rr = rows_fast ? (e & 63) : (e >> 6);
-            const int ll = rows_fast ? (e >> 6) : (e & 63);
-            const int64_t r = r0 + rr, l = l0 + ll;
-            local[q] = (r < rows && l < k)
-                           ? (unsigned long long)__double_as_longlong(fabs(__ldg(R + r * sr + l * sl)))
-                           : 0ull;
-        }
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const int e = threadIdx.x + 256 * q;
-            const int rr = rows_fast ? (e & 63) : (e >> 6);
-            if (local[q]) atomicMax(&tmax[rr], local[q]);
-        }
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// Rows contiguous (sr == 1, e.g. column-major op(A)): thread per row, the
+// grid's y dimension splits k.
+__global__ void oz_rowmax_rows_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
+                                      int64_t sl, int64_t kchunk, unsigned long long* __restrict__ maxbits)
+{
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const int64_t l0 = (int64_t)blockIdx.y * kchunk;
+    const int64_t l1 = (l0 + kchunk < k) ? l0 + kchunk : k;
+    unsigned long long m0 = 0, m1 = 0;
+    int64_t l = l0;
+    for (; l + 1 < l1; l += 2) {
+        const unsigned long long b0 = abs_bits(__ldcs(R + r + l * sl));
+        const unsigned long long b1 = abs_bits(__ldcs(R + r + (l + 1) * sl));
+        m0 = b0 > m0 ? b0 : m0;
+        m1 = b1 > m1 ? b1 : m1;
     }
-    __syncthreads();
-    if (threadIdx.x < 64 && r0 + threadIdx.x < rows && tmax[threadIdx.x])
-        atomicMax(maxbits + r0 + threadIdx.x, tmax[threadIdx.x]);
+    if (l < l1) {
+        const unsigned long long b0 = abs_bits(__ldcs(R + r + l * sl));
+        m0 = b0 > m0 ? b0 : m0;
+    }
+    const unsigned long long mx = m0 > m1 ? m0 : m1;
+    if (mx) atomicMax(maxbits + r, mx);
+}
+
+// Any other layout: warp per row, lanes stride along k.
+__global__ void oz_rowmax_warp_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
+                                      int64_t sr, int64_t sl, int64_t kchunk,
+                                      unsigned long long* __restrict__ maxbits)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (r >= rows) return;
+    const int64_t l0 = (int64_t)blockIdx.y * kchunk;
+    const int64_t l1 = (l0 + kchunk < k) ? l0 + kchunk : k;
+    unsigned long long mx = 0;
+    for (int64_t l = l0 + lane; l < l1; l += 32) {
+        const unsigned long long b = abs_bits(__ldcs(R + r * sr + l * sl));
+        mx = b > mx ? b : mx;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
+        mx = o > mx ? o : mx;
+    }
+    if (lane == 0 && mx) atomicMax(maxbits + r, mx);
+}
+
+__device__ __forceinline__ int clz128(unsigned __int128 u)
+{
+    const unsigned long long hi = (unsigned long long)(u >> 64), lo = (unsigned long long)u;
+    return hi ? __clzll((long long)hi) : (lo ? 64 + __clzll((long long)lo) : 128);
+}
+
+// bf16 bit pattern of an integer |d| <= 256 (exact: at most 8 significant bits).
+__device__ __forceinline__ uint16_t int_to_bf16_bits(int d)
+{
+    if (d == 0) return 0;
+    const uint32_t sgn = d < 0 ? 0x8000u : 0u;
+    const uint32_t a = (uint32_t)(d < 0 ? -d : d);
+    const int p = 31 - __clz((int)a);                // a = 2^p * 1.f
+    const uint32_t man = (a << (7 - p)) & 0x7Fu;     // p <= 8: exact
+    return (uint16_t)(sgn | ((uint32_t)(p + 127) << 7) | man);
+}
+
+// Balanced base-256 digits of |x| 2^-e with the sign of x; integer only.
+template <int S>
+__device__ __forceinline__ void oz_digits(double x, int e, int (&d)[S])
+{
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const bool neg = (bits >> 63) != 0;
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    const unsigned long long frac = bits & ((1ull << 52) - 1);
+#pragma unroll
+    for (int p = 0; p < S; ++p) d[p] = 0;
+    if (ex == 0 && frac == 0) return;
+    const unsigned long long M = ex ? (frac | (1ull << 52)) : frac;
+    const int E2 = ex ? ex - 1075 : -1074;
+    constexpr int F = 8 * S + 2;
+    const int sh = E2 - e + F;
+    __int128 R;
+    bool sticky = false;
+    if (sh >= 0) {
+        R = (__int128)((unsigned __int128)M << sh);
+    } else if (sh > -64) {
+        R = (__int128)(M >> (-sh));
+        sticky = (M & ((1ull << (-sh)) - 1)) != 0;
+    } else {
+        R = 0;
+        sticky = true;
+    }
+#pragma unroll
+    for (int p = 1; p <= S; ++p) {
+        const int w = F - 8 * p;
+        const __int128 q = R >> w;
+        const __int128 rem = R - (q << w);
+        const __int128 half = ((__int128)1) << (w - 1);
+        __int128 dg = q;
+        if (rem > half || (rem == half && (sticky || (q & 1)))) dg = q + 1;
+        R -= dg << w;
+        d[p - 1] = neg ? -(int)dg : (int)dg;
+    }
 }
 
 __device__ __forceinline__ int oz_row_exponent(unsigned long long bits, int* nonfinite)
@@ -330,13 +417,15 @@ __device__ __forceinline__ int oz_row_exponent(unsigned long long bits, int* non
     return ilogb(__longlong_as_double((long long)bits)) + 2;
 }
 
-// Tile of 32 rows x 64 k per block; writes s bf16 digit planes, K-major,
+// Tile of 32 rows x 64 k per block; writes S bf16 digit planes, K-major,
 // zero in the padding.
-__global__ void oz_split_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
-                                int64_t sr, int64_t sl,
-                                const unsigned long long* __restrict__ maxbits, int slices,
-                                int64_t rpad, int64_t kpad, __nv_bfloat16* __restrict__ out,
-                                int32_t* __restrict__ exps, int* __restrict__ nonfinite)
+template <int S>
+__global__ void __launch_bounds__(256) oz_split_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
+                                                       int64_t sr, int64_t sl,
+                                                       const unsigned long long* __restrict__ maxbits,
+                                                       int64_t rpad, int64_t kpad,
+                                                       uint16_t* __restrict__ out, int32_t* __restrict__ exps,
+                                                       int* __restrict__ nonfinite)
 {
     __shared__ double tile[32][65];
     const int64_t l0 = (int64_t)blockIdx.x * 64, r0 = (int64_t)blockIdx.y * 32;
@@ -347,7 +436,7 @@ __global__ void oz_split_kernel(int64_t rows, int64_t k, const double* __restric
         const int rr = rows_fast ? (e & 31) : (e >> 6);
         const int ll = rows_fast ? (e >> 5) : (e & 63);
         const int64_t r = r0 + rr, l = l0 + ll;
-        tile[rr][ll] = (r < rows && l < k) ? __ldg(R + r * sr + l * sl) : 0.0;
+        tile[rr][ll] = (r < rows && l < k) ? __ldcs(R + r * sr + l * sl) : 0.0;
     }
     __syncthreads();
     const int rr = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 8;
@@ -359,50 +448,99 @@ __global__ void oz_split_kernel(int64_t rows, int64_t k, const double* __restric
         if (nf) *nonfinite = 1;
         if (blockIdx.x == 0 && (threadIdx.x & 7) == 0) exps[r] = e;
     }
-    double v[8];
+    uint32_t packed[S][4];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) v[j] = (r < rows) ? ldexp(tile[rr][c0 + j], -e) : 0.0;
-    for (int pl = 0; pl < slices; ++pl) {
-        uint32_t packed[4];
+    for (int j = 0; j < 8; ++j) {
+        int d[S];
+        oz_digits<S>(r < rows ? tile[rr][c0 + j] : 0.0, e, d);
 #pragma unroll
-        for (int j = 0; j < 8; j += 2) {
-            const double t0 = v[j] * 256.0, t1 = v[j + 1] * 256.0;
-            const double d0 = rint(t0), d1 = rint(t1);
-            v[j] = t0 - d0;
-            v[j + 1] = t1 - d1;
-            const __nv_bfloat16 b0 = __float2bfloat16_rn((float)d0);
-            const __nv_bfloat16 b1 = __float2bfloat16_rn((float)d1);
-            packed[j >> 1] = (uint32_t)__bfloat16_as_ushort(b0) | ((uint32_t)__bfloat16_as_ushort(b1) << 16);
+        for (int p = 0; p < S; ++p) {
+            const uint32_t b = int_to_bf16_bits(d[p]);
+            if (j & 1) packed[p][j >> 1] |= b << 16;
+            else packed[p][j >> 1] = b;
         }
-        uint4* dst = reinterpret_cast<uint4*>(out + ((int64_t)pl * rpad + r) * kpad + l0 + c0);
-        *dst = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    }
+#pragma unroll
+    for (int p = 0; p < S; ++p) {
+        uint4* dst = reinterpret_cast<uint4*>(out + ((int64_t)p * rpad + r) * kpad + l0 + c0);
+        *dst = make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
     }
 }
 
 // ---------------------------------------------------------------- recombine
-__global__ void oz_recombine_kernel(int64_t m, int64_t n, const int32_t* __restrict__ planes,
-                                    int slices, int nparts, int64_t mpad, int64_t npad,
-                                    const int32_t* __restrict__ ea, const int32_t* __restrict__ eb,
-                                    double alpha, double beta, double* __restrict__ c,
-                                    int64_t rs_c, int64_t cs_c)
+// RNE(T * 2^E) from integers only, as IEEE bits.
+__device__ __forceinline__ double round_scaled(__int128 T, int E)
 {
-    const int64_t total = m * n;
-    const bool i_fast = (rs_c == 1 || cs_c != 1);
+    if (T == 0) return 0.0;
+    const bool neg = T < 0;
+    const unsigned __int128 u = neg ? (unsigned __int128)0 - (unsigned __int128)T : (unsigned __int128)T;
+    const int msb = 127 - clz128(u);
+    const int lead = msb + E;
+    unsigned long long bits;
+    if (lead > 1023) {
+        bits = 0x7FF0000000000000ull;
+    } else {
+        const int lsb = (lead >= -1022) ? lead - 52 : -1074;
+        const int shift = lsb - E;
+        unsigned __int128 q;
+        if (shift <= 0) {
+            q = u << (-shift);
+        } else if (shift > 128) {
+            q = 0;
+        } else if (shift == 128) {
+            q = (u > ((unsigned __int128)1 << 127)) ? 1 : 0;
+        } else {
+            q = u >> shift;
+            const unsigned __int128 rem = u & ((((unsigned __int128)1) << shift) - 1);
+            const unsigned __int128 half = ((unsigned __int128)1) << (shift - 1);
+            if (rem > half || (rem == half && (q & 1))) q += 1;
+        }
+        bits = ((unsigned long long)(lsb + 1074) << 52) + (unsigned long long)q;
+        if (bits >= 0x7FF0000000000000ull) bits = 0x7FF0000000000000ull;
+    }
+    if (neg) bits |= 0x8000000000000000ull;
+    return __longlong_as_double((long long)bits);
+}
+
+struct OzRecombParams {
+    int slices, nlevels;
+    int64_t m, n, mpad, npad;
+    const int32_t* planes;
+    const int32_t* ea;
+    const int32_t* eb;
+    double alpha, beta;
+    double* c;
+    int64_t rs_c, cs_c;
+    const int* skip;
+    OzLevel lv[OZ_MAX_SLICES];
+};
+
+__global__ void oz_recombine_kernel(const __grid_constant__ OzRecombParams p)
+{
+    if (*p.skip) return;
+    const int64_t total = p.m * p.n;
+    const bool i_fast = (p.rs_c == 1 || p.cs_c != 1);
+    const bool plain = (p.alpha == 1.0 && p.beta == 0.0);
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = i_fast ? e % m : e / n;
-        const int64_t j = i_fast ? e / m : e % n;
-        double acc = 0.0;
-        for (int q = slices - 1; q >= 0; --q) {
+        const int64_t i = i_fast ? e % p.m : e / p.n;
+        const int64_t j = i_fast ? e / p.m : e % p.n;
+        __int128 T = 0;
+        for (int L = 0; L < p.nlevels; ++L) {
+            const OzLevel& lv = p.lv[L];
             long long s = 0;
-            for (int pt = 0; pt < nparts; ++pt)
-                s += planes[(((int64_t)pt * slices + q) * npad + j) * mpad + i];
-            acc += ldexp((double)s, -8 * (q + 2));
+            for (int pt = 0; pt < lv.nparts; ++pt)
+                s += __ldcs(p.planes + ((int64_t)(lv.plane_base + pt) * p.npad + j) * p.mpad + i);
+            T += ((__int128)s) << (8 * (p.slices + 1 - lv.lev));
         }
-        const double ab = ldexp(acc, ea[i] + eb[j]);
-        double* cij = c + i * rs_c + j * cs_c;
-        const double t = __dmul_rn(alpha, ab);
-        *cij = (beta == 0.0) ? t : __fma_rn(beta, *cij, t);
+        const double ab = round_scaled(T, p.ea[i] + p.eb[j] - 8 * (p.slices + 1));
+        double* cij = p.c + i * p.rs_c + j * p.cs_c;
+        if (plain) {
+            *cij = ab;
+        } else {
+            const double t = __dmul_rn(p.alpha, ab);
+            *cij = (p.beta == 0.0) ? t : __fma_rn(p.beta, *cij, t);
+        }
     }
 }
 
@@ -411,11 +549,11 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
         cudaDriverEntryPointQueryResult q;
-        void* p = nullptr;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+        void* ptr = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault,
                                              &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
     }
     return fn;
 }
@@ -449,14 +587,51 @@ int chunk_kb_setting()
     return v;
 }
 
+template <int S>
+void launch_split(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl,
+                  const unsigned long long* mb, int64_t rpad, int64_t kpad, uint16_t* out, int32_t* ex,
+                  int* nonfinite, cudaStream_t s)
+{
+    LaunchScope ls("oz_split", s);
+    oz_split_kernel<S><<<dim3((unsigned)(kpad / 64), (unsigned)(rpad / 32)), 256, 0, s>>>(
+        rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite);
+}
+
+void split_dispatch(int slices, int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl,
+                    const unsigned long long* mb, int64_t rpad, int64_t kpad, uint16_t* out, int32_t* ex,
+                    int* nonfinite, cudaStream_t s)
+{
+    switch (slices) {
+#define GB_SPLIT_CASE(S) \
+    case S: launch_split<S>(rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, s); break;
+        GB_SPLIT_CASE(2) GB_SPLIT_CASE(3) GB_SPLIT_CASE(4) GB_SPLIT_CASE(5) GB_SPLIT_CASE(6)
+        GB_SPLIT_CASE(7) GB_SPLIT_CASE(8) GB_SPLIT_CASE(9) GB_SPLIT_CASE(10) GB_SPLIT_CASE(11)
+        GB_SPLIT_CASE(12)
+#undef GB_SPLIT_CASE
+    default: break;
+    }
+}
+
 }  // namespace
 
-// Largest K of one part: slices * Kpart * 128^2 < 2^31, in whole 1024 chunks.
-int64_t ozaki_kpart_limit(int slices)
+// Largest K of one part of a level with `npairs` slice products:
+// npairs * Kpart * 128^2 < 2^31, Kpart a multiple of the 64-wide k block.
+int64_t ozaki_kpart_limit(int npairs)
 {
-    int64_t lim = (int64_t)2147483647 / ((int64_t)slices * 128 * 128);
-    lim = (lim / 1024) * 1024;
-    return lim < 1024 ? 1024 : lim;
+    int64_t lim = (int64_t)2147483647 / ((int64_t)npairs * 128 * 128);
+    lim = (lim / OZ_BK) * OZ_BK;
+    return lim < OZ_BK ? OZ_BK : lim;
+}
+
+// log2 of the largest |T| the recombination can meet (must stay < 126).
+double ozaki_t_bound_log2(int s, int64_t k)
+{
+    double t = 0.0;
+    for (int l = 2; l <= s + 1; ++l) {
+        const int np = (l - 1 < s) ? l - 1 : s;
+        t += (double)np * (double)k * 16384.0 * ldexp(1.0, 8 * (s + 1 - l));
+    }
+    return log2(t);
 }
 
 int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
@@ -466,30 +641,60 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
 {
     if (m <= 0 || n <= 0) return GB_SUCCESS;
     if (alpha == 0.0 || k <= 0) return scal_matrix(m, n, beta, c, rs_c, cs_c, s);
-    if (slices < 2 || slices > 16) return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices must be in [2, 16]");
+    if (slices < 2 || slices > OZ_MAX_SLICES)
+        return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices must be in [2, 12]");
+    if (ozaki_t_bound_log2(slices, k) >= 126.0)
+        return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices and k exceed the 128-bit recombination range");
 
     const int64_t kpad = round_up(k, OZ_BK), mpad = round_up(m, OZ_BM), npad = round_up(n, OZ_BN);
-    const int64_t lim = ozaki_kpart_limit(slices);
-    const int nparts = (int)((k + lim - 1) / lim);
-    const int kb_total = (int)(kpad / OZ_BK);
-    const int kb_per_part = (kb_total + nparts - 1) / nparts;
-    if ((int64_t)kb_per_part * OZ_BK > lim) return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "k partition");
     if (mpad > INT32_MAX || npad > INT32_MAX || kpad > INT32_MAX)
         return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "dimension too large for TMA coordinates");
+    const int kb_total = (int)(kpad / OZ_BK);
+
+    OzGemmParams p;
+    p.slices = slices;
+    p.nlevels = slices;
+    p.kb_total = kb_total;
+    p.tiles_m = (int)(mpad / OZ_BM);
+    p.tiles_n = (int)(npad / OZ_BN);
+    const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
+    int planes_total = 0;
+    int64_t items = 0;
+    for (int L = 0; L < slices; ++L) {  // heaviest level (most pairs) first
+        OzLevel& lv = p.lv[L];
+        lv.lev = slices + 1 - L;
+        lv.pa_lo = (lv.lev - slices > 1) ? lv.lev - slices : 1;
+        const int pa_hi = (lv.lev - 1 < slices) ? lv.lev - 1 : slices;
+        lv.npairs = pa_hi - lv.pa_lo + 1;
+        const int64_t lim_kb = ozaki_kpart_limit(lv.npairs) / OZ_BK;
+        lv.nparts = (int)((kb_total + lim_kb - 1) / lim_kb);
+        lv.kb_per_part = (kb_total + lv.nparts - 1) / lv.nparts;
+        lv.plane_base = planes_total;
+        lv.item_base = items;
+        planes_total += lv.nparts;
+        items += (int64_t)lv.nparts * tiles;
+    }
+    p.items = items;
+    p.chunk_kb = chunk_kb_setting();
+    p.mpad = mpad;
+    p.npad = npad;
 
     const size_t bytes_sa = (size_t)slices * mpad * kpad * 2, bytes_sb = (size_t)slices * npad * kpad * 2;
-    const size_t bytes_pl = (size_t)nparts * slices * npad * mpad * 4;
+    const size_t bytes_pl = (size_t)planes_total * npad * mpad * 4;
     const size_t bytes_aux = sizeof(unsigned long long) * (m + n) + sizeof(int32_t) * (m + n) + 64;
     uint8_t* ws = static_cast<uint8_t*>(dev_alloc(bytes_sa + bytes_sb + bytes_pl + bytes_aux + 1024, s));
     if (!ws) return GB_ERR_NOMEM;
-    __nv_bfloat16* sa = reinterpret_cast<__nv_bfloat16*>(ws);
-    __nv_bfloat16* sb = reinterpret_cast<__nv_bfloat16*>(ws + bytes_sa);
+    uint16_t* sa = reinterpret_cast<uint16_t*>(ws);
+    uint16_t* sb = reinterpret_cast<uint16_t*>(ws + bytes_sa);
     int32_t* planes = reinterpret_cast<int32_t*>(ws + bytes_sa + bytes_sb);
     unsigned long long* maxa = reinterpret_cast<unsigned long long*>(ws + bytes_sa + bytes_sb + bytes_pl);
     unsigned long long* maxb = maxa + m;
     int32_t* ea = reinterpret_cast<int32_t*>(maxb + n);
     int32_t* eb = ea + m;
     int* nonfinite = reinterpret_cast<int*>(eb + n);
+    p.planes = planes;
+    p.status = device_status_word();
+    p.skip = nonfinite;
 
     int rc = GB_SUCCESS;
     auto bail = [&](int code) { dev_free(ws, s); return code; };
@@ -499,37 +704,33 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
 
     const int sms = sm_count() > 0 ? sm_count() : 148;
     auto rowmax = [&](int64_t rows, const double* R, int64_t sr, int64_t sl, unsigned long long* mb) {
-        const int64_t gx = (rows + 63) / 64;
-        int64_t gy = (k + 63) / 64;
-        const int64_t want = (int64_t)sms * 8;
-        if (gx * gy > want) gy = (want + gx - 1) / gx;
-        if (gy < 1) gy = 1;
-        if (gy > 65535) gy = 65535;
-        LaunchScope ls("oz_rowmax", s);
-        oz_rowmax_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sr, sl, mb);
-    };
-    auto split = [&](int64_t rows, int64_t rpad, const double* R, int64_t sr, int64_t sl,
-                     const unsigned long long* mb, __nv_bfloat16* out, int32_t* ex) {
-        LaunchScope ls("oz_split", s);
-        oz_split_kernel<<<dim3((unsigned)(kpad / 64), (unsigned)(rpad / 32)), 256, 0, s>>>(
-            rows, k, R, sr, sl, mb, slices, rpad, kpad, out, ex, nonfinite);
+        if (sr == 1) {
+            const int64_t gx = (rows + 255) / 256;
+            int64_t gy = ((int64_t)sms * 8 + gx - 1) / gx;
+            if (gy > k) gy = k;
+            if (gy > 65535) gy = 65535;
+            const int64_t kchunk = (k + gy - 1) / gy;
+            gy = (k + kchunk - 1) / kchunk;
+            LaunchScope ls("oz_rowmax", s);
+            oz_rowmax_rows_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sl, kchunk, mb);
+        } else {
+            const int64_t gx = (rows * 32 + 255) / 256;
+            int64_t gy = ((int64_t)sms * 8 + gx - 1) / gx;
+            if (gy > (k + 255) / 256) gy = (k + 255) / 256;
+            if (gy < 1) gy = 1;
+            if (gy > 65535) gy = 65535;
+            const int64_t kchunk = (k + gy - 1) / gy;
+            gy = (k + kchunk - 1) / kchunk;
+            LaunchScope ls("oz_rowmax", s);
+            oz_rowmax_warp_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sr, sl, kchunk, mb);
+        }
     };
     // rows of op(A): element (i, l) = a[i*ars + l*acs]; rows of op(B)^T: (j, l) = b[l*brs + j*bcs]
     rowmax(m, a, ars, acs, maxa);
     rowmax(n, b, bcs, brs, maxb);
-    split(m, mpad, a, ars, acs, maxa, sa, ea);
-    split(n, npad, b, bcs, brs, maxb, sb, eb);
+    split_dispatch(slices, m, k, a, ars, acs, maxa, mpad, kpad, sa, ea, nonfinite, s);
+    split_dispatch(slices, n, k, b, bcs, brs, maxb, npad, kpad, sb, eb, nonfinite, s);
     if ((rc = check_cuda(cudaGetLastError(), "oz_split"))) return bail(rc);
-
-    int nf = 0;
-    if ((rc = check_cuda(cudaMemcpyAsync(&nf, nonfinite, sizeof(int), cudaMemcpyDeviceToHost, s), "nonfinite")))
-        return bail(rc);
-    if ((rc = check_cuda(cudaStreamSynchronize(s), "nonfinite"))) return bail(rc);
-    if (nf) {
-        // Inf/NaN cannot be cut into digits: IEEE semantics come from the native kernel.
-        dev_free(ws, s);
-        return dgemm_native(m, n, k, alpha, a, ars, acs, b, brs, bcs, beta, c, rs_c, cs_c, s);
-    }
 
     CUtensorMap map_a, map_b;
     if ((rc = make_slice_map(&map_a, sa, kpad, mpad, slices, OZ_BM))) return bail(rc);
@@ -543,19 +744,6 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
             return bail(rc);
         attr_set = true;
     }
-    OzGemmParams p;
-    p.slices = slices;
-    p.nparts = nparts;
-    p.kb_per_part = kb_per_part;
-    p.kb_total = kb_total;
-    p.tiles_m = (int)(mpad / OZ_BM);
-    p.tiles_n = (int)(npad / OZ_BN);
-    p.items = (int64_t)slices * nparts * p.tiles_m * p.tiles_n;
-    p.chunk_kb = chunk_kb_setting();
-    p.mpad = mpad;
-    p.npad = npad;
-    p.planes = planes;
-    p.status = device_status_word();
     const int grid = (int)((p.items < sms) ? p.items : sms);
     {
         LaunchScope ls("ozaki_slice_gemm", s);
@@ -563,14 +751,32 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     }
     if ((rc = check_cuda(cudaGetLastError(), "ozaki_slice_gemm"))) return bail(rc);
     {
+        OzRecombParams r;
+        r.slices = slices;
+        r.nlevels = slices;
+        r.m = m;
+        r.n = n;
+        r.mpad = mpad;
+        r.npad = npad;
+        r.planes = planes;
+        r.ea = ea;
+        r.eb = eb;
+        r.alpha = alpha;
+        r.beta = beta;
+        r.c = c;
+        r.rs_c = rs_c;
+        r.cs_c = cs_c;
+        r.skip = nonfinite;
+        for (int L = 0; L < slices; ++L) r.lv[L] = p.lv[L];
         const int64_t total = m * n;
         int64_t blocks = (total + 255) / 256;
         if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
         LaunchScope ls("oz_recombine", s);
-        oz_recombine_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, planes, slices, nparts, mpad, npad,
-                                                            ea, eb, alpha, beta, c, rs_c, cs_c);
+        oz_recombine_kernel<<<(unsigned)blocks, 256, 0, s>>>(r);
     }
-    rc = check_cuda(cudaGetLastError(), "oz_recombine");
+    if ((rc = check_cuda(cudaGetLastError(), "oz_recombine"))) return bail(rc);
+    // IEEE path for non-finite operands: runs only when the split raised the flag
+    rc = dgemm_native_gated(m, n, k, alpha, a, ars, acs, b, brs, bcs, beta, c, rs_c, cs_c, nonfinite, s);
     dev_free(ws, s);
     return rc;
 }

@@ -11,8 +11,12 @@ import torch
 from . import _lib
 
 
+_LEGACY_DEFAULT_STREAM = 1  # cudaStreamLegacy: a NULL handle would select the library's own stream
+
+
 def _stream():
-    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    h = torch.cuda.current_stream().cuda_stream
+    return C.c_void_p(h if h else _LEGACY_DEFAULT_STREAM)
 
 
 def _rc(t):

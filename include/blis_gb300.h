@@ -214,6 +214,29 @@ void bli_ddotv_ex(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t n, const double* x,
                   gb_inc_t incx, const double* y, gb_inc_t incy, double* rho,
                   const void* cntx, const void* rntm);
 
+/* Host-pointer entry points under the addon prefix, with the typed-API
+   argument lists above.  A BLIS build that keeps its own bli_?gemm symbols
+   (for instance the gb300 sandbox's bli_gemm_ex) calls
+   these instead, which cannot resolve back into libblis. */
+void gb_dgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+              const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+              const double* b, gb_inc_t rs_b, gb_inc_t cs_b, const double* beta,
+              double* c, gb_inc_t rs_c, gb_inc_t cs_c);
+void gb_sgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+              const float* alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a,
+              const float* b, gb_inc_t rs_b, gb_inc_t cs_b, const float* beta,
+              float* c, gb_inc_t rs_c, gb_inc_t cs_c);
+void gb_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
+              gb_dim_t m, gb_dim_t n, const double* alpha, const double* a,
+              gb_inc_t rs_a, gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b);
+void gb_dgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n,
+              const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+              const double* x, gb_inc_t incx, const double* beta, double* y, gb_inc_t incy);
+void gb_daxpyv(gb_conj_t conjx, gb_dim_t n, const double* alpha, const double* x,
+               gb_inc_t incx, double* y, gb_inc_t incy);
+void gb_ddotv(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t n, const double* x,
+              gb_inc_t incx, const double* y, gb_inc_t incy, double* rho);
+
 /* ===================================================================== */
 /* 2. gb_ addon: device pointers, explicit stream (NULL = the calling      */
 /*    thread's library stream).  Return GB_SUCCESS or a negative code.     */

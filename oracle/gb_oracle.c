@@ -444,31 +444,133 @@ void orc_dd_dotv(int64_t n, const double* x, int64_t incx, const double* y,
 }
 
 /* ------------------------------------------------------------------ */
-/* Ozaki split-product model.                                          */
+/* Ozaki split-product model (exact integer specification).            */
 /*                                                                     */
-/* Each row r of the row operand (op(A), or op(B)^T) is scaled by       */
-/* 2^-e_r with e_r = ilogb(max_k |r_k|) + 2, so |v| < 1/2, and then cut */
-/* into s balanced base-256 digits by rounding to nearest:              */
-/*     t = 256*v; d_p = rint(t); v = t - d_p         (all exact)        */
-/* so r = 2^e_r * (sum_p d_p 2^-8p + remainder), |d_p| <= 128, and the  */
-/* remainder is at most 2^-(8s+1) * 2^e_r.  Each digit is exact in      */
-/* bf16; a product of two digits is at most 2^14, so 1024 of them sum   */
-/* exactly in fp32 (the GPU's accumulation chunk).                       */
-/* Level sums S_l = sum_{p+q=l} D^A_p (D^B_q)^T for l = 2..s+1 (the     */
-/* triangular product set, s(s+1)/2 products) are exact integers; the   */
-/* GPU keeps them in int32, so K is cut into parts with                 */
-/* s * Kpart * 2^14 < 2^31.                                             */
-/* Recombination, least significant level first, in FP64:               */
-/*     acc = 0; for l = s+1 .. 2: acc += S_l * 2^-8l                    */
-/*     AB  = acc * 2^(e_i + e_j)                                        */
-/*     c   = beta == 0 ? alpha*AB : fma(beta, c, alpha*AB)               */
+/* Each row r of the row operand (op(A), or op(B)^T) gets the exponent  */
+/* e_r = ilogb(max_k |r_k|) + 2, so U = |x| 2^-e_r < 1/2 for every      */
+/* element x of the row, and x = sign(x) 2^e_r sum_p d_p 2^-8p + rem    */
+/* with the balanced base-256 digits of U taken greedily with rounding  */
+/* to nearest, ties to even: t_p = 256 * (remainder); d_p = rint(t_p).  */
+/* |d_p| <= 128, every digit is exact in bf16, |rem| <= 2^-(8s+1) 2^e_r.*/
+/* The digits are computed on the exact value (128-bit fixed point with */
+/* 8s+2 fraction bits and a sticky bit), never in floating point.       */
+/*                                                                     */
+/* Level sums S_l = sum_{p+q=l} D^A_p (D^B_q)^T, l = 2..s+1 (the        */
+/* triangular set, s(s+1)/2 products), are exact integers.  The GPU     */
+/* accumulates 1024 products at a time in fp32 (|sum| <= 2^24, exact)   */
+/* and level sums in int32, cutting K into parts so that                */
+/* npairs(l) * Kpart * 2^14 < 2^31.                                     */
+/*                                                                     */
+/* Recombination is one rounding of an exact value:                     */
+/*     T  = sum_l S_l 2^(8(s+1-l))          (exact, signed 128-bit)     */
+/*     AB = RNE(T * 2^(e_i + e_j - 8(s+1)))                             */
+/*     c  = beta == 0 ? alpha*AB : fma(beta, c, alpha*AB)               */
+/* (alpha == 1, beta == 0 gives c = AB, the correctly rounded value of  */
+/* the truncated split product).                                        */
 /* ------------------------------------------------------------------ */
-int64_t orc_ozaki_kpart_limit(int slices)
+typedef __int128 i128;
+typedef unsigned __int128 u128;
+
+int64_t orc_ozaki_kpart_limit(int npairs)
 {
-    /* level sums must stay below 2^31 in int32: pairs * K * 128^2 < 2^31 */
-    int64_t lim = (int64_t)2147483647 / ((int64_t)slices * 128 * 128);
-    lim = (lim / 1024) * 1024;
-    return lim < 1024 ? 1024 : lim;
+    /* int32 level sums: npairs * Kpart * 128^2 < 2^31, Kpart a multiple of 64 */
+    int64_t lim = (int64_t)2147483647 / ((int64_t)npairs * 128 * 128);
+    lim = (lim / 64) * 64;
+    return lim < 64 ? 64 : lim;
+}
+
+/* Largest |T| the recombination can meet, as a power-of-two exponent. */
+static double oz_t_bound_log2(int s, int64_t k)
+{
+    double t = 0.0;
+    for (int l = 2; l <= s + 1; ++l) {
+        const int np = (l - 1 < s) ? l - 1 : s;
+        t += (double)np * (double)k * 16384.0 * ldexp(1.0, 8 * (s + 1 - l));
+    }
+    return log2(t);
+}
+
+static int clz128(u128 u)
+{
+    const uint64_t hi = (uint64_t)(u >> 64), lo = (uint64_t)u;
+    if (hi) return __builtin_clzll(hi);
+    if (lo) return 64 + __builtin_clzll(lo);
+    return 128;
+}
+
+/* RNE(T * 2^E) as a double, from integers only. */
+static double oz_round_scaled(i128 T, int E)
+{
+    if (T == 0) return 0.0;
+    const int neg = T < 0;
+    const u128 u = neg ? (u128)0 - (u128)T : (u128)T;
+    const int msb = 127 - clz128(u);
+    const int lead = msb + E;
+    uint64_t bits;
+    if (lead > 1023) {
+        bits = 0x7FF0000000000000ull;
+    } else {
+        const int lsb = (lead >= -1022) ? lead - 52 : -1074;  /* exponent of the last kept bit */
+        const int shift = lsb - E;
+        u128 q;
+        if (shift <= 0) {
+            q = u << (-shift);
+        } else if (shift > 128) {
+            q = 0;
+        } else if (shift == 128) {
+            q = (u > ((u128)1 << 127)) ? 1 : 0;
+        } else {
+            q = u >> shift;
+            const u128 rem = u & ((((u128)1) << shift) - 1);
+            const u128 half = ((u128)1) << (shift - 1);
+            if (rem > half || (rem == half && (q & 1))) q += 1;
+        }
+        bits = ((uint64_t)(lsb + 1074) << 52) + (uint64_t)q;
+        if (bits >= 0x7FF0000000000000ull) bits = 0x7FF0000000000000ull;
+    }
+    if (neg) bits |= 0x8000000000000000ull;
+    double r;
+    memcpy(&r, &bits, sizeof r);
+    return r;
+}
+
+/* Balanced base-256 digits of |x| 2^-e (exact), with the sign of x. */
+static void oz_digits(double x, int e, int s, int16_t* d, int64_t stride)
+{
+    uint64_t bits;
+    memcpy(&bits, &x, sizeof bits);
+    const int neg = (int)(bits >> 63);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    const uint64_t frac = bits & ((1ull << 52) - 1);
+    if (ex == 0 && frac == 0) {
+        for (int p = 0; p < s; ++p) d[p * stride] = 0;
+        return;
+    }
+    const uint64_t M = ex ? (frac | (1ull << 52)) : frac;
+    const int E2 = ex ? ex - 1075 : -1074;  /* |x| = M 2^E2 */
+    const int F = 8 * s + 2;                /* fraction bits kept */
+    const int sh = E2 - e + F;              /* U 2^F = M 2^sh */
+    i128 R;
+    int sticky = 0;
+    if (sh >= 0) {
+        R = (i128)((u128)M << sh);
+    } else if (sh > -64) {
+        R = (i128)(M >> (-sh));
+        sticky = (M & ((1ull << (-sh)) - 1)) != 0;
+    } else {
+        R = 0;
+        sticky = 1;
+    }
+    for (int p = 1; p <= s; ++p) {
+        const int w = F - 8 * p;  /* weight of digit p: 2^w */
+        const i128 q = R >> w;    /* floor */
+        const i128 rem = R - (q << w);
+        const i128 half = ((i128)1) << (w - 1);
+        i128 dg = q;
+        if (rem > half || (rem == half && (sticky || (q & 1)))) dg = q + 1;
+        R -= dg << w;
+        d[(p - 1) * stride] = (int16_t)(neg ? -dg : dg);
+    }
 }
 
 void orc_ozaki_split(int64_t rows, int64_t k, const double* r, int64_t rs, int64_t cs,
@@ -479,15 +581,8 @@ void orc_ozaki_split(int64_t rows, int64_t k, const double* r, int64_t rs, int64
         for (int64_t l = 0; l < k; ++l) { double v = fabs(r[i * rs + l * cs]); if (v > mx) mx = v; }
         const int e = (mx == 0.0) ? 0 : ilogb(mx) + 2;
         exps[i] = e;
-        for (int64_t l = 0; l < k; ++l) {
-            double v = ldexp(r[i * rs + l * cs], -e);
-            for (int p = 0; p < slices; ++p) {
-                double t = v * 256.0;
-                double d = rint(t);
-                v = t - d;
-                digits[((int64_t)p * rows + i) * k + l] = (int16_t)d;
-            }
-        }
+        for (int64_t l = 0; l < k; ++l)
+            oz_digits(r[i * rs + l * cs], e, slices, digits + i * k + l, rows * k);
     }
 }
 
@@ -513,10 +608,11 @@ static void oz_task(void* p, int tid, int nt)
                     for (int64_t l = 0; l < g->k; ++l) acc += (int64_t)ra[l] * (int64_t)rb[l];
                     lev[pa + pb] += acc;
                 }
-            double acc = 0.0;
-            for (int l = s + 1; l >= 2; --l) acc += ldexp((double)lev[l], -8 * l);
-            const double ab = ldexp(acc, g->ea[i] + g->eb[j]);
+            i128 T = 0;
+            for (int l = 2; l <= s + 1; ++l) T += (i128)lev[l] * ((i128)1 << (8 * (s + 1 - l)));
+            const double ab = oz_round_scaled(T, g->ea[i] + g->eb[j] - 8 * (s + 1));
             double* cij = g->c + i * g->rs_c + j * g->cs_c;
+            if (g->alpha == 1.0 && g->beta == 0.0) { *cij = ab; continue; }
             const double t = g->alpha * ab;
             *cij = (g->beta == 0.0) ? t : fma(g->beta, *cij, t);
         }
@@ -531,6 +627,7 @@ int orc_ozaki_dgemm(int transa, int transb, int64_t m, int64_t n, int64_t k,
 {
     if (m <= 0 || n <= 0) return 0;
     if (alpha == 0.0 || k <= 0) { d_scalm(m, n, beta, c, rs_c, cs_c); return 0; }
+    if (slices < 2 || slices > 12 || oz_t_bound_log2(slices, k) >= 126.0) return -1;
     const int64_t ars = ORC_TRANS(transa) ? cs_a : rs_a, acs = ORC_TRANS(transa) ? rs_a : cs_a;
     const int64_t brs = ORC_TRANS(transb) ? cs_b : rs_b, bcs = ORC_TRANS(transb) ? rs_b : cs_b;
     /* non-finite operands cannot be sliced: the native FP64 path is used */

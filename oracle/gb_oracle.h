@@ -80,7 +80,7 @@ void orc_dd_dotv(int64_t n, const double* x, int64_t incx, const double* y,
                  int64_t incy, double* hi, double* lo);
 
 /* ---- Ozaki split-product model (bit-exact model of the GPU form) ---- */
-int64_t orc_ozaki_kpart_limit(int slices);
+int64_t orc_ozaki_kpart_limit(int npairs);
 void orc_ozaki_split(int64_t rows, int64_t k, const double* r, int64_t rs, int64_t cs,
                      int slices, int32_t* exps, int16_t* digits);
 int orc_ozaki_dgemm(int transa, int transb, int64_t m, int64_t n, int64_t k,

@@ -24,9 +24,9 @@ def native(gblib):
 def storage(x, kind):
     """Copy x into row ('r'), column ('c') or general-stride ('g') storage."""
     if kind == "c":
-        return np.asfortranarray(x)
+        return np.array(x, order="F", copy=True)
     if kind == "r":
-        return np.ascontiguousarray(x)
+        return np.array(x, order="C", copy=True)
     big = np.full((2 * x.shape[0] + 1, 3 * x.shape[1] + 1), np.nan, order="F")
     v = big[1::2, 1::3][: x.shape[0], : x.shape[1]]
     v[...] = x

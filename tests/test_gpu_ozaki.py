@@ -56,17 +56,50 @@ def test_ozaki_transposes_and_layouts(ta, tb, rowmajor):
     assert np.array_equal(c, ref)
 
 
-def test_ozaki_k_partitions_bit_exact():
-    # 16 slices: one k part holds at most 7168 -> k = 8000 uses two parts
-    assert po.ozaki_kpart_limit(16) < 8000
-    m, n, k = 64, 96, 8000
+@pytest.mark.parametrize("slices,k", [(12, 12000), (8, 16384)])
+def test_ozaki_k_partitions_bit_exact(slices, k):
+    # the level with the most slice pairs needs more than one int32 k part
+    assert po.ozaki_kpart_limit(slices) < k
+    m, n = 64, 96
     a = po.expspread((m, k), 7)
     b = po.expspread((k, n), 8)
     ref = np.zeros((m, n), order="F")
-    po.ozaki_dgemm(N, N, 1.0, a, b, 0.0, ref, 16)
+    po.ozaki_dgemm(N, N, 1.0, a, b, 0.0, ref, slices)
     c = np.zeros((m, n), order="F")
-    _run_gpu(N, N, 1.0, a, b, 0.0, c, 16)
+    _run_gpu(N, N, 1.0, a, b, 0.0, c, slices)
     assert np.array_equal(c, ref)
+
+
+def test_ozaki_device_random_inputs_match_host_generator():
+    torch = pytest.importorskip("torch")
+    from blis_gb300 import dev
+    x = dev.colmajor(300, 70)
+    dev.randm(x, dev.RAND_EXPSPREAD, 99, -20, 20)
+    y = dev.colmajor(300, 70)
+    dev.randm(y, dev.RAND_UNIFORM, 98, -1.0, 1.0)
+    torch.cuda.synchronize()
+    assert np.array_equal(x.cpu().numpy(), po.expspread((300, 70), 99, -20, 20))
+    assert np.array_equal(y.cpu().numpy(), po.uniform((300, 70), 98))
+
+
+def test_ozaki_device_dd_evaluator_matches_cpu():
+    torch = pytest.importorskip("torch")
+    from blis_gb300 import dev
+    m, n, k = 200, 150, 3000
+    a = po.expspread((m, k), 3)
+    b = po.expspread((k, n), 4)
+    c = po.uniform((m, n), 5)
+    ii = np.arange(0, m * n, 97) % m
+    jj = (np.arange(0, m * n, 97) // m) % n
+    hi, lo = po.dd_gemm_entries(0, 0, 1.5, a, b, -0.5, c, ii, jj)
+    ta = torch.from_numpy(a.T.copy()).cuda().t()
+    tb = torch.from_numpy(b.T.copy()).cuda().t()
+    tc = torch.from_numpy(c.T.copy()).cuda().t()
+    dh, dl = dev.dd_gemm_entries(0, 0, 1.5, ta, tb, -0.5, tc, torch.from_numpy(ii).cuda(),
+                                 torch.from_numpy(jj).cuda())
+    g = 1.5 * (np.abs(a) @ np.abs(b))[ii, jj] + 0.5 * np.abs(c[ii, jj])
+    # different summation orders: both are double-double accurate (~2^-100 of the gauge)
+    assert np.all(np.abs((dh.cpu().numpy() - hi) + (dl.cpu().numpy() - lo)) <= 2.0 ** -96 * g)
 
 
 def test_ozaki_error_not_worse_than_native():

@@ -246,9 +246,54 @@ def test_ozaki_split_digits_exact():
 
 
 def test_ozaki_kpart_limit():
-    for s in range(2, 17):
-        lim = po.ozaki_kpart_limit(s)
-        assert lim % 1024 == 0 and s * lim * 128 * 128 < 2 ** 31
+    for npairs in range(1, 13):
+        lim = po.ozaki_kpart_limit(npairs)
+        assert lim % 64 == 0 and npairs * lim * 128 * 128 < 2 ** 31
+        assert npairs * (lim + 64) * 128 * 128 >= 2 ** 31 - 1 or lim + 64 > 2 ** 31
+
+
+def _digits_fp64(x, e, s):
+    """The same digits by the floating-point recurrence t = 256 v; d = rint(t);
+    v = t - d (exact for normal-range values)."""
+    v = np.ldexp(x, -e)
+    out = []
+    for _ in range(s):
+        t = v * 256.0
+        d = np.rint(t)
+        v = t - d
+        out.append(d)
+    return np.array(out)
+
+
+def test_ozaki_integer_digits_match_float_recurrence():
+    r = po.expspread((7, 200), 51)
+    r[3, 5] = 0.0
+    r[4, :] = po.uniform((1, 200), 52)
+    for s in (3, 8, 12):
+        exps, dig = po.ozaki_split(r, s)
+        for i in range(r.shape[0]):
+            ref = _digits_fp64(r[i], exps[i], s)
+            assert np.array_equal(dig[:, i, :], ref.astype(np.int16))
+
+
+def test_ozaki_recombination_is_correctly_rounded():
+    from fractions import Fraction
+    m, n, k, s = 6, 5, 40, 4
+    a = po.expspread((m, k), 61)
+    b = po.expspread((k, n), 62)
+    c = np.zeros((m, n), order="F")
+    po.ozaki_dgemm(0, 0, 1.0, a, b, 0.0, c, s)
+    ea, da = po.ozaki_split(np.asfortranarray(a), s)
+    eb, db = po.ozaki_split(np.asfortranarray(b.T), s)
+    for i in range(m):
+        for j in range(n):
+            tot = Fraction(0)
+            for pa in range(1, s + 1):
+                for pb in range(1, s + 2 - pa):
+                    dot = int(np.dot(da[pa - 1, i].astype(np.int64), db[pb - 1, j].astype(np.int64)))
+                    tot += Fraction(dot) * Fraction(2) ** (-8 * (pa + pb))
+            exact = tot * Fraction(2) ** int(ea[i] + eb[j])
+            assert c[i, j] == float(exact)  # Fraction -> float rounds to nearest even
 
 
 def test_rng_matches_numpy_restatement():
