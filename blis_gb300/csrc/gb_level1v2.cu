@@ -255,24 +255,29 @@ int daxpyv_dev(int64_t n, double alpha, const double* x, int64_t incx, double* y
     return check_cuda(cudaGetLastError(), "daxpyv");
 }
 
-int dotv_nparts(int64_t n)
+// Number of first-pass partial sums for a dot product of length n on a GPU
+// with `sms` SMs: one per 4096 elements, at most 8 per SM.
+static int dotv_nparts_for(int64_t n, int sms)
 {
     int64_t g = (n + 4095) / 4096;
-    const int64_t cap = (int64_t)(sm_count() > 0 ? sm_count() : 152) * 8;
+    const int64_t cap = (int64_t)(sms > 0 ? sms : 152) * 8;
     if (g > cap) g = cap;
     return (int)(g < 1 ? 1 : g);
 }
 
+int dotv_nparts(int64_t n) { return dotv_nparts_for(n, sm_count()); }
+
+// Two-pass dot product with `nparts` first-pass partial sums in `scratch`
+// (at least nparts doubles); the partition depends only on n and nparts.
 int ddotv_dev(int64_t n, const double* x, int64_t incx, const double* y, int64_t incy,
-              double* rho_dev, double* scratch, int64_t scratch_len, cudaStream_t s)
+              double* rho_dev, double* scratch, int64_t nparts, cudaStream_t s)
 {
     if (n <= 0) {
         LaunchScope ls("dotv_zero", s);
         set_scalar_kernel<<<1, 1, 0, s>>>(rho_dev, 0.0);
         return check_cuda(cudaGetLastError(), "ddotv");
     }
-    const int nparts = dotv_nparts(n);
-    if (scratch_len < nparts) return set_error(GB_ERR_ARG, "ddotv", "scratch too small");
+    if (nparts < 1) return set_error(GB_ERR_ARG, "ddotv", "no scratch for the partial sums");
     int64_t chunk = (n + nparts - 1) / nparts;
     chunk = (chunk + 1) & ~int64_t(1);  // keep chunk starts 16-byte aligned
     const int nblk = (int)((n + chunk - 1) / chunk);
@@ -345,3 +350,70 @@ int dgemv_dev(int trans, int64_t m, int64_t n, double alpha, const double* a,
 }
 
 }  // namespace gb
+
+// ---------------------------------------------------------------- allocation-free dotv
+// gb_ddotv_noalloc_dev: the dot product for callers that cannot allocate
+// device memory.  cudaMalloc/cudaFree can synchronize the whole device and
+// some host applications forbid them outright (they own a fixed device
+// memory budget through their own pool, or run latency-bound loops that must
+// not stall).  This entry point takes its partial-sum scratch from the
+// file-scope array below instead of the library's pool, and it also skips the
+// library's one-time initialisation (which allocates a status word).
+//
+// The array lives on every GPU that loads the library until the process
+// exits: GB_DOTV_NOALLOC_MAX_PARTS doubles (16 KiB).  Every call shares it and
+// finds the previous call's partial sums there; each call overwrites all the
+// slots it reads, so nothing needs clearing, but two calls that overlap on the
+// GPU (different streams, no ordering between them) race on the array.
+#include <mutex>
+
+#define GB_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) double gb_dotv_noalloc_scratch[GB_DOTV_NOALLOC_MAX_PARTS];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[GB_NOALLOC_MAX_DEVICES];  // device address of the array, per device
+int g_noalloc_sms[GB_NOALLOC_MAX_DEVICES];
+}  // namespace
+
+extern "C" int gb_ddotv_noalloc_dev(gb_dim_t n, const double* x, gb_inc_t incx, const double* y,
+                                    gb_inc_t incy, double* rho, void* stream)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return gb::check_cuda(e, "gb_ddotv_noalloc_dev: cudaGetDevice");
+    if (dev < 0 || dev >= GB_NOALLOC_MAX_DEVICES)
+        return gb::set_error(GB_ERR_UNSUPPORTED, "gb_ddotv_noalloc_dev", "device index out of range");
+    double* scratch = nullptr;
+    int sms = 0;
+    {
+        // first call on this device (with it current): look up the array's
+        // device address; the host-side name is only a stand-in for it
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, gb_dotv_noalloc_scratch);
+            if (e != cudaSuccess) return gb::check_cuda(e, "gb_ddotv_noalloc_dev: cudaGetSymbolAddress");
+            int nsm = 0;
+            e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return gb::check_cuda(e, "gb_ddotv_noalloc_dev: SM count");
+            g_noalloc_sms[dev] = nsm;
+            g_noalloc_ptr[dev] = static_cast<double*>(p);
+        }
+        scratch = g_noalloc_ptr[dev];
+        sms = g_noalloc_sms[dev];
+    }
+    if (n > 0 && (x == nullptr || y == nullptr || incx == 0 || incy == 0))
+        return gb::set_error(GB_ERR_ARG, "gb_ddotv_noalloc_dev", "null vector or zero increment");
+    if (rho == nullptr) return gb::set_error(GB_ERR_ARG, "gb_ddotv_noalloc_dev", "null rho");
+    const int nparts = gb::dotv_nparts_for(n > 0 ? n : 1, sms);
+    if (nparts > GB_DOTV_NOALLOC_MAX_PARTS) {
+        char buf[160];
+        snprintf(buf, sizeof(buf), "needs %d partial sums; the allocation-free scratch holds %d",
+                 nparts, GB_DOTV_NOALLOC_MAX_PARTS);
+        return gb::set_error(GB_ERR_ARG, "gb_ddotv_noalloc_dev", buf);
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
+    return gb::ddotv_dev(n, x, incx, y, incy, rho, scratch, nparts, s);
+}

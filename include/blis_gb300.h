@@ -270,6 +270,24 @@ int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
                  gb_dim_t m, gb_dim_t n, double alpha, const double* a, gb_inc_t rs_a,
                  gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
 
+/* Allocation-free dot product (no counterpart in the reference).  For callers
+   that cannot call cudaMalloc/cudaFree -- those calls can synchronize the
+   whole device, and some host applications own a fixed device-memory budget
+   or run latency-bound loops where allocation is not allowed.  Same result as
+   gb_ddotv_dev (same partition and reduction order), but the partial-sum
+   scratch is a file-scope device array of GB_DOTV_NOALLOC_MAX_PARTS doubles
+   (16 KiB), resident on every GPU that loads the library until exit, and the
+   library's one-time initialisation (which allocates) is not used.  The first
+   call on a device, with that device current, looks up the array's device
+   address; make that first call before any stream capture.  Calls share the
+   array: calls that overlap on the GPU (unordered streams) race.  A problem
+   that would need more partial sums than the array holds is rejected with
+   GB_ERR_ARG.  x, y, rho are device pointers; stream NULL is the legacy
+   default stream. */
+#define GB_DOTV_NOALLOC_MAX_PARTS 2048
+int gb_ddotv_noalloc_dev(gb_dim_t n, const double* x, gb_inc_t incx, const double* y,
+                         gb_inc_t incy, double* rho, void* stream);
+
 /* Counterparts of the axpyv / dotv / gemv kernels (frame/1/bli_l1v_ker_params.h:61-83,
    frame/2/bli_l2_tapi.c:43-127).  gb_ddotv_dev writes rho to DEVICE memory. */
 int gb_daxpyv_dev(gb_dim_t n, double alpha, const double* x, gb_inc_t incx, double* y,
