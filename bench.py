@@ -42,6 +42,8 @@ SIZE = 16384
 SLICES = 8
 EMIN, EMAX = -20, 20
 SEED_A, SEED_B = 20261204, 20261205
+TRAFFIC_4096_BYTES = 7514446000 + 530606336  # ozaki_slice_gemm, 4096^3, 8 slices (ncu)
+TRAFFIC_SLICES = 8
 
 
 def parse():
@@ -51,7 +53,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--size", type=int, default=SIZE)
-    p.add_argument("--slices", type=int, default=SLICES)
+    p.add_argument("--slices", type=int, default=0,
+                   help="slice count of the timed form; 0 = the smallest count of the 3..8 sweep whose "
+                        "max componentwise error is at most native FP64's")
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     return p.parse_args()
@@ -207,7 +211,6 @@ def run_gpu(args):
     L = _lib.load()
     _lib.check(L.gb_init(local), "gb_init")
     n = args.size
-    s = args.slices
     flops = 2.0 * n * n * n
     peaks, peak_kind = load_peaks()
 
@@ -225,11 +228,52 @@ def run_gpu(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        barrier()
+        return e0.elapsed_time(e1)
+
+    # ---------------- double-double reference values of a fixed entry sample
+    g = torch.Generator(device="cpu").manual_seed(7)
+    ii = torch.randint(0, n, (4096,), generator=g).cuda()
+    jj = torch.randint(0, n, (4096,), generator=g).cuda()
+    hi, lo = dev.dd_gemm_entries(0, 0, 1.0, A, B, 0.0, None, ii, jj)
+
+    # ---------------- native FP64 form on the same inputs (one timed call)
+    Cn = dev.colmajor(n, n)
+    w = min(n, 2048)
+    dev.dgemm(0, 0, 1.0, A[:w, :w], B[:w, :w], 0.0, Cn[:w, :w])
+    native_ms = timed(lambda: dev.dgemm(0, 0, 1.0, A, B, 0.0, Cn))
+    native_tf = flops / (native_ms * 1e-3) / 1e12
+    err_nat = dev.componentwise_error(Cn[ii, jj], hi, lo)
+    del Cn
+
+    # ---------------- slice-count sweep: time and error of each form
+    sweep = []
+    chosen = None
+    for sl in range(3, 9):
+        dev.dgemm_ozaki(0, 0, 1.0, A, B, 0.0, Cz, sl)
+        ms_sl = timed(lambda: dev.dgemm_ozaki(0, 0, 1.0, A, B, 0.0, Cz, sl))
+        err_sl = dev.componentwise_error(Cz[ii, jj], hi, lo)
+        sweep.append({"slices": sl, "products": sl * (sl + 1) // 2, "ms": ms_sl,
+                      "tflops": flops / (ms_sl * 1e-3) / 1e12, "max_componentwise_err": err_sl})
+        if chosen is None and err_sl <= err_nat:
+            chosen = sl
+    if args.slices > 0:
+        s = args.slices
+    else:
+        s = chosen if chosen is not None else 8
+
     # ---------------- Ozaki form, device resident (value)
     for _ in range(args.warmup):
         dev.dgemm_ozaki(0, 0, 1.0, A, B, 0.0, Cz, s)
     barrier()
-    stream = torch.cuda.current_stream()
     dev.set_kernel_timing(True)
     dev.kernel_time_ms("")  # drop earlier records
     l0 = L.gb_launch_count()
@@ -247,6 +291,7 @@ def run_gpu(args):
     gemm_ms, gemm_n = dev.kernel_time_ms("ozaki_slice_gemm")
     split_ms, _ = dev.kernel_time_ms("oz_")
     dev.kernel_time_ms("")
+    err_oz = dev.componentwise_error(Cz[ii, jj], hi, lo)
     if ws > 1:
         import torch.distributed as dist
         t = torch.tensor([ms], device="cuda")
@@ -257,28 +302,6 @@ def run_gpu(args):
     kern_ms = gemm_ms / max(1, gemm_n)
     achieved = npairs * flops / (kern_ms * 1e-3) / 1e12
     peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
-
-    # ---------------- errors of both forms against double-double (sampled)
-    g = torch.Generator(device="cpu").manual_seed(7)
-    ii = torch.randint(0, n, (4096,), generator=g).cuda()
-    jj = torch.randint(0, n, (4096,), generator=g).cuda()
-    hi, lo = dev.dd_gemm_entries(0, 0, 1.0, A, B, 0.0, None, ii, jj)
-    err_oz = dev.componentwise_error(Cz[ii, jj], hi, lo)
-
-    # ---------------- native FP64 form on the same inputs (one timed call)
-    Cn = dev.colmajor(n, n)
-    w = 2048
-    dev.dgemm(0, 0, 1.0, A[:w, :w], B[:w, :w], 0.0, Cn[:w, :w])
-    barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    dev.dgemm(0, 0, 1.0, A, B, 0.0, Cn)
-    e1.record(stream)
-    barrier()
-    native_ms = e0.elapsed_time(e1)
-    native_tf = flops / (native_ms * 1e-3) / 1e12
-    err_nat = dev.componentwise_error(Cn[ii, jj], hi, lo)
-    del Cn
 
     # ---------------- end to end through dgemm_ with pinned host buffers
     Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
@@ -305,13 +328,11 @@ def run_gpu(args):
     # cn holds column-major C, i.e. cn[j, i] == C[i, j]
     e2e_ok = bool(np.array_equal(cn[:64, :64], Cz[:64, :64].t().contiguous().cpu().numpy()))
 
-    # ---------------- traffic of the dominant kernel from the committed ncu summary
-    traffic = None
-    tf_path = os.path.join(ROOT, "profiles", "ozaki_slice_gemm_traffic.json")
-    if os.path.exists(tf_path):
-        with open(tf_path) as f:
-            tinfo = json.load(f)
-        traffic = tinfo.get("bytes_per_launch_scaled", {}).get(str(n))
+    # ---------------- DRAM traffic of the dominant kernel: one ncu capture at 4096^3
+    # (dram__bytes_read.sum + dram__bytes_write.sum, profiles/ozaki_slice_gemm_4096_full.md),
+    # scaled by the slice-product units of this size, (n/4096)^3
+    # and by the slice-product count (traffic per product is the same tiling)
+    traffic = TRAFFIC_4096_BYTES * (n / 4096.0) ** 3 * npairs / (TRAFFIC_SLICES * (TRAFFIC_SLICES + 1) // 2)
 
     if rank != 0:
         if ws > 1:
@@ -339,7 +360,9 @@ def run_gpu(args):
                    "alpha": 1.0, "beta": 0.0, "form": "ozaki bf16 slices=%d (triangular, %d products)" % (s, npairs),
                    "l2": "inputs 2 GiB each, larger than the 126 MB L2", "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "forms": {
-            "ozaki": {"tflops": value / ws, "max_componentwise_err": err_oz, "slices": s},
+            "ozaki": {"tflops": value / ws, "max_componentwise_err": err_oz, "slices": s,
+                      "slice_choice": "smallest of 3..8 with error <= native" if args.slices == 0 else "fixed"},
+            "slice_sweep": sweep,
             "native_fp64": {"tflops": native_tf, "ms": native_ms, "max_componentwise_err": err_nat,
                             "engine": os.environ.get("GB_DGEMM_ENGINE", "dmma")},
             "speedup_vs_native": (value / ws) / native_tf,

@@ -54,6 +54,7 @@ constexpr uint32_t OZ_TMEM_COLS = 512;  // two 128x256 fp32 accumulators
 constexpr int OZ_SMEM_BYTES = OZ_STAGES * OZ_STAGE_BYTES + 1024 + 256;
 constexpr int OZ_CHUNK_KB = 16;  // 16 k-blocks of 64 = 1024 products per exact fp32 chunk
 constexpr int OZ_MAX_SLICES = 12;
+constexpr int OZ_GROUP_M = 16;
 
 struct OzLevel {
     int lev, npairs, pa_lo, nparts, kb_per_part, plane_base;
@@ -86,11 +87,13 @@ __device__ __forceinline__ OzItem oz_decode(const OzGemmParams& p, int64_t it)
     const int64_t rem = it - lv.item_base;
     const int part = (int)(rem / tiles);
     const int64_t t = rem % tiles;
-    // grouped raster over tiles: 8 tile rows per group for L2 reuse
-    const int64_t group = t / (8 * (int64_t)p.tiles_n);
-    const int64_t first_m = group * 8;
-    const int64_t gm = (p.tiles_m - first_m < 8) ? p.tiles_m - first_m : 8;
-    const int64_t wi = t - group * 8 * (int64_t)p.tiles_n;
+    // grouped raster over tiles, OZ_GROUP_M tile rows per group: with ~150
+    // tiles in flight, 16 rows x ~9 columns minimise L2 misses for the
+    // 16 KB A / 32 KB B per k block (misses ~ 16/cols + 32/rows)
+    const int64_t group = t / (OZ_GROUP_M * (int64_t)p.tiles_n);
+    const int64_t first_m = group * OZ_GROUP_M;
+    const int64_t gm = (p.tiles_m - first_m < OZ_GROUP_M) ? p.tiles_m - first_m : OZ_GROUP_M;
+    const int64_t wi = t - group * OZ_GROUP_M * (int64_t)p.tiles_n;
     w.tm = (int)(first_m + wi % gm);
     w.tn = (int)(wi / gm);
     w.kb0 = part * lv.kb_per_part;
@@ -357,18 +360,19 @@ __device__ __forceinline__ int clz128(unsigned __int128 u)
     return hi ? __clzll((long long)hi) : (lo ? 64 + __clzll((long long)lo) : 128);
 }
 
-// bf16 bit pattern of an integer |d| <= 256 (exact: at most 8 significant bits).
-__device__ __forceinline__ uint16_t int_to_bf16_bits(int d)
+// bf16 bit pattern of an integer |d| <= 256: the fp32 image of d has at most
+// 8 significant bits, so its upper half is exactly the bf16 value.
+__device__ __forceinline__ uint32_t int_to_bf16_bits(int d)
 {
-    if (d == 0) return 0;
-    const uint32_t sgn = d < 0 ? 0x8000u : 0u;
-    const uint32_t a = (uint32_t)(d < 0 ? -d : d);
-    const int p = 31 - __clz((int)a);                // a = 2^p * 1.f
-    const uint32_t man = (a << (7 - p)) & 0x7Fu;     // p <= 8: exact
-    return (uint16_t)(sgn | ((uint32_t)(p + 127) << 7) | man);
+    return __float_as_uint(__int2float_rn(d)) >> 16;
 }
 
-// Balanced base-256 digits of |x| 2^-e with the sign of x; integer only.
+// Balanced base-256 digits of U = |x| 2^-e (greedy, rounding to nearest,
+// ties to even) with the sign of x; 64-bit integer only.  With F = 8S+2
+// fraction bits, U 2^F = M 2^sh for the 53-bit mantissa M.  The remainder
+// is kept as R 2^z with |R| < 2^54 (its low z bits are known zeros), so every
+// digit step is a few 64-bit shifts and compares; bits below 2^-F survive
+// only as a sticky flag, which decides exact ties.
 template <int S>
 __device__ __forceinline__ void oz_digits(double x, int e, int (&d)[S])
 {
@@ -383,26 +387,38 @@ __device__ __forceinline__ void oz_digits(double x, int e, int (&d)[S])
     const int E2 = ex ? ex - 1075 : -1074;
     constexpr int F = 8 * S + 2;
     const int sh = E2 - e + F;
-    __int128 R;
+    long long R;
+    int z;
     bool sticky = false;
     if (sh >= 0) {
-        R = (__int128)((unsigned __int128)M << sh);
+        R = (long long)M;
+        z = sh;
     } else if (sh > -64) {
-        R = (__int128)(M >> (-sh));
+        R = (long long)(M >> (-sh));
         sticky = (M & ((1ull << (-sh)) - 1)) != 0;
+        z = 0;
     } else {
         R = 0;
         sticky = true;
+        z = 0;
     }
 #pragma unroll
     for (int p = 1; p <= S; ++p) {
-        const int w = F - 8 * p;
-        const __int128 q = R >> w;
-        const __int128 rem = R - (q << w);
-        const __int128 half = ((__int128)1) << (w - 1);
-        __int128 dg = q;
-        if (rem > half || (rem == half && (sticky || (q & 1)))) dg = q + 1;
-        R -= dg << w;
+        const int dz = (F - 8 * p) - z;  // digit weight relative to the remainder's scale
+        long long dg;
+        if (dz <= 0) {
+            dg = R * (1ll << (-dz));  // exact multiple of the digit unit (|dg| <= 128)
+            R = 0;
+        } else if (dz >= 62) {
+            dg = 0;  // |R| < 2^54 is far below half a digit unit
+        } else {
+            const long long q = R >> dz;  // floor
+            const long long rem = R - q * (1ll << dz);
+            const long long half = 1ll << (dz - 1);
+            dg = q;
+            if (rem > half || (rem == half && (sticky || (q & 1)))) dg = q + 1;
+            R -= dg * (1ll << dz);
+        }
         d[p - 1] = neg ? -(int)dg : (int)dg;
     }
 }
@@ -477,7 +493,22 @@ __device__ __forceinline__ double round_scaled(__int128 T, int E)
     const int msb = 127 - clz128(u);
     const int lead = msb + E;
     unsigned long long bits;
-    if (lead > 1023) {
+    if (lead >= -1022 && lead <= 1023) {
+        // normal result: take the 64 bits below the leading one, round at bit 11
+        unsigned long long top;
+        bool rest = false;
+        if (msb >= 63) {
+            top = (unsigned long long)(u >> (msb - 63));
+            rest = (msb > 63) && ((u & ((((unsigned __int128)1) << (msb - 63)) - 1)) != 0);
+        } else {
+            top = (unsigned long long)u << (63 - msb);
+        }
+        unsigned long long q = top >> 11;
+        const unsigned long long rb = top & 0x7FFull;
+        if (rb > 0x400ull || (rb == 0x400ull && (rest || (q & 1ull)))) q += 1;
+        bits = ((unsigned long long)(lead + 1022) << 52) + q;  // q in [2^52, 2^53]
+        if (bits >= 0x7FF0000000000000ull) bits = 0x7FF0000000000000ull;
+    } else if (lead > 1023) {
         bits = 0x7FF0000000000000ull;
     } else {
         const int lsb = (lead >= -1022) ? lead - 52 : -1074;
@@ -525,13 +556,17 @@ __global__ void oz_recombine_kernel(const __grid_constant__ OzRecombParams p)
          e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = i_fast ? e % p.m : e / p.n;
         const int64_t j = i_fast ? e / p.m : e % p.n;
+        // Horner from the most significant level (l = 2, last in the table):
+        // T = sum_l S_l 2^(8(s+1-l)) with constant 8-bit shifts
+        const int64_t off = j * p.mpad + i;
+        const int64_t plane_stride = p.npad * p.mpad;
         __int128 T = 0;
-        for (int L = 0; L < p.nlevels; ++L) {
+        for (int L = p.nlevels - 1; L >= 0; --L) {
             const OzLevel& lv = p.lv[L];
-            long long s = 0;
-            for (int pt = 0; pt < lv.nparts; ++pt)
-                s += __ldcs(p.planes + ((int64_t)(lv.plane_base + pt) * p.npad + j) * p.mpad + i);
-            T += ((__int128)s) << (8 * (p.slices + 1 - lv.lev));
+            long long s = __ldcs(p.planes + (int64_t)lv.plane_base * plane_stride + off);
+            for (int pt = 1; pt < lv.nparts; ++pt)
+                s += __ldcs(p.planes + (int64_t)(lv.plane_base + pt) * plane_stride + off);
+            T = (T << 8) + (__int128)s;
         }
         const double ab = round_scaled(T, p.ea[i] + p.eb[j] - 8 * (p.slices + 1));
         double* cij = p.c + i * p.rs_c + j * p.cs_c;
