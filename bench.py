@@ -6,9 +6,12 @@ C := A*B with m = n = k = 16384, column-major FP64, entries (1+u)*2^e with
 e uniform in [-20, 20] and random sign, generated on the device by the
 library's seeded generator.  A "step" is one full DGEMM.
 
-  value      Ozaki DGEMM (8 bf16 slices, tcgen05) in FP64-equivalent
+  value      Ozaki DGEMM (bf16 slices on tcgen05) in FP64-equivalent
              TFLOP/s (2mnk per step), operands resident in HBM, CUDA events
-             on the launching stream, K steps after W warm-up steps.
+             on the launching stream, K steps after W warm-up steps.  The
+             slice count is the smallest of a 3..8 sweep whose max
+             componentwise error is at most native FP64 DGEMM's on the same
+             inputs (--slices fixes it instead).
   e2e        the same DGEMM through the BLAS entry point dgemm_ (C ABI) on
              pinned host buffers: H2D of A and B and D2H of C inside the
              timed region of every step.
@@ -289,7 +292,9 @@ def run_gpu(args):
     dev.set_kernel_timing(False)
     ms = ev0.elapsed_time(ev1) / args.steps
     gemm_ms, gemm_n = dev.kernel_time_ms("ozaki_slice_gemm")
-    split_ms, _ = dev.kernel_time_ms("oz_")
+    stage_ms = {nm: dev.kernel_time_ms(nm)[0] / max(1, args.steps)
+                for nm in ("oz_rowmax", "oz_split", "oz_recombine", "dgemm_dmma_gated")}
+    split_ms = sum(stage_ms.values()) * max(1, args.steps)
     dev.kernel_time_ms("")
     err_oz = dev.componentwise_error(Cz[ii, jj], hi, lo)
     if ws > 1:
@@ -376,7 +381,8 @@ def run_gpu(args):
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "%s bf16_tflops_sustained" % peak_kind,
                      "kernel_ms": kern_ms, "algorithmic_flops_per_launch": npairs * flops,
-                     "split_recombine_ms_per_step": (split_ms / max(1, args.steps))},
+                     "split_recombine_ms_per_step": (split_ms / max(1, args.steps)),
+                     "stage_ms_per_step": stage_ms},
         "cpu_baseline": {"value": cpu_tf, "unit": "TFLOP/s", "cores": threads, "kind": "port", "sample": cpu_sample},
         "gpu_launches": launches,
         "clocks": clk.summary(),

@@ -10,8 +10,9 @@
 //     op(B)^T gets e = ilogb(row max) + 2, so U = |x| 2^-e < 1/2, and is cut
 //     into s balanced base-256 digits of the exact value U (greedy, rounding
 //     to nearest, ties to even), |d| <= 128, each exact in bf16.  The digits
-//     come from a 128-bit fixed-point image of the mantissa.  Slices are
-//     stored K-major: s planes of [rows_pad][K_pad] bf16, zero padded.
+//     come from the 53-bit mantissa with 64-bit shifts (a sticky flag keeps
+//     the bits below the last digit for exact ties).  Slices are stored
+//     K-major: s planes of [rows_pad][K_pad] bf16, zero padded.
 //  2. ozaki_slice_gemm: a persistent tcgen05 kernel computes the integer
 //     level sums S_l = sum_{p+q=l} A_p B_q^T, l = 2..s+1 (the triangular
 //     set, s(s+1)/2 slice products).  Tiles arrive by TMA (128B swizzle)
@@ -546,36 +547,72 @@ struct OzRecombParams {
     OzLevel lv[OZ_MAX_SLICES];
 };
 
-__global__ void oz_recombine_kernel(const __grid_constant__ OzRecombParams p)
+// Thread per 4 consecutive rows of one column: all S level planes are
+// loaded up front as 16-byte vectors (S x 16 B in flight per thread), then
+// T = sum_l S_l 2^(8(s+1-l)) is formed by Horner from the most significant
+// level (l = 2, last in the table) and rounded once.
+template <int S>
+__global__ void __launch_bounds__(256) oz_recombine_kernel(const __grid_constant__ OzRecombParams p)
 {
     if (*p.skip) return;
-    const int64_t total = p.m * p.n;
-    const bool i_fast = (p.rs_c == 1 || p.cs_c != 1);
+    const int64_t mq = (p.m + 3) >> 2;
+    const int64_t total = mq * p.n;
     const bool plain = (p.alpha == 1.0 && p.beta == 0.0);
+    const int64_t plane_stride = p.npad * p.mpad;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = i_fast ? e % p.m : e / p.n;
-        const int64_t j = i_fast ? e / p.m : e % p.n;
-        // Horner from the most significant level (l = 2, last in the table):
-        // T = sum_l S_l 2^(8(s+1-l)) with constant 8-bit shifts
-        const int64_t off = j * p.mpad + i;
-        const int64_t plane_stride = p.npad * p.mpad;
-        __int128 T = 0;
-        for (int L = p.nlevels - 1; L >= 0; --L) {
-            const OzLevel& lv = p.lv[L];
-            long long s = __ldcs(p.planes + (int64_t)lv.plane_base * plane_stride + off);
-            for (int pt = 1; pt < lv.nparts; ++pt)
-                s += __ldcs(p.planes + (int64_t)(lv.plane_base + pt) * plane_stride + off);
-            T = (T << 8) + (__int128)s;
+        const int64_t j = e / mq, i0 = (e - j * mq) * 4;
+        const int64_t off = j * p.mpad + i0;  // mpad is a multiple of 128: 16-byte aligned
+        int4 v[S];
+#pragma unroll
+        for (int L = 0; L < S; ++L)
+            v[L] = __ldcs(reinterpret_cast<const int4*>(p.planes + (int64_t)p.lv[L].plane_base * plane_stride + off));
+        long long acc[S][4];
+#pragma unroll
+        for (int L = 0; L < S; ++L) {
+            acc[L][0] = v[L].x;
+            acc[L][1] = v[L].y;
+            acc[L][2] = v[L].z;
+            acc[L][3] = v[L].w;
+            for (int pt = 1; pt < p.lv[L].nparts; ++pt) {
+                const int4 w = __ldcs(reinterpret_cast<const int4*>(
+                    p.planes + (int64_t)(p.lv[L].plane_base + pt) * plane_stride + off));
+                acc[L][0] += w.x;
+                acc[L][1] += w.y;
+                acc[L][2] += w.z;
+                acc[L][3] += w.w;
+            }
         }
-        const double ab = round_scaled(T, p.ea[i] + p.eb[j] - 8 * (p.slices + 1));
-        double* cij = p.c + i * p.rs_c + j * p.cs_c;
-        if (plain) {
-            *cij = ab;
-        } else {
-            const double t = __dmul_rn(p.alpha, ab);
-            *cij = (p.beta == 0.0) ? t : __fma_rn(p.beta, *cij, t);
+        const int ebj = p.eb[j] - 8 * (S + 1);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int64_t i = i0 + r;
+            if (i >= p.m) break;
+            __int128 T = 0;
+#pragma unroll
+            for (int L = S - 1; L >= 0; --L) T = (T << 8) + (__int128)acc[L][r];
+            const double ab = round_scaled(T, p.ea[i] + ebj);
+            double* cij = p.c + i * p.rs_c + j * p.cs_c;
+            if (plain) {
+                *cij = ab;
+            } else {
+                const double t = __dmul_rn(p.alpha, ab);
+                *cij = (p.beta == 0.0) ? t : __fma_rn(p.beta, *cij, t);
+            }
         }
+    }
+}
+
+void launch_recombine(int slices, const OzRecombParams& r, unsigned blocks, cudaStream_t s)
+{
+    switch (slices) {
+#define GB_RECOMB_CASE(S) \
+    case S: oz_recombine_kernel<S><<<blocks, 256, 0, s>>>(r); break;
+        GB_RECOMB_CASE(2) GB_RECOMB_CASE(3) GB_RECOMB_CASE(4) GB_RECOMB_CASE(5) GB_RECOMB_CASE(6)
+        GB_RECOMB_CASE(7) GB_RECOMB_CASE(8) GB_RECOMB_CASE(9) GB_RECOMB_CASE(10) GB_RECOMB_CASE(11)
+        GB_RECOMB_CASE(12)
+#undef GB_RECOMB_CASE
+    default: break;
     }
 }
 
@@ -803,11 +840,11 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
         r.cs_c = cs_c;
         r.skip = nonfinite;
         for (int L = 0; L < slices; ++L) r.lv[L] = p.lv[L];
-        const int64_t total = m * n;
+        const int64_t total = ((m + 3) / 4) * n;
         int64_t blocks = (total + 255) / 256;
-        if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
+        if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
         LaunchScope ls("oz_recombine", s);
-        oz_recombine_kernel<<<(unsigned)blocks, 256, 0, s>>>(r);
+        launch_recombine(slices, r, (unsigned)blocks, s);
     }
     if ((rc = check_cuda(cudaGetLastError(), "oz_recombine"))) return bail(rc);
     // IEEE path for non-finite operands: runs only when the split raised the flag

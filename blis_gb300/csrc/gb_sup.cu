@@ -1,0 +1,267 @@
+// gb_sup.cu -- small / skinny GEMM (the gemmsup path) and the
+// configuration-explicit GEMM entry used by the autotuner and selector.
+//
+// BLIS sends problems with a dimension below its sup thresholds
+// (frame/base/bli_cntx.h:186-193, MT/NT/KT = 201 on haswell) to unpacked
+// kernels (frame/3/bli_l3_sup.c:37-131, bli_l3_sup_var1n2m.c) because the
+// packing and the large MC/NC blocking of the conventional path do not pay
+// off there.  On the GPU the analogous waste is idle SMs: a 300 x 300 C has
+// only 9 tiles of 128 x 128.  This engine uses 64 x 64 tiles (4 warps) and an
+// optional split of K across blockIdx.z; split partial sums go to a
+// workspace and a second kernel folds them in fixed order, so results are
+// deterministic.  The same config space covers FP64 (DMMA m8n8k4) and FP32
+// (FMA):
+//   config 0      the 128 x 128 engine of gb_dgemm.cu
+//   config 1..5   64 x 64 tiles with a K split of 1, 2, 4, 8, 16
+#include "gb_internal.h"
+
+namespace gb {
+namespace {
+
+constexpr int SBM = 64, SBN = 64, SBK = 16, SNT = 128;
+constexpr int SLDS = SBM + 8;
+
+template <typename T>
+struct SupArgs {
+    int64_t m, n, k, kchunk;
+    T alpha, beta;
+    const T* a;
+    int64_t ars, acs;
+    const T* b;
+    int64_t brs, bcs;
+    T* c;
+    int64_t rs_c, cs_c;
+    T* ws;  // split partial sums [split][n][m], or nullptr when not split
+};
+
+template <typename T>
+__device__ __forceinline__ void sup_load(const SupArgs<T>& p, int64_t bm, int64_t bn, int64_t k0, int64_t k1,
+                                         T (&ra)[8], T (&rb)[8])
+{
+    const int tid = threadIdx.x;
+    const bool a_rows_fast = (p.ars == 1);
+    const bool b_k_fast = (p.brs == 1);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int e = tid + SNT * r;
+        int i, l;
+        if (a_rows_fast) { i = e % SBM; l = e / SBM; } else { i = e / SBK; l = e % SBK; }
+        const int64_t gi = bm + i, gl = k0 + l;
+        ra[r] = (gi < p.m && gl < k1) ? __ldg(p.a + gi * p.ars + gl * p.acs) : T(0);
+        int j;
+        if (b_k_fast) { l = e % SBK; j = e / SBK; } else { j = e % SBN; l = e / SBN; }
+        const int64_t gj = bn + j, gl2 = k0 + l;
+        rb[r] = (gj < p.n && gl2 < k1) ? __ldg(p.b + gl2 * p.brs + gj * p.bcs) : T(0);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void sup_store(const SupArgs<T>& p, T (&ra)[8], T (&rb)[8], T* As, T* Bs)
+{
+    const int tid = threadIdx.x;
+    const bool a_rows_fast = (p.ars == 1);
+    const bool b_k_fast = (p.brs == 1);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int e = tid + SNT * r;
+        int i, l;
+        if (a_rows_fast) { i = e % SBM; l = e / SBM; } else { i = e / SBK; l = e % SBK; }
+        As[l * SLDS + i] = ra[r];
+        int j;
+        if (b_k_fast) { l = e % SBK; j = e / SBK; } else { j = e % SBN; l = e / SBN; }
+        Bs[l * SLDS + j] = rb[r];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void sup_out(const SupArgs<T>& p, int64_t i, int64_t j, T ab)
+{
+    if (i >= p.m || j >= p.n) return;
+    if (p.ws) {
+        p.ws[((int64_t)blockIdx.z * p.n + j) * p.m + i] = ab;
+    } else {
+        T* cij = p.c + i * p.rs_c + j * p.cs_c;
+        const T t = p.alpha * ab;
+        *cij = (p.beta == T(0)) ? t : fma(p.beta, *cij, t);
+    }
+}
+
+__device__ __forceinline__ void dmma(double& d0, double& d1, double a, double b)
+{
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                 : "+d"(d0), "+d"(d1)
+                 : "d"(a), "d"(b));
+}
+
+// FP64: 2 x 2 warps of 32 x 32, DMMA.  FP32: 16 x 8 threads of 4 x 8, FMA.
+template <typename T>
+__global__ void __launch_bounds__(SNT) sup_gemm_kernel(SupArgs<T> p)
+{
+    __shared__ T As[SBK * SLDS];
+    __shared__ T Bs[SBK * SLDS];
+    const int64_t bm = (int64_t)blockIdx.y * SBM, bn = (int64_t)blockIdx.x * SBN;
+    const int64_t k0 = (int64_t)blockIdx.z * p.kchunk;
+    const int64_t k1 = (k0 + p.kchunk < p.k) ? k0 + p.kchunk : p.k;
+    T ra[8], rb[8];
+    if constexpr (sizeof(T) == 8) {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int wm = warp & 1, wn = warp >> 1;
+        double acc[4][4][2];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+        sup_load(p, bm, bn, k0, k1, ra, rb);
+        for (int64_t kk0 = k0; kk0 < k1; kk0 += SBK) {
+            __syncthreads();
+            sup_store(p, ra, rb, As, Bs);
+            __syncthreads();
+            if (kk0 + SBK < k1) sup_load(p, bm, bn, kk0 + SBK, k1, ra, rb);
+#pragma unroll
+            for (int kk = 0; kk < SBK; kk += 4) {
+                const int kr = kk + (lane & 3);
+                double af[4], bf[4];
+#pragma unroll
+                for (int mi = 0; mi < 4; ++mi) af[mi] = As[kr * SLDS + wm * 32 + mi * 8 + (lane >> 2)];
+#pragma unroll
+                for (int ni = 0; ni < 4; ++ni) bf[ni] = Bs[kr * SLDS + wn * 32 + ni * 8 + (lane >> 2)];
+#pragma unroll
+                for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+                    for (int ni = 0; ni < 4; ++ni) dmma(acc[mi][ni][0], acc[mi][ni][1], af[mi], bf[ni]);
+            }
+        }
+#pragma unroll
+        for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+            for (int ni = 0; ni < 4; ++ni) {
+                const int64_t i = bm + wm * 32 + mi * 8 + (lane >> 2);
+                const int64_t j = bn + wn * 32 + ni * 8 + 2 * (lane & 3);
+                sup_out(p, i, j, (T)acc[mi][ni][0]);
+                sup_out(p, i, j + 1, (T)acc[mi][ni][1]);
+            }
+    } else {
+        const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;  // 8 x 16 threads
+        T acc[4][8];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[i][j] = T(0);
+        sup_load(p, bm, bn, k0, k1, ra, rb);
+        for (int64_t kk0 = k0; kk0 < k1; kk0 += SBK) {
+            __syncthreads();
+            sup_store(p, ra, rb, As, Bs);
+            __syncthreads();
+            if (kk0 + SBK < k1) sup_load(p, bm, bn, kk0 + SBK, k1, ra, rb);
+#pragma unroll
+            for (int kk = 0; kk < SBK; ++kk) {
+                T av[4], bv[8];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) av[i] = As[kk * SLDS + ty * 4 + i];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) bv[j] = Bs[kk * SLDS + tx * 8 + j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) sup_out(p, bm + ty * 4 + i, bn + tx * 8 + j, acc[i][j]);
+    }
+}
+
+// c = alpha * sum_z ws[z] (+ beta c), z in increasing order.
+template <typename T>
+__global__ void sup_fold_kernel(int64_t m, int64_t n, int splits, const T* __restrict__ ws, T alpha, T beta,
+                                T* __restrict__ c, int64_t rs_c, int64_t cs_c)
+{
+    const int64_t total = m * n;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e % m, j = e / m;
+        T acc = ws[e];
+        for (int z = 1; z < splits; ++z) acc += ws[(int64_t)z * total + e];
+        T* cij = c + i * rs_c + j * cs_c;
+        const T t = alpha * acc;
+        *cij = (beta == T(0)) ? t : fma(beta, *cij, t);
+    }
+}
+
+template <typename T>
+int sup_gemm(int splits, int64_t m, int64_t n, int64_t k, T alpha, const T* a, int64_t ars, int64_t acs,
+             const T* b, int64_t brs, int64_t bcs, T beta, T* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
+{
+    int64_t kchunk = (k + splits - 1) / splits;
+    kchunk = (kchunk + SBK - 1) / SBK * SBK;
+    const int sz = (int)((k + kchunk - 1) / kchunk);  // splits actually used
+    const int64_t gx = (n + SBN - 1) / SBN, gy = (m + SBM - 1) / SBM;
+    if (gy > 65535 || sz > 65535) return set_error(GB_ERR_ARG, "gemm_sup", "grid too large");
+    T* ws = nullptr;
+    if (sz > 1) {
+        ws = static_cast<T*>(dev_alloc(sizeof(T) * (size_t)sz * m * n, s));
+        if (!ws) return GB_ERR_NOMEM;
+    }
+    SupArgs<T> p{m, n, k, kchunk, alpha, beta, a, ars, acs, b, brs, bcs, c, rs_c, cs_c, ws};
+    {
+        LaunchScope ls(sizeof(T) == 8 ? "sup_dmma" : "sup_ffma", s);
+        sup_gemm_kernel<T><<<dim3((unsigned)gx, (unsigned)gy, (unsigned)sz), SNT, 0, s>>>(p);
+    }
+    int rc = check_cuda(cudaGetLastError(), "gemm_sup");
+    if (!rc && sz > 1) {
+        int64_t blocks = (m * n + 255) / 256;
+        const int64_t cap = (int64_t)(sm_count() > 0 ? sm_count() : 148) * 8;
+        if (blocks > cap) blocks = cap;
+        LaunchScope ls("sup_fold", s);
+        sup_fold_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(m, n, sz, ws, alpha, beta, c, rs_c, cs_c);
+        rc = check_cuda(cudaGetLastError(), "sup_fold");
+    }
+    dev_free(ws, s);
+    return rc;
+}
+
+}  // namespace
+
+int gemm_config_dev(int dtype, int config, int64_t m, int64_t n, int64_t k, double alpha,
+                    const void* a, int64_t ars, int64_t acs, const void* b, int64_t brs, int64_t bcs,
+                    double beta, void* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
+{
+    if (config < 0 || config >= GB_GEMM_NUM_CONFIGS) return set_error(GB_ERR_ARG, "gemm_config", "unknown config");
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    if (alpha == 0.0 || k <= 0) {
+        if (dtype == 0) return scal_matrix(m, n, beta, (double*)c, rs_c, cs_c, s);
+        return scal_matrix_f(m, n, (float)beta, (float*)c, rs_c, cs_c, s);
+    }
+    if (config == 0) {
+        if (dtype == 0)
+            return dgemm_native(m, n, k, alpha, (const double*)a, ars, acs, (const double*)b, brs, bcs, beta,
+                                (double*)c, rs_c, cs_c, s);
+        return sgemm_dev(m, n, k, (float)alpha, (const float*)a, ars, acs, (const float*)b, brs, bcs, (float)beta,
+                         (float*)c, rs_c, cs_c, s);
+    }
+    const int splits = 1 << (config - 1);
+    if (dtype == 0)
+        return sup_gemm<double>(splits, m, n, k, alpha, (const double*)a, ars, acs, (const double*)b, brs, bcs,
+                                beta, (double*)c, rs_c, cs_c, s);
+    return sup_gemm<float>(splits, m, n, k, (float)alpha, (const float*)a, ars, acs, (const float*)b, brs, bcs,
+                           (float)beta, (float*)c, rs_c, cs_c, s);
+}
+
+}  // namespace gb
+
+extern "C" int gb_gemm_config_dev(int dtype, int config, gb_trans_t transa, gb_trans_t transb, gb_dim_t m,
+                                  gb_dim_t n, gb_dim_t k, double alpha, const void* a, gb_inc_t rs_a,
+                                  gb_inc_t cs_a, const void* b, gb_inc_t rs_b, gb_inc_t cs_b, double beta,
+                                  void* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (dtype != 0 && dtype != 1) return gb::set_error(GB_ERR_ARG, "gb_gemm_config_dev", "dtype must be 0 or 1");
+    if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_gemm_config_dev", "negative dimension");
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : gb::thread_stream();
+    return gb::gemm_config_dev(dtype, config, m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b,
+                               tb ? cs_b : rs_b, tb ? rs_b : cs_b, beta, c, rs_c, cs_c, s);
+}
