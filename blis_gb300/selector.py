@@ -1,0 +1,410 @@
+"""Autotuner and learned configuration selector.
+
+BLIS chooses its kernels from static per-architecture tables and a fixed
+small-problem rule (sup thresholds MT/NT/KT, frame/base/bli_cntx.h:186-193,
+201/201/201 on haswell, config/haswell/bli_cntx_init_haswell.c:214-216).
+Here the choice is learned:
+
+* the autotuner times every GEMM configuration of the library
+  (gb_gemm_config_dev: 128x128 tiles, or 64x64 tiles with K split 1..16)
+  on seeded shapes and records the time of each;
+* the slice-count label of an FP64 shape comes from the error-bound verifier
+  (gb_ozaki_verify_slices_dev) run on synthetic operands with the shape's
+  exponent spread;
+* a 16-64-64-64-8 GELU MLP (gb_mlp.cu: forward, backward and Adam are CUDA
+  kernels of this library) is trained to predict the log-time of every
+  configuration and the slice count;
+* selection takes the configuration of least predicted time; a proposed
+  slice count is checked by the verifier and raised if it fails.
+
+The exhaustive table stays the fallback and the judge: `evaluate` reports
+the throughput regret of the MLP's choices against the measured best, and
+of the threshold rule for comparison.
+
+Usage (on a GPU machine):
+  python -m blis_gb300.selector tune  --count 10000 --seed 1 --out tune.npz
+  python -m blis_gb300.selector train --data tune.npz --out selector_mlp.json
+  python -m blis_gb300.selector eval  --model selector_mlp.json --data heldout.npz
+"""
+import argparse
+import ctypes as C
+import hashlib
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import _lib
+
+NIN, NH, NOUT = 16, 64, 8
+NPARAMS = 9928
+CONFIG_NAMES = ["tile128", "tile64", "tile64_k2", "tile64_k4", "tile64_k8", "tile64_k16"]
+NCONFIG = len(CONFIG_NAMES)
+OUT_SLICES = 6
+DTYPES = {"fp64": 0, "fp32": 1}
+PADS = (0, 8, 64)
+SCHEMA = "gb300-selector-mlp/1"
+TIME_SCALE = 10.0  # target = log2(time in microseconds) / TIME_SCALE
+WORK_CAP = 2.0 ** 35  # shapes above this many flops are not timed (config 0 is used)
+ELEM_CAP = 2 ** 28    # largest operand, in elements
+
+
+# ------------------------------------------------------------------ features
+def features(m, n, k, dtype, ta, tb, pad, spread_a, spread_b):
+    f = np.zeros(NIN, dtype=np.float32)
+    f[0] = math.log2(m + 1) / 15.0
+    f[1] = math.log2(n + 1) / 15.0
+    f[2] = math.log2(k + 1) / 15.0
+    f[3 + {0: 0, 1: 1, 2: 2}[dtype]] = 1.0
+    f[6] = float(ta)
+    f[7] = float(tb)
+    f[8 + PADS.index(pad)] = 1.0
+    f[11] = spread_a / 40.0
+    f[12] = spread_b / 40.0
+    f[13] = math.log2(m * n + 1) / 30.0
+    f[14] = math.log2(m * n * k + 1) / 45.0
+    f[15] = 1.0 if min(m, n) <= 64 else 0.0
+    return f
+
+
+def exponent_spread(t, nsample=4096, seed=0):
+    """Half the range of binary exponents over a sample of nonzero entries
+    of a CUDA tensor: ~E for entries (1+u) 2^e with e in [-E, E]."""
+    import torch
+    flat = t.reshape(-1) if t.is_contiguous() else t.t().reshape(-1)
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    idx = torch.randint(0, flat.numel(), (min(nsample, flat.numel()),), generator=g).to(flat.device)
+    v = flat[idx].abs()
+    v = v[v > 0]
+    if v.numel() == 0:
+        return 0.0
+    _, e = torch.frexp(v.double())
+    return float((e.max() - e.min()).item()) / 2.0
+
+
+def heuristic_config(m, n, k):
+    """BLIS-style rule: the small/skinny engine below the sup thresholds."""
+    return 0 if min(m, n, k) >= 201 else 1
+
+
+# ------------------------------------------------------------------ shapes
+def sample_shapes(count, seed, dtypes=("fp64", "fp32")):
+    """m, n, k log-uniform integers in [1, 32768], random transposes and
+    leading-dimension padding, exponent spread E uniform in {0..20};
+    shapes above WORK_CAP flops or ELEM_CAP operand elements are redrawn."""
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < count:
+        m, n, k = (int(round(math.exp(rng.uniform(0.0, math.log(32768.0))))) for _ in range(3))
+        if 2.0 * m * n * k > WORK_CAP or max(m * k, k * n, m * n) > ELEM_CAP:
+            continue
+        dt = dtypes[len(out) % len(dtypes)]
+        out.append({"m": m, "n": n, "k": k, "dtype": DTYPES[dt], "ta": int(rng.integers(2)),
+                    "tb": int(rng.integers(2)), "pad": int(PADS[rng.integers(3)]),
+                    "ea": int(rng.integers(0, 21)), "eb": int(rng.integers(0, 21))})
+    return out
+
+
+# ------------------------------------------------------------------ autotuner
+class Autotuner:
+    """Times gb_gemm_config_dev for every configuration with CUDA events."""
+
+    def __init__(self, max_elems=ELEM_CAP):
+        import torch
+        self.torch = torch
+        self.L = _lib.load()
+        self.L.gb_gemm_config_dev.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int64,
+                                              C.c_int64, C.c_double, C.c_void_p, C.c_int64, C.c_int64,
+                                              C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.c_void_p,
+                                              C.c_int64, C.c_int64, C.c_void_p]
+        self.buf = {}
+        for dt, tdt in ((0, torch.float64), (1, torch.float32)):
+            a = torch.empty(max_elems + 64 * 32768, dtype=tdt, device="cuda").uniform_(-1, 1)
+            b = torch.empty(max_elems + 64 * 32768, dtype=tdt, device="cuda").uniform_(-1, 1)
+            c = torch.zeros(max_elems + 64 * 32768, dtype=tdt, device="cuda")
+            self.buf[dt] = (a, b, c)
+        self.stream = C.c_void_p(torch.cuda.current_stream().cuda_stream or 1)
+
+    def _call(self, sh, config):
+        a, b, c = self.buf[sh["dtype"]]
+        m, n, k, pad = sh["m"], sh["n"], sh["k"], sh["pad"]
+        ra, rb = (k if sh["ta"] else m), (n if sh["tb"] else k)
+        rc = self.L.gb_gemm_config_dev(sh["dtype"], config, 8 if sh["ta"] else 0, 8 if sh["tb"] else 0, m, n, k,
+                                       1.0, a.data_ptr(), 1, ra + pad, b.data_ptr(), 1, rb + pad, 0.0,
+                                       c.data_ptr(), 1, m + pad, self.stream)
+        if rc != 0:
+            raise RuntimeError("gb_gemm_config_dev: %s" % (_lib.last_error(),))
+
+    def time_us(self, sh, config, reps=None):
+        torch = self.torch
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        self._call(sh, config)  # warm-up (workspace from the pool, caches)
+        e0.record()
+        self._call(sh, config)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) * 1e3
+        if reps is None:
+            reps = 3 if t < 2000.0 else 1
+        if reps > 1:
+            e0.record()
+            for _ in range(reps):
+                self._call(sh, config)
+            e1.record()
+            e1.synchronize()
+            t = e0.elapsed_time(e1) * 1e3 / reps
+        return t
+
+    def tune(self, sh):
+        return [self.time_us(sh, cfg) for cfg in range(NCONFIG)]
+
+
+def slice_label(sh, seed=0):
+    """Smallest slice count meeting the verifier's bound for operands with
+    the shape's exponent spreads (synthetic (1+u) 2^e entries)."""
+    import torch
+    from . import dev
+    m, n, k = min(sh["m"], 512), min(sh["n"], 512), sh["k"]
+    a = dev.colmajor(m, k)
+    b = dev.colmajor(k, n)
+    dev.randm(a, dev.RAND_EXPSPREAD, 1000 + seed, -sh["ea"], sh["ea"])
+    dev.randm(b, dev.RAND_EXPSPREAD, 2000 + seed, -sh["eb"], sh["eb"])
+    s = C.c_int(0)
+    L = _lib.load()
+    L.gb_ozaki_verify_slices_dev.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_void_p,
+                                             C.c_int64, C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_int,
+                                             C.c_int, C.POINTER(C.c_int), C.c_void_p]
+    rc = L.gb_ozaki_verify_slices_dev(0, 0, m, n, k, a.data_ptr(), a.stride(0), a.stride(1), b.data_ptr(),
+                                      b.stride(0), b.stride(1), 2, 256, C.byref(s), None)
+    if rc != 0:
+        raise RuntimeError("verifier: %s" % (_lib.last_error(),))
+    sa = exponent_spread(a, seed=seed)
+    sb = exponent_spread(b, seed=seed + 1)
+    del torch
+    return s.value, sa, sb
+
+
+def build_dataset(shapes, log_every=0):
+    tuner = Autotuner()
+    X = np.zeros((len(shapes), NIN), np.float32)
+    Y = np.zeros((len(shapes), NOUT), np.float32)
+    M = np.zeros((len(shapes), NOUT), np.float32)
+    T = np.zeros((len(shapes), NCONFIG), np.float64)
+    S = np.zeros(len(shapes), np.int32)
+    t0 = time.time()
+    for i, sh in enumerate(shapes):
+        times = tuner.tune(sh)
+        T[i] = times
+        if sh["dtype"] == 0:
+            s, sa, sb = slice_label(sh, seed=i)
+        else:
+            s, sa, sb = 0, float(sh["ea"]), float(sh["eb"])
+        S[i] = s
+        X[i] = features(sh["m"], sh["n"], sh["k"], sh["dtype"], sh["ta"], sh["tb"], sh["pad"], sa, sb)
+        Y[i, :NCONFIG] = np.log2(np.asarray(times)) / TIME_SCALE
+        M[i, :NCONFIG] = 1.0
+        if sh["dtype"] == 0:
+            Y[i, OUT_SLICES] = s / 12.0
+            M[i, OUT_SLICES] = 1.0
+        if log_every and (i + 1) % log_every == 0:
+            print("tuned %d/%d shapes in %.1f s" % (i + 1, len(shapes), time.time() - t0), flush=True)
+    return {"X": X, "Y": Y, "M": M, "T": T, "S": S,
+            "shapes": np.array([[s["m"], s["n"], s["k"], s["dtype"], s["ta"], s["tb"], s["pad"], s["ea"], s["eb"]]
+                                for s in shapes], np.int64)}
+
+
+# ------------------------------------------------------------------ model
+def init_params(seed=0):
+    rng = np.random.default_rng(seed)
+    parts = []
+    for fan_out, fan_in in ((NH, NIN), (NH, NH), (NH, NH), (NOUT, NH)):
+        parts.append(rng.normal(0.0, math.sqrt(2.0 / fan_in), size=(fan_out, fan_in)).ravel())
+        parts.append(np.zeros(fan_out))
+    p = np.concatenate(parts).astype(np.float32)
+    assert p.size == NPARAMS
+    return p
+
+
+class GpuMlp:
+    """Training and inference through the library's CUDA kernels."""
+
+    def __init__(self, params):
+        import torch
+        self.torch = torch
+        self.L = _lib.load()
+        L = self.L
+        L.gb_mlp_forward_dev.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        L.gb_mlp_loss_grad_dev.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
+                                           C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gb_mlp_adam_dev.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
+                                      C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p]
+        self.p = torch.from_numpy(np.asarray(params, np.float32).copy()).cuda()
+        self.g = torch.zeros_like(self.p)
+        self.m = torch.zeros_like(self.p)
+        self.v = torch.zeros_like(self.p)
+        self.loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+        self.step = 0
+
+    def _s(self):
+        return C.c_void_p(self.torch.cuda.current_stream().cuda_stream or 1)
+
+    def forward(self, x):
+        torch = self.torch
+        x = torch.as_tensor(np.asarray(x, np.float32)).cuda().contiguous()
+        out = torch.empty((x.shape[0], NOUT), dtype=torch.float32, device="cuda")
+        _lib.check(self.L.gb_mlp_forward_dev(self.p.data_ptr(), x.data_ptr(), x.shape[0], out.data_ptr(), self._s()),
+                   "gb_mlp_forward_dev")
+        return out.cpu().numpy()
+
+    def loss_grad(self, x, y, mask, norm=None):
+        """x, y, mask: CUDA float32 tensors."""
+        norm = float(mask.sum().item()) if norm is None else norm
+        _lib.check(self.L.gb_mlp_loss_grad_dev(self.p.data_ptr(), x.data_ptr(), y.data_ptr(), mask.data_ptr(),
+                                               x.shape[0], norm, self.g.data_ptr(), self.loss.data_ptr(), self._s()),
+                   "gb_mlp_loss_grad_dev")
+        return self.loss, self.g
+
+    def adam(self, lr, b1=0.9, b2=0.999, eps=1e-8, wd=0.0):
+        self.step += 1
+        _lib.check(self.L.gb_mlp_adam_dev(self.p.data_ptr(), self.g.data_ptr(), self.m.data_ptr(), self.v.data_ptr(),
+                                          NPARAMS, lr, b1, b2, eps, wd, self.step, self._s()), "gb_mlp_adam_dev")
+
+    def params(self):
+        return self.p.cpu().numpy()
+
+
+def train(X, Y, M, epochs=300, batch=512, lr=3e-3, seed=0, log=None):
+    import torch
+    rng = np.random.default_rng(seed)
+    net = GpuMlp(init_params(seed))
+    Xd, Yd, Md = (torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda() for a in (X, Y, M))
+    n = X.shape[0]
+    curve = []
+    for ep in range(epochs):
+        perm = torch.from_numpy(rng.permutation(n)).cuda()
+        lr_ep = lr * 0.5 * (1.0 + math.cos(math.pi * ep / epochs))
+        tot = 0.0
+        for b0 in range(0, n, batch):
+            idx = perm[b0:b0 + batch]
+            xb, yb, mb = Xd[idx].contiguous(), Yd[idx].contiguous(), Md[idx].contiguous()
+            loss, _ = net.loss_grad(xb, yb, mb)
+            net.adam(lr_ep, wd=1e-5)
+            tot += float(loss.item()) * idx.numel()
+        curve.append(tot / n)
+        if log and (ep % 25 == 0 or ep == epochs - 1):
+            log("epoch %d loss %.5f" % (ep, curve[-1]))
+    return net.params(), curve
+
+
+# ------------------------------------------------------------------ evaluation
+def evaluate(params, data):
+    """Throughput regret of the MLP's and of the threshold rule's choices
+    against the exhaustive table, and the slice proposals' violations."""
+    net = GpuMlp(params)
+    pred = net.forward(data["X"])
+    T = data["T"]
+    best = T.min(1)
+    ch_mlp = pred[:, :NCONFIG].argmin(1)
+    sh = data["shapes"]
+    ch_heur = np.array([heuristic_config(int(r[0]), int(r[1]), int(r[2])) for r in sh])
+    t_mlp = T[np.arange(len(T)), ch_mlp]
+    t_heur = T[np.arange(len(T)), ch_heur]
+    flops = 2.0 * sh[:, 0] * sh[:, 1] * sh[:, 2]
+
+    def stats(t):
+        return {"mean_throughput_regret": float(1.0 - np.mean(best / t)),
+                "aggregate_throughput_regret": float(1.0 - best.sum() / t.sum()),
+                "median_time_ratio": float(np.median(t / best)),
+                "p95_time_ratio": float(np.percentile(t / best, 95)),
+                "exact_choice_rate": float(np.mean(np.isclose(t, best)))}
+
+    res = {"n": int(len(T)), "mlp": stats(t_mlp), "threshold_rule": stats(t_heur),
+           "exhaustive_mean_gflops": float(np.mean(flops / best / 1e3))}
+    fp64 = sh[:, 3] == 0
+    if fp64.any():
+        s_true = data["S"][fp64]
+        s_prop = np.clip(np.ceil(pred[fp64, OUT_SLICES] * 12.0 - 0.25), 2, 12).astype(int)
+        res["slices"] = {"n": int(fp64.sum()),
+                         "proposal_below_verifier": int((s_prop < s_true).sum()),
+                         "violations_after_verifier": 0,
+                         "mean_proposed": float(s_prop.mean()), "mean_required": float(s_true.mean()),
+                         "mean_final": float(np.maximum(s_prop, s_true).mean()),
+                         "default_without_mlp": 8}
+    return res
+
+
+# ------------------------------------------------------------------ persistence
+def save_model(path, params, meta):
+    p = np.asarray(params, np.float32)
+    blob = p.tobytes()
+    doc = {"schema": SCHEMA, "nin": NIN, "nhidden": NH, "nout": NOUT, "configs": CONFIG_NAMES,
+           "time_scale": TIME_SCALE, "sha256": hashlib.sha256(blob).hexdigest(),
+           "params": [float(v) for v in p], "meta": meta}
+    with open(path, "w") as f:
+        json.dump(doc, f)
+
+
+def load_model(path):
+    with open(path) as f:
+        doc = json.load(f)
+    if doc.get("schema") != SCHEMA:
+        raise ValueError("unknown selector schema %r" % doc.get("schema"))
+    p = np.asarray(doc["params"], np.float32)
+    if p.size != NPARAMS or hashlib.sha256(p.tobytes()).hexdigest() != doc["sha256"]:
+        raise ValueError("selector weights fail their checksum")
+    return p, doc
+
+
+class Selector:
+    """Configuration choice for one call: MLP if a model loads, else the
+    exhaustive table entry if present, else the threshold rule."""
+
+    def __init__(self, model_path=None):
+        self.net = None
+        self.table = {}
+        if model_path and os.path.exists(model_path):
+            try:
+                p, _ = load_model(model_path)
+                self.net = GpuMlp(p)
+            except (ValueError, KeyError, OSError):
+                self.net = None
+
+    def choose(self, m, n, k, dtype, ta=0, tb=0, pad=0, spread_a=0.0, spread_b=0.0):
+        if 2.0 * m * n * k > WORK_CAP:
+            return 0, 8
+        key = (m, n, k, dtype, ta, tb, pad)
+        if key in self.table:
+            return self.table[key]
+        if self.net is None:
+            return heuristic_config(m, n, k), 8
+        out = self.net.forward(features(m, n, k, dtype, ta, tb, pad, spread_a, spread_b)[None, :])[0]
+        s = int(np.clip(math.ceil(out[OUT_SLICES] * 12.0 - 0.25), 2, 12))
+        return int(out[:NCONFIG].argmin()), s
+
+
+def _main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("cmd", choices=["tune", "train", "eval"])
+    ap.add_argument("--count", type=int, default=1000)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--out")
+    ap.add_argument("--data")
+    ap.add_argument("--model")
+    ap.add_argument("--epochs", type=int, default=300)
+    a = ap.parse_args()
+    if a.cmd == "tune":
+        d = build_dataset(sample_shapes(a.count, a.seed), log_every=500)
+        np.savez_compressed(a.out, **d)
+    elif a.cmd == "train":
+        d = np.load(a.data)
+        p, curve = train(d["X"], d["Y"], d["M"], epochs=a.epochs, log=print)
+        save_model(a.out, p, {"train_samples": int(d["X"].shape[0]), "final_loss": curve[-1]})
+    else:
+        p, _ = load_model(a.model)
+        print(json.dumps(evaluate(p, np.load(a.data)), indent=1))
+
+
+if __name__ == "__main__":
+    _main()

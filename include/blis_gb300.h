@@ -361,6 +361,42 @@ int gb_dd_gemm_entries_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t k, dou
                            const int64_t* jj, double* hi, double* lo, void* stream);
 
 /* ===================================================================== */
+/* 2b. Learned configuration selector (no reference counterpart: BLIS picks */
+/*     kernels from static per-architecture tables,                        */
+/*     config/<arch>/bli_cntx_init_<arch>.c)                                */
+/* ===================================================================== */
+
+/* MLP 16 -> 64 -> 64 -> 64 -> 8, GELU, FP32.  Parameters are one vector of
+   GB_MLP_NPARAMS floats: W1[64][16] b1[64] W2[64][64] b2[64] W3[64][64] b3[64]
+   W4[8][64] b4[8].  Inputs x[batch][16], outputs / targets / mask [batch][8];
+   all pointers are device pointers. */
+#define GB_MLP_IN 16
+#define GB_MLP_HIDDEN 64
+#define GB_MLP_OUT 8
+#define GB_MLP_NPARAMS 9928
+int gb_mlp_forward_dev(const float* params, const float* x, gb_dim_t batch, float* out, void* stream);
+/* grad := d/dparams of sum_b sum_o mask*(out - y)^2 / norm, loss := that sum;
+   deterministic (fixed-order fold of per-block partials). */
+int gb_mlp_loss_grad_dev(const float* params, const float* x, const float* y, const float* mask,
+                         gb_dim_t batch, float norm, float* grad, float* loss, void* stream);
+/* One Adam step (step counts from 1) with decoupled weight decay added to the gradient. */
+int gb_mlp_adam_dev(float* params, const float* grad, float* m, float* v, gb_dim_t n, float lr,
+                    float beta1, float beta2, float eps, float weight_decay, int step, void* stream);
+
+/* Error-bound verifier for the Ozaki slice count: the smallest s >= s_min
+   such that, on a deterministic sample of `nsample` entries (i, j),
+     2^-(8s+1) (2^e_i |B_j|_1 + |A_i|_1 2^e_j) + sqrt(k) s 2^(e_i+e_j-8s-2)
+       <= sqrt(k) u (|A||B|)_ij,          u = 2^-53,
+   i.e. the split's representation error plus the dropped slice products
+   (random-sign growth) stays at the level of a typical FP64 dot-product
+   error.  *s_out receives s (at most 12; a
+   sample that needs more reports 13).  Device operands, host s_out. */
+int gb_ozaki_verify_slices_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+                               gb_dim_t k, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                               const double* b, gb_inc_t rs_b, gb_inc_t cs_b, int s_min,
+                               int nsample, int* s_out, void* stream);
+
+/* ===================================================================== */
 /* 3. Controls and introspection                                           */
 /* ===================================================================== */
 
