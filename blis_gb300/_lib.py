@@ -95,6 +95,7 @@ def load(path=None):
     _sig(L, "gb_randm_dev", C.c_int, [C.c_int, C.c_int, _vp, _i64, _i64, _i64, _i64, C.c_uint64, _d, _d, _vp])
     _sig(L, "gb_dd_gemm_entries_dev", C.c_int, [C.c_int, C.c_int, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64,
                                                  _d, _vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp, _vp])
+    _sig(L, "gb_set_ozaki_ctas", C.c_int, [C.c_int])
     _sig(L, "gb_init", C.c_int, [C.c_int])
     _sig(L, "gb_set_dgemm_mode", C.c_int, [C.c_int, C.c_int])
     _sig(L, "gb_get_last_error", C.c_int, [C.c_char_p, C.c_size_t])

@@ -299,6 +299,229 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (warp == OZ_MMA_WARP) tmem_dealloc(tmem_base, OZ_TMEM_COLS);
 }
 
+// ---------------------------------------------------------------- CTA-pair form
+// The same computation on clusters of two CTAs (cta_group::2): a pair owns a
+// 256 x 256 tile; each CTA stages 128 rows of A and 128 rows of B per k block
+// (32 KB, six stages), the even CTA issues M=256 N=256 K=16 MMAs that read
+// both CTAs' shared memory and write each CTA's 128 accumulator rows into
+// its own TMEM.  Per SM this halves the B bytes moved through shared memory
+// (TMA writes plus MMA reads fall from ~192 to ~128 bytes per clock at full
+// MMA rate).  Both CTAs' TMA loads count on the even CTA's `full` barrier;
+// MMA completion is multicast to both CTAs' `empty` and `tfull` barriers; the
+// odd CTA's epilogue warps release TMEM by arriving on the even CTA's
+// `tempty` barrier.
+constexpr int OZ2_STAGES = 6;
+constexpr int OZ2_ROWS = 128;                       // rows of A and of B per CTA
+constexpr int OZ2_A_BYTES = OZ2_ROWS * OZ_BK * 2;   // 16 KB
+constexpr int OZ2_B_BYTES = OZ2_ROWS * OZ_BK * 2;   // 16 KB
+constexpr int OZ2_STAGE_BYTES = OZ2_A_BYTES + OZ2_B_BYTES;
+constexpr int OZ2_SMEM_BYTES = OZ2_STAGES * OZ2_STAGE_BYTES + 1024 + 256;
+
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    ozaki_slice_gemm_pair_kernel(const __grid_constant__ CUtensorMap map_a,
+                                 const __grid_constant__ CUtensorMap map_b, const __grid_constant__ OzGemmParams p)
+{
+    if (*p.skip) return;  // both CTAs of a pair read the same flag
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                               ~uintptr_t(1023));
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + OZ2_STAGES * OZ2_STAGE_BYTES);
+    uint64_t* empty = full + OZ2_STAGES;
+    uint64_t* tfull = empty + OZ2_STAGES;
+    uint64_t* tempty = tfull + 2;
+    uint64_t* drain = tempty + 2;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = cluster_ctarank();
+    const bool leader = (rank == 0);
+    const int64_t pair = blockIdx.x >> 1, npair = gridDim.x >> 1;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < OZ2_STAGES; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&tfull[i], 1);
+            mbar_init(&tempty[i], 2 * OZ_EPI_WARPS);
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        fence_barrier_init();
+        fence_proxy_async();
+    }
+    if (warp == OZ_MMA_WARP) {
+        tmem_alloc_pair(tmem_slot, OZ_TMEM_COLS);
+        tmem_relinquish_pair();
+    }
+    if (warp == OZ_PRODUCER_WARP && lane == 0) {
+        prefetch_tensormap(&map_a);
+        prefetch_tensormap(&map_b);
+    }
+    tc_fence_before();
+    __syncthreads();
+    cluster_sync();  // the peer's barriers exist before any cross-CTA signal
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == OZ_PRODUCER_WARP) {
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            uint32_t issued_mask = 0, last_phase = 0;
+            bool ok = true;
+            for (int64_t it = pair; it < p.items && ok; it += npair) {
+                if (*abort_flag) break;
+                const OzItem w = oz_decode(p, it);
+                for (int pi = 0; pi < w.npairs && ok; ++pi) {
+                    const int pa = w.pa_lo + pi, pb = w.lev - pa;
+                    for (int kb = 0; kb < w.kbn; ++kb) {
+                        if (!mbar_wait_bounded(&empty[stage], phase ^ 1u, kWaitBudgetNs)) {
+                            oz_fail(p, abort_flag);
+                            ok = false;
+                            break;
+                        }
+                        uint8_t* sa = smem + stage * OZ2_STAGE_BYTES;
+                        uint8_t* sb = sa + OZ2_A_BYTES;
+                        if (leader) mbar_arrive_expect_tx(&full[stage], 2 * OZ2_STAGE_BYTES);
+                        const uint32_t bar = mapa_shared(smem_addr(&full[stage]), 0);
+                        const int kx = (w.kb0 + kb) * OZ_BK;
+                        tma_load_3d_pair(sa, &map_a, bar, kx, w.tm * (2 * OZ2_ROWS) + (int)rank * OZ2_ROWS, pa - 1);
+                        tma_load_3d_pair(sb, &map_b, bar, kx, w.tn * OZ_BN + (int)rank * OZ2_ROWS, pb - 1);
+                        issued_mask |= 1u << stage;
+                        last_phase = (last_phase & ~(1u << stage)) | (phase << stage);
+                        if (++stage == OZ2_STAGES) {
+                            stage = 0;
+                            phase ^= 1u;
+                        }
+                    }
+                }
+            }
+            if (*abort_flag) {
+                if (leader) {
+                    for (int s2 = 0; s2 < OZ2_STAGES; ++s2)
+                        if (issued_mask & (1u << s2))
+                            mbar_wait_bounded(&full[s2], (last_phase >> s2) & 1u, kWaitBudgetNs);
+                } else {
+                    // the odd CTA's copies complete on the even CTA's barrier: give
+                    // them time to land before this CTA's shared memory is released
+                    const uint64_t t0 = globaltimer();
+                    while (globaltimer() - t0 < 2000000ull) {
+                    }
+                }
+            }
+        }
+    } else if (warp == OZ_MMA_WARP) {
+        if (lane == 0 && leader) {
+            constexpr uint32_t idesc = idesc_bf16_f32(2 * OZ2_ROWS, OZ_BN);
+            int stage = 0;
+            uint32_t phase = 0;
+            uint32_t chunk_ctr = 0;
+            bool ok = true, issued_any = false;
+            for (int64_t it = pair; it < p.items && ok; it += npair) {
+                if (*abort_flag) break;
+                const OzItem w = oz_decode(p, it);
+                const int total = w.npairs * w.kbn;
+                for (int t0 = 0; t0 < total && ok; t0 += p.chunk_kb) {
+                    const int nkb = (total - t0 < p.chunk_kb) ? total - t0 : p.chunk_kb;
+                    const uint32_t buf = chunk_ctr & 1u, tph = (chunk_ctr >> 1) & 1u;
+                    if (!mbar_wait_bounded(&tempty[buf], tph ^ 1u, kWaitBudgetNs)) {
+                        oz_fail(p, abort_flag);
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d_tmem = tmem_base + buf * OZ_BN;
+                    for (int q = 0; q < nkb; ++q) {
+                        if (!mbar_wait_bounded(&full[stage], phase, kWaitBudgetNs)) {
+                            oz_fail(p, abort_flag);
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t sa = smem_addr(smem + stage * OZ2_STAGE_BYTES);
+                        const uint32_t sb = sa + OZ2_A_BYTES;
+                        const uint64_t ad = sdesc_kmajor_sw128(sa), bd = sdesc_kmajor_sw128(sb);
+#pragma unroll
+                        for (int j = 0; j < OZ_BK / 16; ++j)
+                            mma_bf16_pair(d_tmem, ad + 2 * j, bd + 2 * j, idesc, (q | j) != 0);
+                        issued_any = true;
+                        mma_commit_pair(&empty[stage], 0x3);
+                        if (++stage == OZ2_STAGES) {
+                            stage = 0;
+                            phase ^= 1u;
+                        }
+                    }
+                    if (!ok) break;
+                    mma_commit_pair(&tfull[buf], 0x3);
+                    ++chunk_ctr;
+                }
+            }
+            if (*abort_flag && issued_any) {
+                mma_commit_pair(drain, 0x1);
+                mbar_wait_bounded(drain, 0, kWaitBudgetNs);
+            }
+        }
+    } else {
+        // epilogue: this CTA's 128 accumulator rows, as in the single-CTA form
+        const int quad = warp & 3, half = warp >> 2;
+        const uint32_t leader_tempty0 = mapa_shared(smem_addr(&tempty[0]), 0);
+        uint32_t chunk_ctr = 0;
+        bool ok = true;
+        for (int64_t it = pair; it < p.items && ok; it += npair) {
+            if (__shfl_sync(0xffffffffu, *abort_flag, 0)) break;
+            const OzItem w = oz_decode(p, it);
+            const int total = w.npairs * w.kbn;
+            const int nchunks = (total + p.chunk_kb - 1) / p.chunk_kb;
+            int32_t acc[128];
+#pragma unroll
+            for (int i = 0; i < 128; ++i) acc[i] = 0;
+            for (int c = 0; c < nchunks; ++c) {
+                const uint32_t buf = chunk_ctr & 1u, tph = (chunk_ctr >> 1) & 1u;
+                int got = 1;
+                if (lane == 0) got = mbar_wait_bounded(&tfull[buf], tph, kWaitBudgetNs) ? 1 : 0;
+                got = __shfl_sync(0xffffffffu, got, 0);
+                if (!got) {
+                    if (lane == 0) oz_fail(p, abort_flag);
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t taddr = tmem_base + ((uint32_t)(quad * 32) << 16) + buf * OZ_BN + half * 128;
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    uint32_t r[32];
+                    tmem_ld_32x32b_x32(taddr + g * 32, r);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) acc[g * 32 + i] += __float2int_rn(__uint_as_float(r[i]));
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) {
+                    if (leader) mbar_arrive(&tempty[buf]);
+                    else mbar_arrive_cluster(leader_tempty0 + buf * (uint32_t)sizeof(uint64_t));
+                }
+                ++chunk_ctr;
+            }
+            if (!ok) break;
+            const int64_t i = (int64_t)w.tm * (2 * OZ2_ROWS) + (int64_t)rank * OZ2_ROWS + quad * 32 + lane;
+            const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
+            int32_t* dst = p.planes + ((int64_t)w.plane * p.npad + j0) * p.mpad + i;
+#pragma unroll
+            for (int c = 0; c < 128; ++c) dst[(int64_t)c * p.mpad] = acc[c];
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    cluster_sync();  // no CTA leaves while its peer may still touch its memory
+    tc_fence_after();
+    if (warp == OZ_MMA_WARP) tmem_dealloc_pair(tmem_base, OZ_TMEM_COLS);
+}
+
 // ---------------------------------------------------------------- split
 // Row r of the row operand R: element (r, l) at R[r*sr + l*sl].  |x| as its
 // IEEE bit pattern is monotone in |x|, so the row maximum is an integer max.
@@ -659,6 +882,31 @@ int chunk_kb_setting()
     return v;
 }
 
+}  // namespace
+
+// Slice-GEMM engine: 1 = one CTA per 128x256 tile, 2 = CTA pairs per
+// 256x256 tile (cta_group::2).  gb_set_ozaki_ctas() or the environment
+// variable GB_OZAKI_CTAS select; the pair form is the default.
+static int g_ozaki_ctas = 0;
+
+int ozaki_ctas_setting()
+{
+    if (g_ozaki_ctas == 0) {
+        const char* e = getenv("GB_OZAKI_CTAS");
+        g_ozaki_ctas = (e && atoi(e) == 1) ? 1 : 2;
+    }
+    return g_ozaki_ctas;
+}
+
+int set_ozaki_ctas(int ctas)
+{
+    if (ctas != 1 && ctas != 2) return set_error(GB_ERR_ARG, "gb_set_ozaki_ctas", "ctas must be 1 or 2");
+    g_ozaki_ctas = ctas;
+    return GB_SUCCESS;
+}
+
+namespace {
+
 template <int S>
 void launch_split(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl,
                   const unsigned long long* mb, int64_t rpad, int64_t kpad, uint16_t* out, int32_t* ex,
@@ -718,7 +966,9 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     if (ozaki_t_bound_log2(slices, k) >= 126.0)
         return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices and k exceed the 128-bit recombination range");
 
-    const int64_t kpad = round_up(k, OZ_BK), mpad = round_up(m, OZ_BM), npad = round_up(n, OZ_BN);
+    const bool pair_form = (ozaki_ctas_setting() == 2);
+    const int64_t row_tile = pair_form ? 2 * OZ2_ROWS : OZ_BM;
+    const int64_t kpad = round_up(k, OZ_BK), mpad = round_up(m, row_tile), npad = round_up(n, OZ_BN);
     if (mpad > INT32_MAX || npad > INT32_MAX || kpad > INT32_MAX)
         return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "dimension too large for TMA coordinates");
     const int kb_total = (int)(kpad / OZ_BK);
@@ -727,7 +977,7 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     p.slices = slices;
     p.nlevels = slices;
     p.kb_total = kb_total;
-    p.tiles_m = (int)(mpad / OZ_BM);
+    p.tiles_m = (int)(mpad / row_tile);
     p.tiles_n = (int)(npad / OZ_BN);
     const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
     int planes_total = 0;
@@ -806,18 +1056,55 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
 
     CUtensorMap map_a, map_b;
     if ((rc = make_slice_map(&map_a, sa, kpad, mpad, slices, OZ_BM))) return bail(rc);
-    if ((rc = make_slice_map(&map_b, sb, kpad, npad, slices, OZ_BN))) return bail(rc);
+    if ((rc = make_slice_map(&map_b, sb, kpad, npad, slices, pair_form ? OZ2_ROWS : OZ_BN))) return bail(rc);
 
     static bool attr_set = false;
+    static int max_pairs = 0;
     if (!attr_set) {
         if ((rc = check_cuda(cudaFuncSetAttribute(ozaki_slice_gemm_kernel,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   OZ_SMEM_BYTES), "smem attr")))
             return bail(rc);
+        if ((rc = check_cuda(cudaFuncSetAttribute(ozaki_slice_gemm_pair_kernel,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  OZ2_SMEM_BYTES), "smem attr")))
+            return bail(rc);
+        cudaLaunchConfig_t qc = {};
+        cudaLaunchAttribute qa[1];
+        qa[0].id = cudaLaunchAttributeClusterDimension;
+        qa[0].val.clusterDim.x = 2;
+        qa[0].val.clusterDim.y = 1;
+        qa[0].val.clusterDim.z = 1;
+        qc.gridDim = dim3(2 * (unsigned)(sms / 2));
+        qc.blockDim = dim3(OZ_THREADS);
+        qc.dynamicSmemBytes = OZ2_SMEM_BYTES;
+        qc.attrs = qa;
+        qc.numAttrs = 1;
+        if ((rc = check_cuda(cudaOccupancyMaxActiveClusters(&max_pairs, ozaki_slice_gemm_pair_kernel, &qc),
+                             "cluster occupancy")))
+            return bail(rc);
         attr_set = true;
     }
-    const int grid = (int)((p.items < sms) ? p.items : sms);
-    {
+    if (pair_form) {
+        if (max_pairs < 1) return bail(set_error(GB_ERR_UNSUPPORTED, "ozaki", "no CTA pair fits on this GPU"));
+        const int npair = (int)((p.items < max_pairs) ? p.items : max_pairs);
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 2;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(2 * (unsigned)npair);
+        cfg.blockDim = dim3(OZ_THREADS);
+        cfg.dynamicSmemBytes = OZ2_SMEM_BYTES;
+        cfg.stream = s;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        LaunchScope ls("ozaki_slice_gemm", s);
+        rc = check_cuda(cudaLaunchKernelEx(&cfg, ozaki_slice_gemm_pair_kernel, map_a, map_b, p), "pair launch");
+        if (rc) return bail(rc);
+    } else {
+        const int grid = (int)((p.items < sms) ? p.items : sms);
         LaunchScope ls("ozaki_slice_gemm", s);
         ozaki_slice_gemm_kernel<<<grid, OZ_THREADS, OZ_SMEM_BYTES, s>>>(map_a, map_b, p);
     }
@@ -854,3 +1141,5 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
 }
 
 }  // namespace gb
+
+extern "C" int gb_set_ozaki_ctas(int ctas) { return gb::set_ozaki_ctas(ctas); }

@@ -1,0 +1,208 @@
+"""Throughput of the hot path's other configurations on one GPU.
+
+bench.py measures the headline (emulated vs native DGEMM 16384^3); this
+module measures the remaining workloads of the same path, device resident,
+with CUDA events on the launching stream after warm-up, inputs larger than
+L2 where the workload allows:
+
+  dgemm_1024      C := A B + 0.5 C, m=n=k=1024, U[-1,1]          (FP64 pipe)
+  dgemm_8192      native FP64 and Ozaki (7 slices), m=n=k=8192
+  sgemm_8192      FP32, m=n=k=8192
+  dtrsm_8192x4096 L/L/N/N, diag 8192+|u|, native and Ozaki updates (m^2 n flop)
+  dgemv_32768     N and T, 8(mn + n + 2m) bytes                    (HBM)
+  daxpyv_2^28     24 n bytes; ddotv_2^28: 16 n bytes                (HBM)
+  batch_4096      4096 problems, m,n,k log-uniform in [16,1024], random
+                  transposes: one grouped launch (captured graph) vs a
+                  per-problem launch loop, FP64 and FP32
+
+Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl]
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+
+import numpy as np
+
+from . import _lib, dev
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def _timer(fn, reps=5, warmup=2):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _mat(m, n, kind=dev.RAND_UNIFORM, seed=1, p0=-1.0, p1=1.0, dtype=None):
+    import torch
+    x = dev.colmajor(m, n, dtype or torch.float64)
+    dev.randm(x, kind, seed, p0, p1)
+    return x
+
+
+def run_gemm(out):
+    import torch
+    pk, _ = peaks()
+    a, b, c = _mat(1024, 1024, seed=1), _mat(1024, 1024, seed=2), _mat(1024, 1024, seed=3)
+    ms = _timer(lambda: dev.dgemm(0, 0, 1.0, a, b, 0.5, c), reps=20)
+    out.append({"workload": "dgemm_1024", "form": "native_fp64", "ms": ms, "tflops": 2 * 1024 ** 3 / ms / 1e9})
+    n = 8192
+    a, b, c = _mat(n, n, seed=4), _mat(n, n, seed=5), _mat(n, n, seed=6)
+    ms = _timer(lambda: dev.dgemm(0, 0, 1.0, a, b, 0.0, c), reps=1, warmup=1)
+    out.append({"workload": "dgemm_8192", "form": "native_fp64", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
+    ms = _timer(lambda: dev.dgemm_ozaki(0, 0, 1.0, a, b, 0.0, c, 7), reps=3)
+    out.append({"workload": "dgemm_8192", "form": "ozaki_s7", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9,
+                "bf16_frac_of_measured_peak": 28 * 2 * n ** 3 / ms / 1e9 / pk.get("bf16_tflops", 1900.0)})
+    del a, b, c
+    fa, fb, fc = (_mat(n, n, seed=s, dtype=torch.float32) for s in (7, 8, 9))
+    ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
+    out.append({"workload": "sgemm_8192", "form": "ffma_fp32", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
+
+
+def run_trsm(out):
+    import torch
+    m, n = 8192, 4096
+    L = _mat(m, m, seed=11)
+    L.copy_(torch.tril(L))
+    d = torch.arange(m, device="cuda")
+    L[d, d] = m + L[d, d].abs()
+    b0 = _mat(m, n, seed=12)
+    flops = float(m) * m * n
+    for mode, name in ((0, "native_fp64"), (1, "ozaki_s7_updates")):
+        _lib.load().gb_set_dgemm_mode(mode, 7)
+        x = b0.clone()
+        ms = _timer(lambda: (x.copy_(b0), dev.dtrsm(0, 0xC0, 0, 0, 1.0, L, x)), reps=1, warmup=1)
+        copy_ms = _timer(lambda: x.copy_(b0), reps=3, warmup=1)
+        out.append({"workload": "dtrsm_8192x4096", "form": name, "ms": ms - copy_ms,
+                    "tflops": flops / (ms - copy_ms) / 1e9})
+    _lib.load().gb_set_dgemm_mode(0, 8)
+
+
+def run_level12(out):
+    import torch
+    pk, kind = peaks()
+    hbm = pk.get("hbm_gbs", 6800.0)
+    n = 1 << 28
+    x = torch.empty(n, dtype=torch.float64, device="cuda").uniform_(-1, 1)
+    y = torch.empty(n, dtype=torch.float64, device="cuda").uniform_(-1, 1)
+    rho = torch.zeros(1, dtype=torch.float64, device="cuda")
+    ms = _timer(lambda: dev.daxpyv(0.5, x, y), reps=10)
+    gbs = 24.0 * n / ms / 1e6
+    out.append({"workload": "daxpyv_2^28", "ms": ms, "gbs": gbs, "hbm_frac": gbs / hbm, "peak": "%s hbm_gbs" % kind})
+    ms = _timer(lambda: dev.ddotv(x, y, rho), reps=10)
+    gbs = 16.0 * n / ms / 1e6
+    out.append({"workload": "ddotv_2^28", "ms": ms, "gbs": gbs, "hbm_frac": gbs / hbm, "peak": "%s hbm_gbs" % kind})
+    del x, y
+    m = 32768
+    a = _mat(m, m, seed=21)
+    xv = torch.empty(m, dtype=torch.float64, device="cuda").uniform_(-1, 1)
+    yv = torch.empty(m, dtype=torch.float64, device="cuda").uniform_(-1, 1)
+    for t, name in ((0, "N"), (8, "T")):
+        ms = _timer(lambda: dev.dgemv(t, 1.0, a, xv, 0.5, yv), reps=5)
+        gbs = 8.0 * (m * m + m + 2 * m) / ms / 1e6
+        out.append({"workload": "dgemv_32768_%s" % name, "ms": ms, "gbs": gbs, "hbm_frac": gbs / hbm,
+                    "peak": "%s hbm_gbs" % kind})
+
+
+class _Prob(C.Structure):
+    _fields_ = [("transa", C.c_int), ("transb", C.c_int), ("m", C.c_int64), ("n", C.c_int64),
+                ("k", C.c_int64), ("alpha", C.c_double), ("beta", C.c_double), ("a", C.c_void_p),
+                ("lda", C.c_int64), ("b", C.c_void_p), ("ldb", C.c_int64), ("c", C.c_void_p),
+                ("ldc", C.c_int64)]
+
+
+def batch_problems(count, seed, dtype, lo=16, hi=1024):
+    """The batching configuration: m, n, k log-uniform integers in [lo, hi],
+    transposes random per operand, U[-1,1] entries; operands packed in one
+    device arena per operand kind."""
+    import torch
+    rng = np.random.default_rng(seed)
+    dims = np.round(np.exp(rng.uniform(math.log(lo), math.log(hi), size=(count, 3)))).astype(np.int64)
+    tr = rng.integers(0, 2, size=(count, 2))
+    tdt = torch.float64 if dtype == 0 else torch.float32
+    na = int((dims[:, 0] * dims[:, 2]).sum())
+    nb = int((dims[:, 2] * dims[:, 1]).sum())
+    nc = int((dims[:, 0] * dims[:, 1]).sum())
+    A = torch.empty(na, dtype=tdt, device="cuda").uniform_(-1, 1)
+    B = torch.empty(nb, dtype=tdt, device="cuda").uniform_(-1, 1)
+    Cc = torch.zeros(nc, dtype=tdt, device="cuda")
+    es = A.element_size()
+    probs = (_Prob * count)()
+    oa = ob = oc = 0
+    flops = 0.0
+    for i in range(count):
+        m, n, k = (int(v) for v in dims[i])
+        ta, tb = int(tr[i, 0]), int(tr[i, 1])
+        probs[i] = _Prob(8 * ta, 8 * tb, m, n, k, 1.0, 0.0, A.data_ptr() + oa * es, k if ta else m,
+                         B.data_ptr() + ob * es, n if tb else k, Cc.data_ptr() + oc * es, m)
+        oa += m * k
+        ob += k * n
+        oc += m * n
+        flops += 2.0 * m * n * k
+    return probs, (A, B, Cc), flops
+
+
+def run_batch(out):
+    L = _lib.load()
+    L.gb_gemm_batch_dev.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_void_p]
+    L.gb_batch_plan_create.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]
+    L.gb_batch_plan_run.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    L.gb_batch_plan_destroy.argtypes = [C.c_void_p]
+    for dtype, name in ((0, "fp64"), (1, "fp32")):
+        probs, keep, flops = batch_problems(4096, 4, dtype)
+        plan = C.c_void_p()
+        _lib.check(L.gb_batch_plan_create(C.addressof(probs), 4096, dtype, C.byref(plan)), "plan")
+        ms_g = _timer(lambda: _lib.check(L.gb_batch_plan_run(plan, 1, None), "run"), reps=3, warmup=1)
+        ms_l = _timer(lambda: _lib.check(L.gb_gemm_batch_dev(C.addressof(probs), 4096, dtype, 1, None), "loop"),
+                      reps=1, warmup=1)
+        L.gb_batch_plan_destroy(plan)
+        out.append({"workload": "batch_4096_%s" % name, "flops": flops, "grouped_graph_ms": ms_g,
+                    "grouped_tflops": flops / ms_g / 1e9, "loop_ms": ms_l, "loop_tflops": flops / ms_l / 1e9,
+                    "speedup": ms_l / ms_g})
+        del keep
+
+
+SUITES = {"gemm": run_gemm, "trsm": run_trsm, "level12": run_level12, "batch": run_batch}
+
+
+def main():
+    import torch
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default="")
+    ap.add_argument("--json")
+    a = ap.parse_args()
+    torch.cuda.set_device(0)
+    _lib.check(_lib.load().gb_init(0), "gb_init")
+    names = [s for s in a.only.split(",") if s] or list(SUITES)
+    out = []
+    for nm in names:
+        SUITES[nm](out)
+    for r in out:
+        print(json.dumps(r), flush=True)
+    if a.json:
+        with open(a.json, "w") as f:
+            for r in out:
+                f.write(json.dumps(r) + "\n")
+
+
+if __name__ == "__main__":
+    main()

@@ -409,6 +409,10 @@ int gb_init(int device);
 #define GB_DGEMM_OZAKI 1
 int gb_set_dgemm_mode(int mode, int slices);
 
+/* Engine of the Ozaki slice products: 1 = one CTA per 128x256 tile,
+   2 = pairs of CTAs on two SMs per 256x256 tile (cta_group::2, default). */
+int gb_set_ozaki_ctas(int ctas);
+
 /* Last error of the calling thread (GB_SUCCESS if none), with its message. */
 int gb_get_last_error(char* msg, size_t len);
 void gb_clear_last_error(void);

@@ -16,9 +16,12 @@ pytestmark = pytest.mark.gpu
 N, T = blas.NO_TRANSPOSE, blas.TRANSPOSE
 
 
-@pytest.fixture(autouse=True)
-def reset_mode(gblib):
-    yield
+@pytest.fixture(autouse=True, params=[2, 1], ids=["cta_pair", "one_cta"])
+def engine(gblib, request):
+    """Every test runs on both slice-GEMM engines (CTA pairs and single CTAs)."""
+    assert gblib.gb_set_ozaki_ctas(request.param) == 0
+    yield request.param
+    gblib.gb_set_ozaki_ctas(2)
     blas.set_dgemm_mode(blas.DGEMM_NATIVE)
 
 
