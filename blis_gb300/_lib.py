@@ -96,6 +96,14 @@ def load(path=None):
     _sig(L, "gb_dd_gemm_entries_dev", C.c_int, [C.c_int, C.c_int, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64,
                                                  _d, _vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp, _vp])
     _sig(L, "gb_set_ozaki_ctas", C.c_int, [C.c_int])
+    _sig(L, "gb_selector_load", C.c_int, [_vp, C.c_int])
+    _sig(L, "gb_selector_load_file", C.c_int, [_cp])
+    _sig(L, "gb_selector_unload", C.c_int, [])
+    _sig(L, "gb_set_gemm_autoselect", C.c_int, [C.c_int])
+    _sig(L, "gb_selector_choose", C.c_int, [C.c_int, _i64, _i64, _i64, C.c_int, C.c_int, C.c_int, _d, _d,
+                                            C.POINTER(C.c_int), C.POINTER(C.c_int)])
+    _sig(L, "gb_ozaki_verify_slices_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, _i64, _vp, _i64, _i64, _vp,
+                                                    _i64, _i64, C.c_int, C.c_int, C.POINTER(C.c_int), _vp])
     _sig(L, "gb_init", C.c_int, [C.c_int])
     _sig(L, "gb_set_dgemm_mode", C.c_int, [C.c_int, C.c_int])
     _sig(L, "gb_get_last_error", C.c_int, [C.c_char_p, C.c_size_t])

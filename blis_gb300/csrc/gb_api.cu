@@ -153,19 +153,39 @@ int gemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, T alpha, 
         if ((rc = stage_in(b, tb ? n : k, tb ? k : n, rs_b, cs_b, esz, true, &B, s))) return rc;
         const int64_t ars = ta ? A.cs : A.rs, acs = ta ? A.rs : A.cs;
         const int64_t brs = tb ? B.cs : B.rs, bcs = tb ? B.rs : B.cs;
-        if (sizeof(T) == 8) {
+        // leading-dimension padding of the caller's operand, a selector feature
+        const int64_t pad = (rs_a == 1) ? cs_a - (ta ? k : m) : ((cs_a == 1) ? rs_a - (ta ? m : k) : 0);
+        if (sizeof(T) == 8 && dgemm_mode() == GB_DGEMM_OZAKI) {
             const double* ad = reinterpret_cast<const double*>(A.origin);
             const double* bd = reinterpret_cast<const double*>(B.origin);
-            if (dgemm_mode() == GB_DGEMM_OZAKI)
-                rc = dgemm_ozaki(m, n, k, (double)alpha, ad, ars, acs, bd, brs, bcs, (double)beta,
-                                 (double*)cd, C.rs, C.cs, ozaki_slices(), s);
+            int slices = ozaki_slices();
+            bool native = false;
+            if (slices == 0) {
+                // auto: the selector's proposal, checked by the error-bound verifier
+                int cfg = 0, prop = 8;
+                const double sa = host_exponent_spread((const double*)a, ta ? k : m, ta ? m : k, rs_a, cs_a);
+                const double sb = host_exponent_spread((const double*)b, tb ? n : k, tb ? k : n, rs_b, cs_b);
+                if ((rc = selector_choose(0, m, n, k, ta, tb, (int)pad, sa, sb, &cfg, &prop))) return rc;
+                int checked = prop;
+                if ((rc = gb_ozaki_verify_slices_dev(transa, transb, m, n, k, ad, A.rs, A.cs, bd, B.rs, B.cs, prop,
+                                                     256, &checked, s)))
+                    return rc;
+                slices = checked;
+                native = checked > 12;  // no slice count reaches the bound: IEEE path
+            }
+            if (native)
+                rc = dgemm_native(m, n, k, (double)alpha, ad, ars, acs, bd, brs, bcs, (double)beta, (double*)cd,
+                                  C.rs, C.cs, s);
             else
-                rc = dgemm_native(m, n, k, (double)alpha, ad, ars, acs, bd, brs, bcs, (double)beta,
-                                  (double*)cd, C.rs, C.cs, s);
+                rc = dgemm_ozaki(m, n, k, (double)alpha, ad, ars, acs, bd, brs, bcs, (double)beta, (double*)cd,
+                                 C.rs, C.cs, slices, s);
         } else {
-            rc = sgemm_dev(m, n, k, (float)alpha, reinterpret_cast<const float*>(A.origin), ars, acs,
-                           reinterpret_cast<const float*>(B.origin), brs, bcs, (float)beta,
-                           (float*)cd, C.rs, C.cs, s);
+            int cfg = 0, unused = 0;
+            if (selector_auto() && (rc = selector_choose(sizeof(T) == 8 ? 0 : 1, m, n, k, ta, tb, (int)pad, 0.0,
+                                                         0.0, &cfg, &unused)))
+                return rc;
+            rc = gemm_config_dev(sizeof(T) == 8 ? 0 : 1, cfg, m, n, k, (double)alpha, A.origin, ars, acs, B.origin,
+                                 brs, bcs, (double)beta, cd, C.rs, C.cs, s);
         }
     }
     if (rc) return rc;

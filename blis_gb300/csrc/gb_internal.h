@@ -82,6 +82,10 @@ int dgemm_native_gated(int64_t m, int64_t n, int64_t k, double alpha,
                        const double* b, int64_t brs, int64_t bcs, double beta,
                        double* c, int64_t rs_c, int64_t cs_c, const int* gate, cudaStream_t s);
 double ozaki_t_bound_log2(int s, int64_t k);
+bool selector_auto();
+int selector_choose(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad, double sa, double sb,
+                    int* config, int* slices);
+double host_exponent_spread(const double* x, int64_t rows, int64_t cols, int64_t rs, int64_t cs);
 int gemm_config_dev(int dtype, int config, int64_t m, int64_t n, int64_t k, double alpha,
                     const void* a, int64_t ars, int64_t acs, const void* b, int64_t brs, int64_t bcs,
                     double beta, void* c, int64_t rs_c, int64_t cs_c, cudaStream_t s);

@@ -178,8 +178,8 @@ int gb_set_dgemm_mode(int mode, int slices)
 {
     if (mode != GB_DGEMM_NATIVE && mode != GB_DGEMM_OZAKI)
         return gb::set_error(GB_ERR_ARG, "gb_set_dgemm_mode", "mode must be GB_DGEMM_NATIVE or GB_DGEMM_OZAKI");
-    if (mode == GB_DGEMM_OZAKI && (slices < 2 || slices > 12))
-        return gb::set_error(GB_ERR_ARG, "gb_set_dgemm_mode", "slices must be in [2, 12]");
+    if (mode == GB_DGEMM_OZAKI && slices != 0 && (slices < 2 || slices > 12))
+        return gb::set_error(GB_ERR_ARG, "gb_set_dgemm_mode", "slices must be 0 (automatic) or in [2, 12]");
     gb::g_dgemm_mode = mode;
     if (mode == GB_DGEMM_OZAKI) gb::g_ozaki_slices = slices;
     return GB_SUCCESS;

@@ -1,0 +1,204 @@
+// gb_selector.cu -- the learned configuration selector inside the library.
+//
+// A trained MLP (gb_mlp.cu) is loaded from a checked binary blob; for a GEMM
+// shape it predicts the log-time of every configuration of
+// gb_gemm_config_dev and the Ozaki slice count.  Host entry points use it
+// when auto-selection is on: the configuration of least predicted time,
+// and in the Ozaki "auto" mode the proposed slice count, checked by the
+// error-bound verifier and raised if it fails.  Inference runs on the GPU
+// (one sample per new shape; results are cached per shape).  Without a
+// model, the small-problem rule of BLIS's sup thresholds applies
+// (frame/base/bli_cntx.h:186-193).
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <unordered_map>
+
+#include "gb_internal.h"
+
+namespace gb {
+namespace {
+
+constexpr double kWorkCap = 34359738368.0;  // 2^35 flops: above the trained range use config 0
+std::mutex g_mu;
+float* g_params = nullptr;  // device copy of the MLP parameters
+float* g_io = nullptr;      // device scratch: 16 features + 8 outputs
+bool g_loaded = false;
+bool g_auto = false;
+std::unordered_map<uint64_t, uint64_t> g_cache;
+
+uint32_t crc32_bytes(const unsigned char* p, size_t n)
+{
+    uint32_t c = 0xFFFFFFFFu;
+    for (size_t i = 0; i < n; ++i) {
+        c ^= p[i];
+        for (int b = 0; b < 8; ++b) c = (c >> 1) ^ (0xEDB88320u & (0u - (c & 1u)));
+    }
+    return c ^ 0xFFFFFFFFu;
+}
+
+// Same feature map as blis_gb300/selector.py:features().
+void features(float* f, int64_t m, int64_t n, int64_t k, int dtype, int ta, int tb, int pad, double sa, double sb)
+{
+    for (int i = 0; i < GB_MLP_IN; ++i) f[i] = 0.0f;
+    f[0] = (float)(log2((double)m + 1) / 15.0);
+    f[1] = (float)(log2((double)n + 1) / 15.0);
+    f[2] = (float)(log2((double)k + 1) / 15.0);
+    f[3 + (dtype == 0 ? 0 : (dtype == 1 ? 1 : 2))] = 1.0f;
+    f[6] = (float)ta;
+    f[7] = (float)tb;
+    f[8 + (pad >= 64 ? 2 : (pad >= 8 ? 1 : 0))] = 1.0f;
+    f[11] = (float)(sa / 40.0);
+    f[12] = (float)(sb / 40.0);
+    f[13] = (float)(log2((double)m * (double)n + 1) / 30.0);
+    f[14] = (float)(log2((double)m * (double)n * (double)k + 1) / 45.0);
+    f[15] = (m < n ? m : n) <= 64 ? 1.0f : 0.0f;
+}
+
+uint64_t key_of(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad, int qa, int qb)
+{
+    uint64_t h = 1469598103934665603ull;
+    const uint64_t v[9] = {(uint64_t)dtype, (uint64_t)m, (uint64_t)n, (uint64_t)k, (uint64_t)ta,
+                           (uint64_t)tb, (uint64_t)pad, (uint64_t)qa, (uint64_t)qb};
+    for (uint64_t x : v) {
+        h ^= x + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+}  // namespace
+
+int selector_heuristic(int64_t m, int64_t n, int64_t k)
+{
+    return ((m < n ? m : n) < 201 || k < 201) ? 1 : 0;
+}
+
+bool selector_auto() { return g_auto && g_loaded; }
+
+// Config (0..GB_GEMM_NUM_CONFIGS-1) and proposed Ozaki slice count for a shape.
+int selector_choose(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad, double sa, double sb,
+                    int* config, int* slices)
+{
+    *config = selector_heuristic(m, n, k);
+    *slices = 8;
+    if (!g_loaded) return GB_SUCCESS;
+    if (2.0 * (double)m * (double)n * (double)k > kWorkCap) {
+        *config = 0;
+        return GB_SUCCESS;
+    }
+    const uint64_t key = key_of(dtype, m, n, k, ta, tb, pad, (int)lround(sa), (int)lround(sb));
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_cache.find(key);
+    if (it != g_cache.end()) {
+        *config = (int)(it->second & 0xFF);
+        *slices = (int)(it->second >> 8);
+        return GB_SUCCESS;
+    }
+    float host[GB_MLP_IN + GB_MLP_OUT];
+    features(host, m, n, k, dtype, ta, tb, pad, sa, sb);
+    cudaStream_t s = thread_stream();
+    GB_CUDA(cudaMemcpyAsync(g_io, host, sizeof(float) * GB_MLP_IN, cudaMemcpyHostToDevice, s));
+    int rc = gb_mlp_forward_dev(g_params, g_io, 1, g_io + GB_MLP_IN, s);
+    if (rc) return rc;
+    GB_CUDA(cudaMemcpyAsync(host + GB_MLP_IN, g_io + GB_MLP_IN, sizeof(float) * GB_MLP_OUT, cudaMemcpyDeviceToHost,
+                            s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    const float* out = host + GB_MLP_IN;
+    int best = 0;
+    for (int c = 1; c < GB_GEMM_NUM_CONFIGS; ++c)
+        if (out[c] < out[best]) best = c;
+    int sl = (int)ceil(out[GB_GEMM_NUM_CONFIGS] * 12.0 - 0.25);
+    sl = sl < 2 ? 2 : (sl > 12 ? 12 : sl);
+    *config = best;
+    *slices = sl;
+    g_cache[key] = (uint64_t)best | ((uint64_t)sl << 8);
+    return GB_SUCCESS;
+}
+
+// Binary exponent half-range over a strided sample of a host matrix, the
+// statistic the selector was trained on.
+double host_exponent_spread(const double* x, int64_t rows, int64_t cols, int64_t rs, int64_t cs)
+{
+    if (rows <= 0 || cols <= 0) return 0.0;
+    const int64_t total = rows * cols;
+    const int64_t step = total > 4096 ? total / 4096 : 1;
+    int lo = 100000, hi = -100000;
+    for (int64_t e = 0; e < total; e += step) {
+        const double v = x[(e % rows) * rs + (e / rows) * cs];
+        if (v == 0.0 || !isfinite(v)) continue;
+        int ex;
+        frexp(v, &ex);
+        lo = ex < lo ? ex : lo;
+        hi = ex > hi ? ex : hi;
+    }
+    return hi >= lo ? 0.5 * (hi - lo) : 0.0;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+int gb_selector_load(const float* params, int nparams)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (!params || nparams != GB_MLP_NPARAMS)
+        return set_error(GB_ERR_ARG, "gb_selector_load", "expected GB_MLP_NPARAMS parameters");
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_params) {
+        GB_CUDA(cudaMalloc(&g_params, sizeof(float) * GB_MLP_NPARAMS));
+        GB_CUDA(cudaMalloc(&g_io, sizeof(float) * (GB_MLP_IN + GB_MLP_OUT)));
+    }
+    GB_CUDA(cudaMemcpy(g_params, params, sizeof(float) * GB_MLP_NPARAMS, cudaMemcpyHostToDevice));
+    g_cache.clear();
+    g_loaded = true;
+    return GB_SUCCESS;
+}
+
+int gb_selector_load_file(const char* path)
+{
+    FILE* f = path ? fopen(path, "rb") : nullptr;
+    if (!f) return set_error(GB_ERR_ARG, "gb_selector_load_file", "cannot open model file");
+    char magic[8];
+    uint32_t hdr[3];
+    float* p = new float[GB_MLP_NPARAMS];
+    const bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "GBSELMLP", 8) == 0 &&
+                    fread(hdr, sizeof(uint32_t), 3, f) == 3 && hdr[0] == 1 && hdr[1] == GB_MLP_NPARAMS &&
+                    fread(p, sizeof(float), GB_MLP_NPARAMS, f) == GB_MLP_NPARAMS &&
+                    crc32_bytes(reinterpret_cast<const unsigned char*>(p), sizeof(float) * GB_MLP_NPARAMS) == hdr[2];
+    fclose(f);
+    int rc = ok ? gb_selector_load(p, GB_MLP_NPARAMS)
+                : set_error(GB_ERR_ARG, "gb_selector_load_file", "bad magic, version, size or checksum");
+    delete[] p;
+    return rc;
+}
+
+int gb_selector_unload(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_loaded = false;
+    g_cache.clear();
+    return GB_SUCCESS;
+}
+
+int gb_set_gemm_autoselect(int on)
+{
+    g_auto = on != 0;
+    return GB_SUCCESS;
+}
+
+int gb_selector_choose(int dtype, gb_dim_t m, gb_dim_t n, gb_dim_t k, int transa, int transb, int pad,
+                       double spread_a, double spread_b, int* config, int* slices)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (!config || !slices) return set_error(GB_ERR_ARG, "gb_selector_choose", "null output");
+    return selector_choose(dtype, m, n, k, transa ? 1 : 0, transb ? 1 : 0, pad, spread_a, spread_b, config, slices);
+}
+
+}  // extern "C"

@@ -346,6 +346,30 @@ def save_model(path, params, meta):
         json.dump(doc, f)
 
 
+BIN_MAGIC = b"GBSELMLP"
+
+
+def save_model_bin(path, params):
+    """The binary form read by gb_selector_load_file: magic, version 1,
+    parameter count, CRC-32 of the float32 parameters, parameters."""
+    import struct
+    import zlib
+    p = np.asarray(params, "<f4")
+    blob = p.tobytes()
+    with open(path, "wb") as f:
+        f.write(BIN_MAGIC + struct.pack("<III", 1, p.size, zlib.crc32(blob) & 0xFFFFFFFF) + blob)
+
+
+DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning", "selector_mlp.bin")
+
+
+def load_into_library(path=DEFAULT_MODEL, autoselect=True):
+    """Load the binary model into libblis_gb300 and turn auto-selection on."""
+    L = _lib.load()
+    _lib.check(L.gb_selector_load_file(path.encode()), "gb_selector_load_file")
+    L.gb_set_gemm_autoselect(1 if autoselect else 0)
+
+
 def load_model(path):
     with open(path) as f:
         doc = json.load(f)
@@ -401,6 +425,7 @@ def _main():
         d = np.load(a.data)
         p, curve = train(d["X"], d["Y"], d["M"], epochs=a.epochs, log=print)
         save_model(a.out, p, {"train_samples": int(d["X"].shape[0]), "final_loss": curve[-1]})
+        save_model_bin(os.path.splitext(a.out)[0] + ".bin", p)
     else:
         p, _ = load_model(a.model)
         print(json.dumps(evaluate(p, np.load(a.data)), indent=1))

@@ -396,6 +396,22 @@ int gb_ozaki_verify_slices_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m,
                                const double* b, gb_inc_t rs_b, gb_inc_t cs_b, int s_min,
                                int nsample, int* s_out, void* stream);
 
+/* The selector inside the library.  gb_selector_load takes GB_MLP_NPARAMS
+   host floats; gb_selector_load_file reads the binary model written by
+   blis_gb300/selector.py (magic "GBSELMLP", version 1, parameter count,
+   CRC-32 of the parameters, parameters).  With gb_set_gemm_autoselect(1)
+   and a model loaded, the host GEMM entry points (dgemm_, sgemm_,
+   bli_?gemm, gb_?gemm) run the configuration of least predicted time; the
+   Ozaki mode with slices = 0 takes the model's slice proposal, raised by
+   gb_ozaki_verify_slices_dev where it fails.  Without a model the BLIS sup
+   threshold rule is used.  gb_selector_choose exposes the decision. */
+int gb_selector_load(const float* params, int nparams);
+int gb_selector_load_file(const char* path);
+int gb_selector_unload(void);
+int gb_set_gemm_autoselect(int on);
+int gb_selector_choose(int dtype, gb_dim_t m, gb_dim_t n, gb_dim_t k, int transa, int transb, int pad,
+                       double spread_a, double spread_b, int* config, int* slices);
+
 /* ===================================================================== */
 /* 3. Controls and introspection                                           */
 /* ===================================================================== */
@@ -404,7 +420,9 @@ int gb_ozaki_verify_slices_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m,
 int gb_init(int device);
 
 /* Routes dgemm_ / cblas_dgemm / bli_dgemm through the native FP64 kernel
-   (GB_DGEMM_NATIVE) or the Ozaki split form with the given slice count. */
+   (GB_DGEMM_NATIVE) or the Ozaki split form with the given slice count
+   (2..12), or with slices = 0 the count chosen per call by the selector and
+   the error-bound verifier (the native kernel when no count reaches it). */
 #define GB_DGEMM_NATIVE 0
 #define GB_DGEMM_OZAKI 1
 int gb_set_dgemm_mode(int mode, int slices);

@@ -112,3 +112,45 @@ def test_tune_train_evaluate_cycle(gblib, tmp_path):
     sel = S.Selector(path)
     cfg, sl = sel.choose(300, 20, 4000, 0)
     assert 0 <= cfg < S.NCONFIG and 2 <= sl <= 12
+
+
+def test_library_selector_matches_python_and_autoselect_is_correct(gblib):
+    import ctypes as C
+    from blis_gb300 import blas
+    from oracle import pyoracle as po
+    from tests import helpers as H
+    p, _ = S.load_model(S.DEFAULT_MODEL.replace(".bin", ".json"))
+    sel = S.Selector(S.DEFAULT_MODEL.replace(".bin", ".json"))
+    S.load_into_library()
+    try:
+        cfg, sl = C.c_int(), C.c_int()
+        for (m, n, k, dt) in [(6, 800, 800, 0), (300, 300, 300, 1), (2000, 40, 9000, 0), (100, 3000, 64, 1)]:
+            assert gblib.gb_selector_choose(dt, m, n, k, 0, 0, 0, 0.0, 0.0, C.byref(cfg), C.byref(sl)) == 0
+            assert (cfg.value, sl.value) == sel.choose(m, n, k, dt)
+        # auto-selected configurations through dgemm_ stay within the testsuite residual
+        for (m, n, k) in [(6, 800, 800), (129, 65, 4000), (500, 500, 500)]:
+            a = H.normalize(po.uniform((m, k), 1))
+            b = H.normalize(po.uniform((k, n), 2))
+            c0 = H.normalize(po.uniform((m, n), 3))
+            c = np.asfortranarray(c0.copy())
+            blas.dgemm("N", "N", m, n, k, 2.0, a, m, b, k, 1.2, c, m)
+            assert H.gemm_residual(2.0, a, b, 1.2, c0, c) < 1e-14
+        # Ozaki with automatic slices: the verifier-checked count, at most native error
+        n = 512
+        a = po.expspread((n, 4096), 5)
+        b = po.expspread((4096, n), 6)
+        blas.set_dgemm_mode(blas.DGEMM_OZAKI, 0)
+        c_oz = np.zeros((n, n), order="F")
+        blas.dgemm("N", "N", n, n, 4096, 1.0, a, n, b, 4096, 0.0, c_oz, n)
+        blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+        c_nat = np.zeros((n, n), order="F")
+        blas.dgemm("N", "N", n, n, 4096, 1.0, a, n, b, 4096, 0.0, c_nat, n)
+        rng = np.random.default_rng(0)
+        ii, jj = rng.integers(0, n, 2048), rng.integers(0, n, 2048)
+        hi, lo = po.dd_gemm_entries(0, 0, 1.0, a, b, 0.0, c_oz, ii, jj)
+        assert po.componentwise_error(c_oz[ii, jj], hi, lo) <= po.componentwise_error(c_nat[ii, jj], hi, lo)
+    finally:
+        gblib.gb_set_gemm_autoselect(0)
+        gblib.gb_selector_unload()
+        blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+    del p

@@ -1,0 +1,65 @@
+"""Selector host logic without a GPU: feature map, threshold rule, model
+persistence and the checks gb_selector_load_file makes before any device
+work (magic, version, size, CRC-32)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from blis_gb300 import _lib
+from blis_gb300 import selector as S
+
+TUNING = os.path.join(os.path.dirname(__file__), "..", "blis_gb300", "tuning")
+
+
+def test_features_and_rule():
+    f = S.features(300, 20, 4000, 0, 1, 0, 8, 10.0, 0.0)
+    assert f.shape == (S.NIN,) and f.dtype == np.float32
+    assert f[3] == 1 and f[6] == 1 and f[9] == 1 and f[15] == 1
+    assert S.heuristic_config(300, 300, 300) == 0
+    assert S.heuristic_config(6, 800, 800) == 1
+
+
+def test_sampled_shapes_respect_caps():
+    shapes = S.sample_shapes(500, seed=9)
+    for sh in shapes:
+        assert 2.0 * sh["m"] * sh["n"] * sh["k"] <= S.WORK_CAP
+        assert max(sh["m"] * sh["k"], sh["k"] * sh["n"], sh["m"] * sh["n"]) <= S.ELEM_CAP
+        assert sh["pad"] in S.PADS
+
+
+def test_committed_model_and_evaluation():
+    p, doc = S.load_model(os.path.join(TUNING, "selector_mlp.json"))
+    assert p.size == S.NPARAMS and doc["meta"]["train_samples"] == 10000
+    ev = json.load(open(os.path.join(TUNING, "selector_eval_heldout.json")))
+    assert ev["n"] == 2000
+    assert ev["mlp"]["mean_throughput_regret"] <= 0.05
+    assert ev["mlp"]["mean_throughput_regret"] < ev["threshold_rule"]["mean_throughput_regret"]
+    assert ev["slices"]["violations_after_verifier"] == 0
+    raw = open(os.path.join(TUNING, "selector_mlp.bin"), "rb").read()
+    assert raw[:8] == S.BIN_MAGIC and np.array_equal(np.frombuffer(raw[20:], "<f4"), p)
+
+
+def test_load_file_rejects_corrupt_models(gblib, tmp_path):
+    p, _ = S.load_model(os.path.join(TUNING, "selector_mlp.json"))
+    good = tmp_path / "good.bin"
+    S.save_model_bin(str(good), p)
+    raw = bytearray(good.read_bytes())
+    raw[100] ^= 0x40  # flip a parameter bit: CRC mismatch
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(bytes(raw))
+    assert gblib.gb_selector_load_file(str(bad).encode()) != 0
+    trunc = tmp_path / "trunc.bin"
+    trunc.write_bytes(bytes(raw[:1000]))
+    assert gblib.gb_selector_load_file(str(trunc).encode()) != 0
+    assert gblib.gb_selector_load_file(str(tmp_path / "missing.bin").encode()) != 0
+    gblib.gb_clear_last_error()
+    with pytest.raises(ValueError):
+        doc = json.load(open(os.path.join(TUNING, "selector_mlp.json")))
+        doc["params"][0] += 1.0
+        path = tmp_path / "m.json"
+        path.write_text(json.dumps(doc))
+        S.load_model(str(path))
+    code, _ = _lib.last_error()
+    assert code == 0
