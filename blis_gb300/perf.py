@@ -38,6 +38,11 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def _stream():
+    import torch
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream or 1)
+
+
 def _timer(fn, reps=5, warmup=2):
     import torch
     for _ in range(warmup):
@@ -171,8 +176,9 @@ def run_batch(out):
         probs, keep, flops = batch_problems(4096, 4, dtype)
         plan = C.c_void_p()
         _lib.check(L.gb_batch_plan_create(C.addressof(probs), 4096, dtype, C.byref(plan)), "plan")
-        ms_g = _timer(lambda: _lib.check(L.gb_batch_plan_run(plan, 1, None), "run"), reps=3, warmup=1)
-        ms_l = _timer(lambda: _lib.check(L.gb_gemm_batch_dev(C.addressof(probs), 4096, dtype, 1, None), "loop"),
+        st = _stream()  # the library works on the stream the events are recorded on
+        ms_g = _timer(lambda: _lib.check(L.gb_batch_plan_run(plan, 1, st), "run"), reps=3, warmup=1)
+        ms_l = _timer(lambda: _lib.check(L.gb_gemm_batch_dev(C.addressof(probs), 4096, dtype, 1, st), "loop"),
                       reps=1, warmup=1)
         L.gb_batch_plan_destroy(plan)
         out.append({"workload": "batch_4096_%s" % name, "flops": flops, "grouped_graph_ms": ms_g,
