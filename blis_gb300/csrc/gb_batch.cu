@@ -38,8 +38,9 @@ struct BatchDesc {
 template <typename T, bool DMMA>
 __global__ void __launch_bounds__(NT) grouped_gemm_kernel(const BatchDesc* __restrict__ d, int nprob,
                                                           int64_t total_tiles,
-                                                          unsigned long long* counter)
+                                                          unsigned long long* counter, const int* gate)
 {
+    if (gate && *gate == 0) return;  // fallback launch of the Ozaki form: only on Inf/NaN operands
     __shared__ T As[BK * LDS];
     __shared__ T Bs[BK * LDS];
     __shared__ long long tile_s;
@@ -68,8 +69,13 @@ __global__ void __launch_bounds__(NT) grouped_gemm_kernel(const BatchDesc* __res
 }  // namespace
 
 // A resident batch: descriptor table in HBM, tile counter, optional graph.
+// The Ozaki form (GB_BATCH_FP64_OZAKI) adds the grouped Ozaki tables and
+// arenas; this plan's own table then holds the same problems for the native
+// launch gated on the Ozaki form's Inf/NaN flag, `rest` the problems with
+// k == 0 or alpha == 0 (C := beta C) and `singles` those with a k too long
+// for the grouped form.
 struct BatchPlan {
-    int dtype;  // 0 = FP64, 1 = FP32
+    int dtype;  // GB_BATCH_FP64, GB_BATCH_FP32, GB_BATCH_FP64_OZAKI
     int nprob;
     int64_t total_tiles;
     BatchDesc* d_desc;
@@ -77,26 +83,77 @@ struct BatchPlan {
     std::vector<BatchDesc> host;
     cudaGraphExec_t graph;
     cudaStream_t graph_stream;
+    OzBatch* oz = nullptr;
+    const int* gate = nullptr;
+    BatchPlan* rest = nullptr;
+    std::vector<gb_gemm_problem_t> singles;
+    int slices = 0;
 };
 
 static int launch_plan(BatchPlan* pl, cudaStream_t s)
 {
+    int rc;
+    if (pl->oz && (rc = ozaki_batch_launch(pl->oz, s))) return rc;
+    if (pl->rest && (rc = launch_plan(pl->rest, s))) return rc;
+    for (const gb_gemm_problem_t& p : pl->singles) {
+        const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
+        rc = dgemm_ozaki(p.m, p.n, p.k, p.alpha, (const double*)p.a, ta ? p.lda : 1, ta ? 1 : p.lda,
+                         (const double*)p.b, tb ? p.ldb : 1, tb ? 1 : p.ldb, p.beta, (double*)p.c, 1, p.ldc,
+                         pl->slices, s);
+        if (rc) return rc;
+    }
     if (pl->total_tiles == 0) return GB_SUCCESS;
     GB_CUDA(cudaMemsetAsync(pl->d_counter, 0, sizeof(unsigned long long), s));
     const int sms = sm_count() > 0 ? sm_count() : 148;
     int64_t grid = (int64_t)sms * 2;  // 2 resident CTAs of 256 threads per SM (DMMA: 240 regs)
     if (grid > pl->total_tiles) grid = pl->total_tiles;
-    LaunchScope ls(pl->dtype == 0 ? "batch_grouped_dmma" : "batch_grouped_ffma", s);
-    if (pl->dtype == 0)
+    LaunchScope ls(pl->dtype == 1 ? "batch_grouped_ffma" : (pl->gate ? "batch_grouped_dmma_gated"
+                                                                      : "batch_grouped_dmma"), s);
+    if (pl->dtype != 1)
         grouped_gemm_kernel<double, true><<<(unsigned)grid, NT, 0, s>>>(pl->d_desc, pl->nprob,
-                                                                       pl->total_tiles, pl->d_counter);
+                                                                       pl->total_tiles, pl->d_counter, pl->gate);
     else
         grouped_gemm_kernel<float, false><<<(unsigned)grid, NT, 0, s>>>(pl->d_desc, pl->nprob,
-                                                                       pl->total_tiles, pl->d_counter);
+                                                                       pl->total_tiles, pl->d_counter, nullptr);
     return check_cuda(cudaGetLastError(), "grouped_gemm");
 }
 
+void batch_plan_destroy(BatchPlan* pl);
+static int batch_plan_build(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out);
+
 int batch_plan_create(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out)
+{
+    *out = nullptr;
+    if (dtype != GB_BATCH_FP64_OZAKI) return batch_plan_build(probs, count, dtype, out);
+    int slices = ozaki_slices();
+    if (slices < 2) slices = 8;  // automatic: the verifier is per problem; the batch uses 8
+    std::vector<gb_gemm_problem_t> grouped, rest, singles;
+    for (int64_t i = 0; i < count; ++i) {
+        const gb_gemm_problem_t& p = probs[i];
+        if (p.m < 0 || p.n < 0 || p.k < 0) return set_error(GB_ERR_ARG, "gb_batch", "negative dimension");
+        if (p.m == 0 || p.n == 0) continue;
+        if (p.k == 0 || p.alpha == 0.0) rest.push_back(p);
+        else if (ozaki_batch_accepts(p.k, slices)) grouped.push_back(p);
+        else singles.push_back(p);
+    }
+    BatchPlan* pl = nullptr;
+    int rc = batch_plan_build(grouped.data(), (int64_t)grouped.size(), GB_BATCH_FP64, &pl);
+    if (rc) return rc;
+    pl->dtype = GB_BATCH_FP64_OZAKI;
+    pl->slices = slices;
+    pl->singles = singles;
+    cudaStream_t s = thread_stream();
+    if ((rc = ozaki_batch_create(grouped.data(), (int64_t)grouped.size(), slices, s, &pl->oz)) ||
+        (!rest.empty() && (rc = batch_plan_build(rest.data(), (int64_t)rest.size(), GB_BATCH_FP64, &pl->rest)))) {
+        batch_plan_destroy(pl);
+        return rc;
+    }
+    pl->gate = ozaki_batch_flag(pl->oz);
+    *out = pl;
+    return GB_SUCCESS;
+}
+
+static int batch_plan_build(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out)
 {
     *out = nullptr;
     BatchPlan* pl = new BatchPlan();
@@ -158,7 +215,8 @@ int batch_plan_create(const gb_gemm_problem_t* probs, int64_t count, int dtype, 
 
 int batch_plan_run(BatchPlan* pl, cudaStream_t s, bool use_graph)
 {
-    if (!use_graph) return launch_plan(pl, s);
+    // problems run one by one through the Ozaki form allocate workspace per call: no graph
+    if (!use_graph || !pl->singles.empty()) return launch_plan(pl, s);
     if (!pl->graph) {
         cudaStream_t cap;
         GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -188,7 +246,9 @@ void batch_plan_destroy(BatchPlan* pl)
     if (pl->graph_stream) cudaStreamDestroy(pl->graph_stream);
     dev_free(pl->d_desc, s);
     dev_free(pl->d_counter, s);
+    ozaki_batch_destroy(pl->oz, s);
     cudaStreamSynchronize(s);
+    batch_plan_destroy(pl->rest);
     delete pl;
 }
 
@@ -199,7 +259,13 @@ int batch_loop(const gb_gemm_problem_t* probs, int64_t count, int dtype, cudaStr
         const gb_gemm_problem_t& p = probs[i];
         const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
         int rc;
-        if (dtype == 0)
+        if (dtype == GB_BATCH_FP64_OZAKI) {
+            int slices = ozaki_slices();
+            if (slices < 2) slices = 8;
+            rc = dgemm_ozaki(p.m, p.n, p.k, p.alpha, (const double*)p.a, ta ? p.lda : 1, ta ? 1 : p.lda,
+                             (const double*)p.b, tb ? p.ldb : 1, tb ? 1 : p.ldb, p.beta, (double*)p.c, 1, p.ldc,
+                             slices, s);
+        } else if (dtype == GB_BATCH_FP64)
             rc = dgemm_native(p.m, p.n, p.k, p.alpha, (const double*)p.a, ta ? p.lda : 1, ta ? 1 : p.lda,
                               (const double*)p.b, tb ? p.ldb : 1, tb ? 1 : p.ldb, p.beta, (double*)p.c, 1,
                               p.ldc, s);
@@ -327,7 +393,10 @@ void batch_blas(const char* name, const char* transa_array, const char* transb_a
         probs.push_back(p);
     }
     BatchPlan* pl = nullptr;
-    int rc = batch_plan_create(probs.data(), (int64_t)probs.size(), sizeof(T) == 8 ? 0 : 1, &pl);
+    // dgemm_batch_ follows the precision mode of dgemm_ (gb_set_dgemm_mode)
+    const int dtype = sizeof(T) == 4 ? GB_BATCH_FP32
+                                     : (dgemm_mode() == GB_DGEMM_OZAKI ? GB_BATCH_FP64_OZAKI : GB_BATCH_FP64);
+    int rc = batch_plan_create(probs.data(), (int64_t)probs.size(), dtype, &pl);
     if (!rc) rc = batch_plan_run(pl, s, false);
     if (!rc) {
         for (auto& h : hs) {
@@ -401,7 +470,8 @@ int gb_gemm_batch_dev(const gb_gemm_problem_t* probs, gb_dim_t count, int dtype,
     int rc = ensure_init();
     if (rc) return rc;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : thread_stream();
-    if (dtype != 0 && dtype != 1) return set_error(GB_ERR_ARG, "gb_gemm_batch_dev", "dtype must be 0 (FP64) or 1 (FP32)");
+    if (dtype != GB_BATCH_FP64 && dtype != GB_BATCH_FP32 && dtype != GB_BATCH_FP64_OZAKI)
+        return set_error(GB_ERR_ARG, "gb_gemm_batch_dev", "dtype must be GB_BATCH_FP64, FP32 or FP64_OZAKI");
     if (mode == GB_BATCH_LOOP) return batch_loop(probs, count, dtype, s);
     BatchPlan* pl = nullptr;
     if ((rc = batch_plan_create(probs, count, dtype, &pl))) return rc;
@@ -415,7 +485,8 @@ int gb_batch_plan_create(const gb_gemm_problem_t* probs, gb_dim_t count, int dty
 {
     int rc = ensure_init();
     if (rc) return rc;
-    if (dtype != 0 && dtype != 1) return set_error(GB_ERR_ARG, "gb_batch_plan_create", "dtype must be 0 or 1");
+    if (dtype != GB_BATCH_FP64 && dtype != GB_BATCH_FP32 && dtype != GB_BATCH_FP64_OZAKI)
+        return set_error(GB_ERR_ARG, "gb_batch_plan_create", "dtype must be GB_BATCH_FP64, FP32 or FP64_OZAKI");
     BatchPlan* pl = nullptr;
     rc = batch_plan_create(probs, count, dtype, &pl);
     *plan = pl;

@@ -101,6 +101,17 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
               const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b,
               int64_t cs_b, int slices, cudaStream_t s);
 int64_t ozaki_kpart_limit(int slices);
+// Grouped Ozaki form for gemm_batch (gb_ozaki.cu): every accepted problem
+// (m, n, k > 0, alpha != 0, ozaki_batch_accepts) in three launches.  The
+// flag is raised when an operand holds Inf/NaN; the launches then do
+// nothing and a native grouped launch gated on the flag must follow.
+struct OzBatch;
+bool ozaki_batch_accepts(int64_t k, int slices);
+int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices, cudaStream_t s,
+                       OzBatch** out);
+int ozaki_batch_launch(OzBatch* ob, cudaStream_t s);
+const int* ozaki_batch_flag(const OzBatch* ob);
+void ozaki_batch_destroy(OzBatch* ob, cudaStream_t s);
 int dotv_nparts(int64_t n);
 int scal_matrix(int64_t m, int64_t n, double beta, double* c, int64_t rs_c, int64_t cs_c,
                 cudaStream_t s);

@@ -35,6 +35,9 @@
 #include <cuda_bf16.h>
 #include <stdlib.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "gb_internal.h"
 #include "gb_sm100.cuh"
 
@@ -73,6 +76,41 @@ struct OzGemmParams {
 
 struct OzItem {
     int lev, npairs, pa_lo, tm, tn, kb0, kbn, plane;
+    int prob;  // grouped form only: index into the problem table
+};
+
+// Grouped form (gemm_batch): every problem's slices live in one arena of
+// 64-deep k blocks ("boxes": 128 rows x 64 k of A = 16 KB, 256 rows x 64 k
+// of B = 32 KB, contiguous, the layout a 128-byte-swizzled TMA box expects),
+// so one 3-D tensor map per operand serves all problems; a box is addressed
+// by its index alone.  Level sums go to per-problem planes [level][n][ld].
+struct OzBatchProb {
+    const double* a;
+    int64_t ars, acs;  // rows of op(A): (i, l) at a[i*ars + l*acs]
+    const double* b;
+    int64_t brs, bcs;  // rows of op(B)^T: (j, l) at b[j*brs + l*bcs]
+    double* c;
+    int64_t rs_c, cs_c;
+    double alpha, beta;
+    int64_t m, n, k;
+    int32_t tiles_m, tiles_n, kb, pad0;
+    int32_t* ea;  // row exponents of op(A), op(B)^T
+    int32_t* eb;
+    int64_t abox, bbox;  // first box of this problem in one slice plane
+    int32_t* planes;     // [level][n][ld], ld = m rounded up to 4
+    int64_t ld;
+    int64_t units_a;     // split units (32-row blocks) of op(A); op(B)^T's follow
+};
+
+struct OzBatchParams {
+    int slices, nlevels, chunk_kb, nprob;
+    int64_t items, boxes_a, boxes_b;  // work items; boxes per slice plane
+    const OzBatchProb* probs;
+    const int32_t* item_prob;  // work item -> problem
+    const int64_t* item_base;  // first work item of each problem
+    unsigned int* status;
+    const int* skip;
+    OzLevel lv[OZ_MAX_SLICES];
 };
 
 __device__ __forceinline__ OzItem oz_decode(const OzGemmParams& p, int64_t it)
@@ -101,18 +139,93 @@ __device__ __forceinline__ OzItem oz_decode(const OzGemmParams& p, int64_t it)
     const int kb_end = (w.kb0 + lv.kb_per_part < p.kb_total) ? w.kb0 + lv.kb_per_part : p.kb_total;
     w.kbn = kb_end - w.kb0;
     w.plane = lv.plane_base + part;
+    w.prob = 0;
     return w;
 }
 
-__device__ __forceinline__ void oz_fail(const OzGemmParams& p, volatile int* abort_flag)
+// Grouped form: items are (problem, level, tile) with levels heaviest first
+// inside a problem; one part per level (the host keeps npairs * k small
+// enough).  Tiles of a problem in column-major raster.
+__device__ __forceinline__ OzItem oz_decode(const OzBatchParams& p, int64_t it)
+{
+    const int pi = __ldg(p.item_prob + it);
+    const OzBatchProb& q = p.probs[pi];
+    const int64_t tiles = (int64_t)q.tiles_m * q.tiles_n;
+    const int64_t rem = it - __ldg(p.item_base + pi);
+    const int L = (int)(rem / tiles);
+    const int64_t t = rem - (int64_t)L * tiles;
+    const OzLevel& lv = p.lv[L];
+    OzItem w;
+    w.lev = lv.lev;
+    w.npairs = lv.npairs;
+    w.pa_lo = lv.pa_lo;
+    w.tm = (int)(t % q.tiles_m);
+    w.tn = (int)(t / q.tiles_m);
+    w.kb0 = 0;
+    w.kbn = q.kb;
+    w.plane = L;
+    w.prob = pi;
+    return w;
+}
+
+// One k block of the pair (A_pa, B_pb) into a stage.
+__device__ __forceinline__ void oz_load_stage(const OzGemmParams&, const CUtensorMap* ma, const CUtensorMap* mb,
+                                              uint8_t* sa, uint8_t* sb, uint64_t* bar, const OzItem& w, int pa,
+                                              int pb, int kb)
+{
+    const int kx = (w.kb0 + kb) * OZ_BK;
+    tma_load_3d(sa, ma, bar, kx, w.tm * OZ_BM, pa - 1);
+    tma_load_3d(sb, mb, bar, kx, w.tn * OZ_BN, pb - 1);
+}
+
+__device__ __forceinline__ void oz_load_stage(const OzBatchParams& p, const CUtensorMap* ma,
+                                              const CUtensorMap* mb, uint8_t* sa, uint8_t* sb, uint64_t* bar,
+                                              const OzItem& w, int pa, int pb, int kb)
+{
+    const OzBatchProb& q = p.probs[w.prob];
+    const int64_t za = (int64_t)(pa - 1) * p.boxes_a + q.abox + (int64_t)w.tm * q.kb + kb;
+    const int64_t zb = (int64_t)(pb - 1) * p.boxes_b + q.bbox + (int64_t)w.tn * q.kb + kb;
+    tma_load_3d(sa, ma, bar, 0, 0, (int)za);
+    tma_load_3d(sb, mb, bar, 0, 0, (int)zb);
+}
+
+// Level sums of one epilogue thread (row quad*32 + lane, columns half*128 ..
+// +127 of the tile) into the level plane.
+__device__ __forceinline__ void oz_store_sums(const OzGemmParams& p, const OzItem& w, int quad, int half,
+                                              int lane, const int32_t (&acc)[128])
+{
+    const int64_t i = (int64_t)w.tm * OZ_BM + quad * 32 + lane;
+    const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
+    int32_t* dst = p.planes + ((int64_t)w.plane * p.npad + j0) * p.mpad + i;
+#pragma unroll
+    for (int c = 0; c < 128; ++c) dst[(int64_t)c * p.mpad] = acc[c];
+}
+
+__device__ __forceinline__ void oz_store_sums(const OzBatchParams& p, const OzItem& w, int quad, int half,
+                                              int lane, const int32_t (&acc)[128])
+{
+    const OzBatchProb& q = p.probs[w.prob];
+    const int64_t i = (int64_t)w.tm * OZ_BM + quad * 32 + lane;
+    const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
+    if (i >= q.m) return;
+    int32_t* dst = q.planes + ((int64_t)w.plane * q.n + j0) * q.ld + i;
+    const int64_t jn = q.n - j0;  // columns of this half that exist
+#pragma unroll
+    for (int c = 0; c < 128; ++c)
+        if (c < jn) dst[(int64_t)c * q.ld] = acc[c];
+}
+
+template <class P>
+__device__ __forceinline__ void oz_fail(const P& p, volatile int* abort_flag)
 {
     atomicOr(p.status, DEV_WAIT_TIMEOUT);
     *abort_flag = 1;
 }
 
+template <class P>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     ozaki_slice_gemm_kernel(const __grid_constant__ CUtensorMap map_a,
-                            const __grid_constant__ CUtensorMap map_b, const __grid_constant__ OzGemmParams p)
+                            const __grid_constant__ CUtensorMap map_b, const __grid_constant__ P p)
 {
     if (*p.skip) return;  // uniform across the CTA: the native kernel takes over
     extern __shared__ uint8_t smem_raw[];
@@ -175,9 +288,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                         uint8_t* sa = smem + stage * OZ_STAGE_BYTES;
                         uint8_t* sb = sa + OZ_A_BYTES;
                         mbar_arrive_expect_tx(&full[stage], OZ_STAGE_BYTES);
-                        const int kx = (w.kb0 + kb) * OZ_BK;
-                        tma_load_3d(sa, &map_a, &full[stage], kx, w.tm * OZ_BM, pa - 1);
-                        tma_load_3d(sb, &map_b, &full[stage], kx, w.tn * OZ_BN, pb - 1);
+                        oz_load_stage(p, &map_a, &map_b, sa, sb, &full[stage], w, pa, pb, kb);
                         issued_mask |= 1u << stage;
                         last_phase = (last_phase & ~(1u << stage)) | (phase << stage);
                         if (++stage == OZ_STAGES) {
@@ -285,11 +396,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 ++chunk_ctr;
             }
             if (!ok) break;
-            const int64_t i = (int64_t)w.tm * OZ_BM + quad * 32 + lane;
-            const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
-            int32_t* dst = p.planes + ((int64_t)w.plane * p.npad + j0) * p.mpad + i;
-#pragma unroll
-            for (int c = 0; c < 128; ++c) dst[(int64_t)c * p.mpad] = acc[c];
+            oz_store_sums(p, w, quad, half, lane, acc);
         }
     }
 
@@ -826,6 +933,150 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const __grid_constant
     }
 }
 
+// ---------------------------------------------------------------- grouped form
+// Split for every problem of a batch in one launch.  A block owns 32 rows of
+// op(A_i) or op(B_i)^T over the whole k range: pass 1 takes the row maxima
+// (8 threads per row), pass 2 cuts 64-wide k blocks into digits and writes
+// them into the problem's boxes.  Rows past m (n) up to the box height and
+// k past k_i up to the block width are written as zeros.
+template <int S>
+__global__ void __launch_bounds__(256) oz_split_batch_kernel(const OzBatchProb* __restrict__ probs,
+                                                             const int32_t* __restrict__ unit_prob,
+                                                             const int64_t* __restrict__ unit_base,
+                                                             int64_t boxes_a, int64_t boxes_b,
+                                                             uint16_t* __restrict__ sa, uint16_t* __restrict__ sb,
+                                                             int* __restrict__ nonfinite)
+{
+    __shared__ double tile[32][65];
+    __shared__ unsigned long long red[8][32];
+    __shared__ int rowe[32];
+    const int pi = unit_prob[blockIdx.x];
+    const OzBatchProb& q = probs[pi];
+    int64_t u = (int64_t)blockIdx.x - unit_base[pi];
+    const bool isb = (u >= q.units_a);
+    if (isb) u -= q.units_a;
+    const int64_t rows = isb ? q.n : q.m, k = q.k;
+    const double* R = isb ? q.b : q.a;
+    const int64_t sr = isb ? q.brs : q.ars, sl = isb ? q.bcs : q.acs;
+    const int box_rows = isb ? OZ_BN : OZ_BM;
+    const int64_t r0 = u * 32;
+    const bool rows_fast = (sr == 1);
+    const int t = threadIdx.x;
+
+    // pass 1: row maxima of |x| as IEEE bits
+    {
+        const int rr = rows_fast ? (t & 31) : (t >> 3);
+        const int l0 = rows_fast ? (t >> 5) : (t & 7);
+        const int64_t r = r0 + rr;
+        unsigned long long mx = 0;
+        if (r < rows)
+            for (int64_t l = l0; l < k; l += 8) {
+                const unsigned long long b = abs_bits(__ldg(R + r * sr + l * sl));
+                mx = b > mx ? b : mx;
+            }
+        red[rows_fast ? (t >> 5) : (t & 7)][rr] = mx;
+    }
+    __syncthreads();
+    if (t < 32) {
+        unsigned long long mx = 0;
+#pragma unroll
+        for (int g = 0; g < 8; ++g) mx = red[g][t] > mx ? red[g][t] : mx;
+        int e = 0;
+        const int64_t r = r0 + t;
+        if (r < rows) {
+            int nf = 0;
+            e = oz_row_exponent(mx, &nf);
+            if (nf) *nonfinite = 1;
+            (isb ? q.eb : q.ea)[r] = e;
+        }
+        rowe[t] = e;
+    }
+    __syncthreads();
+
+    // pass 2: digits, one 32 x 64 tile at a time
+    uint16_t* out = isb ? sb : sa;
+    const int64_t boxes = isb ? boxes_b : boxes_a;
+    const int64_t box0 = (isb ? q.bbox : q.abox) + (r0 / box_rows) * q.kb;
+    const int64_t rb = (r0 % box_rows);
+    const int rr = t >> 3, c0 = (t & 7) * 8;
+    const int e = rowe[rr];
+    const bool live = (r0 + rr < rows);
+    for (int kb = 0; kb < q.kb; ++kb) {
+        const int64_t l0 = (int64_t)kb * 64;
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const int idx = t + 256 * g;
+            const int tr = rows_fast ? (idx & 31) : (idx >> 6);
+            const int tl = rows_fast ? (idx >> 5) : (idx & 63);
+            const int64_t r = r0 + tr, l = l0 + tl;
+            tile[tr][tl] = (r < rows && l < k) ? __ldg(R + r * sr + l * sl) : 0.0;
+        }
+        __syncthreads();
+        uint32_t packed[S][4];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            int d[S];
+            oz_digits<S>(live ? tile[rr][c0 + j] : 0.0, e, d);
+#pragma unroll
+            for (int p = 0; p < S; ++p) {
+                const uint32_t b = int_to_bf16_bits(d[p]);
+                if (j & 1) packed[p][j >> 1] |= b << 16;
+                else packed[p][j >> 1] = b;
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < S; ++p) {
+            const int64_t z = (int64_t)p * boxes + box0 + kb;
+            uint4* dst = reinterpret_cast<uint4*>(out + (z * box_rows + rb + rr) * 64 + c0);
+            *dst = make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
+        }
+        __syncthreads();
+    }
+}
+
+// Recombination for every problem of a batch in one launch: blocks are
+// assigned to problems by a table, each thread takes 4 rows of one column.
+template <int S>
+__global__ void __launch_bounds__(256) oz_recombine_batch_kernel(const OzBatchProb* __restrict__ probs,
+                                                                 const int32_t* __restrict__ block_prob,
+                                                                 const int64_t* __restrict__ block_base,
+                                                                 const int* __restrict__ skip)
+{
+    if (*skip) return;
+    const int pi = block_prob[blockIdx.x];
+    const OzBatchProb& q = probs[pi];
+    const int64_t mq = (q.m + 3) >> 2;
+    const int64_t e = ((int64_t)blockIdx.x - block_base[pi]) * 256 + threadIdx.x;
+    if (e >= mq * q.n) return;
+    const int64_t j = e / mq, i0 = (e - j * mq) * 4;
+    const int64_t plane_stride = q.n * q.ld;
+    const int32_t* src = q.planes + j * q.ld + i0;  // ld is a multiple of 4: 16-byte aligned
+    int4 v[S];
+#pragma unroll
+    for (int L = 0; L < S; ++L) v[L] = __ldcs(reinterpret_cast<const int4*>(src + (int64_t)L * plane_stride));
+    const bool plain = (q.alpha == 1.0 && q.beta == 0.0);
+    const int ebj = q.eb[j] - 8 * (S + 1);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int64_t i = i0 + r;
+        if (i >= q.m) break;
+        __int128 T = 0;
+#pragma unroll
+        for (int L = S - 1; L >= 0; --L) {
+            const int x = (r == 0) ? v[L].x : (r == 1) ? v[L].y : (r == 2) ? v[L].z : v[L].w;
+            T = (T << 8) + (__int128)x;
+        }
+        const double ab = round_scaled(T, q.ea[i] + ebj);
+        double* cij = q.c + i * q.rs_c + j * q.cs_c;
+        if (plain) {
+            *cij = ab;
+        } else {
+            const double tt = __dmul_rn(q.alpha, ab);
+            *cij = (q.beta == 0.0) ? tt : __fma_rn(q.beta, *cij, tt);
+        }
+    }
+}
+
 void launch_recombine(int slices, const OzRecombParams& r, unsigned blocks, cudaStream_t s)
 {
     switch (slices) {
@@ -1061,7 +1312,7 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     static bool attr_set = false;
     static int max_pairs = 0;
     if (!attr_set) {
-        if ((rc = check_cuda(cudaFuncSetAttribute(ozaki_slice_gemm_kernel,
+        if ((rc = check_cuda(cudaFuncSetAttribute(ozaki_slice_gemm_kernel<OzGemmParams>,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   OZ_SMEM_BYTES), "smem attr")))
             return bail(rc);
@@ -1106,7 +1357,7 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     } else {
         const int grid = (int)((p.items < sms) ? p.items : sms);
         LaunchScope ls("ozaki_slice_gemm", s);
-        ozaki_slice_gemm_kernel<<<grid, OZ_THREADS, OZ_SMEM_BYTES, s>>>(map_a, map_b, p);
+        ozaki_slice_gemm_kernel<OzGemmParams><<<grid, OZ_THREADS, OZ_SMEM_BYTES, s>>>(map_a, map_b, p);
     }
     if ((rc = check_cuda(cudaGetLastError(), "ozaki_slice_gemm"))) return bail(rc);
     {
@@ -1138,6 +1389,284 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     rc = dgemm_native_gated(m, n, k, alpha, a, ars, acs, b, brs, bcs, beta, c, rs_c, cs_c, nonfinite, s);
     dev_free(ws, s);
     return rc;
+}
+
+// ---------------------------------------------------------------- grouped form
+// Every problem of a gemm_batch call through the Ozaki form in three
+// launches (split, slice GEMM, recombine) plus the gated native fallback the
+// caller adds.  The tables and arenas are built once and stay resident, so
+// a plan can replay the launches (or a graph of them).
+struct OzBatch {
+    int slices = 0;
+    int nprob = 0;
+    int64_t items = 0, units = 0, rblocks = 0, boxes_a = 0, boxes_b = 0;
+    uint8_t* arena = nullptr;  // slices, planes, exponents, tables, flag
+    OzBatchProb* d_probs = nullptr;
+    int32_t* d_item_prob = nullptr;
+    int64_t* d_item_base = nullptr;
+    int32_t* d_unit_prob = nullptr;
+    int64_t* d_unit_base = nullptr;
+    int32_t* d_rblock_prob = nullptr;
+    int64_t* d_rblock_base = nullptr;
+    int* d_flag = nullptr;
+    uint16_t* sa = nullptr;
+    uint16_t* sb = nullptr;
+    CUtensorMap map_a, map_b;
+    OzBatchParams gp;
+};
+
+namespace {
+
+int make_box_map(CUtensorMap* map, const void* base, int box_rows, int64_t nboxes)
+{
+    auto fn = encode_fn();
+    if (!fn) return set_error(GB_ERR_CUDA, "ozaki", "cuTensorMapEncodeTiled unavailable");
+    if (nboxes > INT32_MAX) return set_error(GB_ERR_ARG, "ozaki batch", "too many k blocks for TMA coordinates");
+    cuuint64_t dims[3] = {(cuuint64_t)OZ_BK, (cuuint64_t)box_rows, (cuuint64_t)nboxes};
+    cuuint64_t strides[2] = {(cuuint64_t)(OZ_BK * 2), (cuuint64_t)box_rows * OZ_BK * 2};
+    cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
+                    estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(GB_ERR_CUDA, "ozaki batch", "cuTensorMapEncodeTiled failed");
+    return GB_SUCCESS;
+}
+
+template <int S>
+void launch_split_batch(const OzBatch& ob, cudaStream_t s)
+{
+    oz_split_batch_kernel<S><<<(unsigned)ob.units, 256, 0, s>>>(ob.d_probs, ob.d_unit_prob, ob.d_unit_base,
+                                                                 ob.boxes_a, ob.boxes_b, ob.sa, ob.sb, ob.d_flag);
+}
+
+template <int S>
+void launch_recombine_batch(const OzBatch& ob, cudaStream_t s)
+{
+    oz_recombine_batch_kernel<S><<<(unsigned)ob.rblocks, 256, 0, s>>>(ob.d_probs, ob.d_rblock_prob,
+                                                                       ob.d_rblock_base, ob.d_flag);
+}
+
+}  // namespace
+
+// Whether the grouped form takes a problem: one k part per level and the
+// 128-bit recombination range.
+bool ozaki_batch_accepts(int64_t k, int slices)
+{
+    const int64_t kpad = round_up(k, OZ_BK);
+    return kpad <= ozaki_kpart_limit(slices) && ozaki_t_bound_log2(slices, k) < 126.0;
+}
+
+int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices, cudaStream_t s,
+                       OzBatch** out)
+{
+    *out = nullptr;
+    if (slices < 2 || slices > OZ_MAX_SLICES)
+        return set_error(GB_ERR_ARG, "ozaki batch", "slices must be in [2, 12]");
+    std::vector<OzBatchProb> h;
+    h.reserve((size_t)count);
+    for (int64_t i = 0; i < count; ++i) {
+        const gb_gemm_problem_t& p = probs[i];
+        if (p.m <= 0 || p.n <= 0 || p.k <= 0 || p.alpha == 0.0 || !ozaki_batch_accepts(p.k, slices))
+            return set_error(GB_ERR_ARG, "ozaki batch", "problem not eligible for the grouped form");
+        const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
+        OzBatchProb q = {};
+        q.a = static_cast<const double*>(p.a);
+        q.ars = ta ? p.lda : 1;
+        q.acs = ta ? 1 : p.lda;
+        q.b = static_cast<const double*>(p.b);
+        q.brs = tb ? 1 : p.ldb;  // rows of op(B)^T are columns of op(B)
+        q.bcs = tb ? p.ldb : 1;
+        q.c = static_cast<double*>(p.c);
+        q.rs_c = 1;
+        q.cs_c = p.ldc;
+        q.alpha = p.alpha;
+        q.beta = p.beta;
+        q.m = p.m;
+        q.n = p.n;
+        q.k = p.k;
+        q.tiles_m = (int32_t)((p.m + OZ_BM - 1) / OZ_BM);
+        q.tiles_n = (int32_t)((p.n + OZ_BN - 1) / OZ_BN);
+        q.kb = (int32_t)((p.k + OZ_BK - 1) / OZ_BK);
+        q.units_a = (int64_t)q.tiles_m * (OZ_BM / 32);
+        q.ld = round_up(p.m, 4);
+        h.push_back(q);
+    }
+    // longest k first: the last items handed out are the cheapest
+    std::stable_sort(h.begin(), h.end(), [](const OzBatchProb& x, const OzBatchProb& y) { return x.k > y.k; });
+
+    OzBatch* ob = new OzBatch();
+    ob->slices = slices;
+    ob->nprob = (int)h.size();
+    OzBatchParams& gp = ob->gp;
+    gp.slices = slices;
+    gp.nlevels = slices;
+    gp.chunk_kb = chunk_kb_setting();
+    gp.nprob = ob->nprob;
+    for (int L = 0; L < slices; ++L) {  // same level table as the single-problem form, one part each
+        OzLevel& lv = gp.lv[L];
+        lv.lev = slices + 1 - L;
+        lv.pa_lo = (lv.lev - slices > 1) ? lv.lev - slices : 1;
+        const int pa_hi = (lv.lev - 1 < slices) ? lv.lev - 1 : slices;
+        lv.npairs = pa_hi - lv.pa_lo + 1;
+        lv.nparts = 1;
+        lv.kb_per_part = 0;
+        lv.plane_base = L;
+        lv.item_base = 0;
+    }
+    // tables: boxes, level planes, exponents, work items, split units, recombine blocks
+    std::vector<int32_t> item_prob, unit_prob, rblock_prob;
+    std::vector<int64_t> item_base, unit_base, rblock_base;
+    int64_t planes_elems = 0, exps = 0;
+    for (int i = 0; i < ob->nprob; ++i) {
+        OzBatchProb& q = h[(size_t)i];
+        q.abox = ob->boxes_a;
+        q.bbox = ob->boxes_b;
+        ob->boxes_a += (int64_t)q.tiles_m * q.kb;
+        ob->boxes_b += (int64_t)q.tiles_n * q.kb;
+        planes_elems += (int64_t)slices * q.n * q.ld;
+        exps += q.m + q.n;
+        const int64_t it = (int64_t)slices * q.tiles_m * q.tiles_n;
+        item_base.push_back(ob->items);
+        item_prob.insert(item_prob.end(), (size_t)it, i);
+        ob->items += it;
+        const int64_t un = q.units_a + (int64_t)q.tiles_n * (OZ_BN / 32);
+        unit_base.push_back(ob->units);
+        unit_prob.insert(unit_prob.end(), (size_t)un, i);
+        ob->units += un;
+        const int64_t rb = (((q.m + 3) / 4) * q.n + 255) / 256;
+        rblock_base.push_back(ob->rblocks);
+        rblock_prob.insert(rblock_prob.end(), (size_t)rb, i);
+        ob->rblocks += rb;
+    }
+    if (ob->units > INT32_MAX || ob->rblocks > INT32_MAX) {
+        delete ob;
+        return set_error(GB_ERR_ARG, "ozaki batch", "batch too large for one launch");
+    }
+    auto al = [](size_t x) { return (x + 1023) & ~size_t(1023); };
+    const size_t b_sa = al((size_t)slices * ob->boxes_a * OZ_BM * OZ_BK * 2);
+    const size_t b_sb = al((size_t)slices * ob->boxes_b * OZ_BN * OZ_BK * 2);
+    const size_t b_pl = al((size_t)planes_elems * 4);
+    const size_t b_ex = al((size_t)exps * 4);
+    const size_t b_pr = al(sizeof(OzBatchProb) * h.size());
+    const size_t b_it = al(4 * item_prob.size()), b_ib = al(8 * item_base.size());
+    const size_t b_up = al(4 * unit_prob.size()), b_ub = al(8 * unit_base.size());
+    const size_t b_rp = al(4 * rblock_prob.size()), b_rb = al(8 * rblock_base.size());
+    const size_t total = b_sa + b_sb + b_pl + b_ex + b_pr + b_it + b_ib + b_up + b_ub + b_rp + b_rb + 1024;
+    ob->arena = static_cast<uint8_t*>(dev_alloc(total, s));
+    if (!ob->arena) {
+        delete ob;
+        return GB_ERR_NOMEM;
+    }
+    uint8_t* cur = ob->arena;
+    auto take = [&](size_t b) { uint8_t* r = cur; cur += b; return r; };
+    ob->sa = reinterpret_cast<uint16_t*>(take(b_sa));
+    ob->sb = reinterpret_cast<uint16_t*>(take(b_sb));
+    int32_t* planes = reinterpret_cast<int32_t*>(take(b_pl));
+    int32_t* ex = reinterpret_cast<int32_t*>(take(b_ex));
+    ob->d_probs = reinterpret_cast<OzBatchProb*>(take(b_pr));
+    ob->d_item_prob = reinterpret_cast<int32_t*>(take(b_it));
+    ob->d_item_base = reinterpret_cast<int64_t*>(take(b_ib));
+    ob->d_unit_prob = reinterpret_cast<int32_t*>(take(b_up));
+    ob->d_unit_base = reinterpret_cast<int64_t*>(take(b_ub));
+    ob->d_rblock_prob = reinterpret_cast<int32_t*>(take(b_rp));
+    ob->d_rblock_base = reinterpret_cast<int64_t*>(take(b_rb));
+    ob->d_flag = reinterpret_cast<int*>(take(1024));
+    int64_t pl_off = 0, ex_off = 0;
+    for (auto& q : h) {
+        q.planes = planes + pl_off;
+        pl_off += (int64_t)slices * q.n * q.ld;
+        q.ea = ex + ex_off;
+        q.eb = q.ea + q.m;
+        ex_off += q.m + q.n;
+    }
+    int rc = GB_SUCCESS;
+    auto up = [&](void* d, const void* src, size_t b) {
+        if (!rc && b) rc = check_cuda(cudaMemcpyAsync(d, src, b, cudaMemcpyHostToDevice, s), "batch tables");
+    };
+    up(ob->d_probs, h.data(), sizeof(OzBatchProb) * h.size());
+    up(ob->d_item_prob, item_prob.data(), 4 * item_prob.size());
+    up(ob->d_item_base, item_base.data(), 8 * item_base.size());
+    up(ob->d_unit_prob, unit_prob.data(), 4 * unit_prob.size());
+    up(ob->d_unit_base, unit_base.data(), 8 * unit_base.size());
+    up(ob->d_rblock_prob, rblock_prob.data(), 4 * rblock_prob.size());
+    up(ob->d_rblock_base, rblock_base.data(), 8 * rblock_base.size());
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "batch tables");  // host vectors go out of scope
+    if (!rc) rc = make_box_map(&ob->map_a, ob->sa, OZ_BM, (int64_t)slices * ob->boxes_a);
+    if (!rc) rc = make_box_map(&ob->map_b, ob->sb, OZ_BN, (int64_t)slices * ob->boxes_b);
+    if (!rc && ob->nprob > 0) {
+        static bool attr = false;
+        if (!attr) {
+            rc = check_cuda(cudaFuncSetAttribute(ozaki_slice_gemm_kernel<OzBatchParams>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM_BYTES),
+                            "smem attr");
+            attr = (rc == GB_SUCCESS);
+        }
+    }
+    if (rc) {
+        dev_free(ob->arena, s);
+        delete ob;
+        return rc;
+    }
+    gp.items = ob->items;
+    gp.boxes_a = ob->boxes_a;
+    gp.boxes_b = ob->boxes_b;
+    gp.probs = ob->d_probs;
+    gp.item_prob = ob->d_item_prob;
+    gp.item_base = ob->d_item_base;
+    gp.status = device_status_word();
+    gp.skip = ob->d_flag;
+    *out = ob;
+    return GB_SUCCESS;
+}
+
+const int* ozaki_batch_flag(const OzBatch* ob) { return ob ? ob->d_flag : nullptr; }
+
+int ozaki_batch_launch(OzBatch* ob, cudaStream_t s)
+{
+    if (!ob || ob->nprob == 0) return GB_SUCCESS;
+    int rc;
+    if ((rc = check_cuda(cudaMemsetAsync(ob->d_flag, 0, sizeof(int), s), "memset"))) return rc;
+    {
+        LaunchScope ls("oz_split_batch", s);
+        switch (ob->slices) {
+#define GB_SPLITB_CASE(S) \
+    case S: launch_split_batch<S>(*ob, s); break;
+            GB_SPLITB_CASE(2) GB_SPLITB_CASE(3) GB_SPLITB_CASE(4) GB_SPLITB_CASE(5) GB_SPLITB_CASE(6)
+            GB_SPLITB_CASE(7) GB_SPLITB_CASE(8) GB_SPLITB_CASE(9) GB_SPLITB_CASE(10) GB_SPLITB_CASE(11)
+            GB_SPLITB_CASE(12)
+#undef GB_SPLITB_CASE
+        default: break;
+        }
+    }
+    if ((rc = check_cuda(cudaGetLastError(), "oz_split_batch"))) return rc;
+    {
+        const int sms = sm_count() > 0 ? sm_count() : 148;
+        const int grid = (int)((ob->items < sms) ? ob->items : sms);
+        LaunchScope ls("ozaki_slice_gemm_batch", s);
+        ozaki_slice_gemm_kernel<OzBatchParams><<<grid, OZ_THREADS, OZ_SMEM_BYTES, s>>>(ob->map_a, ob->map_b, ob->gp);
+    }
+    if ((rc = check_cuda(cudaGetLastError(), "ozaki_slice_gemm batch"))) return rc;
+    {
+        LaunchScope ls("oz_recombine_batch", s);
+        switch (ob->slices) {
+#define GB_RECB_CASE(S) \
+    case S: launch_recombine_batch<S>(*ob, s); break;
+            GB_RECB_CASE(2) GB_RECB_CASE(3) GB_RECB_CASE(4) GB_RECB_CASE(5) GB_RECB_CASE(6)
+            GB_RECB_CASE(7) GB_RECB_CASE(8) GB_RECB_CASE(9) GB_RECB_CASE(10) GB_RECB_CASE(11)
+            GB_RECB_CASE(12)
+#undef GB_RECB_CASE
+        default: break;
+        }
+    }
+    return check_cuda(cudaGetLastError(), "oz_recombine_batch");
+}
+
+void ozaki_batch_destroy(OzBatch* ob, cudaStream_t s)
+{
+    if (!ob) return;
+    dev_free(ob->arena, s);
+    delete ob;
 }
 
 }  // namespace gb

@@ -11,9 +11,12 @@ L2 where the workload allows:
   dtrsm_8192x4096 L/L/N/N, diag 8192+|u|, native and Ozaki updates (m^2 n flop)
   dgemv_32768     N and T, 8(mn + n + 2m) bytes                    (HBM)
   daxpyv_2^28     24 n bytes; ddotv_2^28: 16 n bytes                (HBM)
+  dtrsm_16384     L/L/N/N, B entries (1+u) 2^e, e in [-20,20]: native and
+                  Ozaki updates, sampled componentwise backward error
   batch_4096      4096 problems, m,n,k log-uniform in [16,1024], random
-                  transposes: one grouped launch (captured graph) vs a
-                  per-problem launch loop, FP64 and FP32
+                  transposes: grouped launches (captured graph) vs a
+                  per-problem launch loop, FP64 native, FP64 Ozaki (7
+                  slices) and FP32
 
 Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl]
 """
@@ -102,6 +105,42 @@ def run_trsm(out):
     _lib.load().gb_set_dgemm_mode(0, 8)
 
 
+def run_trsm_ozaki(out):
+    """DTRSM L/L/N/N m = n = 16384: L as above (diagonal 16384+|u|), B with
+    entries (1+u) 2^e, e in [-20, 20].  Native FP64 and Ozaki off-diagonal
+    updates (7 slices; FP64 diagonal-block solves), each with its sampled
+    componentwise backward error |B - L X|_ij / (|L||X| + |B|)_ij, numerator
+    and denominator evaluated in double-double on the device."""
+    import torch
+    m = n = 16384
+    L = _mat(m, m, seed=31)
+    L.copy_(torch.tril(L))
+    d = torch.arange(m, device="cuda")
+    L[d, d] = m + L[d, d].abs()
+    b0 = _mat(m, n, kind=dev.RAND_EXPSPREAD, seed=32, p0=-20, p1=20)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    ii = torch.randint(0, m, (4096,), generator=g).cuda()
+    jj = torch.randint(0, n, (4096,), generator=g).cuda()
+    absL, absB = L.abs(), b0.abs()
+    flops = float(m) * m * n
+    for mode, name in ((0, "native_fp64"), (1, "ozaki_s7_updates")):
+        _lib.load().gb_set_dgemm_mode(mode, 7)
+        x = b0.clone()
+        reps = 1 if mode == 0 else 3
+        ms = _timer(lambda: (x.copy_(b0), dev.dtrsm(0, 0xC0, 0, 0, 1.0, L, x)), reps=reps, warmup=1)
+        copy_ms = _timer(lambda: x.copy_(b0), reps=3, warmup=1)
+        x.copy_(b0)
+        dev.dtrsm(0, 0xC0, 0, 0, 1.0, L, x)
+        rh, rl = dev.dd_gemm_entries(0, 0, 1.0, L, x, -1.0, b0, ii, jj)
+        dh, dl = dev.dd_gemm_entries(0, 0, 1.0, absL, x.abs(), 1.0, absB, ii, jj)
+        berr = float(((rh + rl).abs() / (dh + dl)).max())
+        out.append({"workload": "dtrsm_16384x16384_expspread", "form": name, "ms": ms - copy_ms,
+                    "tflops": flops / (ms - copy_ms) / 1e9, "max_componentwise_backward_err": berr,
+                    "err_sample": "4096 random entries, double-double on the device"})
+        del x
+    _lib.load().gb_set_dgemm_mode(0, 8)
+
+
 def run_level12(out):
     import torch
     pk, kind = peaks()
@@ -167,27 +206,39 @@ def batch_problems(count, seed, dtype, lo=16, hi=1024):
 
 
 def run_batch(out):
+    import torch
     L = _lib.load()
-    L.gb_gemm_batch_dev.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_void_p]
-    L.gb_batch_plan_create.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]
-    L.gb_batch_plan_run.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
-    L.gb_batch_plan_destroy.argtypes = [C.c_void_p]
-    for dtype, name in ((0, "fp64"), (1, "fp32")):
-        probs, keep, flops = batch_problems(4096, 4, dtype)
+    for dtype, name in ((0, "fp64"), (2, "fp64_ozaki_s7"), (1, "fp32")):
+        if dtype == 2:
+            L.gb_set_dgemm_mode(1, 7)
+        probs, keep, flops = batch_problems(4096, 4, 1 if dtype == 1 else 0)
         plan = C.c_void_p()
         _lib.check(L.gb_batch_plan_create(C.addressof(probs), 4096, dtype, C.byref(plan)), "plan")
         st = _stream()  # the library works on the stream the events are recorded on
         ms_g = _timer(lambda: _lib.check(L.gb_batch_plan_run(plan, 1, st), "run"), reps=3, warmup=1)
+        rec = {"workload": "batch_4096_%s" % name, "flops": flops, "grouped_graph_ms": ms_g,
+               "grouped_tflops": flops / ms_g / 1e9}
+        if dtype == 2:
+            # against the native grouped launch on the same operands
+            c_oz = keep[2].clone()
+            L.gb_batch_plan_destroy(plan)
+            _lib.check(L.gb_batch_plan_create(C.addressof(probs), 4096, 0, C.byref(plan)), "plan")
+            _lib.check(L.gb_batch_plan_run(plan, 0, st), "run")
+            torch.cuda.synchronize()
+            c_nat = keep[2]
+            rec["max_abs_diff_vs_native"] = float((c_oz - c_nat).abs().max())
+            rec["max_abs_c"] = float(c_nat.abs().max())
         ms_l = _timer(lambda: _lib.check(L.gb_gemm_batch_dev(C.addressof(probs), 4096, dtype, 1, st), "loop"),
                       reps=1, warmup=1)
         L.gb_batch_plan_destroy(plan)
-        out.append({"workload": "batch_4096_%s" % name, "flops": flops, "grouped_graph_ms": ms_g,
-                    "grouped_tflops": flops / ms_g / 1e9, "loop_ms": ms_l, "loop_tflops": flops / ms_l / 1e9,
-                    "speedup": ms_l / ms_g})
+        rec.update({"loop_ms": ms_l, "loop_tflops": flops / ms_l / 1e9, "speedup": ms_l / ms_g})
+        out.append(rec)
+        L.gb_set_dgemm_mode(0, 8)
         del keep
 
 
-SUITES = {"gemm": run_gemm, "trsm": run_trsm, "level12": run_level12, "batch": run_batch}
+SUITES = {"gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
+          "batch": run_batch}
 
 
 def main():

@@ -327,14 +327,26 @@ typedef struct {
 #define GB_BATCH_GROUPED 0  /* one persistent launch, device tile scheduler */
 #define GB_BATCH_LOOP 1     /* one launch per problem (comparison baseline) */
 
+#define GB_BATCH_FP64 0        /* native FP64 (DMMA) */
+#define GB_BATCH_FP32 1        /* FP32 */
+#define GB_BATCH_FP64_OZAKI 2  /* FP64 through the Ozaki form, slice count of gb_set_dgemm_mode
+                                  (8 when that is 0 = automatic) */
+
 /* Counterpart of dgemm_batch_/sgemm_batch_ (frame/compat/extra/bla_gemm_batch.c:
-   135-249) on device operands; dtype 0 = FP64, 1 = FP32. */
+   135-249) on device operands; dtype is one of GB_BATCH_FP64/FP32/FP64_OZAKI.
+   GB_BATCH_FP64_OZAKI runs all problems in three grouped launches (split,
+   slice GEMM, recombine); a problem with an Inf/NaN operand sends the batch
+   to the native grouped launch, and problems whose k exceeds one exact
+   integer part are run one by one through the Ozaki form.  Its results are
+   bit-identical to gb_dgemm_ozaki_dev on each problem with the same slices.
+   With GB_BATCH_LOOP each problem gets its own launches. */
 int gb_gemm_batch_dev(const gb_gemm_problem_t* probs, gb_dim_t count, int dtype, int mode,
                       void* stream);
 
-/* Resident plan for repeated grouped launches: the descriptor table stays in
-   HBM and gb_batch_plan_run(use_graph=1) replays the counter reset and the
-   grouped launch as one captured CUDA graph. */
+/* Resident plan for repeated grouped launches: the descriptor tables (and for
+   GB_BATCH_FP64_OZAKI the slice and level-sum arenas) stay in HBM and
+   gb_batch_plan_run(use_graph=1) replays the launches as one captured CUDA
+   graph. */
 int gb_batch_plan_create(const gb_gemm_problem_t* probs, gb_dim_t count, int dtype, void** plan);
 int gb_batch_plan_run(void* plan, int use_graph, void* stream);
 int gb_batch_plan_destroy(void* plan);
