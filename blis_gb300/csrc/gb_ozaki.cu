@@ -1592,8 +1592,8 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
     up(ob->d_rblock_prob, rblock_prob.data(), 4 * rblock_prob.size());
     up(ob->d_rblock_base, rblock_base.data(), 8 * rblock_base.size());
     if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "batch tables");  // host vectors go out of scope
-    if (!rc) rc = make_box_map(&ob->map_a, ob->sa, OZ_BM, (int64_t)slices * ob->boxes_a);
-    if (!rc) rc = make_box_map(&ob->map_b, ob->sb, OZ_BN, (int64_t)slices * ob->boxes_b);
+    if (!rc && ob->nprob > 0) rc = make_box_map(&ob->map_a, ob->sa, OZ_BM, (int64_t)slices * ob->boxes_a);
+    if (!rc && ob->nprob > 0) rc = make_box_map(&ob->map_b, ob->sb, OZ_BN, (int64_t)slices * ob->boxes_b);
     if (!rc && ob->nprob > 0) {
         static bool attr = false;
         if (!attr) {
