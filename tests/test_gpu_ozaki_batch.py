@@ -177,3 +177,15 @@ def test_dgemm_batch_blas_follows_ozaki_mode(gblib):
             assert np.array_equal(got, ref)
     finally:
         blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+
+
+def test_grouped_ozaki_only_trivial_problems(gblib):
+    # nothing for the grouped launches: k = 0 and alpha = 0 only, C := beta C
+    batch = Batch([(4, 5, 0, 0, 0, 1.0, 0.5), (3, 3, 7, 1, 1, 0.0, 2.0)], 4000)
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 0)
+    try:
+        got = _run_batch(gblib, batch, FP64_OZAKI, GROUPED)
+    finally:
+        blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+    assert np.array_equal(got[0], 0.5 * batch.host[0][2])
+    assert np.array_equal(got[1], 2.0 * batch.host[1][2])
