@@ -335,6 +335,61 @@ def evaluate(params, data):
     return res
 
 
+def measure_slice_errors(params, data, nsample=256):
+    """Run the Ozaki form at the final slice count (the MLP's proposal raised
+    by the verifier) on the operands each FP64 label was made from, and
+    measure on `nsample` random entries, in double-double:
+      err_ij = |C_ij - (AB)_ij| / (|A||B|)_ij
+    against the verifier's target sqrt(k) u (u = 2^-53) plus the one
+    rounding of the result to FP64 (u |C_ij| <= u (|A||B|)_ij) that every
+    FP64 result carries, i.e. (sqrt(k) + 1) u, and against native FP64 on the
+    same entries.  A violation is an entry above that bound."""
+    import torch
+    from . import dev
+    net = GpuMlp(params)
+    pred = net.forward(data["X"])
+    sh = data["shapes"]
+    L = _lib.load()
+    out = {"shapes": 0, "entries": 0, "bound_violations": 0, "native_above_bound": 0, "ozaki_le_native": 0,
+           "max_err_over_bound": 0.0, "mean_final_slices": 0.0}
+    finals = []
+    for i in np.nonzero(sh[:, 3] == 0)[0]:
+        m, n, k = min(int(sh[i, 0]), 512), min(int(sh[i, 1]), 512), int(sh[i, 2])
+        ea, eb = int(sh[i, 7]), int(sh[i, 8])
+        a = dev.colmajor(m, k)
+        b = dev.colmajor(k, n)
+        dev.randm(a, dev.RAND_EXPSPREAD, 1000 + int(i), -ea, ea)
+        dev.randm(b, dev.RAND_EXPSPREAD, 2000 + int(i), -eb, eb)
+        prop = int(np.clip(math.ceil(pred[i, OUT_SLICES] * 12.0 - 0.25), 2, 12))
+        s = C.c_int(0)
+        _lib.check(L.gb_ozaki_verify_slices_dev(0, 0, m, n, k, a.data_ptr(), 1, m, b.data_ptr(), 1, k, prop, 256,
+                                                C.byref(s), None), "verify")
+        if s.value > 12:
+            continue  # the library runs native FP64 here
+        finals.append(s.value)
+        c_oz = dev.colmajor(m, n)
+        c_nat = dev.colmajor(m, n)
+        dev.dgemm_ozaki(0, 0, 1.0, a, b, 0.0, c_oz, s.value)
+        dev.dgemm(0, 0, 1.0, a, b, 0.0, c_nat)
+        g = torch.Generator(device="cpu").manual_seed(int(i))
+        ii = torch.randint(0, m, (nsample,), generator=g).cuda()
+        jj = torch.randint(0, n, (nsample,), generator=g).cuda()
+        hi, lo = dev.dd_gemm_entries(0, 0, 1.0, a, b, 0.0, None, ii, jj)
+        ah, al_ = dev.dd_gemm_entries(0, 0, 1.0, a.abs(), b.abs(), 0.0, None, ii, jj)
+        den = ah + al_
+        e_oz = ((c_oz[ii, jj] - hi) - lo).abs() / den
+        e_nat = ((c_nat[ii, jj] - hi) - lo).abs() / den
+        bound = (math.sqrt(k) + 1.0) * 2.0 ** -53
+        out["shapes"] += 1
+        out["entries"] += nsample
+        out["bound_violations"] += int((e_oz > bound).sum())
+        out["native_above_bound"] += int((e_nat > bound).sum())
+        out["ozaki_le_native"] += int(float(e_oz.max()) <= float(e_nat.max()))
+        out["max_err_over_bound"] = max(out["max_err_over_bound"], float(e_oz.max()) / bound)
+    out["mean_final_slices"] = float(np.mean(finals)) if finals else 0.0
+    return out
+
+
 # ------------------------------------------------------------------ persistence
 def save_model(path, params, meta):
     p = np.asarray(params, np.float32)
@@ -417,18 +472,27 @@ def _main():
     ap.add_argument("--data")
     ap.add_argument("--model")
     ap.add_argument("--epochs", type=int, default=300)
+    ap.add_argument("--measure", action="store_true",
+                    help="eval: also run the Ozaki form at the final slice counts and measure the errors")
     a = ap.parse_args()
     if a.cmd == "tune":
         d = build_dataset(sample_shapes(a.count, a.seed), log_every=500)
         np.savez_compressed(a.out, **d)
     elif a.cmd == "train":
-        d = np.load(a.data)
-        p, curve = train(d["X"], d["Y"], d["M"], epochs=a.epochs, log=print)
-        save_model(a.out, p, {"train_samples": int(d["X"].shape[0]), "final_loss": curve[-1]})
+        # --data may name several tuning files (comma separated); they are concatenated
+        parts = [np.load(p) for p in a.data.split(",")]
+        X, Y, M = (np.concatenate([d[key] for d in parts]) for key in ("X", "Y", "M"))
+        p, curve = train(X, Y, M, epochs=a.epochs, log=print)
+        save_model(a.out, p, {"train_samples": int(X.shape[0]), "final_loss": curve[-1]})
         save_model_bin(os.path.splitext(a.out)[0] + ".bin", p)
     else:
         p, _ = load_model(a.model)
-        print(json.dumps(evaluate(p, np.load(a.data)), indent=1))
+        d = np.load(a.data)
+        res = evaluate(p, d)
+        if a.measure and "slices" in res:
+            res["slices"]["measured"] = measure_slice_errors(p, d)
+            res["slices"]["violations_after_verifier"] = res["slices"]["measured"]["bound_violations"]
+        print(json.dumps(res, indent=1))
 
 
 if __name__ == "__main__":

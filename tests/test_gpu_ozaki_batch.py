@@ -170,10 +170,12 @@ def test_dgemm_batch_blas_follows_ozaki_mode(gblib):
                          [s[5] for s in shapes], [d[0] for d in data], [d[0].shape[0] for d in data],
                          [d[1] for d in data], [d[1].shape[0] for d in data], [s[6] for s in shapes], cs,
                          [s[0] for s in shapes], [1] * len(shapes))
+        # the CPU model of the Ozaki form (not dgemm_: it sends m == 1 or n == 1 to gemv,
+        # frame/compat/bla_gemm.c:180-218, while the batch path runs every problem as a gemm,
+        # frame/compat/extra/bla_gemm_batch.c:227)
         for (m, n, k, ta, tb, al, be), (a, b, c), got in zip(shapes, data, cs):
             ref = np.asfortranarray(c.copy())
-            blas.dgemm("T" if ta else "N", "T" if tb else "N", m, n, k, al, a, a.shape[0], b, b.shape[0], be,
-                       ref, m)
+            po.ozaki_dgemm(8 * ta, 8 * tb, al, a, b, be, ref, 7)
             assert np.array_equal(got, ref)
     finally:
         blas.set_dgemm_mode(blas.DGEMM_NATIVE)
