@@ -41,6 +41,13 @@ __global__ void __launch_bounds__(NT) gemm_simt_kernel(GArgs<T> p, const int* ga
     simt_tile<T>(p, (int64_t)blockIdx.y * BM, (int64_t)blockIdx.x * BN, As, Bs);
 }
 
+__global__ void __launch_bounds__(NT) sgemm_kernel(GArgs<float> p)
+{
+    __shared__ __align__(16) float As[2 * BK * LDS];
+    __shared__ __align__(16) float Bs[2 * BK * LDS];
+    sgemm_tile(p, (int64_t)blockIdx.y * BM, (int64_t)blockIdx.x * BN, As, Bs);
+}
+
 template <typename T>
 __global__ void scal_matrix_kernel(int64_t m, int64_t n, T beta, T* c, int64_t rs_c, int64_t cs_c)
 {
@@ -131,7 +138,7 @@ int sgemm_dev(int64_t m, int64_t n, int64_t k, float alpha,
     if (gy > 65535) return set_error(GB_ERR_ARG, "gb_sgemm", "m too large for one launch");
     GArgs<float> p{m, n, k, alpha, beta, a, ars, acs, b, brs, bcs, c, rs_c, cs_c};
     LaunchScope ls("sgemm_ffma", s);
-    gemm_simt_kernel<float><<<dim3((unsigned)gx, (unsigned)gy), NT, 0, s>>>(p, nullptr);
+    sgemm_kernel<<<dim3((unsigned)gx, (unsigned)gy), NT, 0, s>>>(p);
     return check_cuda(cudaGetLastError(), "sgemm");
 }
 

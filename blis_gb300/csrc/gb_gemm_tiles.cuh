@@ -171,6 +171,60 @@ __device__ __forceinline__ void simt_tile(const GArgs<T>& p, int64_t bm, int64_t
         for (int j = 0; j < 8; ++j) write_c(p, bm + ty * 8 + i, bn + tx * 8 + j, acc[i][j]);
 }
 
+// FP32 tile engine: two shared-memory stages (one barrier per 16-deep k
+// block, the next block's global loads overlap the FMAs), and each thread's
+// 8x8 block split into 4-row/4-column halves 64 apart so its fragments are
+// two 16-byte loads per operand per k step: B's are conflict-free across the
+// warp, A's are broadcasts.  As/Bs hold 2*BK*LDS floats each.
+__device__ __forceinline__ void sgemm_tile(const GArgs<float>& p, int64_t bm, int64_t bn, float* As, float* Bs)
+{
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+    float ra[8], rb[8];
+    load_tiles(p, bm, bn, 0, ra, rb);
+    store_tiles(p, ra, rb, As, Bs);
+    __syncthreads();
+    int cur = 0;
+    for (int64_t k0 = 0; k0 < p.k; k0 += BK) {
+        const bool more = (k0 + BK < p.k);
+        if (more) load_tiles(p, bm, bn, k0 + BK, ra, rb);
+        const float* A = As + cur * (BK * LDS);
+        const float* B = Bs + cur * (BK * LDS);
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            const float4 a0 = *reinterpret_cast<const float4*>(A + kk * LDS + ty * 4);
+            const float4 a1 = *reinterpret_cast<const float4*>(A + kk * LDS + 64 + ty * 4);
+            const float4 b0 = *reinterpret_cast<const float4*>(B + kk * LDS + tx * 4);
+            const float4 b1 = *reinterpret_cast<const float4*>(B + kk * LDS + 64 + tx * 4);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+        if (more) {
+            // the other stage was last read before the previous barrier
+            store_tiles(p, ra, rb, As + (cur ^ 1) * (BK * LDS), Bs + (cur ^ 1) * (BK * LDS));
+            __syncthreads();
+            cur ^= 1;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int64_t gi = bm + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int64_t gj = bn + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+            write_c(p, gi, gj, acc[i][j]);
+        }
+    }
+}
+
 
 }  // namespace tiles
 }  // namespace gb

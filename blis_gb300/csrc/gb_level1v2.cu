@@ -52,14 +52,26 @@ __global__ void dotv_partial_kernel(int64_t n, int64_t chunk, const double* __re
     __shared__ double red[NT / 32];
     const int64_t lo = (int64_t)blockIdx.x * chunk;
     const int64_t hi = (lo + chunk < n) ? lo + chunk : n;
-    double acc0 = 0.0, acc1 = 0.0;
+    double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;
     const bool vec = (incx == 1 && incy == 1 && ((reinterpret_cast<uintptr_t>(x + lo) |
                                                   reinterpret_cast<uintptr_t>(y + lo)) & 15) == 0);
     if (vec) {
         const int64_t len2 = (hi - lo) >> 1;
         const double2* x2 = reinterpret_cast<const double2*>(x + lo);
         const double2* y2 = reinterpret_cast<const double2*>(y + lo);
-        for (int64_t i = threadIdx.x; i < len2; i += NT) {
+        int64_t i = threadIdx.x;
+        // four 16-byte loads of each vector in flight per thread
+        for (; i + 3 * NT < len2; i += 4 * NT) {
+            const double2 a0 = __ldcs(x2 + i), a1 = __ldcs(x2 + i + NT);
+            const double2 a2 = __ldcs(x2 + i + 2 * NT), a3 = __ldcs(x2 + i + 3 * NT);
+            const double2 b0 = __ldcs(y2 + i), b1 = __ldcs(y2 + i + NT);
+            const double2 b2 = __ldcs(y2 + i + 2 * NT), b3 = __ldcs(y2 + i + 3 * NT);
+            acc0 = fma(a0.x, b0.x, acc0); acc1 = fma(a0.y, b0.y, acc1);
+            acc2 = fma(a1.x, b1.x, acc2); acc3 = fma(a1.y, b1.y, acc3);
+            acc0 = fma(a2.x, b2.x, acc0); acc1 = fma(a2.y, b2.y, acc1);
+            acc2 = fma(a3.x, b3.x, acc2); acc3 = fma(a3.y, b3.y, acc3);
+        }
+        for (; i < len2; i += NT) {
             const double2 a = __ldcs(x2 + i), b = __ldcs(y2 + i);
             acc0 = fma(a.x, b.x, acc0);
             acc1 = fma(a.y, b.y, acc1);
@@ -68,7 +80,7 @@ __global__ void dotv_partial_kernel(int64_t n, int64_t chunk, const double* __re
     } else {
         for (int64_t i = lo + threadIdx.x; i < hi; i += NT) acc0 = fma(x[i * incx], y[i * incy], acc0);
     }
-    double v = warp_sum(acc0 + acc1);
+    double v = warp_sum((acc0 + acc1) + (acc2 + acc3));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
     if (threadIdx.x < 32) {

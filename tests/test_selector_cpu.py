@@ -31,12 +31,17 @@ def test_sampled_shapes_respect_caps():
 
 def test_committed_model_and_evaluation():
     p, doc = S.load_model(os.path.join(TUNING, "selector_mlp.json"))
-    assert p.size == S.NPARAMS and doc["meta"]["train_samples"] == 10000
+    assert p.size == S.NPARAMS and doc["meta"]["train_samples"] == 20000
     ev = json.load(open(os.path.join(TUNING, "selector_eval_heldout.json")))
     assert ev["n"] == 2000
     assert ev["mlp"]["mean_throughput_regret"] <= 0.05
     assert ev["mlp"]["mean_throughput_regret"] < ev["threshold_rule"]["mean_throughput_regret"]
+    # measured: the Ozaki form run at every final slice count, errors in double-double
+    meas = ev["slices"]["measured"]
+    assert meas["shapes"] == ev["slices"]["n"] and meas["bound_violations"] == 0
     assert ev["slices"]["violations_after_verifier"] == 0
+    train = [np.load(os.path.join(TUNING, f)) for f in ("autotune_train.npz", "autotune_train2.npz")]
+    assert sum(t["X"].shape[0] for t in train) == 20000
     raw = open(os.path.join(TUNING, "selector_mlp.bin"), "rb").read()
     assert raw[:8] == S.BIN_MAGIC and np.array_equal(np.frombuffer(raw[20:], "<f4"), p)
 
