@@ -940,7 +940,7 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const __grid_constant
 // them into the problem's boxes.  Rows past m (n) up to the box height and
 // k past k_i up to the block width are written as zeros.
 template <int S>
-__global__ void __launch_bounds__(256) oz_split_batch_kernel(const OzBatchProb* __restrict__ probs,
+__global__ void __launch_bounds__(256, 2) oz_split_batch_kernel(const OzBatchProb* __restrict__ probs,
                                                              const int32_t* __restrict__ unit_prob,
                                                              const int64_t* __restrict__ unit_base,
                                                              int64_t boxes_a, int64_t boxes_b,
@@ -970,6 +970,7 @@ __global__ void __launch_bounds__(256) oz_split_batch_kernel(const OzBatchProb* 
         const int64_t r = r0 + rr;
         unsigned long long mx = 0;
         if (r < rows)
+#pragma unroll 4
             for (int64_t l = l0; l < k; l += 8) {
                 const unsigned long long b = abs_bits(__ldg(R + r * sr + l * sl));
                 mx = b > mx ? b : mx;
@@ -1001,7 +1002,9 @@ __global__ void __launch_bounds__(256) oz_split_batch_kernel(const OzBatchProb* 
     const int rr = t >> 3, c0 = (t & 7) * 8;
     const int e = rowe[rr];
     const bool live = (r0 + rr < rows);
-    for (int kb = 0; kb < q.kb; ++kb) {
+    // the next k block's elements are loaded into registers while this one is cut
+    double nxt[8];
+    auto fetch = [&](int kb) {
         const int64_t l0 = (int64_t)kb * 64;
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
@@ -1009,9 +1012,18 @@ __global__ void __launch_bounds__(256) oz_split_batch_kernel(const OzBatchProb* 
             const int tr = rows_fast ? (idx & 31) : (idx >> 6);
             const int tl = rows_fast ? (idx >> 5) : (idx & 63);
             const int64_t r = r0 + tr, l = l0 + tl;
-            tile[tr][tl] = (r < rows && l < k) ? __ldg(R + r * sr + l * sl) : 0.0;
+            nxt[g] = (r < rows && l < k) ? __ldg(R + r * sr + l * sl) : 0.0;
+        }
+    };
+    fetch(0);
+    for (int kb = 0; kb < q.kb; ++kb) {
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const int idx = t + 256 * g;
+            tile[rows_fast ? (idx & 31) : (idx >> 6)][rows_fast ? (idx >> 5) : (idx & 63)] = nxt[g];
         }
         __syncthreads();
+        if (kb + 1 < q.kb) fetch(kb + 1);
         uint32_t packed[S][4];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {

@@ -18,7 +18,7 @@ L2 where the workload allows:
                   per-problem launch loop, FP64 native, FP64 Ozaki (7
                   slices) and FP32
 
-Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl]
+Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl] [--batch-count N]
 """
 import argparse
 import ctypes as C
@@ -81,6 +81,15 @@ def run_gemm(out):
     out.append({"workload": "dgemm_8192", "form": "ozaki_s7", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9,
                 "bf16_frac_of_measured_peak": 28 * 2 * n ** 3 / ms / 1e9 / pk.get("bf16_tflops", 1900.0)})
     del a, b, c
+    fa, fb, fc = (_mat(n, n, seed=s, dtype=torch.float32) for s in (7, 8, 9))
+    ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
+    out.append({"workload": "sgemm_8192", "form": "ffma_fp32", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
+
+
+def run_sgemm(out):
+    """SGEMM 8192^3 alone (the FP32 tile engine)."""
+    import torch
+    n = 8192
     fa, fb, fc = (_mat(n, n, seed=s, dtype=torch.float32) for s in (7, 8, 9))
     ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
     out.append({"workload": "sgemm_8192", "form": "ffma_fp32", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
@@ -205,6 +214,33 @@ def batch_problems(count, seed, dtype, lo=16, hi=1024):
     return probs, (A, B, Cc), flops
 
 
+BATCH_COUNT = 4096
+
+
+def run_batch_ozaki(out):
+    """The grouped Ozaki batch alone (7 slices), BATCH_COUNT problems: plan
+    replay time and per-stage device times from the library's own events."""
+    L = _lib.load()
+    L.gb_set_dgemm_mode(1, 7)
+    probs, keep, flops = batch_problems(BATCH_COUNT, 4, 0)
+    plan = C.c_void_p()
+    _lib.check(L.gb_batch_plan_create(C.addressof(probs), BATCH_COUNT, 2, C.byref(plan)), "plan")
+    st = _stream()
+    ms = _timer(lambda: _lib.check(L.gb_batch_plan_run(plan, 1, st), "run"), reps=3, warmup=2)
+    dev.set_kernel_timing(True)
+    for _ in range(3):
+        _lib.check(L.gb_batch_plan_run(plan, 0, st), "run")
+    stages = {}
+    for pre in ("oz_split_batch", "ozaki_slice_gemm_batch", "oz_recombine_batch", "batch_grouped_dmma_gated"):
+        stages[pre] = dev.kernel_time_ms(pre)[0] / 3
+    dev.set_kernel_timing(False)
+    L.gb_batch_plan_destroy(plan)
+    L.gb_set_dgemm_mode(0, 8)
+    out.append({"workload": "batch_%d_fp64_ozaki_s7" % BATCH_COUNT, "flops": flops, "grouped_graph_ms": ms,
+                "grouped_tflops": flops / ms / 1e9, "stage_ms": stages})
+    del keep
+
+
 def run_batch(out):
     import torch
     L = _lib.load()
@@ -238,7 +274,7 @@ def run_batch(out):
 
 
 SUITES = {"gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
-          "batch": run_batch}
+          "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm}
 
 
 def main():
@@ -246,7 +282,10 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default="")
     ap.add_argument("--json")
+    ap.add_argument("--batch-count", type=int, default=4096, help="problems of the batch_ozaki suite")
     a = ap.parse_args()
+    global BATCH_COUNT
+    BATCH_COUNT = a.batch_count
     torch.cuda.set_device(0)
     _lib.check(_lib.load().gb_init(0), "gb_init")
     names = [s for s in a.only.split(",") if s] or list(SUITES)
