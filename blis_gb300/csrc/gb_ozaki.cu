@@ -8,11 +8,10 @@
 //
 //  1. oz_rowmax / oz_split (integer only): every row of op(A) and of
 //     op(B)^T gets e = ilogb(row max) + 2, so U = |x| 2^-e < 1/2, and is cut
-//     into s balanced base-256 digits of the exact value U (greedy, rounding
-//     to nearest, ties to even), |d| <= 128, each exact in bf16.  The digits
-//     come from the 53-bit mantissa with 64-bit shifts (a sticky flag keeps
-//     the bits below the last digit for exact ties).  Slices are stored
-//     K-major: s planes of [rows_pad][K_pad] bf16, zero padded.
+//     into s balanced base-256 digits, |d| <= 128, each exact in bf16: the
+//     fixed-point value U 2^(8s+2) plus a constant bias, read byte by byte
+//     (oz_digits).  Slices are stored K-major: s planes of [rows_pad][K_pad]
+//     bf16, zero padded.
 //  2. ozaki_slice_gemm: a persistent tcgen05 kernel computes the integer
 //     level sums S_l = sum_{p+q=l} A_p B_q^T, l = 2..s+1 (the triangular
 //     set, s(s+1)/2 slice products).  Tiles arrive by TMA (128B swizzle)
@@ -698,12 +697,22 @@ __device__ __forceinline__ uint32_t int_to_bf16_bits(int d)
     return __float_as_uint(__int2float_rn(d)) >> 16;
 }
 
-// Balanced base-256 digits of U = |x| 2^-e (greedy, rounding to nearest,
-// ties to even) with the sign of x; 64-bit integer only.  With F = 8S+2
-// fraction bits, U 2^F = M 2^sh for the 53-bit mantissa M.  The remainder
-// is kept as R 2^z with |R| < 2^54 (its low z bits are known zeros), so every
-// digit step is a few 64-bit shifts and compares; bits below 2^-F survive
-// only as a sticky flag, which decides exact ties.
+// Balanced base-256 digits of U = |x| 2^-e with the sign of x, from
+// integers only.  X = U 2^F truncated (F = 8S+2 fraction bits); adding
+// B = sum_p 128 2^(F-8p) + 2 makes the balanced digits the plain base-256
+// digits of Y = X + B: d_1 = (Y >> (F-8)) - 128 (at most 128), d_p =
+// ((Y >> (F-8p)) & 255) - 128.  The remainder lies in [-2, 2) units of
+// 2^-F, i.e. |rem| <= 2^-(8S+1) 2^e, and truncating X never changes a digit
+// (the rounding threshold is an integer).  One add and S shifts: the split
+// is integer-bound, so this is its cost.
+template <typename U>
+__host__ __device__ constexpr U oz_bias(int S)
+{
+    U b = 2;
+    for (int p = 1; p <= S; ++p) b += (U)128 << (8 * S + 2 - 8 * p);
+    return b;
+}
+
 template <int S>
 __device__ __forceinline__ void oz_digits(double x, int e, int (&d)[S])
 {
@@ -717,40 +726,25 @@ __device__ __forceinline__ void oz_digits(double x, int e, int (&d)[S])
     const unsigned long long M = ex ? (frac | (1ull << 52)) : frac;
     const int E2 = ex ? ex - 1075 : -1074;
     constexpr int F = 8 * S + 2;
-    const int sh = E2 - e + F;
-    long long R;
-    int z;
-    bool sticky = false;
-    if (sh >= 0) {
-        R = (long long)M;
-        z = sh;
-    } else if (sh > -64) {
-        R = (long long)(M >> (-sh));
-        sticky = (M & ((1ull << (-sh)) - 1)) != 0;
-        z = 0;
-    } else {
-        R = 0;
-        sticky = true;
-        z = 0;
-    }
+    const int sh = E2 - e + F;  // U 2^F = M 2^sh < 2^(F-1)
+    if constexpr (F + 1 < 64) {
+        // Y < 2^(F+1): 64 bits suffice (S <= 7)
+        const unsigned long long X = (sh >= 0) ? (M << sh) : (sh > -64 ? (M >> (-sh)) : 0ull);
+        const unsigned long long Y = X + oz_bias<unsigned long long>(S);
+        d[0] = (int)(Y >> (F - 8)) - 128;
 #pragma unroll
-    for (int p = 1; p <= S; ++p) {
-        const int dz = (F - 8 * p) - z;  // digit weight relative to the remainder's scale
-        long long dg;
-        if (dz <= 0) {
-            dg = R * (1ll << (-dz));  // exact multiple of the digit unit (|dg| <= 128)
-            R = 0;
-        } else if (dz >= 62) {
-            dg = 0;  // |R| < 2^54 is far below half a digit unit
-        } else {
-            const long long q = R >> dz;  // floor
-            const long long rem = R - q * (1ll << dz);
-            const long long half = 1ll << (dz - 1);
-            dg = q;
-            if (rem > half || (rem == half && (sticky || (q & 1)))) dg = q + 1;
-            R -= dg * (1ll << dz);
-        }
-        d[p - 1] = neg ? -(int)dg : (int)dg;
+        for (int p = 2; p <= S; ++p) d[p - 1] = (int)((Y >> (F - 8 * p)) & 255ull) - 128;
+    } else {
+        using u128 = unsigned __int128;
+        const u128 X = (sh >= 0) ? ((u128)M << sh) : (u128)(sh > -64 ? (M >> (-sh)) : 0ull);
+        const u128 Y = X + oz_bias<u128>(S);
+        d[0] = (int)(unsigned long long)(Y >> (F - 8)) - 128;
+#pragma unroll
+        for (int p = 2; p <= S; ++p) d[p - 1] = (int)((unsigned long long)(Y >> (F - 8 * p)) & 255ull) - 128;
+    }
+    if (neg) {
+#pragma unroll
+        for (int p = 0; p < S; ++p) d[p] = -d[p];
     }
 }
 

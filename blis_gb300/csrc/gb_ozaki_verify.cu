@@ -74,7 +74,9 @@ __global__ void verify_kernel(int64_t m, int64_t n, int64_t k, const double* __r
             // remainders: |x - sum of s digits| <= 2^-(8s+1) of the row scale
             const double rep = ldexp(1.0, -(8 * s + 1)) * (sa * rb + ra * sb);
             // dropped pairs p+q > s+1: sum_p A_p * R^B_{s+1-p}, |A_p| <= 2^(e-8p+7),
-            // |R^B_t| <= 2^(e-8t-1), i.e. s 2^(e_i+e_j-8s-2) per product; random
+            // |R^B_t| <= (1 + 2^-7) 2^(e-8t-1) (the digits after t are at most 128 in
+            // magnitude, the last remainder at most half a unit; the factor 1.01
+            // covers the excess), i.e. s 2^(e_i+e_j-8s-2) per product; random
             // signs accumulate like sqrt(k), as the FP64 error it is compared with
             const double drop = sqrt((double)k) * sa * sb * ldexp(1.0, -8 * s - 2) * (double)s * 1.01;
             if (rep + drop <= target) {

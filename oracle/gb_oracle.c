@@ -449,11 +449,10 @@ void orc_dd_dotv(int64_t n, const double* x, int64_t incx, const double* y,
 /* Each row r of the row operand (op(A), or op(B)^T) gets the exponent  */
 /* e_r = ilogb(max_k |r_k|) + 2, so U = |x| 2^-e_r < 1/2 for every      */
 /* element x of the row, and x = sign(x) 2^e_r sum_p d_p 2^-8p + rem    */
-/* with the balanced base-256 digits of U taken greedily with rounding  */
-/* to nearest, ties to even: t_p = 256 * (remainder); d_p = rint(t_p).  */
-/* |d_p| <= 128, every digit is exact in bf16, |rem| <= 2^-(8s+1) 2^e_r.*/
-/* The digits are computed on the exact value (128-bit fixed point with */
-/* 8s+2 fraction bits and a sticky bit), never in floating point.       */
+/* with balanced base-256 digits of U read off the fixed-point value    */
+/* U 2^(8s+2) plus a constant bias (oz_digits below): |d_p| <= 128,     */
+/* every digit is exact in bf16, |rem| <= 2^-(8s+1) 2^e_r.  The digits  */
+/* come from integers only, never from floating point.                  */
 /*                                                                     */
 /* Level sums S_l = sum_{p+q=l} D^A_p (D^B_q)^T, l = 2..s+1 (the        */
 /* triangular set, s(s+1)/2 products), are exact integers.  The GPU     */
@@ -534,7 +533,14 @@ static double oz_round_scaled(i128 T, int E)
     return r;
 }
 
-/* Balanced base-256 digits of |x| 2^-e (exact), with the sign of x. */
+/* Balanced base-256 digits of |x| 2^-e, with the sign of x.  X is       */
+/* U 2^F truncated to an integer (F = 8s+2 fraction bits); adding        */
+/* B = sum_p 128 2^(F-8p) + 2 turns the balanced digits into the plain   */
+/* base-256 digits of Y = X + B: d_1 = floor(Y / 2^(F-8)) - 128 (up to   */
+/* 128), d_p = (floor(Y / 2^(F-8p)) mod 256) - 128 for p >= 2.  The      */
+/* remainder X_exact - sum_p d_p 2^(F-8p) lies in [-2, 2), i.e.          */
+/* |rem| <= 2^-(8s+1) 2^e; the truncated bits of X never change a digit  */
+/* (the rounding threshold 2 is an integer).                             */
 static void oz_digits(double x, int e, int s, int16_t* d, int64_t stride)
 {
     uint64_t bits;
@@ -550,25 +556,16 @@ static void oz_digits(double x, int e, int s, int16_t* d, int64_t stride)
     const int E2 = ex ? ex - 1075 : -1074;  /* |x| = M 2^E2 */
     const int F = 8 * s + 2;                /* fraction bits kept */
     const int sh = E2 - e + F;              /* U 2^F = M 2^sh */
-    i128 R;
-    int sticky = 0;
-    if (sh >= 0) {
-        R = (i128)((u128)M << sh);
-    } else if (sh > -64) {
-        R = (i128)(M >> (-sh));
-        sticky = (M & ((1ull << (-sh)) - 1)) != 0;
-    } else {
-        R = 0;
-        sticky = 1;
-    }
+    u128 X;
+    if (sh >= 0) X = (u128)M << sh;
+    else if (sh > -64) X = (u128)(M >> (-sh));
+    else X = 0;
+    u128 B = 2;
+    for (int p = 1; p <= s; ++p) B += (u128)128 << (F - 8 * p);
+    const u128 Y = X + B;
     for (int p = 1; p <= s; ++p) {
-        const int w = F - 8 * p;  /* weight of digit p: 2^w */
-        const i128 q = R >> w;    /* floor */
-        const i128 rem = R - (q << w);
-        const i128 half = ((i128)1) << (w - 1);
-        i128 dg = q;
-        if (rem > half || (rem == half && (sticky || (q & 1)))) dg = q + 1;
-        R -= dg << w;
+        const u128 q = Y >> (F - 8 * p);
+        const int dg = (int)(p == 1 ? (uint64_t)q : (uint64_t)(q & 255)) - 128;
         d[(p - 1) * stride] = (int16_t)(neg ? -dg : dg);
     }
 }

@@ -252,28 +252,37 @@ def test_ozaki_kpart_limit():
         assert npairs * (lim + 64) * 128 * 128 >= 2 ** 31 - 1 or lim + 64 > 2 ** 31
 
 
-def _digits_fp64(x, e, s):
-    """The same digits by the floating-point recurrence t = 256 v; d = rint(t);
-    v = t - d (exact for normal-range values)."""
-    v = np.ldexp(x, -e)
+def _digits_exact(x, e, s):
+    """The digit rule restated with Python integers: X = floor(|x| 2^(F-e)),
+    F = 8s+2; Y = X + sum_p 128 2^(F-8p) + 2; d_1 = Y >> (F-8) - 128,
+    d_p = ((Y >> (F-8p)) & 255) - 128; the sign of x on every digit."""
+    from fractions import Fraction
+    F = 8 * s + 2
     out = []
-    for _ in range(s):
-        t = v * 256.0
-        d = np.rint(t)
-        v = t - d
-        out.append(d)
-    return np.array(out)
+    for v in x:
+        X = int(Fraction(abs(float(v))) * Fraction(2) ** (F - int(e)))  # floor of a nonnegative value
+        Y = X + sum(128 << (F - 8 * p) for p in range(1, s + 1)) + 2
+        ds = [(Y >> (F - 8)) - 128] + [((Y >> (F - 8 * p)) & 255) - 128 for p in range(2, s + 1)]
+        out.append([-d if v < 0 else d for d in ds])
+    return np.array(out, dtype=np.int64).T
 
 
-def test_ozaki_integer_digits_match_float_recurrence():
+def test_ozaki_digits_match_integer_restatement():
     r = po.expspread((7, 200), 51)
     r[3, 5] = 0.0
     r[4, :] = po.uniform((1, 200), 52)
-    for s in (3, 8, 12):
+    # the row maximum just below half the row scale: the first digit reaches 128
+    r[5, 0] = np.nextafter(2.0 ** 3, 0.0) * 0.5 * 1.999
+    r[6, :] = 0.0
+    r[6, 3] = 5e-320  # subnormal
+    for s in (3, 7, 8, 12):
         exps, dig = po.ozaki_split(r, s)
+        assert np.abs(dig).max() <= 128
         for i in range(r.shape[0]):
-            ref = _digits_fp64(r[i], exps[i], s)
-            assert np.array_equal(dig[:, i, :], ref.astype(np.int16))
+            ref = _digits_exact(r[i], exps[i], s)
+            assert np.array_equal(dig[:, i, :].astype(np.int64), ref), (s, i)
+    _, dig = po.ozaki_split(np.array([[0.999999]]), 3)
+    assert dig[0, 0, 0] == 128  # U just below 1/2: 128 is the first digit
 
 
 def test_ozaki_recombination_is_correctly_rounded():
