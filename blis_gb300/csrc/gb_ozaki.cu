@@ -65,11 +65,13 @@ struct OzLevel {
 };
 
 struct OzGemmParams {
+    static constexpr bool kDynamic = false;  // items b, b + grid, ... for CTA b
     int slices, nlevels, kb_total, tiles_m, tiles_n, chunk_kb;
     int64_t items, mpad, npad;
     int32_t* planes;  // [plane][npad][mpad]
     unsigned int* status;
     const int* skip;  // non-finite flag of the split kernels
+    unsigned long long* counter;  // unused here
     OzLevel lv[OZ_MAX_SLICES];
 };
 
@@ -101,7 +103,13 @@ struct OzBatchProb {
     int64_t units_a;     // split units (32-row blocks) of op(A); op(B)^T's follow
 };
 
+// Items of the grouped form are handed out by a device counter (zeroed
+// before each launch): the producer warp of a CTA takes the next index and
+// passes it to the MMA and epilogue warps through a shared-memory ring, so
+// the CTAs always work on neighbouring items and share their slices in L2
+// (a fixed stride lets fast and slow CTAs drift apart across problems).
 struct OzBatchParams {
+    static constexpr bool kDynamic = true;
     int slices, nlevels, chunk_kb, nprob;
     int64_t items, boxes_a, boxes_b;  // work items; boxes per slice plane
     const OzBatchProb* probs;
@@ -109,8 +117,61 @@ struct OzBatchParams {
     const int64_t* item_base;  // first work item of each problem
     unsigned int* status;
     const int* skip;
+    unsigned long long* counter;
     OzLevel lv[OZ_MAX_SLICES];
 };
+
+constexpr int OZ_IRING = 4;  // work-item ring depth (dynamic form)
+
+// Work-item ring of one CTA: the producer publishes, the MMA warp and the 8
+// epilogue warps (one arrival each) release.  `it` starts at -2; the next
+// index is returned in it, -1 when there is none.  False: a wait timed out.
+struct OzRing {
+    uint64_t* full;
+    uint64_t* empty;
+    volatile long long* slot_val;
+    int slot;
+    uint32_t phase;
+};
+
+template <class P>
+__device__ __forceinline__ bool oz_publish_item(const P& p, OzRing& r, int64_t& it)
+{
+    if constexpr (P::kDynamic) {
+        if (!mbar_wait_bounded(&r.empty[r.slot], r.phase ^ 1u, kWaitBudgetNs)) return false;
+        long long v = (long long)atomicAdd(p.counter, 1ull);
+        if (v >= p.items) v = -1;
+        r.slot_val[r.slot] = v;
+        mbar_arrive(&r.full[r.slot]);
+        if (++r.slot == OZ_IRING) {
+            r.slot = 0;
+            r.phase ^= 1u;
+        }
+        it = v;
+    } else {
+        it = (it == -2) ? (int64_t)blockIdx.x : it + gridDim.x;
+        if (it >= p.items) it = -1;
+    }
+    return true;
+}
+
+template <class P>
+__device__ __forceinline__ bool oz_receive_item(const P& p, OzRing& r, int64_t& it)
+{
+    if constexpr (P::kDynamic) {
+        if (!mbar_wait_bounded(&r.full[r.slot], r.phase, kWaitBudgetNs)) return false;
+        it = r.slot_val[r.slot];
+        mbar_arrive(&r.empty[r.slot]);
+        if (++r.slot == OZ_IRING) {
+            r.slot = 0;
+            r.phase ^= 1u;
+        }
+    } else {
+        it = (it == -2) ? (int64_t)blockIdx.x : it + gridDim.x;
+        if (it >= p.items) it = -1;
+    }
+    return true;
+}
 
 __device__ __forceinline__ OzItem oz_decode(const OzGemmParams& p, int64_t it)
 {
@@ -235,7 +296,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     uint64_t* tfull = empty + OZ_STAGES;
     uint64_t* tempty = tfull + 2;
     uint64_t* drain = tempty + 2;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+    uint64_t* ifull = drain + 1;  // work-item ring (dynamic form)
+    uint64_t* iempty = ifull + OZ_IRING;
+    volatile long long* iring = reinterpret_cast<volatile long long*>(iempty + OZ_IRING);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(const_cast<long long*>(iring + OZ_IRING));
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -250,6 +314,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             mbar_init(&tempty[i], OZ_EPI_WARPS);
         }
         mbar_init(drain, 1);
+        for (int i = 0; i < OZ_IRING; ++i) {
+            mbar_init(&ifull[i], 1);
+            mbar_init(&iempty[i], 1 + OZ_EPI_WARPS);  // the MMA warp and every epilogue warp
+        }
         *abort_flag = 0;
         fence_barrier_init();
         fence_proxy_async();
@@ -273,8 +341,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             uint32_t phase = 0;
             uint32_t issued_mask = 0, last_phase = 0;
             bool ok = true;
-            for (int64_t it = blockIdx.x; it < p.items && ok; it += gridDim.x) {
+            OzRing ring{ifull, iempty, iring, 0, 0u};
+            for (int64_t it = -2; ok;) {
                 if (*abort_flag) break;
+                if (!oz_publish_item(p, ring, it)) {
+                    oz_fail(p, abort_flag);
+                    break;
+                }
+                if (it < 0) break;
                 const OzItem w = oz_decode(p, it);
                 for (int pi = 0; pi < w.npairs && ok; ++pi) {
                     const int pa = w.pa_lo + pi, pb = w.lev - pa;
@@ -311,8 +385,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             uint32_t phase = 0;
             uint32_t chunk_ctr = 0;
             bool ok = true, issued_any = false;
-            for (int64_t it = blockIdx.x; it < p.items && ok; it += gridDim.x) {
+            OzRing ring{ifull, iempty, iring, 0, 0u};
+            for (int64_t it = -2; ok;) {
                 if (*abort_flag) break;
+                if (!oz_receive_item(p, ring, it)) {
+                    oz_fail(p, abort_flag);
+                    break;
+                }
+                if (it < 0) break;
                 const OzItem w = oz_decode(p, it);
                 const int total = w.npairs * w.kbn;
                 for (int t0 = 0; t0 < total && ok; t0 += p.chunk_kb) {
@@ -361,8 +441,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         const int quad = warp & 3, half = warp >> 2;
         uint32_t chunk_ctr = 0;
         bool ok = true;
-        for (int64_t it = blockIdx.x; it < p.items && ok; it += gridDim.x) {
+        OzRing ring{ifull, iempty, iring, 0, 0u};
+        for (int64_t it = -2; ok;) {
             if (__shfl_sync(0xffffffffu, *abort_flag, 0)) break;
+            long long next = 0;
+            int got = 1;
+            if (lane == 0) {
+                int64_t t = it;
+                got = oz_receive_item(p, ring, t) ? 1 : 0;
+                next = t;
+            }
+            got = __shfl_sync(0xffffffffu, got, 0);
+            next = __shfl_sync(0xffffffffu, next, 0);
+            if (!got) {
+                if (lane == 0) oz_fail(p, abort_flag);
+                break;
+            }
+            it = next;
+            if (it < 0) break;
             const OzItem w = oz_decode(p, it);
             const int total = w.npairs * w.kbn;
             const int nchunks = (total + p.chunk_kb - 1) / p.chunk_kb;
@@ -1274,6 +1370,7 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     p.planes = planes;
     p.status = device_status_word();
     p.skip = nonfinite;
+    p.counter = nullptr;
 
     int rc = GB_SUCCESS;
     auto bail = [&](int code) { dev_free(ws, s); return code; };
@@ -1414,7 +1511,8 @@ struct OzBatch {
     int64_t* d_unit_base = nullptr;
     int32_t* d_rblock_prob = nullptr;
     int64_t* d_rblock_base = nullptr;
-    int* d_flag = nullptr;
+    int* d_flag = nullptr;                   // Inf/NaN flag; the work-item counter 256 bytes on
+    unsigned long long* d_counter = nullptr;
     uint16_t* sa = nullptr;
     uint16_t* sb = nullptr;
     CUtensorMap map_a, map_b;
@@ -1578,6 +1676,7 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
     ob->d_rblock_prob = reinterpret_cast<int32_t*>(take(b_rp));
     ob->d_rblock_base = reinterpret_cast<int64_t*>(take(b_rb));
     ob->d_flag = reinterpret_cast<int*>(take(1024));
+    ob->d_counter = reinterpret_cast<unsigned long long*>(reinterpret_cast<uint8_t*>(ob->d_flag) + 256);
     int64_t pl_off = 0, ex_off = 0;
     for (auto& q : h) {
         q.planes = planes + pl_off;
@@ -1622,6 +1721,7 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
     gp.item_base = ob->d_item_base;
     gp.status = device_status_word();
     gp.skip = ob->d_flag;
+    gp.counter = ob->d_counter;
     *out = ob;
     return GB_SUCCESS;
 }
@@ -1632,7 +1732,9 @@ int ozaki_batch_launch(OzBatch* ob, cudaStream_t s)
 {
     if (!ob || ob->nprob == 0) return GB_SUCCESS;
     int rc;
-    if ((rc = check_cuda(cudaMemsetAsync(ob->d_flag, 0, sizeof(int), s), "memset"))) return rc;
+    // the flag and the work-item counter (256 bytes further) in one memset
+    if ((rc = check_cuda(cudaMemsetAsync(ob->d_flag, 0, 256 + sizeof(unsigned long long), s), "memset")))
+        return rc;
     {
         LaunchScope ls("oz_split_batch", s);
         switch (ob->slices) {
