@@ -41,8 +41,8 @@ __global__ void __launch_bounds__(NT) grouped_gemm_kernel(const BatchDesc* __res
                                                           unsigned long long* counter, const int* gate)
 {
     if (gate && *gate == 0) return;  // fallback launch of the Ozaki form: only on Inf/NaN operands
-    __shared__ __align__(16) T As[(DMMA ? 1 : 2) * BK * LDS];  // FP32: two stages
-    __shared__ __align__(16) T Bs[(DMMA ? 1 : 2) * BK * LDS];
+    __shared__ T As[BK * LDS];
+    __shared__ T Bs[BK * LDS];
     __shared__ long long tile_s;
     for (;;) {
         if (threadIdx.x == 0) tile_s = (long long)atomicAdd(counter, 1ull);
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(NT) grouped_gemm_kernel(const BatchDesc* __res
         GArgs<T> p{q.m, q.n, q.k, (T)q.alpha, (T)q.beta, static_cast<const T*>(q.a), q.ars, q.acs,
                    static_cast<const T*>(q.b), q.brs, q.bcs, static_cast<T*>(q.c), q.rs_c, q.cs_c};
         if constexpr (DMMA) dmma_tile(p, bm, bn, As, Bs);
-        else sgemm_tile(p, bm, bn, As, Bs);
+        else simt_tile<T>(p, bm, bn, As, Bs);
     }
 }
 

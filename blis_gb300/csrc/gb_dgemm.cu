@@ -41,11 +41,27 @@ __global__ void __launch_bounds__(NT) gemm_simt_kernel(GArgs<T> p, const int* ga
     simt_tile<T>(p, (int64_t)blockIdx.y * BM, (int64_t)blockIdx.x * BN, As, Bs);
 }
 
+template <bool VEC, bool A_RC, bool B_RC>
 __global__ void __launch_bounds__(NT) sgemm_kernel(GArgs<float> p)
 {
     __shared__ __align__(16) float As[2 * BK * LDS];
     __shared__ __align__(16) float Bs[2 * BK * LDS];
-    sgemm_tile(p, (int64_t)blockIdx.y * BM, (int64_t)blockIdx.x * BN, As, Bs);
+    sgemm_tile<VEC, A_RC, B_RC>(p, (int64_t)blockIdx.y * BM, (int64_t)blockIdx.x * BN, As, Bs);
+}
+
+// Whole tiles and k blocks only, 16-byte aligned operands, one unit stride
+// per operand with the other stride a multiple of 4 floats.
+bool sgemm_vec_ok(const GArgs<float>& p, bool* a_rc, bool* b_rc)
+{
+    if (p.m % BM || p.n % BN || p.k % BK) return false;
+    if ((reinterpret_cast<uintptr_t>(p.a) | reinterpret_cast<uintptr_t>(p.b)) & 15) return false;
+    if (p.ars == 1 && p.acs % 4 == 0) *a_rc = true;
+    else if (p.acs == 1 && p.ars % 4 == 0) *a_rc = false;
+    else return false;
+    if (p.bcs == 1 && p.brs % 4 == 0) *b_rc = true;
+    else if (p.brs == 1 && p.bcs % 4 == 0) *b_rc = false;
+    else return false;
+    return true;
 }
 
 template <typename T>
@@ -137,8 +153,14 @@ int sgemm_dev(int64_t m, int64_t n, int64_t k, float alpha,
     const int64_t gx = (n + BN - 1) / BN, gy = (m + BM - 1) / BM;
     if (gy > 65535) return set_error(GB_ERR_ARG, "gb_sgemm", "m too large for one launch");
     GArgs<float> p{m, n, k, alpha, beta, a, ars, acs, b, brs, bcs, c, rs_c, cs_c};
+    const dim3 grid((unsigned)gx, (unsigned)gy);
+    bool a_rc = true, b_rc = false;
     LaunchScope ls("sgemm_ffma", s);
-    sgemm_kernel<<<dim3((unsigned)gx, (unsigned)gy), NT, 0, s>>>(p);
+    if (!sgemm_vec_ok(p, &a_rc, &b_rc)) sgemm_kernel<false, true, false><<<grid, NT, 0, s>>>(p);
+    else if (a_rc && !b_rc) sgemm_kernel<true, true, false><<<grid, NT, 0, s>>>(p);
+    else if (a_rc && b_rc) sgemm_kernel<true, true, true><<<grid, NT, 0, s>>>(p);
+    else if (!a_rc && !b_rc) sgemm_kernel<true, false, false><<<grid, NT, 0, s>>>(p);
+    else sgemm_kernel<true, false, true><<<grid, NT, 0, s>>>(p);
     return check_cuda(cudaGetLastError(), "sgemm");
 }
 

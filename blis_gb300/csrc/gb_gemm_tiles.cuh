@@ -171,11 +171,53 @@ __device__ __forceinline__ void simt_tile(const GArgs<T>& p, int64_t bm, int64_t
         for (int j = 0; j < 8; ++j) write_c(p, bm + ty * 8 + i, bn + tx * 8 + j, acc[i][j]);
 }
 
+// Aligned operand tiles for the FP32 engine: a 128 x 16 (rows x k) tile of
+// X(r, l) = x[r*rs + l*ls] as two 16-byte loads per thread, when either the
+// rows are contiguous (rs == 1, ls a multiple of 4: vectors along r) or k
+// is (ls == 1, rs a multiple of 4: vectors along l); the tile must lie
+// inside the matrix.  S[l*LDS + r] is the shared-memory image.
+template <bool R_CONTIG>
+__device__ __forceinline__ void load_vec_tile(const float* __restrict__ x, int64_t rs, int64_t ls, int64_t r0,
+                                              int64_t l0, float4 (&v)[2])
+{
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        int r, l;
+        if (R_CONTIG) { r = (t & 31) * 4; l = (t >> 5) + 8 * q; }
+        else { l = (t & 3) * 4; r = (t >> 2) + 64 * q; }
+        v[q] = __ldg(reinterpret_cast<const float4*>(x + (r0 + r) * rs + (l0 + l) * ls));
+    }
+}
+
+template <bool R_CONTIG>
+__device__ __forceinline__ void store_vec_tile(const float4 (&v)[2], float* S)
+{
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        if (R_CONTIG) {
+            *reinterpret_cast<float4*>(S + ((t >> 5) + 8 * q) * LDS + (t & 31) * 4) = v[q];
+        } else {
+            const int l = (t & 3) * 4, r = (t >> 2) + 64 * q;
+            S[(l + 0) * LDS + r] = v[q].x;
+            S[(l + 1) * LDS + r] = v[q].y;
+            S[(l + 2) * LDS + r] = v[q].z;
+            S[(l + 3) * LDS + r] = v[q].w;
+        }
+    }
+}
+
 // FP32 tile engine: two shared-memory stages (one barrier per 16-deep k
 // block, the next block's global loads overlap the FMAs), and each thread's
 // 8x8 block split into 4-row/4-column halves 64 apart so its fragments are
 // two 16-byte loads per operand per k step: B's are conflict-free across the
-// warp, A's are broadcasts.  As/Bs hold 2*BK*LDS floats each.
+// warp, A's are broadcasts.  As/Bs hold 2*BK*LDS floats each.  VEC: every
+// tile and k block lies inside the matrices and both operands meet the
+// conditions of load_vec_tile; A_RC: op(A)(i, l) contiguous in i (ars == 1),
+// otherwise in l; B_RC: op(B)(l, j) contiguous in j (bcs == 1), otherwise
+// in l.
+template <bool VEC = false, bool A_RC = true, bool B_RC = false>
 __device__ __forceinline__ void sgemm_tile(const GArgs<float>& p, int64_t bm, int64_t bn, float* As, float* Bs)
 {
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -185,13 +227,31 @@ __device__ __forceinline__ void sgemm_tile(const GArgs<float>& p, int64_t bm, in
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
     float ra[8], rb[8];
-    load_tiles(p, bm, bn, 0, ra, rb);
-    store_tiles(p, ra, rb, As, Bs);
+    float4 va[2], vb[2];
+    // B's tile as rows j (= n index) x k: X(j, l) = b[j*bcs + l*brs]
+    auto fetch = [&](int64_t k0) {
+        if constexpr (VEC) {
+            load_vec_tile<A_RC>(p.a, p.ars, p.acs, bm, k0, va);
+            load_vec_tile<B_RC>(p.b, p.bcs, p.brs, bn, k0, vb);
+        } else {
+            load_tiles(p, bm, bn, k0, ra, rb);
+        }
+    };
+    auto stash = [&](float* A, float* B) {
+        if constexpr (VEC) {
+            store_vec_tile<A_RC>(va, A);
+            store_vec_tile<B_RC>(vb, B);
+        } else {
+            store_tiles(p, ra, rb, A, B);
+        }
+    };
+    fetch(0);
+    stash(As, Bs);
     __syncthreads();
     int cur = 0;
     for (int64_t k0 = 0; k0 < p.k; k0 += BK) {
         const bool more = (k0 + BK < p.k);
-        if (more) load_tiles(p, bm, bn, k0 + BK, ra, rb);
+        if (more) fetch(k0 + BK);
         const float* A = As + cur * (BK * LDS);
         const float* B = Bs + cur * (BK * LDS);
 #pragma unroll
@@ -209,7 +269,7 @@ __device__ __forceinline__ void sgemm_tile(const GArgs<float>& p, int64_t bm, in
         }
         if (more) {
             // the other stage was last read before the previous barrier
-            store_tiles(p, ra, rb, As + (cur ^ 1) * (BK * LDS), Bs + (cur ^ 1) * (BK * LDS));
+            stash(As + (cur ^ 1) * (BK * LDS), Bs + (cur ^ 1) * (BK * LDS));
             __syncthreads();
             cur ^= 1;
         }
