@@ -145,7 +145,8 @@ def test_dgemm_device_config1_vs_dd():
     assert np.all(np.abs(c[ii, jj] - hi - lo) <= 2 * n * H.EPS * g)
 
 
-@pytest.mark.parametrize("m,n,k", [(100, 100, 100), (257, 129, 300)])
+# (256, 384, 128): whole 128 x 128 tiles and 16-deep k blocks, the aligned fast path
+@pytest.mark.parametrize("m,n,k", [(100, 100, 100), (257, 129, 300), (256, 384, 128)])
 @pytest.mark.parametrize("ta", [N, T])
 @pytest.mark.parametrize("tb", [N, T])
 def test_sgemm_testsuite_residual(m, n, k, ta, tb):
@@ -160,8 +161,8 @@ def test_sgemm_testsuite_residual(m, n, k, ta, tb):
     assert r < 1e-5
 
 
-def test_sgemm_narrow_pow2_bit_exact():
-    m, n, k = 200, 150, 300
+@pytest.mark.parametrize("m,n,k", [(200, 150, 300), (256, 128, 64)])
+def test_sgemm_narrow_pow2_bit_exact(m, n, k):
     a = po.narrow_pow2((m, k), 8).astype(np.float32, order="F")
     b = po.narrow_pow2((k, n), 9).astype(np.float32, order="F")
     c = np.zeros((m, n), np.float32, order="F")
