@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(NT) gemm_simt_kernel(GArgs<T> p, const int* ga
 }
 
 template <bool VEC, bool A_RC, bool B_RC>
-__global__ void __launch_bounds__(NT) sgemm_kernel(GArgs<float> p)
+__global__ void __launch_bounds__(NT, 2) sgemm_kernel(GArgs<float> p)  // two CTAs (16 warps) per SM
 {
     __shared__ __align__(16) float As[2 * BK * LDS];
     __shared__ __align__(16) float Bs[2 * BK * LDS];

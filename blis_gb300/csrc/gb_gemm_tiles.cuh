@@ -190,6 +190,13 @@ __device__ __forceinline__ void load_vec_tile(const float* __restrict__ x, int64
     }
 }
 
+// Group swizzle of a transposed tile: in row l the 4-float groups are
+// permuted by XOR with vec_swz(l), so the four rows a warp stores at once
+// (l = 0, 4, 8, 12 apart) land in different banks; readers of row l XOR the
+// group index the same way (a permutation: 16-byte fragments stay whole and
+// conflict-free).
+__device__ __forceinline__ int vec_swz(int l) { return ((l >> 2) & 3) << 1; }
+
 template <bool R_CONTIG>
 __device__ __forceinline__ void store_vec_tile(const float4 (&v)[2], float* S)
 {
@@ -200,10 +207,10 @@ __device__ __forceinline__ void store_vec_tile(const float4 (&v)[2], float* S)
             *reinterpret_cast<float4*>(S + ((t >> 5) + 8 * q) * LDS + (t & 31) * 4) = v[q];
         } else {
             const int l = (t & 3) * 4, r = (t >> 2) + 64 * q;
-            S[(l + 0) * LDS + r] = v[q].x;
-            S[(l + 1) * LDS + r] = v[q].y;
-            S[(l + 2) * LDS + r] = v[q].z;
-            S[(l + 3) * LDS + r] = v[q].w;
+            const float e[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                S[(l + u) * LDS + (((r >> 2) ^ vec_swz(l + u)) << 2) + (r & 3)] = e[u];
         }
     }
 }
@@ -256,10 +263,12 @@ __device__ __forceinline__ void sgemm_tile(const GArgs<float>& p, int64_t bm, in
         const float* B = Bs + cur * (BK * LDS);
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
-            const float4 a0 = *reinterpret_cast<const float4*>(A + kk * LDS + ty * 4);
-            const float4 a1 = *reinterpret_cast<const float4*>(A + kk * LDS + 64 + ty * 4);
-            const float4 b0 = *reinterpret_cast<const float4*>(B + kk * LDS + tx * 4);
-            const float4 b1 = *reinterpret_cast<const float4*>(B + kk * LDS + 64 + tx * 4);
+            // transposed tiles of the aligned path carry the group swizzle
+            const int sa = (VEC && !A_RC) ? vec_swz(kk) : 0, sb = (VEC && !B_RC) ? vec_swz(kk) : 0;
+            const float4 a0 = *reinterpret_cast<const float4*>(A + kk * LDS + ((ty ^ sa) << 2));
+            const float4 a1 = *reinterpret_cast<const float4*>(A + kk * LDS + 64 + ((ty ^ sa) << 2));
+            const float4 b0 = *reinterpret_cast<const float4*>(B + kk * LDS + ((tx ^ sb) << 2));
+            const float4 b1 = *reinterpret_cast<const float4*>(B + kk * LDS + 64 + ((tx ^ sb) << 2));
             const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
             const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
