@@ -45,8 +45,10 @@ SIZE = 16384
 SLICES = 8
 EMIN, EMAX = -20, 20
 SEED_A, SEED_B = 20261204, 20261205
-TRAFFIC_4096_BYTES = 7514446000 + 530606336  # ozaki_slice_gemm, 4096^3, 8 slices (ncu)
-TRAFFIC_SLICES = 8
+# DRAM read + write bytes of one ozaki_slice_gemm_pair_kernel launch at 4096^3, 7 slices, from
+# one ncu --set full capture (dram__bytes_read.sum + dram__bytes_write.sum)
+TRAFFIC_4096_BYTES = 7672756000 + 470106624
+TRAFFIC_SLICES = 7
 
 
 def parse():
@@ -333,10 +335,9 @@ def run_gpu(args):
     # cn holds column-major C, i.e. cn[j, i] == C[i, j]
     e2e_ok = bool(np.array_equal(cn[:64, :64], Cz[:64, :64].t().contiguous().cpu().numpy()))
 
-    # ---------------- DRAM traffic of the dominant kernel: one ncu capture at 4096^3
-    # (dram__bytes_read.sum + dram__bytes_write.sum, profiles/ozaki_slice_gemm_4096_full.md),
-    # scaled by the slice-product units of this size, (n/4096)^3
-    # and by the slice-product count (traffic per product is the same tiling)
+    # ---------------- DRAM traffic of the dominant kernel: the ncu capture at 4096^3 above,
+    # scaled by the slice-product units of this size, (n/4096)^3, and by the slice-product
+    # count (traffic per product is the same tiling)
     traffic = TRAFFIC_4096_BYTES * (n / 4096.0) ** 3 * npairs / (TRAFFIC_SLICES * (TRAFFIC_SLICES + 1) // 2)
 
     if rank != 0:

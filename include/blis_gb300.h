@@ -216,7 +216,7 @@ void bli_ddotv_ex(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t n, const double* x,
 
 /* Host-pointer entry points under the addon prefix, with the typed-API
    argument lists above.  A BLIS build that keeps its own bli_?gemm symbols
-   (for instance the gb300 sandbox's bli_gemm_ex) calls
+   (for instance a sandbox bli_gemm_ex that forwards to this library) calls
    these instead, which cannot resolve back into libblis. */
 void gb_dgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
               const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
