@@ -88,6 +88,10 @@ def load(path=None):
     _sig(L, "gb_daxpyv_dev", C.c_int, [_i64, _d, _vp, _i64, _vp, _i64, _vp])
     _sig(L, "gb_ddotv_dev", C.c_int, [_i64, _vp, _i64, _vp, _i64, _vp, _vp])
     _sig(L, "gb_dgemv_dev", C.c_int, [C.c_int, _i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _d, _vp, _i64, _vp])
+    _sig(L, "gb_bgemm_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, _i64, _f, _vp, _i64, _i64, _vp, _i64, _i64,
+                                        _f, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_gemm_config_dev", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _i64, _i64, _i64, _d, _vp, _i64,
+                                            _i64, _vp, _i64, _i64, _d, _vp, _i64, _i64, _vp])
     _sig(L, "gb_gemm_batch_dev", C.c_int, [_vp, _i64, C.c_int, C.c_int, _vp])
     _sig(L, "gb_batch_plan_create", C.c_int, [_vp, _i64, C.c_int, C.POINTER(C.c_void_p)])
     _sig(L, "gb_batch_plan_run", C.c_int, [_vp, C.c_int, _vp])

@@ -101,6 +101,11 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
               const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b,
               int64_t cs_b, int slices, cudaStream_t s);
 int64_t ozaki_kpart_limit(int slices);
+// bf16 GEMM on the tensor cores (gb_ozaki.cu): C fp32, A and B as bf16 bit
+// patterns with element strides.
+int bgemm_tc(int64_t m, int64_t n, int64_t k, float alpha, const uint16_t* a, int64_t ars, int64_t acs,
+             const uint16_t* b, int64_t brs, int64_t bcs, float beta, float* c, int64_t rs_c, int64_t cs_c,
+             cudaStream_t s);
 // Grouped Ozaki form for gemm_batch (gb_ozaki.cu): every accepted problem
 // (m, n, k > 0, alpha != 0, ozaki_batch_accepts) in three launches.  The
 // flag is raised when an operand holds Inf/NaN; the launches then do

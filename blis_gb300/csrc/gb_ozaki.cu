@@ -66,6 +66,7 @@ struct OzLevel {
 
 struct OzGemmParams {
     static constexpr bool kDynamic = false;  // items b, b + grid, ... for CTA b
+    static constexpr bool kRawAcc = false;   // chunks are converted to int32 and summed
     int slices, nlevels, kb_total, tiles_m, tiles_n, chunk_kb;
     int64_t items, mpad, npad;
     int32_t* planes;  // [plane][npad][mpad]
@@ -110,6 +111,7 @@ struct OzBatchProb {
 // (a fixed stride lets fast and slow CTAs drift apart across problems).
 struct OzBatchParams {
     static constexpr bool kDynamic = true;
+    static constexpr bool kRawAcc = false;
     int slices, nlevels, chunk_kb, nprob;
     int64_t items, boxes_a, boxes_b;  // work items; boxes per slice plane
     const OzBatchProb* probs;
@@ -275,6 +277,72 @@ __device__ __forceinline__ void oz_store_sums(const OzBatchParams& p, const OzIt
         if (c < jn) dst[(int64_t)c * q.ld] = acc[c];
 }
 
+// ---------------------------------------------------------------- BF16 GEMM
+// The same kernel as a plain bf16 GEMM (no Ozaki slices): C (fp32) :=
+// alpha A B + beta C with A, B in bf16.  One "slice", one level with one
+// product, a single chunk over the whole k range (fp32 accumulation in TMEM
+// needs no exactness here), and an epilogue that writes fp32 C instead of
+// int32 level sums.  Operands arrive by TMA straight from the caller's
+// K-contiguous rows (or from a packed copy); zero fill past m, n and k.
+struct BgemmParams {
+    static constexpr bool kDynamic = false;
+    static constexpr bool kRawAcc = true;
+    int tiles_m, tiles_n, kb_total, chunk_kb;
+    int64_t items, m, n;
+    float alpha, beta;
+    float* c;
+    int64_t rs_c, cs_c;
+    unsigned int* status;
+    const int* skip;  // null: nothing gates this form
+    unsigned long long* counter;
+};
+
+__device__ __forceinline__ OzItem oz_decode(const BgemmParams& p, int64_t it)
+{
+    // grouped raster as in the Ozaki form: OZ_GROUP_M tile rows per group
+    const int64_t group = it / (OZ_GROUP_M * (int64_t)p.tiles_n);
+    const int64_t first_m = group * OZ_GROUP_M;
+    const int64_t gm = (p.tiles_m - first_m < OZ_GROUP_M) ? p.tiles_m - first_m : OZ_GROUP_M;
+    const int64_t wi = it - group * OZ_GROUP_M * (int64_t)p.tiles_n;
+    OzItem w;
+    w.lev = 2;
+    w.npairs = 1;
+    w.pa_lo = 1;
+    w.tm = (int)(first_m + wi % gm);
+    w.tn = (int)(wi / gm);
+    w.kb0 = 0;
+    w.kbn = p.kb_total;
+    w.plane = 0;
+    w.prob = 0;
+    return w;
+}
+
+__device__ __forceinline__ void oz_load_stage(const BgemmParams&, const CUtensorMap* ma, const CUtensorMap* mb,
+                                              uint8_t* sa, uint8_t* sb, uint64_t* bar, const OzItem& w, int,
+                                              int, int kb)
+{
+    tma_load_3d(sa, ma, bar, kb * OZ_BK, w.tm * OZ_BM, 0);
+    tma_load_3d(sb, mb, bar, kb * OZ_BK, w.tn * OZ_BN, 0);
+}
+
+__device__ __forceinline__ void oz_store_sums(const BgemmParams& p, const OzItem& w, int quad, int half, int lane,
+                                              const int32_t (&acc)[128])
+{
+    const int64_t i = (int64_t)w.tm * OZ_BM + quad * 32 + lane;
+    const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
+    if (i >= p.m) return;
+    const int64_t jn = p.n - j0;
+    float* ci = p.c + i * p.rs_c + j0 * p.cs_c;
+#pragma unroll
+    for (int c = 0; c < 128; ++c) {
+        if (c < jn) {
+            float* cij = ci + (int64_t)c * p.cs_c;
+            const float t = p.alpha * __int_as_float(acc[c]);
+            *cij = (p.beta == 0.0f) ? t : fmaf(p.beta, *cij, t);
+        }
+    }
+}
+
 template <class P>
 __device__ __forceinline__ void oz_fail(const P& p, volatile int* abort_flag)
 {
@@ -287,7 +355,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     ozaki_slice_gemm_kernel(const __grid_constant__ CUtensorMap map_a,
                             const __grid_constant__ CUtensorMap map_b, const __grid_constant__ P p)
 {
-    if (*p.skip) return;  // uniform across the CTA: the native kernel takes over
+    if (p.skip && *p.skip) return;  // uniform across the CTA: the native kernel takes over
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                ~uintptr_t(1023));
@@ -483,7 +551,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                     tmem_ld_32x32b_x32(taddr + g * 32, r);
                     tmem_ld_wait();
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) acc[g * 32 + i] += __float2int_rn(__uint_as_float(r[i]));
+                    for (int i = 0; i < 32; ++i) {
+                        if constexpr (P::kRawAcc) acc[g * 32 + i] = (int32_t)r[i];  // one chunk: fp32 bits
+                        else acc[g * 32 + i] += __float2int_rn(__uint_as_float(r[i]));
+                    }
                 }
                 tc_fence_before();
                 __syncwarp();
@@ -1775,6 +1846,140 @@ void ozaki_batch_destroy(OzBatch* ob, cudaStream_t s)
     if (!ob) return;
     dev_free(ob->arena, s);
     delete ob;
+}
+
+// ---------------------------------------------------------------- BF16 GEMM host side
+namespace {
+
+// K-major copy of a bf16 operand: out[r*kst + l] = X(r, l) = x[r*rs + l*ls],
+// 32 x 32 tiles through shared memory (coalesced on both sides).
+__global__ void bf16_pack_kernel(int64_t rows, int64_t k, const uint16_t* __restrict__ x, int64_t rs, int64_t ls,
+                                 uint16_t* __restrict__ out, int64_t kst)
+{
+    __shared__ uint16_t t[32][33];
+    const int64_t r0 = (int64_t)blockIdx.y * 32, l0 = (int64_t)blockIdx.x * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+    const bool rows_fast = (rs == 1);
+    for (int q = ty; q < 32; q += 8) {
+        const int64_t r = r0 + (rows_fast ? tx : q), l = l0 + (rows_fast ? q : tx);
+        const uint16_t v = (r < rows && l < k) ? x[r * rs + l * ls] : (uint16_t)0;
+        if (rows_fast) t[tx][q] = v;
+        else t[q][tx] = v;
+    }
+    __syncthreads();
+    for (int q = ty; q < 32; q += 8) {
+        const int64_t r = r0 + q, l = l0 + tx;
+        if (r < rows && l < kst) out[r * kst + l] = (l < k) ? t[q][tx] : (uint16_t)0;
+    }
+}
+
+// Rows x k bf16 with row stride `rst` elements (k contiguous), boxes of
+// 64 k x box_rows rows, zero fill outside.
+int make_kmajor_map(CUtensorMap* map, const void* base, int64_t k, int64_t rows, int64_t rst, int box_rows)
+{
+    auto fn = encode_fn();
+    if (!fn) return set_error(GB_ERR_CUDA, "bgemm", "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[3] = {(cuuint64_t)k, (cuuint64_t)rows, 1};
+    cuuint64_t strides[2] = {(cuuint64_t)(rst * 2), (cuuint64_t)(rst * 2 * rows)};
+    cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(GB_ERR_CUDA, "bgemm", "cuTensorMapEncodeTiled failed");
+    return GB_SUCCESS;
+}
+
+// The operand as TMA-loadable K-major rows: the caller's memory when k is
+// contiguous (ls == 1) with a 16-byte row stride and base, else a packed copy.
+int bf16_kmajor(const uint16_t* x, int64_t rows, int64_t k, int64_t rs, int64_t ls, cudaStream_t s,
+                const uint16_t** out, int64_t* rst, uint16_t** owned)
+{
+    *owned = nullptr;
+    if (ls == 1 && rs % 8 == 0 && rs >= k && (reinterpret_cast<uintptr_t>(x) & 15) == 0) {
+        *out = x;
+        *rst = rs;
+        return GB_SUCCESS;
+    }
+    const int64_t kst = round_up(k, 8);
+    uint16_t* buf = static_cast<uint16_t*>(dev_alloc(sizeof(uint16_t) * (size_t)(rows * kst), s));
+    if (!buf) return GB_ERR_NOMEM;
+    const int64_t gy = (rows + 31) / 32, gx = (kst + 31) / 32;
+    if (gy > 65535) {
+        dev_free(buf, s);
+        return set_error(GB_ERR_ARG, "bgemm", "too many rows for the pack grid");
+    }
+    {
+        LaunchScope ls2("bf16_pack", s);
+        bf16_pack_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, x, rs, ls, buf, kst);
+    }
+    int rc = check_cuda(cudaGetLastError(), "bf16_pack");
+    if (rc) {
+        dev_free(buf, s);
+        return rc;
+    }
+    *out = buf;
+    *rst = kst;
+    *owned = buf;
+    return GB_SUCCESS;
+}
+
+}  // namespace
+
+// C (fp32) := alpha op(A) op(B) + beta C with bf16 A, B on the tensor cores
+// (tcgen05.mma kind::f16, bf16 in, fp32 accumulate).  op(A)(i, l) =
+// a[i*ars + l*acs], op(B)(l, j) = b[l*brs + j*bcs].
+int bgemm_tc(int64_t m, int64_t n, int64_t k, float alpha, const uint16_t* a, int64_t ars, int64_t acs,
+             const uint16_t* b, int64_t brs, int64_t bcs, float beta, float* c, int64_t rs_c, int64_t cs_c,
+             cudaStream_t s)
+{
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    if (alpha == 0.0f || k <= 0) return scal_matrix_f(m, n, beta, c, rs_c, cs_c, s);
+    if (m > INT32_MAX || n > INT32_MAX || k > INT32_MAX)
+        return set_error(GB_ERR_ARG, "bgemm", "dimension too large for TMA coordinates");
+    const uint16_t *ak, *bk;
+    int64_t ast, bst;
+    uint16_t *own_a = nullptr, *own_b = nullptr;
+    int rc = bf16_kmajor(a, m, k, ars, acs, s, &ak, &ast, &own_a);
+    if (!rc) rc = bf16_kmajor(b, n, k, bcs, brs, s, &bk, &bst, &own_b);  // rows of op(B)^T
+    CUtensorMap map_a, map_b;
+    if (!rc) rc = make_kmajor_map(&map_a, ak, k, m, ast, OZ_BM);
+    if (!rc) rc = make_kmajor_map(&map_b, bk, k, n, bst, OZ_BN);
+    if (!rc) {
+        static bool attr = false;
+        if (!attr) {
+            rc = check_cuda(cudaFuncSetAttribute(ozaki_slice_gemm_kernel<BgemmParams>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM_BYTES),
+                            "smem attr");
+            attr = (rc == GB_SUCCESS);
+        }
+    }
+    if (!rc) {
+        BgemmParams p;
+        p.tiles_m = (int)((m + OZ_BM - 1) / OZ_BM);
+        p.tiles_n = (int)((n + OZ_BN - 1) / OZ_BN);
+        p.kb_total = (int)((k + OZ_BK - 1) / OZ_BK);
+        p.chunk_kb = p.kb_total;  // one chunk: fp32 accumulation over the whole k range
+        p.items = (int64_t)p.tiles_m * p.tiles_n;
+        p.m = m;
+        p.n = n;
+        p.alpha = alpha;
+        p.beta = beta;
+        p.c = c;
+        p.rs_c = rs_c;
+        p.cs_c = cs_c;
+        p.status = device_status_word();
+        p.skip = nullptr;
+        p.counter = nullptr;
+        const int sms = sm_count() > 0 ? sm_count() : 148;
+        const int grid = (int)((p.items < sms) ? p.items : sms);
+        LaunchScope ls("bgemm_tcgen05", s);
+        ozaki_slice_gemm_kernel<BgemmParams><<<grid, OZ_THREADS, OZ_SMEM_BYTES, s>>>(map_a, map_b, p);
+        rc = check_cuda(cudaGetLastError(), "bgemm");
+    }
+    dev_free(own_a, s);
+    dev_free(own_b, s);
+    return rc;
 }
 
 }  // namespace gb

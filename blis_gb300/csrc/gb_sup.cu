@@ -11,31 +11,41 @@
 // workspace and a second kernel folds them in fixed order, so results are
 // deterministic.  The same config space covers FP64 (DMMA m8n8k4) and FP32
 // (FMA):
-//   config 0      the 128 x 128 engine of gb_dgemm.cu
-//   config 1..5   64 x 64 tiles with a K split of 1, 2, 4, 8, 16
+//   config 0      the 128 x 128 engine of gb_dgemm.cu (BF16: the tcgen05
+//                 kernel of gb_ozaki.cu)
+//   config 1..5   64 x 64 tiles with a K split of 1, 2, 4, 8, 16 (BF16:
+//                 bf16 loads, FP32 arithmetic)
+#include <cuda_bf16.h>
+
 #include "gb_internal.h"
 
 namespace gb {
 namespace {
 
+// Element loads widened to the arithmetic type.
+template <typename T>
+__device__ __forceinline__ T sup_ld(const T* p) { return __ldg(p); }
+__device__ __forceinline__ float sup_ld(const __nv_bfloat16* p) { return __bfloat162float(__ldg(p)); }
+
 constexpr int SBM = 64, SBN = 64, SBK = 16, SNT = 128;
 constexpr int SLDS = SBM + 8;
 
-template <typename T>
+// T: arithmetic and C; TI: the element type of A and B (T, or bf16 for T = float).
+template <typename T, typename TI = T>
 struct SupArgs {
     int64_t m, n, k, kchunk;
     T alpha, beta;
-    const T* a;
+    const TI* a;
     int64_t ars, acs;
-    const T* b;
+    const TI* b;
     int64_t brs, bcs;
     T* c;
     int64_t rs_c, cs_c;
     T* ws;  // split partial sums [split][n][m], or nullptr when not split
 };
 
-template <typename T>
-__device__ __forceinline__ void sup_load(const SupArgs<T>& p, int64_t bm, int64_t bn, int64_t k0, int64_t k1,
+template <typename T, typename TI>
+__device__ __forceinline__ void sup_load(const SupArgs<T, TI>& p, int64_t bm, int64_t bn, int64_t k0, int64_t k1,
                                          T (&ra)[8], T (&rb)[8])
 {
     const int tid = threadIdx.x;
@@ -47,16 +57,16 @@ __device__ __forceinline__ void sup_load(const SupArgs<T>& p, int64_t bm, int64_
         int i, l;
         if (a_rows_fast) { i = e % SBM; l = e / SBM; } else { i = e / SBK; l = e % SBK; }
         const int64_t gi = bm + i, gl = k0 + l;
-        ra[r] = (gi < p.m && gl < k1) ? __ldg(p.a + gi * p.ars + gl * p.acs) : T(0);
+        ra[r] = (gi < p.m && gl < k1) ? sup_ld(p.a + gi * p.ars + gl * p.acs) : T(0);
         int j;
         if (b_k_fast) { l = e % SBK; j = e / SBK; } else { j = e % SBN; l = e / SBN; }
         const int64_t gj = bn + j, gl2 = k0 + l;
-        rb[r] = (gj < p.n && gl2 < k1) ? __ldg(p.b + gl2 * p.brs + gj * p.bcs) : T(0);
+        rb[r] = (gj < p.n && gl2 < k1) ? sup_ld(p.b + gl2 * p.brs + gj * p.bcs) : T(0);
     }
 }
 
-template <typename T>
-__device__ __forceinline__ void sup_store(const SupArgs<T>& p, T (&ra)[8], T (&rb)[8], T* As, T* Bs)
+template <typename T, typename TI>
+__device__ __forceinline__ void sup_store(const SupArgs<T, TI>& p, T (&ra)[8], T (&rb)[8], T* As, T* Bs)
 {
     const int tid = threadIdx.x;
     const bool a_rows_fast = (p.ars == 1);
@@ -73,8 +83,8 @@ __device__ __forceinline__ void sup_store(const SupArgs<T>& p, T (&ra)[8], T (&r
     }
 }
 
-template <typename T>
-__device__ __forceinline__ void sup_out(const SupArgs<T>& p, int64_t i, int64_t j, T ab)
+template <typename T, typename TI>
+__device__ __forceinline__ void sup_out(const SupArgs<T, TI>& p, int64_t i, int64_t j, T ab)
 {
     if (i >= p.m || j >= p.n) return;
     if (p.ws) {
@@ -94,8 +104,8 @@ __device__ __forceinline__ void dmma(double& d0, double& d1, double a, double b)
 }
 
 // FP64: 2 x 2 warps of 32 x 32, DMMA.  FP32: 16 x 8 threads of 4 x 8, FMA.
-template <typename T>
-__global__ void __launch_bounds__(SNT) sup_gemm_kernel(SupArgs<T> p)
+template <typename T, typename TI>
+__global__ void __launch_bounds__(SNT) sup_gemm_kernel(SupArgs<T, TI> p)
 {
     __shared__ T As[SBK * SLDS];
     __shared__ T Bs[SBK * SLDS];
@@ -190,9 +200,9 @@ __global__ void sup_fold_kernel(int64_t m, int64_t n, int splits, const T* __res
     }
 }
 
-template <typename T>
-int sup_gemm(int splits, int64_t m, int64_t n, int64_t k, T alpha, const T* a, int64_t ars, int64_t acs,
-             const T* b, int64_t brs, int64_t bcs, T beta, T* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
+template <typename T, typename TI = T>
+int sup_gemm(int splits, int64_t m, int64_t n, int64_t k, T alpha, const TI* a, int64_t ars, int64_t acs,
+             const TI* b, int64_t brs, int64_t bcs, T beta, T* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
 {
     int64_t kchunk = (k + splits - 1) / splits;
     kchunk = (kchunk + SBK - 1) / SBK * SBK;
@@ -204,10 +214,10 @@ int sup_gemm(int splits, int64_t m, int64_t n, int64_t k, T alpha, const T* a, i
         ws = static_cast<T*>(dev_alloc(sizeof(T) * (size_t)sz * m * n, s));
         if (!ws) return GB_ERR_NOMEM;
     }
-    SupArgs<T> p{m, n, k, kchunk, alpha, beta, a, ars, acs, b, brs, bcs, c, rs_c, cs_c, ws};
+    SupArgs<T, TI> p{m, n, k, kchunk, alpha, beta, a, ars, acs, b, brs, bcs, c, rs_c, cs_c, ws};
     {
-        LaunchScope ls(sizeof(T) == 8 ? "sup_dmma" : "sup_ffma", s);
-        sup_gemm_kernel<T><<<dim3((unsigned)gx, (unsigned)gy, (unsigned)sz), SNT, 0, s>>>(p);
+        LaunchScope ls(sizeof(T) == 8 ? "sup_dmma" : (sizeof(TI) == 2 ? "sup_bf16" : "sup_ffma"), s);
+        sup_gemm_kernel<T, TI><<<dim3((unsigned)gx, (unsigned)gy, (unsigned)sz), SNT, 0, s>>>(p);
     }
     int rc = check_cuda(cudaGetLastError(), "gemm_sup");
     if (!rc && sz > 1) {
@@ -230,9 +240,19 @@ int gemm_config_dev(int dtype, int config, int64_t m, int64_t n, int64_t k, doub
 {
     if (config < 0 || config >= GB_GEMM_NUM_CONFIGS) return set_error(GB_ERR_ARG, "gemm_config", "unknown config");
     if (m <= 0 || n <= 0) return GB_SUCCESS;
+    if (dtype < 0 || dtype > 2) return set_error(GB_ERR_ARG, "gemm_config", "dtype must be 0 (FP64), 1 (FP32) or 2 (BF16)");
     if (alpha == 0.0 || k <= 0) {
         if (dtype == 0) return scal_matrix(m, n, beta, (double*)c, rs_c, cs_c, s);
         return scal_matrix_f(m, n, (float)beta, (float*)c, rs_c, cs_c, s);
+    }
+    if (dtype == 2) {
+        // bf16 A, B; fp32 C and arithmetic: config 0 the tensor-core kernel, 1..5 the 64 x 64 engine
+        if (config == 0)
+            return bgemm_tc(m, n, k, (float)alpha, (const uint16_t*)a, ars, acs, (const uint16_t*)b, brs, bcs,
+                            (float)beta, (float*)c, rs_c, cs_c, s);
+        return sup_gemm<float, __nv_bfloat16>(1 << (config - 1), m, n, k, (float)alpha, (const __nv_bfloat16*)a,
+                                              ars, acs, (const __nv_bfloat16*)b, brs, bcs, (float)beta,
+                                              (float*)c, rs_c, cs_c, s);
     }
     if (config == 0) {
         if (dtype == 0)
@@ -258,10 +278,27 @@ extern "C" int gb_gemm_config_dev(int dtype, int config, gb_trans_t transa, gb_t
 {
     int rc = gb::ensure_init();
     if (rc) return rc;
-    if (dtype != 0 && dtype != 1) return gb::set_error(GB_ERR_ARG, "gb_gemm_config_dev", "dtype must be 0 or 1");
+    if (dtype < 0 || dtype > 2) return gb::set_error(GB_ERR_ARG, "gb_gemm_config_dev", "dtype must be 0, 1 or 2");
     if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_gemm_config_dev", "negative dimension");
     const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : gb::thread_stream();
     return gb::gemm_config_dev(dtype, config, m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b,
                                tb ? cs_b : rs_b, tb ? rs_b : cs_b, beta, c, rs_c, cs_c, s);
+}
+
+extern "C" int gb_bgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k, float alpha,
+                            const void* a, gb_inc_t rs_a, gb_inc_t cs_a, const void* b, gb_inc_t rs_b,
+                            gb_inc_t cs_b, float beta, float* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_bgemm_dev", "negative dimension");
+    int cfg = (m >= 201 && n >= 201 && k >= 201) ? 0 : 1;
+    if (gb::selector_auto()) {
+        int sl = 0;
+        if (gb::selector_choose(2, m, n, k, GB_IS_TRANS(transa), GB_IS_TRANS(transb), 0, 0.0, 0.0, &cfg, &sl))
+            return gb_get_last_error(nullptr, 0);
+    }
+    return gb_gemm_config_dev(2, cfg, transa, transb, m, n, k, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c,
+                              cs_c, stream);
 }

@@ -49,6 +49,20 @@ def sgemm(transa, transb, alpha, a, b, beta, c):
     return _lib.check(rc, "gb_sgemm_dev")
 
 
+def bgemm(transa, transb, alpha, a, b, beta, c, config=None):
+    """C (fp32) := alpha op(A) op(B) + beta C for bf16 tensors a, b; config
+    None lets the library choose (selector or threshold rule)."""
+    k = _k(transa, a)
+    L = _lib.load()
+    if config is None:
+        rc = L.gb_bgemm_dev(transa, transb, c.shape[0], c.shape[1], k, alpha, a.data_ptr(), *_rc(a), b.data_ptr(),
+                            *_rc(b), beta, c.data_ptr(), *_rc(c), _stream())
+    else:
+        rc = L.gb_gemm_config_dev(2, config, transa, transb, c.shape[0], c.shape[1], k, alpha, a.data_ptr(), *_rc(a),
+                                  b.data_ptr(), *_rc(b), beta, c.data_ptr(), *_rc(c), _stream())
+    _lib.check(rc, "gb_bgemm_dev")
+
+
 def dtrsm(side, uplo, transa, diag, alpha, a, b):
     m, n = b.shape
     rc = _lib.load().gb_dtrsm_dev(side, uplo, transa, diag, m, n, alpha, a.data_ptr(), *_rc(a),

@@ -6,8 +6,9 @@ small-problem rule (sup thresholds MT/NT/KT, frame/base/bli_cntx.h:186-193,
 Here the choice is learned:
 
 * the autotuner times every GEMM configuration of the library
-  (gb_gemm_config_dev: 128x128 tiles, or 64x64 tiles with K split 1..16)
-  on seeded shapes and records the time of each;
+  (gb_gemm_config_dev: 128x128 tiles -- for bf16 the tcgen05 kernel -- or
+  64x64 tiles with K split 1..16) on seeded FP64, FP32 and BF16 shapes and
+  records the time of each;
 * the slice-count label of an FP64 shape comes from the error-bound verifier
   (gb_ozaki_verify_slices_dev) run on synthetic operands with the shape's
   exponent spread;
@@ -43,7 +44,7 @@ NPARAMS = 9928
 CONFIG_NAMES = ["tile128", "tile64", "tile64_k2", "tile64_k4", "tile64_k8", "tile64_k16"]
 NCONFIG = len(CONFIG_NAMES)
 OUT_SLICES = 6
-DTYPES = {"fp64": 0, "fp32": 1}
+DTYPES = {"fp64": 0, "fp32": 1, "bf16": 2}  # bf16: A, B bf16, C and arithmetic fp32
 PADS = (0, 8, 64)
 SCHEMA = "gb300-selector-mlp/1"
 TIME_SCALE = 10.0  # target = log2(time in microseconds) / TIME_SCALE
@@ -90,7 +91,7 @@ def heuristic_config(m, n, k):
 
 
 # ------------------------------------------------------------------ shapes
-def sample_shapes(count, seed, dtypes=("fp64", "fp32")):
+def sample_shapes(count, seed, dtypes=("fp64", "fp32", "bf16")):
     """m, n, k log-uniform integers in [1, 32768], random transposes and
     leading-dimension padding, exponent spread E uniform in {0..20};
     shapes above WORK_CAP flops or ELEM_CAP operand elements are redrawn."""
@@ -120,10 +121,11 @@ class Autotuner:
                                               C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.c_void_p,
                                               C.c_int64, C.c_int64, C.c_void_p]
         self.buf = {}
-        for dt, tdt in ((0, torch.float64), (1, torch.float32)):
+        for dt, tdt, cdt in ((0, torch.float64, torch.float64), (1, torch.float32, torch.float32),
+                             (2, torch.bfloat16, torch.float32)):
             a = torch.empty(max_elems + 64 * 32768, dtype=tdt, device="cuda").uniform_(-1, 1)
             b = torch.empty(max_elems + 64 * 32768, dtype=tdt, device="cuda").uniform_(-1, 1)
-            c = torch.zeros(max_elems + 64 * 32768, dtype=tdt, device="cuda")
+            c = torch.zeros(max_elems + 64 * 32768, dtype=cdt, device="cuda")
             self.buf[dt] = (a, b, c)
         self.stream = C.c_void_p(torch.cuda.current_stream().cuda_stream or 1)
 

@@ -299,16 +299,28 @@ int gb_dgemv_dev(gb_trans_t transa, gb_dim_t m, gb_dim_t n, double alpha, const 
                  double beta, double* y, gb_inc_t incy, void* stream);
 
 /* GEMM with an explicit kernel configuration (the autotuner's and the
-   selector's vocabulary); dtype 0 = FP64, 1 = FP32, alpha/beta passed as
-   double.  Config 0: 128x128 tiles; configs 1..5: the small/skinny (gemmsup)
-   engine with 64x64 tiles and K split into 1, 2, 4, 8, 16 parts (split
-   partials folded in a fixed order).  Counterpart of the gemmsup decision of
-   frame/3/bli_l3_sup.c:37-131 (thresholds frame/base/bli_cntx.h:186-193). */
+   selector's vocabulary); dtype 0 = FP64, 1 = FP32, 2 = BF16 (A and B bf16,
+   C and arithmetic FP32), alpha/beta passed as double.  Config 0: 128x128
+   tiles (BF16: the tcgen05 kernel, 128x256 tiles); configs 1..5: the
+   small/skinny (gemmsup) engine with 64x64 tiles and K split into 1, 2, 4,
+   8, 16 parts (split partials folded in a fixed order).  Counterpart of the
+   gemmsup decision of frame/3/bli_l3_sup.c:37-131 (thresholds
+   frame/base/bli_cntx.h:186-193). */
 #define GB_GEMM_NUM_CONFIGS 6
 int gb_gemm_config_dev(int dtype, int config, gb_trans_t transa, gb_trans_t transb, gb_dim_t m,
                        gb_dim_t n, gb_dim_t k, double alpha, const void* a, gb_inc_t rs_a,
                        gb_inc_t cs_a, const void* b, gb_inc_t rs_b, gb_inc_t cs_b, double beta,
                        void* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+
+/* BF16 GEMM, C := alpha op(A) op(B) + beta C with A, B bf16 (bit patterns,
+   BLIS-style strides) and C fp32.  BLIS 1.0 has no bf16 datatype; this entry
+   completes the selector's dtype set.  The configuration comes from the
+   selector when gb_set_gemm_autoselect(1) and a model are loaded, else from
+   the small-problem threshold rule (tensor cores when every dimension is at
+   least 201). */
+int gb_bgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k, float alpha,
+                 const void* a, gb_inc_t rs_a, gb_inc_t cs_a, const void* b, gb_inc_t rs_b, gb_inc_t cs_b,
+                 float beta, float* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
 
 /* One problem of a grouped GEMM on device operands (column-major, BLAS
    leading dimensions): C := beta*C + alpha*op(A)*op(B). */
