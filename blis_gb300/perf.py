@@ -8,6 +8,7 @@ L2 where the workload allows:
   dgemm_1024      C := A B + 0.5 C, m=n=k=1024, U[-1,1]          (FP64 pipe)
   dgemm_8192      native FP64 and Ozaki (7 slices), m=n=k=8192
   sgemm_8192      FP32, m=n=k=8192
+  bgemm_8192      BF16 A, B, FP32 C, m=n=k=8192 (tensor cores)
   dtrsm_8192x4096 L/L/N/N, diag 8192+|u|, native and Ozaki updates (m^2 n flop)
   dgemv_32768     N and T, 8(mn + n + 2m) bytes                    (HBM)
   daxpyv_2^28     24 n bytes; ddotv_2^28: 16 n bytes                (HBM)
@@ -93,6 +94,24 @@ def run_sgemm(out):
     fa, fb, fc = (_mat(n, n, seed=s, dtype=torch.float32) for s in (7, 8, 9))
     ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
     out.append({"workload": "sgemm_8192", "form": "ffma_fp32", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
+
+
+def run_bgemm(out):
+    """BF16 GEMM 8192^3 (fp32 C) on the tensor-core kernel: op(A) = A^T (k
+    contiguous, loaded by TMA in place) and op(A) = A (packed to k-major
+    first); against the measured cuBLAS bf16 peak."""
+    import torch
+    pk, kind = peaks()
+    n = 8192
+    a = _mat(n, n, seed=41).to(torch.bfloat16)
+    b = _mat(n, n, seed=42).to(torch.bfloat16)
+    a, b = a.t().contiguous().t(), b.t().contiguous().t()  # column-major bf16
+    c = dev.colmajor(n, n, torch.float32)
+    for ta, name in ((8, "TN_tma_in_place"), (0, "NN_packed")):
+        ms = _timer(lambda: dev.bgemm(ta, 0, 1.0, a, b, 0.0, c, config=0), reps=5)
+        tf = 2 * n ** 3 / ms / 1e9
+        out.append({"workload": "bgemm_8192", "form": name, "ms": ms, "tflops": tf,
+                    "frac_of_bf16_burst": tf / pk.get("bf16_tflops", 1900.0), "peak": "%s bf16_tflops" % kind})
 
 
 def run_trsm(out):
@@ -274,7 +293,7 @@ def run_batch(out):
 
 
 SUITES = {"gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
-          "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm}
+          "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm, "bgemm": run_bgemm}
 
 
 def main():
