@@ -48,7 +48,7 @@ def _run(config, ta, tb, m, n, k, alpha, beta, pow2=False, lda_pad=0):
     A = (a.t() if ta else a).double()
     B = (b.t() if tb else b).double()
     ref = alpha * (A @ B) + beta * c0.double()
-    bound = alpha * (A.abs() @ B.abs()) * (k + 2) * 2.0 ** -24 + abs(beta) * c0.double().abs() * 2.0 ** -23
+    bound = abs(alpha) * (A.abs() @ B.abs()) * (k + 2) * 2.0 ** -24 + abs(beta) * c0.double().abs() * 2.0 ** -23
     return cd.cpu().double(), ref, bound
 
 
