@@ -324,6 +324,13 @@ def evaluate(params, data):
 
     res = {"n": int(len(T)), "mlp": stats(t_mlp), "threshold_rule": stats(t_heur),
            "exhaustive_mean_gflops": float(np.mean(flops / best / 1e3))}
+    res["per_dtype"] = {}
+    for name, code in DTYPES.items():
+        sel = sh[:, 3] == code
+        if sel.any():
+            res["per_dtype"][name] = {"n": int(sel.sum()),
+                                      "mlp_mean_throughput_regret": float(1.0 - np.mean(best[sel] / t_mlp[sel])),
+                                      "rule_mean_throughput_regret": float(1.0 - np.mean(best[sel] / t_heur[sel]))}
     fp64 = sh[:, 3] == 0
     if fp64.any():
         s_true = data["S"][fp64]

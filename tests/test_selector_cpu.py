@@ -68,3 +68,23 @@ def test_load_file_rejects_corrupt_models(gblib, tmp_path):
         S.load_model(str(path))
     code, _ = _lib.last_error()
     assert code == 0
+
+
+def test_committed_model_regret_per_dtype_on_cpu():
+    """The committed model's choices on the held-out shapes, recomputed with the
+    FP64 restatement of the network: below 5% mean throughput regret for every
+    dtype and better than the threshold rule."""
+    from oracle import mlp_ref as R
+    p, _ = S.load_model(os.path.join(TUNING, "selector_mlp.json"))
+    d = np.load(os.path.join(TUNING, "autotune_heldout.npz"))
+    pred = R.forward(p.astype(np.float64), d["X"].astype(np.float64))
+    T, sh = d["T"], d["shapes"]
+    best = T.min(1)
+    t_mlp = T[np.arange(len(T)), pred[:, :S.NCONFIG].argmin(1)]
+    rule = np.array([S.heuristic_config(int(r[0]), int(r[1]), int(r[2])) for r in sh])
+    t_rule = T[np.arange(len(T)), rule]
+    for code in (0, 1, 2):
+        sel = sh[:, 3] == code
+        assert sel.sum() >= 600
+        regret = 1.0 - np.mean(best[sel] / t_mlp[sel])
+        assert regret < 0.05 and regret < 1.0 - np.mean(best[sel] / t_rule[sel])
