@@ -127,6 +127,71 @@ int finish(cudaStream_t s, const char* where)
 }
 
 // ---------------------------------------------------------------- host ops
+// The Ozaki form on host buffers, pipelined: op(A) goes to HBM and is split
+// once while op(B) (column-major) streams in column blocks on one copy stream
+// and finished blocks of C (column-major) stream back on another, so the
+// host<->device transfers of B and C overlap the slice GEMMs.  Column blocks
+// of op(B) are split independently: the result is bit-identical to one call.
+int ozaki_host_pipelined(int transa, int64_t m, int64_t n, int64_t k, double alpha, const double* a,
+                         int64_t rs_a, int64_t cs_a, const double* b, int64_t ldb, double beta, double* c,
+                         int64_t ldc, int slices, int nch, const char* where)
+{
+    cudaStream_t s = thread_stream(), cin = thread_copy_stream(0), cout = thread_copy_stream(1);
+    const bool ta = GB_IS_TRANS(transa);
+    int rc;
+    Bufs bufs(s);
+    Staged& A = bufs.next();
+    if ((rc = stage_in(a, ta ? k : m, ta ? m : k, rs_a, cs_a, sizeof(double), true, &A, s))) return rc;
+    OzA prep;
+    if ((rc = ozaki_prepare_a(m, k, reinterpret_cast<const double*>(A.origin), ta ? A.cs : A.rs, ta ? A.rs : A.cs,
+                              slices, s, &prep)))
+        return rc;
+    double* bd = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(k * n), s));
+    double* cd = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(m * n), s));
+    cudaEvent_t ev[2 * 8 + 3];
+    const int nev = 2 * nch + 3;
+    for (int i = 0; i < nev; ++i) cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+    cudaEvent_t *ev_in = ev, *ev_out = ev + nch, ev_alloc = ev[2 * nch], ev_in_done = ev[2 * nch + 1],
+                ev_out_done = ev[2 * nch + 2];
+    rc = (bd && cd) ? GB_SUCCESS : GB_ERR_NOMEM;
+    if (!rc) {
+        // the copy streams may touch bd/cd only after their stream-ordered allocation
+        cudaEventRecord(ev_alloc, s);
+        cudaStreamWaitEvent(cin, ev_alloc, 0);
+        cudaStreamWaitEvent(cout, ev_alloc, 0);
+        for (int j = 0; j < nch && !rc; ++j) {
+            const int64_t j0 = n * j / nch, nj = n * (j + 1) / nch - j0;
+            rc = check_cuda(cudaMemcpy2DAsync(bd + j0 * k, k * sizeof(double), b + j0 * ldb, ldb * sizeof(double),
+                                              k * sizeof(double), nj, cudaMemcpyDefault, cin), "B block");
+            if (!rc && beta != 0.0)
+                rc = check_cuda(cudaMemcpy2DAsync(cd + j0 * m, m * sizeof(double), c + j0 * ldc, ldc * sizeof(double),
+                                                  m * sizeof(double), nj, cudaMemcpyDefault, cin), "C block");
+            cudaEventRecord(ev_in[j], cin);
+        }
+        for (int j = 0; j < nch && !rc; ++j) {
+            const int64_t j0 = n * j / nch, nj = n * (j + 1) / nch - j0;
+            cudaStreamWaitEvent(s, ev_in[j], 0);
+            rc = ozaki_multiply(&prep, nj, bd + j0 * k, 1, k, alpha, beta, cd + j0 * m, 1, m, s);
+            cudaEventRecord(ev_out[j], s);
+            cudaStreamWaitEvent(cout, ev_out[j], 0);
+            if (!rc)
+                rc = check_cuda(cudaMemcpy2DAsync(c + j0 * ldc, ldc * sizeof(double), cd + j0 * m, m * sizeof(double),
+                                                  m * sizeof(double), nj, cudaMemcpyDefault, cout), "C back");
+        }
+        // frees below are ordered after every copy on either copy stream
+        cudaEventRecord(ev_in_done, cin);
+        cudaEventRecord(ev_out_done, cout);
+        cudaStreamWaitEvent(s, ev_in_done, 0);
+        cudaStreamWaitEvent(s, ev_out_done, 0);
+    }
+    ozaki_release_a(&prep, s);
+    dev_free(bd, s);
+    dev_free(cd, s);
+    const int rc2 = finish(s, where);
+    for (int i = 0; i < nev; ++i) cudaEventDestroy(ev[i]);
+    return rc ? rc : rc2;
+}
+
 template <typename T>
 int gemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, T alpha, const T* a,
               int64_t rs_a, int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, T beta, T* c,
@@ -135,6 +200,15 @@ int gemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, T alpha, 
     int rc = ensure_init();
     if (rc) return rc;
     if (m <= 0 || n <= 0) return GB_SUCCESS;
+    if (sizeof(T) == 8 && dgemm_mode() == GB_DGEMM_OZAKI && ozaki_slices() >= 2 && alpha != T(0) && k > 0 &&
+        !GB_IS_TRANS(transb) && rs_b == 1 && cs_b >= k && rs_c == 1 && cs_c >= m && n >= 2048 &&
+        m * k >= (int64_t(1) << 22)) {
+        // large products with a fixed slice count, column-major op(B) and C: the transfers
+        // of op(B) and C overlap the compute
+        const int nch = (n >= 8192) ? 4 : 2;
+        return ozaki_host_pipelined(transa, m, n, k, (double)alpha, (const double*)a, rs_a, cs_a, (const double*)b,
+                                    cs_b, (double)beta, (double*)c, cs_c, ozaki_slices(), nch, where);
+    }
     cudaStream_t s = thread_stream();
     Bufs bufs(s);
     const size_t esz = sizeof(T);

@@ -31,6 +31,7 @@ int check_cuda(cudaError_t e, const char* where);
 // device); device memory comes from a stream-ordered pool that keeps freed
 // blocks cached.
 cudaStream_t thread_stream();
+cudaStream_t thread_copy_stream(int i);  // i = 0, 1: copy streams of the calling thread
 int ensure_init();
 int sm_count();
 
@@ -101,6 +102,25 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
               const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b,
               int64_t cs_b, int slices, cudaStream_t s);
 int64_t ozaki_kpart_limit(int slices);
+// The Ozaki form in two phases (gb_ozaki.cu): op(A) split once, then any
+// number of products with column blocks of op(B) (bit-identical to one call).
+struct OzA {
+    int slices = 0;
+    bool pair_form = false;
+    int64_t m = 0, k = 0, mpad = 0, kpad = 0;
+    const double* a = nullptr;  // op(A) (i, l) = a[i*ars + l*acs], kept for the IEEE fallback
+    int64_t ars = 0, acs = 0;
+    uint8_t* ws = nullptr;      // slices, row maxima, exponents, Inf/NaN flag
+    uint16_t* sa = nullptr;
+    unsigned long long* maxa = nullptr;
+    int32_t* ea = nullptr;
+    int* nonfinite = nullptr;
+};
+int ozaki_prepare_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t acs, int slices,
+                    cudaStream_t s, OzA* A);
+int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, double alpha,
+                   double beta, double* c, int64_t rs_c, int64_t cs_c, cudaStream_t s);
+void ozaki_release_a(OzA* A, cudaStream_t s);
 // bf16 GEMM on the tensor cores (gb_ozaki.cu): C fp32, A and B as bf16 bit
 // patterns with element strides.
 int bgemm_tc(int64_t m, int64_t n, int64_t k, float alpha, const uint16_t* a, int64_t ars, int64_t acs,

@@ -1378,23 +1378,136 @@ double ozaki_t_bound_log2(int s, int64_t k)
     return log2(t);
 }
 
-int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
-                const double* a, int64_t ars, int64_t acs,
-                const double* b, int64_t brs, int64_t bcs, double beta,
-                double* c, int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s)
+namespace {
+
+void launch_rowmax(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl, unsigned long long* mb,
+                   cudaStream_t s)
 {
-    if (m <= 0 || n <= 0) return GB_SUCCESS;
-    if (alpha == 0.0 || k <= 0) return scal_matrix(m, n, beta, c, rs_c, cs_c, s);
+    const int sms = sm_count() > 0 ? sm_count() : 148;
+    if (sr == 1) {
+        const int64_t gx = (rows + 255) / 256;
+        int64_t gy = ((int64_t)sms * 8 + gx - 1) / gx;
+        if (gy > k) gy = k;
+        if (gy > 65535) gy = 65535;
+        const int64_t kchunk = (k + gy - 1) / gy;
+        gy = (k + kchunk - 1) / kchunk;
+        LaunchScope ls("oz_rowmax", s);
+        oz_rowmax_rows_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sl, kchunk, mb);
+    } else {
+        const int64_t gx = (rows * 32 + 255) / 256;
+        int64_t gy = ((int64_t)sms * 8 + gx - 1) / gx;
+        if (gy > (k + 255) / 256) gy = (k + 255) / 256;
+        if (gy < 1) gy = 1;
+        if (gy > 65535) gy = 65535;
+        const int64_t kchunk = (k + gy - 1) / gy;
+        gy = (k + kchunk - 1) / kchunk;
+        LaunchScope ls("oz_rowmax", s);
+        oz_rowmax_warp_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sr, sl, kchunk, mb);
+    }
+}
+
+// One-time kernel attributes of the slice GEMM engines and the number of
+// CTA pairs that fit at once.
+int slice_gemm_setup(int* max_pairs)
+{
+    static bool attr_set = false;
+    static int pairs = 0;
+    int rc;
+    if (!attr_set) {
+        const int sms = sm_count() > 0 ? sm_count() : 148;
+        if ((rc = check_cuda(cudaFuncSetAttribute(ozaki_slice_gemm_kernel<OzGemmParams>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM_BYTES),
+                             "smem attr")))
+            return rc;
+        if ((rc = check_cuda(cudaFuncSetAttribute(ozaki_slice_gemm_pair_kernel,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, OZ2_SMEM_BYTES),
+                             "smem attr")))
+            return rc;
+        cudaLaunchConfig_t qc = {};
+        cudaLaunchAttribute qa[1];
+        qa[0].id = cudaLaunchAttributeClusterDimension;
+        qa[0].val.clusterDim.x = 2;
+        qa[0].val.clusterDim.y = 1;
+        qa[0].val.clusterDim.z = 1;
+        qc.gridDim = dim3(2 * (unsigned)(sms / 2));
+        qc.blockDim = dim3(OZ_THREADS);
+        qc.dynamicSmemBytes = OZ2_SMEM_BYTES;
+        qc.attrs = qa;
+        qc.numAttrs = 1;
+        if ((rc = check_cuda(cudaOccupancyMaxActiveClusters(&pairs, ozaki_slice_gemm_pair_kernel, &qc),
+                             "cluster occupancy")))
+            return rc;
+        attr_set = true;
+    }
+    *max_pairs = pairs;
+    return GB_SUCCESS;
+}
+
+}  // namespace
+
+// Phase 1 of the Ozaki form: row maxima, exponents and digit slices of op(A)
+// (element (i, l) = a[i*ars + l*acs]), kept in HBM for any number of
+// multiplications.  The Inf/NaN flag lives here and is shared by them.
+int ozaki_prepare_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t acs, int slices,
+                    cudaStream_t s, OzA* A)
+{
+    *A = OzA();
     if (slices < 2 || slices > OZ_MAX_SLICES)
         return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices must be in [2, 12]");
     if (ozaki_t_bound_log2(slices, k) >= 126.0)
         return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices and k exceed the 128-bit recombination range");
-
-    const bool pair_form = (ozaki_ctas_setting() == 2);
-    const int64_t row_tile = pair_form ? 2 * OZ2_ROWS : OZ_BM;
-    const int64_t kpad = round_up(k, OZ_BK), mpad = round_up(m, row_tile), npad = round_up(n, OZ_BN);
-    if (mpad > INT32_MAX || npad > INT32_MAX || kpad > INT32_MAX)
+    A->pair_form = (ozaki_ctas_setting() == 2);
+    const int64_t row_tile = A->pair_form ? 2 * OZ2_ROWS : OZ_BM;
+    A->slices = slices;
+    A->m = m;
+    A->k = k;
+    A->kpad = round_up(k, OZ_BK);
+    A->mpad = round_up(m, row_tile);
+    if (A->mpad > INT32_MAX || A->kpad > INT32_MAX)
         return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "dimension too large for TMA coordinates");
+    A->a = a;
+    A->ars = ars;
+    A->acs = acs;
+    const size_t bytes_sa = (size_t)slices * A->mpad * A->kpad * 2;
+    const size_t bytes_aux = sizeof(unsigned long long) * m + sizeof(int32_t) * m + 64;
+    A->ws = static_cast<uint8_t*>(dev_alloc(bytes_sa + bytes_aux + 1024, s));
+    if (!A->ws) return GB_ERR_NOMEM;
+    A->sa = reinterpret_cast<uint16_t*>(A->ws);
+    A->maxa = reinterpret_cast<unsigned long long*>(A->ws + bytes_sa);
+    A->ea = reinterpret_cast<int32_t*>(A->maxa + m);
+    A->nonfinite = reinterpret_cast<int*>(A->ea + m);
+    int rc;
+    if ((rc = check_cuda(cudaMemsetAsync(A->maxa, 0, sizeof(unsigned long long) * m, s), "memset")) ||
+        (rc = check_cuda(cudaMemsetAsync(A->nonfinite, 0, sizeof(int), s), "memset"))) {
+        ozaki_release_a(A, s);
+        return rc;
+    }
+    launch_rowmax(m, k, a, ars, acs, A->maxa, s);
+    split_dispatch(slices, m, k, a, ars, acs, A->maxa, A->mpad, A->kpad, A->sa, A->ea, A->nonfinite, s);
+    if ((rc = check_cuda(cudaGetLastError(), "oz_split"))) ozaki_release_a(A, s);
+    return rc;
+}
+
+void ozaki_release_a(OzA* A, cudaStream_t s)
+{
+    dev_free(A->ws, s);
+    A->ws = nullptr;
+}
+
+// Phase 2: C := alpha op(A) op(B) + beta C for the prepared op(A) and an
+// op(B) of n columns ((l, j) = b[l*brs + j*bcs]); the split of op(B), the
+// slice GEMM, the recombination and the gated IEEE fallback.  Columns of
+// op(B) are split independently, so a product done in column blocks gives
+// the same bits as one call.
+int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, double alpha, double beta,
+                   double* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
+{
+    const int64_t m = A->m, k = A->k, mpad = A->mpad, kpad = A->kpad;
+    const int slices = A->slices;
+    const bool pair_form = A->pair_form;
+    const int64_t row_tile = pair_form ? 2 * OZ2_ROWS : OZ_BM;
+    const int64_t npad = round_up(n, OZ_BN);
+    if (npad > INT32_MAX) return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "dimension too large for TMA coordinates");
     const int kb_total = (int)(kpad / OZ_BK);
 
     OzGemmParams p;
@@ -1425,91 +1538,34 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     p.mpad = mpad;
     p.npad = npad;
 
-    const size_t bytes_sa = (size_t)slices * mpad * kpad * 2, bytes_sb = (size_t)slices * npad * kpad * 2;
+    const size_t bytes_sb = (size_t)slices * npad * kpad * 2;
     const size_t bytes_pl = (size_t)planes_total * npad * mpad * 4;
-    const size_t bytes_aux = sizeof(unsigned long long) * (m + n) + sizeof(int32_t) * (m + n) + 64;
-    uint8_t* ws = static_cast<uint8_t*>(dev_alloc(bytes_sa + bytes_sb + bytes_pl + bytes_aux + 1024, s));
+    const size_t bytes_aux = sizeof(unsigned long long) * n + sizeof(int32_t) * n + 64;
+    uint8_t* ws = static_cast<uint8_t*>(dev_alloc(bytes_sb + bytes_pl + bytes_aux + 1024, s));
     if (!ws) return GB_ERR_NOMEM;
-    uint16_t* sa = reinterpret_cast<uint16_t*>(ws);
-    uint16_t* sb = reinterpret_cast<uint16_t*>(ws + bytes_sa);
-    int32_t* planes = reinterpret_cast<int32_t*>(ws + bytes_sa + bytes_sb);
-    unsigned long long* maxa = reinterpret_cast<unsigned long long*>(ws + bytes_sa + bytes_sb + bytes_pl);
-    unsigned long long* maxb = maxa + m;
-    int32_t* ea = reinterpret_cast<int32_t*>(maxb + n);
-    int32_t* eb = ea + m;
-    int* nonfinite = reinterpret_cast<int*>(eb + n);
+    uint16_t* sb = reinterpret_cast<uint16_t*>(ws);
+    int32_t* planes = reinterpret_cast<int32_t*>(ws + bytes_sb);
+    unsigned long long* maxb = reinterpret_cast<unsigned long long*>(ws + bytes_sb + bytes_pl);
+    int32_t* eb = reinterpret_cast<int32_t*>(maxb + n);
     p.planes = planes;
     p.status = device_status_word();
-    p.skip = nonfinite;
+    p.skip = A->nonfinite;
     p.counter = nullptr;
 
     int rc = GB_SUCCESS;
     auto bail = [&](int code) { dev_free(ws, s); return code; };
-    if ((rc = check_cuda(cudaMemsetAsync(maxa, 0, sizeof(unsigned long long) * (m + n), s), "memset")))
-        return bail(rc);
-    if ((rc = check_cuda(cudaMemsetAsync(nonfinite, 0, sizeof(int), s), "memset"))) return bail(rc);
-
-    const int sms = sm_count() > 0 ? sm_count() : 148;
-    auto rowmax = [&](int64_t rows, const double* R, int64_t sr, int64_t sl, unsigned long long* mb) {
-        if (sr == 1) {
-            const int64_t gx = (rows + 255) / 256;
-            int64_t gy = ((int64_t)sms * 8 + gx - 1) / gx;
-            if (gy > k) gy = k;
-            if (gy > 65535) gy = 65535;
-            const int64_t kchunk = (k + gy - 1) / gy;
-            gy = (k + kchunk - 1) / kchunk;
-            LaunchScope ls("oz_rowmax", s);
-            oz_rowmax_rows_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sl, kchunk, mb);
-        } else {
-            const int64_t gx = (rows * 32 + 255) / 256;
-            int64_t gy = ((int64_t)sms * 8 + gx - 1) / gx;
-            if (gy > (k + 255) / 256) gy = (k + 255) / 256;
-            if (gy < 1) gy = 1;
-            if (gy > 65535) gy = 65535;
-            const int64_t kchunk = (k + gy - 1) / gy;
-            gy = (k + kchunk - 1) / kchunk;
-            LaunchScope ls("oz_rowmax", s);
-            oz_rowmax_warp_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sr, sl, kchunk, mb);
-        }
-    };
-    // rows of op(A): element (i, l) = a[i*ars + l*acs]; rows of op(B)^T: (j, l) = b[l*brs + j*bcs]
-    rowmax(m, a, ars, acs, maxa);
-    rowmax(n, b, bcs, brs, maxb);
-    split_dispatch(slices, m, k, a, ars, acs, maxa, mpad, kpad, sa, ea, nonfinite, s);
-    split_dispatch(slices, n, k, b, bcs, brs, maxb, npad, kpad, sb, eb, nonfinite, s);
+    if ((rc = check_cuda(cudaMemsetAsync(maxb, 0, sizeof(unsigned long long) * n, s), "memset"))) return bail(rc);
+    // rows of op(B)^T: (j, l) = b[l*brs + j*bcs]
+    launch_rowmax(n, k, b, bcs, brs, maxb, s);
+    split_dispatch(slices, n, k, b, bcs, brs, maxb, npad, kpad, sb, eb, A->nonfinite, s);
     if ((rc = check_cuda(cudaGetLastError(), "oz_split"))) return bail(rc);
 
     CUtensorMap map_a, map_b;
-    if ((rc = make_slice_map(&map_a, sa, kpad, mpad, slices, OZ_BM))) return bail(rc);
+    if ((rc = make_slice_map(&map_a, A->sa, kpad, mpad, slices, OZ_BM))) return bail(rc);
     if ((rc = make_slice_map(&map_b, sb, kpad, npad, slices, pair_form ? OZ2_ROWS : OZ_BN))) return bail(rc);
-
-    static bool attr_set = false;
-    static int max_pairs = 0;
-    if (!attr_set) {
-        if ((rc = check_cuda(cudaFuncSetAttribute(ozaki_slice_gemm_kernel<OzGemmParams>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  OZ_SMEM_BYTES), "smem attr")))
-            return bail(rc);
-        if ((rc = check_cuda(cudaFuncSetAttribute(ozaki_slice_gemm_pair_kernel,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  OZ2_SMEM_BYTES), "smem attr")))
-            return bail(rc);
-        cudaLaunchConfig_t qc = {};
-        cudaLaunchAttribute qa[1];
-        qa[0].id = cudaLaunchAttributeClusterDimension;
-        qa[0].val.clusterDim.x = 2;
-        qa[0].val.clusterDim.y = 1;
-        qa[0].val.clusterDim.z = 1;
-        qc.gridDim = dim3(2 * (unsigned)(sms / 2));
-        qc.blockDim = dim3(OZ_THREADS);
-        qc.dynamicSmemBytes = OZ2_SMEM_BYTES;
-        qc.attrs = qa;
-        qc.numAttrs = 1;
-        if ((rc = check_cuda(cudaOccupancyMaxActiveClusters(&max_pairs, ozaki_slice_gemm_pair_kernel, &qc),
-                             "cluster occupancy")))
-            return bail(rc);
-        attr_set = true;
-    }
+    int max_pairs = 0;
+    if ((rc = slice_gemm_setup(&max_pairs))) return bail(rc);
+    const int sms = sm_count() > 0 ? sm_count() : 148;
     if (pair_form) {
         if (max_pairs < 1) return bail(set_error(GB_ERR_UNSUPPORTED, "ozaki", "no CTA pair fits on this GPU"));
         const int npair = (int)((p.items < max_pairs) ? p.items : max_pairs);
@@ -1543,14 +1599,14 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
         r.mpad = mpad;
         r.npad = npad;
         r.planes = planes;
-        r.ea = ea;
+        r.ea = A->ea;
         r.eb = eb;
         r.alpha = alpha;
         r.beta = beta;
         r.c = c;
         r.rs_c = rs_c;
         r.cs_c = cs_c;
-        r.skip = nonfinite;
+        r.skip = A->nonfinite;
         for (int L = 0; L < slices; ++L) r.lv[L] = p.lv[L];
         const int64_t total = ((m + 3) / 4) * n;
         int64_t blocks = (total + 255) / 256;
@@ -1559,9 +1615,24 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
         launch_recombine(slices, r, (unsigned)blocks, s);
     }
     if ((rc = check_cuda(cudaGetLastError(), "oz_recombine"))) return bail(rc);
-    // IEEE path for non-finite operands: runs only when the split raised the flag
-    rc = dgemm_native_gated(m, n, k, alpha, a, ars, acs, b, brs, bcs, beta, c, rs_c, cs_c, nonfinite, s);
+    // IEEE path for non-finite operands: runs only when a split raised the flag
+    rc = dgemm_native_gated(m, n, k, alpha, A->a, A->ars, A->acs, b, brs, bcs, beta, c, rs_c, cs_c, A->nonfinite, s);
     dev_free(ws, s);
+    return rc;
+}
+
+int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
+                const double* a, int64_t ars, int64_t acs,
+                const double* b, int64_t brs, int64_t bcs, double beta,
+                double* c, int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s)
+{
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    if (alpha == 0.0 || k <= 0) return scal_matrix(m, n, beta, c, rs_c, cs_c, s);
+    OzA A;
+    int rc = ozaki_prepare_a(m, k, a, ars, acs, slices, s, &A);
+    if (rc) return rc;
+    rc = ozaki_multiply(&A, n, b, brs, bcs, alpha, beta, c, rs_c, cs_c, s);
+    ozaki_release_a(&A, s);
     return rc;
 }
 

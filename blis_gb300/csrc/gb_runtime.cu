@@ -102,6 +102,21 @@ cudaStream_t thread_stream()
     return t_stream;
 }
 
+// Two more non-blocking streams per calling thread for host<->device copies
+// that overlap the compute stream (the pipelined host entry points).
+thread_local cudaStream_t t_copy[2] = {nullptr, nullptr};
+thread_local int t_copy_dev = -1;
+
+cudaStream_t thread_copy_stream(int i)
+{
+    if (t_copy_dev != g_device) {
+        t_copy[0] = t_copy[1] = nullptr;
+        t_copy_dev = g_device;
+    }
+    if (t_copy[i & 1] == nullptr) cudaStreamCreateWithFlags(&t_copy[i & 1], cudaStreamNonBlocking);
+    return t_copy[i & 1];
+}
+
 void* dev_alloc(size_t bytes, cudaStream_t s)
 {
     void* p = nullptr;

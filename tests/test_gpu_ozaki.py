@@ -169,3 +169,35 @@ def test_ozaki_device_api_matches_model():
     dev.dgemm_ozaki(N, N, 1.0, ta, tb, 0.0, tc, 8)
     torch.cuda.synchronize()
     assert np.array_equal(tc.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("ta,beta,pad", [(0, 0.0, 0), (1, 1.5, 3)])
+def test_ozaki_pipelined_host_path_bit_identical(ta, beta, pad):
+    """dgemm_ on host buffers large enough for the pipelined path (op(A) split
+    once, op(B) and C in column blocks on copy streams) gives the bits of one
+    device call on the same operands."""
+    torch = pytest.importorskip("torch")
+    from blis_gb300 import dev
+    m, n, k = 2048, 2304, 2048
+    a0 = po.expspread((k, m) if ta else (m, k), 41, -12, 12)
+    b0 = po.expspread((k, n), 42, -12, 12)
+    c0 = po.uniform((m, n), 43)
+    lda, ldb, ldc = a0.shape[0] + pad, k + pad, m + pad
+    a = np.zeros((lda, a0.shape[1]), order="F")
+    a[: a0.shape[0]] = a0
+    b = np.zeros((ldb, n), order="F")
+    b[:k] = b0
+    c = np.zeros((ldc, n), order="F")
+    c[:m] = c0
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 7)
+    try:
+        blas.dgemm("T" if ta else "N", "N", m, n, k, -0.5, a, lda, b, ldb, beta, c, ldc)
+    finally:
+        blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+    ad = torch.from_numpy(np.ascontiguousarray(a0.T)).cuda().t()
+    bd = torch.from_numpy(np.ascontiguousarray(b0.T)).cuda().t()
+    cd = torch.from_numpy(np.ascontiguousarray(c0.T)).cuda().t()
+    dev.dgemm_ozaki(8 if ta else 0, 0, -0.5, ad, bd, beta, cd, 7)
+    torch.cuda.synchronize()
+    assert np.array_equal(c[:m], cd.cpu().numpy())
+    assert np.all(c[m:] == 0.0)  # padding rows of C untouched
