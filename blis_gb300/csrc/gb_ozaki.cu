@@ -1098,8 +1098,10 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const __grid_constant
 // Split for every problem of a batch in one launch.  A block owns 32 rows of
 // op(A_i) or op(B_i)^T over the whole k range: pass 1 takes the row maxima
 // (8 threads per row), pass 2 cuts 64-wide k blocks into digits and writes
-// them into the problem's boxes.  Rows past m (n) up to the box height and
-// k past k_i up to the block width are written as zeros.
+// them into the problem's boxes.  Only blocks holding rows of the matrix
+// run; their rows past m (n) and k past k_i up to the block width are
+// written as zeros, and the remaining padding rows of a box stay as the
+// plan's one-time zero fill left them.
 template <int S>
 __global__ void __launch_bounds__(256, 2) oz_split_batch_kernel(const OzBatchProb* __restrict__ probs,
                                                              const int32_t* __restrict__ unit_prob,
@@ -1734,7 +1736,7 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
         q.tiles_m = (int32_t)((p.m + OZ_BM - 1) / OZ_BM);
         q.tiles_n = (int32_t)((p.n + OZ_BN - 1) / OZ_BN);
         q.kb = (int32_t)((p.k + OZ_BK - 1) / OZ_BK);
-        q.units_a = (int64_t)q.tiles_m * (OZ_BM / 32);
+        q.units_a = (p.m + 31) / 32;  // 32-row blocks holding rows of op(A); the padding is zeroed once
         q.ld = round_up(p.m, 4);
         h.push_back(q);
     }
@@ -1776,7 +1778,7 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
         item_base.push_back(ob->items);
         item_prob.insert(item_prob.end(), (size_t)it, i);
         ob->items += it;
-        const int64_t un = q.units_a + (int64_t)q.tiles_n * (OZ_BN / 32);
+        const int64_t un = q.units_a + (q.n + 31) / 32;
         unit_base.push_back(ob->units);
         unit_prob.insert(unit_prob.end(), (size_t)un, i);
         ob->units += un;
@@ -1827,7 +1829,8 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
         q.eb = q.ea + q.m;
         ex_off += q.m + q.n;
     }
-    int rc = GB_SUCCESS;
+    // rows past m (n) up to the tile height are never written by the split: zero them once here
+    int rc = check_cuda(cudaMemsetAsync(ob->sa, 0, b_sa + b_sb, s), "memset slices");
     auto up = [&](void* d, const void* src, size_t b) {
         if (!rc && b) rc = check_cuda(cudaMemcpyAsync(d, src, b, cudaMemcpyHostToDevice, s), "batch tables");
     };
