@@ -84,6 +84,7 @@ struct BatchPlan {
     cudaGraphExec_t graph;
     cudaStream_t graph_stream;
     OzBatch* oz = nullptr;
+    SupGroup* sup = nullptr;  // problems the selector sends to the 64 x 64 engine
     const int* gate = nullptr;
     BatchPlan* rest = nullptr;
     std::vector<gb_gemm_problem_t> singles;
@@ -102,6 +103,7 @@ static int launch_plan(BatchPlan* pl, cudaStream_t s)
                          pl->slices, s);
         if (rc) return rc;
     }
+    if (pl->sup && (rc = sup_group_launch(pl->sup, s))) return rc;
     if (pl->total_tiles == 0) return GB_SUCCESS;
     GB_CUDA(cudaMemsetAsync(pl->d_counter, 0, sizeof(unsigned long long), s));
     const int sms = sm_count() > 0 ? sm_count() : 148;
@@ -121,10 +123,46 @@ static int launch_plan(BatchPlan* pl, cudaStream_t s)
 void batch_plan_destroy(BatchPlan* pl);
 static int batch_plan_build(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out);
 
+// Native FP64/FP32 batch.  With a selector model loaded and auto-selection on
+// (gb_set_gemm_autoselect), each problem gets the configuration the model
+// picks from the autotuned timings: config 0 problems share the 128 x 128
+// grouped launch, the others the grouped 64 x 64 / split-K launch.  Without a
+// model every problem takes the 128 x 128 engine.
+static int batch_plan_selected(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out)
+{
+    std::vector<gb_gemm_problem_t> big, small;
+    std::vector<int> cfgs;
+    for (int64_t i = 0; i < count; ++i) {
+        const gb_gemm_problem_t& p = probs[i];
+        if (p.m < 0 || p.n < 0 || p.k < 0) return set_error(GB_ERR_ARG, "gb_batch", "negative dimension");
+        int cfg = 0, sl = 0;
+        if (selector_auto() && p.m > 0 && p.n > 0 && p.k > 0 && p.alpha != 0.0 &&
+            selector_choose(dtype, p.m, p.n, p.k, GB_IS_TRANS(p.transa), GB_IS_TRANS(p.transb), 0, 0.0, 0.0, &cfg,
+                            &sl) != GB_SUCCESS)
+            cfg = 0;
+        if (cfg >= 1 && cfg < GB_GEMM_NUM_CONFIGS) {
+            small.push_back(p);
+            cfgs.push_back(cfg);
+        } else {
+            big.push_back(p);
+        }
+    }
+    BatchPlan* pl = nullptr;
+    int rc = batch_plan_build(big.data(), (int64_t)big.size(), dtype, &pl);
+    if (rc) return rc;
+    if (!small.empty() &&
+        (rc = sup_group_create(dtype, small.data(), cfgs.data(), (int64_t)small.size(), thread_stream(), &pl->sup))) {
+        batch_plan_destroy(pl);
+        return rc;
+    }
+    *out = pl;
+    return GB_SUCCESS;
+}
+
 int batch_plan_create(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out)
 {
     *out = nullptr;
-    if (dtype != GB_BATCH_FP64_OZAKI) return batch_plan_build(probs, count, dtype, out);
+    if (dtype != GB_BATCH_FP64_OZAKI) return batch_plan_selected(probs, count, dtype, out);
     int slices = ozaki_slices();
     if (slices < 2) slices = 8;  // automatic: the verifier is per problem; the batch uses 8
     std::vector<gb_gemm_problem_t> grouped, rest, singles;
@@ -247,6 +285,7 @@ void batch_plan_destroy(BatchPlan* pl)
     dev_free(pl->d_desc, s);
     dev_free(pl->d_counter, s);
     ozaki_batch_destroy(pl->oz, s);
+    sup_group_destroy(pl->sup, s);
     cudaStreamSynchronize(s);
     batch_plan_destroy(pl->rest);
     delete pl;

@@ -137,6 +137,14 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
 int ozaki_batch_launch(OzBatch* ob, cudaStream_t s);
 const int* ozaki_batch_flag(const OzBatch* ob);
 void ozaki_batch_destroy(OzBatch* ob, cudaStream_t s);
+// gemm_batch problems whose selected configuration is the 64 x 64 engine
+// (configs 1..5; m, n, k > 0, alpha != 0), grouped in one launch plus one
+// fold launch for the problems split along k (gb_sup.cu).
+struct SupGroup;
+int sup_group_create(int dtype, const gb_gemm_problem_t* probs, const int* configs, int64_t count, cudaStream_t s,
+                     SupGroup** out);
+int sup_group_launch(SupGroup* g, cudaStream_t s);
+void sup_group_destroy(SupGroup* g, cudaStream_t s);
 int dotv_nparts(int64_t n);
 int scal_matrix(int64_t m, int64_t n, double beta, double* c, int64_t rs_c, int64_t cs_c,
                 cudaStream_t s);

@@ -17,6 +17,9 @@
 //                 bf16 loads, FP32 arithmetic)
 #include <cuda_bf16.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "gb_internal.h"
 
 namespace gb {
@@ -84,11 +87,11 @@ __device__ __forceinline__ void sup_store(const SupArgs<T, TI>& p, T (&ra)[8], T
 }
 
 template <typename T, typename TI>
-__device__ __forceinline__ void sup_out(const SupArgs<T, TI>& p, int64_t i, int64_t j, T ab)
+__device__ __forceinline__ void sup_out(const SupArgs<T, TI>& p, int64_t i, int64_t j, T ab, int z)
 {
     if (i >= p.m || j >= p.n) return;
     if (p.ws) {
-        p.ws[((int64_t)blockIdx.z * p.n + j) * p.m + i] = ab;
+        p.ws[((int64_t)z * p.n + j) * p.m + i] = ab;
     } else {
         T* cij = p.c + i * p.rs_c + j * p.cs_c;
         const T t = p.alpha * ab;
@@ -103,14 +106,12 @@ __device__ __forceinline__ void dmma(double& d0, double& d1, double a, double b)
                  : "d"(a), "d"(b));
 }
 
+// One 64 x 64 tile of C (rows bm.., columns bn..) over the z-th k chunk.
 // FP64: 2 x 2 warps of 32 x 32, DMMA.  FP32: 16 x 8 threads of 4 x 8, FMA.
 template <typename T, typename TI>
-__global__ void __launch_bounds__(SNT) sup_gemm_kernel(SupArgs<T, TI> p)
+__device__ __forceinline__ void sup_tile(const SupArgs<T, TI>& p, int64_t bm, int64_t bn, int z, T* As, T* Bs)
 {
-    __shared__ T As[SBK * SLDS];
-    __shared__ T Bs[SBK * SLDS];
-    const int64_t bm = (int64_t)blockIdx.y * SBM, bn = (int64_t)blockIdx.x * SBN;
-    const int64_t k0 = (int64_t)blockIdx.z * p.kchunk;
+    const int64_t k0 = (int64_t)z * p.kchunk;
     const int64_t k1 = (k0 + p.kchunk < p.k) ? k0 + p.kchunk : p.k;
     T ra[8], rb[8];
     if constexpr (sizeof(T) == 8) {
@@ -147,8 +148,8 @@ __global__ void __launch_bounds__(SNT) sup_gemm_kernel(SupArgs<T, TI> p)
             for (int ni = 0; ni < 4; ++ni) {
                 const int64_t i = bm + wm * 32 + mi * 8 + (lane >> 2);
                 const int64_t j = bn + wn * 32 + ni * 8 + 2 * (lane & 3);
-                sup_out(p, i, j, (T)acc[mi][ni][0]);
-                sup_out(p, i, j + 1, (T)acc[mi][ni][1]);
+                sup_out(p, i, j, (T)acc[mi][ni][0], z);
+                sup_out(p, i, j + 1, (T)acc[mi][ni][1], z);
             }
     } else {
         const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;  // 8 x 16 threads
@@ -179,8 +180,16 @@ __global__ void __launch_bounds__(SNT) sup_gemm_kernel(SupArgs<T, TI> p)
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int j = 0; j < 8; ++j) sup_out(p, bm + ty * 4 + i, bn + tx * 8 + j, acc[i][j]);
+            for (int j = 0; j < 8; ++j) sup_out(p, bm + ty * 4 + i, bn + tx * 8 + j, acc[i][j], z);
     }
+}
+
+template <typename T, typename TI>
+__global__ void __launch_bounds__(SNT) sup_gemm_kernel(SupArgs<T, TI> p)
+{
+    __shared__ T As[SBK * SLDS];
+    __shared__ T Bs[SBK * SLDS];
+    sup_tile(p, (int64_t)blockIdx.y * SBM, (int64_t)blockIdx.x * SBN, (int)blockIdx.z, As, Bs);
 }
 
 // c = alpha * sum_z ws[z] (+ beta c), z in increasing order.
@@ -232,7 +241,206 @@ int sup_gemm(int splits, int64_t m, int64_t n, int64_t k, T alpha, const TI* a, 
     return rc;
 }
 
+// ---------------------------------------------------------------- grouped form
+// The gemm_batch problems whose selected configuration is the 64 x 64 engine
+// (configs 1..5) run in one persistent launch: a device counter hands out
+// tiles (problem, k chunk z, tile row, tile column) in the order of a table
+// sorted by work; problems split along k write partial sums to their own
+// workspace and one grouped fold launch adds them in order of z.
+template <typename T>
+struct SupGroupDesc {
+    SupArgs<T> p;
+    int64_t tile_start;  // first tile of this problem
+    int64_t fold_start;  // first fold block (split problems only)
+    int32_t tiles_m, tiles_n, splits, pad;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(SNT) sup_grouped_kernel(const SupGroupDesc<T>* __restrict__ d, int nprob,
+                                                          int64_t total_tiles, unsigned long long* counter)
+{
+    __shared__ T As[SBK * SLDS];
+    __shared__ T Bs[SBK * SLDS];
+    __shared__ long long tile_s;
+    for (;;) {
+        if (threadIdx.x == 0) tile_s = (long long)atomicAdd(counter, 1ull);
+        __syncthreads();
+        const long long tile = tile_s;
+        __syncthreads();
+        if (tile >= total_tiles) break;
+        int lo = 0, hi = nprob - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (d[mid].tile_start <= tile) lo = mid;
+            else hi = mid - 1;
+        }
+        const SupGroupDesc<T>& q = d[lo];
+        const int64_t local = tile - q.tile_start;
+        const int64_t per = (int64_t)q.tiles_m * q.tiles_n;
+        const int z = (int)(local / per);
+        const int64_t t = local - (int64_t)z * per;
+        sup_tile(q.p, (t / q.tiles_n) * SBM, (t % q.tiles_n) * SBN, z, As, Bs);
+    }
+}
+
+template <typename T>
+__global__ void sup_grouped_fold_kernel(const SupGroupDesc<T>* __restrict__ d, const int32_t* __restrict__ fprob)
+{
+    const int pi = fprob[blockIdx.x];
+    const SupGroupDesc<T>& q = d[pi];
+    const int64_t total = q.p.m * q.p.n;
+    const int64_t e = ((int64_t)blockIdx.x - q.fold_start) * 256 + threadIdx.x;
+    if (e >= total) return;
+    const int64_t i = e % q.p.m, j = e / q.p.m;
+    T acc = q.p.ws[e];
+    for (int z = 1; z < q.splits; ++z) acc += q.p.ws[(int64_t)z * total + e];
+    T* cij = q.p.c + i * q.p.rs_c + j * q.p.cs_c;
+    const T t = q.p.alpha * acc;
+    *cij = (q.p.beta == T(0)) ? t : fma(q.p.beta, *cij, t);
+}
+
 }  // namespace
+
+struct SupGroup {
+    int dtype = 0;
+    int nprob = 0;
+    int64_t total_tiles = 0, fblocks = 0;
+    uint8_t* arena = nullptr;  // descriptors, fold table, counter, split workspaces
+    void* d_desc = nullptr;
+    int32_t* d_fprob = nullptr;
+    unsigned long long* d_counter = nullptr;
+};
+
+namespace {
+
+template <typename T>
+int sup_group_build(const gb_gemm_problem_t* probs, const int* configs, int64_t count, cudaStream_t s,
+                    SupGroup* g)
+{
+    std::vector<SupGroupDesc<T>> h;
+    std::vector<int64_t> work;
+    size_t ws_elems = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        const gb_gemm_problem_t& q = probs[i];
+        const int cfg = configs[i];
+        if (cfg < 1 || cfg >= GB_GEMM_NUM_CONFIGS || q.m <= 0 || q.n <= 0 || q.k <= 0 || q.alpha == 0.0)
+            return set_error(GB_ERR_ARG, "gemm_batch", "problem not eligible for the 64 x 64 engine");
+        const bool ta = GB_IS_TRANS(q.transa), tb = GB_IS_TRANS(q.transb);
+        SupGroupDesc<T> d = {};
+        const int splits = 1 << (cfg - 1);
+        int64_t kchunk = (q.k + splits - 1) / splits;
+        kchunk = (kchunk + SBK - 1) / SBK * SBK;
+        d.splits = (int32_t)((q.k + kchunk - 1) / kchunk);
+        d.p = SupArgs<T>{q.m, q.n, q.k, kchunk, (T)q.alpha, (T)q.beta, static_cast<const T*>(q.a),
+                         ta ? q.lda : 1, ta ? 1 : q.lda, static_cast<const T*>(q.b), tb ? q.ldb : 1, tb ? 1 : q.ldb,
+                         static_cast<T*>(q.c), 1, q.ldc, nullptr};
+        d.tiles_m = (int32_t)((q.m + SBM - 1) / SBM);
+        d.tiles_n = (int32_t)((q.n + SBN - 1) / SBN);
+        if (d.splits > 1) {
+            d.p.ws = reinterpret_cast<T*>((uintptr_t)ws_elems);  // offset until the arena exists
+            ws_elems += (size_t)d.splits * q.m * q.n;
+        }
+        h.push_back(d);
+        work.push_back(q.k / d.splits);
+    }
+    // longest k chunk first
+    std::vector<size_t> order(h.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return work[x] > work[y]; });
+    std::vector<SupGroupDesc<T>> hs;
+    std::vector<int32_t> fprob;
+    for (size_t i : order) hs.push_back(h[i]);
+    int64_t tiles = 0, fb = 0;
+    for (size_t i = 0; i < hs.size(); ++i) {
+        SupGroupDesc<T>& d = hs[i];
+        d.tile_start = tiles;
+        tiles += (int64_t)d.splits * d.tiles_m * d.tiles_n;
+        d.fold_start = fb;
+        if (d.splits > 1) {
+            const int64_t nb = (d.p.m * d.p.n + 255) / 256;
+            fprob.insert(fprob.end(), (size_t)nb, (int32_t)i);
+            fb += nb;
+        }
+    }
+    if (fb > INT32_MAX) return set_error(GB_ERR_ARG, "gemm_batch", "fold too large for one launch");
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t b_desc = al(sizeof(SupGroupDesc<T>) * (hs.size() + 1)), b_fp = al(4 * (fprob.size() + 1));
+    const size_t b_ws = al(sizeof(T) * ws_elems);
+    g->arena = static_cast<uint8_t*>(dev_alloc(b_desc + b_fp + 256 + b_ws, s));
+    if (!g->arena) return GB_ERR_NOMEM;
+    g->d_desc = g->arena;
+    g->d_fprob = reinterpret_cast<int32_t*>(g->arena + b_desc);
+    g->d_counter = reinterpret_cast<unsigned long long*>(g->arena + b_desc + b_fp);
+    T* ws = reinterpret_cast<T*>(g->arena + b_desc + b_fp + 256);
+    for (auto& d : hs)
+        if (d.splits > 1) d.p.ws = ws + (size_t)(uintptr_t)d.p.ws;
+    g->nprob = (int)hs.size();
+    g->total_tiles = tiles;
+    g->fblocks = fb;
+    int rc = GB_SUCCESS;
+    if (!hs.empty())
+        rc = check_cuda(cudaMemcpyAsync(g->d_desc, hs.data(), sizeof(SupGroupDesc<T>) * hs.size(),
+                                        cudaMemcpyHostToDevice, s), "sup group table");
+    if (!rc && !fprob.empty())
+        rc = check_cuda(cudaMemcpyAsync(g->d_fprob, fprob.data(), 4 * fprob.size(), cudaMemcpyHostToDevice, s),
+                        "sup group table");
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "sup group table");  // host tables go out of scope
+    return rc;
+}
+
+template <typename T>
+int sup_group_run(SupGroup* g, cudaStream_t s)
+{
+    if (g->total_tiles == 0) return GB_SUCCESS;
+    GB_CUDA(cudaMemsetAsync(g->d_counter, 0, sizeof(unsigned long long), s));
+    const int sms = sm_count() > 0 ? sm_count() : 148;
+    int64_t grid = (int64_t)sms * 8;  // 128-thread CTAs, several per SM
+    if (grid > g->total_tiles) grid = g->total_tiles;
+    {
+        LaunchScope ls(sizeof(T) == 8 ? "batch_grouped_sup_dmma" : "batch_grouped_sup_ffma", s);
+        sup_grouped_kernel<T><<<(unsigned)grid, SNT, 0, s>>>(static_cast<const SupGroupDesc<T>*>(g->d_desc),
+                                                              g->nprob, g->total_tiles, g->d_counter);
+    }
+    int rc = check_cuda(cudaGetLastError(), "grouped sup");
+    if (!rc && g->fblocks > 0) {
+        LaunchScope ls("batch_grouped_sup_fold", s);
+        sup_grouped_fold_kernel<T><<<(unsigned)g->fblocks, 256, 0, s>>>(
+            static_cast<const SupGroupDesc<T>*>(g->d_desc), g->d_fprob);
+        rc = check_cuda(cudaGetLastError(), "grouped sup fold");
+    }
+    return rc;
+}
+
+}  // namespace
+
+int sup_group_create(int dtype, const gb_gemm_problem_t* probs, const int* configs, int64_t count, cudaStream_t s,
+                     SupGroup** out)
+{
+    *out = nullptr;
+    SupGroup* g = new SupGroup();
+    g->dtype = dtype;
+    const int rc = (dtype == 0) ? sup_group_build<double>(probs, configs, count, s, g)
+                                : sup_group_build<float>(probs, configs, count, s, g);
+    if (rc) {
+        sup_group_destroy(g, s);
+        return rc;
+    }
+    *out = g;
+    return GB_SUCCESS;
+}
+
+int sup_group_launch(SupGroup* g, cudaStream_t s)
+{
+    if (!g) return GB_SUCCESS;
+    return (g->dtype == 0) ? sup_group_run<double>(g, s) : sup_group_run<float>(g, s);
+}
+
+void sup_group_destroy(SupGroup* g, cudaStream_t s)
+{
+    if (!g) return;
+    dev_free(g->arena, s);
+    delete g;
+}
 
 int gemm_config_dev(int dtype, int config, int64_t m, int64_t n, int64_t k, double alpha,
                     const void* a, int64_t ars, int64_t acs, const void* b, int64_t brs, int64_t bcs,

@@ -145,3 +145,69 @@ class _lib_problem(C.Structure):
                 ("k", C.c_int64), ("alpha", C.c_double), ("beta", C.c_double), ("a", C.c_void_p),
                 ("lda", C.c_int64), ("b", C.c_void_p), ("ldb", C.c_int64), ("c", C.c_void_p),
                 ("ldc", C.c_int64)]
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_batch_with_selected_configs(gblib, dtype):
+    """With the trained selector loaded, each problem of a batch gets its own
+    configuration (128 x 128 grouped launch, or the grouped 64 x 64 engine with
+    split-K and the grouped fold); results meet the testsuite residual, repeat
+    bit for bit under graph replay, and some problems take each class."""
+    torch = pytest.importorskip("torch")
+    from blis_gb300 import selector as S
+    rng = np.random.default_rng(9)
+    probs = []
+    for i in range(96):
+        m, n = (int(rng.integers(8, 400)) for _ in range(2))
+        k = int(rng.integers(8, 3000)) if i % 3 else 6000  # long k: split-K candidates
+        ta, tb = rng.integers(0, 2, 2)
+        a = po.uniform((k, m) if ta else (m, k), 100 + 3 * i, dtype=dtype)
+        b = po.uniform((n, k) if tb else (k, n), 101 + 3 * i, dtype=dtype)
+        c = po.uniform((m, n), 102 + 3 * i, dtype=dtype)
+        probs.append(("T" if ta else "N", "T" if tb else "N", m, n, k, a, b, c))
+    tdt = torch.float64 if dtype == np.float64 else torch.float32
+    descs = (_lib_problem * len(probs))()
+    keep, outs = [], []
+    for i, (ta, tb, m, n, k, a, b, c) in enumerate(probs):
+        A = torch.from_numpy(np.asfortranarray(a).T.copy()).cuda()
+        B = torch.from_numpy(np.asfortranarray(b).T.copy()).cuda()
+        Cg = torch.from_numpy(np.asfortranarray(c).T.copy()).cuda()
+        keep += [A, B]
+        outs.append(Cg)
+        descs[i] = _lib_problem(8 if ta == "T" else 0, 8 if tb == "T" else 0, m, n, k, 1.25, -0.5, A.data_ptr(),
+                                a.shape[0], B.data_ptr(), b.shape[0], Cg.data_ptr(), m)
+    L = _lib.load()
+    code = 0 if dtype == np.float64 else 1
+    S.load_into_library()
+    try:
+        cfgs = []
+        for (ta, tb, m, n, k, a, b, c) in probs:
+            cfg, sl = C.c_int(), C.c_int()
+            assert gblib.gb_selector_choose(code, m, n, k, int(ta == "T"), int(tb == "T"), 0, 0.0, 0.0,
+                                            C.byref(cfg), C.byref(sl)) == 0
+            cfgs.append(cfg.value)
+        assert 0 in cfgs and any(v >= 1 for v in cfgs)
+        c0 = [o.clone() for o in outs]
+        plan = C.c_void_p()
+        assert L.gb_batch_plan_create(C.addressof(descs), len(probs), code, C.byref(plan)) == 0
+        first = None
+        for rep in range(3):
+            for o, z in zip(outs, c0):
+                o.copy_(z)
+            assert L.gb_batch_plan_run(plan, 1, None) == 0
+            assert L.gb_synchronize() == 0
+            got = [o.clone() for o in outs]
+            if first is None:
+                first = got
+            else:
+                assert all(torch.equal(x, y) for x, y in zip(first, got))
+        L.gb_batch_plan_destroy(plan)
+    finally:
+        gblib.gb_set_gemm_autoselect(0)
+        gblib.gb_selector_unload()
+    thresh = 1e-14 if dtype == np.float64 else 1e-5
+    for (ta, tb, m, n, k, a, b, c), g in zip(probs, first):
+        r = H.gemm_residual(1.25, H.op(a, 8 if ta == "T" else 0).astype(np.float64),
+                            H.op(b, 8 if tb == "T" else 0).astype(np.float64), -0.5, c.astype(np.float64),
+                            g.cpu().numpy().T.astype(np.float64))
+        assert r < thresh
