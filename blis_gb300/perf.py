@@ -287,6 +287,19 @@ def run_batch(out):
                       reps=1, warmup=1)
         L.gb_batch_plan_destroy(plan)
         rec.update({"loop_ms": ms_l, "loop_tflops": flops / ms_l / 1e9, "speedup": ms_l / ms_g})
+        if dtype in (0, 1):
+            # the same batch with per-problem configurations from the trained selector
+            from . import selector as S
+            S.load_into_library()
+            try:
+                plan2 = C.c_void_p()
+                _lib.check(L.gb_batch_plan_create(C.addressof(probs), 4096, dtype, C.byref(plan2)), "plan")
+                ms_s = _timer(lambda: _lib.check(L.gb_batch_plan_run(plan2, 1, st), "run"), reps=3, warmup=1)
+                L.gb_batch_plan_destroy(plan2)
+            finally:
+                L.gb_set_gemm_autoselect(0)
+                L.gb_selector_unload()
+            rec.update({"grouped_selected_ms": ms_s, "grouped_selected_tflops": flops / ms_s / 1e9})
         out.append(rec)
         L.gb_set_dgemm_mode(0, 8)
         del keep
