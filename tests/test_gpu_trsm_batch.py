@@ -196,6 +196,7 @@ def test_batch_with_selected_configs(gblib, dtype):
         for rep in range(3):
             for o, z in zip(outs, c0):
                 o.copy_(z)
+            torch.cuda.synchronize()  # the plan runs on the library's stream, not torch's
             assert L.gb_batch_plan_run(plan, 1, None) == 0
             assert L.gb_synchronize() == 0
             got = [o.clone() for o in outs]
