@@ -96,6 +96,8 @@ def load(path=None):
     _sig(L, "gb_batch_plan_create", C.c_int, [_vp, _i64, C.c_int, C.POINTER(C.c_void_p)])
     _sig(L, "gb_batch_plan_run", C.c_int, [_vp, C.c_int, _vp])
     _sig(L, "gb_batch_plan_destroy", C.c_int, [_vp])
+    _sig(L, "gb_batch_plan_create_ex", C.c_int, [_vp, _i64, C.c_int, C.c_int, C.POINTER(C.c_void_p)])
+    _sig(L, "gb_batch_plan_policy", C.c_int, [_vp])
     _sig(L, "gb_randm_dev", C.c_int, [C.c_int, C.c_int, _vp, _i64, _i64, _i64, _i64, C.c_uint64, _d, _d, _vp])
     _sig(L, "gb_dd_gemm_entries_dev", C.c_int, [C.c_int, C.c_int, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64,
                                                  _d, _vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp, _vp])

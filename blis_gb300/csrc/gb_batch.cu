@@ -85,6 +85,7 @@ struct BatchPlan {
     cudaStream_t graph_stream;
     OzBatch* oz = nullptr;
     SupGroup* sup = nullptr;  // problems the selector sends to the 64 x 64 engine
+    int policy = 0;           // configuration policy the plan's autotuning kept (native plans)
     const int* gate = nullptr;
     BatchPlan* rest = nullptr;
     std::vector<gb_gemm_problem_t> singles;
@@ -121,14 +122,14 @@ static int launch_plan(BatchPlan* pl, cudaStream_t s)
 }
 
 void batch_plan_destroy(BatchPlan* pl);
+int batch_plan_run(BatchPlan* pl, cudaStream_t s, bool use_graph);
 static int batch_plan_build(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out);
 
-// Native FP64/FP32 batch.  With a selector model loaded and auto-selection on
-// (gb_set_gemm_autoselect), each problem gets the configuration the model
-// picks from the autotuned timings: config 0 problems share the 128 x 128
-// grouped launch, the others the grouped 64 x 64 / split-K launch.  Without a
-// model every problem takes the 128 x 128 engine.
-static int batch_plan_selected(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out)
+// Native FP64/FP32 batch with one configuration policy: 0 = every problem
+// on the 128 x 128 engine; 1 = the 64 x 64 engine for the problems whose
+// selected configuration is 1..5, without split-K (a batch already has
+// parallelism); 2 = the selected configuration including its split-K.
+int batch_plan_policy(const gb_gemm_problem_t* probs, int64_t count, int dtype, int policy, BatchPlan** out)
 {
     std::vector<gb_gemm_problem_t> big, small;
     std::vector<int> cfgs;
@@ -136,10 +137,11 @@ static int batch_plan_selected(const gb_gemm_problem_t* probs, int64_t count, in
         const gb_gemm_problem_t& p = probs[i];
         if (p.m < 0 || p.n < 0 || p.k < 0) return set_error(GB_ERR_ARG, "gb_batch", "negative dimension");
         int cfg = 0, sl = 0;
-        if (selector_auto() && p.m > 0 && p.n > 0 && p.k > 0 && p.alpha != 0.0 &&
+        if (policy > 0 && p.m > 0 && p.n > 0 && p.k > 0 && p.alpha != 0.0 &&
             selector_choose(dtype, p.m, p.n, p.k, GB_IS_TRANS(p.transa), GB_IS_TRANS(p.transb), 0, 0.0, 0.0, &cfg,
                             &sl) != GB_SUCCESS)
             cfg = 0;
+        if (policy == 1 && cfg > 1) cfg = 1;
         if (cfg >= 1 && cfg < GB_GEMM_NUM_CONFIGS) {
             small.push_back(p);
             cfgs.push_back(cfg);
@@ -159,10 +161,66 @@ static int batch_plan_selected(const gb_gemm_problem_t* probs, int64_t count, in
     return GB_SUCCESS;
 }
 
-int batch_plan_create(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out)
+// Native FP64/FP32 plan.  Without a selector model (gb_selector_load_file +
+// gb_set_gemm_autoselect) every problem takes the 128 x 128 engine.  With
+// one, the plan is autotuned when it is created: each policy runs twice on
+// the batch's own shapes with scratch outputs (the caller's C is not
+// touched), timed with CUDA events, and the fastest is kept.
+static int batch_plan_selected(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out)
+{
+    if (!selector_auto()) return batch_plan_policy(probs, count, dtype, 0, out);
+    cudaStream_t s = thread_stream();
+    const size_t esz = dtype == GB_BATCH_FP32 ? 4 : 8;
+    std::vector<gb_gemm_problem_t> tune(probs, probs + count);
+    size_t elems = 0;
+    for (const auto& p : tune) elems += (p.m > 0 && p.n > 0) ? (size_t)(p.m * p.n) : 0;
+    char* scratch = static_cast<char*>(dev_alloc(esz * (elems + 1), s));
+    if (!scratch) return GB_ERR_NOMEM;
+    size_t off = 0;
+    for (auto& p : tune) {
+        if (p.m <= 0 || p.n <= 0) continue;
+        p.c = scratch + off * esz;
+        p.ldc = p.m;
+        off += (size_t)(p.m * p.n);
+    }
+    int rc = check_cuda(cudaMemsetAsync(scratch, 0, esz * (elems + 1), s), "batch tuning");
+    int best = 0;
+    float best_ms = 0.0f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int policy = 0; policy < 3 && !rc; ++policy) {
+        BatchPlan* t = nullptr;
+        if ((rc = batch_plan_policy(tune.data(), count, dtype, policy, &t))) break;
+        rc = batch_plan_run(t, s, false);  // warm-up
+        cudaEventRecord(e0, s);
+        if (!rc) rc = batch_plan_run(t, s, false);
+        cudaEventRecord(e1, s);
+        if (!rc) rc = check_cuda(cudaEventSynchronize(e1), "batch tuning");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (!rc && (policy == 0 || ms < best_ms)) {
+            best = policy;
+            best_ms = ms;
+        }
+        batch_plan_destroy(t);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    dev_free(scratch, s);
+    if (rc) return rc;
+    rc = batch_plan_policy(probs, count, dtype, best, out);
+    if (!rc) (*out)->policy = best;
+    return rc;
+}
+
+// `tune`: resident plans autotune their configuration policy (see above);
+// one-shot grouped calls take the 128 x 128 engine for every problem.
+int batch_plan_create(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out, bool tune)
 {
     *out = nullptr;
-    if (dtype != GB_BATCH_FP64_OZAKI) return batch_plan_selected(probs, count, dtype, out);
+    if (dtype != GB_BATCH_FP64_OZAKI)
+        return tune ? batch_plan_selected(probs, count, dtype, out) : batch_plan_policy(probs, count, dtype, 0, out);
     int slices = ozaki_slices();
     if (slices < 2) slices = 8;  // automatic: the verifier is per problem; the batch uses 8
     std::vector<gb_gemm_problem_t> grouped, rest, singles;
@@ -435,7 +493,7 @@ void batch_blas(const char* name, const char* transa_array, const char* transb_a
     // dgemm_batch_ follows the precision mode of dgemm_ (gb_set_dgemm_mode)
     const int dtype = sizeof(T) == 4 ? GB_BATCH_FP32
                                      : (dgemm_mode() == GB_DGEMM_OZAKI ? GB_BATCH_FP64_OZAKI : GB_BATCH_FP64);
-    int rc = batch_plan_create(probs.data(), (int64_t)probs.size(), dtype, &pl);
+    int rc = batch_plan_create(probs.data(), (int64_t)probs.size(), dtype, &pl, false);
     if (!rc) rc = batch_plan_run(pl, s, false);
     if (!rc) {
         for (auto& h : hs) {
@@ -513,7 +571,7 @@ int gb_gemm_batch_dev(const gb_gemm_problem_t* probs, gb_dim_t count, int dtype,
         return set_error(GB_ERR_ARG, "gb_gemm_batch_dev", "dtype must be GB_BATCH_FP64, FP32 or FP64_OZAKI");
     if (mode == GB_BATCH_LOOP) return batch_loop(probs, count, dtype, s);
     BatchPlan* pl = nullptr;
-    if ((rc = batch_plan_create(probs, count, dtype, &pl))) return rc;
+    if ((rc = batch_plan_create(probs, count, dtype, &pl, false))) return rc;
     rc = batch_plan_run(pl, s, false);
     cudaStreamSynchronize(s);
     batch_plan_destroy(pl);
@@ -527,7 +585,7 @@ int gb_batch_plan_create(const gb_gemm_problem_t* probs, gb_dim_t count, int dty
     if (dtype != GB_BATCH_FP64 && dtype != GB_BATCH_FP32 && dtype != GB_BATCH_FP64_OZAKI)
         return set_error(GB_ERR_ARG, "gb_batch_plan_create", "dtype must be GB_BATCH_FP64, FP32 or FP64_OZAKI");
     BatchPlan* pl = nullptr;
-    rc = batch_plan_create(probs, count, dtype, &pl);
+    rc = batch_plan_create(probs, count, dtype, &pl, true);
     *plan = pl;
     return rc;
 }
@@ -546,3 +604,28 @@ int gb_batch_plan_destroy(void* plan)
 }
 
 }  // extern "C"
+
+extern "C" int gb_batch_plan_create_ex(const gb_gemm_problem_t* probs, gb_dim_t count, int dtype, int policy,
+                                       void** plan)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    *plan = nullptr;
+    if (dtype != GB_BATCH_FP64 && dtype != GB_BATCH_FP32)
+        return gb::set_error(GB_ERR_ARG, "gb_batch_plan_create_ex", "dtype must be GB_BATCH_FP64 or FP32");
+    if (policy < -1 || policy > 2) return gb::set_error(GB_ERR_ARG, "gb_batch_plan_create_ex", "policy in -1..2");
+    if (policy > 0 && !gb::selector_auto())
+        return gb::set_error(GB_ERR_ARG, "gb_batch_plan_create_ex", "policies 1 and 2 need a loaded selector");
+    gb::BatchPlan* pl = nullptr;
+    rc = (policy < 0) ? gb::batch_plan_create(probs, count, dtype, &pl, true)
+                      : gb::batch_plan_policy(probs, count, dtype, policy, &pl);
+    if (!rc && policy >= 0) pl->policy = policy;
+    *plan = pl;
+    return rc;
+}
+
+extern "C" int gb_batch_plan_policy(const void* plan)
+{
+    if (!plan) return gb::set_error(GB_ERR_ARG, "gb_batch_plan_policy", "null plan");
+    return static_cast<const gb::BatchPlan*>(plan)->policy;
+}

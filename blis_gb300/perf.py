@@ -292,14 +292,20 @@ def run_batch(out):
             from . import selector as S
             S.load_into_library()
             try:
-                plan2 = C.c_void_p()
-                _lib.check(L.gb_batch_plan_create(C.addressof(probs), 4096, dtype, C.byref(plan2)), "plan")
-                ms_s = _timer(lambda: _lib.check(L.gb_batch_plan_run(plan2, 1, st), "run"), reps=3, warmup=1)
-                L.gb_batch_plan_destroy(plan2)
+                pol = {}
+                for policy in (1, 2, -1):  # fixed policies, then the plan's own autotuning
+                    plan2 = C.c_void_p()
+                    _lib.check(L.gb_batch_plan_create_ex(C.addressof(probs), 4096, dtype, policy, C.byref(plan2)),
+                               "plan")
+                    ms_p = _timer(lambda: _lib.check(L.gb_batch_plan_run(plan2, 1, st), "run"), reps=3, warmup=1)
+                    pol[policy] = (ms_p, L.gb_batch_plan_policy(plan2))
+                    L.gb_batch_plan_destroy(plan2)
             finally:
                 L.gb_set_gemm_autoselect(0)
                 L.gb_selector_unload()
-            rec.update({"grouped_selected_ms": ms_s, "grouped_selected_tflops": flops / ms_s / 1e9})
+            rec.update({"policy1_selected_tiles_ms": pol[1][0], "policy2_selected_tiles_splitk_ms": pol[2][0],
+                        "autotuned_plan_ms": pol[-1][0], "autotuned_policy": pol[-1][1],
+                        "autotuned_tflops": flops / pol[-1][0] / 1e9})
         out.append(rec)
         L.gb_set_dgemm_mode(0, 8)
         del keep

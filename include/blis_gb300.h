@@ -363,6 +363,18 @@ int gb_batch_plan_create(const gb_gemm_problem_t* probs, gb_dim_t count, int dty
 int gb_batch_plan_run(void* plan, int use_graph, void* stream);
 int gb_batch_plan_destroy(void* plan);
 
+/* Configuration policy of a native (FP64 / FP32) plan: 0 = every problem on
+   the 128x128 engine; 1 = the 64x64 engine for the problems the selector
+   assigns to configs 1..5, without split-K; 2 = the selected configuration
+   including split-K (those problems run in a second grouped launch and a
+   grouped fold, in the same graph).  gb_batch_plan_create autotunes it when
+   a selector model is loaded and auto-selection is on: each policy runs on
+   the batch's shapes with scratch outputs and the fastest is kept (without a
+   model: policy 0).  One-shot gb_gemm_batch_dev / dgemm_batch_ calls use
+   policy 0.  gb_batch_plan_create_ex fixes the policy (-1 = autotune). */
+int gb_batch_plan_create_ex(const gb_gemm_problem_t* probs, gb_dim_t count, int dtype, int policy, void** plan);
+int gb_batch_plan_policy(const void* plan);
+
 /* Seeded matrix fill on the device, the counterpart of bli_randm (frame/util,
    value generators frame/include/bli_cast_macro_defs.h:465-525) with a
    counter-based generator: element (i, j) of the logical m x n matrix takes

@@ -190,30 +190,36 @@ def test_batch_with_selected_configs(gblib, dtype):
             cfgs.append(cfg.value)
         assert any(v >= 1 for v in cfgs)  # the grouped 64 x 64 launch is exercised
         c0 = [o.clone() for o in outs]
-        plan = C.c_void_p()
-        assert L.gb_batch_plan_create(C.addressof(descs), len(probs), code, C.byref(plan)) == 0
-        first = None
-        for rep in range(3):
-            for o, z in zip(outs, c0):
-                o.copy_(z)
-            torch.cuda.synchronize()  # the plan runs on the library's stream, not torch's
-            assert L.gb_batch_plan_run(plan, 1, None) == 0
-            assert L.gb_synchronize() == 0
-            got = [o.clone() for o in outs]
-            if first is None:
-                first = got
-            else:
-                assert all(torch.equal(x, y) for x, y in zip(first, got))
-        L.gb_batch_plan_destroy(plan)
+        results = {}
+        for policy in (1, 2, -1):  # fixed policies, then the plan's own autotuning
+            plan = C.c_void_p()
+            assert L.gb_batch_plan_create_ex(C.addressof(descs), len(probs), code, policy, C.byref(plan)) == 0
+            assert L.gb_batch_plan_policy(plan) in ((0, 1, 2) if policy < 0 else (policy,))
+            first = None
+            for rep in range(3):
+                for o, z in zip(outs, c0):
+                    o.copy_(z)
+                torch.cuda.synchronize()  # the plan runs on the library's stream, not torch's
+                assert L.gb_batch_plan_run(plan, 1, None) == 0
+                assert L.gb_synchronize() == 0
+                got = [o.clone() for o in outs]
+                if first is None:
+                    first = got
+                else:
+                    assert all(torch.equal(x, y) for x, y in zip(first, got))
+            L.gb_batch_plan_destroy(plan)
+            results[policy] = first
+        # the autotuning ran the batch on scratch outputs: C itself was only written by the runs above
     finally:
         gblib.gb_set_gemm_autoselect(0)
         gblib.gb_selector_unload()
     # componentwise: |C - C_ref| <= 2 k u (|alpha| |A| |B| + |beta| |C0|) (operands are not
     # normalized as in the testsuite, so its absolute residual does not apply)
     u = 2.0 ** -53 if dtype == np.float64 else 2.0 ** -24
-    for (ta, tb, m, n, k, a, b, c), g in zip(probs, first):
+    for (ta, tb, m, n, k, a, b, c), g1, g2 in zip(probs, results[1], results[2]):
         A = H.op(a, 8 if ta == "T" else 0).astype(np.float64)
         B = H.op(b, 8 if tb == "T" else 0).astype(np.float64)
         ref = 1.25 * (A @ B) - 0.5 * c.astype(np.float64)
         bound = 2 * (k + 2) * u * (1.25 * (np.abs(A) @ np.abs(B)) + 0.5 * np.abs(c.astype(np.float64)))
-        assert np.all(np.abs(g.cpu().numpy().T.astype(np.float64) - ref) <= bound)
+        for g in (g1, g2):
+            assert np.all(np.abs(g.cpu().numpy().T.astype(np.float64) - ref) <= bound)
