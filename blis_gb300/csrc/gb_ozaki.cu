@@ -67,7 +67,7 @@ struct OzLevel {
 struct OzGemmParams {
     static constexpr bool kDynamic = false;  // items b, b + grid, ... for CTA b
     static constexpr bool kRawAcc = false;   // chunks are converted to int32 and summed
-    int slices, nlevels, kb_total, tiles_m, tiles_n, chunk_kb;
+    int slices, nlevels, kb_total, tiles_m, tiles_n, chunk_kb, group_m;
     int64_t items, mpad, npad;
     int32_t* planes;  // [plane][npad][mpad]
     unsigned int* status;
@@ -188,13 +188,14 @@ __device__ __forceinline__ OzItem oz_decode(const OzGemmParams& p, int64_t it)
     const int64_t rem = it - lv.item_base;
     const int part = (int)(rem / tiles);
     const int64_t t = rem % tiles;
-    // grouped raster over tiles, OZ_GROUP_M tile rows per group: with ~150
-    // tiles in flight, 16 rows x ~9 columns minimise L2 misses for the
-    // 16 KB A / 32 KB B per k block (misses ~ 16/cols + 32/rows)
-    const int64_t group = t / (OZ_GROUP_M * (int64_t)p.tiles_n);
-    const int64_t first_m = group * OZ_GROUP_M;
-    const int64_t gm = (p.tiles_m - first_m < OZ_GROUP_M) ? p.tiles_m - first_m : OZ_GROUP_M;
-    const int64_t wi = t - group * OZ_GROUP_M * (int64_t)p.tiles_n;
+    // grouped raster over tiles, p.group_m tile rows per group (default
+    // OZ_GROUP_M = 16): the tiles in flight then share a few A and B panels
+    // in L2 instead of streaming whole rows of tiles
+    const int64_t G = p.group_m;
+    const int64_t group = t / (G * (int64_t)p.tiles_n);
+    const int64_t first_m = group * G;
+    const int64_t gm = (p.tiles_m - first_m < G) ? p.tiles_m - first_m : G;
+    const int64_t wi = t - group * G * (int64_t)p.tiles_n;
     w.tm = (int)(first_m + wi % gm);
     w.tn = (int)(wi / gm);
     w.kb0 = part * lv.kb_per_part;
@@ -1297,6 +1298,18 @@ int make_slice_map(CUtensorMap* map, const void* base, int64_t kpad, int64_t rpa
 
 inline int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
+// Tile rows per raster group of the slice GEMM (GB_OZAKI_GROUP_M, 1..64).
+int group_m_setting()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("GB_OZAKI_GROUP_M");
+        const int g = e ? atoi(e) : OZ_GROUP_M;
+        v = (g >= 1 && g <= 64) ? g : OZ_GROUP_M;
+    }
+    return v;
+}
+
 int chunk_kb_setting()
 {
     static int v = -1;
@@ -1537,6 +1550,7 @@ int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_
     }
     p.items = items;
     p.chunk_kb = chunk_kb_setting();
+    p.group_m = group_m_setting();
     p.mpad = mpad;
     p.npad = npad;
 
