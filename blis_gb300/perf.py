@@ -19,7 +19,8 @@ L2 where the workload allows:
                   per-problem launch loop, FP64 native, FP64 Ozaki (7
                   slices) and FP32
 
-Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl] [--batch-count N]
+Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl] [--batch-count N] [--small]
+(--small: 4096^3 GEMMs, 4096 x 2048 DTRSM, 2^25 vectors, 8192^2 GEMV, for ncu captures)
 """
 import argparse
 import ctypes as C
@@ -32,6 +33,7 @@ import numpy as np
 from . import _lib, dev
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SMALL = False  # --small: profiling sizes (inputs still larger than the 126 MB L2)
 
 
 def peaks():
@@ -74,26 +76,26 @@ def run_gemm(out):
     a, b, c = _mat(1024, 1024, seed=1), _mat(1024, 1024, seed=2), _mat(1024, 1024, seed=3)
     ms = _timer(lambda: dev.dgemm(0, 0, 1.0, a, b, 0.5, c), reps=20)
     out.append({"workload": "dgemm_1024", "form": "native_fp64", "ms": ms, "tflops": 2 * 1024 ** 3 / ms / 1e9})
-    n = 8192
+    n = 4096 if SMALL else 8192
     a, b, c = _mat(n, n, seed=4), _mat(n, n, seed=5), _mat(n, n, seed=6)
     ms = _timer(lambda: dev.dgemm(0, 0, 1.0, a, b, 0.0, c), reps=1, warmup=1)
-    out.append({"workload": "dgemm_8192", "form": "native_fp64", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
+    out.append({"workload": "dgemm_%d" % n, "form": "native_fp64", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
     ms = _timer(lambda: dev.dgemm_ozaki(0, 0, 1.0, a, b, 0.0, c, 7), reps=3)
-    out.append({"workload": "dgemm_8192", "form": "ozaki_s7", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9,
+    out.append({"workload": "dgemm_%d" % n, "form": "ozaki_s7", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9,
                 "bf16_frac_of_measured_peak": 28 * 2 * n ** 3 / ms / 1e9 / pk.get("bf16_tflops", 1900.0)})
     del a, b, c
     fa, fb, fc = (_mat(n, n, seed=s, dtype=torch.float32) for s in (7, 8, 9))
     ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
-    out.append({"workload": "sgemm_8192", "form": "ffma_fp32", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
+    out.append({"workload": "sgemm_%d" % n, "form": "ffma_fp32", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
 
 
 def run_sgemm(out):
     """SGEMM 8192^3 alone (the FP32 tile engine)."""
     import torch
-    n = 8192
+    n = 4096 if SMALL else 8192
     fa, fb, fc = (_mat(n, n, seed=s, dtype=torch.float32) for s in (7, 8, 9))
     ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
-    out.append({"workload": "sgemm_8192", "form": "ffma_fp32", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
+    out.append({"workload": "sgemm_%d" % n, "form": "ffma_fp32", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
 
 
 def run_bgemm(out):
@@ -102,7 +104,7 @@ def run_bgemm(out):
     first); against the measured cuBLAS bf16 peak."""
     import torch
     pk, kind = peaks()
-    n = 8192
+    n = 4096 if SMALL else 8192
     a = _mat(n, n, seed=41).to(torch.bfloat16)
     b = _mat(n, n, seed=42).to(torch.bfloat16)
     a, b = a.t().contiguous().t(), b.t().contiguous().t()  # column-major bf16
@@ -110,13 +112,13 @@ def run_bgemm(out):
     for ta, name in ((8, "TN_tma_in_place"), (0, "NN_packed")):
         ms = _timer(lambda: dev.bgemm(ta, 0, 1.0, a, b, 0.0, c, config=0), reps=5)
         tf = 2 * n ** 3 / ms / 1e9
-        out.append({"workload": "bgemm_8192", "form": name, "ms": ms, "tflops": tf,
+        out.append({"workload": "bgemm_%d" % n, "form": name, "ms": ms, "tflops": tf,
                     "frac_of_bf16_burst": tf / pk.get("bf16_tflops", 1900.0), "peak": "%s bf16_tflops" % kind})
 
 
 def run_trsm(out):
     import torch
-    m, n = 8192, 4096
+    m, n = (4096, 2048) if SMALL else (8192, 4096)
     L = _mat(m, m, seed=11)
     L.copy_(torch.tril(L))
     d = torch.arange(m, device="cuda")
@@ -128,7 +130,7 @@ def run_trsm(out):
         x = b0.clone()
         ms = _timer(lambda: (x.copy_(b0), dev.dtrsm(0, 0xC0, 0, 0, 1.0, L, x)), reps=1, warmup=1)
         copy_ms = _timer(lambda: x.copy_(b0), reps=3, warmup=1)
-        out.append({"workload": "dtrsm_8192x4096", "form": name, "ms": ms - copy_ms,
+        out.append({"workload": "dtrsm_%dx%d" % (m, n), "form": name, "ms": ms - copy_ms,
                     "tflops": flops / (ms - copy_ms) / 1e9})
     _lib.load().gb_set_dgemm_mode(0, 8)
 
@@ -173,25 +175,25 @@ def run_level12(out):
     import torch
     pk, kind = peaks()
     hbm = pk.get("hbm_gbs", 6800.0)
-    n = 1 << 28
+    n = 1 << (25 if SMALL else 28)
     x = torch.empty(n, dtype=torch.float64, device="cuda").uniform_(-1, 1)
     y = torch.empty(n, dtype=torch.float64, device="cuda").uniform_(-1, 1)
     rho = torch.zeros(1, dtype=torch.float64, device="cuda")
     ms = _timer(lambda: dev.daxpyv(0.5, x, y), reps=10)
     gbs = 24.0 * n / ms / 1e6
-    out.append({"workload": "daxpyv_2^28", "ms": ms, "gbs": gbs, "hbm_frac": gbs / hbm, "peak": "%s hbm_gbs" % kind})
+    out.append({"workload": "daxpyv_%d" % n, "ms": ms, "gbs": gbs, "hbm_frac": gbs / hbm, "peak": "%s hbm_gbs" % kind})
     ms = _timer(lambda: dev.ddotv(x, y, rho), reps=10)
     gbs = 16.0 * n / ms / 1e6
-    out.append({"workload": "ddotv_2^28", "ms": ms, "gbs": gbs, "hbm_frac": gbs / hbm, "peak": "%s hbm_gbs" % kind})
+    out.append({"workload": "ddotv_%d" % n, "ms": ms, "gbs": gbs, "hbm_frac": gbs / hbm, "peak": "%s hbm_gbs" % kind})
     del x, y
-    m = 32768
+    m = 8192 if SMALL else 32768
     a = _mat(m, m, seed=21)
     xv = torch.empty(m, dtype=torch.float64, device="cuda").uniform_(-1, 1)
     yv = torch.empty(m, dtype=torch.float64, device="cuda").uniform_(-1, 1)
     for t, name in ((0, "N"), (8, "T")):
         ms = _timer(lambda: dev.dgemv(t, 1.0, a, xv, 0.5, yv), reps=5)
         gbs = 8.0 * (m * m + m + 2 * m) / ms / 1e6
-        out.append({"workload": "dgemv_32768_%s" % name, "ms": ms, "gbs": gbs, "hbm_frac": gbs / hbm,
+        out.append({"workload": "dgemv_%d_%s" % (m, name), "ms": ms, "gbs": gbs, "hbm_frac": gbs / hbm,
                     "peak": "%s hbm_gbs" % kind})
 
 
@@ -321,9 +323,11 @@ def main():
     ap.add_argument("--only", default="")
     ap.add_argument("--json")
     ap.add_argument("--batch-count", type=int, default=4096, help="problems of the batch_ozaki suite")
+    ap.add_argument("--small", action="store_true", help="profiling sizes (workload names keep the full size)")
     a = ap.parse_args()
-    global BATCH_COUNT
+    global BATCH_COUNT, SMALL
     BATCH_COUNT = a.batch_count
+    SMALL = a.small
     torch.cuda.set_device(0)
     _lib.check(_lib.load().gb_init(0), "gb_init")
     names = [s for s in a.only.split(",") if s] or list(SUITES)
