@@ -6,9 +6,9 @@
 // its macro-kernel walks MR-row panels serially (bli_trsm_ll_ker_var2.c).
 // On a GPU the serial part must stay small, so the solve is recursive:
 //     X1 = inv(L11) B1;  B2 -= L21 X1;  X2 = inv(L22) B2
-// down to diagonal blocks of at most 64 rows, which one kernel solves with
-// one thread per right-hand side on a shared-memory panel (FP64, diagonal
-// pre-inverted as with BLIS_ENABLE_TRSM_PREINVERSION,
+// down to diagonal blocks of at most 64 rows, which one kernel solves by
+// substitution on a shared-memory panel, 8 lanes per right-hand side (FP64,
+// diagonal pre-inverted as with BLIS_ENABLE_TRSM_PREINVERSION,
 // ref_kernels/3/bli_trsm_ref.c:110-134).
 // Nearly all m^2 n flops land in the off-diagonal gemm updates, which run
 // on the native FP64 kernel or, in the precision form, on the Ozaki kernel.
@@ -24,72 +24,73 @@ namespace {
 constexpr int TRSM_NB = 64;
 
 // Solves op(A11) X = B1 in place for an nb x nb diagonal block.
-// op(A)(i, l) = a[i*ars + l*acs]; B(i, j) = b[i*brs + j*bcs].  A CTA of
-// TRSM_COLS threads owns TRSM_COLS right-hand sides: the triangle and the
-// CTA's nb x TRSM_COLS panel of B are staged in shared memory (coalesced
-// along B's contiguous direction), each thread runs forward / backward
-// substitution on its column in shared memory with the pre-inverted
-// diagonal, and the panel is written back the same way.
-constexpr int TRSM_COLS = 64;
+// op(A)(i, l) = a[i*ars + l*acs]; B(i, j) = b[i*brs + j*bcs].  A CTA owns
+// TRSM_COLS right-hand sides: the triangle and the CTA's nb x TRSM_COLS panel
+// of B are staged in shared memory (coalesced along B's contiguous
+// direction).  Substitution keeps its row order, but each row's dot product
+// with the solved part is split over TRSM_LANES lanes of a warp (lane g takes
+// l = g, g + 8, ...) and combined with shuffles, so the dependent chain per
+// row is a few FMAs instead of up to 63; the diagonal is pre-inverted.
+constexpr int TRSM_COLS = 32, TRSM_LANES = 8, TRSM_THREADS = TRSM_COLS * TRSM_LANES;
 
-__global__ void __launch_bounds__(TRSM_COLS) trsm_diag_kernel(int nb, int lower, int unit,
-                                                              const double* __restrict__ a, int64_t ars,
-                                                              int64_t acs, double* __restrict__ b, int64_t brs,
-                                                              int64_t bcs, int64_t ncols)
+__global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int lower, int unit,
+                                                                 const double* __restrict__ a, int64_t ars,
+                                                                 int64_t acs, double* __restrict__ b,
+                                                                 int64_t brs, int64_t bcs, int64_t ncols)
 {
     extern __shared__ double trsm_smem[];
-    double* L = trsm_smem;                         // [TRSM_NB][TRSM_NB + 1]
-    double* dinv = L + TRSM_NB * (TRSM_NB + 1);    // [TRSM_NB]
-    double* X = dinv + TRSM_NB;                    // [TRSM_NB][TRSM_COLS + 1]
     constexpr int LL = TRSM_NB + 1, LX = TRSM_COLS + 1;
+    double* L = trsm_smem;                 // [TRSM_NB][LL]
+    double* dinv = L + TRSM_NB * LL;       // [TRSM_NB]
+    double* X = dinv + TRSM_NB;            // [TRSM_NB][LX]
     const int t = threadIdx.x;
     const int64_t j0 = (int64_t)blockIdx.x * TRSM_COLS;
     const int cols = (ncols - j0 < TRSM_COLS) ? (int)(ncols - j0) : TRSM_COLS;
-    for (int e = t; e < nb * nb; e += TRSM_COLS) {
+    for (int e = t; e < nb * nb; e += TRSM_THREADS) {
         const int i = e % nb, l = e / nb;
         const bool in_tri = lower ? (l <= i) : (l >= i);
         L[i * LL + l] = in_tri ? a[i * ars + l * acs] : 0.0;
     }
     const bool rows_fast = (brs == 1);
-    for (int e = t; e < nb * TRSM_COLS; e += TRSM_COLS) {
+    for (int e = t; e < nb * TRSM_COLS; e += TRSM_THREADS) {
         const int i = rows_fast ? e % nb : e / TRSM_COLS, c = rows_fast ? e / nb : e % TRSM_COLS;
-        if (c < cols) X[i * LX + c] = b[i * brs + (j0 + c) * bcs];
+        X[i * LX + c] = (c < cols) ? b[i * brs + (j0 + c) * bcs] : 0.0;
     }
     __syncthreads();
     if (t < nb) dinv[t] = unit ? 1.0 : 1.0 / L[t * LL + t];
     __syncthreads();
-    if (t < cols) {
+    const int c = t / TRSM_LANES, g = t % TRSM_LANES;  // the 8 lanes of a column share a warp
+    for (int step = 0; step < nb; ++step) {
+        const int i = lower ? step : nb - 1 - step;
+        double part = 0.0;
         if (lower) {
-            for (int i = 0; i < nb; ++i) {
-                double s = X[i * LX + t];
-                for (int l = 0; l < i; ++l) s = fma(-L[i * LL + l], X[l * LX + t], s);
-                X[i * LX + t] = s * dinv[i];
-            }
+            for (int l = g; l < i; l += TRSM_LANES) part = fma(L[i * LL + l], X[l * LX + c], part);
         } else {
-            for (int i = nb - 1; i >= 0; --i) {
-                double s = X[i * LX + t];
-                for (int l = i + 1; l < nb; ++l) s = fma(-L[i * LL + l], X[l * LX + t], s);
-                X[i * LX + t] = s * dinv[i];
-            }
+            for (int l = i + 1 + g; l < nb; l += TRSM_LANES) part = fma(L[i * LL + l], X[l * LX + c], part);
         }
+#pragma unroll
+        for (int off = TRSM_LANES / 2; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+        if (g == 0) X[i * LX + c] = (X[i * LX + c] - part) * dinv[i];
+        __syncwarp();
     }
     __syncthreads();
-    for (int e = t; e < nb * TRSM_COLS; e += TRSM_COLS) {
-        const int i = rows_fast ? e % nb : e / TRSM_COLS, c = rows_fast ? e / nb : e % TRSM_COLS;
-        if (c < cols) b[i * brs + (j0 + c) * bcs] = X[i * LX + c];
+    for (int e = t; e < nb * TRSM_COLS; e += TRSM_THREADS) {
+        const int i = rows_fast ? e % nb : e / TRSM_COLS, cc = rows_fast ? e / nb : e % TRSM_COLS;
+        if (cc < cols) b[i * brs + (j0 + cc) * bcs] = X[i * LX + cc];
     }
 }
 
 constexpr size_t TRSM_SMEM = sizeof(double) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB + TRSM_NB * (TRSM_COLS + 1));
 
 // Multiply-adds below which a TRSM update runs natively in the precision form
-// (GB_TRSM_OZAKI_MIN_FMA; default 2^27).
+// (GB_TRSM_OZAKI_MIN_FMA; default 0: measured on GB300, even the 64 x n x 64
+// updates at the bottom of the recursion are faster in the Ozaki form).
 double trsm_ozaki_min_fma()
 {
     static double v = -1.0;
     if (v < 0.0) {
         const char* e = getenv("GB_TRSM_OZAKI_MIN_FMA");
-        v = e ? atof(e) : 134217728.0;
+        v = e ? atof(e) : 0.0;
         if (v < 0.0) v = 0.0;
     }
     return v;
@@ -111,8 +112,6 @@ int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t cco
     const double* ap = t.a + r0 * t.ars + c0 * t.acs;
     const double* xp = t.b + c0 * t.brs;
     double* bp = t.b + r0 * t.brs;
-    // small updates (deep in the recursion) cost less on the FP64 pipe than
-    // the Ozaki form's fixed split/recombine launches
     if (t.slices > 0 && (double)rcount * (double)ccount * (double)t.n >= trsm_ozaki_min_fma())
         return dgemm_ozaki(rcount, t.n, ccount, -1.0, ap, t.ars, t.acs, xp, t.brs, t.bcs, 1.0, bp,
                            t.brs, t.bcs, t.slices, t.s);
@@ -133,7 +132,7 @@ int solve(const TrsmCtx& t, int64_t r0, int64_t mm)
         const int64_t blocks = (t.n + TRSM_COLS - 1) / TRSM_COLS;
         if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "dtrsm", "too many right-hand sides");
         LaunchScope ls("trsm_diag", t.s);
-        trsm_diag_kernel<<<(unsigned)blocks, TRSM_COLS, TRSM_SMEM, t.s>>>((int)mm, t.lower, t.unit,
+        trsm_diag_kernel<<<(unsigned)blocks, TRSM_THREADS, TRSM_SMEM, t.s>>>((int)mm, t.lower, t.unit,
                                                                          t.a + r0 * t.ars + r0 * t.acs, t.ars,
                                                                          t.acs, t.b + r0 * t.brs, t.brs, t.bcs, t.n);
         return check_cuda(cudaGetLastError(), "trsm_diag");
