@@ -46,12 +46,14 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int low
     const int t = threadIdx.x;
     const int64_t j0 = (int64_t)blockIdx.x * TRSM_COLS;
     const int cols = (ncols - j0 < TRSM_COLS) ? (int)(ncols - j0) : TRSM_COLS;
-    for (int e = t; e < nb * nb; e += TRSM_THREADS) {
+#pragma unroll 8
+    for (int e = t; e < nb * nb; e += TRSM_THREADS) {  // up to 16 loads per thread, kept in flight
         const int i = e % nb, l = e / nb;
         const bool in_tri = lower ? (l <= i) : (l >= i);
         L[i * LL + l] = in_tri ? a[i * ars + l * acs] : 0.0;
     }
     const bool rows_fast = (brs == 1);
+#pragma unroll 8
     for (int e = t; e < nb * TRSM_COLS; e += TRSM_THREADS) {
         const int i = rows_fast ? e % nb : e / TRSM_COLS, c = rows_fast ? e / nb : e % TRSM_COLS;
         X[i * LX + c] = (c < cols) ? b[i * brs + (j0 + c) * bcs] : 0.0;
@@ -64,8 +66,10 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int low
         const int i = lower ? step : nb - 1 - step;
         double part = 0.0;
         if (lower) {
+#pragma unroll 4
             for (int l = g; l < i; l += TRSM_LANES) part = fma(L[i * LL + l], X[l * LX + c], part);
         } else {
+#pragma unroll 4
             for (int l = i + 1 + g; l < nb; l += TRSM_LANES) part = fma(L[i * LL + l], X[l * LX + c], part);
         }
 #pragma unroll
@@ -74,6 +78,7 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int low
         __syncwarp();
     }
     __syncthreads();
+#pragma unroll 8
     for (int e = t; e < nb * TRSM_COLS; e += TRSM_THREADS) {
         const int i = rows_fast ? e % nb : e / TRSM_COLS, cc = rows_fast ? e / nb : e % TRSM_COLS;
         if (cc < cols) b[i * brs + (j0 + cc) * bcs] = X[i * LX + cc];
