@@ -31,7 +31,7 @@ constexpr int TRSM_NB = 64;
 // with the solved part is split over TRSM_LANES lanes of a warp (lane g takes
 // l = g, g + 8, ...) and combined with shuffles, so the dependent chain per
 // row is a few FMAs instead of up to 63; the diagonal is pre-inverted.
-constexpr int TRSM_COLS = 32, TRSM_LANES = 8, TRSM_THREADS = TRSM_COLS * TRSM_LANES;
+constexpr int TRSM_COLS = 16, TRSM_LANES = 8, TRSM_THREADS = TRSM_COLS * TRSM_LANES;
 
 __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int lower, int unit,
                                                                  const double* __restrict__ a, int64_t ars,
