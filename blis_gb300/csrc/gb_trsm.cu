@@ -7,8 +7,8 @@
 // On a GPU the serial part must stay small, so the solve is recursive:
 //     X1 = inv(L11) B1;  B2 -= L21 X1;  X2 = inv(L22) B2
 // down to diagonal blocks of at most 64 rows, which one kernel solves by
-// substitution on a shared-memory panel, 8 lanes per right-hand side (FP64,
-// diagonal pre-inverted as with BLIS_ENABLE_TRSM_PREINVERSION,
+// substitution on a shared-memory panel, one thread per right-hand side
+// (FP64, diagonal pre-inverted as with BLIS_ENABLE_TRSM_PREINVERSION,
 // ref_kernels/3/bli_trsm_ref.c:110-134).
 // Nearly all m^2 n flops land in the off-diagonal gemm updates, which run
 // on the native FP64 kernel or, in the precision form, on the Ozaki kernel.
@@ -25,13 +25,14 @@ constexpr int TRSM_NB = 64;
 
 // Solves op(A11) X = B1 in place for an nb x nb diagonal block.
 // op(A)(i, l) = a[i*ars + l*acs]; B(i, j) = b[i*brs + j*bcs].  A CTA owns
-// TRSM_COLS right-hand sides: the triangle and the CTA's nb x TRSM_COLS panel
-// of B are staged in shared memory (coalesced along B's contiguous
-// direction).  Substitution keeps its row order, but each row's dot product
-// with the solved part is split over TRSM_LANES lanes of a warp (lane g takes
-// l = g, g + 8, ...) and combined with shuffles, so the dependent chain per
-// row is a few FMAs instead of up to 63; the diagonal is pre-inverted.
-constexpr int TRSM_COLS = 16, TRSM_LANES = 8, TRSM_THREADS = TRSM_COLS * TRSM_LANES;
+// TRSM_COLS right-hand sides, one per thread: the triangle and the CTA's
+// nb x TRSM_COLS panel of B are staged in shared memory (coalesced along B's
+// contiguous direction), each thread runs forward / backward substitution on
+// its column with four independent partial sums per row (a dependent chain
+// of i/4 FMAs instead of i) and the pre-inverted diagonal, and the panel is
+// written back.  One thread per column issues the fewest FP64 instructions,
+// which is what bounds this kernel on GB300's narrow FP64 pipe.
+constexpr int TRSM_COLS = 64, TRSM_THREADS = TRSM_COLS;
 
 __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int lower, int unit,
                                                                  const double* __restrict__ a, int64_t ars,
@@ -47,7 +48,7 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int low
     const int64_t j0 = (int64_t)blockIdx.x * TRSM_COLS;
     const int cols = (ncols - j0 < TRSM_COLS) ? (int)(ncols - j0) : TRSM_COLS;
 #pragma unroll 8
-    for (int e = t; e < nb * nb; e += TRSM_THREADS) {  // up to 16 loads per thread, kept in flight
+    for (int e = t; e < nb * nb; e += TRSM_THREADS) {
         const int i = e % nb, l = e / nb;
         const bool in_tri = lower ? (l <= i) : (l >= i);
         L[i * LL + l] = in_tri ? a[i * ars + l * acs] : 0.0;
@@ -61,21 +62,19 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int low
     __syncthreads();
     if (t < nb) dinv[t] = unit ? 1.0 : 1.0 / L[t * LL + t];
     __syncthreads();
-    const int c = t / TRSM_LANES, g = t % TRSM_LANES;  // the 8 lanes of a column share a warp
     for (int step = 0; step < nb; ++step) {
         const int i = lower ? step : nb - 1 - step;
-        double part = 0.0;
-        if (lower) {
-#pragma unroll 4
-            for (int l = g; l < i; l += TRSM_LANES) part = fma(L[i * LL + l], X[l * LX + c], part);
-        } else {
-#pragma unroll 4
-            for (int l = i + 1 + g; l < nb; l += TRSM_LANES) part = fma(L[i * LL + l], X[l * LX + c], part);
+        const int l0 = lower ? 0 : i + 1, l1 = lower ? i : nb;
+        double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
+        int l = l0;
+        for (; l + 3 < l1; l += 4) {
+            p0 = fma(L[i * LL + l], X[l * LX + t], p0);
+            p1 = fma(L[i * LL + l + 1], X[(l + 1) * LX + t], p1);
+            p2 = fma(L[i * LL + l + 2], X[(l + 2) * LX + t], p2);
+            p3 = fma(L[i * LL + l + 3], X[(l + 3) * LX + t], p3);
         }
-#pragma unroll
-        for (int off = TRSM_LANES / 2; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-        if (g == 0) X[i * LX + c] = (X[i * LX + c] - part) * dinv[i];
-        __syncwarp();
+        for (; l < l1; ++l) p0 = fma(L[i * LL + l], X[l * LX + t], p0);
+        X[i * LX + t] = (X[i * LX + t] - ((p0 + p1) + (p2 + p3))) * dinv[i];
     }
     __syncthreads();
 #pragma unroll 8
