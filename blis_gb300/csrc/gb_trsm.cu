@@ -8,7 +8,8 @@
 //     X1 = inv(L11) B1;  B2 -= L21 X1;  X2 = inv(L22) B2
 // down to diagonal blocks of at most 64 rows, which one kernel solves by
 // substitution on a shared-memory panel, one thread per right-hand side
-// (FP64, diagonal pre-inverted as with BLIS_ENABLE_TRSM_PREINVERSION,
+// (or 8 lanes per right-hand side when there are few of them; FP64,
+// diagonal pre-inverted as with BLIS_ENABLE_TRSM_PREINVERSION,
 // ref_kernels/3/bli_trsm_ref.c:110-134).
 // Nearly all m^2 n flops land in the off-diagonal gemm updates, which run
 // on the native FP64 kernel or, in the precision form, on the Ozaki kernel.
@@ -84,6 +85,62 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int low
     }
 }
 
+// The same solve with 8 lanes per right-hand side, for few right-hand sides
+// (fewer than one 64-column CTA per SM): each row's dot product is split over
+// the lanes (lane g takes l = g, g + 8, ...) and combined with shuffles.  It
+// spends more FP64 issue slots per column but keeps more SMs busy.
+constexpr int TRSM_SCOLS = 32, TRSM_LANES = 8, TRSM_STHREADS = TRSM_SCOLS * TRSM_LANES;
+
+__global__ void __launch_bounds__(TRSM_STHREADS) trsm_diag_split_kernel(int nb, int lower, int unit,
+                                                                        const double* __restrict__ a, int64_t ars,
+                                                                        int64_t acs, double* __restrict__ b,
+                                                                        int64_t brs, int64_t bcs, int64_t ncols)
+{
+    extern __shared__ double trsm_smem[];
+    constexpr int LL = TRSM_NB + 1, LX = TRSM_SCOLS + 1;
+    double* L = trsm_smem;
+    double* dinv = L + TRSM_NB * LL;
+    double* X = dinv + TRSM_NB;
+    const int t = threadIdx.x;
+    const int64_t j0 = (int64_t)blockIdx.x * TRSM_SCOLS;
+    const int cols = (ncols - j0 < TRSM_SCOLS) ? (int)(ncols - j0) : TRSM_SCOLS;
+#pragma unroll 8
+    for (int e = t; e < nb * nb; e += TRSM_STHREADS) {
+        const int i = e % nb, l = e / nb;
+        const bool in_tri = lower ? (l <= i) : (l >= i);
+        L[i * LL + l] = in_tri ? a[i * ars + l * acs] : 0.0;
+    }
+    const bool rows_fast = (brs == 1);
+#pragma unroll 8
+    for (int e = t; e < nb * TRSM_SCOLS; e += TRSM_STHREADS) {
+        const int i = rows_fast ? e % nb : e / TRSM_SCOLS, c = rows_fast ? e / nb : e % TRSM_SCOLS;
+        X[i * LX + c] = (c < cols) ? b[i * brs + (j0 + c) * bcs] : 0.0;
+    }
+    __syncthreads();
+    if (t < nb) dinv[t] = unit ? 1.0 : 1.0 / L[t * LL + t];
+    __syncthreads();
+    const int c = t / TRSM_LANES, g = t % TRSM_LANES;  // the 8 lanes of a column share a warp
+    for (int step = 0; step < nb; ++step) {
+        const int i = lower ? step : nb - 1 - step;
+        const int l0 = lower ? 0 : i + 1, l1 = lower ? i : nb;
+        double part = 0.0;
+#pragma unroll 4
+        for (int l = l0 + g; l < l1; l += TRSM_LANES) part = fma(L[i * LL + l], X[l * LX + c], part);
+#pragma unroll
+        for (int off = TRSM_LANES / 2; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+        if (g == 0) X[i * LX + c] = (X[i * LX + c] - part) * dinv[i];
+        __syncwarp();
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int e = t; e < nb * TRSM_SCOLS; e += TRSM_STHREADS) {
+        const int i = rows_fast ? e % nb : e / TRSM_SCOLS, cc = rows_fast ? e / nb : e % TRSM_SCOLS;
+        if (cc < cols) b[i * brs + (j0 + cc) * bcs] = X[i * LX + cc];
+    }
+}
+
+constexpr size_t TRSM_SSMEM = sizeof(double) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB + TRSM_NB * (TRSM_SCOLS + 1));
+
 constexpr size_t TRSM_SMEM = sizeof(double) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB + TRSM_NB * (TRSM_COLS + 1));
 
 // Multiply-adds below which a TRSM update runs natively in the precision form
@@ -130,15 +187,27 @@ int solve(const TrsmCtx& t, int64_t r0, int64_t mm)
         if (!attr) {
             int rc0 = check_cuda(cudaFuncSetAttribute(trsm_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                       (int)TRSM_SMEM), "trsm smem attr");
+            if (!rc0)
+                rc0 = check_cuda(cudaFuncSetAttribute(trsm_diag_split_kernel,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRSM_SSMEM),
+                                 "trsm smem attr");
             if (rc0) return rc0;
             attr = true;
         }
+        const int sms = sm_count() > 0 ? sm_count() : 148;
         const int64_t blocks = (t.n + TRSM_COLS - 1) / TRSM_COLS;
-        if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "dtrsm", "too many right-hand sides");
         LaunchScope ls("trsm_diag", t.s);
-        trsm_diag_kernel<<<(unsigned)blocks, TRSM_THREADS, TRSM_SMEM, t.s>>>((int)mm, t.lower, t.unit,
-                                                                         t.a + r0 * t.ars + r0 * t.acs, t.ars,
-                                                                         t.acs, t.b + r0 * t.brs, t.brs, t.bcs, t.n);
+        if (blocks >= sms) {
+            if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "dtrsm", "too many right-hand sides");
+            trsm_diag_kernel<<<(unsigned)blocks, TRSM_THREADS, TRSM_SMEM, t.s>>>(
+                (int)mm, t.lower, t.unit, t.a + r0 * t.ars + r0 * t.acs, t.ars, t.acs, t.b + r0 * t.brs, t.brs,
+                t.bcs, t.n);
+        } else {
+            const int64_t sblocks = (t.n + TRSM_SCOLS - 1) / TRSM_SCOLS;
+            trsm_diag_split_kernel<<<(unsigned)sblocks, TRSM_STHREADS, TRSM_SSMEM, t.s>>>(
+                (int)mm, t.lower, t.unit, t.a + r0 * t.ars + r0 * t.acs, t.ars, t.acs, t.b + r0 * t.brs, t.brs,
+                t.bcs, t.n);
+        }
         return check_cuda(cudaGetLastError(), "trsm_diag");
     }
     // split on a multiple of the diagonal block size

@@ -223,3 +223,16 @@ def test_batch_with_selected_configs(gblib, dtype):
         bound = 2 * (k + 2) * u * (1.25 * (np.abs(A) @ np.abs(B)) + 0.5 * np.abs(c.astype(np.float64)))
         for g in (g1, g2):
             assert np.all(np.abs(g.cpu().numpy().T.astype(np.float64) - ref) <= bound)
+
+
+@pytest.mark.parametrize("uplo,trans", [("L", "N"), ("U", "N"), ("L", "T")])
+def test_dtrsm_many_right_hand_sides(uplo, trans):
+    # n large enough for the one-thread-per-column diagonal kernel (at least one 64-column CTA per SM)
+    m, n = 192, 10000
+    a = np.asfortranarray(H.normalize(po.uniform((m, m), 14)) + 2.0 * np.eye(m))
+    b0 = H.normalize(po.uniform((m, n), 15))
+    x = np.asfortranarray(b0.copy())
+    blas.dtrsm("L", uplo, trans, "N", m, n, 1.5, a, m, x, m)
+    tri = _tri(a, uplo, "N")
+    r = H.trsm_residual(0, 1.5, tri.T if trans == "T" else tri, b0, x)
+    assert r < 1e-12
