@@ -20,7 +20,7 @@ L2 where the workload allows:
                   slices) and FP32
 
 Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl] [--batch-count N] [--small]
-(--small: 4096^3 GEMMs, 4096 x 2048 DTRSM, 2^25 vectors, 8192^2 GEMV, for ncu captures)
+(--small: 4096^3 GEMMs, 2048 x 10240 DTRSM, 2^25 vectors, 8192^2 GEMV, for ncu captures)
 """
 import argparse
 import ctypes as C
@@ -118,7 +118,7 @@ def run_bgemm(out):
 
 def run_trsm(out):
     import torch
-    m, n = (4096, 2048) if SMALL else (8192, 4096)
+    m, n = (2048, 10240) if SMALL else (8192, 4096)  # small: enough columns for the one-thread diagonal kernel
     L = _mat(m, m, seed=11)
     L.copy_(torch.tril(L))
     d = torch.arange(m, device="cuda")
