@@ -7,9 +7,8 @@
 // On a GPU the serial part must stay small, so the solve is recursive:
 //     X1 = inv(L11) B1;  B2 -= L21 X1;  X2 = inv(L22) B2
 // down to diagonal blocks of at most 64 rows, which one kernel solves by
-// substitution on a shared-memory panel, one thread per right-hand side
-// (or 8 lanes per right-hand side when there are few of them; FP64,
-// diagonal pre-inverted as with BLIS_ENABLE_TRSM_PREINVERSION,
+// right-looking substitution in registers with 1 to 8 lanes per right-hand
+// side (FP64, diagonal pre-inverted as with BLIS_ENABLE_TRSM_PREINVERSION,
 // ref_kernels/3/bli_trsm_ref.c:110-134).
 // Nearly all m^2 n flops land in the off-diagonal gemm updates, which run
 // on the native FP64 kernel or, in the precision form, on the Ozaki kernel.
@@ -25,123 +24,106 @@ namespace {
 constexpr int TRSM_NB = 64;
 
 // Solves op(A11) X = B1 in place for an nb x nb diagonal block.
-// op(A)(i, l) = a[i*ars + l*acs]; B(i, j) = b[i*brs + j*bcs].  A CTA owns
-// TRSM_COLS right-hand sides, one per thread: the triangle and the CTA's
-// nb x TRSM_COLS panel of B are staged in shared memory (coalesced along B's
-// contiguous direction), each thread runs forward / backward substitution on
-// its column with four independent partial sums per row (a dependent chain
-// of i/4 FMAs instead of i) and the pre-inverted diagonal, and the panel is
-// written back.  One thread per column issues the fewest FP64 instructions,
-// which is what bounds this kernel on GB300's narrow FP64 pipe.
-constexpr int TRSM_COLS = 64, TRSM_THREADS = TRSM_COLS;
+// op(A)(i, l) = a[i*ars + l*acs]; B(i, j) = b[i*brs + j*bcs].  A CTA of
+// TRSM_THREADS threads owns TRSM_THREADS / LANES right-hand sides.  The
+// triangle (padded to 64 x 64 with identity rows) and the CTA's panel of B
+// are staged in shared memory, coalesced along B's contiguous direction;
+// each lane then holds 64 / LANES rows of its column in registers (row
+// r = q * LANES + g in x[q] of lane g) and runs right-looking substitution:
+// x_i = b_i * inv(a_ii) from the lane that owns row i (shuffled to the
+// column's other lanes), then b_r -= a_ri x_i for every later row r.  Every
+// FP64 instruction but one multiply per row is an FMA of the triangle, so
+// the FP64 pipe (GB300's narrowest) does no reduction work, and one row's
+// updates are independent of each other.  LANES trades those instructions
+// (the per-row multiply is repeated on every lane) against how many warps
+// there are to fill the SM sub-partitions; the host picks it from a cost
+// model.  Both loops are unrolled, so every register index is a constant.
+constexpr int TRSM_THREADS = 128;
 
-__global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int lower, int unit,
-                                                                 const double* __restrict__ a, int64_t ars,
-                                                                 int64_t acs, double* __restrict__ b,
+template <int LANES, bool LOWER>
+__global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int unit, const double* __restrict__ a,
+                                                                 int64_t ars, int64_t acs, double* __restrict__ b,
                                                                  int64_t brs, int64_t bcs, int64_t ncols)
 {
+    constexpr int COLS = TRSM_THREADS / LANES, R = TRSM_NB / LANES, LL = TRSM_NB + 1, LX = COLS + 1;
     extern __shared__ double trsm_smem[];
-    constexpr int LL = TRSM_NB + 1, LX = TRSM_COLS + 1;
     double* L = trsm_smem;                 // [TRSM_NB][LL]
     double* dinv = L + TRSM_NB * LL;       // [TRSM_NB]
     double* X = dinv + TRSM_NB;            // [TRSM_NB][LX]
     const int t = threadIdx.x;
-    const int64_t j0 = (int64_t)blockIdx.x * TRSM_COLS;
-    const int cols = (ncols - j0 < TRSM_COLS) ? (int)(ncols - j0) : TRSM_COLS;
+    const int64_t j0 = (int64_t)blockIdx.x * COLS;
+    const int cols = (ncols - j0 < COLS) ? (int)(ncols - j0) : COLS;
 #pragma unroll 8
-    for (int e = t; e < nb * nb; e += TRSM_THREADS) {
-        const int i = e % nb, l = e / nb;
-        const bool in_tri = lower ? (l <= i) : (l >= i);
-        L[i * LL + l] = in_tri ? a[i * ars + l * acs] : 0.0;
+    for (int e = t; e < TRSM_NB * TRSM_NB; e += TRSM_THREADS) {
+        const int i = e % TRSM_NB, l = e / TRSM_NB;
+        const bool in_tri = LOWER ? (l < i) : (l > i);
+        double v = (i == l) ? 1.0 : 0.0;
+        if (i < nb && l < nb && (in_tri || i == l)) v = a[i * ars + l * acs];
+        L[i * LL + l] = v;
     }
     const bool rows_fast = (brs == 1);
 #pragma unroll 8
-    for (int e = t; e < nb * TRSM_COLS; e += TRSM_THREADS) {
-        const int i = rows_fast ? e % nb : e / TRSM_COLS, c = rows_fast ? e / nb : e % TRSM_COLS;
-        X[i * LX + c] = (c < cols) ? b[i * brs + (j0 + c) * bcs] : 0.0;
+    for (int e = t; e < TRSM_NB * COLS; e += TRSM_THREADS) {
+        const int i = rows_fast ? e % TRSM_NB : e / COLS, c = rows_fast ? e / TRSM_NB : e % COLS;
+        X[i * LX + c] = (c < cols && i < nb) ? b[i * brs + (j0 + c) * bcs] : 0.0;
     }
     __syncthreads();
-    if (t < nb) dinv[t] = unit ? 1.0 : 1.0 / L[t * LL + t];
+    if (t < TRSM_NB) dinv[t] = (unit || t >= nb) ? 1.0 : 1.0 / L[t * LL + t];
     __syncthreads();
-    for (int step = 0; step < nb; ++step) {
-        const int i = lower ? step : nb - 1 - step;
-        const int l0 = lower ? 0 : i + 1, l1 = lower ? i : nb;
-        double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
-        int l = l0;
-        for (; l + 3 < l1; l += 4) {
-            p0 = fma(L[i * LL + l], X[l * LX + t], p0);
-            p1 = fma(L[i * LL + l + 1], X[(l + 1) * LX + t], p1);
-            p2 = fma(L[i * LL + l + 2], X[(l + 2) * LX + t], p2);
-            p3 = fma(L[i * LL + l + 3], X[(l + 3) * LX + t], p3);
-        }
-        for (; l < l1; ++l) p0 = fma(L[i * LL + l], X[l * LX + t], p0);
-        X[i * LX + t] = (X[i * LX + t] - ((p0 + p1) + (p2 + p3))) * dinv[i];
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int e = t; e < nb * TRSM_COLS; e += TRSM_THREADS) {
-        const int i = rows_fast ? e % nb : e / TRSM_COLS, cc = rows_fast ? e / nb : e % TRSM_COLS;
-        if (cc < cols) b[i * brs + (j0 + cc) * bcs] = X[i * LX + cc];
-    }
-}
-
-// The same solve with 8 lanes per right-hand side, for few right-hand sides
-// (fewer than one 64-column CTA per SM): each row's dot product is split over
-// the lanes (lane g takes l = g, g + 8, ...) and combined with shuffles.  It
-// spends more FP64 issue slots per column but keeps more SMs busy.
-constexpr int TRSM_SCOLS = 32, TRSM_LANES = 8, TRSM_STHREADS = TRSM_SCOLS * TRSM_LANES;
-
-__global__ void __launch_bounds__(TRSM_STHREADS) trsm_diag_split_kernel(int nb, int lower, int unit,
-                                                                        const double* __restrict__ a, int64_t ars,
-                                                                        int64_t acs, double* __restrict__ b,
-                                                                        int64_t brs, int64_t bcs, int64_t ncols)
-{
-    extern __shared__ double trsm_smem[];
-    constexpr int LL = TRSM_NB + 1, LX = TRSM_SCOLS + 1;
-    double* L = trsm_smem;
-    double* dinv = L + TRSM_NB * LL;
-    double* X = dinv + TRSM_NB;
-    const int t = threadIdx.x;
-    const int64_t j0 = (int64_t)blockIdx.x * TRSM_SCOLS;
-    const int cols = (ncols - j0 < TRSM_SCOLS) ? (int)(ncols - j0) : TRSM_SCOLS;
-#pragma unroll 8
-    for (int e = t; e < nb * nb; e += TRSM_STHREADS) {
-        const int i = e % nb, l = e / nb;
-        const bool in_tri = lower ? (l <= i) : (l >= i);
-        L[i * LL + l] = in_tri ? a[i * ars + l * acs] : 0.0;
-    }
-    const bool rows_fast = (brs == 1);
-#pragma unroll 8
-    for (int e = t; e < nb * TRSM_SCOLS; e += TRSM_STHREADS) {
-        const int i = rows_fast ? e % nb : e / TRSM_SCOLS, c = rows_fast ? e / nb : e % TRSM_SCOLS;
-        X[i * LX + c] = (c < cols) ? b[i * brs + (j0 + c) * bcs] : 0.0;
-    }
-    __syncthreads();
-    if (t < nb) dinv[t] = unit ? 1.0 : 1.0 / L[t * LL + t];
-    __syncthreads();
-    const int c = t / TRSM_LANES, g = t % TRSM_LANES;  // the 8 lanes of a column share a warp
-    for (int step = 0; step < nb; ++step) {
-        const int i = lower ? step : nb - 1 - step;
-        const int l0 = lower ? 0 : i + 1, l1 = lower ? i : nb;
-        double part = 0.0;
-#pragma unroll 4
-        for (int l = l0 + g; l < l1; l += TRSM_LANES) part = fma(L[i * LL + l], X[l * LX + c], part);
+    const int c = t / LANES, g = t % LANES;  // the lanes of a column share a warp
+    const int src0 = (t % 32) - g;           // the column's first lane within the warp
+    double x[R];
 #pragma unroll
-        for (int off = TRSM_LANES / 2; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-        if (g == 0) X[i * LX + c] = (X[i * LX + c] - part) * dinv[i];
-        __syncwarp();
+    for (int q = 0; q < R; ++q) x[q] = X[(q * LANES + g) * LX + c];
+#pragma unroll
+    for (int step = 0; step < TRSM_NB; ++step) {
+        const int i = LOWER ? step : TRSM_NB - 1 - step;
+        const int qi = i / LANES, gi = i % LANES;
+        double v = x[qi] * dinv[i];
+        if constexpr (LANES > 1) v = __shfl_sync(0xffffffffu, v, src0 + gi);
+        if (g == gi) x[qi] = v;
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            // rows q * LANES .. q * LANES + LANES - 1 of this q; skip the q no lane needs
+            if (LOWER ? (q * LANES + LANES - 1 > i) : (q * LANES < i)) {
+                const int r = q * LANES + g;
+                if (LOWER ? (r > i) : (r < i)) x[q] = fma(-L[r * LL + i], v, x[q]);
+            }
+        }
     }
+#pragma unroll
+    for (int q = 0; q < R; ++q) X[(q * LANES + g) * LX + c] = x[q];
     __syncthreads();
 #pragma unroll 8
-    for (int e = t; e < nb * TRSM_SCOLS; e += TRSM_STHREADS) {
-        const int i = rows_fast ? e % nb : e / TRSM_SCOLS, cc = rows_fast ? e / nb : e % TRSM_SCOLS;
-        if (cc < cols) b[i * brs + (j0 + cc) * bcs] = X[i * LX + cc];
+    for (int e = t; e < TRSM_NB * COLS; e += TRSM_THREADS) {
+        const int i = rows_fast ? e % TRSM_NB : e / COLS, cc = rows_fast ? e / TRSM_NB : e % COLS;
+        if (cc < cols && i < nb) b[i * brs + (j0 + cc) * bcs] = X[i * LX + cc];
     }
 }
 
-constexpr size_t TRSM_SSMEM = sizeof(double) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB + TRSM_NB * (TRSM_SCOLS + 1));
+constexpr size_t trsm_smem_bytes(int lanes)
+{
+    return sizeof(double) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB + TRSM_NB * (TRSM_THREADS / lanes + 1));
+}
 
-constexpr size_t TRSM_SMEM = sizeof(double) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB + TRSM_NB * (TRSM_COLS + 1));
+template <int LANES, bool LOWER>
+int launch_trsm_diag(int nb, int unit, const double* a, int64_t ars, int64_t acs, double* b, int64_t brs,
+                     int64_t bcs, int64_t ncols, cudaStream_t s)
+{
+    static bool attr = false;
+    if (!attr) {
+        const int rc = check_cuda(cudaFuncSetAttribute(trsm_diag_kernel<LANES, LOWER>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)trsm_smem_bytes(LANES)), "trsm smem attr");
+        if (rc) return rc;
+        attr = true;
+    }
+    const int64_t blocks = (ncols + TRSM_THREADS / LANES - 1) / (TRSM_THREADS / LANES);
+    if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "dtrsm", "too many right-hand sides");
+    trsm_diag_kernel<LANES, LOWER><<<(unsigned)blocks, TRSM_THREADS, trsm_smem_bytes(LANES), s>>>(
+        nb, unit, a, ars, acs, b, brs, bcs, ncols);
+    return check_cuda(cudaGetLastError(), "trsm_diag");
+}
 
 // Multiply-adds below which a TRSM update runs natively in the precision form
 // (GB_TRSM_OZAKI_MIN_FMA; default 0: measured on GB300, even the 64 x n x 64
@@ -180,35 +162,53 @@ int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t cco
                         t.brs, t.bcs, t.s);
 }
 
+// Lanes per right-hand side for the diagonal kernel.  Each warp issues, per
+// step, one FP64 multiply and one FMA for every group of LANES rows that has
+// a row left to update: 64 + 64R - LANES R (R - 1) / 2 - R instructions in
+// all (R = 64 / LANES rows per lane; 2080, 1088, 592, 344 for 1, 2, 4, 8
+// lanes), for 32 / LANES columns.  GB300's FP64 pipe takes tens of cycles
+// per warp instruction on each of an SM's four sub-partitions, so the solve
+// time is about the instructions of one warp times the warps that share a
+// sub-partition: CTAs of four warps, ceil(CTAs / SMs) of them on the
+// busiest SM.  The fewest lanes win near-ties.
+int trsm_diag_lanes(int64_t ncols)
+{
+    const int64_t sms = sm_count() > 0 ? sm_count() : 148;
+    int best = 1;
+    int64_t best_cost = 0;
+    for (int lanes = 1; lanes <= 8; lanes *= 2) {
+        const int64_t r = TRSM_NB / lanes;
+        const int64_t per_warp = 64 + 64 * r - lanes * r * (r - 1) / 2 - r;
+        const int64_t ctas = (ncols + TRSM_THREADS / lanes - 1) / (TRSM_THREADS / lanes);
+        const int64_t cost = per_warp * ((ctas + sms - 1) / sms);
+        if (lanes == 1 || cost * 50 < best_cost * 49) {
+            best = lanes;
+            best_cost = cost;
+        }
+    }
+    return best;
+}
+
 int solve(const TrsmCtx& t, int64_t r0, int64_t mm)
 {
     if (mm <= TRSM_NB) {
-        static bool attr = false;
-        if (!attr) {
-            int rc0 = check_cuda(cudaFuncSetAttribute(trsm_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      (int)TRSM_SMEM), "trsm smem attr");
-            if (!rc0)
-                rc0 = check_cuda(cudaFuncSetAttribute(trsm_diag_split_kernel,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRSM_SSMEM),
-                                 "trsm smem attr");
-            if (rc0) return rc0;
-            attr = true;
-        }
-        const int sms = sm_count() > 0 ? sm_count() : 148;
-        const int64_t blocks = (t.n + TRSM_COLS - 1) / TRSM_COLS;
+        const double* a11 = t.a + r0 * t.ars + r0 * t.acs;
+        double* b1 = t.b + r0 * t.brs;
         LaunchScope ls("trsm_diag", t.s);
-        if (blocks >= sms) {
-            if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "dtrsm", "too many right-hand sides");
-            trsm_diag_kernel<<<(unsigned)blocks, TRSM_THREADS, TRSM_SMEM, t.s>>>(
-                (int)mm, t.lower, t.unit, t.a + r0 * t.ars + r0 * t.acs, t.ars, t.acs, t.b + r0 * t.brs, t.brs,
-                t.bcs, t.n);
-        } else {
-            const int64_t sblocks = (t.n + TRSM_SCOLS - 1) / TRSM_SCOLS;
-            trsm_diag_split_kernel<<<(unsigned)sblocks, TRSM_STHREADS, TRSM_SSMEM, t.s>>>(
-                (int)mm, t.lower, t.unit, t.a + r0 * t.ars + r0 * t.acs, t.ars, t.acs, t.b + r0 * t.brs, t.brs,
-                t.bcs, t.n);
+        switch (trsm_diag_lanes(t.n)) {
+        case 1:
+            return t.lower ? launch_trsm_diag<1, true>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_trsm_diag<1, false>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s);
+        case 2:
+            return t.lower ? launch_trsm_diag<2, true>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_trsm_diag<2, false>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s);
+        case 4:
+            return t.lower ? launch_trsm_diag<4, true>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_trsm_diag<4, false>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s);
+        default:
+            return t.lower ? launch_trsm_diag<8, true>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_trsm_diag<8, false>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s);
         }
-        return check_cuda(cudaGetLastError(), "trsm_diag");
     }
     // split on a multiple of the diagonal block size
     int64_t m1 = ((mm / 2 + TRSM_NB - 1) / TRSM_NB) * TRSM_NB;

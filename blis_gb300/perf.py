@@ -118,7 +118,7 @@ def run_bgemm(out):
 
 def run_trsm(out):
     import torch
-    m, n = (2048, 10240) if SMALL else (8192, 4096)  # small: enough columns for the one-thread diagonal kernel
+    m, n = (2048, 10240) if SMALL else (8192, 4096)  # small: fewer rows, more right-hand sides
     L = _mat(m, m, seed=11)
     L.copy_(torch.tril(L))
     d = torch.arange(m, device="cuda")

@@ -225,10 +225,11 @@ def test_batch_with_selected_configs(gblib, dtype):
             assert np.all(np.abs(g.cpu().numpy().T.astype(np.float64) - ref) <= bound)
 
 
+@pytest.mark.parametrize("n", [300, 4096, 9000, 31000])
 @pytest.mark.parametrize("uplo,trans", [("L", "N"), ("U", "N"), ("L", "T")])
-def test_dtrsm_many_right_hand_sides(uplo, trans):
-    # n large enough for the one-thread-per-column diagonal kernel (at least one 64-column CTA per SM)
-    m, n = 192, 10000
+def test_dtrsm_many_right_hand_sides(uplo, trans, n):
+    # on 152 SMs these n take the diagonal kernel with 8, 4, 2 and 1 lanes per right-hand side
+    m = 200  # three full 64-row diagonal blocks and one of 8 rows
     a = np.asfortranarray(H.normalize(po.uniform((m, m), 14)) + 2.0 * np.eye(m))
     b0 = H.normalize(po.uniform((m, n), 15))
     x = np.asfortranarray(b0.copy())
