@@ -1096,34 +1096,22 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const __grid_constant
 }
 
 // ---------------------------------------------------------------- grouped form
-// Split for every problem of a batch in one launch.  A block owns 32 rows of
-// op(A_i) or op(B_i)^T over the whole k range: pass 1 takes the row maxima
-// (8 threads per row), pass 2 cuts 64-wide k blocks into digits and writes
-// them into the problem's boxes.  Only blocks holding rows of the matrix
-// run; their rows past m (n) and k past k_i up to the block width are
-// written as zeros, and the remaining padding rows of a box stay as the
-// plan's one-time zero fill left them.
-template <int S>
-__global__ void __launch_bounds__(256, 2) oz_split_batch_kernel(const OzBatchProb* __restrict__ probs,
-                                                             const int32_t* __restrict__ unit_prob,
-                                                             const int64_t* __restrict__ unit_base,
-                                                             int64_t boxes_a, int64_t boxes_b,
-                                                             uint16_t* __restrict__ sa, uint16_t* __restrict__ sb,
-                                                             int* __restrict__ nonfinite)
+// One block's share of a split with the row maxima taken in the same
+// launch: 32 rows (r0 ..) of a row operand R (element (r, l) at
+// R[r*sr + l*sl]) over the whole k range.  Pass 1 takes the row maxima
+// (8 threads per row) and writes the rows' exponents; pass 2 cuts nkb
+// 64-wide k blocks into digits, the next block's elements loaded into
+// registers while one is cut, and hands each thread's 8 bf16 digits of a
+// slice to store(p, kb, rr, c0, v) (slice p, k block kb, tile row rr,
+// columns c0 .. c0 + 7).  Rows past `rows` and k past `k` give zero digits.
+template <int S, typename Store>
+__device__ __forceinline__ void oz_split_unit(const double* __restrict__ R, int64_t rows, int64_t sr, int64_t sl,
+                                              int64_t k, int nkb, int64_t r0, int32_t* __restrict__ exps,
+                                              int* __restrict__ nonfinite, Store store)
 {
     __shared__ double tile[32][65];
     __shared__ unsigned long long red[8][32];
     __shared__ int rowe[32];
-    const int pi = unit_prob[blockIdx.x];
-    const OzBatchProb& q = probs[pi];
-    int64_t u = (int64_t)blockIdx.x - unit_base[pi];
-    const bool isb = (u >= q.units_a);
-    if (isb) u -= q.units_a;
-    const int64_t rows = isb ? q.n : q.m, k = q.k;
-    const double* R = isb ? q.b : q.a;
-    const int64_t sr = isb ? q.brs : q.ars, sl = isb ? q.bcs : q.acs;
-    const int box_rows = isb ? OZ_BN : OZ_BM;
-    const int64_t r0 = u * 32;
     const bool rows_fast = (sr == 1);
     const int t = threadIdx.x;
 
@@ -1152,21 +1140,16 @@ __global__ void __launch_bounds__(256, 2) oz_split_batch_kernel(const OzBatchPro
             int nf = 0;
             e = oz_row_exponent(mx, &nf);
             if (nf) *nonfinite = 1;
-            (isb ? q.eb : q.ea)[r] = e;
+            exps[r] = e;
         }
         rowe[t] = e;
     }
     __syncthreads();
 
     // pass 2: digits, one 32 x 64 tile at a time
-    uint16_t* out = isb ? sb : sa;
-    const int64_t boxes = isb ? boxes_b : boxes_a;
-    const int64_t box0 = (isb ? q.bbox : q.abox) + (r0 / box_rows) * q.kb;
-    const int64_t rb = (r0 % box_rows);
     const int rr = t >> 3, c0 = (t & 7) * 8;
     const int e = rowe[rr];
     const bool live = (r0 + rr < rows);
-    // the next k block's elements are loaded into registers while this one is cut
     double nxt[8];
     auto fetch = [&](int kb) {
         const int64_t l0 = (int64_t)kb * 64;
@@ -1180,14 +1163,14 @@ __global__ void __launch_bounds__(256, 2) oz_split_batch_kernel(const OzBatchPro
         }
     };
     fetch(0);
-    for (int kb = 0; kb < q.kb; ++kb) {
+    for (int kb = 0; kb < nkb; ++kb) {
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
             const int idx = t + 256 * g;
             tile[rows_fast ? (idx & 31) : (idx >> 6)][rows_fast ? (idx >> 5) : (idx & 63)] = nxt[g];
         }
         __syncthreads();
-        if (kb + 1 < q.kb) fetch(kb + 1);
+        if (kb + 1 < nkb) fetch(kb + 1);
         uint32_t packed[S][4];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
@@ -1201,13 +1184,59 @@ __global__ void __launch_bounds__(256, 2) oz_split_batch_kernel(const OzBatchPro
             }
         }
 #pragma unroll
-        for (int p = 0; p < S; ++p) {
-            const int64_t z = (int64_t)p * boxes + box0 + kb;
-            uint4* dst = reinterpret_cast<uint4*>(out + (z * box_rows + rb + rr) * 64 + c0);
-            *dst = make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
-        }
+        for (int p = 0; p < S; ++p) store(p, kb, rr, c0, make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]));
         __syncthreads();
     }
+}
+
+// Split of one operand of a single product with its row maxima in the same
+// launch (oz_split_unit): block u owns rows 32u .. 32u + 31 of the padded
+// row range, so the padding rows up to rpad and the k padding up to kpad
+// are written as zeros, in the slice planes' layout of oz_split_kernel.
+template <int S>
+__global__ void __launch_bounds__(256, 2) oz_split_rows_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
+                                                            int64_t sr, int64_t sl, int64_t rpad, int64_t kpad,
+                                                            uint16_t* __restrict__ out, int32_t* __restrict__ exps,
+                                                            int* __restrict__ nonfinite)
+{
+    const int64_t r0 = (int64_t)blockIdx.x * 32;
+    oz_split_unit<S>(R, rows, sr, sl, k, (int)(kpad / 64), r0, exps, nonfinite,
+                     [&](int p, int kb, int rr, int c0, uint4 v) {
+                         *reinterpret_cast<uint4*>(out + ((int64_t)p * rpad + r0 + rr) * kpad + kb * 64 + c0) = v;
+                     });
+}
+
+// ---------------------------------------------------------------- grouped form
+// Split for every problem of a batch in one launch.  A block owns 32 rows of
+// op(A_i) or op(B_i)^T over the whole k range (oz_split_unit) and writes
+// them into the problem's boxes.  Only blocks holding rows of the matrix
+// run; their rows past m (n) and k past k_i up to the block width are
+// written as zeros, and the remaining padding rows of a box stay as the
+// plan's one-time zero fill left them.
+template <int S>
+__global__ void __launch_bounds__(256, 2) oz_split_batch_kernel(const OzBatchProb* __restrict__ probs,
+                                                             const int32_t* __restrict__ unit_prob,
+                                                             const int64_t* __restrict__ unit_base,
+                                                             int64_t boxes_a, int64_t boxes_b,
+                                                             uint16_t* __restrict__ sa, uint16_t* __restrict__ sb,
+                                                             int* __restrict__ nonfinite)
+{
+    const int pi = unit_prob[blockIdx.x];
+    const OzBatchProb& q = probs[pi];
+    int64_t u = (int64_t)blockIdx.x - unit_base[pi];
+    const bool isb = (u >= q.units_a);
+    if (isb) u -= q.units_a;
+    const int box_rows = isb ? OZ_BN : OZ_BM;
+    const int64_t r0 = u * 32;
+    uint16_t* out = isb ? sb : sa;
+    const int64_t boxes = isb ? boxes_b : boxes_a;
+    const int64_t box0 = (isb ? q.bbox : q.abox) + (r0 / box_rows) * q.kb;
+    const int64_t rb = (r0 % box_rows);
+    oz_split_unit<S>(isb ? q.b : q.a, isb ? q.n : q.m, isb ? q.brs : q.ars, isb ? q.bcs : q.acs, q.k, q.kb, r0,
+                     isb ? q.eb : q.ea, nonfinite, [&](int p, int kb, int rr, int c0, uint4 v) {
+                         const int64_t z = (int64_t)p * boxes + box0 + kb;
+                         *reinterpret_cast<uint4*>(out + (z * box_rows + rb + rr) * 64 + c0) = v;
+                     });
 }
 
 // Recombination for every problem of a batch in one launch: blocks are
@@ -1371,6 +1400,57 @@ void split_dispatch(int slices, int64_t rows, int64_t k, const double* R, int64_
     }
 }
 
+// The fused split (row maxima and digits in one launch, no maxima array)
+// for k up to GB_OZAKI_FUSED_SPLIT_K (default 4096).  Beyond it the two
+// passes of a block over its rows outgrow what L2 keeps between them: at
+// 16384^3 on GB300 the fused form took 5.6 ms against 4.6 ms for the
+// row-maximum kernel plus the tiled split, while the TRSM updates (k up to
+// 4096, many small launches) ran 2-3% faster fused.
+int64_t fused_split_max_k()
+{
+    static int64_t v = -1;
+    if (v < 0) {
+        const char* e = getenv("GB_OZAKI_FUSED_SPLIT_K");
+        v = e ? atoll(e) : 4096;
+        if (v < 0) v = 0;
+    }
+    return v;
+}
+
+template <int S>
+void launch_split_rows(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl, int64_t rpad,
+                       int64_t kpad, uint16_t* out, int32_t* ex, int* nonfinite, cudaStream_t s)
+{
+    LaunchScope ls("oz_split_rows", s);
+    oz_split_rows_kernel<S><<<(unsigned)(rpad / 32), 256, 0, s>>>(rows, k, R, sr, sl, rpad, kpad, out, ex, nonfinite);
+}
+
+void launch_rowmax(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl, unsigned long long* mb,
+                   cudaStream_t s);
+
+// Row maxima and digit slices of one row operand: fused for small k, else
+// the row-maximum kernel into mb (zeroed here) and the tiled split.
+void split_operand(int slices, int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl,
+                   unsigned long long* mb, int64_t rpad, int64_t kpad, uint16_t* out, int32_t* ex, int* nonfinite,
+                   cudaStream_t s)
+{
+    if (k <= fused_split_max_k() && rpad / 32 <= INT32_MAX) {
+        switch (slices) {
+#define GB_SPLIT_CASE(S) \
+    case S: launch_split_rows<S>(rows, k, R, sr, sl, rpad, kpad, out, ex, nonfinite, s); break;
+            GB_SPLIT_CASE(2) GB_SPLIT_CASE(3) GB_SPLIT_CASE(4) GB_SPLIT_CASE(5) GB_SPLIT_CASE(6)
+            GB_SPLIT_CASE(7) GB_SPLIT_CASE(8) GB_SPLIT_CASE(9) GB_SPLIT_CASE(10) GB_SPLIT_CASE(11)
+            GB_SPLIT_CASE(12)
+#undef GB_SPLIT_CASE
+        default: break;
+        }
+        return;
+    }
+    cudaMemsetAsync(mb, 0, sizeof(unsigned long long) * rows, s);
+    launch_rowmax(rows, k, R, sr, sl, mb, s);
+    split_dispatch(slices, rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, s);
+}
+
 }  // namespace
 
 // Largest K of one part of a level with `npairs` slice products:
@@ -1492,13 +1572,11 @@ int ozaki_prepare_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t 
     A->ea = reinterpret_cast<int32_t*>(A->maxa + m);
     A->nonfinite = reinterpret_cast<int*>(A->ea + m);
     int rc;
-    if ((rc = check_cuda(cudaMemsetAsync(A->maxa, 0, sizeof(unsigned long long) * m, s), "memset")) ||
-        (rc = check_cuda(cudaMemsetAsync(A->nonfinite, 0, sizeof(int), s), "memset"))) {
+    if ((rc = check_cuda(cudaMemsetAsync(A->nonfinite, 0, sizeof(int), s), "memset"))) {
         ozaki_release_a(A, s);
         return rc;
     }
-    launch_rowmax(m, k, a, ars, acs, A->maxa, s);
-    split_dispatch(slices, m, k, a, ars, acs, A->maxa, A->mpad, A->kpad, A->sa, A->ea, A->nonfinite, s);
+    split_operand(slices, m, k, a, ars, acs, A->maxa, A->mpad, A->kpad, A->sa, A->ea, A->nonfinite, s);
     if ((rc = check_cuda(cudaGetLastError(), "oz_split"))) ozaki_release_a(A, s);
     return rc;
 }
@@ -1570,10 +1648,8 @@ int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_
 
     int rc = GB_SUCCESS;
     auto bail = [&](int code) { dev_free(ws, s); return code; };
-    if ((rc = check_cuda(cudaMemsetAsync(maxb, 0, sizeof(unsigned long long) * n, s), "memset"))) return bail(rc);
     // rows of op(B)^T: (j, l) = b[l*brs + j*bcs]
-    launch_rowmax(n, k, b, bcs, brs, maxb, s);
-    split_dispatch(slices, n, k, b, bcs, brs, maxb, npad, kpad, sb, eb, A->nonfinite, s);
+    split_operand(slices, n, k, b, bcs, brs, maxb, npad, kpad, sb, eb, A->nonfinite, s);
     if ((rc = check_cuda(cudaGetLastError(), "oz_split"))) return bail(rc);
 
     CUtensorMap map_a, map_b;

@@ -23,52 +23,82 @@ namespace {
 
 constexpr int TRSM_NB = 64;
 
-// Solves op(A11) X = B1 in place for an nb x nb diagonal block.
-// op(A)(i, l) = a[i*ars + l*acs]; B(i, j) = b[i*brs + j*bcs].  A CTA of
-// TRSM_THREADS threads owns TRSM_THREADS / LANES right-hand sides.  The
-// triangle (padded to 64 x 64 with identity rows) and the CTA's panel of B
-// are staged in shared memory, coalesced along B's contiguous direction;
-// each lane then holds 64 / LANES rows of its column in registers (row
-// r = q * LANES + g in x[q] of lane g) and runs right-looking substitution:
-// x_i = b_i * inv(a_ii) from the lane that owns row i (shuffled to the
-// column's other lanes), then b_r -= a_ri x_i for every later row r.  Every
-// FP64 instruction but one multiply per row is an FMA of the triangle, so
-// the FP64 pipe (GB300's narrowest) does no reduction work, and one row's
-// updates are independent of each other.  LANES trades those instructions
-// (the per-row multiply is repeated on every lane) against how many warps
-// there are to fill the SM sub-partitions; the host picks it from a cost
-// model.  Both loops are unrolled, so every register index is a constant.
+// Every diagonal block of op(A) in the form the solves read, packed once per
+// call: block q (rows and columns 64q .. 64q + nb - 1) becomes a row-major
+// 64 x 64 array P with P[r][r] = inv(a_rr) (1 for a unit diagonal and for
+// the identity rows that pad a short last block), P[r][i] = a_ri inv(a_ii)
+// inside the strict triangle and 0 elsewhere.  The scaling lets the solve
+// work on y = D X (D = diag(a)) with a unit triangle; see trsm_diag_kernel.
+template <bool LOWER>
+__global__ void __launch_bounds__(256) trsm_pack_diag_kernel(int64_t m, int unit, const double* __restrict__ a,
+                                                             int64_t ars, int64_t acs, double* __restrict__ packed)
+{
+    __shared__ double T[TRSM_NB][TRSM_NB + 1];
+    __shared__ double dinv[TRSM_NB];
+    const int64_t r0 = (int64_t)blockIdx.x * TRSM_NB;
+    const int nb = (m - r0 < TRSM_NB) ? (int)(m - r0) : TRSM_NB;
+    const double* blk = a + r0 * ars + r0 * acs;
+    const bool rows_fast = (ars == 1);
+    for (int e = threadIdx.x; e < TRSM_NB * TRSM_NB; e += 256) {
+        const int i = rows_fast ? e % TRSM_NB : e / TRSM_NB, l = rows_fast ? e / TRSM_NB : e % TRSM_NB;
+        const bool keep = (i < nb && l < nb) && (LOWER ? (l <= i) : (l >= i));
+        T[i][l] = keep ? blk[i * ars + l * acs] : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x < TRSM_NB) {
+        const int i = threadIdx.x;
+        dinv[i] = (unit || i >= nb) ? 1.0 : 1.0 / T[i][i];
+    }
+    __syncthreads();
+    double* out = packed + (int64_t)blockIdx.x * TRSM_NB * TRSM_NB;
+    for (int e = threadIdx.x; e < TRSM_NB * TRSM_NB; e += 256) {
+        const int r = e / TRSM_NB, i = e % TRSM_NB;
+        double v = 0.0;
+        if (r == i) v = dinv[r];
+        else if (LOWER ? (i < r) : (i > r)) v = T[r][i] * dinv[i];
+        out[e] = v;
+    }
+}
+
+// Solves op(A11) X = B1 in place for one diagonal block, from its packed form
+// P; B(i, j) = b[i*brs + j*bcs], rows of B past nb are neither read nor
+// written.  A CTA of TRSM_THREADS threads owns TRSM_THREADS / LANES
+// right-hand sides: P and the CTA's panel of B are staged in shared memory
+// (coalesced along B's contiguous direction), then each lane holds
+// 64 / LANES rows of its column in registers (row r = q * LANES + g in x[q]
+// of lane g) and runs right-looking substitution on y = D X with the unit
+// triangle of P: y_i is final once the rows before it have been applied; the
+// lane that owns row i shuffles it to the column's other lanes, which do
+// y_r -= P[r][i] y_i for every later row r; at the end x_r = y_r inv(a_rr)
+// (pre-inverted diagonal, as the reference's trsm kernels use).  Every FP64
+// instruction of the substitution is an FMA of the triangle, so the FP64
+// pipe (GB300's narrowest) does no reduction work and each row's dependent
+// chain is one FMA and one shuffle.  LANES trades issue slots (the FMA of a
+// group of LANES rows is one warp instruction however few of its rows are
+// left) against how many warps there are to fill the SM sub-partitions.  Both
+// loops are unrolled, so every register index is a constant.
 constexpr int TRSM_THREADS = 128;
 
 template <int LANES, bool LOWER>
-__global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int unit, const double* __restrict__ a,
-                                                                 int64_t ars, int64_t acs, double* __restrict__ b,
-                                                                 int64_t brs, int64_t bcs, int64_t ncols)
+__global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, const double* __restrict__ pk,
+                                                                 double* __restrict__ b, int64_t brs, int64_t bcs,
+                                                                 int64_t ncols)
 {
     constexpr int COLS = TRSM_THREADS / LANES, R = TRSM_NB / LANES, LL = TRSM_NB + 1, LX = COLS + 1;
     extern __shared__ double trsm_smem[];
     double* L = trsm_smem;                 // [TRSM_NB][LL]
-    double* dinv = L + TRSM_NB * LL;       // [TRSM_NB]
-    double* X = dinv + TRSM_NB;            // [TRSM_NB][LX]
+    double* X = L + TRSM_NB * LL;          // [TRSM_NB][LX]
     const int t = threadIdx.x;
     const int64_t j0 = (int64_t)blockIdx.x * COLS;
     const int cols = (ncols - j0 < COLS) ? (int)(ncols - j0) : COLS;
 #pragma unroll 8
-    for (int e = t; e < TRSM_NB * TRSM_NB; e += TRSM_THREADS) {
-        const int i = e % TRSM_NB, l = e / TRSM_NB;
-        const bool in_tri = LOWER ? (l < i) : (l > i);
-        double v = (i == l) ? 1.0 : 0.0;
-        if (i < nb && l < nb && (in_tri || i == l)) v = a[i * ars + l * acs];
-        L[i * LL + l] = v;
-    }
+    for (int e = t; e < TRSM_NB * TRSM_NB; e += TRSM_THREADS) L[(e / TRSM_NB) * LL + e % TRSM_NB] = pk[e];
     const bool rows_fast = (brs == 1);
 #pragma unroll 8
     for (int e = t; e < TRSM_NB * COLS; e += TRSM_THREADS) {
         const int i = rows_fast ? e % TRSM_NB : e / COLS, c = rows_fast ? e / TRSM_NB : e % COLS;
         X[i * LX + c] = (c < cols && i < nb) ? b[i * brs + (j0 + c) * bcs] : 0.0;
     }
-    __syncthreads();
-    if (t < TRSM_NB) dinv[t] = (unit || t >= nb) ? 1.0 : 1.0 / L[t * LL + t];
     __syncthreads();
     const int c = t / LANES, g = t % LANES;  // the lanes of a column share a warp
     const int src0 = (t % 32) - g;           // the column's first lane within the warp
@@ -79,9 +109,8 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int uni
     for (int step = 0; step < TRSM_NB; ++step) {
         const int i = LOWER ? step : TRSM_NB - 1 - step;
         const int qi = i / LANES, gi = i % LANES;
-        double v = x[qi] * dinv[i];
+        double v = x[qi];
         if constexpr (LANES > 1) v = __shfl_sync(0xffffffffu, v, src0 + gi);
-        if (g == gi) x[qi] = v;
 #pragma unroll
         for (int q = 0; q < R; ++q) {
             // rows q * LANES .. q * LANES + LANES - 1 of this q; skip the q no lane needs
@@ -92,7 +121,10 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int uni
         }
     }
 #pragma unroll
-    for (int q = 0; q < R; ++q) X[(q * LANES + g) * LX + c] = x[q];
+    for (int q = 0; q < R; ++q) {
+        const int r = q * LANES + g;
+        X[r * LX + c] = x[q] * L[r * LL + r];
+    }
     __syncthreads();
 #pragma unroll 8
     for (int e = t; e < TRSM_NB * COLS; e += TRSM_THREADS) {
@@ -103,12 +135,11 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, int uni
 
 constexpr size_t trsm_smem_bytes(int lanes)
 {
-    return sizeof(double) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB + TRSM_NB * (TRSM_THREADS / lanes + 1));
+    return sizeof(double) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB * (TRSM_THREADS / lanes + 1));
 }
 
 template <int LANES, bool LOWER>
-int launch_trsm_diag(int nb, int unit, const double* a, int64_t ars, int64_t acs, double* b, int64_t brs,
-                     int64_t bcs, int64_t ncols, cudaStream_t s)
+int launch_trsm_diag(int nb, const double* pk, double* b, int64_t brs, int64_t bcs, int64_t ncols, cudaStream_t s)
 {
     static bool attr = false;
     if (!attr) {
@@ -121,7 +152,7 @@ int launch_trsm_diag(int nb, int unit, const double* a, int64_t ars, int64_t acs
     const int64_t blocks = (ncols + TRSM_THREADS / LANES - 1) / (TRSM_THREADS / LANES);
     if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "dtrsm", "too many right-hand sides");
     trsm_diag_kernel<LANES, LOWER><<<(unsigned)blocks, TRSM_THREADS, trsm_smem_bytes(LANES), s>>>(
-        nb, unit, a, ars, acs, b, brs, bcs, ncols);
+        nb, pk, b, brs, bcs, ncols);
     return check_cuda(cudaGetLastError(), "trsm_diag");
 }
 
@@ -141,6 +172,7 @@ double trsm_ozaki_min_fma()
 
 struct TrsmCtx {
     int lower, unit, slices;
+    const double* packed;  // the diagonal blocks, trsm_pack_diag_kernel's layout
     const double* a;
     int64_t ars, acs;
     double* b;
@@ -162,25 +194,37 @@ int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t cco
                         t.brs, t.bcs, t.s);
 }
 
-// Lanes per right-hand side for the diagonal kernel.  Each warp issues, per
-// step, one FP64 multiply and one FMA for every group of LANES rows that has
-// a row left to update: 64 + 64R - LANES R (R - 1) / 2 - R instructions in
-// all (R = 64 / LANES rows per lane; 2080, 1088, 592, 344 for 1, 2, 4, 8
-// lanes), for 32 / LANES columns.  GB300's FP64 pipe takes tens of cycles
-// per warp instruction on each of an SM's four sub-partitions, so the solve
-// time is about the instructions of one warp times the warps that share a
-// sub-partition: CTAs of four warps, ceil(CTAs / SMs) of them on the
-// busiest SM.  The fewest lanes win near-ties.
+// Lanes per right-hand side for the diagonal kernel (GB_TRSM_DIAG_LANES =
+// 1, 2, 4 or 8 fixes it).  Each warp issues one FMA per step for every group
+// of LANES rows that has a row left to update, 64R - LANES R (R - 1) / 2 - R
+// instructions (R = 64 / LANES rows per lane), and R multiplies: 2080, 1056,
+// 544, 288 for 1, 2, 4, 8 lanes, for 32 / LANES columns; staging the packed
+// block and the panel costs about as much as 96 more.  GB300's FP64 pipe
+// takes tens of cycles per warp instruction on each of an SM's four
+// sub-partitions, so the solve time is about one warp's cost times the warps
+// that share a sub-partition (CTAs of four warps: ceil(CTAs / SMs) on the
+// busiest SM), but no less than four of them: below that the dependent chain
+// of each row, not the pipe, sets the time.  The constants were fitted to
+// solves of 2048 to 16384 right-hand sides timed on GB300.  The fewest lanes
+// win near-ties.
 int trsm_diag_lanes(int64_t ncols)
 {
+    static int forced = -1;
+    if (forced < 0) {
+        const char* e = getenv("GB_TRSM_DIAG_LANES");
+        const int v = e ? atoi(e) : 0;
+        forced = (v == 1 || v == 2 || v == 4 || v == 8) ? v : 0;
+    }
+    if (forced) return forced;
     const int64_t sms = sm_count() > 0 ? sm_count() : 148;
     int best = 1;
     int64_t best_cost = 0;
     for (int lanes = 1; lanes <= 8; lanes *= 2) {
         const int64_t r = TRSM_NB / lanes;
-        const int64_t per_warp = 64 + 64 * r - lanes * r * (r - 1) / 2 - r;
+        const int64_t per_warp = 64 * r - lanes * r * (r - 1) / 2 + 96;
         const int64_t ctas = (ncols + TRSM_THREADS / lanes - 1) / (TRSM_THREADS / lanes);
-        const int64_t cost = per_warp * ((ctas + sms - 1) / sms);
+        const int64_t waves = (ctas + sms - 1) / sms;
+        const int64_t cost = per_warp * (waves > 4 ? waves : 4);
         if (lanes == 1 || cost * 50 < best_cost * 49) {
             best = lanes;
             best_cost = cost;
@@ -192,22 +236,24 @@ int trsm_diag_lanes(int64_t ncols)
 int solve(const TrsmCtx& t, int64_t r0, int64_t mm)
 {
     if (mm <= TRSM_NB) {
-        const double* a11 = t.a + r0 * t.ars + r0 * t.acs;
+        // r0 is a multiple of the block size: the split below keeps it so
+        const double* pk = t.packed + (r0 / TRSM_NB) * TRSM_NB * TRSM_NB;
         double* b1 = t.b + r0 * t.brs;
+        const int nb = (int)mm;
         LaunchScope ls("trsm_diag", t.s);
         switch (trsm_diag_lanes(t.n)) {
         case 1:
-            return t.lower ? launch_trsm_diag<1, true>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_trsm_diag<1, false>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s);
+            return t.lower ? launch_trsm_diag<1, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_trsm_diag<1, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
         case 2:
-            return t.lower ? launch_trsm_diag<2, true>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_trsm_diag<2, false>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s);
+            return t.lower ? launch_trsm_diag<2, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_trsm_diag<2, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
         case 4:
-            return t.lower ? launch_trsm_diag<4, true>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_trsm_diag<4, false>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s);
+            return t.lower ? launch_trsm_diag<4, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_trsm_diag<4, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
         default:
-            return t.lower ? launch_trsm_diag<8, true>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_trsm_diag<8, false>((int)mm, t.unit, a11, t.ars, t.acs, b1, t.brs, t.bcs, t.n, t.s);
+            return t.lower ? launch_trsm_diag<8, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_trsm_diag<8, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
         }
     }
     // split on a multiple of the diagonal block size
@@ -258,7 +304,22 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     t.bcs = bcs;
     t.n = nn;
     t.s = s;
-    return solve(t, 0, mm);
+    const int64_t nblk = (mm + TRSM_NB - 1) / TRSM_NB;
+    if (nblk > INT32_MAX) return set_error(GB_ERR_ARG, "dtrsm", "too many diagonal blocks");
+    double* packed = static_cast<double*>(dev_alloc(sizeof(double) * nblk * TRSM_NB * TRSM_NB, s));
+    if (!packed) return GB_ERR_NOMEM;
+    {
+        LaunchScope ls("trsm_pack_diag", s);
+        if (t.lower)
+            trsm_pack_diag_kernel<true><<<(unsigned)nblk, 256, 0, s>>>(mm, t.unit, a, t.ars, t.acs, packed);
+        else
+            trsm_pack_diag_kernel<false><<<(unsigned)nblk, 256, 0, s>>>(mm, t.unit, a, t.ars, t.acs, packed);
+    }
+    int rc = check_cuda(cudaGetLastError(), "trsm_pack_diag");
+    t.packed = packed;
+    if (!rc) rc = solve(t, 0, mm);
+    dev_free(packed, s);
+    return rc;
 }
 
 }  // namespace gb

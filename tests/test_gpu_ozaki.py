@@ -73,6 +73,20 @@ def test_ozaki_k_partitions_bit_exact(slices, k):
     assert np.array_equal(c, ref)
 
 
+@pytest.mark.parametrize("ta,tb,order", [(N, N, "F"), (T, T, "F"), (N, T, "C"), (T, N, "C")])
+def test_ozaki_long_k_split_layouts(ta, tb, order):
+    # k above 4096 takes the row-maximum kernel and the tiled split instead of the fused split
+    m, n, k = 70, 90, 5000
+    a = po.expspread((k, m) if ta else (m, k), 9, order=order)
+    b = po.expspread((n, k) if tb else (k, n), 10, order=order)
+    c0 = po.uniform((m, n), 11, order=order)
+    ref = c0.copy(order=order)
+    po.ozaki_dgemm(ta, tb, 0.75, a, b, -1.0, ref, 7)
+    c = c0.copy(order=order)
+    _run_gpu(ta, tb, 0.75, a, b, -1.0, c, 7)
+    assert np.array_equal(c, ref)
+
+
 def test_ozaki_device_random_inputs_match_host_generator():
     torch = pytest.importorskip("torch")
     from blis_gb300 import dev
