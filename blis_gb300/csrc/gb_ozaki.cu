@@ -69,6 +69,7 @@ struct OzGemmParams {
     static constexpr bool kRawAcc = false;   // chunks are converted to int32 and summed
     int slices, nlevels, kb_total, tiles_m, tiles_n, chunk_kb, group_m;
     int64_t items, mpad, npad;
+    int64_t m, n;     // rows and columns of C: level sums of the padding are not stored
     int32_t* planes;  // [plane][npad][mpad]
     unsigned int* status;
     const int* skip;  // non-finite flag of the split kernels
@@ -259,9 +260,17 @@ __device__ __forceinline__ void oz_store_sums(const OzGemmParams& p, const OzIte
 {
     const int64_t i = (int64_t)w.tm * OZ_BM + quad * 32 + lane;
     const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
+    if (i >= p.m) return;
     int32_t* dst = p.planes + ((int64_t)w.plane * p.npad + j0) * p.mpad + i;
+    const int64_t jn = p.n - j0;  // columns of this half that exist
+    if (jn >= 128) {
 #pragma unroll
-    for (int c = 0; c < 128; ++c) dst[(int64_t)c * p.mpad] = acc[c];
+        for (int c = 0; c < 128; ++c) dst[(int64_t)c * p.mpad] = acc[c];
+    } else {
+#pragma unroll
+        for (int c = 0; c < 128; ++c)
+            if (c < jn) dst[(int64_t)c * p.mpad] = acc[c];
+    }
 }
 
 __device__ __forceinline__ void oz_store_sums(const OzBatchParams& p, const OzItem& w, int quad, int half,
@@ -783,9 +792,18 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             if (!ok) break;
             const int64_t i = (int64_t)w.tm * (2 * OZ2_ROWS) + (int64_t)rank * OZ2_ROWS + quad * 32 + lane;
             const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
-            int32_t* dst = p.planes + ((int64_t)w.plane * p.npad + j0) * p.mpad + i;
+            if (i < p.m) {  // level sums of padding rows and columns are not stored
+                int32_t* dst = p.planes + ((int64_t)w.plane * p.npad + j0) * p.mpad + i;
+                const int64_t jn = p.n - j0;
+                if (jn >= 128) {
 #pragma unroll
-            for (int c = 0; c < 128; ++c) dst[(int64_t)c * p.mpad] = acc[c];
+                    for (int c = 0; c < 128; ++c) dst[(int64_t)c * p.mpad] = acc[c];
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 128; ++c)
+                        if (c < jn) dst[(int64_t)c * p.mpad] = acc[c];
+                }
+            }
         }
     }
 
@@ -1631,6 +1649,8 @@ int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_
     p.group_m = group_m_setting();
     p.mpad = mpad;
     p.npad = npad;
+    p.m = m;
+    p.n = n;
 
     const size_t bytes_sb = (size_t)slices * npad * kpad * 2;
     const size_t bytes_pl = (size_t)planes_total * npad * mpad * 4;

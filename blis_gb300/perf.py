@@ -20,6 +20,7 @@ L2 where the workload allows:
                   slices) and FP32
 
 Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl] [--batch-count N] [--small]
+                                [--trsm-forms native,ozaki]
 (--small: 4096^3 GEMMs, 2048 x 10240 DTRSM, 2^25 vectors, 8192^2 GEMV, for ncu captures)
 """
 import argparse
@@ -34,6 +35,7 @@ from . import _lib, dev
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SMALL = False  # --small: profiling sizes (inputs still larger than the 126 MB L2)
+TRSM_FORMS = ("native", "ozaki")  # --trsm-forms: which DTRSM forms the trsm suites time
 
 
 def peaks():
@@ -126,6 +128,8 @@ def run_trsm(out):
     b0 = _mat(m, n, seed=12)
     flops = float(m) * m * n
     for mode, name in ((0, "native_fp64"), (1, "ozaki_s7_updates")):
+        if ("ozaki" if mode else "native") not in TRSM_FORMS:
+            continue
         _lib.load().gb_set_dgemm_mode(mode, 7)
         x = b0.clone()
         ms = _timer(lambda: (x.copy_(b0), dev.dtrsm(0, 0xC0, 0, 0, 1.0, L, x)), reps=1, warmup=1)
@@ -154,6 +158,8 @@ def run_trsm_ozaki(out):
     absL, absB = L.abs(), b0.abs()
     flops = float(m) * m * n
     for mode, name in ((0, "native_fp64"), (1, "ozaki_s7_updates")):
+        if ("ozaki" if mode else "native") not in TRSM_FORMS:
+            continue
         _lib.load().gb_set_dgemm_mode(mode, 7)
         x = b0.clone()
         reps = 1 if mode == 0 else 3
@@ -324,10 +330,12 @@ def main():
     ap.add_argument("--json")
     ap.add_argument("--batch-count", type=int, default=4096, help="problems of the batch_ozaki suite")
     ap.add_argument("--small", action="store_true", help="profiling sizes (workload names keep the full size)")
+    ap.add_argument("--trsm-forms", default="native,ozaki", help="DTRSM forms of the trsm suites")
     a = ap.parse_args()
-    global BATCH_COUNT, SMALL
+    global BATCH_COUNT, SMALL, TRSM_FORMS
     BATCH_COUNT = a.batch_count
     SMALL = a.small
+    TRSM_FORMS = tuple(f for f in a.trsm_forms.split(",") if f)
     torch.cuda.set_device(0)
     _lib.check(_lib.load().gb_init(0), "gb_init")
     names = [s for s in a.only.split(",") if s] or list(SUITES)
