@@ -143,9 +143,6 @@ int ozaki_host_pipelined(int transa, int64_t m, int64_t n, int64_t k, double alp
     Staged& A = bufs.next();
     if ((rc = stage_in(a, ta ? k : m, ta ? m : k, rs_a, cs_a, sizeof(double), true, &A, s))) return rc;
     OzA prep;
-    if ((rc = ozaki_prepare_a(m, k, reinterpret_cast<const double*>(A.origin), ta ? A.cs : A.rs, ta ? A.rs : A.cs,
-                              slices, s, &prep)))
-        return rc;
     double* bd = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(k * n), s));
     double* cd = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(m * n), s));
     cudaEvent_t ev[2 * 8 + 3];
@@ -155,7 +152,10 @@ int ozaki_host_pipelined(int transa, int64_t m, int64_t n, int64_t k, double alp
                 ev_out_done = ev[2 * nch + 2];
     rc = (bd && cd) ? GB_SUCCESS : GB_ERR_NOMEM;
     if (!rc) {
-        // the copy streams may touch bd/cd only after their stream-ordered allocation
+        // The copy streams may touch bd/cd only after their stream-ordered allocation, and
+        // op(B)'s blocks go up only after A (both ordered by ev_alloc): sharing the link with
+        // them would delay A, which every slice product needs.  A's split below then overlaps
+        // the first block's transfer.
         cudaEventRecord(ev_alloc, s);
         cudaStreamWaitEvent(cin, ev_alloc, 0);
         cudaStreamWaitEvent(cout, ev_alloc, 0);
@@ -168,6 +168,9 @@ int ozaki_host_pipelined(int transa, int64_t m, int64_t n, int64_t k, double alp
                                                   m * sizeof(double), nj, cudaMemcpyDefault, cin), "C block");
             cudaEventRecord(ev_in[j], cin);
         }
+        if (!rc)
+            rc = ozaki_prepare_a(m, k, reinterpret_cast<const double*>(A.origin), ta ? A.cs : A.rs,
+                                 ta ? A.rs : A.cs, slices, s, &prep);
         for (int j = 0; j < nch && !rc; ++j) {
             const int64_t j0 = n * j / nch, nj = n * (j + 1) / nch - j0;
             cudaStreamWaitEvent(s, ev_in[j], 0);
