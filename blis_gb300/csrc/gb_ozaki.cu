@@ -876,21 +876,13 @@ __device__ __forceinline__ int clz128(unsigned __int128 u)
     return hi ? __clzll((long long)hi) : (lo ? 64 + __clzll((long long)lo) : 128);
 }
 
-// bf16 bit pattern of an integer |d| <= 256: the fp32 image of d has at most
-// 8 significant bits, so its upper half is exactly the bf16 value.
-__device__ __forceinline__ uint32_t int_to_bf16_bits(int d)
-{
-    return __float_as_uint(__int2float_rn(d)) >> 16;
-}
-
 // Balanced base-256 digits of U = |x| 2^-e with the sign of x, from
 // integers only.  X = U 2^F truncated (F = 8S+2 fraction bits); adding
 // B = sum_p 128 2^(F-8p) + 2 makes the balanced digits the plain base-256
 // digits of Y = X + B: d_1 = (Y >> (F-8)) - 128 (at most 128), d_p =
 // ((Y >> (F-8p)) & 255) - 128.  The remainder lies in [-2, 2) units of
 // 2^-F, i.e. |rem| <= 2^-(8S+1) 2^e, and truncating X never changes a digit
-// (the rounding threshold is an integer).  One add and S shifts: the split
-// is integer-bound, so this is its cost.
+// (the rounding threshold is an integer).  x = 0 gives Y = B, all digits 0.
 template <typename U>
 __host__ __device__ constexpr U oz_bias(int S)
 {
@@ -899,17 +891,25 @@ __host__ __device__ constexpr U oz_bias(int S)
     return b;
 }
 
+// The split is integer-bound, so each digit costs one shift, one LOP3 and
+// one add on the integer pipe: with m = all ones for a negative x (else 0),
+// (raw ^ m) + c is raw - 128 for x >= 0 and 128 - raw for x < 0 when c is
+// -128 or +129, and adding 0x4B400000 (the fp32 1.5 * 2^23, whose unit in
+// the last place is 1) to c makes that sum the fp32 bit pattern of
+// 1.5 * 2^23 + d; one fp32 subtract (FMA pipe) leaves the exact float(d).
+// float(d) has at most 8 significant bits for |d| <= 128, so its upper half
+// is exactly the bf16 value.
+constexpr uint32_t OZ_MAGIC_BITS = 0x4B400000u;  // 12582912.0f
+constexpr float OZ_MAGIC = 12582912.0f;
+
 template <int S>
-__device__ __forceinline__ void oz_digits(double x, int e, int (&d)[S])
+__device__ __forceinline__ void oz_digit_floats(double x, int e, float (&f)[S])
 {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    const bool neg = (bits >> 63) != 0;
+    const uint32_t m = (uint32_t)((long long)bits >> 63);
+    const uint32_t c = m ? OZ_MAGIC_BITS + 129u : OZ_MAGIC_BITS - 128u;
     const int ex = (int)((bits >> 52) & 0x7FF);
-    const unsigned long long frac = bits & ((1ull << 52) - 1);
-#pragma unroll
-    for (int p = 0; p < S; ++p) d[p] = 0;
-    if (ex == 0 && frac == 0) return;
-    const unsigned long long M = ex ? (frac | (1ull << 52)) : frac;
+    const unsigned long long M = (bits & ((1ull << 52) - 1)) | (ex ? (1ull << 52) : 0ull);
     const int E2 = ex ? ex - 1075 : -1074;
     constexpr int F = 8 * S + 2;
     const int sh = E2 - e + F;  // U 2^F = M 2^sh < 2^(F-1)
@@ -917,21 +917,32 @@ __device__ __forceinline__ void oz_digits(double x, int e, int (&d)[S])
         // Y < 2^(F+1): 64 bits suffice (S <= 7)
         const unsigned long long X = (sh >= 0) ? (M << sh) : (sh > -64 ? (M >> (-sh)) : 0ull);
         const unsigned long long Y = X + oz_bias<unsigned long long>(S);
-        d[0] = (int)(Y >> (F - 8)) - 128;
+        f[0] = __uint_as_float(((uint32_t)(Y >> (F - 8)) ^ m) + c) - OZ_MAGIC;
 #pragma unroll
-        for (int p = 2; p <= S; ++p) d[p - 1] = (int)((Y >> (F - 8 * p)) & 255ull) - 128;
+        for (int p = 2; p <= S; ++p)
+            f[p - 1] = __uint_as_float((((uint32_t)(Y >> (F - 8 * p)) & 255u) ^ m) + c) - OZ_MAGIC;
     } else {
         using u128 = unsigned __int128;
         const u128 X = (sh >= 0) ? ((u128)M << sh) : (u128)(sh > -64 ? (M >> (-sh)) : 0ull);
         const u128 Y = X + oz_bias<u128>(S);
-        d[0] = (int)(unsigned long long)(Y >> (F - 8)) - 128;
+        f[0] = __uint_as_float(((uint32_t)(unsigned long long)(Y >> (F - 8)) ^ m) + c) - OZ_MAGIC;
 #pragma unroll
-        for (int p = 2; p <= S; ++p) d[p - 1] = (int)((unsigned long long)(Y >> (F - 8 * p)) & 255ull) - 128;
+        for (int p = 2; p <= S; ++p)
+            f[p - 1] = __uint_as_float((((uint32_t)(unsigned long long)(Y >> (F - 8 * p)) & 255u) ^ m) + c) -
+                       OZ_MAGIC;
     }
-    if (neg) {
+}
+
+// Digits of two elements, slice by slice as bf16 pairs (x0 in the low half):
+// one byte permute takes the upper halves of both fp32 images.
+template <int S>
+__device__ __forceinline__ void oz_digits_bf16x2(double x0, double x1, int e, uint32_t (&w)[S])
+{
+    float f0[S], f1[S];
+    oz_digit_floats<S>(x0, e, f0);
+    oz_digit_floats<S>(x1, e, f1);
 #pragma unroll
-        for (int p = 0; p < S; ++p) d[p] = -d[p];
-    }
+    for (int p = 0; p < S; ++p) w[p] = __byte_perm(__float_as_uint(f0[p]), __float_as_uint(f1[p]), 0x7632);
 }
 
 __device__ __forceinline__ int oz_row_exponent(unsigned long long bits, int* nonfinite)
@@ -977,15 +988,11 @@ __global__ void __launch_bounds__(256) oz_split_kernel(int64_t rows, int64_t k, 
     }
     uint32_t packed[S][4];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        int d[S];
-        oz_digits<S>(r < rows ? tile[rr][c0 + j] : 0.0, e, d);
+    for (int h = 0; h < 4; ++h) {
+        uint32_t w[S];
+        oz_digits_bf16x2<S>(r < rows ? tile[rr][c0 + 2 * h] : 0.0, r < rows ? tile[rr][c0 + 2 * h + 1] : 0.0, e, w);
 #pragma unroll
-        for (int p = 0; p < S; ++p) {
-            const uint32_t b = int_to_bf16_bits(d[p]);
-            if (j & 1) packed[p][j >> 1] |= b << 16;
-            else packed[p][j >> 1] = b;
-        }
+        for (int p = 0; p < S; ++p) packed[p][h] = w[p];
     }
 #pragma unroll
     for (int p = 0; p < S; ++p) {
@@ -1191,15 +1198,11 @@ __device__ __forceinline__ void oz_split_unit(const double* __restrict__ R, int6
         if (kb + 1 < nkb) fetch(kb + 1);
         uint32_t packed[S][4];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            int d[S];
-            oz_digits<S>(live ? tile[rr][c0 + j] : 0.0, e, d);
+        for (int h = 0; h < 4; ++h) {
+            uint32_t w[S];
+            oz_digits_bf16x2<S>(live ? tile[rr][c0 + 2 * h] : 0.0, live ? tile[rr][c0 + 2 * h + 1] : 0.0, e, w);
 #pragma unroll
-            for (int p = 0; p < S; ++p) {
-                const uint32_t b = int_to_bf16_bits(d[p]);
-                if (j & 1) packed[p][j >> 1] |= b << 16;
-                else packed[p][j >> 1] = b;
-            }
+            for (int p = 0; p < S; ++p) packed[p][h] = w[p];
         }
 #pragma unroll
         for (int p = 0; p < S; ++p) store(p, kb, rr, c0, make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]));
