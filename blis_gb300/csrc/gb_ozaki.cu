@@ -87,6 +87,12 @@ struct OzItem {
 // of B = 32 KB, contiguous, the layout a 128-byte-swizzled TMA box expects),
 // so one 3-D tensor map per operand serves all problems; a box is addressed
 // by its index alone.  Level sums go to per-problem planes [level][n][ld].
+// A problem whose C is taller than wide can cover fewer 128 x 256 tiles as
+// C^T = op(B)^T op(A)^T; `swap` marks that form.  a, b, m, n, k, the tiles,
+// boxes, split units and exponents then describe the product that runs
+// (its "A" is op(B)^T), while c, rs_c, cs_c, ld and the level planes keep
+// C's own orientation, so the recombination reads and writes as for any
+// other problem.  The digit products are the same either way: bit-identical.
 struct OzBatchProb {
     const double* a;
     int64_t ars, acs;  // rows of op(A): (i, l) at a[i*ars + l*acs]
@@ -96,11 +102,11 @@ struct OzBatchProb {
     int64_t rs_c, cs_c;
     double alpha, beta;
     int64_t m, n, k;
-    int32_t tiles_m, tiles_n, kb, pad0;
+    int32_t tiles_m, tiles_n, kb, swap;
     int32_t* ea;  // row exponents of op(A), op(B)^T
     int32_t* eb;
     int64_t abox, bbox;  // first box of this problem in one slice plane
-    int32_t* planes;     // [level][n][ld], ld = m rounded up to 4
+    int32_t* planes;     // [level][columns of C][ld], ld = rows of C rounded up to 4
     int64_t ld;
     int64_t units_a;     // split units (32-row blocks) of op(A); op(B)^T's follow
 };
@@ -280,11 +286,26 @@ __device__ __forceinline__ void oz_store_sums(const OzBatchParams& p, const OzIt
     const int64_t i = (int64_t)w.tm * OZ_BM + quad * 32 + lane;
     const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
     if (i >= q.m) return;
-    int32_t* dst = q.planes + ((int64_t)w.plane * q.n + j0) * q.ld + i;
     const int64_t jn = q.n - j0;  // columns of this half that exist
+    if (!q.swap) {
+        int32_t* dst = q.planes + ((int64_t)w.plane * q.n + j0) * q.ld + i;
 #pragma unroll
-    for (int c = 0; c < 128; ++c)
-        if (c < jn) dst[(int64_t)c * q.ld] = acc[c];
+        for (int c = 0; c < 128; ++c)
+            if (c < jn) dst[(int64_t)c * q.ld] = acc[c];
+    } else {
+        // row i of the product is column i of C: the thread's 128 sums are contiguous in the
+        // plane (j0 and ld are multiples of 4, so 16-byte stores)
+        int32_t* dst = q.planes + ((int64_t)w.plane * q.m + i) * q.ld + j0;
+        if (jn >= 128) {
+#pragma unroll
+            for (int c = 0; c < 128; c += 4)
+                *reinterpret_cast<int4*>(dst + c) = make_int4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 128; ++c)
+                if (c < jn) dst[c] = acc[c];
+        }
+    }
 }
 
 // ---------------------------------------------------------------- BF16 GEMM
@@ -1271,28 +1292,32 @@ __global__ void __launch_bounds__(256) oz_recombine_batch_kernel(const OzBatchPr
     if (*skip) return;
     const int pi = block_prob[blockIdx.x];
     const OzBatchProb& q = probs[pi];
-    const int64_t mq = (q.m + 3) >> 2;
+    // C's own orientation (see OzBatchProb)
+    const int64_t m = q.swap ? q.n : q.m, n = q.swap ? q.m : q.n;
+    const int32_t* ea = q.swap ? q.eb : q.ea;
+    const int32_t* eb = q.swap ? q.ea : q.eb;
+    const int64_t mq = (m + 3) >> 2;
     const int64_t e = ((int64_t)blockIdx.x - block_base[pi]) * 256 + threadIdx.x;
-    if (e >= mq * q.n) return;
+    if (e >= mq * n) return;
     const int64_t j = e / mq, i0 = (e - j * mq) * 4;
-    const int64_t plane_stride = q.n * q.ld;
+    const int64_t plane_stride = n * q.ld;
     const int32_t* src = q.planes + j * q.ld + i0;  // ld is a multiple of 4: 16-byte aligned
     int4 v[S];
 #pragma unroll
     for (int L = 0; L < S; ++L) v[L] = __ldcs(reinterpret_cast<const int4*>(src + (int64_t)L * plane_stride));
     const bool plain = (q.alpha == 1.0 && q.beta == 0.0);
-    const int ebj = q.eb[j] - 8 * (S + 1);
+    const int ebj = eb[j] - 8 * (S + 1);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         const int64_t i = i0 + r;
-        if (i >= q.m) break;
+        if (i >= m) break;
         __int128 T = 0;
 #pragma unroll
         for (int L = S - 1; L >= 0; --L) {
             const int x = (r == 0) ? v[L].x : (r == 1) ? v[L].y : (r == 2) ? v[L].z : v[L].w;
             T = (T << 8) + (__int128)x;
         }
-        const double ab = round_scaled(T, q.ea[i] + ebj);
+        const double ab = round_scaled(T, ea[i] + ebj);
         double* cij = q.c + i * q.rs_c + j * q.cs_c;
         if (plain) {
             *cij = ab;
@@ -1356,6 +1381,18 @@ int group_m_setting()
         const char* e = getenv("GB_OZAKI_GROUP_M");
         const int g = e ? atoi(e) : OZ_GROUP_M;
         v = (g >= 1 && g <= 64) ? g : OZ_GROUP_M;
+    }
+    return v;
+}
+
+// Whether the grouped form may run a problem as C^T (GB_OZAKI_BATCH_ORIENT,
+// default 1; 0 keeps every problem as given).
+int ozaki_batch_orient_setting()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("GB_OZAKI_BATCH_ORIENT");
+        v = e ? (atoi(e) != 0) : 1;
     }
     return v;
 }
@@ -1832,25 +1869,33 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
             return set_error(GB_ERR_ARG, "ozaki batch", "problem not eligible for the grouped form");
         const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
         OzBatchProb q = {};
-        q.a = static_cast<const double*>(p.a);
-        q.ars = ta ? p.lda : 1;
-        q.acs = ta ? 1 : p.lda;
-        q.b = static_cast<const double*>(p.b);
-        q.brs = tb ? 1 : p.ldb;  // rows of op(B)^T are columns of op(B)
-        q.bcs = tb ? p.ldb : 1;
+        const double* pa = static_cast<const double*>(p.a);
+        const int64_t ars = ta ? p.lda : 1, acs = ta ? 1 : p.lda;
+        const double* pb = static_cast<const double*>(p.b);
+        const int64_t brs = tb ? 1 : p.ldb, bcs = tb ? p.ldb : 1;  // rows of op(B)^T are columns of op(B)
+        // tiles covered as C and as C^T; the transposed form when it needs fewer
+        const int64_t cover = ((p.m + OZ_BM - 1) / OZ_BM) * ((p.n + OZ_BN - 1) / OZ_BN);
+        const int64_t cover_t = ((p.n + OZ_BM - 1) / OZ_BM) * ((p.m + OZ_BN - 1) / OZ_BN);
+        q.swap = (cover_t < cover && ozaki_batch_orient_setting()) ? 1 : 0;
+        q.a = q.swap ? pb : pa;
+        q.ars = q.swap ? brs : ars;
+        q.acs = q.swap ? bcs : acs;
+        q.b = q.swap ? pa : pb;
+        q.brs = q.swap ? ars : brs;
+        q.bcs = q.swap ? acs : bcs;
         q.c = static_cast<double*>(p.c);
         q.rs_c = 1;
         q.cs_c = p.ldc;
         q.alpha = p.alpha;
         q.beta = p.beta;
-        q.m = p.m;
-        q.n = p.n;
+        q.m = q.swap ? p.n : p.m;
+        q.n = q.swap ? p.m : p.n;
         q.k = p.k;
-        q.tiles_m = (int32_t)((p.m + OZ_BM - 1) / OZ_BM);
-        q.tiles_n = (int32_t)((p.n + OZ_BN - 1) / OZ_BN);
         q.kb = (int32_t)((p.k + OZ_BK - 1) / OZ_BK);
-        q.units_a = (p.m + 31) / 32;  // 32-row blocks holding rows of op(A); the padding is zeroed once
-        q.ld = round_up(p.m, 4);
+        q.tiles_m = (int32_t)((q.m + OZ_BM - 1) / OZ_BM);
+        q.tiles_n = (int32_t)((q.n + OZ_BN - 1) / OZ_BN);
+        q.units_a = (q.m + 31) / 32;  // 32-row blocks holding rows of op(A); the padding is zeroed once
+        q.ld = round_up(p.m, 4);      // rows of C
         h.push_back(q);
     }
     // longest k first: the last items handed out are the cheapest
@@ -1885,7 +1930,7 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
         q.bbox = ob->boxes_b;
         ob->boxes_a += (int64_t)q.tiles_m * q.kb;
         ob->boxes_b += (int64_t)q.tiles_n * q.kb;
-        planes_elems += (int64_t)slices * q.n * q.ld;
+        planes_elems += (int64_t)slices * (q.swap ? q.m : q.n) * q.ld;
         exps += q.m + q.n;
         const int64_t it = (int64_t)slices * q.tiles_m * q.tiles_n;
         item_base.push_back(ob->items);
@@ -1895,7 +1940,8 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
         unit_base.push_back(ob->units);
         unit_prob.insert(unit_prob.end(), (size_t)un, i);
         ob->units += un;
-        const int64_t rb = (((q.m + 3) / 4) * q.n + 255) / 256;
+        const int64_t mc = q.swap ? q.n : q.m, nc = q.swap ? q.m : q.n;  // C's rows and columns
+        const int64_t rb = (((mc + 3) / 4) * nc + 255) / 256;
         rblock_base.push_back(ob->rblocks);
         rblock_prob.insert(rblock_prob.end(), (size_t)rb, i);
         ob->rblocks += rb;
@@ -1937,7 +1983,7 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
     int64_t pl_off = 0, ex_off = 0;
     for (auto& q : h) {
         q.planes = planes + pl_off;
-        pl_off += (int64_t)slices * q.n * q.ld;
+        pl_off += (int64_t)slices * (q.swap ? q.m : q.n) * q.ld;
         q.ea = ex + ex_off;
         q.eb = q.ea + q.m;
         ex_off += q.m + q.n;

@@ -92,9 +92,11 @@ def _single_ozaki(gblib, batch, slices):
 
 @pytest.mark.parametrize("slices", [5, 8])
 def test_grouped_ozaki_bit_identical_to_single_calls_and_model(gblib, slices):
-    # k = 0, alpha = 0 and m = 0 problems; k = 17000 exceeds one exact part at 8 slices
+    # k = 0, alpha = 0 and m = 0 problems; k = 17000 exceeds one exact part at 8 slices; tall C
+    # (fewer tiles as C^T: the grouped form runs op(B)^T op(A)^T, a partial last column half)
     extra = [(7, 9, 0, 0, 0, 1.0, 0.5), (5, 4, 30, 1, 0, 0.0, 0.5), (0, 3, 5, 0, 0, 1.0, 0.0),
-             (5, 6, 17000, 0, 1, 1.0, 0.0), (300, 260, 1024, 1, 1, 1.0, 0.0)]
+             (5, 6, 17000, 0, 1, 1.0, 0.0), (300, 260, 1024, 1, 1, 1.0, 0.0),
+             (1000, 40, 300, 1, 0, -0.5, 0.5), (600, 129, 70, 0, 1, 1.0, 0.0)]
     batch = Batch(_shapes(11, 40, extra), 1000)
     blas.set_dgemm_mode(blas.DGEMM_OZAKI, slices)
     try:
@@ -107,7 +109,7 @@ def test_grouped_ozaki_bit_identical_to_single_calls_and_model(gblib, slices):
         assert np.array_equal(g, s), i
         assert np.array_equal(l, s), i
     # the CPU model of the same arithmetic, on a subset (it is a scalar loop)
-    for i in list(range(0, 40, 7)) + [41, 43, 44]:
+    for i in list(range(0, 40, 7)) + [41, 43, 44, 45, 46]:
         m, n, k, ta, tb, al, be = batch.shapes[i]
         a, b, c = batch.host[i]
         ref = np.asfortranarray(c.copy())
