@@ -1023,6 +1023,30 @@ __global__ void __launch_bounds__(256) oz_split_kernel(int64_t rows, int64_t k, 
 }
 
 // ---------------------------------------------------------------- recombine
+// T = sum_L a_L 2^(8L), the exact weighted sum of the level sums.  Four
+// levels make a group that is exact in 64 bits (|a_L| < 2^31 P for P k parts:
+// |group| < 2^(55.01) P, below 2^63 for P <= 64); for 32-bit a_L each term is
+// one 32 x 32 -> 64-bit multiply-add, and only one 128-bit shift and add per
+// group remains (against one of each per level in a 128-bit Horner loop).
+template <int S, typename A>
+__device__ __forceinline__ __int128 oz_weighted_sum(const A (&a)[S])
+{
+    constexpr int G = (S + 3) / 4;
+    long long g[G];
+#pragma unroll
+    for (int gi = 0; gi < G; ++gi) {
+        long long v = 0;
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            if (4 * gi + t < S) v += (long long)a[4 * gi + t] * (1ll << (8 * t));
+        g[gi] = v;
+    }
+    __int128 T = g[G - 1];
+#pragma unroll
+    for (int gi = G - 2; gi >= 0; --gi) T = (__int128)((unsigned __int128)T << 32) + g[gi];
+    return T;
+}
+
 // RNE(T * 2^E) from integers only, as IEEE bits.
 __device__ __forceinline__ double round_scaled(__int128 T, int E)
 {
@@ -1090,12 +1114,18 @@ struct OzRecombParams {
 // T = sum_l S_l 2^(8(s+1-l)) is formed by Horner from the most significant
 // level (l = 2, last in the table) and rounded once.
 template <int S>
-__global__ void __launch_bounds__(256) oz_recombine_kernel(const __grid_constant__ OzRecombParams p)
+__global__ void __launch_bounds__(256, (S <= 7 ? 3 : 2)) oz_recombine_kernel(const __grid_constant__ OzRecombParams p)
 {
     if (*p.skip) return;
     const int64_t mq = (p.m + 3) >> 2;
     const int64_t total = mq * p.n;
     const bool plain = (p.alpha == 1.0 && p.beta == 0.0);
+    bool one_part = true, few_parts = true;  // the level sums fit 32 bits / the groups fit 64 bits
+#pragma unroll
+    for (int L = 0; L < S; ++L) {
+        one_part = one_part && p.lv[L].nparts == 1;
+        few_parts = few_parts && p.lv[L].nparts <= 64;
+    }
     const int64_t plane_stride = p.npad * p.mpad;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -1127,8 +1157,20 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const __grid_constant
             const int64_t i = i0 + r;
             if (i >= p.m) break;
             __int128 T = 0;
+            if (one_part) {
+                int a[S];
 #pragma unroll
-            for (int L = S - 1; L >= 0; --L) T = (T << 8) + (__int128)acc[L][r];
+                for (int L = 0; L < S; ++L) a[L] = (int)acc[L][r];
+                T = oz_weighted_sum<S>(a);
+            } else if (few_parts) {
+                long long a[S];
+#pragma unroll
+                for (int L = 0; L < S; ++L) a[L] = acc[L][r];
+                T = oz_weighted_sum<S>(a);
+            } else {
+#pragma unroll
+                for (int L = S - 1; L >= 0; --L) T = (__int128)((unsigned __int128)T << 8) + (__int128)acc[L][r];
+            }
             const double ab = round_scaled(T, p.ea[i] + ebj);
             double* cij = p.c + i * p.rs_c + j * p.cs_c;
             if (plain) {
@@ -1311,12 +1353,10 @@ __global__ void __launch_bounds__(256) oz_recombine_batch_kernel(const OzBatchPr
     for (int r = 0; r < 4; ++r) {
         const int64_t i = i0 + r;
         if (i >= m) break;
-        __int128 T = 0;
+        int a[S];
 #pragma unroll
-        for (int L = S - 1; L >= 0; --L) {
-            const int x = (r == 0) ? v[L].x : (r == 1) ? v[L].y : (r == 2) ? v[L].z : v[L].w;
-            T = (T << 8) + (__int128)x;
-        }
+        for (int L = 0; L < S; ++L) a[L] = (r == 0) ? v[L].x : (r == 1) ? v[L].y : (r == 2) ? v[L].z : v[L].w;
+        const __int128 T = oz_weighted_sum<S>(a);
         const double ab = round_scaled(T, ea[i] + ebj);
         double* cij = q.c + i * q.rs_c + j * q.cs_c;
         if (plain) {
