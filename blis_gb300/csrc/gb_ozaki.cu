@@ -852,19 +852,22 @@ __global__ void oz_rowmax_rows_kernel(int64_t rows, int64_t k, const double* __r
     if (r >= rows) return;
     const int64_t l0 = (int64_t)blockIdx.y * kchunk;
     const int64_t l1 = (l0 + kchunk < k) ? l0 + kchunk : k;
-    unsigned long long m0 = 0, m1 = 0;
+    // eight loads in flight per thread (one HBM round trip hides behind about 40 KB per SM)
+    unsigned long long mq[4] = {0, 0, 0, 0};
     int64_t l = l0;
-    for (; l + 1 < l1; l += 2) {
-        const unsigned long long b0 = abs_bits(__ldcs(R + r + l * sl));
-        const unsigned long long b1 = abs_bits(__ldcs(R + r + (l + 1) * sl));
-        m0 = b0 > m0 ? b0 : m0;
-        m1 = b1 > m1 ? b1 : m1;
+    for (; l + 7 < l1; l += 8) {
+        unsigned long long b[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) b[u] = abs_bits(__ldcs(R + r + (l + u) * sl));
+#pragma unroll
+        for (int u = 0; u < 8; ++u) mq[u & 3] = b[u] > mq[u & 3] ? b[u] : mq[u & 3];
     }
-    if (l < l1) {
+    for (; l < l1; ++l) {
         const unsigned long long b0 = abs_bits(__ldcs(R + r + l * sl));
-        m0 = b0 > m0 ? b0 : m0;
+        mq[0] = b0 > mq[0] ? b0 : mq[0];
     }
-    const unsigned long long mx = m0 > m1 ? m0 : m1;
+    const unsigned long long m01 = mq[0] > mq[1] ? mq[0] : mq[1], m23 = mq[2] > mq[3] ? mq[2] : mq[3];
+    const unsigned long long mx = m01 > m23 ? m01 : m23;
     if (mx) atomicMax(maxbits + r, mx);
 }
 
@@ -878,11 +881,23 @@ __global__ void oz_rowmax_warp_kernel(int64_t rows, int64_t k, const double* __r
     if (r >= rows) return;
     const int64_t l0 = (int64_t)blockIdx.y * kchunk;
     const int64_t l1 = (l0 + kchunk < k) ? l0 + kchunk : k;
-    unsigned long long mx = 0;
-    for (int64_t l = l0 + lane; l < l1; l += 32) {
+    unsigned long long mx = 0, my = 0;
+    int64_t l = l0 + lane;
+    for (; l + 32 * 7 < l1; l += 32 * 8) {  // eight loads in flight per lane
+        unsigned long long b[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) b[u] = abs_bits(__ldcs(R + r * sr + (l + 32 * u) * sl));
+#pragma unroll
+        for (int u = 0; u < 8; u += 2) {
+            mx = b[u] > mx ? b[u] : mx;
+            my = b[u + 1] > my ? b[u + 1] : my;
+        }
+    }
+    for (; l < l1; l += 32) {
         const unsigned long long b = abs_bits(__ldcs(R + r * sr + l * sl));
         mx = b > mx ? b : mx;
     }
+    mx = my > mx ? my : mx;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
