@@ -12,6 +12,8 @@
 #include <ctype.h>
 #include <string.h>
 
+#include <vector>
+
 #include "gb_internal.h"
 
 namespace gb {
@@ -195,6 +197,112 @@ int ozaki_host_pipelined(int transa, int64_t m, int64_t n, int64_t k, double alp
     return rc ? rc : rc2;
 }
 
+// The same with op(A) in row blocks too, for a column-major stored A
+// (rs_a == 1): row block 0 of A and column block 0 of op(B) go up first, the
+// first slice GEMM starts after them, and the other blocks of A arrive (and
+// are split) while it runs; every (row block, column block) of C is one
+// slice GEMM and goes back as soon as it is recombined.  Only about a
+// quarter of A and of one op(B) block, and one C block, are not overlapped
+// with compute.  Rows and columns are split independently: bit-identical to
+// one call.
+int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double alpha, const double* a,
+                            int64_t lda, const double* b, int64_t ldb, double beta, double* c, int64_t ldc,
+                            int slices, int nch, const char* where)
+{
+    cudaStream_t s = thread_stream(), cin = thread_copy_stream(0), cout = thread_copy_stream(1);
+    const bool ta = GB_IS_TRANS(transa);
+    // op(A) on the device: m x k column-major (ars 1, acs m), or for op(A) = A^T the stored k x m
+    // column-major A (ars k, acs 1)
+    double* ad = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(m * k), s));
+    double* bd = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(k * n), s));
+    double* cd = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(m * n), s));
+    int rc = (ad && bd && cd) ? GB_SUCCESS : GB_ERR_NOMEM;
+    OzA prep;
+    if (!rc) rc = ozaki_alloc_a(m, k, ad, ta ? k : 1, ta ? 1 : m, slices, s, &prep);
+    // row blocks on the slice GEMM's row tile
+    const int nra = (m >= 8 * prep.row_tile) ? 4 : ((m >= 2 * prep.row_tile) ? 2 : 1);
+    std::vector<int64_t> rb(1, 0);
+    for (int i = 1; i < nra && !rc; ++i) {
+        const int64_t r = (m * i / nra + prep.row_tile - 1) / prep.row_tile * prep.row_tile;
+        if (r > rb.back() && r < m) rb.push_back(r);
+    }
+    rb.push_back(m);
+    const int na = (int)rb.size() - 1;
+    std::vector<cudaEvent_t> ev((size_t)(na + nch + na * nch + 3));
+    for (auto& e : ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    cudaEvent_t* ev_a = ev.data();
+    cudaEvent_t* ev_b = ev_a + na;
+    cudaEvent_t* ev_c = ev_b + nch;
+    cudaEvent_t ev_alloc = ev_c[na * nch], ev_in_done = ev_c[na * nch + 1], ev_out_done = ev_c[na * nch + 2];
+    auto col0 = [&](int j) { return n * j / nch; };
+    if (!rc) {
+        // copies start after the stream-ordered allocations; A's block 0 and op(B)'s block 0 first
+        cudaEventRecord(ev_alloc, s);
+        cudaStreamWaitEvent(cin, ev_alloc, 0);
+        cudaStreamWaitEvent(cout, ev_alloc, 0);
+        auto copy_a = [&](int i) {
+            const int64_t r0 = rb[i], rows = rb[i + 1] - rb[i];
+            if (!rc)
+                rc = ta ? check_cuda(cudaMemcpy2DAsync(ad + r0 * k, k * sizeof(double), a + r0 * lda,
+                                                       lda * sizeof(double), k * sizeof(double), rows,
+                                                       cudaMemcpyDefault, cin), "A block")
+                        : check_cuda(cudaMemcpy2DAsync(ad + r0, m * sizeof(double), a + r0, lda * sizeof(double),
+                                                       rows * sizeof(double), k, cudaMemcpyDefault, cin), "A block");
+            cudaEventRecord(ev_a[i], cin);
+        };
+        auto copy_b = [&](int j) {
+            const int64_t j0 = col0(j), nj = col0(j + 1) - j0;
+            if (!rc)
+                rc = check_cuda(cudaMemcpy2DAsync(bd + j0 * k, k * sizeof(double), b + j0 * ldb, ldb * sizeof(double),
+                                                  k * sizeof(double), nj, cudaMemcpyDefault, cin), "B block");
+            if (!rc && beta != 0.0)
+                rc = check_cuda(cudaMemcpy2DAsync(cd + j0 * m, m * sizeof(double), c + j0 * ldc, ldc * sizeof(double),
+                                                  m * sizeof(double), nj, cudaMemcpyDefault, cin), "C block");
+            cudaEventRecord(ev_b[j], cin);
+        };
+        copy_a(0);
+        copy_b(0);
+        for (int i = 1; i < na; ++i) copy_a(i);
+        for (int j = 1; j < nch; ++j) copy_b(j);
+        for (int j = 0; j < nch && !rc; ++j) {
+            const int64_t j0 = col0(j), nj = col0(j + 1) - j0;
+            OzB pb;
+            cudaStreamWaitEvent(s, ev_b[j], 0);
+            if (j == 0) cudaStreamWaitEvent(s, ev_a[0], 0);
+            if (j == 0) rc = ozaki_split_a_rows(&prep, rb[0], rb[1], s);
+            if (!rc) rc = ozaki_prepare_b(&prep, nj, bd + j0 * k, 1, k, s, &pb);
+            if (rc) break;
+            for (int i = 0; i < na && !rc; ++i) {
+                const int64_t r0 = rb[i], rows = rb[i + 1] - rb[i];
+                if (j == 0 && i > 0) {
+                    cudaStreamWaitEvent(s, ev_a[i], 0);
+                    rc = ozaki_split_a_rows(&prep, r0, rb[i + 1], s);
+                }
+                if (!rc) rc = ozaki_multiply_rows(&prep, r0, rows, &pb, alpha, beta, cd + j0 * m + r0, 1, m, s);
+                cudaEventRecord(ev_c[i * nch + j], s);
+                cudaStreamWaitEvent(cout, ev_c[i * nch + j], 0);
+                if (!rc)
+                    rc = check_cuda(cudaMemcpy2DAsync(c + j0 * ldc + r0, ldc * sizeof(double), cd + j0 * m + r0,
+                                                      m * sizeof(double), rows * sizeof(double), nj,
+                                                      cudaMemcpyDefault, cout), "C back");
+            }
+            ozaki_release_b(&pb, s);
+        }
+        // frees below are ordered after every copy on either copy stream
+        cudaEventRecord(ev_in_done, cin);
+        cudaEventRecord(ev_out_done, cout);
+        cudaStreamWaitEvent(s, ev_in_done, 0);
+        cudaStreamWaitEvent(s, ev_out_done, 0);
+    }
+    ozaki_release_a(&prep, s);
+    dev_free(ad, s);
+    dev_free(bd, s);
+    dev_free(cd, s);
+    const int rc2 = finish(s, where);
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc ? rc : rc2;
+}
+
 template <typename T>
 int gemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, T alpha, const T* a,
               int64_t rs_a, int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, T beta, T* c,
@@ -209,6 +317,10 @@ int gemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, T alpha, 
         // large products with a fixed slice count, column-major op(B) and C: the transfers
         // of op(B) and C overlap the compute
         const int nch = (n >= 8192) ? 4 : 2;
+        if (rs_a == 1 && cs_a >= (GB_IS_TRANS(transa) ? k : m))
+            return ozaki_host_pipelined_2d(transa, m, n, k, (double)alpha, (const double*)a, cs_a,
+                                           (const double*)b, cs_b, (double)beta, (double*)c, cs_c, ozaki_slices(),
+                                           nch, where);
         return ozaki_host_pipelined(transa, m, n, k, (double)alpha, (const double*)a, rs_a, cs_a, (const double*)b,
                                     cs_b, (double)beta, (double*)c, cs_c, ozaki_slices(), nch, where);
     }

@@ -107,6 +107,7 @@ int64_t ozaki_kpart_limit(int slices);
 struct OzA {
     int slices = 0;
     bool pair_form = false;
+    int64_t row_tile = 0;       // rows of one slice GEMM output tile (256 for CTA pairs, 128 else)
     int64_t m = 0, k = 0, mpad = 0, kpad = 0;
     const double* a = nullptr;  // op(A) (i, l) = a[i*ars + l*acs], kept for the IEEE fallback
     int64_t ars = 0, acs = 0;
@@ -116,8 +117,24 @@ struct OzA {
     int32_t* ea = nullptr;
     int* nonfinite = nullptr;
 };
+struct OzB {
+    int64_t n = 0, npad = 0;
+    const double* b = nullptr;  // op(B) (l, j) = b[l*brs + j*bcs], kept for the IEEE fallback
+    int64_t brs = 0, bcs = 0;
+    uint8_t* ws = nullptr;      // slices, column maxima, exponents
+    uint16_t* sb = nullptr;
+    unsigned long long* maxb = nullptr;
+    int32_t* eb = nullptr;
+};
+int ozaki_alloc_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t acs, int slices, cudaStream_t s,
+                  OzA* A);
+int ozaki_split_a_rows(const OzA* A, int64_t r0, int64_t r1, cudaStream_t s);
 int ozaki_prepare_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t acs, int slices,
                     cudaStream_t s, OzA* A);
+int ozaki_prepare_b(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, cudaStream_t s, OzB* B);
+void ozaki_release_b(OzB* B, cudaStream_t s);
+int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, double alpha, double beta, double* c,
+                        int64_t rs_c, int64_t cs_c, cudaStream_t s);
 int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, double alpha,
                    double beta, double* c, int64_t rs_c, int64_t cs_c, cudaStream_t s);
 void ozaki_release_a(OzA* A, cudaStream_t s);

@@ -1410,13 +1410,17 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
+// Slice planes [slice][plane_rows][kpad] bf16 as a 3-D tensor map of rpad
+// rows from base (rows r0 .. r0 + rpad of the planes when base is offset by
+// r0 rows); plane_rows = 0 means rpad.
 int make_slice_map(CUtensorMap* map, const void* base, int64_t kpad, int64_t rpad, int slices,
-                   int box_rows)
+                   int box_rows, int64_t plane_rows = 0)
 {
     auto fn = encode_fn();
     if (!fn) return set_error(GB_ERR_CUDA, "ozaki", "cuTensorMapEncodeTiled unavailable");
+    if (plane_rows <= 0) plane_rows = rpad;
     cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rpad, (cuuint64_t)slices};
-    cuuint64_t strides[2] = {(cuuint64_t)(kpad * 2), (cuuint64_t)(rpad * kpad * 2)};
+    cuuint64_t strides[2] = {(cuuint64_t)(kpad * 2), (cuuint64_t)(plane_rows * kpad * 2)};
     cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
@@ -1488,23 +1492,26 @@ int set_ozaki_ctas(int ctas)
 
 namespace {
 
+// The split launchers take the slice planes' row stride (rpad) apart from
+// the rows they cover (rcover, a multiple of 32): a block of rows r0.. of a
+// larger operand is split by passing R, mb, out and ex offset to row r0.
 template <int S>
 void launch_split(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl,
-                  const unsigned long long* mb, int64_t rpad, int64_t kpad, uint16_t* out, int32_t* ex,
-                  int* nonfinite, cudaStream_t s)
+                  const unsigned long long* mb, int64_t rpad, int64_t rcover, int64_t kpad, uint16_t* out,
+                  int32_t* ex, int* nonfinite, cudaStream_t s)
 {
     LaunchScope ls("oz_split", s);
-    oz_split_kernel<S><<<dim3((unsigned)(kpad / 64), (unsigned)(rpad / 32)), 256, 0, s>>>(
+    oz_split_kernel<S><<<dim3((unsigned)(kpad / 64), (unsigned)(rcover / 32)), 256, 0, s>>>(
         rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite);
 }
 
 void split_dispatch(int slices, int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl,
-                    const unsigned long long* mb, int64_t rpad, int64_t kpad, uint16_t* out, int32_t* ex,
-                    int* nonfinite, cudaStream_t s)
+                    const unsigned long long* mb, int64_t rpad, int64_t rcover, int64_t kpad, uint16_t* out,
+                    int32_t* ex, int* nonfinite, cudaStream_t s)
 {
     switch (slices) {
 #define GB_SPLIT_CASE(S) \
-    case S: launch_split<S>(rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, s); break;
+    case S: launch_split<S>(rows, k, R, sr, sl, mb, rpad, rcover, kpad, out, ex, nonfinite, s); break;
         GB_SPLIT_CASE(2) GB_SPLIT_CASE(3) GB_SPLIT_CASE(4) GB_SPLIT_CASE(5) GB_SPLIT_CASE(6)
         GB_SPLIT_CASE(7) GB_SPLIT_CASE(8) GB_SPLIT_CASE(9) GB_SPLIT_CASE(10) GB_SPLIT_CASE(11)
         GB_SPLIT_CASE(12)
@@ -1532,25 +1539,28 @@ int64_t fused_split_max_k()
 
 template <int S>
 void launch_split_rows(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl, int64_t rpad,
-                       int64_t kpad, uint16_t* out, int32_t* ex, int* nonfinite, cudaStream_t s)
+                       int64_t rcover, int64_t kpad, uint16_t* out, int32_t* ex, int* nonfinite, cudaStream_t s)
 {
     LaunchScope ls("oz_split_rows", s);
-    oz_split_rows_kernel<S><<<(unsigned)(rpad / 32), 256, 0, s>>>(rows, k, R, sr, sl, rpad, kpad, out, ex, nonfinite);
+    oz_split_rows_kernel<S><<<(unsigned)(rcover / 32), 256, 0, s>>>(rows, k, R, sr, sl, rpad, kpad, out, ex,
+                                                                     nonfinite);
 }
 
 void launch_rowmax(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl, unsigned long long* mb,
                    cudaStream_t s);
 
-// Row maxima and digit slices of one row operand: fused for small k, else
-// the row-maximum kernel into mb (zeroed here) and the tiled split.
+// Row maxima and digit slices of one row operand (or of rows r0.. of one,
+// with R, mb, out and ex offset to row r0 and rcover rows covered): fused
+// for small k, else the row-maximum kernel into mb (zeroed here) and the
+// tiled split.
 void split_operand(int slices, int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl,
-                   unsigned long long* mb, int64_t rpad, int64_t kpad, uint16_t* out, int32_t* ex, int* nonfinite,
-                   cudaStream_t s)
+                   unsigned long long* mb, int64_t rpad, int64_t rcover, int64_t kpad, uint16_t* out, int32_t* ex,
+                   int* nonfinite, cudaStream_t s)
 {
-    if (k <= fused_split_max_k() && rpad / 32 <= INT32_MAX) {
+    if (k <= fused_split_max_k() && rcover / 32 <= INT32_MAX) {
         switch (slices) {
 #define GB_SPLIT_CASE(S) \
-    case S: launch_split_rows<S>(rows, k, R, sr, sl, rpad, kpad, out, ex, nonfinite, s); break;
+    case S: launch_split_rows<S>(rows, k, R, sr, sl, rpad, rcover, kpad, out, ex, nonfinite, s); break;
             GB_SPLIT_CASE(2) GB_SPLIT_CASE(3) GB_SPLIT_CASE(4) GB_SPLIT_CASE(5) GB_SPLIT_CASE(6)
             GB_SPLIT_CASE(7) GB_SPLIT_CASE(8) GB_SPLIT_CASE(9) GB_SPLIT_CASE(10) GB_SPLIT_CASE(11)
             GB_SPLIT_CASE(12)
@@ -1561,7 +1571,7 @@ void split_operand(int slices, int64_t rows, int64_t k, const double* R, int64_t
     }
     cudaMemsetAsync(mb, 0, sizeof(unsigned long long) * rows, s);
     launch_rowmax(rows, k, R, sr, sl, mb, s);
-    split_dispatch(slices, rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, s);
+    split_dispatch(slices, rows, k, R, sr, sl, mb, rpad, rcover, kpad, out, ex, nonfinite, s);
 }
 
 }  // namespace
@@ -1656,8 +1666,10 @@ int slice_gemm_setup(int* max_pairs)
 // Phase 1 of the Ozaki form: row maxima, exponents and digit slices of op(A)
 // (element (i, l) = a[i*ars + l*acs]), kept in HBM for any number of
 // multiplications.  The Inf/NaN flag lives here and is shared by them.
-int ozaki_prepare_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t acs, int slices,
-                    cudaStream_t s, OzA* A)
+// ozaki_alloc_a sets up the arena; ozaki_split_a_rows splits a block of rows
+// (several blocks may be split as they arrive); ozaki_prepare_a does both.
+int ozaki_alloc_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t acs, int slices, cudaStream_t s,
+                  OzA* A)
 {
     *A = OzA();
     if (slices < 2 || slices > OZ_MAX_SLICES)
@@ -1665,12 +1677,12 @@ int ozaki_prepare_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t 
     if (ozaki_t_bound_log2(slices, k) >= 126.0)
         return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices and k exceed the 128-bit recombination range");
     A->pair_form = (ozaki_ctas_setting() == 2);
-    const int64_t row_tile = A->pair_form ? 2 * OZ2_ROWS : OZ_BM;
+    A->row_tile = A->pair_form ? 2 * OZ2_ROWS : OZ_BM;
     A->slices = slices;
     A->m = m;
     A->k = k;
     A->kpad = round_up(k, OZ_BK);
-    A->mpad = round_up(m, row_tile);
+    A->mpad = round_up(m, A->row_tile);
     if (A->mpad > INT32_MAX || A->kpad > INT32_MAX)
         return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "dimension too large for TMA coordinates");
     A->a = a;
@@ -1684,13 +1696,28 @@ int ozaki_prepare_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t 
     A->maxa = reinterpret_cast<unsigned long long*>(A->ws + bytes_sa);
     A->ea = reinterpret_cast<int32_t*>(A->maxa + m);
     A->nonfinite = reinterpret_cast<int*>(A->ea + m);
-    int rc;
-    if ((rc = check_cuda(cudaMemsetAsync(A->nonfinite, 0, sizeof(int), s), "memset"))) {
-        ozaki_release_a(A, s);
-        return rc;
-    }
-    split_operand(slices, m, k, a, ars, acs, A->maxa, A->mpad, A->kpad, A->sa, A->ea, A->nonfinite, s);
-    if ((rc = check_cuda(cudaGetLastError(), "oz_split"))) ozaki_release_a(A, s);
+    const int rc = check_cuda(cudaMemsetAsync(A->nonfinite, 0, sizeof(int), s), "memset");
+    if (rc) ozaki_release_a(A, s);
+    return rc;
+}
+
+// Rows [r0, r1) of op(A); r0 a multiple of the row tile, r1 one too or m.
+int ozaki_split_a_rows(const OzA* A, int64_t r0, int64_t r1, cudaStream_t s)
+{
+    if (r0 < 0 || r1 > A->m || r0 >= r1 || r0 % A->row_tile || (r1 != A->m && r1 % A->row_tile))
+        return set_error(GB_ERR_ARG, "ozaki", "row block not aligned to the slice GEMM tile");
+    const int64_t cover = (r1 == A->m ? A->mpad : r1) - r0;
+    split_operand(A->slices, r1 - r0, A->k, A->a + r0 * A->ars, A->ars, A->acs, A->maxa + r0, A->mpad, cover,
+                  A->kpad, A->sa + r0 * A->kpad, A->ea + r0, A->nonfinite, s);
+    return check_cuda(cudaGetLastError(), "oz_split");
+}
+
+int ozaki_prepare_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t acs, int slices,
+                    cudaStream_t s, OzA* A)
+{
+    int rc = ozaki_alloc_a(m, k, a, ars, acs, slices, s, A);
+    if (rc) return rc;
+    if ((rc = ozaki_split_a_rows(A, 0, m, s))) ozaki_release_a(A, s);
     return rc;
 }
 
@@ -1700,27 +1727,59 @@ void ozaki_release_a(OzA* A, cudaStream_t s)
     A->ws = nullptr;
 }
 
-// Phase 2: C := alpha op(A) op(B) + beta C for the prepared op(A) and an
-// op(B) of n columns ((l, j) = b[l*brs + j*bcs]); the split of op(B), the
-// slice GEMM, the recombination and the gated IEEE fallback.  Columns of
-// op(B) are split independently, so a product done in column blocks gives
-// the same bits as one call.
-int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, double alpha, double beta,
-                   double* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
+// Phase 2: the exponents and digit slices of an op(B) of n columns
+// ((l, j) = b[l*brs + j*bcs]) for multiplications by a prepared op(A).
+// Columns of op(B) are split independently, so a product done in column
+// blocks gives the same bits as one call.
+int ozaki_prepare_b(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, cudaStream_t s, OzB* B)
 {
-    const int64_t m = A->m, k = A->k, mpad = A->mpad, kpad = A->kpad;
+    *B = OzB();
+    B->n = n;
+    B->npad = round_up(n, OZ_BN);
+    if (B->npad > INT32_MAX) return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "dimension too large for TMA coordinates");
+    B->b = b;
+    B->brs = brs;
+    B->bcs = bcs;
+    const size_t bytes_sb = (size_t)A->slices * B->npad * A->kpad * 2;
+    const size_t bytes_aux = sizeof(unsigned long long) * n + sizeof(int32_t) * n + 64;
+    B->ws = static_cast<uint8_t*>(dev_alloc(bytes_sb + bytes_aux + 1024, s));
+    if (!B->ws) return GB_ERR_NOMEM;
+    B->sb = reinterpret_cast<uint16_t*>(B->ws);
+    B->maxb = reinterpret_cast<unsigned long long*>(B->ws + bytes_sb);
+    B->eb = reinterpret_cast<int32_t*>(B->maxb + n);
+    // rows of op(B)^T: (j, l) = b[l*brs + j*bcs]
+    split_operand(A->slices, n, A->k, b, bcs, brs, B->maxb, B->npad, B->npad, A->kpad, B->sb, B->eb, A->nonfinite, s);
+    const int rc = check_cuda(cudaGetLastError(), "oz_split");
+    if (rc) ozaki_release_b(B, s);
+    return rc;
+}
+
+void ozaki_release_b(OzB* B, cudaStream_t s)
+{
+    dev_free(B->ws, s);
+    B->ws = nullptr;
+}
+
+// Phase 3: C := alpha op(A) op(B) + beta C for rows [r0, r0 + rows) of the
+// prepared op(A) (r0 a multiple of the row tile) and a prepared op(B); C is
+// that rows x n block; the slice GEMM, the recombination and the gated IEEE
+// fallback.
+int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, double alpha, double beta, double* c,
+                        int64_t rs_c, int64_t cs_c, cudaStream_t s)
+{
+    if (r0 < 0 || rows <= 0 || r0 + rows > A->m || r0 % A->row_tile)
+        return set_error(GB_ERR_ARG, "ozaki", "row block not aligned to the slice GEMM tile");
+    const int64_t m = rows, n = B->n, k = A->k, kpad = A->kpad, npad = B->npad;
+    const int64_t mpad = round_up(rows, A->row_tile);
     const int slices = A->slices;
     const bool pair_form = A->pair_form;
-    const int64_t row_tile = pair_form ? 2 * OZ2_ROWS : OZ_BM;
-    const int64_t npad = round_up(n, OZ_BN);
-    if (npad > INT32_MAX) return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "dimension too large for TMA coordinates");
     const int kb_total = (int)(kpad / OZ_BK);
 
     OzGemmParams p;
     p.slices = slices;
     p.nlevels = slices;
     p.kb_total = kb_total;
-    p.tiles_m = (int)(mpad / row_tile);
+    p.tiles_m = (int)(mpad / A->row_tile);
     p.tiles_n = (int)(npad / OZ_BN);
     const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
     int planes_total = 0;
@@ -1747,29 +1806,19 @@ int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_
     p.m = m;
     p.n = n;
 
-    const size_t bytes_sb = (size_t)slices * npad * kpad * 2;
     const size_t bytes_pl = (size_t)planes_total * npad * mpad * 4;
-    const size_t bytes_aux = sizeof(unsigned long long) * n + sizeof(int32_t) * n + 64;
-    uint8_t* ws = static_cast<uint8_t*>(dev_alloc(bytes_sb + bytes_pl + bytes_aux + 1024, s));
-    if (!ws) return GB_ERR_NOMEM;
-    uint16_t* sb = reinterpret_cast<uint16_t*>(ws);
-    int32_t* planes = reinterpret_cast<int32_t*>(ws + bytes_sb);
-    unsigned long long* maxb = reinterpret_cast<unsigned long long*>(ws + bytes_sb + bytes_pl);
-    int32_t* eb = reinterpret_cast<int32_t*>(maxb + n);
+    int32_t* planes = static_cast<int32_t*>(dev_alloc(bytes_pl + 1024, s));
+    if (!planes) return GB_ERR_NOMEM;
     p.planes = planes;
     p.status = device_status_word();
     p.skip = A->nonfinite;
     p.counter = nullptr;
 
     int rc = GB_SUCCESS;
-    auto bail = [&](int code) { dev_free(ws, s); return code; };
-    // rows of op(B)^T: (j, l) = b[l*brs + j*bcs]
-    split_operand(slices, n, k, b, bcs, brs, maxb, npad, kpad, sb, eb, A->nonfinite, s);
-    if ((rc = check_cuda(cudaGetLastError(), "oz_split"))) return bail(rc);
-
+    auto bail = [&](int code) { dev_free(planes, s); return code; };
     CUtensorMap map_a, map_b;
-    if ((rc = make_slice_map(&map_a, A->sa, kpad, mpad, slices, OZ_BM))) return bail(rc);
-    if ((rc = make_slice_map(&map_b, sb, kpad, npad, slices, pair_form ? OZ2_ROWS : OZ_BN))) return bail(rc);
+    if ((rc = make_slice_map(&map_a, A->sa + r0 * kpad, kpad, mpad, slices, OZ_BM, A->mpad))) return bail(rc);
+    if ((rc = make_slice_map(&map_b, B->sb, kpad, npad, slices, pair_form ? OZ2_ROWS : OZ_BN))) return bail(rc);
     int max_pairs = 0;
     if ((rc = slice_gemm_setup(&max_pairs))) return bail(rc);
     const int sms = sm_count() > 0 ? sm_count() : 148;
@@ -1806,8 +1855,8 @@ int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_
         r.mpad = mpad;
         r.npad = npad;
         r.planes = planes;
-        r.ea = A->ea;
-        r.eb = eb;
+        r.ea = A->ea + r0;
+        r.eb = B->eb;
         r.alpha = alpha;
         r.beta = beta;
         r.c = c;
@@ -1823,8 +1872,21 @@ int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_
     }
     if ((rc = check_cuda(cudaGetLastError(), "oz_recombine"))) return bail(rc);
     // IEEE path for non-finite operands: runs only when a split raised the flag
-    rc = dgemm_native_gated(m, n, k, alpha, A->a, A->ars, A->acs, b, brs, bcs, beta, c, rs_c, cs_c, A->nonfinite, s);
-    dev_free(ws, s);
+    rc = dgemm_native_gated(m, n, k, alpha, A->a + r0 * A->ars, A->ars, A->acs, B->b, B->brs, B->bcs, beta, c, rs_c,
+                            cs_c, A->nonfinite, s);
+    dev_free(planes, s);
+    return rc;
+}
+
+// Phases 2 and 3 for all rows of op(A).
+int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, double alpha, double beta,
+                   double* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
+{
+    OzB B;
+    int rc = ozaki_prepare_b(A, n, b, brs, bcs, s, &B);
+    if (rc) return rc;
+    rc = ozaki_multiply_rows(A, 0, A->m, &B, alpha, beta, c, rs_c, cs_c, s);
+    ozaki_release_b(&B, s);
     return rc;
 }
 

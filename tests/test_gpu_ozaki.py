@@ -185,14 +185,15 @@ def test_ozaki_device_api_matches_model():
     assert np.array_equal(tc.cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("ta,beta,pad", [(0, 0.0, 0), (1, 1.5, 3)])
-def test_ozaki_pipelined_host_path_bit_identical(ta, beta, pad):
-    """dgemm_ on host buffers large enough for the pipelined path (op(A) split
-    once, op(B) and C in column blocks on copy streams) gives the bits of one
-    device call on the same operands."""
+@pytest.mark.parametrize("ta,beta,pad,m", [(0, 0.0, 0, 2048), (1, 1.5, 3, 2048), (0, 0.5, 1, 2100)])
+def test_ozaki_pipelined_host_path_bit_identical(ta, beta, pad, m):
+    """dgemm_ on host buffers large enough for the pipelined path (op(A) in row
+    blocks, op(B) and C in column blocks on copy streams, one slice GEMM per
+    block of C) gives the bits of one device call on the same operands; m =
+    2100 leaves a last row block of part of a tile."""
     torch = pytest.importorskip("torch")
     from blis_gb300 import dev
-    m, n, k = 2048, 2304, 2048
+    n, k = 2304, 2048
     a0 = po.expspread((k, m) if ta else (m, k), 41, -12, 12)
     b0 = po.expspread((k, n), 42, -12, 12)
     c0 = po.uniform((m, n), 43)
@@ -215,3 +216,26 @@ def test_ozaki_pipelined_host_path_bit_identical(ta, beta, pad):
     torch.cuda.synchronize()
     assert np.array_equal(c[:m], cd.cpu().numpy())
     assert np.all(c[m:] == 0.0)  # padding rows of C untouched
+
+
+def test_ozaki_pipelined_host_path_row_major_a():
+    """A row-major op(A) (no row-block copies) takes the column-block pipeline
+    with op(A) staged whole: the same bits as one device call."""
+    torch = pytest.importorskip("torch")
+    from blis_gb300 import dev
+    m, n, k = 1024, 2304, 4096
+    a = po.expspread((m, k), 51, -12, 12, order="C")
+    b = po.expspread((k, n), 52, -12, 12)
+    c0 = po.uniform((m, n), 53)
+    c = np.asfortranarray(c0.copy())
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 7)
+    try:
+        blas.bli_dgemm(N, N, 0.75, a, b, 0.25, c)
+    finally:
+        blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+    ad = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    bd = torch.from_numpy(np.ascontiguousarray(b.T)).cuda().t()
+    cd = torch.from_numpy(np.ascontiguousarray(c0.T)).cuda().t()
+    dev.dgemm_ozaki(0, 0, 0.75, ad, bd, 0.25, cd, 7)
+    torch.cuda.synchronize()
+    assert np.array_equal(c, cd.cpu().numpy())
