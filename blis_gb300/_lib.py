@@ -57,6 +57,10 @@ def load(path=None):
     _sig(L, "dgemm_batch_", None, batch)
     _sig(L, "sgemm_batch_", None, batch)
     _sig(L, "xerbla_", C.c_int, [_cp, _ip, C.c_long])
+    _sig(L, "dtrmm_", None, [_cp, _cp, _cp, _cp, _ip, _ip, _dp, _vp, _ip, _vp, _ip])
+    _sig(L, "dsymm_", None, [_cp, _cp, _ip, _ip, _dp, _vp, _ip, _vp, _ip, _dp, _vp, _ip])
+    _sig(L, "dsyrk_", None, [_cp, _cp, _ip, _ip, _dp, _vp, _ip, _dp, _vp, _ip])
+    _sig(L, "dgemmt_", None, [_cp, _cp, _cp, _ip, _ip, _dp, _vp, _ip, _vp, _ip, _dp, _vp, _ip])
     _sig(L, "cblas_dgemm", None, [C.c_int] * 3 + [_i32] * 3 + [_d, _vp, _i32, _vp, _i32, _d, _vp, _i32])
     _sig(L, "cblas_sgemm", None, [C.c_int] * 3 + [_i32] * 3 + [_f, _vp, _i32, _vp, _i32, _f, _vp, _i32])
     _sig(L, "cblas_dtrsm", None, [C.c_int] * 5 + [_i32, _i32, _d, _vp, _i32, _vp, _i32])
@@ -72,6 +76,12 @@ def load(path=None):
     tt = [C.c_int] * 4 + [_i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64]
     _sig(L, "bli_dtrsm", None, tt)
     _sig(L, "bli_dtrsm_ex", None, tt + [_vp, _vp])
+    _sig(L, "bli_dtrmm", None, tt)
+    _sig(L, "bli_dsymm", None, [C.c_int] * 4 + [_i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp,
+                                                 _i64, _i64])
+    _sig(L, "bli_dsyrk", None, [C.c_int, C.c_int, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _vp, _i64, _i64])
+    _sig(L, "bli_dgemmt", None, [C.c_int] * 3 + [_i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp,
+                                                  _i64, _i64])
     tv = [C.c_int, C.c_int, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _vp, _vp, _i64]
     _sig(L, "bli_dgemv", None, tv)
     _sig(L, "bli_dgemv_ex", None, tv + [_vp, _vp])
@@ -85,6 +95,13 @@ def load(path=None):
     sg = [C.c_int, C.c_int, _i64, _i64, _i64, _f, _vp, _i64, _i64, _vp, _i64, _i64, _f, _vp, _i64, _i64]
     _sig(L, "gb_sgemm_dev", C.c_int, sg + [_vp])
     _sig(L, "gb_dtrsm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_dtrmm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_dsymm_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _d,
+                                      _vp, _i64, _i64, _vp])
+    _sig(L, "gb_dgemmt_dev", C.c_int, [C.c_int] * 3 + [_i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _d,
+                                                        _vp, _i64, _i64, _vp])
+    _sig(L, "gb_dsyrk_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, _d, _vp, _i64, _i64, _d, _vp, _i64, _i64,
+                                      _vp])
     _sig(L, "gb_daxpyv_dev", C.c_int, [_i64, _d, _vp, _i64, _vp, _i64, _vp])
     _sig(L, "gb_ddotv_dev", C.c_int, [_i64, _vp, _i64, _vp, _i64, _vp, _vp])
     _sig(L, "gb_dgemv_dev", C.c_int, [C.c_int, _i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _d, _vp, _i64, _vp])

@@ -55,6 +55,25 @@ def dtrsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
                        C.byref(C.c_double(alpha)), _p(a), _i(lda), _p(b), _i(ldb))
 
 
+def dtrmm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
+    _lib.load().dtrmm_(_c(side), _c(uplo), _c(transa), _c(diag), _i(m), _i(n), _d(alpha), _p(a), _i(lda),
+                       _p(b), _i(ldb))
+
+
+def dsymm(side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc):
+    _lib.load().dsymm_(_c(side), _c(uplo), _i(m), _i(n), _d(alpha), _p(a), _i(lda), _p(b), _i(ldb), _d(beta),
+                       _p(c), _i(ldc))
+
+
+def dsyrk(uplo, trans, n, k, alpha, a, lda, beta, c, ldc):
+    _lib.load().dsyrk_(_c(uplo), _c(trans), _i(n), _i(k), _d(alpha), _p(a), _i(lda), _d(beta), _p(c), _i(ldc))
+
+
+def dgemmt(uplo, transa, transb, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+    _lib.load().dgemmt_(_c(uplo), _c(transa), _c(transb), _i(n), _i(k), _d(alpha), _p(a), _i(lda), _p(b),
+                        _i(ldb), _d(beta), _p(c), _i(ldc))
+
+
 def dgemv(trans, m, n, alpha, a, lda, x, incx, beta, y, incy):
     _lib.load().dgemv_(_c(trans), _i(m), _i(n), C.byref(C.c_double(alpha)), _p(a), _i(lda), _p(x),
                        _i(incx), C.byref(C.c_double(beta)), _p(y), _i(incy))
@@ -110,6 +129,30 @@ def bli_sgemm(transa, transb, alpha, a, b, beta, c):
 def bli_dtrsm(side, uplo, transa, diag, alpha, a, b):
     m, n = b.shape
     _lib.load().bli_dtrsm(side, uplo, transa, diag, m, n, _d(alpha), _p(a), *_st(a), _p(b), *_st(b))
+
+
+def bli_dtrmm(side, uplo, transa, diag, alpha, a, b):
+    m, n = b.shape
+    _lib.load().bli_dtrmm(side, uplo, transa, diag, m, n, _d(alpha), _p(a), *_st(a), _p(b), *_st(b))
+
+
+def bli_dsymm(side, uplo, alpha, a, b, beta, c, transb=0):
+    m, n = c.shape
+    _lib.load().bli_dsymm(side, uplo, 0, transb, m, n, _d(alpha), _p(a), *_st(a), _p(b), *_st(b), _d(beta),
+                          _p(c), *_st(c))
+
+
+def bli_dsyrk(uplo, transa, alpha, a, beta, c):
+    m = c.shape[0]
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    _lib.load().bli_dsyrk(uplo, transa, m, k, _d(alpha), _p(a), *_st(a), _d(beta), _p(c), *_st(c))
+
+
+def bli_dgemmt(uplo, transa, transb, alpha, a, b, beta, c):
+    m = c.shape[0]
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    _lib.load().bli_dgemmt(uplo, transa, transb, m, k, _d(alpha), _p(a), *_st(a), _p(b), *_st(b), _d(beta),
+                           _p(c), *_st(c))
 
 
 def bli_dgemv(transa, alpha, a, x, beta, y, incx=1, incy=1):

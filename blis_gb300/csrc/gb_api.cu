@@ -479,6 +479,85 @@ int trsm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     return finish(s, "trsm");
 }
 
+int level3_slices() { return (dgemm_mode() == GB_DGEMM_OZAKI) ? ozaki_slices() : 0; }
+
+int trmm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, double alpha, const double* a,
+              int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const int64_t na = (side == GB_LEFT) ? m : n;
+    Staged& B = bufs.next();
+    if ((rc = stage_in(b, m, n, rs_b, cs_b, 8, alpha != 0.0, &B, s))) return rc;
+    Staged& A = bufs.next();
+    if (alpha != 0.0 && (rc = stage_in(a, na, na, rs_a, cs_a, 8, true, &A, s))) return rc;
+    if ((rc = dtrmm_dev(side, uplo, transa, diag, m, n, alpha, reinterpret_cast<const double*>(A.origin), A.rs,
+                        A.cs, reinterpret_cast<double*>(B.origin), B.rs, B.cs, level3_slices(), s)))
+        return rc;
+    if ((rc = stage_out(b, m, n, rs_b, cs_b, 8, B, s))) return rc;
+    return finish(s, where);
+}
+
+int symm_host(int side, int uplo, int64_t m, int64_t n, double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+              const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c,
+              const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const int64_t na = (side == GB_LEFT) ? m : n;
+    Staged& C = bufs.next();
+    if ((rc = stage_in(c, m, n, rs_c, cs_c, 8, beta != 0.0, &C, s))) return rc;
+    Staged& A = bufs.next();
+    Staged& B = bufs.next();
+    if (alpha != 0.0) {
+        if ((rc = stage_in(a, na, na, rs_a, cs_a, 8, true, &A, s))) return rc;
+        if ((rc = stage_in(b, m, n, rs_b, cs_b, 8, true, &B, s))) return rc;
+    }
+    if ((rc = dsymm_dev(side, uplo, m, n, alpha, reinterpret_cast<const double*>(A.origin), A.rs, A.cs,
+                        reinterpret_cast<const double*>(B.origin), B.rs, B.cs, beta,
+                        reinterpret_cast<double*>(C.origin), C.rs, C.cs, level3_slices(), s)))
+        return rc;
+    if ((rc = stage_out(c, m, n, rs_c, cs_c, 8, C, s))) return rc;
+    return finish(s, where);
+}
+
+// C (m x m, one triangle) := alpha op(A) op(B) + beta C; syrk passes B = A with transb = !transa
+int gemmt_host(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha, const double* a, int64_t rs_a,
+               int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c,
+               int64_t cs_c, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    Staged& C = bufs.next();
+    // the whole of C goes up and comes back: the untouched triangle round-trips unchanged
+    if ((rc = stage_in(c, m, m, rs_c, cs_c, 8, true, &C, s))) return rc;
+    Staged& A = bufs.next();
+    Staged& B = bufs.next();
+    const bool need = (alpha != 0.0 && k > 0);
+    if (need) {
+        if ((rc = stage_in(a, ta ? k : m, ta ? m : k, rs_a, cs_a, 8, true, &A, s))) return rc;
+        if (b == a && rs_b == rs_a && cs_b == cs_a) B = Staged{};  // syrk: the same staged copy
+        else if ((rc = stage_in(b, tb ? m : k, tb ? k : m, rs_b, cs_b, 8, true, &B, s))) return rc;
+    }
+    const Staged& Bs = (need && b == a && rs_b == rs_a && cs_b == cs_a) ? A : B;
+    if ((rc = dgemmt_dev(uplo, transa, transb, m, k, alpha, reinterpret_cast<const double*>(A.origin), A.rs, A.cs,
+                         reinterpret_cast<const double*>(Bs.origin), Bs.rs, Bs.cs, beta,
+                         reinterpret_cast<double*>(C.origin), C.rs, C.cs, level3_slices(), s)))
+        return rc;
+    if ((rc = stage_out(c, m, m, rs_c, cs_c, 8, C, s))) return rc;
+    return finish(s, where);
+}
+
 // ---------------------------------------------------------------- BLAS helpers
 bool lsame(char a, char b) { return toupper((unsigned char)a) == toupper((unsigned char)b); }
 
@@ -608,6 +687,108 @@ void dtrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char
     }
     trsm_host(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, map_trans(*transa),
               unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, *n, *alpha, a, 1, *lda, b, 1, *ldb);
+}
+
+void dtrmm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const double* alpha,
+            const double* a, const gb_f77_int* lda, double* b, const gb_f77_int* ldb)
+{
+    // frame/compat/bla_trmm.c:45-121, checks frame/compat/check/bla_trmm_check.h:37-86
+    const bool left = lsame(*side, 'L'), right = lsame(*side, 'R');
+    const bool lower = lsame(*uploa, 'L'), upper = lsame(*uploa, 'U');
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T'), conja = lsame(*transa, 'C');
+    const bool unita = lsame(*diaga, 'U'), nonua = lsame(*diaga, 'N');
+    const int nrowa = left ? *m : *n;
+    int info = 0;
+    if (!left && !right) info = 1;
+    else if (!lower && !upper) info = 2;
+    else if (!nota && !ta && !conja) info = 3;
+    else if (!unita && !nonua) info = 4;
+    else if (*m < 0) info = 5;
+    else if (*n < 0) info = 6;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 9;
+    else if (*ldb < (*m > 1 ? *m : 1)) info = 11;
+    if (info) {
+        call_xerbla("DTRMM ", info);
+        return;
+    }
+    trmm_host(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, map_trans(*transa),
+              unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, *n, *alpha, a, 1, *lda, b, 1, *ldb, "DTRMM");
+}
+
+void dsymm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
+            const double* alpha, const double* a, const gb_f77_int* lda, const double* b, const gb_f77_int* ldb,
+            const double* beta, double* c, const gb_f77_int* ldc)
+{
+    // frame/compat/bla_symm.c:45-119, checks frame/compat/check/bla_hemm_check.h:37-81
+    const bool left = lsame(*side, 'L'), right = lsame(*side, 'R');
+    const bool lower = lsame(*uploa, 'L'), upper = lsame(*uploa, 'U');
+    const int nrowa = left ? *m : *n;
+    int info = 0;
+    if (!left && !right) info = 1;
+    else if (!lower && !upper) info = 2;
+    else if (*m < 0) info = 3;
+    else if (*n < 0) info = 4;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 7;
+    else if (*ldb < (*m > 1 ? *m : 1)) info = 9;
+    else if (*ldc < (*m > 1 ? *m : 1)) info = 12;
+    if (info) {
+        call_xerbla("DSYMM ", info);
+        return;
+    }
+    symm_host(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, *m, *n, *alpha, a, 1, *lda, b, 1, *ldb,
+              *beta, c, 1, *ldc, "DSYMM");
+}
+
+void dsyrk_(const gb_f77_char* uploc, const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* k,
+            const double* alpha, const double* a, const gb_f77_int* lda, const double* beta, double* c,
+            const gb_f77_int* ldc)
+{
+    // frame/compat/bla_syrk.c:45-121, checks frame/compat/check/bla_syrk_check.h:37-84 (real: 'C' is 'T')
+    const bool lower = lsame(*uploc, 'L'), upper = lsame(*uploc, 'U');
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T') || lsame(*transa, 'C');
+    const int nrowa = nota ? *m : *k;
+    int info = 0;
+    if (!lower && !upper) info = 1;
+    else if (!nota && !ta) info = 2;
+    else if (*m < 0) info = 3;
+    else if (*k < 0) info = 4;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 7;
+    else if (*ldc < (*m > 1 ? *m : 1)) info = 10;
+    if (info) {
+        call_xerbla("DSYRK ", info);
+        return;
+    }
+    // C := alpha op(A) op(A)^T + beta C (frame/3/bli_l3_oapi_ex.c:326-345)
+    const int t = nota ? GB_NO_TRANSPOSE : GB_TRANSPOSE;
+    gemmt_host(lower ? GB_LOWER : GB_UPPER, t, nota ? GB_TRANSPOSE : GB_NO_TRANSPOSE, *m, *k, *alpha, a, 1, *lda,
+               a, 1, *lda, *beta, c, 1, *ldc, "DSYRK");
+}
+
+void dgemmt_(const gb_f77_char* uploc, const gb_f77_char* transa, const gb_f77_char* transb, const gb_f77_int* m,
+             const gb_f77_int* k, const double* alpha, const double* a, const gb_f77_int* lda, const double* b,
+             const gb_f77_int* ldb, const double* beta, double* c, const gb_f77_int* ldc)
+{
+    // frame/compat/extra/bla_gemmt.c:45-121, checks frame/compat/check/bla_gemmt_check.h:37-92
+    const bool lower = lsame(*uploc, 'L'), upper = lsame(*uploc, 'U');
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T'), conja = lsame(*transa, 'C');
+    const bool notb = lsame(*transb, 'N'), tb = lsame(*transb, 'T'), conjb = lsame(*transb, 'C');
+    const int nrowa = nota ? *m : *k, nrowb = notb ? *k : *m;
+    int info = 0;
+    if (!lower && !upper) info = 1;
+    else if (!nota && !conja && !ta) info = 2;
+    else if (!notb && !conjb && !tb) info = 3;
+    else if (*m < 0) info = 4;
+    else if (*k < 0) info = 5;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 8;
+    else if (*ldb < (nrowb > 1 ? nrowb : 1)) info = 10;
+    else if (*ldc < (*m > 1 ? *m : 1)) info = 13;
+    if (info) {
+        call_xerbla("DGEMMT", info);
+        return;
+    }
+    gemmt_host(lower ? GB_LOWER : GB_UPPER, map_trans(*transa), map_trans(*transb), *m, *k, *alpha, a, 1, *lda, b,
+               1, *ldb, *beta, c, 1, *ldc, "DGEMMT");
 }
 
 void dgemv_(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n, const double* alpha,
@@ -772,6 +953,40 @@ void bli_dtrsm_ex(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t 
     bli_dtrsm(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b);
 }
 
+void bli_dtrmm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+               const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, double* b, gb_inc_t rs_b,
+               gb_inc_t cs_b)
+{
+    trmm_host(side, uploa, transa, diaga, m, n, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, "bli_dtrmm");
+}
+
+void bli_dsymm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+               const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b, gb_inc_t rs_b,
+               gb_inc_t cs_b, const double* beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    (void)conja;  // real: conjugation is the identity
+    // op(B) by its strides: B^T (element (i, j) at b[j*rs_b + i*cs_b])
+    const bool tb = GB_IS_TRANS(transb);
+    symm_host(side, uploa, m, n, *alpha, a, rs_a, cs_a, b, tb ? cs_b : rs_b, tb ? rs_b : cs_b, *beta, c, rs_c,
+              cs_c, "bli_dsymm");
+}
+
+void bli_dsyrk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const double* alpha, const double* a,
+               gb_inc_t rs_a, gb_inc_t cs_a, const double* beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    const bool ta = GB_IS_TRANS(transa);
+    gemmt_host(uploc, ta ? GB_TRANSPOSE : GB_NO_TRANSPOSE, ta ? GB_NO_TRANSPOSE : GB_TRANSPOSE, m, k, *alpha, a,
+               rs_a, cs_a, a, rs_a, cs_a, *beta, c, rs_c, cs_c, "bli_dsyrk");
+}
+
+void bli_dgemmt(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k, const double* alpha,
+                const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b, gb_inc_t rs_b, gb_inc_t cs_b,
+                const double* beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    gemmt_host(uploc, transa, transb, m, k, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c, cs_c,
+               "bli_dgemmt");
+}
+
 void bli_dgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, const double* alpha,
                const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* x, gb_inc_t incx,
                const double* beta, double* y, gb_inc_t incy)
@@ -922,6 +1137,47 @@ int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
     const int slices = (gb::dgemm_mode() == GB_DGEMM_OZAKI) ? gb::ozaki_slices() : 0;
     return gb::dtrsm_dev(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, slices,
                          pick_stream(stream));
+}
+
+int gb_dtrmm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+                 double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, double* b, gb_inc_t rs_b,
+                 gb_inc_t cs_b, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_dtrmm_dev", "negative dimension");
+    return gb::dtrmm_dev(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, gb::level3_slices(),
+                         pick_stream(stream));
+}
+
+int gb_dsymm_dev(gb_side_t side, gb_uplo_t uploa, gb_dim_t m, gb_dim_t n, double alpha, const double* a,
+                 gb_inc_t rs_a, gb_inc_t cs_a, const double* b, gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c,
+                 gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_dsymm_dev", "negative dimension");
+    return gb::dsymm_dev(side, uploa, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c, cs_c,
+                         gb::level3_slices(), pick_stream(stream));
+}
+
+int gb_dgemmt_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k, double alpha,
+                  const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b, gb_inc_t rs_b, gb_inc_t cs_b,
+                  double beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_dgemmt_dev", "negative dimension");
+    return gb::dgemmt_dev(uploc, transa, transb, m, k, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c, cs_c,
+                          gb::level3_slices(), pick_stream(stream));
+}
+
+int gb_dsyrk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, double alpha, const double* a,
+                 gb_inc_t rs_a, gb_inc_t cs_a, double beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    const bool ta = GB_IS_TRANS(transa);
+    return gb_dgemmt_dev(uploc, ta ? GB_TRANSPOSE : GB_NO_TRANSPOSE, ta ? GB_NO_TRANSPOSE : GB_TRANSPOSE, m, k,
+                         alpha, a, rs_a, cs_a, a, rs_a, cs_a, beta, c, rs_c, cs_c, stream);
 }
 
 int gb_daxpyv_dev(gb_dim_t n, double alpha, const double* x, gb_inc_t incx, double* y, gb_inc_t incy,

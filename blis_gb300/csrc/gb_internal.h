@@ -102,6 +102,18 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
               const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b,
               int64_t cs_b, int slices, cudaStream_t s);
 int64_t ozaki_kpart_limit(int slices);
+// Lanes per right-hand side (1, 2, 4, 8) for the 64-row diagonal-block
+// kernels of trsm and trmm, from the FP64-instruction cost model (gb_trsm.cu).
+int diag_block_lanes(int64_t ncols);
+int dtrmm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, double alpha,
+              const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b, int slices,
+              cudaStream_t s);
+int dsymm_dev(int side, int uplo, int64_t m, int64_t n, double alpha, const double* a, int64_t rs_a,
+              int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c,
+              int64_t cs_c, int slices, cudaStream_t s);
+int dgemmt_dev(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha, const double* a,
+               int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c,
+               int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s);
 // The Ozaki form in two phases (gb_ozaki.cu): op(A) split once, then any
 // number of products with column blocks of op(B) (bit-identical to one call).
 struct OzA {

@@ -194,45 +194,6 @@ int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t cco
                         t.brs, t.bcs, t.s);
 }
 
-// Lanes per right-hand side for the diagonal kernel (GB_TRSM_DIAG_LANES =
-// 1, 2, 4 or 8 fixes it).  Each warp issues one FMA per step for every group
-// of LANES rows that has a row left to update, 64R - LANES R (R - 1) / 2 - R
-// instructions (R = 64 / LANES rows per lane), and R multiplies: 2080, 1056,
-// 544, 288 for 1, 2, 4, 8 lanes, for 32 / LANES columns; staging the packed
-// block and the panel costs about as much as 96 more.  GB300's FP64 pipe
-// takes tens of cycles per warp instruction on each of an SM's four
-// sub-partitions, so the solve time is about one warp's cost times the warps
-// that share a sub-partition (CTAs of four warps: ceil(CTAs / SMs) on the
-// busiest SM), but no less than four of them: below that the dependent chain
-// of each row, not the pipe, sets the time.  The constants were fitted to
-// solves of 2048 to 16384 right-hand sides timed on GB300.  The fewest lanes
-// win near-ties.
-int trsm_diag_lanes(int64_t ncols)
-{
-    static int forced = -1;
-    if (forced < 0) {
-        const char* e = getenv("GB_TRSM_DIAG_LANES");
-        const int v = e ? atoi(e) : 0;
-        forced = (v == 1 || v == 2 || v == 4 || v == 8) ? v : 0;
-    }
-    if (forced) return forced;
-    const int64_t sms = sm_count() > 0 ? sm_count() : 148;
-    int best = 1;
-    int64_t best_cost = 0;
-    for (int lanes = 1; lanes <= 8; lanes *= 2) {
-        const int64_t r = TRSM_NB / lanes;
-        const int64_t per_warp = 64 * r - lanes * r * (r - 1) / 2 + 96;
-        const int64_t ctas = (ncols + TRSM_THREADS / lanes - 1) / (TRSM_THREADS / lanes);
-        const int64_t waves = (ctas + sms - 1) / sms;
-        const int64_t cost = per_warp * (waves > 4 ? waves : 4);
-        if (lanes == 1 || cost * 50 < best_cost * 49) {
-            best = lanes;
-            best_cost = cost;
-        }
-    }
-    return best;
-}
-
 int solve(const TrsmCtx& t, int64_t r0, int64_t mm)
 {
     if (mm <= TRSM_NB) {
@@ -241,7 +202,7 @@ int solve(const TrsmCtx& t, int64_t r0, int64_t mm)
         double* b1 = t.b + r0 * t.brs;
         const int nb = (int)mm;
         LaunchScope ls("trsm_diag", t.s);
-        switch (trsm_diag_lanes(t.n)) {
+        switch (diag_block_lanes(t.n)) {
         case 1:
             return t.lower ? launch_trsm_diag<1, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
                            : launch_trsm_diag<1, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
@@ -272,6 +233,45 @@ int solve(const TrsmCtx& t, int64_t r0, int64_t mm)
 }
 
 }  // namespace
+
+// Lanes per right-hand side for the diagonal kernel (GB_TRSM_DIAG_LANES =
+// 1, 2, 4 or 8 fixes it).  Each warp issues one FMA per step for every group
+// of LANES rows that has a row left to update, 64R - LANES R (R - 1) / 2 - R
+// instructions (R = 64 / LANES rows per lane), and R multiplies: 2080, 1056,
+// 544, 288 for 1, 2, 4, 8 lanes, for 32 / LANES columns; staging the packed
+// block and the panel costs about as much as 96 more.  GB300's FP64 pipe
+// takes tens of cycles per warp instruction on each of an SM's four
+// sub-partitions, so the solve time is about one warp's cost times the warps
+// that share a sub-partition (CTAs of four warps: ceil(CTAs / SMs) on the
+// busiest SM), but no less than four of them: below that the dependent chain
+// of each row, not the pipe, sets the time.  The constants were fitted to
+// solves of 2048 to 16384 right-hand sides timed on GB300.  The fewest lanes
+// win near-ties.
+int diag_block_lanes(int64_t ncols)
+{
+    static int forced = -1;
+    if (forced < 0) {
+        const char* e = getenv("GB_TRSM_DIAG_LANES");
+        const int v = e ? atoi(e) : 0;
+        forced = (v == 1 || v == 2 || v == 4 || v == 8) ? v : 0;
+    }
+    if (forced) return forced;
+    const int64_t sms = sm_count() > 0 ? sm_count() : 148;
+    int best = 1;
+    int64_t best_cost = 0;
+    for (int lanes = 1; lanes <= 8; lanes *= 2) {
+        const int64_t r = TRSM_NB / lanes;
+        const int64_t per_warp = 64 * r - lanes * r * (r - 1) / 2 + 96;
+        const int64_t ctas = (ncols + TRSM_THREADS / lanes - 1) / (TRSM_THREADS / lanes);
+        const int64_t waves = (ctas + sms - 1) / sms;
+        const int64_t cost = per_warp * (waves > 4 ? waves : 4);
+        if (lanes == 1 || cost * 50 < best_cost * 49) {
+            best = lanes;
+            best_cost = cost;
+        }
+    }
+    return best;
+}
 
 int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, double alpha,
               const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b,

@@ -70,6 +70,34 @@ def dtrsm(side, uplo, transa, diag, alpha, a, b):
     return _lib.check(rc, "gb_dtrsm_dev")
 
 
+def dtrmm(side, uplo, transa, diag, alpha, a, b):
+    m, n = b.shape
+    rc = _lib.load().gb_dtrmm_dev(side, uplo, transa, diag, m, n, alpha, a.data_ptr(), *_rc(a),
+                                  b.data_ptr(), *_rc(b), _stream())
+    return _lib.check(rc, "gb_dtrmm_dev")
+
+
+def dsymm(side, uplo, alpha, a, b, beta, c):
+    m, n = c.shape
+    rc = _lib.load().gb_dsymm_dev(side, uplo, m, n, alpha, a.data_ptr(), *_rc(a), b.data_ptr(), *_rc(b), beta,
+                                  c.data_ptr(), *_rc(c), _stream())
+    return _lib.check(rc, "gb_dsymm_dev")
+
+
+def dsyrk(uplo, transa, alpha, a, beta, c):
+    m = c.shape[0]
+    rc = _lib.load().gb_dsyrk_dev(uplo, transa, m, _k(transa, a), alpha, a.data_ptr(), *_rc(a), beta,
+                                  c.data_ptr(), *_rc(c), _stream())
+    return _lib.check(rc, "gb_dsyrk_dev")
+
+
+def dgemmt(uplo, transa, transb, alpha, a, b, beta, c):
+    m = c.shape[0]
+    rc = _lib.load().gb_dgemmt_dev(uplo, transa, transb, m, _k(transa, a), alpha, a.data_ptr(), *_rc(a),
+                                   b.data_ptr(), *_rc(b), beta, c.data_ptr(), *_rc(c), _stream())
+    return _lib.check(rc, "gb_dgemmt_dev")
+
+
 def daxpyv(alpha, x, y, incx=1, incy=1, n=None):
     n = x.numel() if n is None else n
     rc = _lib.load().gb_daxpyv_dev(n, alpha, x.data_ptr(), incx, y.data_ptr(), incy, _stream())

@@ -14,6 +14,8 @@ L2 where the workload allows:
   daxpyv_2^28     24 n bytes; ddotv_2^28: 16 n bytes                (HBM)
   dtrsm_16384     L/L/N/N, B entries (1+u) 2^e, e in [-20,20]: native and
                   Ozaki updates, sampled componentwise backward error
+  level3x         dtrmm 8192x4096 (m^2 n), dsyrk n=k=8192 (n^2 k), dsymm
+                  8192x4096 (2 m^2 n): native FP64 and Ozaki (7 slices)
   batch_4096      4096 problems, m,n,k log-uniform in [16,1024], random
                   transposes: grouped launches (captured graph) vs a
                   per-problem launch loop, FP64 native, FP64 Ozaki (7
@@ -21,7 +23,8 @@ L2 where the workload allows:
 
 Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl] [--batch-count N] [--small]
                                 [--trsm-forms native,ozaki]
-(--small: 4096^3 GEMMs, 2048 x 10240 DTRSM, 2^25 vectors, 8192^2 GEMV, for ncu captures)
+(--small: 4096^3 GEMMs, 2048 x 10240 DTRSM, 2^25 vectors, 8192^2 GEMV, 4096-row level-3 extras,
+for ncu captures)
 """
 import argparse
 import ctypes as C
@@ -319,8 +322,36 @@ def run_batch(out):
         del keep
 
 
+def run_level3x(out):
+    """dtrmm L/L/N/N 8192 x 4096 (m^2 n flop), dsyrk L/N n = k = 8192 (n^2 k),
+    dsymm L/L 8192 x 4096 (2 m^2 n), native FP64 and Ozaki s = 7; U[-1,1]."""
+    m, n = (4096, 2048) if SMALL else (8192, 4096)
+    A = _mat(m, m, seed=51)
+    B = _mat(m, n, seed=52)
+    C0 = _mat(m, n, seed=53)
+    K = _mat(m, m, seed=54)
+    S = _mat(m, m, seed=55)
+    for mode, name in ((0, "native_fp64"), (1, "ozaki_s7")):
+        _lib.load().gb_set_dgemm_mode(mode, 7)
+        reps = 1 if mode == 0 else 3
+        x = B.clone()
+        ms = _timer(lambda: (x.copy_(B), dev.dtrmm(0, 0xC0, 0, 0, 1.0, A, x)), reps=reps, warmup=1)
+        copy_ms = _timer(lambda: x.copy_(B), reps=3, warmup=1)
+        out.append({"workload": "dtrmm_%dx%d" % (m, n), "form": name, "ms": ms - copy_ms,
+                    "tflops": float(m) * m * n / (ms - copy_ms) / 1e9})
+        ms = _timer(lambda: dev.dsyrk(0xC0, 0, 1.0, K, 0.5, S), reps=reps, warmup=1)
+        out.append({"workload": "dsyrk_%d_k%d" % (m, m), "form": name, "ms": ms,
+                    "tflops": float(m) * m * m / ms / 1e9})
+        c = C0.clone()
+        ms = _timer(lambda: dev.dsymm(0, 0xC0, 1.0, A, B, 0.5, c), reps=reps, warmup=1)
+        out.append({"workload": "dsymm_%dx%d" % (m, n), "form": name, "ms": ms,
+                    "tflops": 2.0 * m * m * n / ms / 1e9})
+    _lib.load().gb_set_dgemm_mode(0, 8)
+
+
 SUITES = {"gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
-          "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm, "bgemm": run_bgemm}
+          "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm, "bgemm": run_bgemm,
+          "level3x": run_level3x}
 
 
 def main():

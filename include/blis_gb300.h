@@ -84,6 +84,37 @@ void dtrsm_(const gb_f77_char* side, const gb_f77_char* uploa,
             const gb_f77_int* m, const gb_f77_int* n, const double* alpha,
             const double* a, const gb_f77_int* lda, double* b, const gb_f77_int* ldb);
 
+/* replaces dtrmm_, frame/compat/bla_trmm.c:45-121 (checks
+   frame/compat/check/bla_trmm_check.h:37-86): B := alpha op(A) B or alpha B op(A) */
+void dtrmm_(const gb_f77_char* side, const gb_f77_char* uploa,
+            const gb_f77_char* transa, const gb_f77_char* diaga,
+            const gb_f77_int* m, const gb_f77_int* n, const double* alpha,
+            const double* a, const gb_f77_int* lda, double* b, const gb_f77_int* ldb);
+
+/* replaces dsymm_, frame/compat/bla_symm.c:45-119 (checks
+   frame/compat/check/bla_hemm_check.h:37-81): C := alpha A B + beta C or
+   alpha B A + beta C, A symmetric, only the uploa triangle of A read */
+void dsymm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m,
+            const gb_f77_int* n, const double* alpha, const double* a, const gb_f77_int* lda,
+            const double* b, const gb_f77_int* ldb, const double* beta, double* c,
+            const gb_f77_int* ldc);
+
+/* replaces dsyrk_, frame/compat/bla_syrk.c:45-121 (checks
+   frame/compat/check/bla_syrk_check.h:37-84): C := alpha op(A) op(A)^T + beta C on
+   the uploc triangle, through gemmt as bli_syrk_ex does
+   (frame/3/bli_l3_oapi_ex.c:326-345) */
+void dsyrk_(const gb_f77_char* uploc, const gb_f77_char* transa, const gb_f77_int* m,
+            const gb_f77_int* k, const double* alpha, const double* a, const gb_f77_int* lda,
+            const double* beta, double* c, const gb_f77_int* ldc);
+
+/* replaces dgemmt_, frame/compat/extra/bla_gemmt.c:45-121 (checks
+   frame/compat/check/bla_gemmt_check.h:37-92): C := alpha op(A) op(B) + beta C on
+   the uploc triangle of the m x m C; the other triangle is not touched */
+void dgemmt_(const gb_f77_char* uploc, const gb_f77_char* transa, const gb_f77_char* transb,
+             const gb_f77_int* m, const gb_f77_int* k, const double* alpha, const double* a,
+             const gb_f77_int* lda, const double* b, const gb_f77_int* ldb, const double* beta,
+             double* c, const gb_f77_int* ldc);
+
 /* replaces dgemv_, frame/compat/bla_gemv.c:45-143 (checks
    frame/compat/check/bla_gemv_check.h:37-75; n_x == 0 returns untouched, :95-106) */
 void dgemv_(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n,
@@ -182,6 +213,24 @@ void bli_sgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_
                const float* b, gb_inc_t rs_b, gb_inc_t cs_b, const float* beta,
                float* c, gb_inc_t rs_c, gb_inc_t cs_c);
 
+/* replace bli_dtrmm (frame/3/bli_l3_tapi_ex.c:536-585), bli_dsymm
+   (:104-164; conja is the identity for real data, transb applies to B),
+   bli_dsyrk (:290-339) and bli_dgemmt (:408-463) */
+void bli_dtrmm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+               gb_dim_t n, const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               double* b, gb_inc_t rs_b, gb_inc_t cs_b);
+void bli_dsymm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m,
+               gb_dim_t n, const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               const double* b, gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c,
+               gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_dsyrk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const double* alpha,
+               const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* beta, double* c,
+               gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_dgemmt(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c, gb_inc_t rs_c,
+                gb_inc_t cs_c);
+
 /* replaces bli_dtrsm / bli_dtrsm_ex, frame/3/bli_l3_tapi_ex.c:533-586 */
 void bli_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
                gb_dim_t m, gb_dim_t n, const double* alpha, const double* a,
@@ -269,6 +318,23 @@ int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
 int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
                  gb_dim_t m, gb_dim_t n, double alpha, const double* a, gb_inc_t rs_a,
                  gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
+
+/* Device-pointer forms of trmm, symm, gemmt and syrk (asynchronous on the
+   stream; native FP64 or the Ozaki form by gb_set_dgemm_mode, with a fixed
+   slice count). */
+int gb_dtrmm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+                 gb_dim_t n, double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, double* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
+int gb_dsymm_dev(gb_side_t side, gb_uplo_t uploa, gb_dim_t m, gb_dim_t n, double alpha,
+                 const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b, gb_inc_t rs_b,
+                 gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+int gb_dgemmt_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                  double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                  gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c,
+                  void* stream);
+int gb_dsyrk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, double alpha,
+                 const double* a, gb_inc_t rs_a, gb_inc_t cs_a, double beta, double* c, gb_inc_t rs_c,
+                 gb_inc_t cs_c, void* stream);
 
 /* Allocation-free dot product (no counterpart in the reference).  For callers
    that cannot call cudaMalloc/cudaFree -- those calls can synchronize the

@@ -19,6 +19,11 @@
  *   trsm  left/right reduction frame/3/bli_l3_oapi_ex.c:753-758
  *         blocked solve + gemm frame/3/trsm/bli_trsm_blk_var1.c:37-189
  *         pre-inverted diagonal ref_kernels/3/bli_trsm_ref.c:40-125
+ *   trmm, symm, gemmt (syrk)    frame/3/bli_l3_oapi_ex.c:609-690, 436-520,
+ *                              151-225 (326-345): the operation's definition on
+ *                              dense temporaries (tri(op(A)), the symmetric A,
+ *                              the full product) through the gemm below, so the
+ *                              rounding of each entry is the gemm micro-kernel's
  *   gemv  var2 (axpyf), var1 (dotxf) frame/2/gemv/bli_gemv_unf_var2.c:37-129,
  *                              bli_gemv_unf_var1.c:37-102; beta == 0 is setv
  *   axpyv ref_kernels/1/bli_axpyv_ref.c:37-120 (alpha == 0 returns)
@@ -306,6 +311,75 @@ void orc_dtrsm(int side, int uplo, int transa, int diag, int64_t m, int64_t n,
                       1.0, b, brs, bcs, nthreads);
         }
     }
+}
+
+/* ------------------------------------------------------------------ */
+/* trmm, symm, gemmt: definitions on dense temporaries through orc_dgemm */
+/* ------------------------------------------------------------------ */
+/* B := alpha tri(op(A)) B (left) or alpha B tri(op(A)) (right), in place. */
+void orc_dtrmm(int side, int uplo, int transa, int diag, int64_t m, int64_t n,
+               double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+               double* b, int64_t rs_b, int64_t cs_b, int nthreads)
+{
+    if (m <= 0 || n <= 0) return;
+    const int64_t na = (side == ORC_LEFT) ? m : n;
+    double* t = (double*)calloc((size_t)(na * na), sizeof(double));  /* tri(A), column-major */
+    double* b0 = (double*)malloc(sizeof(double) * (size_t)(m * n));  /* copy of B, column-major */
+    for (int64_t j = 0; j < na; ++j)
+        for (int64_t i = 0; i < na; ++i) {
+            const int in = (uplo == ORC_LOWER) ? (i >= j) : (i <= j);
+            if (i == j) t[i + j * na] = (diag == ORC_UNIT_DIAG) ? 1.0 : a[i * rs_a + j * cs_a];
+            else if (in) t[i + j * na] = a[i * rs_a + j * cs_a];
+        }
+    for (int64_t j = 0; j < n; ++j)
+        for (int64_t i = 0; i < m; ++i) b0[i + j * m] = b[i * rs_b + j * cs_b];
+    if (side == ORC_LEFT)
+        orc_dgemm(transa, ORC_NO_TRANSPOSE, m, n, m, alpha, t, 1, na, b0, 1, m, 0.0, b, rs_b, cs_b, nthreads);
+    else
+        orc_dgemm(ORC_NO_TRANSPOSE, transa, m, n, n, alpha, b0, 1, m, t, 1, na, 0.0, b, rs_b, cs_b, nthreads);
+    free(t);
+    free(b0);
+}
+
+/* C := alpha A B + beta C (left) or alpha B A + beta C (right), A symmetric
+   with only its uplo triangle read. */
+void orc_dsymm(int side, int uplo, int64_t m, int64_t n, double alpha,
+               const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b,
+               int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c, int nthreads)
+{
+    if (m <= 0 || n <= 0) return;
+    const int64_t na = (side == ORC_LEFT) ? m : n;
+    double* f = (double*)malloc(sizeof(double) * (size_t)(na * na));
+    for (int64_t j = 0; j < na; ++j)
+        for (int64_t i = 0; i < na; ++i) {
+            const int in = (uplo == ORC_LOWER) ? (i >= j) : (i <= j);
+            f[i + j * na] = in ? a[i * rs_a + j * cs_a] : a[j * rs_a + i * cs_a];
+        }
+    if (side == ORC_LEFT)
+        orc_dgemm(ORC_NO_TRANSPOSE, ORC_NO_TRANSPOSE, m, n, m, alpha, f, 1, na, b, rs_b, cs_b, beta, c, rs_c,
+                  cs_c, nthreads);
+    else
+        orc_dgemm(ORC_NO_TRANSPOSE, ORC_NO_TRANSPOSE, m, n, n, alpha, b, rs_b, cs_b, f, 1, na, beta, c, rs_c,
+                  cs_c, nthreads);
+    free(f);
+}
+
+/* The uplo triangle of the m x m C := alpha op(A) op(B) + beta C; the other
+   triangle is left as it is.  Each entry is the gemm micro-kernel's
+   (ab *= alpha; beta == 0 ? c = ab : c = fma(beta, c, ab)). */
+void orc_dgemmt(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha,
+                const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b,
+                int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c, int nthreads)
+{
+    if (m <= 0) return;
+    double* p = (double*)malloc(sizeof(double) * (size_t)(m * m));
+    for (int64_t j = 0; j < m; ++j)
+        for (int64_t i = 0; i < m; ++i) p[i + j * m] = c[i * rs_c + j * cs_c];
+    orc_dgemm(transa, transb, m, m, k, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, p, 1, m, nthreads);
+    for (int64_t j = 0; j < m; ++j)
+        for (int64_t i = 0; i < m; ++i)
+            if ((uplo == ORC_LOWER) ? (i >= j) : (i <= j)) c[i * rs_c + j * cs_c] = p[i + j * m];
+    free(p);
 }
 
 /* ------------------------------------------------------------------ */

@@ -59,6 +59,15 @@ void orc_sgemm(int transa, int transb, int64_t m, int64_t n, int64_t k,
 void orc_dtrsm(int side, int uplo, int transa, int diag, int64_t m, int64_t n,
                double alpha, const double* a, int64_t rs_a, int64_t cs_a,
                double* b, int64_t rs_b, int64_t cs_b, int nthreads);
+void orc_dtrmm(int side, int uplo, int transa, int diag, int64_t m, int64_t n,
+               double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+               double* b, int64_t rs_b, int64_t cs_b, int nthreads);
+void orc_dsymm(int side, int uplo, int64_t m, int64_t n, double alpha,
+               const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b,
+               int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c, int nthreads);
+void orc_dgemmt(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha,
+                const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b,
+                int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c, int nthreads);
 
 /* ---- level-2 / level-1v ---- */
 void orc_dgemv(int transa, int conjx, int64_t m, int64_t n, double alpha,

@@ -41,6 +41,13 @@ def lib():
                                     C.c_float, C.c_void_p, _i64, _i64, C.c_int]
         L.orc_dtrsm.argtypes = [C.c_int] * 4 + [_i64, _i64, C.c_double, C.c_void_p, _i64, _i64,
                                                  C.c_void_p, _i64, _i64, C.c_int]
+        L.orc_dtrmm.argtypes = [C.c_int] * 4 + [_i64, _i64, C.c_double, C.c_void_p, _i64, _i64,
+                                                 C.c_void_p, _i64, _i64, C.c_int]
+        L.orc_dsymm.argtypes = [C.c_int, C.c_int, _i64, _i64, C.c_double, C.c_void_p, _i64, _i64,
+                                C.c_void_p, _i64, _i64, C.c_double, C.c_void_p, _i64, _i64, C.c_int]
+        L.orc_dgemmt.argtypes = [C.c_int] * 3 + [_i64, _i64, C.c_double, C.c_void_p, _i64, _i64,
+                                                  C.c_void_p, _i64, _i64, C.c_double, C.c_void_p, _i64,
+                                                  _i64, C.c_int]
         L.orc_dgemv.argtypes = [C.c_int, C.c_int, _i64, _i64, C.c_double, C.c_void_p, _i64, _i64,
                                 C.c_void_p, _i64, C.c_double, C.c_void_p, _i64]
         L.orc_daxpyv.argtypes = [C.c_int, _i64, C.c_double, C.c_void_p, _i64, C.c_void_p, _i64]
@@ -127,6 +134,28 @@ def dtrsm(side, uplo, transa, diag, alpha, a, b, nthreads=None):
     lib().orc_dtrsm(side, uplo, transa, diag, m, n, alpha, _p(a), *_strides(a), _p(b),
                     *_strides(b), nthreads or nthreads_default())
     return b
+
+
+def dtrmm(side, uplo, transa, diag, alpha, a, b, nthreads=None):
+    m, n = b.shape
+    lib().orc_dtrmm(side, uplo, transa, diag, m, n, alpha, _p(a), *_strides(a), _p(b),
+                    *_strides(b), nthreads or nthreads_default())
+    return b
+
+
+def dsymm(side, uplo, alpha, a, b, beta, c, nthreads=None):
+    m, n = c.shape
+    lib().orc_dsymm(side, uplo, m, n, alpha, _p(a), *_strides(a), _p(b), *_strides(b), beta, _p(c),
+                    *_strides(c), nthreads or nthreads_default())
+    return c
+
+
+def dgemmt(uplo, transa, transb, alpha, a, b, beta, c, nthreads=None):
+    m = c.shape[0]
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    lib().orc_dgemmt(uplo, transa, transb, m, k, alpha, _p(a), *_strides(a), _p(b), *_strides(b), beta,
+                     _p(c), *_strides(c), nthreads or nthreads_default())
+    return c
 
 
 def dgemv(transa, alpha, a, x, beta, y, incx=1, incy=1):

@@ -105,3 +105,27 @@ def test_declared_functions_parser():
     for n in ("dgemm_", "cblas_dgemm", "bli_dgemm", "gb_dgemm_ozaki_dev", "gb_batch_plan_run"):
         assert n in names
     assert C.sizeof(C.c_int32) == 4
+
+
+def test_level3x_argument_errors(gblib, capfd):
+    # frame/compat/check/bla_trmm_check.h, bla_hemm_check.h (symm), bla_syrk_check.h, bla_gemmt_check.h
+    a = np.zeros(64)
+    c = np.full(64, 7.0)
+    blas.dtrmm("L", "X", "N", "N", 2, 2, 1.0, a, 2, c, 2)
+    assert "DTRMM" in capfd.readouterr().out
+    blas.dtrmm("R", "L", "N", "N", 2, 3, 1.0, a, 2, c, 2)  # lda < n on the right
+    assert "parameter number  9" in capfd.readouterr().out
+    blas.dsymm("L", "U", 3, 2, 1.0, a, 3, a, 3, 0.0, c, 2)  # ldc < m
+    assert "parameter number 12" in capfd.readouterr().out
+    blas.dsymm("Q", "U", 3, 2, 1.0, a, 3, a, 3, 0.0, c, 3)
+    assert "parameter number  1" in capfd.readouterr().out
+    blas.dsyrk("L", "X", 2, 2, 1.0, a, 2, 0.0, c, 2)
+    assert "parameter number  2" in capfd.readouterr().out
+    blas.dsyrk("L", "T", 2, 3, 1.0, a, 2, 0.0, c, 2)  # trans: lda < k
+    assert "parameter number  7" in capfd.readouterr().out
+    blas.dgemmt("U", "N", "N", 3, 2, 1.0, a, 3, a, 1, 0.0, c, 3)  # ldb < k
+    assert "parameter number 10" in capfd.readouterr().out
+    blas.dgemmt("U", "N", "N", -1, 2, 1.0, a, 3, a, 2, 0.0, c, 3)
+    assert "DGEMMT" in capfd.readouterr().out
+    assert (c == 7.0).all()
+    _last()
