@@ -57,6 +57,11 @@ def load(path=None):
     _sig(L, "dgemm_batch_", None, batch)
     _sig(L, "sgemm_batch_", None, batch)
     _sig(L, "xerbla_", C.c_int, [_cp, _ip, C.c_long])
+    _sig(L, "dscal_", None, [_ip, _dp, _vp, _ip])
+    _sig(L, "dcopy_", None, [_ip, _vp, _ip, _vp, _ip])
+    _sig(L, "idamax_", _i32, [_ip, _vp, _ip])
+    _sig(L, "dger_", None, [_ip, _ip, _dp, _vp, _ip, _vp, _ip, _vp, _ip])
+    _sig(L, "dtrsv_", None, [_cp, _cp, _cp, _ip, _vp, _ip, _vp, _ip])
     _sig(L, "dtrmm_", None, [_cp, _cp, _cp, _cp, _ip, _ip, _dp, _vp, _ip, _vp, _ip])
     _sig(L, "dsymm_", None, [_cp, _cp, _ip, _ip, _dp, _vp, _ip, _vp, _ip, _dp, _vp, _ip])
     _sig(L, "dsyrk_", None, [_cp, _cp, _ip, _ip, _dp, _vp, _ip, _dp, _vp, _ip])
@@ -76,6 +81,11 @@ def load(path=None):
     tt = [C.c_int] * 4 + [_i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64]
     _sig(L, "bli_dtrsm", None, tt)
     _sig(L, "bli_dtrsm_ex", None, tt + [_vp, _vp])
+    _sig(L, "bli_dscalv", None, [C.c_int, _i64, _vp, _vp, _i64])
+    _sig(L, "bli_dcopyv", None, [C.c_int, _i64, _vp, _i64, _vp, _i64])
+    _sig(L, "bli_damaxv", None, [_i64, _vp, _i64, _vp])
+    _sig(L, "bli_dger", None, [C.c_int, C.c_int, _i64, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _i64])
+    _sig(L, "bli_dtrsv", None, [C.c_int] * 3 + [_i64, _vp, _vp, _i64, _i64, _vp, _i64])
     _sig(L, "bli_dtrmm", None, tt)
     _sig(L, "bli_dsymm", None, [C.c_int] * 4 + [_i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp,
                                                  _i64, _i64])
@@ -95,6 +105,11 @@ def load(path=None):
     sg = [C.c_int, C.c_int, _i64, _i64, _i64, _f, _vp, _i64, _i64, _vp, _i64, _i64, _f, _vp, _i64, _i64]
     _sig(L, "gb_sgemm_dev", C.c_int, sg + [_vp])
     _sig(L, "gb_dtrsm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_dscalv_dev", C.c_int, [_i64, _d, _vp, _i64, _vp])
+    _sig(L, "gb_dcopyv_dev", C.c_int, [_i64, _vp, _i64, _vp, _i64, _vp])
+    _sig(L, "gb_damaxv_dev", C.c_int, [_i64, _vp, _i64, _vp, _vp])
+    _sig(L, "gb_dger_dev", C.c_int, [_i64, _i64, _d, _vp, _i64, _vp, _i64, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_dtrsv_dev", C.c_int, [C.c_int] * 3 + [_i64, _d, _vp, _i64, _i64, _vp, _i64, _vp])
     _sig(L, "gb_dtrmm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _vp])
     _sig(L, "gb_dsymm_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _d,
                                       _vp, _i64, _i64, _vp])

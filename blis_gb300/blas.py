@@ -55,6 +55,53 @@ def dtrsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
                        C.byref(C.c_double(alpha)), _p(a), _i(lda), _p(b), _i(ldb))
 
 
+def dscal(n, alpha, x, incx=1):
+    _lib.load().dscal_(_i(n), _d(alpha), _p(x), _i(incx))
+
+
+def dcopy(n, x, incx, y, incy):
+    _lib.load().dcopy_(_i(n), _p(x), _i(incx), _p(y), _i(incy))
+
+
+def idamax(n, x, incx=1):
+    return int(_lib.load().idamax_(_i(n), _p(x), _i(incx)))
+
+
+def dger(m, n, alpha, x, incx, y, incy, a, lda):
+    _lib.load().dger_(_i(m), _i(n), _d(alpha), _p(x), _i(incx), _p(y), _i(incy), _p(a), _i(lda))
+
+
+def dtrsv(uplo, trans, diag, m, a, lda, x, incx=1):
+    _lib.load().dtrsv_(_c(uplo), _c(trans), _c(diag), _i(m), _p(a), _i(lda), _p(x), _i(incx))
+
+
+def bli_dscalv(alpha, x, n=None, incx=1):
+    n = x.size if n is None else n
+    _lib.load().bli_dscalv(0, n, _d(alpha), _p(x), incx)
+
+
+def bli_dcopyv(x, y, n=None, incx=1, incy=1):
+    n = x.size if n is None else n
+    _lib.load().bli_dcopyv(0, n, _p(x), incx, _p(y), incy)
+
+
+def bli_damaxv(x, n=None, incx=1):
+    n = x.size if n is None else n
+    idx = C.c_int64(-1)
+    _lib.load().bli_damaxv(n, _p(x), incx, C.byref(idx))
+    return idx.value
+
+
+def bli_dger(alpha, x, y, a, incx=1, incy=1):
+    m, n = a.shape
+    _lib.load().bli_dger(0, 0, m, n, _d(alpha), _p(x), incx, _p(y), incy, _p(a), *_st(a))
+
+
+def bli_dtrsv(uplo, transa, diag, alpha, a, x, incx=1):
+    m = a.shape[0]
+    _lib.load().bli_dtrsv(uplo, transa, diag, m, _d(alpha), _p(a), *_st(a), _p(x), incx)
+
+
 def dtrmm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
     _lib.load().dtrmm_(_c(side), _c(uplo), _c(transa), _c(diag), _i(m), _i(n), _d(alpha), _p(a), _i(lda),
                        _p(b), _i(ldb))

@@ -558,6 +558,98 @@ int gemmt_host(int uplo, int transa, int transb, int64_t m, int64_t k, double al
     return finish(s, where);
 }
 
+int scalv_host(int64_t n, double alpha, double* x, int64_t incx, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (n <= 0 || alpha == 1.0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    Staged& X = bufs.next();
+    if ((rc = stage_in(x, n, 1, incx, n, 8, alpha != 0.0 || incx == 0, &X, s))) return rc;
+    if ((rc = dscalv_dev(n, alpha, reinterpret_cast<double*>(X.origin), X.rs, s))) return rc;
+    if ((rc = stage_out(x, n, 1, incx, n, 8, X, s))) return rc;
+    return finish(s, where);
+}
+
+int copyv_host(int64_t n, const double* x, int64_t incx, double* y, int64_t incy, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    Staged& X = bufs.next();
+    Staged& Y = bufs.next();
+    if ((rc = stage_in(x, n, 1, incx, n, 8, true, &X, s))) return rc;
+    if ((rc = stage_in(y, n, 1, incy, n, 8, false, &Y, s))) return rc;
+    if ((rc = dcopyv_dev(n, reinterpret_cast<const double*>(X.origin), X.rs, reinterpret_cast<double*>(Y.origin),
+                         Y.rs, s)))
+        return rc;
+    if ((rc = stage_out(y, n, 1, incy, n, 8, Y, s))) return rc;
+    return finish(s, where);
+}
+
+int amaxv_host(int64_t n, const double* x, int64_t incx, int64_t* index, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    *index = 0;
+    if (n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    Staged& X = bufs.next();
+    if ((rc = stage_in(x, n, 1, incx, n, 8, true, &X, s))) return rc;
+    int64_t* d = static_cast<int64_t*>(dev_alloc(sizeof(int64_t), s));
+    if (!d) return GB_ERR_NOMEM;
+    rc = damaxv_dev(n, reinterpret_cast<const double*>(X.origin), X.rs, d, s);
+    if (!rc) rc = check_cuda(cudaMemcpyAsync(index, d, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "amaxv");
+    dev_free(d, s);
+    if (rc) return rc;
+    return finish(s, where);
+}
+
+int ger_host(int64_t m, int64_t n, double alpha, const double* x, int64_t incx, const double* y, int64_t incy,
+             double* a, int64_t rs_a, int64_t cs_a, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0 || alpha == 0.0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    Staged& A = bufs.next();
+    Staged& X = bufs.next();
+    Staged& Y = bufs.next();
+    if ((rc = stage_in(a, m, n, rs_a, cs_a, 8, true, &A, s))) return rc;
+    if ((rc = stage_in(x, m, 1, incx, m, 8, true, &X, s))) return rc;
+    if ((rc = stage_in(y, n, 1, incy, n, 8, true, &Y, s))) return rc;
+    if ((rc = dger_dev(m, n, alpha, reinterpret_cast<const double*>(X.origin), X.rs,
+                       reinterpret_cast<const double*>(Y.origin), Y.rs, reinterpret_cast<double*>(A.origin), A.rs,
+                       A.cs, s)))
+        return rc;
+    if ((rc = stage_out(a, m, n, rs_a, cs_a, 8, A, s))) return rc;
+    return finish(s, where);
+}
+
+int trsv_host(int uplo, int transa, int diag, int64_t m, double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+              double* x, int64_t incx, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    Staged& X = bufs.next();
+    if ((rc = stage_in(x, m, 1, incx, m, 8, true, &X, s))) return rc;
+    Staged& A = bufs.next();
+    if (alpha != 0.0 && (rc = stage_in(a, m, m, rs_a, cs_a, 8, true, &A, s))) return rc;
+    if ((rc = dtrsv_dev(uplo, transa, diag, m, alpha, reinterpret_cast<const double*>(A.origin), A.rs, A.cs,
+                        reinterpret_cast<double*>(X.origin), X.rs, s)))
+        return rc;
+    if ((rc = stage_out(x, m, 1, incx, m, 8, X, s))) return rc;
+    return finish(s, where);
+}
+
 // ---------------------------------------------------------------- BLAS helpers
 bool lsame(char a, char b) { return toupper((unsigned char)a) == toupper((unsigned char)b); }
 
@@ -816,6 +908,69 @@ void dgemv_(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n,
               const_cast<double*>(blas_vec<double>(y, m_y, *incy)), *incy, "DGEMV ");
 }
 
+void dscal_(const gb_f77_int* n, const double* alpha, double* x, const gb_f77_int* incx)
+{
+    // frame/compat/bla_scal.c:44-85: no argument checks; negative increments by pointer
+    const int64_t n0 = (*n > 0) ? *n : 0;
+    scalv_host(n0, *alpha, const_cast<double*>(blas_vec<double>(x, n0, *incx)), *incx, "DSCAL");
+}
+
+void dcopy_(const gb_f77_int* n, const double* x, const gb_f77_int* incx, double* y, const gb_f77_int* incy)
+{
+    // frame/compat/bla_copy.c:44-81
+    const int64_t n0 = (*n > 0) ? *n : 0;
+    copyv_host(n0, blas_vec(x, n0, *incx), *incx, const_cast<double*>(blas_vec<double>(y, n0, *incy)), *incy,
+               "DCOPY");
+}
+
+gb_f77_int idamax_(const gb_f77_int* n, const double* x, const gb_f77_int* incx)
+{
+    // frame/compat/bla_amax.c:44-91: empty vector or non-positive increment -> 0, else 1-based
+    if (*n < 1 || *incx <= 0) return 0;
+    int64_t idx = 0;
+    if (amaxv_host(*n, x, *incx, &idx, "IDAMAX")) return 0;
+    return (gb_f77_int)(idx + 1);
+}
+
+void dger_(const gb_f77_int* m, const gb_f77_int* n, const double* alpha, const double* x, const gb_f77_int* incx,
+           const double* y, const gb_f77_int* incy, double* a, const gb_f77_int* lda)
+{
+    // frame/compat/bla_ger.c:44-106, checks frame/compat/check/bla_ger_check.h:37-68
+    int info = 0;
+    if (*m < 0) info = 1;
+    else if (*n < 0) info = 2;
+    else if (*incx == 0) info = 5;
+    else if (*incy == 0) info = 7;
+    else if (*lda < (*m > 1 ? *m : 1)) info = 9;
+    if (info) {
+        call_xerbla("DGER  ", info);
+        return;
+    }
+    ger_host(*m, *n, *alpha, blas_vec(x, *m, *incx), *incx, blas_vec(y, *n, *incy), *incy, a, 1, *lda, "DGER");
+}
+
+void dtrsv_(const gb_f77_char* uploa, const gb_f77_char* transa, const gb_f77_char* diaga, const gb_f77_int* m,
+            const double* a, const gb_f77_int* lda, double* x, const gb_f77_int* incx)
+{
+    // frame/compat/bla_trsv.c:44-113, checks frame/compat/check/bla_trmv_check.h:37-77
+    const bool lower = lsame(*uploa, 'L'), upper = lsame(*uploa, 'U');
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T'), conja = lsame(*transa, 'C');
+    const bool unita = lsame(*diaga, 'U'), nonua = lsame(*diaga, 'N');
+    int info = 0;
+    if (!lower && !upper) info = 1;
+    else if (!nota && !ta && !conja) info = 2;
+    else if (!unita && !nonua) info = 3;
+    else if (*m < 0) info = 4;
+    else if (*lda < (*m > 1 ? *m : 1)) info = 6;
+    else if (*incx == 0) info = 8;
+    if (info) {
+        call_xerbla("DTRSV ", info);
+        return;
+    }
+    trsv_host(lower ? GB_LOWER : GB_UPPER, map_trans(*transa), unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, 1.0, a,
+              1, *lda, const_cast<double*>(blas_vec<double>(x, *m, *incx)), *incx, "DTRSV");
+}
+
 void daxpy_(const gb_f77_int* n, const double* alpha, const double* x, const gb_f77_int* incx,
             double* y, const gb_f77_int* incy)
 {
@@ -951,6 +1106,39 @@ void bli_dtrsm_ex(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t 
     (void)cntx;
     (void)rntm;
     bli_dtrsm(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b);
+}
+
+void bli_dscalv(gb_conj_t conjalpha, gb_dim_t n, const double* alpha, double* x, gb_inc_t incx)
+{
+    (void)conjalpha;  // real
+    scalv_host(n, *alpha, x, incx, "bli_dscalv");
+}
+
+void bli_dcopyv(gb_conj_t conjx, gb_dim_t n, const double* x, gb_inc_t incx, double* y, gb_inc_t incy)
+{
+    (void)conjx;
+    copyv_host(n, x, incx, y, incy, "bli_dcopyv");
+}
+
+void bli_damaxv(gb_dim_t n, const double* x, gb_inc_t incx, gb_dim_t* index)
+{
+    int64_t idx = 0;
+    amaxv_host(n, x, incx, &idx, "bli_damaxv");
+    *index = idx;
+}
+
+void bli_dger(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t m, gb_dim_t n, const double* alpha, const double* x,
+              gb_inc_t incx, const double* y, gb_inc_t incy, double* a, gb_inc_t rs_a, gb_inc_t cs_a)
+{
+    (void)conjx;
+    (void)conjy;
+    ger_host(m, n, *alpha, x, incx, y, incy, a, rs_a, cs_a, "bli_dger");
+}
+
+void bli_dtrsv(gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, const double* alpha, const double* a,
+               gb_inc_t rs_a, gb_inc_t cs_a, double* x, gb_inc_t incx)
+{
+    trsv_host(uploa, transa, diaga, m, *alpha, a, rs_a, cs_a, x, incx, "bli_dtrsv");
 }
 
 void bli_dtrmm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
@@ -1137,6 +1325,45 @@ int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
     const int slices = (gb::dgemm_mode() == GB_DGEMM_OZAKI) ? gb::ozaki_slices() : 0;
     return gb::dtrsm_dev(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, slices,
                          pick_stream(stream));
+}
+
+int gb_dscalv_dev(gb_dim_t n, double alpha, double* x, gb_inc_t incx, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    return gb::dscalv_dev(n, alpha, x, incx, pick_stream(stream));
+}
+
+int gb_dcopyv_dev(gb_dim_t n, const double* x, gb_inc_t incx, double* y, gb_inc_t incy, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    return gb::dcopyv_dev(n, x, incx, y, incy, pick_stream(stream));
+}
+
+int gb_damaxv_dev(gb_dim_t n, const double* x, gb_inc_t incx, gb_dim_t* index_dev, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    return gb::damaxv_dev(n, x, incx, index_dev, pick_stream(stream));
+}
+
+int gb_dger_dev(gb_dim_t m, gb_dim_t n, double alpha, const double* x, gb_inc_t incx, const double* y, gb_inc_t incy,
+                double* a, gb_inc_t rs_a, gb_inc_t cs_a, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_dger_dev", "negative dimension");
+    return gb::dger_dev(m, n, alpha, x, incx, y, incy, a, rs_a, cs_a, pick_stream(stream));
+}
+
+int gb_dtrsv_dev(gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, double alpha, const double* a,
+                 gb_inc_t rs_a, gb_inc_t cs_a, double* x, gb_inc_t incx, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0) return gb::set_error(GB_ERR_ARG, "gb_dtrsv_dev", "negative dimension");
+    return gb::dtrsv_dev(uploa, transa, diaga, m, alpha, a, rs_a, cs_a, x, incx, pick_stream(stream));
 }
 
 int gb_dtrmm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,

@@ -105,6 +105,13 @@ int64_t ozaki_kpart_limit(int slices);
 // Lanes per right-hand side (1, 2, 4, 8) for the 64-row diagonal-block
 // kernels of trsm and trmm, from the FP64-instruction cost model (gb_trsm.cu).
 int diag_block_lanes(int64_t ncols);
+int dscalv_dev(int64_t n, double alpha, double* x, int64_t incx, cudaStream_t s);
+int dcopyv_dev(int64_t n, const double* x, int64_t incx, double* y, int64_t incy, cudaStream_t s);
+int damaxv_dev(int64_t n, const double* x, int64_t incx, int64_t* index_dev, cudaStream_t s);
+int dger_dev(int64_t m, int64_t n, double alpha, const double* x, int64_t incx, const double* y, int64_t incy,
+             double* a, int64_t rs_a, int64_t cs_a, cudaStream_t s);
+int dtrsv_dev(int uplo, int transa, int diag, int64_t m, double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+              double* x, int64_t incx, cudaStream_t s);
 int dtrmm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, double alpha,
               const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b, int slices,
               cudaStream_t s);

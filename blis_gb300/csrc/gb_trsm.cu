@@ -187,6 +187,8 @@ int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t cco
     const double* ap = t.a + r0 * t.ars + c0 * t.acs;
     const double* xp = t.b + c0 * t.brs;
     double* bp = t.b + r0 * t.brs;
+    if (t.n == 1)  // one right-hand side (trsv): a gemv, in either form
+        return dgemv_dev(GB_NO_TRANSPOSE, rcount, ccount, -1.0, ap, t.ars, t.acs, xp, t.brs, 1.0, bp, t.brs, t.s);
     if (t.slices > 0 && (double)rcount * (double)ccount * (double)t.n >= trsm_ozaki_min_fma())
         return dgemm_ozaki(rcount, t.n, ccount, -1.0, ap, t.ars, t.acs, xp, t.brs, t.bcs, 1.0, bp,
                            t.brs, t.bcs, t.slices, t.s);

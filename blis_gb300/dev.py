@@ -70,6 +70,36 @@ def dtrsm(side, uplo, transa, diag, alpha, a, b):
     return _lib.check(rc, "gb_dtrsm_dev")
 
 
+def dscalv(alpha, x, incx=1, n=None):
+    n = x.numel() if n is None else n
+    return _lib.check(_lib.load().gb_dscalv_dev(n, alpha, x.data_ptr(), incx, _stream()), "gb_dscalv_dev")
+
+
+def dcopyv(x, y, incx=1, incy=1, n=None):
+    n = x.numel() if n is None else n
+    return _lib.check(_lib.load().gb_dcopyv_dev(n, x.data_ptr(), incx, y.data_ptr(), incy, _stream()),
+                      "gb_dcopyv_dev")
+
+
+def damaxv(x, index, incx=1, n=None):
+    """0-based index of the first largest |x_i| (first NaN) into the int64 tensor `index`."""
+    n = x.numel() if n is None else n
+    return _lib.check(_lib.load().gb_damaxv_dev(n, x.data_ptr(), incx, index.data_ptr(), _stream()),
+                      "gb_damaxv_dev")
+
+
+def dger(alpha, x, y, a, incx=1, incy=1):
+    m, n = a.shape
+    return _lib.check(_lib.load().gb_dger_dev(m, n, alpha, x.data_ptr(), incx, y.data_ptr(), incy, a.data_ptr(),
+                                              *_rc(a), _stream()), "gb_dger_dev")
+
+
+def dtrsv(uplo, transa, diag, alpha, a, x, incx=1):
+    m = a.shape[0]
+    return _lib.check(_lib.load().gb_dtrsv_dev(uplo, transa, diag, m, alpha, a.data_ptr(), *_rc(a), x.data_ptr(),
+                                               incx, _stream()), "gb_dtrsv_dev")
+
+
 def dtrmm(side, uplo, transa, diag, alpha, a, b):
     m, n = b.shape
     rc = _lib.load().gb_dtrmm_dev(side, uplo, transa, diag, m, n, alpha, a.data_ptr(), *_rc(a),

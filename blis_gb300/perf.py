@@ -14,6 +14,7 @@ L2 where the workload allows:
   daxpyv_2^28     24 n bytes; ddotv_2^28: 16 n bytes                (HBM)
   dtrsm_16384     L/L/N/N, B entries (1+u) 2^e, e in [-20,20]: native and
                   Ozaki updates, sampled componentwise backward error
+  level12x        dscal / dcopy / idamax at 2^28, dger 32768^2, dtrsv 16384
   level3x         dtrmm 8192x4096 (m^2 n), dsyrk n=k=8192 (n^2 k), dsymm
                   8192x4096 (2 m^2 n): native FP64 and Ozaki (7 slices)
   batch_4096      4096 problems, m,n,k log-uniform in [16,1024], random
@@ -349,9 +350,49 @@ def run_level3x(out):
     _lib.load().gb_set_dgemm_mode(0, 8)
 
 
+def run_level12x(out):
+    """dscal / dcopy (16 B per element) and idamax (8 B) at n = 2^28, dger on
+    32768^2 (16 B per matrix element), dtrsv L/N/N m = 16384 (latency: 256
+    diagonal blocks and gemv updates); HBM figures against the measured copy
+    bandwidth."""
+    import torch
+    pk, kind = peaks()
+    hbm = pk.get("hbm_gbs", 6800.0)
+    n = 1 << (25 if SMALL else 28)
+    x = _mat(n, 1, seed=61).view(-1)
+    y = torch.empty_like(x)
+    idx = torch.zeros(1, dtype=torch.int64, device="cuda")
+    for name, fn, byts in (("dscal", lambda: dev.dscalv(1.0000001, x), 16.0 * n),
+                           ("dcopy", lambda: dev.dcopyv(x, y), 16.0 * n),
+                           ("idamax", lambda: dev.damaxv(x, idx), 8.0 * n)):
+        ms = _timer(fn, reps=10)
+        gbs = byts / ms / 1e6
+        out.append({"workload": "%s_2^%d" % (name, 25 if SMALL else 28), "ms": ms, "gb_s": gbs,
+                    "frac_of_hbm": gbs / hbm, "peak": "%s hbm_gbs" % kind})
+    del x, y
+    m = 8192 if SMALL else 32768
+    a = _mat(m, m, seed=62)
+    xv = _mat(m, 1, seed=63).view(-1)
+    yv = _mat(m, 1, seed=64).view(-1)
+    ms = _timer(lambda: dev.dger(1e-9, xv, yv, a), reps=5)
+    gbs = 16.0 * m * m / ms / 1e6
+    out.append({"workload": "dger_%d" % m, "ms": ms, "gb_s": gbs, "frac_of_hbm": gbs / hbm,
+                "peak": "%s hbm_gbs" % kind})
+    del a
+    mt = 16384
+    t = _mat(mt, mt, seed=65)
+    t.copy_(torch.tril(t))
+    d = torch.arange(mt, device="cuda")
+    t[d, d] = mt + t[d, d].abs()
+    b = _mat(mt, 1, seed=66).view(-1)
+    xs = b.clone()
+    ms = _timer(lambda: (xs.copy_(b), dev.dtrsv(0xC0, 0, 0, 1.0, t, xs)), reps=3, warmup=1)
+    out.append({"workload": "dtrsv_%d" % mt, "ms": ms, "gflops": float(mt) * mt / ms / 1e6})
+
+
 SUITES = {"gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
           "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm, "bgemm": run_bgemm,
-          "level3x": run_level3x}
+          "level3x": run_level3x, "level12x": run_level12x}
 
 
 def main():

@@ -115,6 +115,24 @@ void dgemmt_(const gb_f77_char* uploc, const gb_f77_char* transa, const gb_f77_c
              const gb_f77_int* lda, const double* b, const gb_f77_int* ldb, const double* beta,
              double* c, const gb_f77_int* ldc);
 
+/* replace dscal_ (frame/compat/bla_scal.c:44-85; alpha == 0 sets zeros
+   without reading x, ref_kernels/1/bli_scalv_ref.c:54-75), dcopy_
+   (frame/compat/bla_copy.c:44-81), idamax_ (frame/compat/bla_amax.c:44-91:
+   1-based, 0 for n < 1 or incx <= 0; the first NaN, else the first largest
+   |x_i|, ref_kernels/1/bli_amaxv_ref.c:97-106), dger_ (frame/compat/bla_ger.c:
+   44-106, checks frame/compat/check/bla_ger_check.h:37-68) and dtrsv_
+   (frame/compat/bla_trsv.c:44-113, checks bla_trmv_check.h:37-77) */
+void dscal_(const gb_f77_int* n, const double* alpha, double* x, const gb_f77_int* incx);
+void dcopy_(const gb_f77_int* n, const double* x, const gb_f77_int* incx, double* y,
+            const gb_f77_int* incy);
+gb_f77_int idamax_(const gb_f77_int* n, const double* x, const gb_f77_int* incx);
+void dger_(const gb_f77_int* m, const gb_f77_int* n, const double* alpha, const double* x,
+           const gb_f77_int* incx, const double* y, const gb_f77_int* incy, double* a,
+           const gb_f77_int* lda);
+void dtrsv_(const gb_f77_char* uploa, const gb_f77_char* transa, const gb_f77_char* diaga,
+            const gb_f77_int* m, const double* a, const gb_f77_int* lda, double* x,
+            const gb_f77_int* incx);
+
 /* replaces dgemv_, frame/compat/bla_gemv.c:45-143 (checks
    frame/compat/check/bla_gemv_check.h:37-75; n_x == 0 returns untouched, :95-106) */
 void dgemv_(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n,
@@ -212,6 +230,20 @@ void bli_sgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_
                const float* alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a,
                const float* b, gb_inc_t rs_b, gb_inc_t cs_b, const float* beta,
                float* c, gb_inc_t rs_c, gb_inc_t cs_c);
+
+/* replace bli_dscalv (frame/1/bli_l1v_tapi.c:314-345), bli_dcopyv (:46-77),
+   bli_damaxv (:84-112), bli_dger (frame/2/bli_l2_tapi.c:129-175) and
+   bli_dtrsv (:441-509); conjugation is the identity for real data */
+void bli_dscalv(gb_conj_t conjalpha, gb_dim_t n, const double* alpha, double* x, gb_inc_t incx);
+void bli_dcopyv(gb_conj_t conjx, gb_dim_t n, const double* x, gb_inc_t incx, double* y,
+                gb_inc_t incy);
+void bli_damaxv(gb_dim_t n, const double* x, gb_inc_t incx, gb_dim_t* index);
+void bli_dger(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t m, gb_dim_t n, const double* alpha,
+              const double* x, gb_inc_t incx, const double* y, gb_inc_t incy, double* a,
+              gb_inc_t rs_a, gb_inc_t cs_a);
+void bli_dtrsv(gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+               const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, double* x,
+               gb_inc_t incx);
 
 /* replace bli_dtrmm (frame/3/bli_l3_tapi_ex.c:536-585), bli_dsymm
    (:104-164; conja is the identity for real data, transb applies to B),
@@ -318,6 +350,19 @@ int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
 int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
                  gb_dim_t m, gb_dim_t n, double alpha, const double* a, gb_inc_t rs_a,
                  gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
+
+/* Device-pointer forms of scalv, copyv, amaxv (the 0-based index written to
+   device memory), ger and trsv (asynchronous on the stream). */
+int gb_dscalv_dev(gb_dim_t n, double alpha, double* x, gb_inc_t incx, void* stream);
+int gb_dcopyv_dev(gb_dim_t n, const double* x, gb_inc_t incx, double* y, gb_inc_t incy,
+                  void* stream);
+int gb_damaxv_dev(gb_dim_t n, const double* x, gb_inc_t incx, gb_dim_t* index_dev, void* stream);
+int gb_dger_dev(gb_dim_t m, gb_dim_t n, double alpha, const double* x, gb_inc_t incx,
+                const double* y, gb_inc_t incy, double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                void* stream);
+int gb_dtrsv_dev(gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, double alpha,
+                 const double* a, gb_inc_t rs_a, gb_inc_t cs_a, double* x, gb_inc_t incx,
+                 void* stream);
 
 /* Device-pointer forms of trmm, symm, gemmt and syrk (asynchronous on the
    stream; native FP64 or the Ozaki form by gb_set_dgemm_mode, with a fixed

@@ -27,6 +27,11 @@
  *   gemv  var2 (axpyf), var1 (dotxf) frame/2/gemv/bli_gemv_unf_var2.c:37-129,
  *                              bli_gemv_unf_var1.c:37-102; beta == 0 is setv
  *   axpyv ref_kernels/1/bli_axpyv_ref.c:37-120 (alpha == 0 returns)
+ *   scalv ref_kernels/1/bli_scalv_ref.c:40-98 (alpha == 1 returns, 0 sets)
+ *   copyv ref_kernels/1/bli_copyv_ref.c
+ *   amaxv ref_kernels/1/bli_amaxv_ref.c:44-140 (first NaN, else first max)
+ *   ger   column-wise axpys a_j += (alpha y_j) x, frame/2/ger/bli_ger_unb_var2.c
+ *   trsv  orc_dtrsm on one column (frame/2/trsv: the same substitution)
  *   dotv  ref_kernels/1/bli_dotv_ref.c:37-121 (n == 0 gives rho = 0)
  * Not in the reference: the double-double evaluator (error oracle) and the
  * Ozaki split-product model (Ozaki, Ogita, Oishi & Rump 2012; integer-slice
@@ -418,6 +423,47 @@ void orc_daxpyv(int conjx, int64_t n, double alpha, const double* x, int64_t inc
     (void)conjx;
     if (n <= 0 || alpha == 0.0) return;
     for (int64_t i = 0; i < n; ++i) y[i * incy] = fma(alpha, x[i * incx], y[i * incy]);
+}
+
+void orc_dscalv(int64_t n, double alpha, double* x, int64_t incx)
+{
+    if (n <= 0 || alpha == 1.0) return;
+    for (int64_t i = 0; i < n; ++i) x[i * incx] = (alpha == 0.0) ? 0.0 : alpha * x[i * incx];
+}
+
+void orc_dcopyv(int64_t n, const double* x, int64_t incx, double* y, int64_t incy)
+{
+    for (int64_t i = 0; i < n; ++i) y[i * incy] = x[i * incx];
+}
+
+void orc_damaxv(int64_t n, const double* x, int64_t incx, int64_t* index)
+{
+    int64_t best = 0;
+    double vmax = -1.0;
+    for (int64_t i = 0; i < n; ++i) {
+        const double v = fabs(x[i * incx]);
+        if (vmax < v || (isnan(v) && !isnan(vmax))) {
+            vmax = v;
+            best = i;
+        }
+    }
+    *index = best;
+}
+
+void orc_dger(int64_t m, int64_t n, double alpha, const double* x, int64_t incx, const double* y,
+              int64_t incy, double* a, int64_t rs_a, int64_t cs_a)
+{
+    if (m <= 0 || n <= 0 || alpha == 0.0) return;
+    for (int64_t j = 0; j < n; ++j) {
+        const double ay = alpha * y[j * incy];
+        for (int64_t i = 0; i < m; ++i) a[i * rs_a + j * cs_a] = fma(ay, x[i * incx], a[i * rs_a + j * cs_a]);
+    }
+}
+
+void orc_dtrsv(int uplo, int transa, int diag, int64_t m, double alpha, const double* a, int64_t rs_a,
+               int64_t cs_a, double* x, int64_t incx)
+{
+    orc_dtrsm(ORC_LEFT, uplo, transa, diag, m, 1, alpha, a, rs_a, cs_a, x, incx, 1, 1);
 }
 
 void orc_ddotv(int conjx, int conjy, int64_t n, const double* x, int64_t incx,

@@ -75,6 +75,13 @@ void orc_dgemv(int transa, int conjx, int64_t m, int64_t n, double alpha,
                const double* x, int64_t incx, double beta, double* y, int64_t incy);
 void orc_daxpyv(int conjx, int64_t n, double alpha, const double* x, int64_t incx,
                 double* y, int64_t incy);
+void orc_dscalv(int64_t n, double alpha, double* x, int64_t incx);
+void orc_dcopyv(int64_t n, const double* x, int64_t incx, double* y, int64_t incy);
+void orc_damaxv(int64_t n, const double* x, int64_t incx, int64_t* index);
+void orc_dger(int64_t m, int64_t n, double alpha, const double* x, int64_t incx, const double* y,
+              int64_t incy, double* a, int64_t rs_a, int64_t cs_a);
+void orc_dtrsv(int uplo, int transa, int diag, int64_t m, double alpha, const double* a, int64_t rs_a,
+               int64_t cs_a, double* x, int64_t incx);
 void orc_ddotv(int conjx, int conjy, int64_t n, const double* x, int64_t incx,
                const double* y, int64_t incy, double* rho);
 

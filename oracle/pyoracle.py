@@ -48,6 +48,12 @@ def lib():
         L.orc_dgemmt.argtypes = [C.c_int] * 3 + [_i64, _i64, C.c_double, C.c_void_p, _i64, _i64,
                                                   C.c_void_p, _i64, _i64, C.c_double, C.c_void_p, _i64,
                                                   _i64, C.c_int]
+        L.orc_dscalv.argtypes = [_i64, C.c_double, C.c_void_p, _i64]
+        L.orc_dcopyv.argtypes = [_i64, C.c_void_p, _i64, C.c_void_p, _i64]
+        L.orc_damaxv.argtypes = [_i64, C.c_void_p, _i64, C.c_void_p]
+        L.orc_dger.argtypes = [_i64, _i64, C.c_double, C.c_void_p, _i64, C.c_void_p, _i64, C.c_void_p, _i64,
+                               _i64]
+        L.orc_dtrsv.argtypes = [C.c_int] * 3 + [_i64, C.c_double, C.c_void_p, _i64, _i64, C.c_void_p, _i64]
         L.orc_dgemv.argtypes = [C.c_int, C.c_int, _i64, _i64, C.c_double, C.c_void_p, _i64, _i64,
                                 C.c_void_p, _i64, C.c_double, C.c_void_p, _i64]
         L.orc_daxpyv.argtypes = [C.c_int, _i64, C.c_double, C.c_void_p, _i64, C.c_void_p, _i64]
@@ -156,6 +162,37 @@ def dgemmt(uplo, transa, transb, alpha, a, b, beta, c, nthreads=None):
     lib().orc_dgemmt(uplo, transa, transb, m, k, alpha, _p(a), *_strides(a), _p(b), *_strides(b), beta,
                      _p(c), *_strides(c), nthreads or nthreads_default())
     return c
+
+
+def dscalv(alpha, x, n=None, incx=1):
+    n = x.size if n is None else n
+    lib().orc_dscalv(n, alpha, _p(x), incx)
+    return x
+
+
+def dcopyv(x, y, n=None, incx=1, incy=1):
+    n = x.size if n is None else n
+    lib().orc_dcopyv(n, _p(x), incx, _p(y), incy)
+    return y
+
+
+def damaxv(x, n=None, incx=1):
+    n = x.size if n is None else n
+    idx = C.c_int64(-1)
+    lib().orc_damaxv(n, _p(x), incx, C.byref(idx))
+    return idx.value
+
+
+def dger(alpha, x, y, a, incx=1, incy=1):
+    m, n = a.shape
+    lib().orc_dger(m, n, alpha, _p(x), incx, _p(y), incy, _p(a), *_strides(a))
+    return a
+
+
+def dtrsv(uplo, transa, diag, alpha, a, x, incx=1):
+    m = a.shape[0]
+    lib().orc_dtrsv(uplo, transa, diag, m, alpha, _p(a), *_strides(a), _p(x), incx)
+    return x
 
 
 def dgemv(transa, alpha, a, x, beta, y, incx=1, incy=1):

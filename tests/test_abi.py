@@ -129,3 +129,21 @@ def test_level3x_argument_errors(gblib, capfd):
     assert "DGEMMT" in capfd.readouterr().out
     assert (c == 7.0).all()
     _last()
+
+
+def test_level12x_argument_errors(gblib, capfd):
+    # frame/compat/check/bla_ger_check.h:37-68, bla_trmv_check.h:37-77 (trsv)
+    a = np.full(64, 7.0)
+    x = np.ones(8)
+    blas.dger(2, 2, 1.0, x, 0, x, 1, a, 2)
+    assert "parameter number  5" in capfd.readouterr().out
+    blas.dger(3, 2, 1.0, x, 1, x, 1, a, 2)
+    assert "parameter number  9" in capfd.readouterr().out
+    blas.dtrsv("L", "N", "Z", 2, a, 2, x, 1)
+    assert "parameter number  3" in capfd.readouterr().out
+    blas.dtrsv("L", "N", "N", 2, a, 2, x, 0)
+    assert "parameter number  8" in capfd.readouterr().out
+    assert (a == 7.0).all() and (x == 1.0).all()
+    # idamax_: n < 1 or incx <= 0 return 0 without touching the device
+    assert blas.idamax(0, x, 1) == 0 and blas.idamax(4, x, 0) == 0 and blas.idamax(4, x, -1) == 0
+    _last()
