@@ -24,6 +24,16 @@ _fp = C.POINTER(C.c_float)
 _cp = C.c_char_p
 
 
+class DComplex(C.Structure):
+    """gb_dcomplex (BLIS dcomplex): real, imag."""
+    _fields_ = [("real", C.c_double), ("imag", C.c_double)]
+
+
+class SComplex(C.Structure):
+    """gb_scomplex (BLIS scomplex): real, imag."""
+    _fields_ = [("real", C.c_float), ("imag", C.c_float)]
+
+
 def _sig(L, name, res, args):
     fn = getattr(L, name)
     fn.restype = res
@@ -57,6 +67,15 @@ def load(path=None):
     _sig(L, "dgemm_batch_", None, batch)
     _sig(L, "sgemm_batch_", None, batch)
     _sig(L, "xerbla_", C.c_int, [_cp, _ip, C.c_long])
+    _sig(L, "zgemm_", None, [_cp, _cp, _ip, _ip, _ip, _vp, _vp, _ip, _vp, _ip, _vp, _vp, _ip])
+    _sig(L, "cgemm_", None, [_cp, _cp, _ip, _ip, _ip, _vp, _vp, _ip, _vp, _ip, _vp, _vp, _ip])
+    cz = [C.c_int, C.c_int, _i64, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _i64, _i64]
+    _sig(L, "bli_zgemm", None, cz)
+    _sig(L, "bli_cgemm", None, cz)
+    _sig(L, "gb_zgemm_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, _i64, DComplex, _vp, _i64, _i64, _vp, _i64,
+                                      _i64, DComplex, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_cgemm_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, _i64, SComplex, _vp, _i64, _i64, _vp, _i64,
+                                      _i64, SComplex, _vp, _i64, _i64, _vp])
     _sig(L, "dscal_", None, [_ip, _dp, _vp, _ip])
     _sig(L, "dcopy_", None, [_ip, _vp, _ip, _vp, _ip])
     _sig(L, "idamax_", _i32, [_ip, _vp, _ip])

@@ -55,6 +55,29 @@ def dtrsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
                        C.byref(C.c_double(alpha)), _p(a), _i(lda), _p(b), _i(ldb))
 
 
+def _cscalar(v, dtype):
+    return np.array([v], dtype=dtype)
+
+
+def zgemm(transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+    """Complex gemm on complex128 (zgemm_) or complex64 (cgemm_) Fortran-order arrays."""
+    fn = _lib.load().zgemm_ if c.dtype == np.complex128 else _lib.load().cgemm_
+    al, be = _cscalar(alpha, c.dtype), _cscalar(beta, c.dtype)
+    fn(_c(transa), _c(transb), _i(m), _i(n), _i(k), _p(al), _p(a), _i(lda), _p(b), _i(ldb), _p(be), _p(c), _i(ldc))
+
+
+cgemm = zgemm
+
+
+def bli_zgemm(transa, transb, alpha, a, b, beta, c):
+    """bli_zgemm / bli_cgemm by c's dtype; trans_t may carry the conjugation bit 0x10."""
+    m, n = c.shape
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    fn = _lib.load().bli_zgemm if c.dtype == np.complex128 else _lib.load().bli_cgemm
+    al, be = _cscalar(alpha, c.dtype), _cscalar(beta, c.dtype)
+    fn(transa, transb, m, n, k, _p(al), _p(a), *_st(a), _p(b), *_st(b), _p(be), _p(c), *_st(c))
+
+
 def dscal(n, alpha, x, incx=1):
     _lib.load().dscal_(_i(n), _d(alpha), _p(x), _i(incx))
 

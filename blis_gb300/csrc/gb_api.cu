@@ -650,6 +650,35 @@ int trsv_host(int uplo, int transa, int diag, int64_t m, double alpha, const dou
     return finish(s, where);
 }
 
+template <typename T>
+int cgemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, const T* alpha, const T* a, int64_t rs_a,
+               int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, const T* beta, T* c, int64_t rs_c, int64_t cs_c,
+               const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const size_t esz = 2 * sizeof(T);
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    Staged& C = bufs.next();
+    if ((rc = stage_in(c, m, n, rs_c, cs_c, esz, beta[0] != T(0) || beta[1] != T(0), &C, s))) return rc;
+    Staged& A = bufs.next();
+    Staged& B = bufs.next();
+    if ((alpha[0] != T(0) || alpha[1] != T(0)) && k > 0) {
+        if ((rc = stage_in(a, ta ? k : m, ta ? m : k, rs_a, cs_a, esz, true, &A, s))) return rc;
+        if ((rc = stage_in(b, tb ? n : k, tb ? k : n, rs_b, cs_b, esz, true, &B, s))) return rc;
+    }
+    const int slices = (sizeof(T) == 8) ? level3_slices() : 0;
+    if ((rc = cgemm_dev<T>(transa, transb, m, n, k, alpha, reinterpret_cast<const T*>(A.origin), A.rs, A.cs,
+                           reinterpret_cast<const T*>(B.origin), B.rs, B.cs, beta, reinterpret_cast<T*>(C.origin),
+                           C.rs, C.cs, slices, s)))
+        return rc;
+    if ((rc = stage_out(c, m, n, rs_c, cs_c, esz, C, s))) return rc;
+    return finish(s, where);
+}
+
 // ---------------------------------------------------------------- BLAS helpers
 bool lsame(char a, char b) { return toupper((unsigned char)a) == toupper((unsigned char)b); }
 
@@ -779,6 +808,35 @@ void dtrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char
     }
     trsm_host(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, map_trans(*transa),
               unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, *n, *alpha, a, 1, *lda, b, 1, *ldb);
+}
+
+void zgemm_(const gb_f77_char* transa, const gb_f77_char* transb, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_f77_int* k, const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda,
+            const gb_dcomplex* b, const gb_f77_int* ldb, const gb_dcomplex* beta, gb_dcomplex* c,
+            const gb_f77_int* ldc)
+{
+    // frame/compat/bla_gemm.c:122-262 for dcomplex; checks frame/compat/check/bla_gemm_check.h
+    const int info = gemm_check(*transa, *transb, *m, *n, *k, *lda, *ldb, *ldc);
+    if (info) {
+        call_xerbla("ZGEMM ", info);
+        return;
+    }
+    cgemm_host<double>(map_trans(*transa), map_trans(*transb), *m, *n, *k, &alpha->real, &a->real, 1, *lda,
+                       &b->real, 1, *ldb, &beta->real, &c->real, 1, *ldc, "ZGEMM");
+}
+
+void cgemm_(const gb_f77_char* transa, const gb_f77_char* transb, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_f77_int* k, const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda,
+            const gb_scomplex* b, const gb_f77_int* ldb, const gb_scomplex* beta, gb_scomplex* c,
+            const gb_f77_int* ldc)
+{
+    const int info = gemm_check(*transa, *transb, *m, *n, *k, *lda, *ldb, *ldc);
+    if (info) {
+        call_xerbla("CGEMM ", info);
+        return;
+    }
+    cgemm_host<float>(map_trans(*transa), map_trans(*transb), *m, *n, *k, &alpha->real, &a->real, 1, *lda,
+                      &b->real, 1, *ldb, &beta->real, &c->real, 1, *ldc, "CGEMM");
 }
 
 void dtrmm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
@@ -1108,6 +1166,22 @@ void bli_dtrsm_ex(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t 
     bli_dtrsm(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b);
 }
 
+void bli_zgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k, const gb_dcomplex* alpha,
+               const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b, gb_inc_t rs_b,
+               gb_inc_t cs_b, const gb_dcomplex* beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    cgemm_host<double>(transa, transb, m, n, k, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                       &beta->real, &c->real, rs_c, cs_c, "bli_zgemm");
+}
+
+void bli_cgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k, const gb_scomplex* alpha,
+               const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* b, gb_inc_t rs_b,
+               gb_inc_t cs_b, const gb_scomplex* beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    cgemm_host<float>(transa, transb, m, n, k, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                      &beta->real, &c->real, rs_c, cs_c, "bli_cgemm");
+}
+
 void bli_dscalv(gb_conj_t conjalpha, gb_dim_t n, const double* alpha, double* x, gb_inc_t incx)
 {
     (void)conjalpha;  // real
@@ -1325,6 +1399,28 @@ int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
     const int slices = (gb::dgemm_mode() == GB_DGEMM_OZAKI) ? gb::ozaki_slices() : 0;
     return gb::dtrsm_dev(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, slices,
                          pick_stream(stream));
+}
+
+int gb_zgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k, gb_dcomplex alpha,
+                 const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b, gb_inc_t rs_b,
+                 gb_inc_t cs_b, gb_dcomplex beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_zgemm_dev", "negative dimension");
+    return gb::cgemm_dev<double>(transa, transb, m, n, k, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                                 &beta.real, &c->real, rs_c, cs_c, gb::level3_slices(), pick_stream(stream));
+}
+
+int gb_cgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k, gb_scomplex alpha,
+                 const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* b, gb_inc_t rs_b,
+                 gb_inc_t cs_b, gb_scomplex beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_cgemm_dev", "negative dimension");
+    return gb::cgemm_dev<float>(transa, transb, m, n, k, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                                &beta.real, &c->real, rs_c, cs_c, 0, pick_stream(stream));
 }
 
 int gb_dscalv_dev(gb_dim_t n, double alpha, double* x, gb_inc_t incx, void* stream)

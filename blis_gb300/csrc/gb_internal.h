@@ -105,6 +105,13 @@ int64_t ozaki_kpart_limit(int slices);
 // Lanes per right-hand side (1, 2, 4, 8) for the 64-row diagonal-block
 // kernels of trsm and trmm, from the FP64-instruction cost model (gb_trsm.cu).
 int diag_block_lanes(int64_t ncols);
+// Complex gemm (T = double: dcomplex, float: scomplex; interleaved storage,
+// alpha/beta as {real, imag}); one real gemm on the block-real form
+// (gb_complex.cu).
+template <typename T>
+int cgemm_dev(int transa, int transb, int64_t m, int64_t n, int64_t k, const T* alpha, const T* a, int64_t rs_a,
+              int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, const T* beta, T* c, int64_t rs_c, int64_t cs_c,
+              int slices, cudaStream_t s);
 int dscalv_dev(int64_t n, double alpha, double* x, int64_t incx, cudaStream_t s);
 int dcopyv_dev(int64_t n, const double* x, int64_t incx, double* y, int64_t incy, cudaStream_t s);
 int damaxv_dev(int64_t n, const double* x, int64_t incx, int64_t* index_dev, cudaStream_t s);

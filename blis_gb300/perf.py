@@ -15,6 +15,7 @@ L2 where the workload allows:
   dtrsm_16384     L/L/N/N, B entries (1+u) 2^e, e in [-20,20]: native and
                   Ozaki updates, sampled componentwise backward error
   level12x        dscal / dcopy / idamax at 2^28, dger 32768^2, dtrsv 16384
+  complex         zgemm 4096^3 native / Ozaki, cgemm 4096^3 (8 mnk flop)
   level3x         dtrmm 8192x4096 (m^2 n), dsyrk n=k=8192 (n^2 k), dsymm
                   8192x4096 (2 m^2 n): native FP64 and Ozaki (7 slices)
   batch_4096      4096 problems, m,n,k log-uniform in [16,1024], random
@@ -390,9 +391,37 @@ def run_level12x(out):
     out.append({"workload": "dtrsv_%d" % mt, "ms": ms, "gflops": float(mt) * mt / ms / 1e6})
 
 
+def run_complex(out):
+    """zgemm 4096^3 (8 m n k real flops) native FP64 and Ozaki s = 7, cgemm
+    4096^3 FP32: one real gemm of 2m x n x 2k on the block-real operands."""
+    import torch
+    n = 2048 if SMALL else 4096
+    L = _lib.load()
+    for dt, name in ((torch.complex128, "zgemm"), (torch.complex64, "cgemm")):
+        a = torch.complex(_mat(n, n, seed=71, dtype=torch.float64), _mat(n, n, seed=72, dtype=torch.float64)).to(dt)
+        b = torch.complex(_mat(n, n, seed=73, dtype=torch.float64), _mat(n, n, seed=74, dtype=torch.float64)).to(dt)
+        a, b = a.t().contiguous().t(), b.t().contiguous().t()
+        c = torch.zeros((n, n), dtype=dt, device="cuda").t()
+        forms = ((0, "native_fp64"), (1, "ozaki_s7")) if dt == torch.complex128 else ((0, "native_fp32"),)
+        for mode, form in forms:
+            L.gb_set_dgemm_mode(mode, 7)
+            if dt == torch.complex128:
+                al, be = _lib.DComplex(1.0, 0.5), _lib.DComplex(0.0, 0.0)
+                fn = lambda: _lib.check(L.gb_zgemm_dev(0, 0, n, n, n, al, a.data_ptr(), 1, n, b.data_ptr(), 1, n,
+                                                       be, c.data_ptr(), 1, n, _stream()), "zgemm")
+            else:
+                al, be = _lib.SComplex(1.0, 0.5), _lib.SComplex(0.0, 0.0)
+                fn = lambda: _lib.check(L.gb_cgemm_dev(0, 0, n, n, n, al, a.data_ptr(), 1, n, b.data_ptr(), 1, n,
+                                                       be, c.data_ptr(), 1, n, _stream()), "cgemm")
+            ms = _timer(fn, reps=1 if mode == 0 and dt == torch.complex128 else 3, warmup=1)
+            out.append({"workload": "%s_%d" % (name, n), "form": form, "ms": ms,
+                        "tflops": 8.0 * n ** 3 / ms / 1e9})
+    L.gb_set_dgemm_mode(0, 8)
+
+
 SUITES = {"gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
           "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm, "bgemm": run_bgemm,
-          "level3x": run_level3x, "level12x": run_level12x}
+          "level3x": run_level3x, "level12x": run_level12x, "complex": run_complex}
 
 
 def main():

@@ -45,6 +45,12 @@ typedef int gb_diag_t;     /* diag_t:  0x000 non-unit, 0x100 unit */
 #define GB_CONJ_TRANSPOSE 0x18
 #define GB_NO_CONJUGATE 0x00
 #define GB_CONJUGATE 0x10
+/* scomplex / dcomplex, frame/include/bli_type_defs.h:191-206: interleaved
+   (real, imag); complex strides and leading dimensions count complex
+   elements */
+typedef struct { float real, imag; } gb_scomplex;
+typedef struct { double real, imag; } gb_dcomplex;
+
 #define GB_LOWER 0xC0
 #define GB_UPPER 0x60
 #define GB_LEFT 0
@@ -114,6 +120,23 @@ void dgemmt_(const gb_f77_char* uploc, const gb_f77_char* transa, const gb_f77_c
              const gb_f77_int* m, const gb_f77_int* k, const double* alpha, const double* a,
              const gb_f77_int* lda, const double* b, const gb_f77_int* ldb, const double* beta,
              double* c, const gb_f77_int* ldc);
+
+/* replace zgemm_ / cgemm_ (frame/compat/bla_gemm.c:122-262 for the complex
+   types; checks frame/compat/check/bla_gemm_check.h: 'C' is the conjugate
+   transpose): one real gemm on the block-real form [Ar -Ai; Ai Ar] [Br; Bi],
+   the GPU counterpart of BLIS's induced methods (frame/3/bli_l3_ind.c,
+   ref_kernels/ind/bli_gemm1m_ref.c).  m == 1 or n == 1 is computed as a gemm
+   (the reference sends it to gemv, frame/compat/bla_gemm.c:180-218) */
+void zgemm_(const gb_f77_char* transa, const gb_f77_char* transb,
+            const gb_f77_int* m, const gb_f77_int* n, const gb_f77_int* k,
+            const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda,
+            const gb_dcomplex* b, const gb_f77_int* ldb, const gb_dcomplex* beta,
+            gb_dcomplex* c, const gb_f77_int* ldc);
+void cgemm_(const gb_f77_char* transa, const gb_f77_char* transb,
+            const gb_f77_int* m, const gb_f77_int* n, const gb_f77_int* k,
+            const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda,
+            const gb_scomplex* b, const gb_f77_int* ldb, const gb_scomplex* beta,
+            gb_scomplex* c, const gb_f77_int* ldc);
 
 /* replace dscal_ (frame/compat/bla_scal.c:44-85; alpha == 0 sets zeros
    without reading x, ref_kernels/1/bli_scalv_ref.c:54-75), dcopy_
@@ -230,6 +253,17 @@ void bli_sgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_
                const float* alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a,
                const float* b, gb_inc_t rs_b, gb_inc_t cs_b, const float* beta,
                float* c, gb_inc_t rs_c, gb_inc_t cs_c);
+
+/* replace bli_zgemm / bli_cgemm (frame/3/bli_l3_tapi_ex.c:45-99 for the
+   complex types; trans_t carries the conjugation bit 0x10) */
+void bli_zgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+               const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               const gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const gb_dcomplex* beta,
+               gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_cgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+               const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               const gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const gb_scomplex* beta,
+               gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c);
 
 /* replace bli_dscalv (frame/1/bli_l1v_tapi.c:314-345), bli_dcopyv (:46-77),
    bli_damaxv (:84-112), bli_dger (frame/2/bli_l2_tapi.c:129-175) and
@@ -350,6 +384,17 @@ int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
 int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
                  gb_dim_t m, gb_dim_t n, double alpha, const double* a, gb_inc_t rs_a,
                  gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
+
+/* Device-pointer complex gemm (zgemm: native FP64 or the Ozaki form by
+   gb_set_dgemm_mode with a fixed slice count; cgemm: FP32). */
+int gb_zgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                 gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                 const gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, gb_dcomplex beta,
+                 gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+int gb_cgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                 gb_scomplex alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                 const gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, gb_scomplex beta,
+                 gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
 
 /* Device-pointer forms of scalv, copyv, amaxv (the 0-based index written to
    device memory), ger and trsv (asynchronous on the stream). */

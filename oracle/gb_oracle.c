@@ -32,6 +32,9 @@
  *   amaxv ref_kernels/1/bli_amaxv_ref.c:44-140 (first NaN, else first max)
  *   ger   column-wise axpys a_j += (alpha y_j) x, frame/2/ger/bli_ger_unb_var2.c
  *   trsv  orc_dtrsm on one column (frame/2/trsv: the same substitution)
+ *   zgemm the complex definition, op() with the conjugation bit of trans_t
+ *         (0x10; 'C' = 0x18), accumulation over l in order, then
+ *         beta == 0 ? c = alpha ab : c = alpha ab + beta c (complex)
  *   dotv  ref_kernels/1/bli_dotv_ref.c:37-121 (n == 0 gives rho = 0)
  * Not in the reference: the double-double evaluator (error oracle) and the
  * Ozaki split-product model (Ozaki, Ogita, Oishi & Rump 2012; integer-slice
@@ -423,6 +426,37 @@ void orc_daxpyv(int conjx, int64_t n, double alpha, const double* x, int64_t inc
     (void)conjx;
     if (n <= 0 || alpha == 0.0) return;
     for (int64_t i = 0; i < n; ++i) y[i * incy] = fma(alpha, x[i * incx], y[i * incy]);
+}
+
+/* Interleaved complex operands, strides in complex elements. */
+void orc_zgemm(int transa, int transb, int64_t m, int64_t n, int64_t k, const double* alpha,
+               const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b,
+               const double* beta, double* c, int64_t rs_c, int64_t cs_c)
+{
+    const int ta = ORC_TRANS(transa), tb = ORC_TRANS(transb);
+    const double sa = (transa & 0x10) ? -1.0 : 1.0, sb = (transb & 0x10) ? -1.0 : 1.0;
+    const int64_t ars = ta ? cs_a : rs_a, acs = ta ? rs_a : cs_a;
+    const int64_t brs = tb ? cs_b : rs_b, bcs = tb ? rs_b : cs_b;
+    const int zero_beta = (beta[0] == 0.0 && beta[1] == 0.0);
+    for (int64_t j = 0; j < n; ++j)
+        for (int64_t i = 0; i < m; ++i) {
+            double sr = 0.0, si = 0.0;
+            for (int64_t l = 0; l < k; ++l) {
+                const double* pa = a + 2 * (i * ars + l * acs);
+                const double* pb = b + 2 * (l * brs + j * bcs);
+                const double xr = pa[0], xi = sa * pa[1], yr = pb[0], yi = sb * pb[1];
+                sr = fma(xr, yr, fma(-xi, yi, sr));
+                si = fma(xr, yi, fma(xi, yr, si));
+            }
+            double* pc = c + 2 * (i * rs_c + j * cs_c);
+            double cr = alpha[0] * sr - alpha[1] * si, ci = alpha[0] * si + alpha[1] * sr;
+            if (!zero_beta) {
+                cr += beta[0] * pc[0] - beta[1] * pc[1];
+                ci += beta[0] * pc[1] + beta[1] * pc[0];
+            }
+            pc[0] = cr;
+            pc[1] = ci;
+        }
 }
 
 void orc_dscalv(int64_t n, double alpha, double* x, int64_t incx)

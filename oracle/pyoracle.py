@@ -48,6 +48,8 @@ def lib():
         L.orc_dgemmt.argtypes = [C.c_int] * 3 + [_i64, _i64, C.c_double, C.c_void_p, _i64, _i64,
                                                   C.c_void_p, _i64, _i64, C.c_double, C.c_void_p, _i64,
                                                   _i64, C.c_int]
+        L.orc_zgemm.argtypes = [C.c_int, C.c_int, _i64, _i64, _i64, C.c_void_p, C.c_void_p, _i64, _i64,
+                                C.c_void_p, _i64, _i64, C.c_void_p, C.c_void_p, _i64, _i64]
         L.orc_dscalv.argtypes = [_i64, C.c_double, C.c_void_p, _i64]
         L.orc_dcopyv.argtypes = [_i64, C.c_void_p, _i64, C.c_void_p, _i64]
         L.orc_damaxv.argtypes = [_i64, C.c_void_p, _i64, C.c_void_p]
@@ -161,6 +163,17 @@ def dgemmt(uplo, transa, transb, alpha, a, b, beta, c, nthreads=None):
     k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
     lib().orc_dgemmt(uplo, transa, transb, m, k, alpha, _p(a), *_strides(a), _p(b), *_strides(b), beta,
                      _p(c), *_strides(c), nthreads or nthreads_default())
+    return c
+
+
+def zgemm(transa, transb, alpha, a, b, beta, c):
+    """Complex gemm on complex128 arrays (strides in complex elements); trans_t 0x10 conjugates."""
+    m, n = c.shape
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    al = np.array([alpha], dtype=np.complex128)
+    be = np.array([beta], dtype=np.complex128)
+    st = lambda x: (x.strides[0] // x.itemsize, x.strides[1] // x.itemsize)
+    lib().orc_zgemm(transa, transb, m, n, k, _p(al), _p(a), *st(a), _p(b), *st(b), _p(be), _p(c), *st(c))
     return c
 
 
