@@ -70,6 +70,14 @@ def load(path=None):
     _sig(L, "zgemm_", None, [_cp, _cp, _ip, _ip, _ip, _vp, _vp, _ip, _vp, _ip, _vp, _vp, _ip])
     _sig(L, "cgemm_", None, [_cp, _cp, _ip, _ip, _ip, _vp, _vp, _ip, _vp, _ip, _vp, _vp, _ip])
     cz = [C.c_int, C.c_int, _i64, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _i64, _i64]
+    _sig(L, "ztrsm_", None, [_cp, _cp, _cp, _cp, _ip, _ip, _vp, _vp, _ip, _vp, _ip])
+    _sig(L, "bli_ztrsm", None, [C.c_int] * 4 + [_i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64])
+    _sig(L, "gb_ztrsm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, DComplex, _vp, _i64, _i64, _vp, _i64, _i64,
+                                                      _vp])
+    _sig(L, "gb_zgemm", None, cz)
+    _sig(L, "gb_cgemm", None, cz)
+    _sig(L, "gb_dgemm_ozaki", None, [C.c_int, C.c_int, _i64, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64,
+                                     _vp, _vp, _i64, _i64, C.c_int])
     _sig(L, "bli_zgemm", None, cz)
     _sig(L, "bli_cgemm", None, cz)
     _sig(L, "gb_zgemm_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, _i64, DComplex, _vp, _i64, _i64, _vp, _i64,

@@ -78,6 +78,12 @@ def bli_zgemm(transa, transb, alpha, a, b, beta, c):
     fn(transa, transb, m, n, k, _p(al), _p(a), *_st(a), _p(b), *_st(b), _p(be), _p(c), *_st(c))
 
 
+def ztrsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
+    al = _cscalar(alpha, np.complex128)
+    _lib.load().ztrsm_(_c(side), _c(uplo), _c(transa), _c(diag), _i(m), _i(n), _p(al), _p(a), _i(lda), _p(b),
+                       _i(ldb))
+
+
 def dscal(n, alpha, x, incx=1):
     _lib.load().dscal_(_i(n), _d(alpha), _p(x), _i(incx))
 

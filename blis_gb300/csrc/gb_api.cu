@@ -679,6 +679,27 @@ int cgemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, const T*
     return finish(s, where);
 }
 
+int ztrsm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const double* alpha, const double* a,
+               int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const int64_t na = (side == GB_LEFT) ? m : n;
+    const bool nz = !(alpha[0] == 0.0 && alpha[1] == 0.0);
+    Staged& B = bufs.next();
+    if ((rc = stage_in(b, m, n, rs_b, cs_b, 16, nz, &B, s))) return rc;
+    Staged& A = bufs.next();
+    if (nz && (rc = stage_in(a, na, na, rs_a, cs_a, 16, true, &A, s))) return rc;
+    if ((rc = ztrsm_dev(side, uplo, transa, diag, m, n, alpha, reinterpret_cast<const double*>(A.origin), A.rs, A.cs,
+                        reinterpret_cast<double*>(B.origin), B.rs, B.cs, level3_slices(), s)))
+        return rc;
+    if ((rc = stage_out(b, m, n, rs_b, cs_b, 16, B, s))) return rc;
+    return finish(s, where);
+}
+
 // ---------------------------------------------------------------- BLAS helpers
 bool lsame(char a, char b) { return toupper((unsigned char)a) == toupper((unsigned char)b); }
 
@@ -837,6 +858,34 @@ void cgemm_(const gb_f77_char* transa, const gb_f77_char* transb, const gb_f77_i
     }
     cgemm_host<float>(map_trans(*transa), map_trans(*transb), *m, *n, *k, &alpha->real, &a->real, 1, *lda,
                       &b->real, 1, *ldb, &beta->real, &c->real, 1, *ldc, "CGEMM");
+}
+
+void ztrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const gb_dcomplex* alpha,
+            const gb_dcomplex* a, const gb_f77_int* lda, gb_dcomplex* b, const gb_f77_int* ldb)
+{
+    // frame/compat/bla_trsm.c:121-219 for dcomplex, checks frame/compat/check/bla_trmm_check.h:37-86
+    const bool left = lsame(*side, 'L'), right = lsame(*side, 'R');
+    const bool lower = lsame(*uploa, 'L'), upper = lsame(*uploa, 'U');
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T'), conja = lsame(*transa, 'C');
+    const bool unita = lsame(*diaga, 'U'), nonua = lsame(*diaga, 'N');
+    const int nrowa = left ? *m : *n;
+    int info = 0;
+    if (!left && !right) info = 1;
+    else if (!lower && !upper) info = 2;
+    else if (!nota && !ta && !conja) info = 3;
+    else if (!unita && !nonua) info = 4;
+    else if (*m < 0) info = 5;
+    else if (*n < 0) info = 6;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 9;
+    else if (*ldb < (*m > 1 ? *m : 1)) info = 11;
+    if (info) {
+        call_xerbla("ZTRSM ", info);
+        return;
+    }
+    ztrsm_host(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, map_trans(*transa),
+               unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, *n, &alpha->real, &a->real, 1, *lda, &b->real, 1, *ldb,
+               "ZTRSM");
 }
 
 void dtrmm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
@@ -1182,6 +1231,14 @@ void bli_cgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_
                       &beta->real, &c->real, rs_c, cs_c, "bli_cgemm");
 }
 
+void bli_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+               const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b,
+               gb_inc_t rs_b, gb_inc_t cs_b)
+{
+    ztrsm_host(side, uploa, transa, diaga, m, n, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+               "bli_ztrsm");
+}
+
 void bli_dscalv(gb_conj_t conjalpha, gb_dim_t n, const double* alpha, double* x, gb_inc_t incx)
 {
     (void)conjalpha;  // real
@@ -1306,6 +1363,32 @@ void gb_dgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_d
                       cs_c, "gb_dgemm");
 }
 
+void gb_dgemm_ozaki(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                    const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                    gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c,
+                    int slices)
+{
+    gb::ModeOverride form(GB_DGEMM_OZAKI, slices < 0 ? 0 : slices);
+    gemm_host<double>(transa, transb, m, n, k, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c, cs_c,
+                      "gb_dgemm_ozaki");
+}
+
+void gb_zgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k, const gb_dcomplex* alpha,
+              const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b, gb_inc_t rs_b,
+              gb_inc_t cs_b, const gb_dcomplex* beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    cgemm_host<double>(transa, transb, m, n, k, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                       &beta->real, &c->real, rs_c, cs_c, "gb_zgemm");
+}
+
+void gb_cgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k, const gb_scomplex* alpha,
+              const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* b, gb_inc_t rs_b,
+              gb_inc_t cs_b, const gb_scomplex* beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    cgemm_host<float>(transa, transb, m, n, k, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                      &beta->real, &c->real, rs_c, cs_c, "gb_cgemm");
+}
+
 void gb_sgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
               const float* alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a, const float* b,
               gb_inc_t rs_b, gb_inc_t cs_b, const float* beta, float* c, gb_inc_t rs_c, gb_inc_t cs_c)
@@ -1421,6 +1504,17 @@ int gb_cgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
     if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_cgemm_dev", "negative dimension");
     return gb::cgemm_dev<float>(transa, transb, m, n, k, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
                                 &beta.real, &c->real, rs_c, cs_c, 0, pick_stream(stream));
+}
+
+int gb_ztrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+                 gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_ztrsm_dev", "negative dimension");
+    return gb::ztrsm_dev(side, uploa, transa, diaga, m, n, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                         gb::level3_slices(), pick_stream(stream));
 }
 
 int gb_dscalv_dev(gb_dim_t n, double alpha, double* x, gb_inc_t incx, void* stream)

@@ -158,4 +158,269 @@ template int cgemm_dev<float>(int, int, int64_t, int64_t, int64_t, const float*,
                               const float*, int64_t, int64_t, const float*, float*, int64_t, int64_t, int,
                               cudaStream_t);
 
+// ---------------------------------------------------------------- ztrsm
+// The recursive solve of gb_trsm.cu on dcomplex data: 64-row diagonal blocks
+// and complex gemm updates (block-real, native or Ozaki).  A diagonal block
+// is packed once per call as in the real solver, P[r][r] = inv(a_rr) and
+// P[r][i] = a_ri inv(a_ii) in the strict triangle (conjugated first for
+// A^H), so the substitution works on y = D x with a unit triangle and every
+// complex FMA of the triangle is four real FMAs on the FP64 pipe.
+namespace {
+
+constexpr int ZNB = 64;
+constexpr int ZTHREADS = 128;
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ double2 cinv(double2 a)
+{
+    // 1 / a with the larger component scaled out (Smith's method)
+    if (fabs(a.x) >= fabs(a.y)) {
+        const double r = a.y / a.x, d = a.x + a.y * r;
+        return make_double2(1.0 / d, -r / d);
+    }
+    const double r = a.x / a.y, d = a.x * r + a.y;
+    return make_double2(r / d, -1.0 / d);
+}
+
+template <bool LOWER>
+__global__ void __launch_bounds__(256) ztrsm_pack_diag_kernel(int64_t m, int unit, int conj,
+                                                              const double2* __restrict__ a, int64_t ars,
+                                                              int64_t acs, double2* __restrict__ packed)
+{
+    __shared__ double2 T[ZNB][ZNB + 1];
+    __shared__ double2 dinv[ZNB];
+    const int64_t r0 = (int64_t)blockIdx.x * ZNB;
+    const int nb = (m - r0 < ZNB) ? (int)(m - r0) : ZNB;
+    const double2* blk = a + r0 * ars + r0 * acs;
+    for (int e = threadIdx.x; e < ZNB * ZNB; e += 256) {
+        const int i = e % ZNB, l = e / ZNB;
+        const bool keep = (i < nb && l < nb) && (LOWER ? (l <= i) : (l >= i));
+        double2 v = keep ? blk[i * ars + l * acs] : make_double2(0.0, 0.0);
+        if (conj) v.y = -v.y;
+        T[i][l] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < ZNB) {
+        const int i = threadIdx.x;
+        dinv[i] = (unit || i >= nb) ? make_double2(1.0, 0.0) : cinv(T[i][i]);
+    }
+    __syncthreads();
+    double2* out = packed + (int64_t)blockIdx.x * ZNB * ZNB;
+    for (int e = threadIdx.x; e < ZNB * ZNB; e += 256) {
+        const int r = e / ZNB, i = e % ZNB;
+        double2 v = make_double2(0.0, 0.0);
+        if (r == i) v = dinv[r];
+        else if (LOWER ? (i < r) : (i > r)) v = cmul(T[r][i], dinv[i]);
+        out[e] = v;
+    }
+}
+
+template <int LANES, bool LOWER>
+__global__ void __launch_bounds__(ZTHREADS) ztrsm_diag_kernel(int nb, const double2* __restrict__ pk,
+                                                              double2* __restrict__ b, int64_t brs, int64_t bcs,
+                                                              int64_t ncols)
+{
+    constexpr int COLS = ZTHREADS / LANES, R = ZNB / LANES, LL = ZNB + 1, LX = COLS + 1;
+    extern __shared__ double2 ztrsm_smem[];
+    double2* L = ztrsm_smem;       // [ZNB][LL]
+    double2* X = L + ZNB * LL;     // [ZNB][LX]
+    const int t = threadIdx.x;
+    const int64_t j0 = (int64_t)blockIdx.x * COLS;
+    const int cols = (ncols - j0 < COLS) ? (int)(ncols - j0) : COLS;
+    for (int e = t; e < ZNB * ZNB; e += ZTHREADS) L[(e / ZNB) * LL + e % ZNB] = pk[e];
+    const bool rows_fast = (brs == 1);
+    for (int e = t; e < ZNB * COLS; e += ZTHREADS) {
+        const int i = rows_fast ? e % ZNB : e / COLS, c = rows_fast ? e / ZNB : e % COLS;
+        X[i * LX + c] = (c < cols && i < nb) ? b[i * brs + (j0 + c) * bcs] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    const int c = t / LANES, g = t % LANES;
+    const int src0 = (t % 32) - g;
+    double2 x[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) x[q] = X[(q * LANES + g) * LX + c];
+#pragma unroll
+    for (int step = 0; step < ZNB; ++step) {
+        const int i = LOWER ? step : ZNB - 1 - step;
+        const int qi = i / LANES, gi = i % LANES;
+        double2 v = x[qi];
+        if constexpr (LANES > 1) {
+            v.x = __shfl_sync(0xffffffffu, v.x, src0 + gi);
+            v.y = __shfl_sync(0xffffffffu, v.y, src0 + gi);
+        }
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            if (LOWER ? (q * LANES + LANES - 1 > i) : (q * LANES < i)) {
+                const int r = q * LANES + g;
+                if (LOWER ? (r > i) : (r < i)) {
+                    const double2 p = L[r * LL + i];
+                    x[q].x = fma(-p.x, v.x, fma(p.y, v.y, x[q].x));
+                    x[q].y = fma(-p.x, v.y, fma(-p.y, v.x, x[q].y));
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        const int r = q * LANES + g;
+        X[r * LX + c] = cmul(x[q], L[r * LL + r]);
+    }
+    __syncthreads();
+    for (int e = t; e < ZNB * COLS; e += ZTHREADS) {
+        const int i = rows_fast ? e % ZNB : e / COLS, cc = rows_fast ? e / ZNB : e % COLS;
+        if (cc < cols && i < nb) b[i * brs + (j0 + cc) * bcs] = X[i * LX + cc];
+    }
+}
+
+constexpr size_t ztrsm_smem_bytes(int lanes)
+{
+    return sizeof(double2) * (ZNB * (ZNB + 1) + ZNB * (ZTHREADS / lanes + 1));
+}
+
+template <int LANES, bool LOWER>
+int launch_ztrsm_diag(int nb, const double2* pk, double2* b, int64_t brs, int64_t bcs, int64_t ncols, cudaStream_t s)
+{
+    static bool attr = false;
+    if (!attr) {
+        const int rc = check_cuda(cudaFuncSetAttribute(ztrsm_diag_kernel<LANES, LOWER>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)ztrsm_smem_bytes(LANES)), "ztrsm smem attr");
+        if (rc) return rc;
+        attr = true;
+    }
+    const int64_t blocks = (ncols + ZTHREADS / LANES - 1) / (ZTHREADS / LANES);
+    if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "ztrsm", "too many right-hand sides");
+    ztrsm_diag_kernel<LANES, LOWER><<<(unsigned)blocks, ZTHREADS, ztrsm_smem_bytes(LANES), s>>>(nb, pk, b, brs, bcs,
+                                                                                               ncols);
+    return check_cuda(cudaGetLastError(), "ztrsm_diag");
+}
+
+__global__ void __launch_bounds__(NT) zscal_kernel(int64_t m, int64_t n, double ar, double ai, double2* __restrict__ b,
+                                                   int64_t brs, int64_t bcs)
+{
+    const int64_t total = m * n;
+    for (int64_t e = (int64_t)blockIdx.x * NT + threadIdx.x; e < total; e += (int64_t)gridDim.x * NT) {
+        const int64_t j = e / m, i = e - j * m;
+        double2* p = b + i * brs + j * bcs;
+        *p = (ar == 0.0 && ai == 0.0) ? make_double2(0.0, 0.0) : cmul(make_double2(ar, ai), *p);
+    }
+}
+
+struct ZtrsmCtx {
+    int lower, conj, slices;
+    const double2* packed;
+    const double2* a;
+    int64_t ars, acs;
+    double2* b;
+    int64_t brs, bcs, n;
+    cudaStream_t s;
+};
+
+int ztrsm_update(const ZtrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t ccount)
+{
+    // B[r0..] -= op(A)[r0.., c0..] X[c0..]; op(A) by the folded strides, conjugated when t.conj
+    const double minus_one[2] = {-1.0, 0.0}, one[2] = {1.0, 0.0};
+    return cgemm_dev<double>(t.conj ? 0x10 : 0x00, 0x00, rcount, t.n, ccount, minus_one,
+                             reinterpret_cast<const double*>(t.a + r0 * t.ars + c0 * t.acs), t.ars, t.acs,
+                             reinterpret_cast<const double*>(t.b + c0 * t.brs), t.brs, t.bcs, one,
+                             reinterpret_cast<double*>(t.b + r0 * t.brs), t.brs, t.bcs, t.slices, t.s);
+}
+
+int ztrsm_solve(const ZtrsmCtx& t, int64_t r0, int64_t mm)
+{
+    if (mm <= ZNB) {
+        const double2* pk = t.packed + (r0 / ZNB) * ZNB * ZNB;
+        double2* b1 = t.b + r0 * t.brs;
+        const int nb = (int)mm;
+        int lanes = diag_block_lanes(t.n);
+        if (lanes < 2) lanes = 2;  // 64 complex rows per lane would not fit the registers
+        LaunchScope ls("ztrsm_diag", t.s);
+        switch (lanes) {
+        case 2:
+            return t.lower ? launch_ztrsm_diag<2, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_ztrsm_diag<2, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+        case 4:
+            return t.lower ? launch_ztrsm_diag<4, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_ztrsm_diag<4, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+        default:
+            return t.lower ? launch_ztrsm_diag<8, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_ztrsm_diag<8, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+        }
+    }
+    int64_t m1 = ((mm / 2 + ZNB - 1) / ZNB) * ZNB;
+    if (m1 >= mm) m1 = mm - ZNB;
+    const int64_t m2 = mm - m1;
+    int rc;
+    if (t.lower) {
+        if ((rc = ztrsm_solve(t, r0, m1))) return rc;
+        if ((rc = ztrsm_update(t, r0 + m1, m2, r0, m1))) return rc;
+        return ztrsm_solve(t, r0 + m1, m2);
+    }
+    if ((rc = ztrsm_solve(t, r0 + m1, m2))) return rc;
+    if ((rc = ztrsm_update(t, r0, m1, r0 + m1, m2))) return rc;
+    return ztrsm_solve(t, r0, m1);
+}
+
+}  // namespace
+
+// op(A) X = alpha B (left) or X op(A) = alpha B (right), dcomplex, in place;
+// transa may be N, T or C (conjugate transpose: the 0x10 bit).
+int ztrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const double* alpha, const double* a,
+              int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b, int slices, cudaStream_t s)
+{
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    int64_t brs = rs_b, bcs = cs_b, mm = m, nn = n;
+    bool trans = GB_IS_TRANS(transa);
+    const int conj = (transa & 0x10) ? 1 : 0;
+    if (side == GB_RIGHT) {
+        // X op(A) = alpha B  <=>  op(A)^T X^T = alpha B^T; the conjugation stays
+        brs = cs_b;
+        bcs = rs_b;
+        mm = n;
+        nn = m;
+        trans = !trans;
+    }
+    double2* bz = reinterpret_cast<double2*>(b);
+    if (!(alpha[0] == 1.0 && alpha[1] == 0.0)) {
+        LaunchScope ls("zscal", s);
+        zscal_kernel<<<grid_of(mm * nn), NT, 0, s>>>(mm, nn, alpha[0], alpha[1], bz, brs, bcs);
+        int rc = check_cuda(cudaGetLastError(), "zscal");
+        if (rc || (alpha[0] == 0.0 && alpha[1] == 0.0)) return rc;
+    }
+    ZtrsmCtx t;
+    t.ars = trans ? cs_a : rs_a;
+    t.acs = trans ? rs_a : cs_a;
+    t.lower = ((uplo == GB_LOWER) != trans) ? 1 : 0;
+    t.conj = conj;
+    t.slices = slices;
+    t.a = reinterpret_cast<const double2*>(a);
+    t.b = bz;
+    t.brs = brs;
+    t.bcs = bcs;
+    t.n = nn;
+    t.s = s;
+    const int64_t nblk = (mm + ZNB - 1) / ZNB;
+    if (nblk > INT32_MAX) return set_error(GB_ERR_ARG, "ztrsm", "too many diagonal blocks");
+    double2* packed = static_cast<double2*>(dev_alloc(sizeof(double2) * nblk * ZNB * ZNB, s));
+    if (!packed) return GB_ERR_NOMEM;
+    {
+        LaunchScope ls("ztrsm_pack_diag", s);
+        if (t.lower)
+            ztrsm_pack_diag_kernel<true><<<(unsigned)nblk, 256, 0, s>>>(mm, diag == GB_UNIT_DIAG, conj, t.a, t.ars,
+                                                                        t.acs, packed);
+        else
+            ztrsm_pack_diag_kernel<false><<<(unsigned)nblk, 256, 0, s>>>(mm, diag == GB_UNIT_DIAG, conj, t.a, t.ars,
+                                                                         t.acs, packed);
+    }
+    int rc = check_cuda(cudaGetLastError(), "ztrsm_pack_diag");
+    t.packed = packed;
+    if (!rc) rc = ztrsm_solve(t, 0, mm);
+    dev_free(packed, s);
+    return rc;
+}
+
 }  // namespace gb

@@ -112,6 +112,8 @@ template <typename T>
 int cgemm_dev(int transa, int transb, int64_t m, int64_t n, int64_t k, const T* alpha, const T* a, int64_t rs_a,
               int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, const T* beta, T* c, int64_t rs_c, int64_t cs_c,
               int slices, cudaStream_t s);
+int ztrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const double* alpha, const double* a,
+              int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b, int slices, cudaStream_t s);
 int dscalv_dev(int64_t n, double alpha, double* x, int64_t incx, cudaStream_t s);
 int dcopyv_dev(int64_t n, const double* x, int64_t incx, double* y, int64_t incy, cudaStream_t s);
 int damaxv_dev(int64_t n, const double* x, int64_t incx, int64_t* index_dev, cudaStream_t s);
@@ -205,5 +207,14 @@ int dgemv_dev(int trans, int64_t m, int64_t n, double alpha, const double* a,
 // GB_DGEMM_OZAKI) and slice count, set by gb_set_dgemm_mode().
 int dgemm_mode();
 int ozaki_slices();
+// Scoped per-thread dgemm mode (restored on destruction).
+class ModeOverride {
+public:
+    ModeOverride(int mode, int slices);
+    ~ModeOverride();
+
+private:
+    int mode_, slices_;
+};
 
 }  // namespace gb

@@ -152,8 +152,24 @@ int read_and_clear_device_status(cudaStream_t s, const char* where)
     return set_error(GB_ERR_DEVICE, where, buf);
 }
 
-int dgemm_mode() { return g_dgemm_mode; }
-int ozaki_slices() { return g_ozaki_slices; }
+// A per-call form (gb_dgemm_ozaki) overrides the process-wide mode on the
+// calling thread for the duration of the call.
+thread_local int t_mode = -1, t_slices = -1;
+
+int dgemm_mode() { return t_mode >= 0 ? t_mode : g_dgemm_mode; }
+int ozaki_slices() { return t_slices >= 0 ? t_slices : g_ozaki_slices; }
+
+ModeOverride::ModeOverride(int mode, int slices) : mode_(t_mode), slices_(t_slices)
+{
+    t_mode = mode;
+    t_slices = slices;
+}
+
+ModeOverride::~ModeOverride()
+{
+    t_mode = mode_;
+    t_slices = slices_;
+}
 
 // ---------------------------------------------------------------- launches
 LaunchScope::LaunchScope(const char* name, cudaStream_t s) : name_(name), s_(s), timed_(false)

@@ -15,7 +15,8 @@ L2 where the workload allows:
   dtrsm_16384     L/L/N/N, B entries (1+u) 2^e, e in [-20,20]: native and
                   Ozaki updates, sampled componentwise backward error
   level12x        dscal / dcopy / idamax at 2^28, dger 32768^2, dtrsv 16384
-  complex         zgemm 4096^3 native / Ozaki, cgemm 4096^3 (8 mnk flop)
+  complex         zgemm 4096^3 native / Ozaki, cgemm 4096^3 (8 mnk flop), ztrsm 4096^2
+                  native / Ozaki updates (4 m^2 n flop)
   level3x         dtrmm 8192x4096 (m^2 n), dsyrk n=k=8192 (n^2 k), dsymm
                   8192x4096 (2 m^2 n): native FP64 and Ozaki (7 slices)
   batch_4096      4096 problems, m,n,k log-uniform in [16,1024], random
@@ -416,6 +417,21 @@ def run_complex(out):
             ms = _timer(fn, reps=1 if mode == 0 and dt == torch.complex128 else 3, warmup=1)
             out.append({"workload": "%s_%d" % (name, n), "form": form, "ms": ms,
                         "tflops": 8.0 * n ** 3 / ms / 1e9})
+    # ztrsm L/L/N/N m = n, diagonal n + |u|: 4 m^2 n real flops (half of a complex m x n x m gemm)
+    a = torch.complex(_mat(n, n, seed=75), _mat(n, n, seed=76)).to(torch.complex128)
+    a = torch.tril(a) + n * torch.eye(n, dtype=torch.complex128, device="cuda")
+    a = a.t().contiguous().t()
+    b0 = torch.complex(_mat(n, n, seed=77), _mat(n, n, seed=78)).t().contiguous().t()
+    x = b0.clone()
+    one = _lib.DComplex(1.0, 0.0)
+    for mode, form in ((0, "native_fp64"), (1, "ozaki_s7")):
+        L.gb_set_dgemm_mode(mode, 7)
+        fn = lambda: (x.copy_(b0), _lib.check(L.gb_ztrsm_dev(0, 0xC0, 0, 0, n, n, one, a.data_ptr(), 1, n,
+                                                             x.data_ptr(), 1, n, _stream()), "ztrsm"))
+        ms = _timer(fn, reps=1 if mode == 0 else 3, warmup=1)
+        copy_ms = _timer(lambda: x.copy_(b0), reps=3, warmup=1)
+        out.append({"workload": "ztrsm_%dx%d" % (n, n), "form": form, "ms": ms - copy_ms,
+                    "tflops": 4.0 * n ** 3 / (ms - copy_ms) / 1e9})
     L.gb_set_dgemm_mode(0, 8)
 
 

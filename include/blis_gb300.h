@@ -138,6 +138,15 @@ void cgemm_(const gb_f77_char* transa, const gb_f77_char* transb,
             const gb_scomplex* b, const gb_f77_int* ldb, const gb_scomplex* beta,
             gb_scomplex* c, const gb_f77_int* ldc);
 
+/* replaces ztrsm_, frame/compat/bla_trsm.c:121-219 for dcomplex (checks
+   frame/compat/check/bla_trmm_check.h:37-86; 'C' solves with A^H): the
+   recursive solve with complex diagonal-block kernels and complex gemm
+   updates */
+void ztrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, gb_dcomplex* b,
+            const gb_f77_int* ldb);
+
 /* replace dscal_ (frame/compat/bla_scal.c:44-85; alpha == 0 sets zeros
    without reading x, ref_kernels/1/bli_scalv_ref.c:54-75), dcopy_
    (frame/compat/bla_copy.c:44-81), idamax_ (frame/compat/bla_amax.c:44-91:
@@ -265,6 +274,11 @@ void bli_cgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_
                const gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const gb_scomplex* beta,
                gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c);
 
+/* replaces bli_ztrsm (frame/3/bli_l3_tapi_ex.c:536-586 for dcomplex) */
+void bli_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+               gb_dim_t n, const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a,
+               gb_inc_t cs_a, gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b);
+
 /* replace bli_dscalv (frame/1/bli_l1v_tapi.c:314-345), bli_dcopyv (:46-77),
    bli_damaxv (:84-112), bli_dger (frame/2/bli_l2_tapi.c:129-175) and
    bli_dtrsv (:441-509); conjugation is the identity for real data */
@@ -341,6 +355,22 @@ void gb_sgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_d
               const float* alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a,
               const float* b, gb_inc_t rs_b, gb_inc_t cs_b, const float* beta,
               float* c, gb_inc_t rs_c, gb_inc_t cs_c);
+/* The Ozaki form for one call, whatever gb_set_dgemm_mode says (slices 0:
+   the selector's proposal checked by the verifier); the sandbox maps a
+   comp_prec request on the obj_t to it. */
+void gb_dgemm_ozaki(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                    const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                    const double* b, gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c,
+                    gb_inc_t rs_c, gb_inc_t cs_c, int slices);
+/* Complex host aliases for the sandbox (same as bli_zgemm / bli_cgemm). */
+void gb_zgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+              const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+              const gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const gb_dcomplex* beta,
+              gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c);
+void gb_cgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+              const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+              const gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const gb_scomplex* beta,
+              gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c);
 void gb_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
               gb_dim_t m, gb_dim_t n, const double* alpha, const double* a,
               gb_inc_t rs_a, gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b);
@@ -395,6 +425,10 @@ int gb_cgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
                  gb_scomplex alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
                  const gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, gb_scomplex beta,
                  gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+
+int gb_ztrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+                 gb_dim_t n, gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                 gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
 
 /* Device-pointer forms of scalv, copyv, amaxv (the 0-based index written to
    device memory), ger and trsv (asynchronous on the stream). */

@@ -115,3 +115,70 @@ def test_zgemm_device_entry(gblib):
     assert gblib.gb_synchronize() == 0
     ref = (1.0 - 1.0j) * (a @ b)
     assert np.all(np.abs(cd.cpu().numpy() - ref) <= _bound(1.0 - 1.0j, a, b, 0.0, ref, U64, k))
+
+
+def test_per_call_ozaki_form_and_complex_host_alias(gblib):
+    # gb_dgemm_ozaki: the Ozaki form for one call while the library stays native
+    import ctypes as C
+    m, n, k = 300, 200, 250
+    a = po.expspread((m, k), 20, -10, 10)
+    b = po.expspread((k, n), 21, -10, 10)
+    c = np.zeros((m, n), order="F")
+    al, be = C.c_double(1.0), C.c_double(0.0)
+    p = lambda x: x.ctypes.data_as(C.c_void_p)
+    gblib.gb_dgemm_ozaki(0, 0, m, n, k, C.byref(al), p(a), 1, m, p(b), 1, k, C.byref(be), p(c), 1, m, 7)
+    ref = np.zeros((m, n), order="F")
+    po.ozaki_dgemm(0, 0, 1.0, a, b, 0.0, ref, 7)
+    assert np.array_equal(c, ref)
+    nat = np.zeros((m, n), order="F")
+    blas.dgemm("N", "N", m, n, k, 1.0, a, m, b, k, 0.0, nat, m)  # still the native form
+    assert not np.array_equal(nat, ref)
+    g = np.abs(a) @ np.abs(b)
+    assert np.all(np.abs(nat - ref) <= 4 * (k + 2) * U64 * g)
+    # gb_zgemm: the sandbox's complex alias
+    z1 = _cplx((40, 30), 22)
+    z2 = _cplx((30, 20), 23)
+    zc = np.zeros((40, 20), dtype=np.complex128, order="F")
+    one, zero = np.array([1.0 + 0j]), np.array([0j])
+    gblib.gb_zgemm(0, 0, 40, 20, 30, p(one), p(z1), 1, 40, p(z2), 1, 30, p(zero), p(zc), 1, 40)
+    assert np.all(np.abs(zc - z1 @ z2) <= _bound(1.0, z1, z2, 0.0, zc, U64, 30))
+
+
+def _ztri(a, uplo, diag):
+    t = np.tril(a) if uplo == "L" else np.triu(a)
+    if diag == "U":
+        t = t - np.diag(np.diag(t)) + np.eye(a.shape[0])
+    return t
+
+
+@pytest.mark.parametrize("side", ["L", "R"])
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("trans", ["N", "T", "C"])
+@pytest.mark.parametrize("diag", ["N", "U"])
+@pytest.mark.parametrize("m,n", [(150, 90), (65, 1), (1, 7)])
+def test_ztrsm_residual(side, uplo, trans, diag, m, n):
+    # the testsuite's trsm check: || op(A) X - alpha B || small against || B || (test_trsm.c residual)
+    na = m if side == "L" else n
+    a = _cplx((na, na), 30) / na + 2.0 * np.eye(na)
+    a = np.asfortranarray(a)
+    b0 = _cplx((m, n), 31)
+    x = b0.copy(order="F")
+    alpha = 0.5 + 1.5j
+    blas.ztrsm(side, uplo, trans, diag, m, n, alpha, a, na, x, m)
+    t = _op(_ztri(a, uplo, diag), trans)
+    lhs = t @ x if side == "L" else x @ t
+    assert np.linalg.norm(lhs - alpha * b0) <= 1e-13 * np.linalg.norm(alpha * b0)
+
+
+def test_ztrsm_ozaki_updates_and_alpha_zero():
+    m, n = 700, 300
+    a = np.asfortranarray(_cplx((m, m), 32) / m + 3.0 * np.eye(m))
+    b0 = _cplx((m, n), 33)
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 8)
+    x = b0.copy(order="F")
+    blas.ztrsm("L", "L", "C", "N", m, n, 1.0, a, m, x, m)
+    t = np.conj(np.tril(a)).T
+    assert np.linalg.norm(t @ x - b0) <= 1e-13 * np.linalg.norm(b0)
+    x[:] = np.nan  # alpha = 0: B := 0 without reading it
+    blas.ztrsm("L", "L", "C", "N", m, n, 0.0, a, m, x, m)
+    assert (x == 0).all()
