@@ -47,7 +47,7 @@ EMIN, EMAX = -20, 20
 SEED_A, SEED_B = 20261204, 20261205
 # DRAM read + write bytes of one ozaki_slice_gemm_pair_kernel launch at 4096^3, 7 slices, from
 # one ncu --set full capture (dram__bytes_read.sum + dram__bytes_write.sum)
-TRAFFIC_4096_BYTES = 7672756000 + 470106624
+TRAFFIC_4096_BYTES = 7136346112 + 473230848
 TRAFFIC_SLICES = 7
 
 
