@@ -81,7 +81,7 @@ __global__ void copyv_strided_kernel(int64_t n, const double* __restrict__ x, in
 // |x| is compared as its IEEE bit pattern (sign cleared): monotone in the
 // value, NaN above the infinity pattern, +0 and -0 equal; integer compares
 // keep the search off GB300's narrow FP64 pipe.
-constexpr unsigned long long ABS_MASK = 0x7FFFFFFFFFFFFFFFull, INF_BITS = 0x7FF0000000000000ull;
+constexpr unsigned long long INF_BITS = 0x7FF0000000000000ull;
 
 struct Cand {
     unsigned long long k;  // |x| bits; 0 with i = INT64_MAX for "none yet"
@@ -127,9 +127,13 @@ __device__ __forceinline__ Cand block_best(Cand c)
     return c;
 }
 
+// Built from the two 32-bit halves: a 64-bit mask of the sign bit is the
+// pattern of an FP64 absolute value, which would put every element on the
+// FP64 pipe.
 __device__ __forceinline__ unsigned long long abs_key(double v)
 {
-    return (unsigned long long)__double_as_longlong(v) & ABS_MASK;
+    const unsigned hi = (unsigned)__double2hiint(v) & 0x7FFFFFFFu, lo = (unsigned)__double2loint(v);
+    return ((unsigned long long)hi << 32) | lo;
 }
 
 // Pass 1: block b takes the contiguous range [b*chunk, min(n, (b+1)*chunk)),
@@ -207,7 +211,7 @@ __global__ void __launch_bounds__(NT) ger_kernel(int64_t m, int64_t n, double al
 // Unit-stride x and column-major A with 16-byte aligned columns: a CTA owns
 // GER_COLS columns and walks all rows two at a time (double2 loads and
 // stores with streaming hints), reading each pair of x once for its columns.
-__global__ void __launch_bounds__(NT) ger_vec_kernel(int64_t m2, int64_t n, double alpha,
+__global__ void __launch_bounds__(NT, 4) ger_vec_kernel(int64_t m2, int64_t n, double alpha,
                                                      const double2* __restrict__ x, const double* __restrict__ y,
                                                      int64_t incy, double* __restrict__ a, int64_t cs_a)
 {

@@ -838,9 +838,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 // ---------------------------------------------------------------- split
 // Row r of the row operand R: element (r, l) at R[r*sr + l*sl].  |x| as its
 // IEEE bit pattern is monotone in |x|, so the row maximum is an integer max.
+// Built from the two 32-bit halves: a 64-bit mask of the sign bit is the
+// pattern of an FP64 absolute value, which would put every element on
+// GB300's narrow FP64 pipe.
 __device__ __forceinline__ unsigned long long abs_bits(double x)
 {
-    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+    const unsigned hi = (unsigned)__double2hiint(x) & 0x7FFFFFFFu, lo = (unsigned)__double2loint(x);
+    return ((unsigned long long)hi << 32) | lo;
 }
 
 // Rows contiguous (sr == 1, e.g. column-major op(A)): thread per row, the
