@@ -992,7 +992,13 @@ __device__ __forceinline__ int oz_row_exponent(unsigned long long bits, int* non
         *nonfinite = 1;
         return 0;
     }
-    return ilogb(__longlong_as_double((long long)bits)) + 2;
+    // ilogb of a positive finite double from its bits, integers only (the
+    // tiled split calls this in every thread; a library ilogb would run on
+    // the FP64 pipe): the biased exponent for normal numbers, the position
+    // of the leading mantissa bit for subnormals
+    const int ex = (int)(bits >> 52);
+    if (ex != 0) return ex - 1023 + 2;
+    return (63 - __clzll((long long)bits)) - 1074 + 2;
 }
 
 // Tile of 32 rows x 64 k per block; writes S bf16 digit planes, K-major,
