@@ -159,6 +159,7 @@ int ozaki_alloc_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t ac
 int ozaki_split_a_rows(const OzA* A, int64_t r0, int64_t r1, cudaStream_t s);
 int ozaki_prepare_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t acs, int slices,
                     cudaStream_t s, OzA* A);
+int ozaki_alloc_b(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, cudaStream_t s, OzB* B);
 int ozaki_prepare_b(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, cudaStream_t s, OzB* B);
 void ozaki_release_b(OzB* B, cudaStream_t s);
 int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, double alpha, double beta, double* c,

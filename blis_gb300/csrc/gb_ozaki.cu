@@ -1315,6 +1315,29 @@ __global__ void __launch_bounds__(256, 2) oz_split_rows_kernel(int64_t rows, int
                      });
 }
 
+// Both operands of one product in one launch (oz_split_unit): blocks
+// [0, units_a) take rows of op(A), the rest rows of op(B)^T; each operand's
+// padding rows up to its plane height are written as zeros.
+struct OzSplitOperand {
+    const double* R;
+    int64_t rows, sr, sl, rpad;
+    uint16_t* out;
+    int32_t* exps;
+};
+
+template <int S>
+__global__ void __launch_bounds__(256, 2) oz_split_two_kernel(OzSplitOperand a, OzSplitOperand b, int64_t units_a,
+                                                           int64_t k, int64_t kpad, int* __restrict__ nonfinite)
+{
+    const bool isb = (int64_t)blockIdx.x >= units_a;
+    const OzSplitOperand& o = isb ? b : a;
+    const int64_t r0 = ((int64_t)blockIdx.x - (isb ? units_a : 0)) * 32;
+    oz_split_unit<S>(o.R, o.rows, o.sr, o.sl, k, (int)(kpad / 64), r0, o.exps, nonfinite,
+                     [&](int p, int kb, int rr, int c0, uint4 v) {
+                         *reinterpret_cast<uint4*>(o.out + ((int64_t)p * o.rpad + r0 + rr) * kpad + kb * 64 + c0) = v;
+                     });
+}
+
 // ---------------------------------------------------------------- grouped form
 // Split for every problem of a batch in one launch.  A block owns 32 rows of
 // op(A_i) or op(B_i)^T over the whole k range (oz_split_unit) and writes
@@ -1741,7 +1764,7 @@ void ozaki_release_a(OzA* A, cudaStream_t s)
 // ((l, j) = b[l*brs + j*bcs]) for multiplications by a prepared op(A).
 // Columns of op(B) are split independently, so a product done in column
 // blocks gives the same bits as one call.
-int ozaki_prepare_b(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, cudaStream_t s, OzB* B)
+int ozaki_alloc_b(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, cudaStream_t s, OzB* B)
 {
     *B = OzB();
     B->n = n;
@@ -1757,9 +1780,16 @@ int ozaki_prepare_b(const OzA* A, int64_t n, const double* b, int64_t brs, int64
     B->sb = reinterpret_cast<uint16_t*>(B->ws);
     B->maxb = reinterpret_cast<unsigned long long*>(B->ws + bytes_sb);
     B->eb = reinterpret_cast<int32_t*>(B->maxb + n);
+    return GB_SUCCESS;
+}
+
+int ozaki_prepare_b(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, cudaStream_t s, OzB* B)
+{
+    int rc = ozaki_alloc_b(A, n, b, brs, bcs, s, B);
+    if (rc) return rc;
     // rows of op(B)^T: (j, l) = b[l*brs + j*bcs]
     split_operand(A->slices, n, A->k, b, bcs, brs, B->maxb, B->npad, B->npad, A->kpad, B->sb, B->eb, A->nonfinite, s);
-    const int rc = check_cuda(cudaGetLastError(), "oz_split");
+    rc = check_cuda(cudaGetLastError(), "oz_split");
     if (rc) ozaki_release_b(B, s);
     return rc;
 }
@@ -1900,6 +1930,20 @@ int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_
     return rc;
 }
 
+namespace {
+
+template <int S>
+void launch_split_two(const OzA* A, const OzB* B, cudaStream_t s)
+{
+    OzSplitOperand oa{A->a, A->m, A->ars, A->acs, A->mpad, A->sa, A->ea};
+    OzSplitOperand ob{B->b, B->n, B->bcs, B->brs, B->npad, B->sb, B->eb};  // rows of op(B)^T
+    const int64_t ua = A->mpad / 32, ub = B->npad / 32;
+    LaunchScope ls("oz_split_rows", s);
+    oz_split_two_kernel<S><<<(unsigned)(ua + ub), 256, 0, s>>>(oa, ob, ua, A->k, A->kpad, A->nonfinite);
+}
+
+}  // namespace
+
 int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
                 const double* a, int64_t ars, int64_t acs,
                 const double* b, int64_t brs, int64_t bcs, double beta,
@@ -1908,9 +1952,36 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     if (m <= 0 || n <= 0) return GB_SUCCESS;
     if (alpha == 0.0 || k <= 0) return scal_matrix(m, n, beta, c, rs_c, cs_c, s);
     OzA A;
-    int rc = ozaki_prepare_a(m, k, a, ars, acs, slices, s, &A);
-    if (rc) return rc;
-    rc = ozaki_multiply(&A, n, b, brs, bcs, alpha, beta, c, rs_c, cs_c, s);
+    int rc;
+    if (k > fused_split_max_k()) {
+        if ((rc = ozaki_prepare_a(m, k, a, ars, acs, slices, s, &A))) return rc;
+        rc = ozaki_multiply(&A, n, b, brs, bcs, alpha, beta, c, rs_c, cs_c, s);
+        ozaki_release_a(&A, s);
+        return rc;
+    }
+    // both operands split by one launch (the fused form: small k, so one launch saves a launch
+    // per product, e.g. half the split launches of a trsm)
+    if ((rc = ozaki_alloc_a(m, k, a, ars, acs, slices, s, &A))) return rc;
+    OzB B;
+    if ((rc = ozaki_alloc_b(&A, n, b, brs, bcs, s, &B))) {
+        ozaki_release_a(&A, s);
+        return rc;
+    }
+    if ((A.mpad + B.npad) / 32 > INT32_MAX) rc = set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "operands too large");
+    if (!rc) {
+        switch (slices) {
+#define GB_SPLIT_CASE(S) \
+    case S: launch_split_two<S>(&A, &B, s); break;
+            GB_SPLIT_CASE(2) GB_SPLIT_CASE(3) GB_SPLIT_CASE(4) GB_SPLIT_CASE(5) GB_SPLIT_CASE(6)
+            GB_SPLIT_CASE(7) GB_SPLIT_CASE(8) GB_SPLIT_CASE(9) GB_SPLIT_CASE(10) GB_SPLIT_CASE(11)
+            GB_SPLIT_CASE(12)
+#undef GB_SPLIT_CASE
+        default: break;
+        }
+        rc = check_cuda(cudaGetLastError(), "oz_split");
+    }
+    if (!rc) rc = ozaki_multiply_rows(&A, 0, m, &B, alpha, beta, c, rs_c, cs_c, s);
+    ozaki_release_b(&B, s);
     ozaki_release_a(&A, s);
     return rc;
 }
