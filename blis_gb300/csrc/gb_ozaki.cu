@@ -1233,14 +1233,25 @@ __device__ __forceinline__ void oz_split_unit(const double* __restrict__ R, int6
         const int rr = rows_fast ? (t & 31) : (t >> 3);
         const int l0 = rows_fast ? (t >> 5) : (t & 7);
         const int64_t r = r0 + rr;
-        unsigned long long mx = 0;
-        if (r < rows)
-#pragma unroll 4
-            for (int64_t l = l0; l < k; l += 8) {
+        unsigned long long mx = 0, my = 0;
+        if (r < rows) {
+            int64_t l = l0;
+            for (; l + 8 * 7 < k; l += 8 * 8) {  // eight loads in flight per thread
+                unsigned long long b[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) b[u] = abs_bits(__ldg(R + r * sr + (l + 8 * u) * sl));
+#pragma unroll
+                for (int u = 0; u < 8; u += 2) {
+                    mx = b[u] > mx ? b[u] : mx;
+                    my = b[u + 1] > my ? b[u + 1] : my;
+                }
+            }
+            for (; l < k; l += 8) {
                 const unsigned long long b = abs_bits(__ldg(R + r * sr + l * sl));
                 mx = b > mx ? b : mx;
             }
-        red[rows_fast ? (t >> 5) : (t & 7)][rr] = mx;
+        }
+        red[rows_fast ? (t >> 5) : (t & 7)][rr] = mx > my ? mx : my;
     }
     __syncthreads();
     if (t < 32) {
