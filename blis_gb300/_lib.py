@@ -84,6 +84,34 @@ def load(path=None):
                                       _i64, DComplex, _vp, _i64, _i64, _vp])
     _sig(L, "gb_cgemm_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, _i64, SComplex, _vp, _i64, _i64, _vp, _i64,
                                       _i64, SComplex, _vp, _i64, _i64, _vp])
+    _sig(L, "zherk_", None, [_cp, _cp, _ip, _ip, _vp, _vp, _ip, _vp, _vp, _ip])
+    _sig(L, "cherk_", None, [_cp, _cp, _ip, _ip, _vp, _vp, _ip, _vp, _vp, _ip])
+    her2k_blas = [_cp, _cp, _ip, _ip, _vp, _vp, _ip, _vp, _ip, _vp, _vp, _ip]
+    _sig(L, "zher2k_", None, her2k_blas)
+    _sig(L, "cher2k_", None, her2k_blas)
+    hemm_blas = [_cp, _cp, _ip, _ip, _vp, _vp, _ip, _vp, _ip, _vp, _vp, _ip]
+    for name in ("zhemm_", "chemm_", "zsymm_", "csymm_"):
+        _sig(L, name, None, hemm_blas)
+    _sig(L, "dsyr2k_", None, [_cp, _cp, _ip, _ip, _dp, _vp, _ip, _vp, _ip, _dp, _vp, _ip])
+    herk_t = [C.c_int, C.c_int, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _vp, _i64, _i64]
+    _sig(L, "bli_zherk", None, herk_t)
+    _sig(L, "bli_cherk", None, herk_t)
+    her2k_t = [C.c_int, C.c_int, C.c_int, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _i64, _i64]
+    _sig(L, "bli_zher2k", None, her2k_t)
+    _sig(L, "bli_cher2k", None, her2k_t)
+    _sig(L, "bli_dsyr2k", None, her2k_t)
+    hemm_t = [C.c_int] * 4 + [_i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _i64, _i64]
+    for name in ("bli_zhemm", "bli_chemm", "bli_zsymm", "bli_csymm"):
+        _sig(L, name, None, hemm_t)
+    _sig(L, "gb_zherk_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, _d, _vp, _i64, _i64, _d, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_zher2k_dev", C.c_int, [C.c_int, C.c_int, C.c_int, _i64, _i64, DComplex, _vp, _i64, _i64, _vp, _i64,
+                                       _i64, _d, _vp, _i64, _i64, _vp])
+    zhemm_d = [C.c_int] * 4 + [_i64, _i64, DComplex, _vp, _i64, _i64, _vp, _i64, _i64, DComplex, _vp, _i64, _i64,
+                               _vp]
+    _sig(L, "gb_zhemm_dev", C.c_int, zhemm_d)
+    _sig(L, "gb_zsymm_dev", C.c_int, zhemm_d)
+    _sig(L, "gb_dsyr2k_dev", C.c_int, [C.c_int, C.c_int, C.c_int, _i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64,
+                                       _d, _vp, _i64, _i64, _vp])
     _sig(L, "dscal_", None, [_ip, _dp, _vp, _ip])
     _sig(L, "dcopy_", None, [_ip, _vp, _ip, _vp, _ip])
     _sig(L, "idamax_", _i32, [_ip, _vp, _ip])

@@ -84,6 +84,57 @@ def ztrsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
                        _i(ldb))
 
 
+def _real_dtype(c):
+    return np.float64 if c.dtype == np.complex128 else np.float32
+
+
+def zherk(uplo, trans, n, k, alpha, a, lda, beta, c, ldc):
+    """zherk_ / cherk_ by c's dtype (alpha, beta real; trans 'N' or 'C')."""
+    L = _lib.load()
+    fn = L.zherk_ if c.dtype == np.complex128 else L.cherk_
+    rt = _real_dtype(c)
+    al, be = np.array([alpha], dtype=rt), np.array([beta], dtype=rt)
+    fn(_c(uplo), _c(trans), _i(n), _i(k), _p(al), _p(a), _i(lda), _p(be), _p(c), _i(ldc))
+
+
+cherk = zherk
+
+
+def zher2k(uplo, trans, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+    """zher2k_ / cher2k_ by c's dtype (alpha complex, beta real)."""
+    L = _lib.load()
+    fn = L.zher2k_ if c.dtype == np.complex128 else L.cher2k_
+    al, be = _cscalar(alpha, c.dtype), np.array([beta], dtype=_real_dtype(c))
+    fn(_c(uplo), _c(trans), _i(n), _i(k), _p(al), _p(a), _i(lda), _p(b), _i(ldb), _p(be), _p(c), _i(ldc))
+
+
+cher2k = zher2k
+
+
+def zhemm(side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc, herm=True):
+    """zhemm_ / chemm_ (herm) or zsymm_ / csymm_ by c's dtype."""
+    L = _lib.load()
+    z = c.dtype == np.complex128
+    fn = (L.zhemm_ if z else L.chemm_) if herm else (L.zsymm_ if z else L.csymm_)
+    al, be = _cscalar(alpha, c.dtype), _cscalar(beta, c.dtype)
+    fn(_c(side), _c(uplo), _i(m), _i(n), _p(al), _p(a), _i(lda), _p(b), _i(ldb), _p(be), _p(c), _i(ldc))
+
+
+chemm = zhemm
+
+
+def zsymm(side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc):
+    zhemm(side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc, herm=False)
+
+
+csymm = zsymm
+
+
+def dsyr2k(uplo, trans, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+    _lib.load().dsyr2k_(_c(uplo), _c(trans), _i(n), _i(k), _d(alpha), _p(a), _i(lda), _p(b), _i(ldb), _d(beta),
+                        _p(c), _i(ldc))
+
+
 def dscal(n, alpha, x, incx=1):
     _lib.load().dscal_(_i(n), _d(alpha), _p(x), _i(incx))
 
@@ -229,6 +280,43 @@ def bli_dgemmt(uplo, transa, transb, alpha, a, b, beta, c):
     k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
     _lib.load().bli_dgemmt(uplo, transa, transb, m, k, _d(alpha), _p(a), *_st(a), _p(b), *_st(b), _d(beta),
                            _p(c), *_st(c))
+
+
+def bli_zherk(uplo, transa, alpha, a, beta, c):
+    """bli_zherk / bli_cherk by c's dtype."""
+    m = c.shape[0]
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    L = _lib.load()
+    fn = L.bli_zherk if c.dtype == np.complex128 else L.bli_cherk
+    rt = _real_dtype(c)
+    al, be = np.array([alpha], dtype=rt), np.array([beta], dtype=rt)
+    fn(uplo, transa, m, k, _p(al), _p(a), *_st(a), _p(be), _p(c), *_st(c))
+
+
+def bli_zher2k(uplo, transa, transb, alpha, a, b, beta, c):
+    m = c.shape[0]
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    L = _lib.load()
+    fn = L.bli_zher2k if c.dtype == np.complex128 else L.bli_cher2k
+    al, be = _cscalar(alpha, c.dtype), np.array([beta], dtype=_real_dtype(c))
+    fn(uplo, transa, transb, m, k, _p(al), _p(a), *_st(a), _p(b), *_st(b), _p(be), _p(c), *_st(c))
+
+
+def bli_zhemm(side, uplo, conja, transb, alpha, a, b, beta, c, herm=True):
+    """bli_zhemm / bli_chemm (herm) or bli_zsymm / bli_csymm by c's dtype."""
+    m, n = c.shape
+    L = _lib.load()
+    z = c.dtype == np.complex128
+    fn = (L.bli_zhemm if z else L.bli_chemm) if herm else (L.bli_zsymm if z else L.bli_csymm)
+    al, be = _cscalar(alpha, c.dtype), _cscalar(beta, c.dtype)
+    fn(side, uplo, conja, transb, m, n, _p(al), _p(a), *_st(a), _p(b), *_st(b), _p(be), _p(c), *_st(c))
+
+
+def bli_dsyr2k(uplo, transa, transb, alpha, a, b, beta, c):
+    m = c.shape[0]
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    _lib.load().bli_dsyr2k(uplo, transa, transb, m, k, _d(alpha), _p(a), *_st(a), _p(b), *_st(b), _d(beta), _p(c),
+                           *_st(c))
 
 
 def bli_dgemv(transa, alpha, a, x, beta, y, incx=1, incy=1):

@@ -700,6 +700,116 @@ int ztrsm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, c
     return finish(s, where);
 }
 
+// herk / her2k: the whole of C goes up and comes back, so the untouched
+// triangle round-trips unchanged
+template <typename T>
+int cherk_host(int uplo, int transa, int64_t m, int64_t k, T alpha, const T* a, int64_t rs_a, int64_t cs_a, T beta,
+               T* c, int64_t rs_c, int64_t cs_c, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const size_t esz = 2 * sizeof(T);
+    const bool ta = GB_IS_TRANS(transa);
+    Staged& C = bufs.next();
+    if ((rc = stage_in(c, m, m, rs_c, cs_c, esz, true, &C, s))) return rc;
+    Staged& A = bufs.next();
+    if (alpha != T(0) && k > 0 && (rc = stage_in(a, ta ? k : m, ta ? m : k, rs_a, cs_a, esz, true, &A, s))) return rc;
+    const int slices = (sizeof(T) == 8) ? level3_slices() : 0;
+    if ((rc = cherk_dev<T>(uplo, transa, m, k, alpha, reinterpret_cast<const T*>(A.origin), A.rs, A.cs, beta,
+                           reinterpret_cast<T*>(C.origin), C.rs, C.cs, slices, s)))
+        return rc;
+    if ((rc = stage_out(c, m, m, rs_c, cs_c, esz, C, s))) return rc;
+    return finish(s, where);
+}
+
+template <typename T>
+int cher2k_host(int uplo, int transa, int transb, int64_t m, int64_t k, const T* alpha, const T* a, int64_t rs_a,
+                int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, T beta, T* c, int64_t rs_c, int64_t cs_c,
+                const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const size_t esz = 2 * sizeof(T);
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    Staged& C = bufs.next();
+    if ((rc = stage_in(c, m, m, rs_c, cs_c, esz, true, &C, s))) return rc;
+    Staged& A = bufs.next();
+    Staged& B = bufs.next();
+    if (!(alpha[0] == T(0) && alpha[1] == T(0)) && k > 0) {
+        if ((rc = stage_in(a, ta ? k : m, ta ? m : k, rs_a, cs_a, esz, true, &A, s))) return rc;
+        if ((rc = stage_in(b, tb ? k : m, tb ? m : k, rs_b, cs_b, esz, true, &B, s))) return rc;
+    }
+    const int slices = (sizeof(T) == 8) ? level3_slices() : 0;
+    if ((rc = cher2k_dev<T>(uplo, transa, transb, m, k, alpha, reinterpret_cast<const T*>(A.origin), A.rs, A.cs,
+                            reinterpret_cast<const T*>(B.origin), B.rs, B.cs, beta, reinterpret_cast<T*>(C.origin),
+                            C.rs, C.cs, slices, s)))
+        return rc;
+    if ((rc = stage_out(c, m, m, rs_c, cs_c, esz, C, s))) return rc;
+    return finish(s, where);
+}
+
+template <typename T>
+int chemm_host(int side, int uplo, int herm, int conja, int transb, int64_t m, int64_t n, const T* alpha, const T* a, int64_t rs_a,
+               int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, const T* beta, T* c, int64_t rs_c, int64_t cs_c,
+               const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const size_t esz = 2 * sizeof(T);
+    const int64_t na = (side == GB_LEFT) ? m : n;
+    const bool tb = GB_IS_TRANS(transb);
+    Staged& C = bufs.next();
+    if ((rc = stage_in(c, m, n, rs_c, cs_c, esz, beta[0] != T(0) || beta[1] != T(0), &C, s))) return rc;
+    Staged& A = bufs.next();
+    Staged& B = bufs.next();
+    if (!(alpha[0] == T(0) && alpha[1] == T(0))) {
+        if ((rc = stage_in(a, na, na, rs_a, cs_a, esz, true, &A, s))) return rc;
+        if ((rc = stage_in(b, tb ? n : m, tb ? m : n, rs_b, cs_b, esz, true, &B, s))) return rc;
+    }
+    const int slices = (sizeof(T) == 8) ? level3_slices() : 0;
+    if ((rc = chemm_dev<T>(side, uplo, herm, conja, transb, m, n, alpha, reinterpret_cast<const T*>(A.origin), A.rs, A.cs,
+                           reinterpret_cast<const T*>(B.origin), B.rs, B.cs, beta, reinterpret_cast<T*>(C.origin),
+                           C.rs, C.cs, slices, s)))
+        return rc;
+    if ((rc = stage_out(c, m, n, rs_c, cs_c, esz, C, s))) return rc;
+    return finish(s, where);
+}
+
+int syr2k_host(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha, const double* a, int64_t rs_a,
+               int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c,
+               int64_t cs_c, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    Staged& C = bufs.next();
+    if ((rc = stage_in(c, m, m, rs_c, cs_c, 8, true, &C, s))) return rc;
+    Staged& A = bufs.next();
+    Staged& B = bufs.next();
+    if (alpha != 0.0 && k > 0) {
+        if ((rc = stage_in(a, ta ? k : m, ta ? m : k, rs_a, cs_a, 8, true, &A, s))) return rc;
+        if ((rc = stage_in(b, tb ? k : m, tb ? m : k, rs_b, cs_b, 8, true, &B, s))) return rc;
+    }
+    if ((rc = dsyr2k_dev(uplo, transa, transb, m, k, alpha, reinterpret_cast<const double*>(A.origin), A.rs, A.cs,
+                         reinterpret_cast<const double*>(B.origin), B.rs, B.cs, beta,
+                         reinterpret_cast<double*>(C.origin), C.rs, C.cs, level3_slices(), s)))
+        return rc;
+    if ((rc = stage_out(c, m, m, rs_c, cs_c, 8, C, s))) return rc;
+    return finish(s, where);
+}
+
 // ---------------------------------------------------------------- BLAS helpers
 bool lsame(char a, char b) { return toupper((unsigned char)a) == toupper((unsigned char)b); }
 
@@ -767,6 +877,83 @@ void gemm_blas(const char* name, const char* transa, const char* transb, const g
         }
     }
     gemm_host<T>(ta, tb, m0, n0, k0, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c, cs_c, name);
+}
+
+// herk / her2k checks (frame/compat/check/bla_herk_check.h:37-77,
+// bla_her2k_check.h:37-79): trans N or C only
+int herk_check(gb_f77_char uploc, gb_f77_char trans, gb_f77_int m, gb_f77_int k, gb_f77_int lda,
+                      gb_f77_int ldb, gb_f77_int ldc, bool two)
+{
+    const bool lower = lsame(uploc, 'L'), upper = lsame(uploc, 'U');
+    const bool nota = lsame(trans, 'N'), conja = lsame(trans, 'C');
+    const int nrowa = nota ? m : k;
+    if (!lower && !upper) return 1;
+    if (!nota && !conja) return 2;
+    if (m < 0) return 3;
+    if (k < 0) return 4;
+    if (lda < (nrowa > 1 ? nrowa : 1)) return 7;
+    if (two && ldb < (nrowa > 1 ? nrowa : 1)) return 9;
+    if (ldc < (m > 1 ? m : 1)) return two ? 12 : 10;
+    return 0;
+}
+
+template <typename T, typename C>
+void herk_blas(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+                      const T* alpha, const C* a, const gb_f77_int* lda, const T* beta, C* c, const gb_f77_int* ldc,
+                      const char* name)
+{
+    // frame/compat/bla_herk.c:45-130
+    const int info = herk_check(*uploc, *trans, *m, *k, *lda, 0, *ldc, false);
+    if (info) {
+        call_xerbla(sizeof(T) == 8 ? "ZHERK " : "CHERK ", info);
+        return;
+    }
+    // the BLAS early return: nothing to add and C not scaled (the diagonal is left as it is)
+    if (*m == 0 || ((*alpha == T(0) || *k == 0) && *beta == T(1))) return;
+    cherk_host<T>(lsame(*uploc, 'L') ? GB_LOWER : GB_UPPER, map_trans(*trans), *m, *k, *alpha, &a->real, 1, *lda,
+                  *beta, &c->real, 1, *ldc, name);
+}
+
+template <typename T, typename C>
+void her2k_blas(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+                       const C* alpha, const C* a, const gb_f77_int* lda, const C* b, const gb_f77_int* ldb,
+                       const T* beta, C* c, const gb_f77_int* ldc, const char* name)
+{
+    // frame/compat/bla_her2k.c:45-136
+    const int info = herk_check(*uploc, *trans, *m, *k, *lda, *ldb, *ldc, true);
+    if (info) {
+        call_xerbla(sizeof(T) == 8 ? "ZHER2K" : "CHER2K", info);
+        return;
+    }
+    if (*m == 0 || (((alpha->real == T(0) && alpha->imag == T(0)) || *k == 0) && *beta == T(1))) return;
+    const int t = map_trans(*trans);
+    cher2k_host<T>(lsame(*uploc, 'L') ? GB_LOWER : GB_UPPER, t, t, *m, *k, &alpha->real, &a->real, 1, *lda,
+                   &b->real, 1, *ldb, *beta, &c->real, 1, *ldc, name);
+}
+
+template <typename T, typename C>
+void hemm_blas(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
+                      const C* alpha, const C* a, const gb_f77_int* lda, const C* b, const gb_f77_int* ldb,
+                      const C* beta, C* c, const gb_f77_int* ldc, int herm, const char* xname, const char* name)
+{
+    // frame/compat/bla_hemm.c:45-120 / bla_symm.c:45-120, checks frame/compat/check/bla_hemm_check.h:37-79
+    const bool left = lsame(*side, 'L'), right = lsame(*side, 'R');
+    const bool lower = lsame(*uploa, 'L'), upper = lsame(*uploa, 'U');
+    const int nrowa = left ? *m : *n;
+    int info = 0;
+    if (!left && !right) info = 1;
+    else if (!lower && !upper) info = 2;
+    else if (*m < 0) info = 3;
+    else if (*n < 0) info = 4;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 7;
+    else if (*ldb < (*m > 1 ? *m : 1)) info = 9;
+    else if (*ldc < (*m > 1 ? *m : 1)) info = 12;
+    if (info) {
+        call_xerbla(xname, info);
+        return;
+    }
+    chemm_host<T>(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, herm, 0, GB_NO_TRANSPOSE, *m, *n,
+                  &alpha->real, &a->real, 1, *lda, &b->real, 1, *ldb, &beta->real, &c->real, 1, *ldc, name);
 }
 
 }  // namespace
@@ -888,6 +1075,87 @@ void ztrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char
                "ZTRSM");
 }
 
+void zherk_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+            const double* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const double* beta, gb_dcomplex* c,
+            const gb_f77_int* ldc)
+{
+    herk_blas<double, gb_dcomplex>(uploc, trans, m, k, alpha, a, lda, beta, c, ldc, "ZHERK");
+}
+
+void cherk_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+            const float* alpha, const gb_scomplex* a, const gb_f77_int* lda, const float* beta, gb_scomplex* c,
+            const gb_f77_int* ldc)
+{
+    herk_blas<float, gb_scomplex>(uploc, trans, m, k, alpha, a, lda, beta, c, ldc, "CHERK");
+}
+
+void zher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+             const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* b,
+             const gb_f77_int* ldb, const double* beta, gb_dcomplex* c, const gb_f77_int* ldc)
+{
+    her2k_blas<double, gb_dcomplex>(uploc, trans, m, k, alpha, a, lda, b, ldb, beta, c, ldc, "ZHER2K");
+}
+
+void cher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+             const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
+             const gb_f77_int* ldb, const float* beta, gb_scomplex* c, const gb_f77_int* ldc)
+{
+    her2k_blas<float, gb_scomplex>(uploc, trans, m, k, alpha, a, lda, b, ldb, beta, c, ldc, "CHER2K");
+}
+
+void zhemm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* b,
+            const gb_f77_int* ldb, const gb_dcomplex* beta, gb_dcomplex* c, const gb_f77_int* ldc)
+{
+    hemm_blas<double, gb_dcomplex>(side, uploa, m, n, alpha, a, lda, b, ldb, beta, c, ldc, 1, "ZHEMM ", "ZHEMM");
+}
+
+void chemm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
+            const gb_f77_int* ldb, const gb_scomplex* beta, gb_scomplex* c, const gb_f77_int* ldc)
+{
+    hemm_blas<float, gb_scomplex>(side, uploa, m, n, alpha, a, lda, b, ldb, beta, c, ldc, 1, "CHEMM ", "CHEMM");
+}
+
+void zsymm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* b,
+            const gb_f77_int* ldb, const gb_dcomplex* beta, gb_dcomplex* c, const gb_f77_int* ldc)
+{
+    hemm_blas<double, gb_dcomplex>(side, uploa, m, n, alpha, a, lda, b, ldb, beta, c, ldc, 0, "ZSYMM ", "ZSYMM");
+}
+
+void csymm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
+            const gb_f77_int* ldb, const gb_scomplex* beta, gb_scomplex* c, const gb_f77_int* ldc)
+{
+    hemm_blas<float, gb_scomplex>(side, uploa, m, n, alpha, a, lda, b, ldb, beta, c, ldc, 0, "CSYMM ", "CSYMM");
+}
+
+void dsyr2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+             const double* alpha, const double* a, const gb_f77_int* lda, const double* b, const gb_f77_int* ldb,
+             const double* beta, double* c, const gb_f77_int* ldc)
+{
+    // frame/compat/bla_syr2k.c:45-128, checks frame/compat/check/bla_syr2k_check.h:37-84 (real: 'C' is 'T')
+    const bool lower = lsame(*uploc, 'L'), upper = lsame(*uploc, 'U');
+    const bool nota = lsame(*trans, 'N'), ta = lsame(*trans, 'T') || lsame(*trans, 'C');
+    const int nrowa = nota ? *m : *k;
+    int info = 0;
+    if (!lower && !upper) info = 1;
+    else if (!nota && !ta) info = 2;
+    else if (*m < 0) info = 3;
+    else if (*k < 0) info = 4;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 7;
+    else if (*ldb < (nrowa > 1 ? nrowa : 1)) info = 9;
+    else if (*ldc < (*m > 1 ? *m : 1)) info = 12;
+    if (info) {
+        call_xerbla("DSYR2K", info);
+        return;
+    }
+    const int t = nota ? GB_NO_TRANSPOSE : GB_TRANSPOSE;
+    syr2k_host(lower ? GB_LOWER : GB_UPPER, t, t, *m, *k, *alpha, a, 1, *lda, b, 1, *ldb, *beta, c, 1, *ldc,
+               "DSYR2K");
+}
+
 void dtrmm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
             const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const double* alpha,
             const double* a, const gb_f77_int* lda, double* b, const gb_f77_int* ldb)
@@ -919,7 +1187,7 @@ void dsymm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int*
             const double* alpha, const double* a, const gb_f77_int* lda, const double* b, const gb_f77_int* ldb,
             const double* beta, double* c, const gb_f77_int* ldc)
 {
-    // frame/compat/bla_symm.c:45-119, checks frame/compat/check/bla_hemm_check.h:37-81
+    // frame/compat/bla_symm.c:45-119, checks frame/compat/check/bla_hemm_check.h:37-79
     const bool left = lsame(*side, 'L'), right = lsame(*side, 'R');
     const bool lower = lsame(*uploa, 'L'), upper = lsame(*uploa, 'U');
     const int nrowa = left ? *m : *n;
@@ -1239,6 +1507,75 @@ void bli_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t dia
                "bli_ztrsm");
 }
 
+// frame/3/bli_l3_tapi_ex.c herk / her2k / hemm / symm / syr2k (prototypes
+// frame/3/bli_l3_tapi_ex.h:62-168)
+void bli_zherk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const double* alpha, const gb_dcomplex* a,
+               gb_inc_t rs_a, gb_inc_t cs_a, const double* beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    cherk_host<double>(uploc, transa, m, k, *alpha, &a->real, rs_a, cs_a, *beta, &c->real, rs_c, cs_c, "bli_zherk");
+}
+
+void bli_cherk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const float* alpha, const gb_scomplex* a,
+               gb_inc_t rs_a, gb_inc_t cs_a, const float* beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    cherk_host<float>(uploc, transa, m, k, *alpha, &a->real, rs_a, cs_a, *beta, &c->real, rs_c, cs_c, "bli_cherk");
+}
+
+void bli_zher2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b,
+                gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    cher2k_host<double>(uploc, transa, transb, m, k, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b, *beta,
+                        &c->real, rs_c, cs_c, "bli_zher2k");
+}
+
+void bli_cher2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* b,
+                gb_inc_t rs_b, gb_inc_t cs_b, const float* beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    cher2k_host<float>(uploc, transa, transb, m, k, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b, *beta,
+                       &c->real, rs_c, cs_c, "bli_cher2k");
+}
+
+void bli_zhemm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+               const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b,
+               gb_inc_t rs_b, gb_inc_t cs_b, const gb_dcomplex* beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    chemm_host<double>(side, uploa, 1, conja == GB_CONJUGATE, transb, m, n, &alpha->real, &a->real, rs_a, cs_a,
+                       &b->real, rs_b, cs_b, &beta->real, &c->real, rs_c, cs_c, "bli_zhemm");
+}
+
+void bli_chemm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+               const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* b,
+               gb_inc_t rs_b, gb_inc_t cs_b, const gb_scomplex* beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    chemm_host<float>(side, uploa, 1, conja == GB_CONJUGATE, transb, m, n, &alpha->real, &a->real, rs_a, cs_a,
+                      &b->real, rs_b, cs_b, &beta->real, &c->real, rs_c, cs_c, "bli_chemm");
+}
+
+void bli_zsymm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+               const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b,
+               gb_inc_t rs_b, gb_inc_t cs_b, const gb_dcomplex* beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    chemm_host<double>(side, uploa, 0, conja == GB_CONJUGATE, transb, m, n, &alpha->real, &a->real, rs_a, cs_a,
+                       &b->real, rs_b, cs_b, &beta->real, &c->real, rs_c, cs_c, "bli_zsymm");
+}
+
+void bli_csymm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+               const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* b,
+               gb_inc_t rs_b, gb_inc_t cs_b, const gb_scomplex* beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    chemm_host<float>(side, uploa, 0, conja == GB_CONJUGATE, transb, m, n, &alpha->real, &a->real, rs_a, cs_a,
+                      &b->real, rs_b, cs_b, &beta->real, &c->real, rs_c, cs_c, "bli_csymm");
+}
+
+void bli_dsyr2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k, const double* alpha,
+                const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b, gb_inc_t rs_b, gb_inc_t cs_b,
+                const double* beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    syr2k_host(uploc, transa, transb, m, k, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c, cs_c, "bli_dsyr2k");
+}
+
 void bli_dscalv(gb_conj_t conjalpha, gb_dim_t n, const double* alpha, double* x, gb_inc_t incx)
 {
     (void)conjalpha;  // real
@@ -1515,6 +1852,64 @@ int gb_ztrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
     if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_ztrsm_dev", "negative dimension");
     return gb::ztrsm_dev(side, uploa, transa, diaga, m, n, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
                          gb::level3_slices(), pick_stream(stream));
+}
+
+int gb_zherk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, double alpha, const gb_dcomplex* a,
+                 gb_inc_t rs_a, gb_inc_t cs_a, double beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_zherk_dev", "negative dimension");
+    return gb::cherk_dev<double>(uploc, transa, m, k, alpha, &a->real, rs_a, cs_a, beta, &c->real, rs_c, cs_c,
+                                 gb::level3_slices(), pick_stream(stream));
+}
+
+int gb_zher2k_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k, gb_dcomplex alpha,
+                  const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b, gb_inc_t rs_b,
+                  gb_inc_t cs_b, double beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_zher2k_dev", "negative dimension");
+    return gb::cher2k_dev<double>(uploc, transa, transb, m, k, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                                  beta, &c->real, rs_c, cs_c, gb::level3_slices(), pick_stream(stream));
+}
+
+int gb_zhemm_dev(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+                 gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, gb_dcomplex beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c,
+                 void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_zhemm_dev", "negative dimension");
+    return gb::chemm_dev<double>(side, uploa, 1, conja == GB_CONJUGATE, transb, m, n, &alpha.real, &a->real, rs_a,
+                                 cs_a, &b->real, rs_b, cs_b, &beta.real, &c->real, rs_c, cs_c, gb::level3_slices(),
+                                 pick_stream(stream));
+}
+
+int gb_zsymm_dev(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+                 gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, gb_dcomplex beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c,
+                 void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_zsymm_dev", "negative dimension");
+    return gb::chemm_dev<double>(side, uploa, 0, conja == GB_CONJUGATE, transb, m, n, &alpha.real, &a->real, rs_a,
+                                 cs_a, &b->real, rs_b, cs_b, &beta.real, &c->real, rs_c, cs_c, gb::level3_slices(),
+                                 pick_stream(stream));
+}
+
+int gb_dsyr2k_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k, double alpha,
+                  const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b, gb_inc_t rs_b, gb_inc_t cs_b,
+                  double beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_dsyr2k_dev", "negative dimension");
+    return gb::dsyr2k_dev(uploc, transa, transb, m, k, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c, cs_c,
+                          gb::level3_slices(), pick_stream(stream));
 }
 
 int gb_dscalv_dev(gb_dim_t n, double alpha, double* x, gb_inc_t incx, void* stream)

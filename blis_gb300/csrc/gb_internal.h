@@ -130,6 +130,20 @@ int dsymm_dev(int side, int uplo, int64_t m, int64_t n, double alpha, const doub
 int dgemmt_dev(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha, const double* a,
                int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c,
                int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s);
+int dsyr2k_dev(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+               const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c,
+               int slices, cudaStream_t s);
+template <typename T>
+int cherk_dev(int uplo, int transa, int64_t m, int64_t k, T alpha, const T* a, int64_t rs_a, int64_t cs_a, T beta,
+              T* c, int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s);
+template <typename T>
+int cher2k_dev(int uplo, int transa, int transb, int64_t m, int64_t k, const T* alpha, const T* a, int64_t rs_a,
+               int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, T beta, T* c, int64_t rs_c, int64_t cs_c,
+               int slices, cudaStream_t s);
+template <typename T>
+int chemm_dev(int side, int uplo, int herm, int conja, int transb, int64_t m, int64_t n, const T* alpha, const T* a,
+              int64_t rs_a, int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, const T* beta, T* c, int64_t rs_c,
+              int64_t cs_c, int slices, cudaStream_t s);
 // The Ozaki form in two phases (gb_ozaki.cu): op(A) split once, then any
 // number of products with column blocks of op(B) (bit-identical to one call).
 struct OzA {

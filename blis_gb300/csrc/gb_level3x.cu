@@ -371,4 +371,20 @@ int dgemmt_dev(int uplo, int transa, int transb, int64_t m, int64_t k, double al
     return rc;
 }
 
+// syr2k: the stored triangle of C := alpha op(A) op(B)^T + alpha op(B)
+// op(A)^T + beta C, op(A), op(B) m x k -- as BLIS, two gemmt calls, the
+// second accumulating onto the first (bli_syr2k_ex,
+// frame/3/bli_l3_oapi_ex.c:267-292).
+int dsyr2k_dev(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha, const double* a, int64_t rs_a,
+               int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c,
+               int64_t cs_c, int slices, cudaStream_t s)
+{
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    const int na = ta ? GB_TRANSPOSE : GB_NO_TRANSPOSE, fa = ta ? GB_NO_TRANSPOSE : GB_TRANSPOSE;
+    const int nb = tb ? GB_TRANSPOSE : GB_NO_TRANSPOSE, fb = tb ? GB_NO_TRANSPOSE : GB_TRANSPOSE;
+    int rc = dgemmt_dev(uplo, na, fb, m, k, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c, cs_c, slices, s);
+    if (rc || alpha == 0.0 || k <= 0) return rc;
+    return dgemmt_dev(uplo, nb, fa, m, k, alpha, b, rs_b, cs_b, a, rs_a, cs_a, 1.0, c, rs_c, cs_c, slices, s);
+}
+
 }  // namespace gb

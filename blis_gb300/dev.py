@@ -128,6 +128,13 @@ def dgemmt(uplo, transa, transb, alpha, a, b, beta, c):
     return _lib.check(rc, "gb_dgemmt_dev")
 
 
+def dsyr2k(uplo, transa, transb, alpha, a, b, beta, c):
+    m = c.shape[0]
+    rc = _lib.load().gb_dsyr2k_dev(uplo, transa, transb, m, _k(transa, a), alpha, a.data_ptr(), *_rc(a),
+                                   b.data_ptr(), *_rc(b), beta, c.data_ptr(), *_rc(c), _stream())
+    return _lib.check(rc, "gb_dsyr2k_dev")
+
+
 def daxpyv(alpha, x, y, incx=1, incy=1, n=None):
     n = x.numel() if n is None else n
     rc = _lib.load().gb_daxpyv_dev(n, alpha, x.data_ptr(), incx, y.data_ptr(), incy, _stream())

@@ -435,9 +435,44 @@ def run_complex(out):
     L.gb_set_dgemm_mode(0, 8)
 
 
+def run_hermitian(out):
+    """zherk L/N n = k = 4096 (4 n^2 k real flops: half of the complex product),
+    zher2k (8 n^2 k), zhemm L/L 4096 x 4096 (8 m^2 n) and dsyr2k L/N n = k =
+    8192 (2 n^2 k), native FP64 and Ozaki s = 7; U[-1,1] parts."""
+    import torch
+    n = 2048 if SMALL else 4096
+    L = _lib.load()
+
+    def cm(seed):
+        z = torch.complex(_mat(n, n, seed=seed), _mat(n, n, seed=seed + 1))
+        return z.t().contiguous().t()
+
+    a, b, c = cm(81), cm(83), cm(85)
+    one, half = _lib.DComplex(1.0, 0.0), _lib.DComplex(0.5, 0.0)
+    m2 = 2 * n
+    ra, rb, rc = _mat(m2, m2, seed=87), _mat(m2, m2, seed=88), _mat(m2, m2, seed=89)
+    for mode, form in ((0, "native_fp64"), (1, "ozaki_s7")):
+        L.gb_set_dgemm_mode(mode, 7)
+        reps = 1 if mode == 0 else 3
+        p = lambda t: t.data_ptr()
+        ms = _timer(lambda: _lib.check(L.gb_zherk_dev(0xC0, 0, n, n, 1.0, p(a), 1, n, 0.5, p(c), 1, n, _stream()),
+                                       "zherk"), reps=reps, warmup=1)
+        out.append({"workload": "zherk_%d_k%d" % (n, n), "form": form, "ms": ms, "tflops": 4.0 * n ** 3 / ms / 1e9})
+        ms = _timer(lambda: _lib.check(L.gb_zher2k_dev(0xC0, 0, 0, n, n, one, p(a), 1, n, p(b), 1, n, 0.5, p(c), 1, n,
+                                                       _stream()), "zher2k"), reps=reps, warmup=1)
+        out.append({"workload": "zher2k_%d_k%d" % (n, n), "form": form, "ms": ms, "tflops": 8.0 * n ** 3 / ms / 1e9})
+        ms = _timer(lambda: _lib.check(L.gb_zhemm_dev(0, 0xC0, 0, 0, n, n, one, p(a), 1, n, p(b), 1, n, half, p(c), 1,
+                                                      n, _stream()), "zhemm"), reps=reps, warmup=1)
+        out.append({"workload": "zhemm_%dx%d" % (n, n), "form": form, "ms": ms, "tflops": 8.0 * n ** 3 / ms / 1e9})
+        ms = _timer(lambda: dev.dsyr2k(0xC0, 0, 0, 1.0, ra, rb, 0.5, rc), reps=reps, warmup=1)
+        out.append({"workload": "dsyr2k_%d_k%d" % (m2, m2), "form": form, "ms": ms,
+                    "tflops": 2.0 * float(m2) ** 3 / ms / 1e9})
+    L.gb_set_dgemm_mode(0, 8)
+
+
 SUITES = {"gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
           "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm, "bgemm": run_bgemm,
-          "level3x": run_level3x, "level12x": run_level12x, "complex": run_complex}
+          "level3x": run_level3x, "level12x": run_level12x, "complex": run_complex, "hermitian": run_hermitian}
 
 
 def main():

@@ -147,6 +147,45 @@ void ztrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char
             const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, gb_dcomplex* b,
             const gb_f77_int* ldb);
 
+/* replace zherk_ / cherk_ (frame/compat/bla_herk.c:45-130, checks
+   frame/compat/check/bla_herk_check.h:37-77; trans N or C; the BLAS early
+   return when nothing is added and beta == 1), zher2k_ / cher2k_
+   (frame/compat/bla_her2k.c:45-136, checks bla_her2k_check.h:37-79), zhemm_
+   / chemm_ (frame/compat/bla_hemm.c:45-120), zsymm_ / csymm_
+   (frame/compat/bla_symm.c:45-120; checks bla_hemm_check.h:37-79) and
+   dsyr2k_ (frame/compat/bla_syr2k.c:45-128, checks bla_syr2k_check.h:37-84):
+   herk and her2k as one real gemmt on interleaved block-real operands, the
+   imaginary parts of C's diagonal zeroed (frame/3/bli_l3_oapi_ex.c:229-320);
+   hemm / symm as the complex gemm on the materialised A; syr2k as two
+   gemmt calls (frame/3/bli_l3_oapi_ex.c:267-292) */
+void zherk_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+            const double* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const double* beta,
+            gb_dcomplex* c, const gb_f77_int* ldc);
+void cherk_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+            const float* alpha, const gb_scomplex* a, const gb_f77_int* lda, const float* beta,
+            gb_scomplex* c, const gb_f77_int* ldc);
+void zher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+             const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* b,
+             const gb_f77_int* ldb, const double* beta, gb_dcomplex* c, const gb_f77_int* ldc);
+void cher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+             const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
+             const gb_f77_int* ldb, const float* beta, gb_scomplex* c, const gb_f77_int* ldc);
+void zhemm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* b,
+            const gb_f77_int* ldb, const gb_dcomplex* beta, gb_dcomplex* c, const gb_f77_int* ldc);
+void chemm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
+            const gb_f77_int* ldb, const gb_scomplex* beta, gb_scomplex* c, const gb_f77_int* ldc);
+void zsymm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* b,
+            const gb_f77_int* ldb, const gb_dcomplex* beta, gb_dcomplex* c, const gb_f77_int* ldc);
+void csymm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
+            const gb_f77_int* ldb, const gb_scomplex* beta, gb_scomplex* c, const gb_f77_int* ldc);
+void dsyr2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+             const double* alpha, const double* a, const gb_f77_int* lda, const double* b, const gb_f77_int* ldb,
+             const double* beta, double* c, const gb_f77_int* ldc);
+
 /* replace dscal_ (frame/compat/bla_scal.c:44-85; alpha == 0 sets zeros
    without reading x, ref_kernels/1/bli_scalv_ref.c:54-75), dcopy_
    (frame/compat/bla_copy.c:44-81), idamax_ (frame/compat/bla_amax.c:44-91:
@@ -278,6 +317,44 @@ void bli_cgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_
 void bli_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
                gb_dim_t n, const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a,
                gb_inc_t cs_a, gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b);
+
+/* replace bli_zherk / bli_cherk, bli_zher2k / bli_cher2k, bli_zhemm /
+   bli_chemm, bli_zsymm / bli_csymm and bli_dsyr2k (frame/3/bli_l3_tapi_ex.c;
+   prototypes frame/3/bli_l3_tapi_ex.h:62-168): herk takes real alpha and
+   beta, her2k a real beta; hemm / symm take conja (conjugates A) and transb */
+void bli_zherk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const double* alpha,
+               const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* beta, gb_dcomplex* c,
+               gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_cherk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const float* alpha,
+               const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const float* beta, gb_scomplex* c,
+               gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_zher2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                const gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, gb_dcomplex* c,
+                gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_cher2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                const gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const float* beta, gb_scomplex* c,
+                gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_zhemm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+               const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               const gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const gb_dcomplex* beta, gb_dcomplex* c,
+               gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_chemm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+               const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               const gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const gb_scomplex* beta, gb_scomplex* c,
+               gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_zsymm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+               const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               const gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const gb_dcomplex* beta, gb_dcomplex* c,
+               gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_csymm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
+               const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               const gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const gb_scomplex* beta, gb_scomplex* c,
+               gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_dsyr2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c);
 
 /* replace bli_dscalv (frame/1/bli_l1v_tapi.c:314-345), bli_dcopyv (:46-77),
    bli_damaxv (:84-112), bli_dger (frame/2/bli_l2_tapi.c:129-175) and
@@ -429,6 +506,28 @@ int gb_cgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
 int gb_ztrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
                  gb_dim_t n, gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
                  gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
+
+/* Device-pointer forms of zherk, zher2k, zhemm, zsymm and dsyr2k
+   (asynchronous on the stream). */
+int gb_zherk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, double alpha,
+                 const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, double beta, gb_dcomplex* c,
+                 gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+int gb_zher2k_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                  gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                  const gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, double beta, gb_dcomplex* c,
+                  gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+int gb_zhemm_dev(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m,
+                 gb_dim_t n, gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                 const gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, gb_dcomplex beta, gb_dcomplex* c,
+                 gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+int gb_zsymm_dev(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t transb, gb_dim_t m,
+                 gb_dim_t n, gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                 const gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, gb_dcomplex beta, gb_dcomplex* c,
+                 gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+int gb_dsyr2k_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                  double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                  gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c,
+                  void* stream);
 
 /* Device-pointer forms of scalv, copyv, amaxv (the 0-based index written to
    device memory), ger and trsv (asynchronous on the stream). */

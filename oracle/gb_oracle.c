@@ -35,6 +35,11 @@
  *   zgemm the complex definition, op() with the conjugation bit of trans_t
  *         (0x10; 'C' = 0x18), accumulation over l in order, then
  *         beta == 0 ? c = alpha ab : c = alpha ab + beta c (complex)
+ *   herk, her2k  frame/3/bli_l3_oapi_ex.c:295-320, 229-264: the uplo triangle
+ *         of the product(s) with op(.)^H, accumulated over l in order, the
+ *         imaginary parts of C's diagonal set to zero
+ *   hemm, complex symm  :349-520 on the materialised A, then zgemm
+ *   syr2k :267-292, two gemmt calls (the second with beta = 1)
  *   dotv  ref_kernels/1/bli_dotv_ref.c:37-121 (n == 0 gives rho = 0)
  * Not in the reference: the double-double evaluator (error oracle) and the
  * Ozaki split-product model (Ozaki, Ogita, Oishi & Rump 2012; integer-slice
@@ -802,4 +807,128 @@ int orc_ozaki_dgemm(int transa, int transb, int64_t m, int64_t n, int64_t k,
 native:
     orc_dgemm(transa, transb, m, n, k, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c, cs_c, nthreads);
     return 1;
+}
+
+/* ------------------------------------------------------------------ */
+/* herk / her2k / hemm / complex symm / syr2k                          */
+/* ------------------------------------------------------------------ */
+/* element (i, l) of op(X) with the conjugation bit of trans_t applied */
+static void z_op(const double* x, int64_t rs, int64_t cs, int trans, int64_t i, int64_t l,
+                 double* re, double* im)
+{
+    const int64_t r = ORC_TRANS(trans) ? l : i, c = ORC_TRANS(trans) ? i : l;
+    const double* p = x + 2 * (r * rs + c * cs);
+    *re = p[0];
+    *im = (trans & 0x10) ? -p[1] : p[1];
+}
+
+/* sum_l op(X)(i, l) conj(op(Y)(j, l)), accumulated over l in order */
+static void z_dot_conj(const double* x, int64_t xrs, int64_t xcs, int tx, const double* y,
+                       int64_t yrs, int64_t ycs, int ty, int64_t i, int64_t j, int64_t k,
+                       double* sr, double* si)
+{
+    double ar = 0.0, ai = 0.0;
+    for (int64_t l = 0; l < k; ++l) {
+        double xr, xi, yr, yi;
+        z_op(x, xrs, xcs, tx, i, l, &xr, &xi);
+        z_op(y, yrs, ycs, ty, j, l, &yr, &yi);
+        yi = -yi;
+        ar = fma(xr, yr, fma(-xi, yi, ar));
+        ai = fma(xr, yi, fma(xi, yr, ai));
+    }
+    *sr = ar;
+    *si = ai;
+}
+
+/* herk (frame/3/bli_l3_oapi_ex.c:295-320): gemmt with B = op(A)^H on the
+   uplo triangle, c = alpha s + beta c (beta == 0 does not read c), then the
+   imaginary parts of C's diagonal set to zero (bli_setid). */
+void orc_zherk(int uplo, int transa, int64_t m, int64_t k, double alpha, const double* a,
+               int64_t rs_a, int64_t cs_a, double beta, double* c, int64_t rs_c, int64_t cs_c)
+{
+    for (int64_t j = 0; j < m; ++j)
+        for (int64_t i = 0; i < m; ++i) {
+            if ((uplo == ORC_LOWER) ? (i < j) : (i > j)) continue;
+            double sr = 0.0, si = 0.0;
+            if (alpha != 0.0) z_dot_conj(a, rs_a, cs_a, transa, a, rs_a, cs_a, transa, i, j, k, &sr, &si);
+            double* pc = c + 2 * (i * rs_c + j * cs_c);
+            double cr = alpha * sr, ci = alpha * si;
+            if (beta != 0.0) {
+                cr += beta * pc[0];
+                ci += beta * pc[1];
+            }
+            pc[0] = cr;
+            pc[1] = (i == j) ? 0.0 : ci;
+        }
+}
+
+/* her2k (frame/3/bli_l3_oapi_ex.c:229-264): alpha op(A) op(B)^H +
+   conj(alpha) op(B) op(A)^H + beta c on the uplo triangle, the imaginary
+   parts of C's diagonal set to zero. */
+void orc_zher2k(int uplo, int transa, int transb, int64_t m, int64_t k, const double* alpha,
+                const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b,
+                int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c)
+{
+    const int nz = !(alpha[0] == 0.0 && alpha[1] == 0.0);
+    for (int64_t j = 0; j < m; ++j)
+        for (int64_t i = 0; i < m; ++i) {
+            if ((uplo == ORC_LOWER) ? (i < j) : (i > j)) continue;
+            double s1r = 0.0, s1i = 0.0, s2r = 0.0, s2i = 0.0;
+            if (nz) {
+                z_dot_conj(a, rs_a, cs_a, transa, b, rs_b, cs_b, transb, i, j, k, &s1r, &s1i);
+                z_dot_conj(b, rs_b, cs_b, transb, a, rs_a, cs_a, transa, i, j, k, &s2r, &s2i);
+            }
+            double* pc = c + 2 * (i * rs_c + j * cs_c);
+            double cr = (alpha[0] * s1r - alpha[1] * s1i) + (alpha[0] * s2r + alpha[1] * s2i);
+            double ci = (alpha[0] * s1i + alpha[1] * s1r) + (alpha[0] * s2i - alpha[1] * s2r);
+            if (beta != 0.0) {
+                cr += beta * pc[0];
+                ci += beta * pc[1];
+            }
+            pc[0] = cr;
+            pc[1] = (i == j) ? 0.0 : ci;
+        }
+}
+
+/* hemm (herm = 1) / complex symm (herm = 0) (frame/3/bli_l3_oapi_ex.c:349-520):
+   the full A from its uplo triangle -- the other triangle reflected,
+   conjugated for Hermitian A, the Hermitian diagonal read as real
+   (ref_kernels/1m/bli_packm_cxc_diag_1er_ref.c:214-225) -- conjugated when
+   conja, then the complex gemm with op(B) (transb). */
+void orc_zhemm(int side, int uplo, int herm, int conja, int transb, int64_t m, int64_t n,
+               const double* alpha, const double* a, int64_t rs_a, int64_t cs_a, const double* b,
+               int64_t rs_b, int64_t cs_b, const double* beta, double* c, int64_t rs_c, int64_t cs_c)
+{
+    if (m <= 0 || n <= 0) return;
+    const int64_t na = (side == ORC_LEFT) ? m : n;
+    double* f = (double*)malloc(sizeof(double) * (size_t)(2 * na * na));
+    for (int64_t j = 0; j < na; ++j)
+        for (int64_t i = 0; i < na; ++i) {
+            const int stored = (uplo == ORC_LOWER) ? (i >= j) : (i <= j);
+            const double* p = stored ? a + 2 * (i * rs_a + j * cs_a) : a + 2 * (j * rs_a + i * cs_a);
+            double im = p[1];
+            if (herm && !stored) im = -im;
+            if (herm && i == j) im = 0.0;
+            if (conja) im = -im;
+            f[2 * (i + j * na)] = p[0];
+            f[2 * (i + j * na) + 1] = im;
+        }
+    if (side == ORC_LEFT)
+        orc_zgemm(ORC_NO_TRANSPOSE, transb, m, n, m, alpha, f, 1, na, b, rs_b, cs_b, beta, c, rs_c, cs_c);
+    else
+        orc_zgemm(transb, ORC_NO_TRANSPOSE, m, n, n, alpha, b, rs_b, cs_b, f, 1, na, beta, c, rs_c, cs_c);
+    free(f);
+}
+
+/* syr2k (frame/3/bli_l3_oapi_ex.c:267-292): two gemmt calls, the second
+   with beta = 1. */
+void orc_dsyr2k(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha,
+                const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b,
+                int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c, int nthreads)
+{
+    const int ta = ORC_TRANS(transa), tb = ORC_TRANS(transb);
+    orc_dgemmt(uplo, ta ? ORC_TRANSPOSE : ORC_NO_TRANSPOSE, tb ? ORC_NO_TRANSPOSE : ORC_TRANSPOSE, m, k,
+               alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c, cs_c, nthreads);
+    orc_dgemmt(uplo, tb ? ORC_TRANSPOSE : ORC_NO_TRANSPOSE, ta ? ORC_NO_TRANSPOSE : ORC_TRANSPOSE, m, k,
+               alpha, b, rs_b, cs_b, a, rs_a, cs_a, 1.0, c, rs_c, cs_c, nthreads);
 }

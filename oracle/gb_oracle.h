@@ -78,6 +78,17 @@ void orc_daxpyv(int conjx, int64_t n, double alpha, const double* x, int64_t inc
 void orc_zgemm(int transa, int transb, int64_t m, int64_t n, int64_t k, const double* alpha,
                const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b,
                const double* beta, double* c, int64_t rs_c, int64_t cs_c);
+void orc_zherk(int uplo, int transa, int64_t m, int64_t k, double alpha, const double* a,
+               int64_t rs_a, int64_t cs_a, double beta, double* c, int64_t rs_c, int64_t cs_c);
+void orc_zher2k(int uplo, int transa, int transb, int64_t m, int64_t k, const double* alpha,
+                const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b,
+                int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c);
+void orc_zhemm(int side, int uplo, int herm, int conja, int transb, int64_t m, int64_t n,
+               const double* alpha, const double* a, int64_t rs_a, int64_t cs_a, const double* b,
+               int64_t rs_b, int64_t cs_b, const double* beta, double* c, int64_t rs_c, int64_t cs_c);
+void orc_dsyr2k(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha,
+                const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b,
+                int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c, int nthreads);
 void orc_dscalv(int64_t n, double alpha, double* x, int64_t incx);
 void orc_dcopyv(int64_t n, const double* x, int64_t incx, double* y, int64_t incy);
 void orc_damaxv(int64_t n, const double* x, int64_t incx, int64_t* index);

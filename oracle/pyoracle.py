@@ -50,6 +50,14 @@ def lib():
                                                   _i64, C.c_int]
         L.orc_zgemm.argtypes = [C.c_int, C.c_int, _i64, _i64, _i64, C.c_void_p, C.c_void_p, _i64, _i64,
                                 C.c_void_p, _i64, _i64, C.c_void_p, C.c_void_p, _i64, _i64]
+        L.orc_zherk.argtypes = [C.c_int, C.c_int, _i64, _i64, C.c_double, C.c_void_p, _i64, _i64, C.c_double,
+                                C.c_void_p, _i64, _i64]
+        L.orc_zher2k.argtypes = [C.c_int, C.c_int, C.c_int, _i64, _i64, C.c_void_p, C.c_void_p, _i64, _i64,
+                                 C.c_void_p, _i64, _i64, C.c_double, C.c_void_p, _i64, _i64]
+        L.orc_zhemm.argtypes = [C.c_int] * 5 + [_i64, _i64, C.c_void_p, C.c_void_p, _i64, _i64, C.c_void_p, _i64,
+                                                _i64, C.c_void_p, C.c_void_p, _i64, _i64]
+        L.orc_dsyr2k.argtypes = [C.c_int] * 3 + [_i64, _i64, C.c_double, C.c_void_p, _i64, _i64, C.c_void_p,
+                                                 _i64, _i64, C.c_double, C.c_void_p, _i64, _i64, C.c_int]
         L.orc_dscalv.argtypes = [_i64, C.c_double, C.c_void_p, _i64]
         L.orc_dcopyv.argtypes = [_i64, C.c_void_p, _i64, C.c_void_p, _i64]
         L.orc_damaxv.argtypes = [_i64, C.c_void_p, _i64, C.c_void_p]
@@ -174,6 +182,47 @@ def zgemm(transa, transb, alpha, a, b, beta, c):
     be = np.array([beta], dtype=np.complex128)
     st = lambda x: (x.strides[0] // x.itemsize, x.strides[1] // x.itemsize)
     lib().orc_zgemm(transa, transb, m, n, k, _p(al), _p(a), *st(a), _p(b), *st(b), _p(be), _p(c), *st(c))
+    return c
+
+
+def _zst(x):
+    return (x.strides[0] // x.itemsize, x.strides[1] // x.itemsize)
+
+
+def zherk(uplo, transa, alpha, a, beta, c):
+    """herk on complex128 arrays: the uplo triangle of C := alpha op(A) op(A)^H + beta C, the
+    imaginary parts of C's diagonal zeroed (alpha, beta real)."""
+    m = c.shape[0]
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    lib().orc_zherk(uplo, transa, m, k, alpha, _p(a), *_zst(a), beta, _p(c), *_zst(c))
+    return c
+
+
+def zher2k(uplo, transa, transb, alpha, a, b, beta, c):
+    """her2k on complex128 arrays (alpha complex, beta real)."""
+    m = c.shape[0]
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    al = np.array([alpha], dtype=np.complex128)
+    lib().orc_zher2k(uplo, transa, transb, m, k, _p(al), _p(a), *_zst(a), _p(b), *_zst(b), beta, _p(c),
+                     *_zst(c))
+    return c
+
+
+def zhemm(side, uplo, herm, conja, transb, alpha, a, b, beta, c):
+    """hemm (herm=1) / complex symm (herm=0) on complex128 arrays."""
+    m, n = c.shape
+    al = np.array([alpha], dtype=np.complex128)
+    be = np.array([beta], dtype=np.complex128)
+    lib().orc_zhemm(side, uplo, herm, conja, transb, m, n, _p(al), _p(a), *_zst(a), _p(b), *_zst(b), _p(be),
+                    _p(c), *_zst(c))
+    return c
+
+
+def dsyr2k(uplo, transa, transb, alpha, a, b, beta, c, nthreads=None):
+    m = c.shape[0]
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    lib().orc_dsyr2k(uplo, transa, transb, m, k, alpha, _p(a), *_strides(a), _p(b), *_strides(b), beta,
+                     _p(c), *_strides(c), nthreads or nthreads_default())
     return c
 
 

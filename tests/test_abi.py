@@ -147,3 +147,31 @@ def test_level12x_argument_errors(gblib, capfd):
     # idamax_: n < 1 or incx <= 0 return 0 without touching the device
     assert blas.idamax(0, x, 1) == 0 and blas.idamax(4, x, 0) == 0 and blas.idamax(4, x, -1) == 0
     _last()
+
+
+def test_hermitian_argument_errors(gblib, capfd):
+    # frame/compat/check/bla_herk_check.h:37-77, bla_her2k_check.h:37-79, bla_hemm_check.h:37-79,
+    # bla_syr2k_check.h:37-84
+    a = np.zeros(64, dtype=np.complex128)
+    c = np.full(64, 7.0 + 1.0j)
+    blas.zherk("L", "T", 2, 2, 1.0, a, 2, 0.0, c, 2)  # herk takes N or C only
+    assert "ZHERK" in capfd.readouterr().out
+    blas.zherk("U", "C", 2, 3, 1.0, a, 2, 0.0, c, 2)  # trans C: lda < k
+    assert "parameter number  7" in capfd.readouterr().out
+    blas.zherk("U", "N", 3, 2, 1.0, a, 3, 0.0, c, 2)  # ldc < n
+    assert "parameter number 10" in capfd.readouterr().out
+    blas.zher2k("L", "N", 3, 2, 1.0, a, 3, a, 2, 0.0, c, 3)  # ldb < n
+    assert "parameter number  9" in capfd.readouterr().out
+    blas.zher2k("X", "N", 3, 2, 1.0, a, 3, a, 3, 0.0, c, 3)
+    assert "ZHER2K" in capfd.readouterr().out
+    blas.zhemm("R", "L", 2, 3, 1.0, a, 2, a, 2, 0.0, c, 2)  # right: lda < n
+    assert "ZHEMM" in capfd.readouterr().out
+    blas.zsymm("L", "L", 3, 2, 1.0, a, 3, a, 3, 0.0, c, 2)  # ldc < m
+    assert "parameter number 12" in capfd.readouterr().out
+    blas.cherk("L", "N", -1, 2, 1.0, a.astype(np.complex64), 2, 0.0, c.astype(np.complex64), 2)
+    assert "CHERK" in capfd.readouterr().out
+    d = np.zeros(64)
+    blas.dsyr2k("L", "N", 3, 2, 1.0, d, 3, d, 2, 0.0, d, 3)
+    assert "DSYR2K" in capfd.readouterr().out
+    assert (c == 7.0 + 1.0j).all()
+    _last()
