@@ -150,6 +150,7 @@ struct OzA {
     int slices = 0;
     bool pair_form = false;
     int64_t row_tile = 0;       // rows of one slice GEMM output tile (256 for CTA pairs, 128 else)
+    int tri = 0;                // op(A) zero outside its lower (1) / upper (2) triangle: zero k blocks skipped
     int64_t m = 0, k = 0, mpad = 0, kpad = 0;
     const double* a = nullptr;  // op(A) (i, l) = a[i*ars + l*acs], kept for the IEEE fallback
     int64_t ars = 0, acs = 0;

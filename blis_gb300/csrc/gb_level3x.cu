@@ -14,7 +14,12 @@
 // trmm mirrors the recursive trsm: B = [B1; B2] with A = [A11 0; A21 A22]
 // (lower) becomes B2 := A22 B2; B2 += A21 B1; B1 := A11 B1, down to 64-row
 // diagonal blocks multiplied in shared memory, so nearly all flops are gemm
-// updates.  symm materialises the full symmetric A once (a copy of n^2
+// updates.  In the precision form (more than 256 rows) trmm is instead one
+// Ozaki product on the triangle materialised with zeros, reading the old B
+// from a copy; the slice GEMM skips the k blocks beyond each tile row's
+// triangle, so it does little more than the triangle's products, all at the
+// tensor-core rate.
+// symm materialises the full symmetric A once (a copy of n^2
 // elements against the n^2 m flops of the product) and calls gemm.  gemmt
 // works in 1024-column blocks of C: the part of a block column strictly
 // inside the triangle is one gemm written in place, the diagonal block is a
@@ -164,6 +169,36 @@ __global__ void __launch_bounds__(256) triangle_merge_kernel(int64_t w, int lowe
     }
 }
 
+// tri(op(A)) (m x m, op(A) (i, j) at a[i*ars + j*acs]) as a dense column-
+// major matrix: the uplo triangle, ones on the diagonal when unit, zeros
+// elsewhere
+__global__ void __launch_bounds__(256) tri_materialize_kernel(int64_t m, int lower, int unit,
+                                                              const double* __restrict__ a, int64_t ars,
+                                                              int64_t acs, double* __restrict__ out)
+{
+    const int64_t total = m * m;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = e / m, i = e - j * m;
+        double v = 0.0;
+        if (i == j) v = unit ? 1.0 : a[i * ars + j * acs];
+        else if (lower ? (i > j) : (i < j)) v = a[i * ars + j * acs];
+        out[e] = v;
+    }
+}
+
+// out (m x n column-major) := B (element (i, j) at b[i*rs + j*cs])
+__global__ void __launch_bounds__(256) gather_matrix_kernel(int64_t m, int64_t n, const double* __restrict__ b,
+                                                            int64_t rs, int64_t cs, double* __restrict__ out)
+{
+    const int64_t total = m * n;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = e / m, i = e - j * m;
+        out[e] = b[i * rs + j * cs];
+    }
+}
+
 unsigned grid_for(int64_t total)
 {
     const int sms = sm_count() > 0 ? sm_count() : 148;
@@ -262,6 +297,31 @@ int dtrmm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     t.ars = trans ? cs_a : rs_a;
     t.acs = trans ? rs_a : cs_a;
     t.lower = ((uplo == GB_LOWER) != trans) ? 1 : 0;
+    if (slices > 0 && mm > 4 * DB_NB) {
+        // The precision form as ONE Ozaki product on the triangle materialised
+        // with zeros: twice the products of the triangle, all at the slice
+        // GEMM's rate, where the recursion's FP64 diagonal multiplies and its
+        // many small updates set its pace.  The old B is read from a copy.
+        double* full = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(mm * mm + mm * nn), s));
+        if (!full) return GB_ERR_NOMEM;
+        double* old = full + mm * mm;
+        {
+            LaunchScope ls("trmm_materialize", s);
+            tri_materialize_kernel<<<grid_for(mm * mm), 256, 0, s>>>(mm, t.lower, diag == GB_UNIT_DIAG, a, t.ars,
+                                                                     t.acs, full);
+            gather_matrix_kernel<<<grid_for(mm * nn), 256, 0, s>>>(mm, nn, b, brs, bcs, old);
+        }
+        int rc = check_cuda(cudaGetLastError(), "trmm materialize");
+        OzA prep;
+        if (!rc) rc = ozaki_prepare_a(mm, mm, full, 1, mm, slices, s, &prep);
+        if (!rc) {
+            prep.tri = t.lower ? 1 : 2;  // the slice GEMM skips the k blocks beyond each tile row's triangle
+            rc = ozaki_multiply(&prep, nn, old, 1, mm, alpha, 0.0, b, brs, bcs, s);
+            ozaki_release_a(&prep, s);
+        }
+        dev_free(full, s);
+        return rc;
+    }
     t.slices = slices;
     t.a = a;
     t.b = b;

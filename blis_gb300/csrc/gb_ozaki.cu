@@ -74,6 +74,12 @@ struct OzGemmParams {
     unsigned int* status;
     const int* skip;  // non-finite flag of the split kernels
     unsigned long long* counter;  // unused here
+    // op(A) triangular with zeros outside its triangle (1 lower, 2 upper; 0
+    // dense): a tile row's items cover only the k blocks its rows reach.
+    // Rows of tile tm start at tri_row0 + tm * tri_rows.
+    int tri_mode = 0, tri_rows = 0;
+    int64_t tri_row0 = 0;
+    int64_t sched_p = 0;  // CTAs (pairs) that take items it, it + sched_p, ...
     OzLevel lv[OZ_MAX_SLICES];
 };
 
@@ -184,6 +190,13 @@ __device__ __forceinline__ bool oz_receive_item(const P& p, OzRing& r, int64_t& 
 
 __device__ __forceinline__ OzItem oz_decode(const OzGemmParams& p, int64_t it)
 {
+    if (p.tri_mode && p.sched_p > 0) {
+        // item costs vary with the tile row: the heaviest tile rows come first
+        // in each level (below) and every other full round of sched_p items is
+        // dealt in reverse, so the CTAs' totals even out
+        const int64_t r = it / p.sched_p, c = it - r * p.sched_p;
+        if ((r & 1) && (r + 1) * p.sched_p <= p.items) it = r * p.sched_p + (p.sched_p - 1 - c);
+    }
     int L = 0;
     while (L + 1 < p.nlevels && it >= p.lv[L + 1].item_base) ++L;
     const OzLevel& lv = p.lv[L];
@@ -205,9 +218,35 @@ __device__ __forceinline__ OzItem oz_decode(const OzGemmParams& p, int64_t it)
     const int64_t wi = t - group * G * (int64_t)p.tiles_n;
     w.tm = (int)(first_m + wi % gm);
     w.tn = (int)(wi / gm);
+    if (p.tri_mode) {
+        // tile rows by decreasing k extent: last row first for a lower op(A)
+        const int64_t row = t / p.tiles_n;
+        w.tm = (int)((p.tri_mode == 1) ? p.tiles_m - 1 - row : row);
+        w.tn = (int)(t - row * p.tiles_n);
+    }
     w.kb0 = part * lv.kb_per_part;
     const int kb_end = (w.kb0 + lv.kb_per_part < p.kb_total) ? w.kb0 + lv.kb_per_part : p.kb_total;
     w.kbn = kb_end - w.kb0;
+    if (p.tri_mode) {
+        // the blocks outside [lo, hi) hold only zero digits for these rows and
+        // add nothing to the exact sums; a part with none left keeps its first
+        // block (all zero here) so that its planes are still written
+        const int64_t r_lo = p.tri_row0 + (int64_t)w.tm * p.tri_rows;
+        int lo = w.kb0, hi = kb_end;
+        if (p.tri_mode == 1) {  // lower: row i reaches columns <= i
+            const int64_t need = (r_lo + p.tri_rows + OZ_BK - 1) / OZ_BK;
+            if (need < hi) hi = (int)need;
+        } else {  // upper: row i reaches columns >= i
+            const int64_t need = r_lo / OZ_BK;
+            if (need > lo) lo = (int)need;
+        }
+        if (hi > lo) {
+            w.kb0 = lo;
+            w.kbn = hi - lo;
+        } else {
+            w.kbn = 1;
+        }
+    }
     w.plane = lv.plane_base + part;
     w.prob = 0;
     return w;
@@ -1856,6 +1895,9 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
     p.npad = npad;
     p.m = m;
     p.n = n;
+    p.tri_mode = A->tri;
+    p.tri_rows = (int)A->row_tile;
+    p.tri_row0 = r0;
 
     const size_t bytes_pl = (size_t)planes_total * npad * mpad * 4;
     int32_t* planes = static_cast<int32_t*>(dev_alloc(bytes_pl + 1024, s));
@@ -1876,6 +1918,7 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
     if (pair_form) {
         if (max_pairs < 1) return bail(set_error(GB_ERR_UNSUPPORTED, "ozaki", "no CTA pair fits on this GPU"));
         const int npair = (int)((p.items < max_pairs) ? p.items : max_pairs);
+        p.sched_p = npair;
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1893,6 +1936,7 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
         if (rc) return bail(rc);
     } else {
         const int grid = (int)((p.items < sms) ? p.items : sms);
+        p.sched_p = grid;
         LaunchScope ls("ozaki_slice_gemm", s);
         ozaki_slice_gemm_kernel<OzGemmParams><<<grid, OZ_THREADS, OZ_SMEM_BYTES, s>>>(map_a, map_b, p);
     }

@@ -227,3 +227,29 @@ def test_device_api_syrk_and_trmm(gblib):
     assert gblib.gb_synchronize() == 0
     tri = _tri(t, "L", "U").T
     assert H.dmmch_ratio(0.5, c0, tri, 0.0, np.zeros_like(c0), bd.cpu().numpy()) < 2 * (n + 2)
+
+
+@pytest.mark.parametrize("side,uplo,trans,diag", [("L", "L", "N", "N"), ("L", "U", "T", "U"),
+                                                  ("R", "L", "N", "N"), ("R", "U", "N", "U")])
+def test_dtrmm_ozaki_bit_identical_to_model(side, uplo, trans, diag):
+    # the precision form is one Ozaki product on the triangle materialised with
+    # zeros; the slice GEMM skips each tile row's all-zero k blocks, which add
+    # nothing to the exact digit sums, so the result is the model's bit for bit
+    m, n = 700, 530
+    na = m if side == "L" else n
+    a = po.expspread((na, na), 41, -12, 12)
+    b0 = po.expspread((m, n), 42, -12, 12)
+    t = _tri(a, uplo, diag)
+    t = t.T if trans == "T" else t
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 7)
+    b = np.asfortranarray(b0.copy())
+    blas.dtrmm(side, uplo, trans, diag, m, n, -0.75, a, na, b, m)
+    if side == "L":
+        model = np.zeros((m, n), order="F")
+        po.ozaki_dgemm(0, 0, -0.75, np.asfortranarray(t), b0, 0.0, model, 7)
+    else:
+        # B op(A) runs as op(A)^T B^T
+        mt = np.zeros((n, m), order="F")
+        po.ozaki_dgemm(0, 0, -0.75, np.asfortranarray(t.T), np.asfortranarray(b0.T), 0.0, mt, 7)
+        model = mt.T
+    assert np.array_equal(b, model)
