@@ -117,6 +117,20 @@ cudaStream_t thread_copy_stream(int i)
     return t_copy[i & 1];
 }
 
+// A second compute stream per calling thread (work that forks from the
+// thread's stream and joins it again within one call).
+thread_local cudaStream_t t_aux = nullptr;
+thread_local int t_aux_dev = -1;
+
+cudaStream_t thread_aux_stream()
+{
+    if (t_aux == nullptr || t_aux_dev != g_device) {
+        cudaStreamCreateWithFlags(&t_aux, cudaStreamNonBlocking);
+        t_aux_dev = g_device;
+    }
+    return t_aux;
+}
+
 void* dev_alloc(size_t bytes, cudaStream_t s)
 {
     void* p = nullptr;

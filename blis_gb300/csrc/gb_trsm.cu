@@ -22,6 +22,7 @@ namespace gb {
 namespace {
 
 constexpr int TRSM_NB = 64;
+constexpr int64_t TRSM_SPLIT_MIN_COLS = 1024;  // columns per half for the two-stream precision form
 
 // Every diagonal block of op(A) in the form the solves read, packed once per
 // call: block q (rows and columns 64q .. 64q + nb - 1) becomes a row-major
@@ -196,42 +197,54 @@ int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t cco
                         t.brs, t.bcs, t.s);
 }
 
-int solve(const TrsmCtx& t, int64_t r0, int64_t mm)
+int diag_solve(const TrsmCtx& t, int64_t r0, int64_t mm)
 {
+    // r0 is a multiple of the block size: the split in solve keeps it so
+    const double* pk = t.packed + (r0 / TRSM_NB) * TRSM_NB * TRSM_NB;
+    double* b1 = t.b + r0 * t.brs;
+    const int nb = (int)mm;
+    LaunchScope ls("trsm_diag", t.s);
+    switch (diag_block_lanes(t.n)) {
+    case 1:
+        return t.lower ? launch_trsm_diag<1, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<1, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+    case 2:
+        return t.lower ? launch_trsm_diag<2, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<2, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+    case 4:
+        return t.lower ? launch_trsm_diag<4, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<4, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+    default:
+        return t.lower ? launch_trsm_diag<8, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<8, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+    }
+}
+
+// The recursion over rows for nt independent column groups of B (each with
+// its own stream), issued step by step in turn so that the groups' launches
+// interleave on the device.
+int solve(const TrsmCtx* ts, int nt, int64_t r0, int64_t mm)
+{
+    int rc;
     if (mm <= TRSM_NB) {
-        // r0 is a multiple of the block size: the split below keeps it so
-        const double* pk = t.packed + (r0 / TRSM_NB) * TRSM_NB * TRSM_NB;
-        double* b1 = t.b + r0 * t.brs;
-        const int nb = (int)mm;
-        LaunchScope ls("trsm_diag", t.s);
-        switch (diag_block_lanes(t.n)) {
-        case 1:
-            return t.lower ? launch_trsm_diag<1, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_trsm_diag<1, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
-        case 2:
-            return t.lower ? launch_trsm_diag<2, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_trsm_diag<2, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
-        case 4:
-            return t.lower ? launch_trsm_diag<4, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_trsm_diag<4, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
-        default:
-            return t.lower ? launch_trsm_diag<8, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_trsm_diag<8, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
-        }
+        for (int g = 0; g < nt; ++g)
+            if ((rc = diag_solve(ts[g], r0, mm))) return rc;
+        return GB_SUCCESS;
     }
     // split on a multiple of the diagonal block size
     int64_t m1 = ((mm / 2 + TRSM_NB - 1) / TRSM_NB) * TRSM_NB;
     if (m1 >= mm) m1 = mm - TRSM_NB;
     const int64_t m2 = mm - m1;
-    int rc;
-    if (t.lower) {
-        if ((rc = solve(t, r0, m1))) return rc;
-        if ((rc = update(t, r0 + m1, m2, r0, m1))) return rc;
-        return solve(t, r0 + m1, m2);
+    if (ts[0].lower) {
+        if ((rc = solve(ts, nt, r0, m1))) return rc;
+        for (int g = 0; g < nt; ++g)
+            if ((rc = update(ts[g], r0 + m1, m2, r0, m1))) return rc;
+        return solve(ts, nt, r0 + m1, m2);
     }
-    if ((rc = solve(t, r0 + m1, m2))) return rc;
-    if ((rc = update(t, r0, m1, r0 + m1, m2))) return rc;
-    return solve(t, r0, m1);
+    if ((rc = solve(ts, nt, r0 + m1, m2))) return rc;
+    for (int g = 0; g < nt; ++g)
+        if ((rc = update(ts[g], r0, m1, r0 + m1, m2))) return rc;
+    return solve(ts, nt, r0, m1);
 }
 
 }  // namespace
@@ -319,7 +332,30 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     }
     int rc = check_cuda(cudaGetLastError(), "trsm_pack_diag");
     t.packed = packed;
-    if (!rc) rc = solve(t, 0, mm);
+    if (!rc && slices > 0 && nn >= 2 * TRSM_SPLIT_MIN_COLS && mm > 4 * TRSM_NB) {
+        // the precision form's many small launches (split, slice GEMM,
+        // recombination per update) and the FP64-pipe diagonal solves of two
+        // column halves overlap on two streams
+        TrsmCtx ts[2] = {t, t};
+        const int64_t n1 = (nn / 2 + 7) / 8 * 8;
+        ts[0].n = n1;
+        ts[1].n = nn - n1;
+        ts[1].b = b + n1 * bcs;
+        ts[1].s = thread_aux_stream();
+        cudaEvent_t ev[2];
+        rc = check_cuda(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming), "trsm event");
+        if (!rc) rc = check_cuda(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming), "trsm event");
+        if (!rc) rc = check_cuda(cudaEventRecord(ev[0], s), "trsm fork");
+        if (!rc) rc = check_cuda(cudaStreamWaitEvent(ts[1].s, ev[0], 0), "trsm fork");
+        if (!rc) rc = solve(ts, 2, 0, mm);
+        // the join is recorded whatever happened, so s never runs ahead of the second stream's work
+        cudaEventRecord(ev[1], ts[1].s);
+        cudaStreamWaitEvent(s, ev[1], 0);
+        cudaEventDestroy(ev[0]);
+        cudaEventDestroy(ev[1]);
+    } else if (!rc) {
+        rc = solve(&t, 1, 0, mm);
+    }
     dev_free(packed, s);
     return rc;
 }

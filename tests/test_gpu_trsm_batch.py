@@ -237,3 +237,27 @@ def test_dtrsm_many_right_hand_sides(uplo, trans, n):
     tri = _tri(a, uplo, "N")
     r = H.trsm_residual(0, 1.5, tri.T if trans == "T" else tri, b0, x)
     assert r < 1e-12
+
+
+@pytest.mark.parametrize("side,uplo,trans", [("L", "L", "N"), ("L", "U", "T"), ("R", "U", "N"), ("R", "L", "T")])
+def test_dtrsm_ozaki_two_column_groups(side, uplo, trans):
+    # the precision form with at least 2048 right-hand sides solves two column
+    # halves on two streams; every column must still match the oracle
+    m, n = 700, 2600
+    rows, cols = (m, n) if side == "L" else (n, m)
+    na = m if side == "L" else m
+    a = np.asfortranarray(H.normalize(po.uniform((na, na), 16)) + 2.0 * np.eye(na))
+    b0 = H.normalize(po.uniform((rows, cols), 17))
+    ref = np.asfortranarray(b0.copy())
+    po.dtrsm(po.LEFT if side == "L" else po.RIGHT, po.LOWER if uplo == "L" else po.UPPER, 8 if trans == "T" else 0,
+             po.NONUNIT_DIAG, -0.5, a, ref)
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 8)
+    try:
+        x = np.asfortranarray(b0.copy())
+        blas.dtrsm(side, uplo, trans, "N", rows, cols, -0.5, a, na, x, rows)
+    finally:
+        blas.set_dgemm_mode(blas.DGEMM_NATIVE, 8)
+    tri = _tri(a, uplo, "N")
+    r = H.trsm_residual(0 if side == "L" else 1, -0.5, tri.T if trans == "T" else tri, b0, x)
+    assert r < 1e-12
+    assert np.max(np.abs(x - ref)) <= 1e-12 * np.max(np.abs(ref))
