@@ -182,6 +182,218 @@ struct TrsmCtx {
     cudaStream_t s;
 };
 
+// ---------------------------------------------------------------- trsv
+// One right-hand side in ONE launch.  CTA i (in the order of an atomic
+// ticket, so every block it waits for belongs to a CTA that is already
+// running or done) owns the 64-row block solved i-th: it accumulates op(A)'s
+// off-diagonal blocks times each earlier block of x as soon as that block's
+// flag is set, then solves its diagonal block in one warp (reciprocals of the
+// diagonal, as the packed trsm blocks) and publishes its x block with a
+// release flag.  Every wait is bounded: on timeout (or an abort set by
+// another CTA) the CTA reports DEV_WAIT_TIMEOUT, sets the abort flag and
+// returns.
+constexpr int SV_NB = 64;
+constexpr int SV_THREADS = 256;
+
+struct TrsvArgs {
+    int64_t m, nblk;
+    const double* a;
+    int64_t ars, acs;  // op(A) (i, j) at a[i*ars + j*acs]
+    double* x;
+    int64_t incx;
+    double alpha;
+    int unit;
+    int* flags;   // flags[b] = 1 once block b of x is final
+    int* ticket;  // next solve position
+    int* abort;   // set by a CTA that gave up
+    unsigned int* status;
+};
+
+__device__ __forceinline__ int ld_acquire(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int* p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ uint64_t sv_clock()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ROWMAJOR: op(A) rows contiguous (acs == 1): a warp's lanes run along the
+// columns; otherwise (ars == 1 or general) the threads run along the rows.
+template <bool LOWER, bool ROWMAJOR>
+__global__ void __launch_bounds__(SV_THREADS) trsv_flags_kernel(const TrsvArgs p)
+{
+    __shared__ double T[SV_NB][SV_NB + 1];
+    __shared__ double part[SV_THREADS / SV_NB][SV_NB];
+    __shared__ double xs[SV_NB];
+    __shared__ double dinv[SV_NB];
+    __shared__ int s_pos, s_fail;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        s_pos = atomicAdd(p.ticket, 1);
+        s_fail = 0;
+    }
+    __syncthreads();
+    const int64_t pos = s_pos;
+    if (pos >= p.nblk) return;  // the grid has exactly nblk CTAs
+    const int64_t blk = LOWER ? pos : p.nblk - 1 - pos;
+    const int64_t r0 = blk * SV_NB;
+    const int nb = (p.m - r0 < SV_NB) ? (int)(p.m - r0) : SV_NB;
+    // the diagonal block and this block's right-hand side (no other CTA writes it)
+    for (int e = tid; e < SV_NB * SV_NB; e += SV_THREADS) {
+        const int i = ROWMAJOR ? e / SV_NB : e % SV_NB, k = ROWMAJOR ? e % SV_NB : e / SV_NB;
+        T[i][k] = (i < nb && k < nb) ? p.a[(r0 + i) * p.ars + (r0 + k) * p.acs] : 0.0;
+    }
+    for (int r = tid; r < SV_NB * (SV_THREADS / SV_NB); r += SV_THREADS) (&part[0][0])[r] = 0.0;
+    __syncthreads();
+    // off the critical path, before any wait: the reciprocal diagonal and the
+    // rows of the triangle scaled by it (a unit triangle for y = D^-1 rhs)
+    if (tid < SV_NB) dinv[tid] = (tid < nb && !p.unit) ? 1.0 / T[tid][tid] : 1.0;
+    __syncthreads();
+    if (!p.unit)
+        for (int e = tid; e < SV_NB * SV_NB; e += SV_THREADS) {
+            const int i = e / SV_NB, k = e % SV_NB;
+            if (LOWER ? k < i : k > i) T[i][k] *= dinv[i];
+        }
+    double acc[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc[u] = 0.0;
+    const int rr = tid % SV_NB, q = tid / SV_NB;  // row-running mapping
+    for (int64_t s = 0; s < pos; ++s) {
+        const int64_t j = LOWER ? s : p.nblk - 1 - s;
+        const int64_t c0 = j * SV_NB;
+        if (tid == 0) {
+            const uint64_t t0 = sv_clock();
+            while (!ld_acquire(p.flags + j)) {
+                if (*(volatile int*)p.abort || sv_clock() - t0 > kWaitBudgetNs) {
+                    atomicOr(p.status, DEV_WAIT_TIMEOUT);
+                    atomicExch(p.abort, 1);
+                    s_fail = 1;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __syncthreads();
+        if (s_fail) return;
+        // columns of block j inside the matrix (the last block may be partial:
+        // it is the first one an upper solve reads)
+        const int ncol = (p.m - c0 < SV_NB) ? (int)(p.m - c0) : SV_NB;
+        if (tid < SV_NB) xs[tid] = (tid < ncol) ? __ldcg(p.x + (c0 + tid) * p.incx) : 0.0;
+        __syncthreads();
+        if (ROWMAJOR) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int64_t row = r0 + warp * 8 + u;
+                if (warp * 8 + u < nb) {
+                    const double* ar = p.a + row * p.ars + c0 * p.acs;
+                    if (lane < ncol) acc[u] = fma(ar[lane * p.acs], xs[lane], acc[u]);
+                    if (lane + 32 < ncol) acc[u] = fma(ar[(lane + 32) * p.acs], xs[lane + 32], acc[u]);
+                }
+            }
+        } else if (rr < nb) {
+            const double* ar = p.a + (r0 + rr) * p.ars + c0 * p.acs;
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const int c = q + 4 * u;
+                if (c < ncol) acc[u & 7] = fma(ar[c * p.acs], xs[c], acc[u & 7]);
+            }
+        }
+    }
+    if (ROWMAJOR) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            double v = acc[u];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) part[0][warp * 8 + u] = v;
+        }
+    } else {
+        double v = 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v += acc[u];
+        part[q][rr] = v;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        // rows lane and lane + 32; y = alpha b - (off-diagonal sums), then substitution
+        const int ra = lane, rb = lane + 32;
+        double y0 = 0.0, y1 = 0.0;
+        if (ra < nb)
+            y0 = dinv[ra] * (p.alpha * p.x[(r0 + ra) * p.incx] -
+                             (((part[0][ra] + part[1][ra]) + part[2][ra]) + part[3][ra]));
+        if (rb < nb)
+            y1 = dinv[rb] * (p.alpha * p.x[(r0 + rb) * p.incx] -
+                             (((part[0][rb] + part[1][rb]) + part[2][rb]) + part[3][rb]));
+        // y = D^-1 rhs against the unit triangle: x_i is y_i once the rows
+        // before it are applied; a half whose rows are all final is skipped
+        // by the whole warp
+        for (int step = 0; step < nb; ++step) {
+            const int i = LOWER ? step : nb - 1 - step;
+            const bool high = (i >= 32);
+            const double xi = __shfl_sync(0xffffffffu, high ? y1 : y0, i & 31);
+            if (LOWER ? !high : true) {
+                if (ra < nb && (LOWER ? ra > i : ra < i)) y0 = fma(-T[ra][i], xi, y0);
+            }
+            if (LOWER ? true : high) {
+                if (rb < nb && (LOWER ? rb > i : rb < i)) y1 = fma(-T[rb][i], xi, y1);
+            }
+        }
+        if (ra < nb) p.x[(r0 + ra) * p.incx] = y0;
+        if (rb < nb) p.x[(r0 + rb) * p.incx] = y1;
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(p.flags + blk, 1);
+    }
+}
+
+int launch_trsv(bool lower, bool unit, int64_t m, double alpha, const double* a, int64_t ars, int64_t acs, double* x,
+                int64_t incx, cudaStream_t s)
+{
+    const int64_t nblk = (m + SV_NB - 1) / SV_NB;
+    if (nblk > INT32_MAX / 2) return set_error(GB_ERR_ARG, "dtrsv", "too many blocks");
+    int* ws = static_cast<int*>(dev_alloc(sizeof(int) * (size_t)(nblk + 2), s));
+    if (!ws) return GB_ERR_NOMEM;
+    int rc = check_cuda(cudaMemsetAsync(ws, 0, sizeof(int) * (size_t)(nblk + 2), s), "trsv flags");
+    if (!rc) {
+        TrsvArgs p;
+        p.m = m;
+        p.nblk = nblk;
+        p.a = a;
+        p.ars = ars;
+        p.acs = acs;
+        p.x = x;
+        p.incx = incx;
+        p.alpha = alpha;
+        p.unit = unit ? 1 : 0;
+        p.flags = ws;
+        p.ticket = ws + nblk;
+        p.abort = ws + nblk + 1;
+        p.status = device_status_word();
+        const bool rowmajor = (acs == 1 && ars != 1);
+        LaunchScope ls("trsv_flags", s);
+        if (lower)
+            rowmajor ? trsv_flags_kernel<true, true><<<(unsigned)nblk, SV_THREADS, 0, s>>>(p)
+                     : trsv_flags_kernel<true, false><<<(unsigned)nblk, SV_THREADS, 0, s>>>(p);
+        else
+            rowmajor ? trsv_flags_kernel<false, true><<<(unsigned)nblk, SV_THREADS, 0, s>>>(p)
+                     : trsv_flags_kernel<false, false><<<(unsigned)nblk, SV_THREADS, 0, s>>>(p);
+        rc = check_cuda(cudaGetLastError(), "trsv_flags");
+    }
+    dev_free(ws, s);
+    return rc;
+}
+
 int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t ccount)
 {
     // B[r0:r0+rcount, :] -= op(A)[r0:.., c0:c0+ccount] * X[c0:c0+ccount, :]
@@ -303,6 +515,11 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
         trans = !trans;
     }
     if (alpha == 0.0) return scal_matrix(mm, nn, 0.0, b, brs, bcs, s);
+    if (nn == 1) {
+        // one right-hand side (trsv): the flag-ordered single launch, alpha folded in
+        const int64_t ars = trans ? cs_a : rs_a, acs = trans ? rs_a : cs_a;
+        return launch_trsv((uplo == GB_LOWER) != trans, diag == GB_UNIT_DIAG, mm, alpha, a, ars, acs, b, brs, s);
+    }
     if (alpha != 1.0) {
         int rc = scal_matrix(mm, nn, alpha, b, brs, bcs, s);
         if (rc) return rc;
