@@ -25,7 +25,7 @@ L2 where the workload allows:
                   slices) and FP32
 
 Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl] [--batch-count N] [--small]
-                                [--trsm-forms native,ozaki]
+                                [--trsm-forms native,ozaki] [--forms native,ozaki]
 (--small: 4096^3 GEMMs, 2048 x 10240 DTRSM, 2^25 vectors, 8192^2 GEMV, 4096-row level-3 extras,
 for ncu captures)
 """
@@ -42,6 +42,12 @@ from . import _lib, dev
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SMALL = False  # --small: profiling sizes (inputs still larger than the 126 MB L2)
 TRSM_FORMS = ("native", "ozaki")  # --trsm-forms: which DTRSM forms the trsm suites time
+FORMS = ("native", "ozaki")  # --forms: which forms the level3x, hermitian and complex suites time
+
+
+def _forms(pairs):
+    """The (mode, name) pairs of the forms selected by --forms (mode 0 native, 1 Ozaki)."""
+    return tuple(f for f in pairs if ("ozaki" if f[0] else "native") in FORMS)
 
 
 def peaks():
@@ -334,7 +340,7 @@ def run_level3x(out):
     C0 = _mat(m, n, seed=53)
     K = _mat(m, m, seed=54)
     S = _mat(m, m, seed=55)
-    for mode, name in ((0, "native_fp64"), (1, "ozaki_s7")):
+    for mode, name in _forms(((0, "native_fp64"), (1, "ozaki_s7"))):
         _lib.load().gb_set_dgemm_mode(mode, 7)
         reps = 1 if mode == 0 else 3
         x = B.clone()
@@ -403,7 +409,7 @@ def run_complex(out):
         b = torch.complex(_mat(n, n, seed=73, dtype=torch.float64), _mat(n, n, seed=74, dtype=torch.float64)).to(dt)
         a, b = a.t().contiguous().t(), b.t().contiguous().t()
         c = torch.zeros((n, n), dtype=dt, device="cuda").t()
-        forms = ((0, "native_fp64"), (1, "ozaki_s7")) if dt == torch.complex128 else ((0, "native_fp32"),)
+        forms = _forms(((0, "native_fp64"), (1, "ozaki_s7")) if dt == torch.complex128 else ((0, "native_fp32"),))
         for mode, form in forms:
             L.gb_set_dgemm_mode(mode, 7)
             if dt == torch.complex128:
@@ -424,7 +430,7 @@ def run_complex(out):
     b0 = torch.complex(_mat(n, n, seed=77), _mat(n, n, seed=78)).t().contiguous().t()
     x = b0.clone()
     one = _lib.DComplex(1.0, 0.0)
-    for mode, form in ((0, "native_fp64"), (1, "ozaki_s7")):
+    for mode, form in _forms(((0, "native_fp64"), (1, "ozaki_s7"))):
         L.gb_set_dgemm_mode(mode, 7)
         fn = lambda: (x.copy_(b0), _lib.check(L.gb_ztrsm_dev(0, 0xC0, 0, 0, n, n, one, a.data_ptr(), 1, n,
                                                              x.data_ptr(), 1, n, _stream()), "ztrsm"))
@@ -451,7 +457,7 @@ def run_hermitian(out):
     one, half = _lib.DComplex(1.0, 0.0), _lib.DComplex(0.5, 0.0)
     m2 = 2 * n
     ra, rb, rc = _mat(m2, m2, seed=87), _mat(m2, m2, seed=88), _mat(m2, m2, seed=89)
-    for mode, form in ((0, "native_fp64"), (1, "ozaki_s7")):
+    for mode, form in _forms(((0, "native_fp64"), (1, "ozaki_s7"))):
         L.gb_set_dgemm_mode(mode, 7)
         reps = 1 if mode == 0 else 3
         p = lambda t: t.data_ptr()
@@ -483,11 +489,13 @@ def main():
     ap.add_argument("--batch-count", type=int, default=4096, help="problems of the batch_ozaki suite")
     ap.add_argument("--small", action="store_true", help="profiling sizes (workload names keep the full size)")
     ap.add_argument("--trsm-forms", default="native,ozaki", help="DTRSM forms of the trsm suites")
+    ap.add_argument("--forms", default="native,ozaki", help="forms of the level3x, hermitian and complex suites")
     a = ap.parse_args()
-    global BATCH_COUNT, SMALL, TRSM_FORMS
+    global BATCH_COUNT, SMALL, TRSM_FORMS, FORMS
     BATCH_COUNT = a.batch_count
     SMALL = a.small
     TRSM_FORMS = tuple(f for f in a.trsm_forms.split(",") if f)
+    FORMS = tuple(f for f in a.forms.split(",") if f)
     torch.cuda.set_device(0)
     _lib.check(_lib.load().gb_init(0), "gb_init")
     names = [s for s in a.only.split(",") if s] or list(SUITES)
