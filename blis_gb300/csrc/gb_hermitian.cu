@@ -27,8 +27,9 @@
 // concatenates along k: X = [alpha op(A) | conj(alpha) op(B)],
 // Y = [op(B) | op(A)]^H (alpha folded into the packing, as BLIS folds
 // alpha into a packed operand).  The real gemm is the native FP64 / FP32
-// kernel or, for dcomplex in the precision form, the Ozaki kernel with
-// Xb split once for every block column.
+// kernel or, for dcomplex in the precision form, ONE Ozaki product on C's
+// real view that runs only the tiles holding part of the triangle and writes
+// only the triangle.
 //
 // hemm / symm materialise the full A from its stored triangle (the other
 // triangle reflected, conjugated for Hermitian A, whose diagonal is read as
@@ -177,11 +178,37 @@ int launch_merge(int64_t rows, int64_t cols, int64_t r0, int64_t c0, bool lower,
 // kernels above.  Column blocks of width W: the diagonal block through a
 // scratch block and the merge; the panel beside it straight into C when C is
 // column-stored, else through the scratch panel and the merge.
+// the imaginary parts of C's diagonal set to zero
+template <typename T>
+__global__ void __launch_bounds__(NT) zero_diag_imag_kernel(int64_t m, T* __restrict__ c, int64_t rs_c, int64_t cs_c)
+{
+    for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < m; i += (int64_t)gridDim.x * NT)
+        c[2 * (i * rs_c + i * cs_c) + 1] = T(0);
+}
+
 template <typename T>
 int herk_blocks(bool lower, int64_t m, int64_t kk, T alpha, const T* xb, const T* yb, T beta, T* c, int64_t rs_c,
                 int64_t cs_c, int slices, cudaStream_t s)
 {
     const bool direct = (rs_c == 1);
+    if constexpr (sizeof(T) == 8) {
+        if (slices > 0 && direct) {
+            // the precision form in one product on C's real view (rows 2i, 2i + 1
+            // of complex row i: out_rpc = 2), only the tiles and elements of the
+            // stored triangle, then the diagonal's imaginary parts
+            OzA prep;
+            int rc = ozaki_prepare_a(2 * m, 2 * kk, xb, 1, 2 * m, slices, s, &prep);
+            if (rc) return rc;
+            prep.out_tri = lower ? 1 : 2;
+            prep.out_rpc = 2;
+            rc = ozaki_multiply(&prep, m, yb, 1, 2 * kk, alpha, beta, c, 1, 2 * cs_c, s);
+            ozaki_release_a(&prep, s);
+            if (rc) return rc;
+            LaunchScope ls("herk_zero_diag", s);
+            zero_diag_imag_kernel<T><<<grid_of(m), NT, 0, s>>>(m, c, rs_c, cs_c);
+            return check_cuda(cudaGetLastError(), "herk zero diagonal");
+        }
+    }
     const int64_t wmax = (m < W) ? m : W;
     const int64_t srows = direct ? wmax : m;  // complex rows the scratch holds
     T* scratch = static_cast<T*>(dev_alloc(sizeof(T) * (size_t)(2 * srows * wmax), s));

@@ -152,6 +152,8 @@ struct OzA {
     bool pair_form = false;
     int64_t row_tile = 0;       // rows of one slice GEMM output tile (256 for CTA pairs, 128 else)
     int tri = 0;                // op(A) zero outside its lower (1) / upper (2) triangle: zero k blocks skipped
+    int out_tri = 0;            // write only C's lower (1) / upper (2) triangle: row i, column j stored when
+    int out_rpc = 1;            //   i / out_rpc >= j (<= j); out_rpc = 2 for a complex C's real view
     int64_t m = 0, k = 0, mpad = 0, kpad = 0;
     const double* a = nullptr;  // op(A) (i, l) = a[i*ars + l*acs], kept for the IEEE fallback
     int64_t ars = 0, acs = 0;

@@ -25,7 +25,9 @@
 // inside the triangle is one gemm written in place, the diagonal block is a
 // gemm into scratch merged into the triangle (beta applied there), so the
 // other triangle is never computed beyond the diagonal blocks (at most
-// 1024/m of the flops) and never touched.
+// 1024/m of the flops) and never touched.  In the precision form gemmt is
+// one Ozaki product whose slice GEMM runs only the tiles holding part of the
+// triangle and whose recombination writes only the triangle.
 #include "gb_internal.h"
 
 namespace gb {
@@ -390,10 +392,19 @@ int dgemmt_dev(int uplo, int transa, int transb, int64_t m, int64_t k, double al
     if (!scratch) return GB_ERR_NOMEM;
     int rc = GB_SUCCESS;
     const bool trivial = (alpha == 0.0 || k <= 0);
-    // the precision form splits op(A) once for every block column
-    OzA prep;
-    const bool oz = (slices > 0 && !trivial);
-    if (oz) rc = ozaki_prepare_a(m, k, a, ars, acs, slices, s, &prep);
+    if (slices > 0 && !trivial) {
+        // the precision form in one product: the slice GEMM runs only the
+        // tiles that hold part of the triangle and the recombination writes
+        // only the triangle (beta applied there)
+        dev_free(scratch, s);
+        OzA prep;
+        if ((rc = ozaki_prepare_a(m, k, a, ars, acs, slices, s, &prep))) return rc;
+        prep.out_tri = lower ? 1 : 2;
+        rc = ozaki_multiply(&prep, m, b, brs, bcs, alpha, beta, c, rs_c, cs_c, s);
+        ozaki_release_a(&prep, s);
+        return rc;
+    }
+    // the native form (and a trivial product) in 1024-column blocks
     for (int64_t j0 = 0; j0 < m && !rc; j0 += W) {
         const int64_t w = (m - j0 < W) ? m - j0 : W;
         double* cblk = c + j0 * rs_c + j0 * cs_c;
@@ -403,22 +414,15 @@ int dgemmt_dev(int uplo, int transa, int transb, int64_t m, int64_t k, double al
         }
         // strictly-triangle panel of this block column: rows below (lower) or above (upper)
         const int64_t pr0 = lower ? j0 + w : 0, prows = lower ? m - (j0 + w) : j0;
-        OzB pb;
-        if (oz && (rc = ozaki_prepare_b(&prep, w, b + j0 * bcs, brs, bcs, s, &pb))) break;
         if (!trivial) {
             // diagonal block into scratch (alpha applied, beta 0), merged below
-            rc = oz ? ozaki_multiply_rows(&prep, j0, w, &pb, alpha, 0.0, scratch, 1, w, s)
-                    : dgemm_native(w, w, k, alpha, a + j0 * ars, ars, acs, b + j0 * bcs, brs, bcs, 0.0, scratch, 1,
-                                   w, s);
+            rc = dgemm_native(w, w, k, alpha, a + j0 * ars, ars, acs, b + j0 * bcs, brs, bcs, 0.0, scratch, 1, w, s);
             if (!rc && prows > 0)
-                rc = oz ? ozaki_multiply_rows(&prep, pr0, prows, &pb, alpha, beta, c + pr0 * rs_c + j0 * cs_c, rs_c,
-                                              cs_c, s)
-                        : dgemm_native(prows, w, k, alpha, a + pr0 * ars, ars, acs, b + j0 * bcs, brs, bcs, beta,
-                                       c + pr0 * rs_c + j0 * cs_c, rs_c, cs_c, s);
+                rc = dgemm_native(prows, w, k, alpha, a + pr0 * ars, ars, acs, b + j0 * bcs, brs, bcs, beta,
+                                  c + pr0 * rs_c + j0 * cs_c, rs_c, cs_c, s);
         } else if (prows > 0) {
             rc = scal_matrix(prows, w, beta, c + pr0 * rs_c + j0 * cs_c, rs_c, cs_c, s);
         }
-        if (oz) ozaki_release_b(&pb, s);
         if (rc) break;
         {
             LaunchScope ls("triangle_merge", s);
@@ -426,7 +430,6 @@ int dgemmt_dev(int uplo, int transa, int transb, int64_t m, int64_t k, double al
         }
         rc = check_cuda(cudaGetLastError(), "triangle_merge");
     }
-    if (oz) ozaki_release_a(&prep, s);
     dev_free(scratch, s);
     return rc;
 }

@@ -80,6 +80,12 @@ struct OzGemmParams {
     int tri_mode = 0, tri_rows = 0;
     int64_t tri_row0 = 0;
     int64_t sched_p = 0;  // CTAs (pairs) that take items it, it + sched_p, ...
+    // only C's stored triangle (out_tri 1 lower, 2 upper): items run over the
+    // tiles_valid tiles that hold part of it, tile_cum[tm] of them in the
+    // tile rows before tm, the first at column tile tile_first[tm]
+    int out_tri = 0, tiles_valid = 0;
+    const int* tile_cum = nullptr;
+    const int* tile_first = nullptr;
     OzLevel lv[OZ_MAX_SLICES];
 };
 
@@ -204,20 +210,32 @@ __device__ __forceinline__ OzItem oz_decode(const OzGemmParams& p, int64_t it)
     w.lev = lv.lev;
     w.npairs = lv.npairs;
     w.pa_lo = lv.pa_lo;
-    const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
+    const int64_t tiles = p.out_tri ? (int64_t)p.tiles_valid : (int64_t)p.tiles_m * p.tiles_n;
     const int64_t rem = it - lv.item_base;
     const int part = (int)(rem / tiles);
     const int64_t t = rem % tiles;
-    // grouped raster over tiles, p.group_m tile rows per group (default
-    // OZ_GROUP_M = 16): the tiles in flight then share a few A and B panels
-    // in L2 instead of streaming whole rows of tiles
-    const int64_t G = p.group_m;
-    const int64_t group = t / (G * (int64_t)p.tiles_n);
-    const int64_t first_m = group * G;
-    const int64_t gm = (p.tiles_m - first_m < G) ? p.tiles_m - first_m : G;
-    const int64_t wi = t - group * G * (int64_t)p.tiles_n;
-    w.tm = (int)(first_m + wi % gm);
-    w.tn = (int)(wi / gm);
+    if (p.out_tri) {
+        // the t-th tile holding part of C's triangle: tile rows in order
+        int lo = 0, hi = p.tiles_m;  // tile_cum[lo] <= t < tile_cum[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(p.tile_cum + mid) <= t) lo = mid;
+            else hi = mid;
+        }
+        w.tm = lo;
+        w.tn = __ldg(p.tile_first + lo) + (int)(t - __ldg(p.tile_cum + lo));
+    } else {
+        // grouped raster over tiles, p.group_m tile rows per group (default
+        // OZ_GROUP_M = 16): the tiles in flight then share a few A and B
+        // panels in L2 instead of streaming whole rows of tiles
+        const int64_t G = p.group_m;
+        const int64_t group = t / (G * (int64_t)p.tiles_n);
+        const int64_t first_m = group * G;
+        const int64_t gm = (p.tiles_m - first_m < G) ? p.tiles_m - first_m : G;
+        const int64_t wi = t - group * G * (int64_t)p.tiles_n;
+        w.tm = (int)(first_m + wi % gm);
+        w.tn = (int)(wi / gm);
+    }
     if (p.tri_mode) {
         // tile rows by decreasing k extent: last row first for a lower op(A)
         const int64_t row = t / p.tiles_n;
@@ -1170,6 +1188,7 @@ struct OzRecombParams {
     double* c;
     int64_t rs_c, cs_c;
     const int* skip;
+    int out_tri = 0, out_rpc = 1;  // only C's stored triangle is read and written (as OzA::out_tri)
     OzLevel lv[OZ_MAX_SLICES];
 };
 
@@ -1194,6 +1213,9 @@ __global__ void __launch_bounds__(256, (S <= 7 ? 3 : 2)) oz_recombine_kernel(con
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = e / mq, i0 = (e - j * mq) * 4;
+        // rows of column j's diagonal element: lower keeps rows >= dlo, upper rows <= dhi
+        const int64_t dlo = (int64_t)p.out_rpc * j, dhi = dlo + p.out_rpc - 1;
+        if (p.out_tri && (p.out_tri == 1 ? i0 + 3 < dlo : i0 > dhi)) continue;
         const int64_t off = j * p.mpad + i0;  // mpad is a multiple of 128: 16-byte aligned
         int4 v[S];
 #pragma unroll
@@ -1220,6 +1242,7 @@ __global__ void __launch_bounds__(256, (S <= 7 ? 3 : 2)) oz_recombine_kernel(con
         for (int r = 0; r < 4; ++r) {
             const int64_t i = i0 + r;
             if (i >= p.m) break;
+            if (p.out_tri && (p.out_tri == 1 ? i < dlo : i > dhi)) continue;
             __int128 T = 0;
             if (one_part) {
                 int a[S];
@@ -1850,6 +1873,72 @@ void ozaki_release_b(OzB* B, cudaStream_t s)
     B->ws = nullptr;
 }
 
+// Tables of the tiles holding part of C's stored triangle (OzGemmParams::
+// out_tri): kept tiles before each tile row, and each row's first column
+// tile.  One thread; the host counts the same tiles for the item total.
+__global__ void oz_tri_tiles_kernel(int tiles_m, int tiles_n, int64_t row_tile, int64_t m, int rpc, int out_tri,
+                                    int* __restrict__ cum, int* __restrict__ first)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    int total = 0;
+    for (int tm = 0; tm < tiles_m; ++tm) {
+        const int64_t r_lo = (int64_t)tm * row_tile;
+        const int64_t r_hi = (((int64_t)(tm + 1) * row_tile < m) ? (int64_t)(tm + 1) * row_tile : m) - 1;
+        int f = 0, cnt;
+        if (out_tri == 1) {
+            int64_t last = (r_hi / rpc) / OZ_BN;
+            if (last > tiles_n - 1) last = tiles_n - 1;
+            cnt = (int)last + 1;
+        } else {
+            const int64_t f64 = (r_lo / rpc) / OZ_BN;
+            f = (int)(f64 < tiles_n ? f64 : tiles_n);
+            cnt = tiles_n - f;
+        }
+        cum[tm] = total;
+        first[tm] = f;
+        total += cnt;
+    }
+    cum[tiles_m] = total;
+}
+
+int64_t oz_tri_tiles_count(int tiles_m, int tiles_n, int64_t row_tile, int64_t m, int rpc, int out_tri)
+{
+    int64_t total = 0;
+    for (int tm = 0; tm < tiles_m; ++tm) {
+        const int64_t r_lo = (int64_t)tm * row_tile;
+        const int64_t r_hi = (((int64_t)(tm + 1) * row_tile < m) ? (int64_t)(tm + 1) * row_tile : m) - 1;
+        if (out_tri == 1) {
+            int64_t last = (r_hi / rpc) / OZ_BN;
+            if (last > tiles_n - 1) last = tiles_n - 1;
+            total += last + 1;
+        } else {
+            const int64_t f = (r_lo / rpc) / OZ_BN;
+            total += tiles_n - (f < tiles_n ? f : tiles_n);
+        }
+    }
+    return total;
+}
+
+// The IEEE fallback's diagonal block: C := D + beta C on the stored triangle
+// of the rows x cols block at (r0, c0) (row i, column j stored when i / rpc
+// >= j, lower, or <= j, upper); runs only when a split raised the flag.
+__global__ void __launch_bounds__(256) oz_tri_merge_gated_kernel(int64_t rows, int64_t cols, int64_t r0, int64_t c0,
+                                                                 int lower, int rpc, const double* __restrict__ d,
+                                                                 double beta, double* __restrict__ c, int64_t rs_c,
+                                                                 int64_t cs_c, const int* __restrict__ gate)
+{
+    if (!*gate) return;
+    const int64_t total = rows * cols;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = e / rows, i = e - j * rows;
+        const int64_t ci = (r0 + i) / rpc, cj = c0 + j;
+        if (lower ? ci < cj : ci > cj) continue;
+        double* cij = c + (r0 + i) * rs_c + cj * cs_c;
+        *cij = (beta == 0.0) ? d[e] : __fma_rn(beta, *cij, d[e]);
+    }
+}
+
 // Phase 3: C := alpha op(A) op(B) + beta C for rows [r0, r0 + rows) of the
 // prepared op(A) (r0 a multiple of the row tile) and a prepared op(B); C is
 // that rows x n block; the slice GEMM, the recombination and the gated IEEE
@@ -1859,6 +1948,8 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
 {
     if (r0 < 0 || rows <= 0 || r0 + rows > A->m || r0 % A->row_tile)
         return set_error(GB_ERR_ARG, "ozaki", "row block not aligned to the slice GEMM tile");
+    if (A->out_tri && (r0 != 0 || rows != A->m || A->tri || A->out_rpc < 1))
+        return set_error(GB_ERR_ARG, "ozaki", "a triangle of C is written from the whole of op(A) only");
     const int64_t m = rows, n = B->n, k = A->k, kpad = A->kpad, npad = B->npad;
     const int64_t mpad = round_up(rows, A->row_tile);
     const int slices = A->slices;
@@ -1871,7 +1962,8 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
     p.kb_total = kb_total;
     p.tiles_m = (int)(mpad / A->row_tile);
     p.tiles_n = (int)(npad / OZ_BN);
-    const int64_t tiles = (int64_t)p.tiles_m * p.tiles_n;
+    const int64_t tiles = A->out_tri ? oz_tri_tiles_count(p.tiles_m, p.tiles_n, A->row_tile, m, A->out_rpc, A->out_tri)
+                                     : (int64_t)p.tiles_m * p.tiles_n;
     int planes_total = 0;
     int64_t items = 0;
     for (int L = 0; L < slices; ++L) {  // heaviest level (most pairs) first
@@ -1900,8 +1992,18 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
     p.tri_row0 = r0;
 
     const size_t bytes_pl = (size_t)planes_total * npad * mpad * 4;
-    int32_t* planes = static_cast<int32_t*>(dev_alloc(bytes_pl + 1024, s));
+    const size_t bytes_tab = A->out_tri ? sizeof(int) * (size_t)(2 * p.tiles_m + 1) : 0;
+    int32_t* planes = static_cast<int32_t*>(dev_alloc(bytes_pl + 1024 + bytes_tab, s));
     if (!planes) return GB_ERR_NOMEM;
+    if (A->out_tri) {
+        int* tab = reinterpret_cast<int*>(reinterpret_cast<uint8_t*>(planes) + bytes_pl + 1024);
+        p.out_tri = A->out_tri;
+        p.tiles_valid = (int)tiles;
+        p.tile_cum = tab;
+        p.tile_first = tab + p.tiles_m + 1;
+        oz_tri_tiles_kernel<<<1, 1, 0, s>>>(p.tiles_m, p.tiles_n, A->row_tile, m, A->out_rpc, A->out_tri, tab,
+                                            tab + p.tiles_m + 1);
+    }
     p.planes = planes;
     p.status = device_status_word();
     p.skip = A->nonfinite;
@@ -1958,6 +2060,8 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
         r.rs_c = rs_c;
         r.cs_c = cs_c;
         r.skip = A->nonfinite;
+        r.out_tri = A->out_tri;
+        r.out_rpc = A->out_rpc;
         for (int L = 0; L < slices; ++L) r.lv[L] = p.lv[L];
         const int64_t total = ((m + 3) / 4) * n;
         int64_t blocks = (total + 255) / 256;
@@ -1967,8 +2071,39 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
     }
     if ((rc = check_cuda(cudaGetLastError(), "oz_recombine"))) return bail(rc);
     // IEEE path for non-finite operands: runs only when a split raised the flag
-    rc = dgemm_native_gated(m, n, k, alpha, A->a + r0 * A->ars, A->ars, A->acs, B->b, B->brs, B->bcs, beta, c, rs_c,
-                            cs_c, A->nonfinite, s);
+    if (!A->out_tri) {
+        rc = dgemm_native_gated(m, n, k, alpha, A->a + r0 * A->ars, A->ars, A->acs, B->b, B->brs, B->bcs, beta, c,
+                                rs_c, cs_c, A->nonfinite, s);
+    } else {
+        // only the stored triangle: per 1024-column block, the rows strictly
+        // inside it in place, the diagonal block through scratch and a merge
+        const int64_t rpc = A->out_rpc, W = 1024;
+        const int64_t wmax = (n < W) ? n : W;
+        double* d = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(rpc * wmax * wmax), s));
+        if (!d) return bail(GB_ERR_NOMEM);
+        const bool lower = (A->out_tri == 1);
+        for (int64_t j0 = 0; j0 < n && !rc; j0 += W) {
+            const int64_t w = (n - j0 < W) ? n - j0 : W;
+            const int64_t d0 = rpc * j0, dr = (rpc * (j0 + w) < m ? rpc * (j0 + w) : m) - d0;
+            const int64_t pr0 = lower ? d0 + dr : 0, prows = lower ? m - (d0 + dr) : d0;
+            const double* bj = B->b + j0 * B->bcs;
+            if (prows > 0)
+                rc = dgemm_native_gated(prows, w, k, alpha, A->a + pr0 * A->ars, A->ars, A->acs, bj, B->brs, B->bcs,
+                                        beta, c + pr0 * rs_c + j0 * cs_c, rs_c, cs_c, A->nonfinite, s);
+            if (!rc && dr > 0) {
+                rc = dgemm_native_gated(dr, w, k, alpha, A->a + d0 * A->ars, A->ars, A->acs, bj, B->brs, B->bcs, 0.0,
+                                        d, 1, dr, A->nonfinite, s);
+                if (!rc) {
+                    int64_t blocks = (dr * w + 255) / 256;
+                    if (blocks > 4096) blocks = 4096;
+                    oz_tri_merge_gated_kernel<<<(unsigned)blocks, 256, 0, s>>>(dr, w, d0, j0, lower ? 1 : 0, (int)rpc,
+                                                                               d, beta, c, rs_c, cs_c, A->nonfinite);
+                    rc = check_cuda(cudaGetLastError(), "ozaki triangle fallback");
+                }
+            }
+        }
+        dev_free(d, s);
+    }
     dev_free(planes, s);
     return rc;
 }

@@ -307,3 +307,26 @@ def test_device_entry_points(gblib):
                   <= (2 * 8 * (2 * k + 4) * U64 * (oa @ oa.T))[~np.tri(m, k=-1, dtype=bool)])
     assert gblib.gb_zherk_dev(po.LOWER, 0, -1, k, 1.0, p(ad), 1, m, 0.0, p(cd), 1, m, None) != 0
     _lib.load().gb_clear_last_error()
+
+
+def test_zherk_ozaki_nonfinite_keeps_other_triangle():
+    m, k = 700, 90
+    a = _cplx((m, k), 45)
+    a[300, 10] = np.nan
+    c0 = _cplx((m, m), 46)
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 8)
+    c = c0.copy(order="F")
+    blas.zherk("L", "N", m, k, 1.0, a, m, 1.0, c, m)
+    t = _tri(True, m)
+    assert np.array_equal(c[~t], c0[~t])
+    assert np.all(c.diagonal().imag == 0)
+    assert np.isnan(c[300, 0].real) and np.isnan(c[699, 300].real)
+    ok = np.ones(m, bool)
+    ok[300] = False
+    sub = np.ix_(ok, ok)
+    ref = c0.copy(order="F")
+    po.zherk(po.LOWER, 0, 1.0, a, 1.0, ref)
+    oa = np.abs(np.nan_to_num(a))
+    bound = 8 * (k + 4) * U64 * ((oa @ oa.T) + np.abs(c0))
+    d = np.abs(c - ref)[sub][t[sub]]
+    assert np.all(d <= bound[sub][t[sub]])

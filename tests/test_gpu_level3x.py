@@ -253,3 +253,26 @@ def test_dtrmm_ozaki_bit_identical_to_model(side, uplo, trans, diag):
         po.ozaki_dgemm(0, 0, -0.75, np.asfortranarray(t.T), np.asfortranarray(b0.T), 0.0, mt, 7)
         model = mt.T
     assert np.array_equal(b, model)
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_dsyrk_ozaki_nonfinite_keeps_other_triangle(uplo):
+    # the precision form writes C's triangle from one product; with an Inf in
+    # A the gated IEEE fallback takes over, still on the triangle only
+    m, k = 1300, 200
+    a = po.uniform((m, k), 43)
+    a[700, 50] = np.inf
+    c0 = po.uniform((m, m), 44)
+    blas.set_dgemm_mode(blas.DGEMM_NATIVE, 8)
+    nat = np.asfortranarray(c0.copy())
+    blas.dsyrk(uplo, "N", m, k, 1.5, a, m, 0.5, nat, m)
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 8)
+    c = np.asfortranarray(c0.copy())
+    blas.dsyrk(uplo, "N", m, k, 1.5, a, m, 0.5, c, m)
+    t = np.tril(np.ones((m, m), bool)) if uplo == "L" else np.triu(np.ones((m, m), bool))
+    assert np.array_equal(c[~t], c0[~t])
+    assert np.array_equal(np.isfinite(c), np.isfinite(nat))
+    f = np.isfinite(nat) & t
+    oa = np.abs(np.where(np.isfinite(a), a, 0.0))
+    bound = 8 * (k + 2) * H.EPS * (1.5 * (oa @ oa.T) + 0.5 * np.abs(c0))
+    assert np.all(np.abs(c - nat)[f] <= bound[f])
