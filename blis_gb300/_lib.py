@@ -110,6 +110,10 @@ def load(path=None):
                                _vp]
     _sig(L, "gb_zhemm_dev", C.c_int, zhemm_d)
     _sig(L, "gb_zsymm_dev", C.c_int, zhemm_d)
+    _sig(L, "bli_dtrmm3", None, [C.c_int] * 5 + [_i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _i64,
+                                                  _i64])
+    _sig(L, "gb_dtrmm3_dev", C.c_int, [C.c_int] * 5 + [_i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _d, _vp,
+                                                         _i64, _i64, _vp])
     _sig(L, "gb_dsyr2k_dev", C.c_int, [C.c_int, C.c_int, C.c_int, _i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64,
                                        _d, _vp, _i64, _i64, _vp])
     _sig(L, "dscal_", None, [_ip, _dp, _vp, _ip])

@@ -312,6 +312,13 @@ def bli_zhemm(side, uplo, conja, transb, alpha, a, b, beta, c, herm=True):
     fn(side, uplo, conja, transb, m, n, _p(al), _p(a), *_st(a), _p(b), *_st(b), _p(be), _p(c), *_st(c))
 
 
+def bli_dtrmm3(side, uplo, transa, diag, transb, alpha, a, b, beta, c):
+    """C := beta C + alpha op(A) op(B) (LEFT) or beta C + alpha op(B) op(A) (RIGHT), A triangular."""
+    m, n = c.shape
+    _lib.load().bli_dtrmm3(side, uplo, transa, diag, transb, m, n, _d(alpha), _p(a), *_st(a), _p(b), *_st(b),
+                           _d(beta), _p(c), *_st(c))
+
+
 def bli_dsyr2k(uplo, transa, transb, alpha, a, b, beta, c):
     m = c.shape[0]
     k = a.shape[0] if transa & TRANSPOSE else a.shape[1]

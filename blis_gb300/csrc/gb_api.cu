@@ -784,6 +784,33 @@ int chemm_host(int side, int uplo, int herm, int conja, int transb, int64_t m, i
     return finish(s, where);
 }
 
+int trmm3_host(int side, int uplo, int transa, int diag, int transb, int64_t m, int64_t n, double alpha,
+               const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta,
+               double* c, int64_t rs_c, int64_t cs_c, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const int64_t na = (side == GB_LEFT) ? m : n;
+    const bool tb = GB_IS_TRANS(transb);
+    Staged& C = bufs.next();
+    if ((rc = stage_in(c, m, n, rs_c, cs_c, 8, beta != 0.0, &C, s))) return rc;
+    Staged& A = bufs.next();
+    Staged& B = bufs.next();
+    if (alpha != 0.0) {
+        if ((rc = stage_in(a, na, na, rs_a, cs_a, 8, true, &A, s))) return rc;
+        if ((rc = stage_in(b, tb ? n : m, tb ? m : n, rs_b, cs_b, 8, true, &B, s))) return rc;
+    }
+    if ((rc = dtrmm3_dev(side, uplo, transa, diag, transb, m, n, alpha, reinterpret_cast<const double*>(A.origin), A.rs,
+                         A.cs, reinterpret_cast<const double*>(B.origin), B.rs, B.cs, beta,
+                         reinterpret_cast<double*>(C.origin), C.rs, C.cs, level3_slices(), s)))
+        return rc;
+    if ((rc = stage_out(c, m, n, rs_c, cs_c, 8, C, s))) return rc;
+    return finish(s, where);
+}
+
 int syr2k_host(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha, const double* a, int64_t rs_a,
                int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c,
                int64_t cs_c, const char* where)
@@ -1569,6 +1596,14 @@ void bli_csymm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t tran
                       &b->real, rs_b, cs_b, &beta->real, &c->real, rs_c, cs_c, "bli_csymm");
 }
 
+void bli_dtrmm3(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_trans_t transb, gb_dim_t m,
+                gb_dim_t n, const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    trmm3_host(side, uploa, transa, diaga, transb, m, n, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, *beta, c, rs_c, cs_c,
+               "bli_dtrmm3");
+}
+
 void bli_dsyr2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k, const double* alpha,
                 const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b, gb_inc_t rs_b, gb_inc_t cs_b,
                 const double* beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c)
@@ -1899,6 +1934,17 @@ int gb_zsymm_dev(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t tr
     return gb::chemm_dev<double>(side, uploa, 0, conja == GB_CONJUGATE, transb, m, n, &alpha.real, &a->real, rs_a,
                                  cs_a, &b->real, rs_b, cs_b, &beta.real, &c->real, rs_c, cs_c, gb::level3_slices(),
                                  pick_stream(stream));
+}
+
+int gb_dtrmm3_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_trans_t transb, gb_dim_t m,
+                  gb_dim_t n, double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                  gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_dtrmm3_dev", "negative dimension");
+    return gb::dtrmm3_dev(side, uploa, transa, diaga, transb, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c,
+                          cs_c, gb::level3_slices(), pick_stream(stream));
 }
 
 int gb_dsyr2k_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k, double alpha,

@@ -131,6 +131,9 @@ int dsymm_dev(int side, int uplo, int64_t m, int64_t n, double alpha, const doub
 int dgemmt_dev(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha, const double* a,
                int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c,
                int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s);
+int dtrmm3_dev(int side, int uplo, int transa, int diag, int transb, int64_t m, int64_t n, double alpha,
+               const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta,
+               double* c, int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s);
 int dsyr2k_dev(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha, const double* a, int64_t rs_a, int64_t cs_a,
                const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c,
                int slices, cudaStream_t s);

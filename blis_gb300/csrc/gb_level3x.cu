@@ -353,6 +353,59 @@ int dtrmm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     return rc;
 }
 
+// trmm3: C := beta C + alpha op(A) op(B) (left, A m x m) or beta C + alpha
+// op(B) op(A) (right, A n x n), A triangular, C m x n; B is not written
+// (bli_trmm3_ex, frame/3/bli_l3_oapi_ex.c:523-608; alpha == 0 scales C only,
+// frame/3/bli_l3_util.c:41-65).  tri(op(A)) is materialised with zeros and
+// multiplied as a gemm: in the precision form one Ozaki product whose slice
+// GEMM skips the all-zero k blocks (as trmm), natively the dense DMMA gemm.
+int dtrmm3_dev(int side, int uplo, int transa, int diag, int transb, int64_t m, int64_t n, double alpha,
+               const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta,
+               double* c, int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s)
+{
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    // op(B) (i, j) at b[i*brs + j*bcs]
+    int64_t brs = GB_IS_TRANS(transb) ? cs_b : rs_b, bcs = GB_IS_TRANS(transb) ? rs_b : cs_b;
+    int64_t crs = rs_c, ccs = cs_c, mm = m, nn = n;
+    bool trans = GB_IS_TRANS(transa);
+    if (side == GB_RIGHT) {
+        // C^T = beta C^T + alpha op(A)^T op(B)^T: the left form on the transposes
+        const int64_t t0 = brs;
+        brs = bcs;
+        bcs = t0;
+        crs = cs_c;
+        ccs = rs_c;
+        mm = n;
+        nn = m;
+        trans = !trans;
+    }
+    if (alpha == 0.0) return scal_matrix(mm, nn, beta, c, crs, ccs, s);  // A and B are not read
+    const int64_t ars = trans ? cs_a : rs_a, acs = trans ? rs_a : cs_a;
+    const bool lower = (uplo == GB_LOWER) != trans;
+    double* full = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(mm * mm), s));
+    if (!full) return GB_ERR_NOMEM;
+    int rc;
+    {
+        LaunchScope ls("trmm_materialize", s);
+        tri_materialize_kernel<<<grid_for(mm * mm), 256, 0, s>>>(mm, lower ? 1 : 0, diag == GB_UNIT_DIAG, a, ars, acs,
+                                                                 full);
+        rc = check_cuda(cudaGetLastError(), "trmm3 materialize");
+    }
+    if (!rc && slices > 0) {
+        OzA prep;
+        rc = ozaki_prepare_a(mm, mm, full, 1, mm, slices, s, &prep);
+        if (!rc) {
+            prep.tri = lower ? 1 : 2;
+            rc = ozaki_multiply(&prep, nn, b, brs, bcs, alpha, beta, c, crs, ccs, s);
+            ozaki_release_a(&prep, s);
+        }
+    } else if (!rc) {
+        rc = dgemm_native(mm, nn, mm, alpha, full, 1, mm, b, brs, bcs, beta, c, crs, ccs, s);
+    }
+    dev_free(full, s);
+    return rc;
+}
+
 int dsymm_dev(int side, int uplo, int64_t m, int64_t n, double alpha, const double* a, int64_t rs_a,
               int64_t cs_a, const double* b, int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c,
               int64_t cs_c, int slices, cudaStream_t s)

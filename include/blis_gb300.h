@@ -352,6 +352,13 @@ void bli_csymm(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t tran
                const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
                const gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, const gb_scomplex* beta, gb_scomplex* c,
                gb_inc_t rs_c, gb_inc_t cs_c);
+/* replaces bli_dtrmm3 (frame/3/bli_l3_tapi_ex.c; prototype frame/3/bli_l3_tapi_ex.h:170-192; object
+   form frame/3/bli_l3_oapi_ex.c:523-608): C := beta C + alpha op(A) op(B) (left) or
+   beta C + alpha op(B) op(A) (right), A triangular, B not written */
+void bli_dtrmm3(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_trans_t transb,
+                gb_dim_t m, gb_dim_t n, const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                const double* b, gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c, gb_inc_t rs_c,
+                gb_inc_t cs_c);
 void bli_dsyr2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
                 const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
                 gb_inc_t rs_b, gb_inc_t cs_b, const double* beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c);
@@ -507,7 +514,7 @@ int gb_ztrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
                  gb_dim_t n, gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
                  gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
 
-/* Device-pointer forms of zherk, zher2k, zhemm, zsymm and dsyr2k
+/* Device-pointer forms of zherk, zher2k, zhemm, zsymm, dtrmm3 and dsyr2k
    (asynchronous on the stream). */
 int gb_zherk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, double alpha,
                  const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, double beta, gb_dcomplex* c,
@@ -524,6 +531,10 @@ int gb_zsymm_dev(gb_side_t side, gb_uplo_t uploa, gb_conj_t conja, gb_trans_t tr
                  gb_dim_t n, gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
                  const gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, gb_dcomplex beta, gb_dcomplex* c,
                  gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+int gb_dtrmm3_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_trans_t transb,
+                  gb_dim_t m, gb_dim_t n, double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                  const double* b, gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c,
+                  gb_inc_t cs_c, void* stream);
 int gb_dsyr2k_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
                   double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
                   gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c,

@@ -40,6 +40,7 @@
  *         imaginary parts of C's diagonal set to zero
  *   hemm, complex symm  :349-520 on the materialised A, then zgemm
  *   syr2k :267-292, two gemmt calls (the second with beta = 1)
+ *   trmm3 :523-608, the dense tri(A) through the gemm (B not written)
  *   dotv  ref_kernels/1/bli_dotv_ref.c:37-121 (n == 0 gives rho = 0)
  * Not in the reference: the double-double evaluator (error oracle) and the
  * Ozaki split-product model (Ozaki, Ogita, Oishi & Rump 2012; integer-slice
@@ -931,4 +932,34 @@ void orc_dsyr2k(int uplo, int transa, int transb, int64_t m, int64_t k, double a
                alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c, cs_c, nthreads);
     orc_dgemmt(uplo, tb ? ORC_TRANSPOSE : ORC_NO_TRANSPOSE, ta ? ORC_NO_TRANSPOSE : ORC_TRANSPOSE, m, k,
                alpha, b, rs_b, cs_b, a, rs_a, cs_a, 1.0, c, rs_c, cs_c, nthreads);
+}
+
+/* trmm3 (frame/3/bli_l3_oapi_ex.c:523-608): C := beta C + alpha op(A) op(B)
+   (left) or beta C + alpha op(B) op(A) (right) on the dense tri(A) through
+   the gemm below; alpha == 0 scales C only (frame/3/bli_l3_util.c:41-65). */
+void orc_dtrmm3(int side, int uplo, int transa, int diag, int transb, int64_t m, int64_t n,
+                double alpha, const double* a, int64_t rs_a, int64_t cs_a, const double* b,
+                int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c,
+                int nthreads)
+{
+    if (m <= 0 || n <= 0) return;
+    const int64_t na = (side == ORC_LEFT) ? m : n;
+    if (alpha == 0.0) {
+        for (int64_t j = 0; j < n; ++j)
+            for (int64_t i = 0; i < m; ++i)
+                c[i * rs_c + j * cs_c] = (beta == 0.0) ? 0.0 : beta * c[i * rs_c + j * cs_c];
+        return;
+    }
+    double* t = (double*)calloc((size_t)(na * na), sizeof(double));
+    for (int64_t j = 0; j < na; ++j)
+        for (int64_t i = 0; i < na; ++i) {
+            const int in = (uplo == ORC_LOWER) ? (i >= j) : (i <= j);
+            if (i == j) t[i + j * na] = (diag == ORC_UNIT_DIAG) ? 1.0 : a[i * rs_a + j * cs_a];
+            else if (in) t[i + j * na] = a[i * rs_a + j * cs_a];
+        }
+    if (side == ORC_LEFT)
+        orc_dgemm(transa, transb, m, n, m, alpha, t, 1, na, b, rs_b, cs_b, beta, c, rs_c, cs_c, nthreads);
+    else
+        orc_dgemm(transb, transa, m, n, n, alpha, b, rs_b, cs_b, t, 1, na, beta, c, rs_c, cs_c, nthreads);
+    free(t);
 }

@@ -86,6 +86,10 @@ void orc_zher2k(int uplo, int transa, int transb, int64_t m, int64_t k, const do
 void orc_zhemm(int side, int uplo, int herm, int conja, int transb, int64_t m, int64_t n,
                const double* alpha, const double* a, int64_t rs_a, int64_t cs_a, const double* b,
                int64_t rs_b, int64_t cs_b, const double* beta, double* c, int64_t rs_c, int64_t cs_c);
+void orc_dtrmm3(int side, int uplo, int transa, int diag, int transb, int64_t m, int64_t n,
+                double alpha, const double* a, int64_t rs_a, int64_t cs_a, const double* b,
+                int64_t rs_b, int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c,
+                int nthreads);
 void orc_dsyr2k(int uplo, int transa, int transb, int64_t m, int64_t k, double alpha,
                 const double* a, int64_t rs_a, int64_t cs_a, const double* b, int64_t rs_b,
                 int64_t cs_b, double beta, double* c, int64_t rs_c, int64_t cs_c, int nthreads);

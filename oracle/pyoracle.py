@@ -56,6 +56,8 @@ def lib():
                                  C.c_void_p, _i64, _i64, C.c_double, C.c_void_p, _i64, _i64]
         L.orc_zhemm.argtypes = [C.c_int] * 5 + [_i64, _i64, C.c_void_p, C.c_void_p, _i64, _i64, C.c_void_p, _i64,
                                                 _i64, C.c_void_p, C.c_void_p, _i64, _i64]
+        L.orc_dtrmm3.argtypes = [C.c_int] * 5 + [_i64, _i64, C.c_double, C.c_void_p, _i64, _i64, C.c_void_p, _i64,
+                                                 _i64, C.c_double, C.c_void_p, _i64, _i64, C.c_int]
         L.orc_dsyr2k.argtypes = [C.c_int] * 3 + [_i64, _i64, C.c_double, C.c_void_p, _i64, _i64, C.c_void_p,
                                                  _i64, _i64, C.c_double, C.c_void_p, _i64, _i64, C.c_int]
         L.orc_dscalv.argtypes = [_i64, C.c_double, C.c_void_p, _i64]
@@ -215,6 +217,13 @@ def zhemm(side, uplo, herm, conja, transb, alpha, a, b, beta, c):
     be = np.array([beta], dtype=np.complex128)
     lib().orc_zhemm(side, uplo, herm, conja, transb, m, n, _p(al), _p(a), *_zst(a), _p(b), *_zst(b), _p(be),
                     _p(c), *_zst(c))
+    return c
+
+
+def dtrmm3(side, uplo, transa, diag, transb, alpha, a, b, beta, c, nthreads=None):
+    m, n = c.shape
+    lib().orc_dtrmm3(side, uplo, transa, diag, transb, m, n, alpha, _p(a), *_strides(a), _p(b), *_strides(b), beta,
+                     _p(c), *_strides(c), nthreads or nthreads_default())
     return c
 
 

@@ -276,3 +276,35 @@ def test_dsyrk_ozaki_nonfinite_keeps_other_triangle(uplo):
     oa = np.abs(np.where(np.isfinite(a), a, 0.0))
     bound = 8 * (k + 2) * H.EPS * (1.5 * (oa @ oa.T) + 0.5 * np.abs(c0))
     assert np.all(np.abs(c - nat)[f] <= bound[f])
+
+
+@pytest.mark.parametrize("side,uplo,transa,diag,transb", [("L", "L", "N", "N", "N"), ("R", "U", "T", "U", "T"),
+                                                          ("L", "U", "T", "N", "T"), ("R", "L", "N", "U", "N")])
+@pytest.mark.parametrize("mode", ["native", "ozaki"])
+def test_dtrmm3_vs_oracle(side, uplo, transa, diag, transb, mode):
+    m, n = 700, 530
+    na = m if side == "L" else n
+    a = po.uniform((na, na), 47)
+    b = po.uniform((n, m) if transb == "T" else (m, n), 48)
+    c0 = po.uniform((m, n), 49)
+    code = {"N": blas.NO_TRANSPOSE, "T": blas.TRANSPOSE}
+    sd = blas.LEFT if side == "L" else blas.RIGHT
+    ul = blas.LOWER if uplo == "L" else blas.UPPER
+    dg = blas.UNIT_DIAG if diag == "U" else blas.NONUNIT_DIAG
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI if mode == "ozaki" else blas.DGEMM_NATIVE, 8)
+    try:
+        c = np.asfortranarray(c0.copy())
+        b_before = b.copy()
+        blas.bli_dtrmm3(sd, ul, code[transa], dg, code[transb], 1.5, a, b, -0.5, c)
+    finally:
+        blas.set_dgemm_mode(blas.DGEMM_NATIVE, 8)
+    assert np.array_equal(b, b_before)  # B is not written
+    ref = np.asfortranarray(c0.copy())
+    po.dtrmm3(po.LEFT if side == "L" else po.RIGHT, po.LOWER if uplo == "L" else po.UPPER,
+              po.TRANSPOSE if transa == "T" else po.NO_TRANSPOSE, po.UNIT_DIAG if diag == "U" else po.NONUNIT_DIAG,
+              po.TRANSPOSE if transb == "T" else po.NO_TRANSPOSE, 1.5, a, b, -0.5, ref)
+    t = np.abs(_tri(a, uplo, diag))
+    t = t.T if transa == "T" else t
+    ob = np.abs(b.T if transb == "T" else b)
+    g = 1.5 * (t @ ob if side == "L" else ob @ t) + 0.5 * np.abs(c0)
+    assert np.all(np.abs(c - ref) <= 4 * (na + 2) * H.EPS * g)

@@ -104,3 +104,27 @@ def test_oracle_dsyr2k_definition(uplo, ta, tb):
     t = _tri(uplo, m)
     assert np.allclose(c[t], full[t], rtol=0, atol=1e-13)
     assert np.array_equal(c[~t], c0[~t])
+
+
+@pytest.mark.parametrize("side", [po.LEFT, po.RIGHT])
+@pytest.mark.parametrize("uplo,ta,diag", [(po.LOWER, po.NO_TRANSPOSE, po.NONUNIT_DIAG),
+                                          (po.UPPER, po.TRANSPOSE, po.UNIT_DIAG)])
+@pytest.mark.parametrize("tb", [po.NO_TRANSPOSE, po.TRANSPOSE])
+def test_oracle_dtrmm3_definition(side, uplo, ta, diag, tb):
+    m, n = 12, 9
+    na = m if side == po.LEFT else n
+    a = po.uniform((na, na), 12)
+    b = po.uniform((n, m) if tb else (m, n), 13)
+    c0 = po.uniform((m, n), 14)
+    t = np.tril(a) if uplo == po.LOWER else np.triu(a)
+    if diag == po.UNIT_DIAG:
+        t = t - np.diag(np.diag(t)) + np.eye(na)
+    t = t.T if ta else t
+    ob = b.T if tb else b
+    c = c0.copy(order="F")
+    po.dtrmm3(side, uplo, ta, diag, tb, -0.5, a, b, 2.0, c, nthreads=1)
+    ref = -0.5 * (t @ ob if side == po.LEFT else ob @ t) + 2.0 * c0
+    assert np.allclose(c, ref, rtol=0, atol=1e-13)
+    c = np.full((m, n), np.nan, order="F")
+    po.dtrmm3(side, uplo, ta, diag, tb, 0.0, a, b, 0.0, c, nthreads=1)  # alpha = beta = 0: C := 0
+    assert (c == 0).all()
