@@ -14,6 +14,10 @@
 // on the native FP64 kernel or, in the precision form, on the Ozaki kernel.
 // Right-side solves are turned into left-side ones by swapping B's strides
 // and transposing A, the reduction of frame/3/bli_l3_oapi_ex.c:753-758.
+// In the precision form with at least 2048 right-hand sides the two column
+// halves recurse on two streams.  A single right-hand side (trsv, or trsm
+// with one column) is one launch of the flag-ordered kernel below instead
+// of the recursion.
 #include <stdlib.h>
 
 #include "gb_internal.h"
@@ -400,8 +404,6 @@ int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t cco
     const double* ap = t.a + r0 * t.ars + c0 * t.acs;
     const double* xp = t.b + c0 * t.brs;
     double* bp = t.b + r0 * t.brs;
-    if (t.n == 1)  // one right-hand side (trsv): a gemv, in either form
-        return dgemv_dev(GB_NO_TRANSPOSE, rcount, ccount, -1.0, ap, t.ars, t.acs, xp, t.brs, 1.0, bp, t.brs, t.s);
     if (t.slices > 0 && (double)rcount * (double)ccount * (double)t.n >= trsm_ozaki_min_fma())
         return dgemm_ozaki(rcount, t.n, ccount, -1.0, ap, t.ars, t.acs, xp, t.brs, t.bcs, 1.0, bp,
                            t.brs, t.bcs, t.slices, t.s);
