@@ -21,11 +21,15 @@ library's seeded generator.  A "step" is one full DGEMM.
   roofline   the dominant kernel (ozaki_slice_gemm): slice-product flops
              (s(s+1)/2 * 2mnk) per launch over its event-timed duration,
              against the measured bf16 tensor peak.
-  cpu_baseline  the CPU restatement of BLIS's five-loop DGEMM
-             (oracle/gb_oracle.c) on the host cores, on a column sample.
+  cpu_baseline  BLIS's own DGEMM (the reference compiled from its sources
+             by oracle/ref_blis.py, the sub-configuration BLIS picks on this
+             host, all host cores) on a column sample of the workload;
+             cpu_baseline_port is the oracle's C restatement of the five-loop
+             DGEMM on the same kind of sample, for comparison.
 
-`--impl reference` times that CPU implementation alone on the same
-workload (a column sample per step) and prints the reference line.
+`--impl reference` times BLIS's own DGEMM alone on the same workload (a
+column sample per step) and prints the reference line (the restatement when
+the reference build is missing, which the line's cpu_baseline.kind says).
 Multi-GPU: the path is replicated (one independent DGEMM per rank, no
 collective); `value` sums the ranks' flops over the slowest rank's time.
 """
@@ -61,7 +65,7 @@ def parse():
     p.add_argument("--slices", type=int, default=0,
                    help="slice count of the timed form; 0 = the smallest count of the 3..8 sweep whose "
                         "max componentwise error is at most native FP64's")
-    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=0, help="end-to-end steps (0: --steps)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     return p.parse_args()
 
@@ -137,28 +141,53 @@ def dist_setup(args):
     return ws, rank, local
 
 
-def cpu_dgemm_sample(n, seconds, threads, seed=SEED_A):
-    """Times the CPU five-loop DGEMM on an n x cols x n column sample sized
-    for about `seconds` of work; returns (TFLOP/s, description)."""
+def _blis_ref():
+    """ctypes handle of the reference BLIS build, or None when it is not built here."""
+    try:
+        from oracle import blis_ctypes as bc
+        if bc.available():
+            bc.lib()
+            return bc
+    except OSError:
+        pass
+    return None
+
+
+def cpu_dgemm_sample(n, seconds, threads, seed=SEED_A, use_blis=True):
+    """Times a CPU DGEMM on an n x cols x n column sample sized for about `seconds` of
+    work: BLIS's own bli_dgemm when the reference build is present (kind "reference"),
+    else the oracle's restatement (kind "port").  Returns (TFLOP/s, kind, description, s)."""
     import numpy as np
     from oracle import pyoracle as po
+    bc = _blis_ref() if use_blis else None
+    if bc is not None:
+        bc.set_threads(threads)
+
+        def gemm(a, b, c):
+            bc.dgemm(0, 0, 1.0, a, b, 0.0, c)
+        kind, what = "reference", "BLIS bli_dgemm (%s sub-configuration, pthreads)" % bc.arch_name()
+    else:
+        def gemm(a, b, c):
+            po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+        kind, what = "port", "five-loop C restatement of bli_gemm"
     a = po.expspread((n, n), seed, EMIN, EMAX)
     cols = 64
     b = po.expspread((n, cols), seed + 1, EMIN, EMAX)
     c = np.zeros((n, cols), order="F")
+    gemm(a, b, c)  # warm-up (thread pool, packing buffers)
     t0 = time.perf_counter()
-    po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+    gemm(a, b, c)
     dt = time.perf_counter() - t0
     rate = 2.0 * n * n * cols / dt
     cols2 = int(max(64, min(n, rate * seconds / (2.0 * n * n)))) // 64 * 64
     b = po.expspread((n, cols2), seed + 1, EMIN, EMAX)
     c = np.zeros((n, cols2), order="F")
     t0 = time.perf_counter()
-    po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+    gemm(a, b, c)
     dt = time.perf_counter() - t0
     tf = 2.0 * n * n * cols2 / dt / 1e12
-    return tf, "m=k=%d, n=%d column sample of the %d^3 DGEMM (%.1f s), five-loop C restatement, %d threads" % (
-        n, cols2, n, dt, threads), dt
+    return tf, kind, "m=k=%d, n=%d column sample of the %d^3 DGEMM (%.1f s), %s, %d threads" % (
+        n, cols2, n, dt, what, threads), dt
 
 
 def run_reference(args):
@@ -169,27 +198,39 @@ def run_reference(args):
     n = args.size
     import numpy as np
     from oracle import pyoracle as po
+    bc = _blis_ref()
+    if bc is not None:
+        bc.set_threads(threads)
+
+        def gemm(a, b, c):
+            bc.dgemm(0, 0, 1.0, a, b, 0.0, c)
+        kind, what = "reference", "BLIS bli_dgemm (%s sub-configuration, pthreads)" % bc.arch_name()
+    else:
+        def gemm(a, b, c):
+            po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+        kind, what = "port", "five-loop C restatement of bli_gemm (reference build missing)"
     a = po.expspread((n, n), SEED_A, EMIN, EMAX)
     cols = 64
     b = po.expspread((n, cols), SEED_B, EMIN, EMAX)
     c = np.zeros((n, cols), order="F")
+    gemm(a, b, c)
     # per-step sample sized so that warm-up + steps stay within a few minutes
     t0 = time.perf_counter()
-    po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+    gemm(a, b, c)
     rate = 2.0 * n * n * cols / (time.perf_counter() - t0)
     budget = 120.0 / max(1, args.steps + args.warmup)
     cols = int(max(64, min(n, rate * budget / (2.0 * n * n)))) // 64 * 64
     b = po.expspread((n, cols), SEED_B, EMIN, EMAX)
     c = np.zeros((n, cols), order="F")
     for _ in range(args.warmup):
-        po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+        gemm(a, b, c)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        po.dgemm(0, 0, 1.0, a, b, 0.0, c, nthreads=threads)
+        gemm(a, b, c)
     dt = (time.perf_counter() - t0) / max(1, args.steps)
     tf = 2.0 * n * n * cols / dt / 1e12
-    sample = "m=k=%d, n=%d column sample per step of the %d^3 DGEMM, five-loop C restatement of bli_gemm" % (
-        n, cols, n)
+    sample = "m=k=%d, n=%d column sample per step of the %d^3 DGEMM, %s, %d threads" % (
+        n, cols, n, what, threads)
     line = {
         "impl": "reference", "metric": "Emulated vs native DGEMM TFLOP/s on 1 GB300 at FP64-level error; % of roofline",
         "value": tf, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -197,10 +238,32 @@ def run_reference(args):
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": "dgemm_%d_expspread" % n, "m": n, "n": n, "k": n, "e_range": [EMIN, EMAX],
                    "sample_cols": cols},
-        "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def host_link_gbs(nbytes=1 << 30, reps=3):
+    """Pinned host<->device copy bandwidth of this machine (GB/s), H2D and D2H, one
+    cudaMemcpyAsync of `nbytes` at a time on the current stream."""
+    import torch
+    h = torch.empty(nbytes // 8, dtype=torch.float64, pin_memory=True)
+    d = torch.empty(nbytes // 8, dtype=torch.float64, device="cuda")
+    h.fill_(1.0)
+    out = []
+    for direction in ("h2d", "d2h"):
+        fn = (lambda: d.copy_(h, non_blocking=True)) if direction == "h2d" else \
+             (lambda: h.copy_(d, non_blocking=True))
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        out.append(nbytes * reps / (time.perf_counter() - t0) / 1e9)
+    del h, d
+    return out
 
 
 def run_gpu(args):
@@ -311,6 +374,7 @@ def run_gpu(args):
     peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
 
     # ---------------- end to end through dgemm_ with pinned host buffers
+    h2d_gbs, d2h_gbs = host_link_gbs()
     Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
     Bh = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
     Ch = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
@@ -320,11 +384,12 @@ def run_gpu(args):
     blas.set_dgemm_mode(blas.DGEMM_OZAKI, s)
     an, bn, cn = Ah.numpy(), Bh.numpy(), Ch.numpy()
     blas.dgemm("N", "N", n, n, n, 1.0, an, n, bn, n, 0.0, cn, n)  # warm-up
+    e2e_steps = args.e2e_steps if args.e2e_steps > 0 else args.steps
     barrier()
     t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    for _ in range(e2e_steps):
         blas.dgemm("N", "N", n, n, n, 1.0, an, n, bn, n, 0.0, cn, n)
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     blas.set_dgemm_mode(blas.DGEMM_NATIVE)
     if ws > 1:
         import torch.distributed as dist
@@ -332,8 +397,13 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
     e2e_tf = flops * ws / (e2e_ms * 1e-3) / 1e12
-    # cn holds column-major C, i.e. cn[j, i] == C[i, j]
-    e2e_ok = bool(np.array_equal(cn[:64, :64], Cz[:64, :64].t().contiguous().cpu().numpy()))
+    # cn holds column-major C, i.e. cn[j, i] == C[i, j]: the whole product against the
+    # device-resident run's, bit for bit
+    Ch2 = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    Ch2.copy_(Cz.t())
+    torch.cuda.synchronize()
+    e2e_ok = bool(np.array_equal(cn, Ch2.numpy()))
+    del Ch2
 
     # ---------------- DRAM traffic of the dominant kernel: the ncu capture at 4096^3 above,
     # scaled by the slice-product units of this size, (n/4096)^3, and by the slice-product
@@ -347,7 +417,8 @@ def run_gpu(args):
         return
 
     threads = os.cpu_count() or 1
-    cpu_tf, cpu_sample, _ = cpu_dgemm_sample(min(n, 16384), args.cpu_seconds, threads)
+    cpu_tf, cpu_kind, cpu_sample, _ = cpu_dgemm_sample(min(n, 16384), args.cpu_seconds, threads)
+    port_tf, _, port_sample, _ = cpu_dgemm_sample(min(n, 16384), args.cpu_seconds / 3, threads, use_blis=False)
 
     line = {
         "metric": "Emulated vs native DGEMM TFLOP/s on 1 GB300 at FP64-level error; % of roofline",
@@ -376,15 +447,22 @@ def run_gpu(args):
             "err_sample": "4096 random entries, double-double evaluation on the device",
         },
         "e2e": {"value": e2e_tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 2 * 8 * n * n,
-                "d2h_bytes_per_step": 8 * n * n, "ms_per_step": e2e_ms, "api": "dgemm_ (C ABI), pinned host buffers",
-                "matches_device_result": e2e_ok},
+                "d2h_bytes_per_step": 8 * n * n, "ms_per_step": e2e_ms, "steps": e2e_steps,
+                "api": "dgemm_ (C ABI), pinned host buffers",
+                "matches_device_result": e2e_ok, "compared": "all of C, bit for bit",
+                "host_link_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs},
+                "copy_ms_if_serial": (2 * 8 * n * n / (h2d_gbs * 1e9) + 8 * n * n / (d2h_gbs * 1e9)) * 1e3,
+                "exposed_ms": e2e_ms - ms},
         "roofline": {"bound": "tensor", "kernel": "ozaki_slice_gemm", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "%s bf16_tflops_sustained" % peak_kind,
                      "kernel_ms": kern_ms, "algorithmic_flops_per_launch": npairs * flops,
                      "split_recombine_ms_per_step": (split_ms / max(1, args.steps)),
                      "stage_ms_per_step": stage_ms},
-        "cpu_baseline": {"value": cpu_tf, "unit": "TFLOP/s", "cores": threads, "kind": "port", "sample": cpu_sample},
+        "cpu_baseline": {"value": cpu_tf, "unit": "TFLOP/s", "cores": threads, "kind": cpu_kind,
+                         "sample": cpu_sample},
+        "cpu_baseline_port": {"value": port_tf, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+                              "sample": port_sample},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

@@ -203,13 +203,18 @@ int ozaki_host_pipelined(int transa, int64_t m, int64_t n, int64_t k, double alp
 // are split) while it runs; every (row block, column block) of C is one
 // slice GEMM and goes back as soon as it is recombined.  Only about a
 // quarter of A and of one op(B) block, and one C block, are not overlapped
-// with compute.  Rows and columns are split independently: bit-identical to
-// one call.
+// with compute.  The block products alternate between the thread's stream
+// and a second compute stream, so one block's last wave of tiles shares the
+// SMs with the next block's first (a 4096 x 4096 block is 256 tiles of
+// 256 x 256, 3.4 waves of 76 CTA pairs); the splits run on a third stream as
+// the blocks land, and each product waits only for the splits it reads.
+// Rows and columns are split independently: bit-identical to one call.
 int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double alpha, const double* a,
                             int64_t lda, const double* b, int64_t ldb, double beta, double* c, int64_t ldc,
                             int slices, int nch, const char* where)
 {
     cudaStream_t s = thread_stream(), cin = thread_copy_stream(0), cout = thread_copy_stream(1);
+    cudaStream_t sp[2] = {s, thread_aux_stream(0)}, ss = thread_aux_stream(1);
     const bool ta = GB_IS_TRANS(transa);
     // op(A) on the device: m x k column-major (ars 1, acs m), or for op(A) = A^T the stored k x m
     // column-major A (ars k, acs 1)
@@ -228,18 +233,27 @@ int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double 
     }
     rb.push_back(m);
     const int na = (int)rb.size() - 1;
-    std::vector<cudaEvent_t> ev((size_t)(na + nch + na * nch + 3));
+    // events: A blocks in, B blocks in, A blocks split, B blocks split, C blocks done, then
+    // the allocation, the two copy streams' ends, the second compute stream's end and the
+    // split stream's end
+    std::vector<cudaEvent_t> ev((size_t)(2 * na + 2 * nch + na * nch + 5));
     for (auto& e : ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     cudaEvent_t* ev_a = ev.data();
     cudaEvent_t* ev_b = ev_a + na;
-    cudaEvent_t* ev_c = ev_b + nch;
-    cudaEvent_t ev_alloc = ev_c[na * nch], ev_in_done = ev_c[na * nch + 1], ev_out_done = ev_c[na * nch + 2];
+    cudaEvent_t* ev_sa = ev_b + nch;
+    cudaEvent_t* ev_sb = ev_sa + na;
+    cudaEvent_t* ev_c = ev_sb + nch;
+    cudaEvent_t ev_alloc = ev_c[na * nch], ev_in_done = ev_c[na * nch + 1], ev_out_done = ev_c[na * nch + 2],
+                ev_aux_done = ev_c[na * nch + 3], ev_split_done = ev_c[na * nch + 4];
     auto col0 = [&](int j) { return n * j / nch; };
+    std::vector<OzB> pb((size_t)nch);
     if (!rc) {
         // copies start after the stream-ordered allocations; A's block 0 and op(B)'s block 0 first
         cudaEventRecord(ev_alloc, s);
         cudaStreamWaitEvent(cin, ev_alloc, 0);
         cudaStreamWaitEvent(cout, ev_alloc, 0);
+        cudaStreamWaitEvent(sp[1], ev_alloc, 0);
+        cudaStreamWaitEvent(ss, ev_alloc, 0);
         auto copy_a = [&](int i) {
             const int64_t r0 = rb[i], rows = rb[i + 1] - rb[i];
             if (!rc)
@@ -264,36 +278,50 @@ int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double 
         copy_b(0);
         for (int i = 1; i < na; ++i) copy_a(i);
         for (int j = 1; j < nch; ++j) copy_b(j);
-        for (int j = 0; j < nch && !rc; ++j) {
+        // splits on their own stream, in arrival order: A0, B0, the other A blocks, the other B blocks
+        auto split_a = [&](int i) {
+            cudaStreamWaitEvent(ss, ev_a[i], 0);
+            if (!rc) rc = ozaki_split_a_rows(&prep, rb[i], rb[i + 1], ss);
+            cudaEventRecord(ev_sa[i], ss);
+        };
+        auto split_b = [&](int j) {
             const int64_t j0 = col0(j), nj = col0(j + 1) - j0;
-            OzB pb;
-            cudaStreamWaitEvent(s, ev_b[j], 0);
-            if (j == 0) cudaStreamWaitEvent(s, ev_a[0], 0);
-            if (j == 0) rc = ozaki_split_a_rows(&prep, rb[0], rb[1], s);
-            if (!rc) rc = ozaki_prepare_b(&prep, nj, bd + j0 * k, 1, k, s, &pb);
-            if (rc) break;
-            for (int i = 0; i < na && !rc; ++i) {
-                const int64_t r0 = rb[i], rows = rb[i + 1] - rb[i];
-                if (j == 0 && i > 0) {
-                    cudaStreamWaitEvent(s, ev_a[i], 0);
-                    rc = ozaki_split_a_rows(&prep, r0, rb[i + 1], s);
-                }
-                if (!rc) rc = ozaki_multiply_rows(&prep, r0, rows, &pb, alpha, beta, cd + j0 * m + r0, 1, m, s);
-                cudaEventRecord(ev_c[i * nch + j], s);
-                cudaStreamWaitEvent(cout, ev_c[i * nch + j], 0);
-                if (!rc)
-                    rc = check_cuda(cudaMemcpy2DAsync(c + j0 * ldc + r0, ldc * sizeof(double), cd + j0 * m + r0,
-                                                      m * sizeof(double), rows * sizeof(double), nj,
-                                                      cudaMemcpyDefault, cout), "C back");
-            }
-            ozaki_release_b(&pb, s);
-        }
-        // frees below are ordered after every copy on either copy stream
+            cudaStreamWaitEvent(ss, ev_b[j], 0);
+            if (!rc) rc = ozaki_prepare_b(&prep, nj, bd + j0 * k, 1, k, ss, &pb[(size_t)j]);
+            cudaEventRecord(ev_sb[j], ss);
+        };
+        int q = 0;  // product stream of the next block
+        auto product = [&](int i, int j) {
+            const int64_t j0 = col0(j), nj = col0(j + 1) - j0, r0 = rb[i], rows = rb[i + 1] - rb[i];
+            cudaStream_t ps = sp[q];
+            q ^= 1;
+            cudaStreamWaitEvent(ps, ev_sa[i], 0);
+            cudaStreamWaitEvent(ps, ev_sb[j], 0);
+            if (!rc) rc = ozaki_multiply_rows(&prep, r0, rows, &pb[(size_t)j], alpha, beta, cd + j0 * m + r0, 1, m, ps);
+            cudaEventRecord(ev_c[i * nch + j], ps);
+            cudaStreamWaitEvent(cout, ev_c[i * nch + j], 0);
+            if (!rc)
+                rc = check_cuda(cudaMemcpy2DAsync(c + j0 * ldc + r0, ldc * sizeof(double), cd + j0 * m + r0,
+                                                  m * sizeof(double), rows * sizeof(double), nj, cudaMemcpyDefault,
+                                                  cout), "C back");
+        };
+        split_a(0);
+        split_b(0);
+        for (int i = 1; i < na; ++i) split_a(i);
+        for (int j = 1; j < nch; ++j) split_b(j);
+        for (int j = 0; j < nch; ++j)
+            for (int i = 0; i < na; ++i) product(i, j);
+        // frees below are ordered after every copy and every product on either compute stream
         cudaEventRecord(ev_in_done, cin);
         cudaEventRecord(ev_out_done, cout);
+        cudaEventRecord(ev_aux_done, sp[1]);
+        cudaEventRecord(ev_split_done, ss);
         cudaStreamWaitEvent(s, ev_in_done, 0);
         cudaStreamWaitEvent(s, ev_out_done, 0);
+        cudaStreamWaitEvent(s, ev_aux_done, 0);
+        cudaStreamWaitEvent(s, ev_split_done, 0);
     }
+    for (auto& x : pb) ozaki_release_b(&x, s);
     ozaki_release_a(&prep, s);
     dev_free(ad, s);
     dev_free(bd, s);
@@ -362,14 +390,18 @@ int gemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, T alpha, 
                 slices = checked;
                 native = checked > 12;  // no slice count reaches the bound: IEEE path
             }
-            if (native)
+            if (native) {
+                note_ozaki_slices(0);
                 rc = dgemm_native(m, n, k, (double)alpha, ad, ars, acs, bd, brs, bcs, (double)beta, (double*)cd,
                                   C.rs, C.cs, s);
+            }
             else
                 rc = dgemm_ozaki(m, n, k, (double)alpha, ad, ars, acs, bd, brs, bcs, (double)beta, (double*)cd,
                                  C.rs, C.cs, slices, s);
         } else {
-            int cfg = 0, unused = 0;
+            // the learned selector when it is on (by default: the committed model), else the
+            // occupancy rule
+            int cfg = selector_heuristic(m, n, k), unused = 0;
             if (selector_auto() && (rc = selector_choose(sizeof(T) == 8 ? 0 : 1, m, n, k, ta, tb, (int)pad, 0.0,
                                                          0.0, &cfg, &unused)))
                 return rc;
@@ -1774,6 +1806,14 @@ void gb_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diag
               double* b, gb_inc_t rs_b, gb_inc_t cs_b)
 {
     trsm_host(side, uploa, transa, diaga, m, n, *alpha, a, rs_a, cs_a, b, rs_b, cs_b);
+}
+
+void gb_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+              const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b,
+              gb_inc_t rs_b, gb_inc_t cs_b)
+{
+    ztrsm_host(side, uploa, transa, diaga, m, n, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+               "gb_ztrsm");
 }
 
 void gb_dgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, const double* alpha,

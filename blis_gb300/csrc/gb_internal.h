@@ -32,7 +32,7 @@ int check_cuda(cudaError_t e, const char* where);
 // blocks cached.
 cudaStream_t thread_stream();
 cudaStream_t thread_copy_stream(int i);  // i = 0, 1: copy streams of the calling thread
-cudaStream_t thread_aux_stream();         // a second compute stream of the calling thread
+cudaStream_t thread_aux_stream(int i = 0);  // i = 0, 1: more compute streams of the calling thread
 int ensure_init();
 int sm_count();
 
@@ -70,6 +70,10 @@ class LaunchScope {
 // Bounded-wait budget for spin loops in device code (nanoseconds of
 // %globaltimer); a wait that exceeds it reports DEV_WAIT_TIMEOUT.
 constexpr unsigned long long kWaitBudgetNs = 2000000000ull;
+// Failure-detection test hook (gb_test_trsv_wait_fault): the budget of the
+// one-launch trsv's flag waits, and a block whose flag it withholds (-1 none).
+unsigned long long trsv_wait_budget_ns();
+int64_t trsv_withheld_block();
 
 // ---------------------------------------------------------------- kernels
 // All take device pointers and BLIS-style element strides (rs, cs).  op(A)
@@ -85,6 +89,7 @@ int dgemm_native_gated(int64_t m, int64_t n, int64_t k, double alpha,
                        double* c, int64_t rs_c, int64_t cs_c, const int* gate, cudaStream_t s);
 double ozaki_t_bound_log2(int s, int64_t k);
 bool selector_auto();
+int selector_heuristic(int64_t m, int64_t n, int64_t k);
 int selector_choose(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad, double sa, double sb,
                     int* config, int* slices);
 double host_exponent_spread(const double* x, int64_t rows, int64_t cols, int64_t rs, int64_t cs);
@@ -230,6 +235,9 @@ int dgemv_dev(int trans, int64_t m, int64_t n, double alpha, const double* a,
 int dgemm_mode();
 int ozaki_slices();
 // Scoped per-thread dgemm mode (restored on destruction).
+// Records the slice count of an Ozaki product on the calling thread
+// (gb_last_ozaki_slices); 0 when a gemm's product ran on the native kernel.
+void note_ozaki_slices(int slices);
 class ModeOverride {
 public:
     ModeOverride(int mode, int slices);

@@ -269,13 +269,16 @@ int daxpyv_dev(int64_t n, double alpha, const double* x, int64_t incx, double* y
 
 // Number of first-pass partial sums for a dot product of length n on a GPU
 // with `sms` SMs: one per 4096 elements, at most 8 per SM.
-static int dotv_nparts_for(int64_t n, int sms)
+static constexpr int dotv_nparts_for(int64_t n, int sms)
 {
     int64_t g = (n + 4095) / 4096;
     const int64_t cap = (int64_t)(sms > 0 ? sms : 152) * 8;
     if (g > cap) g = cap;
     return (int)(g < 1 ? 1 : g);
 }
+// the allocation-free dotv's scratch covers every partition on GPUs of up to 256 SMs
+static_assert(dotv_nparts_for(INT64_MAX / 2, 256) <= GB_DOTV_NOALLOC_MAX_PARTS,
+              "allocation-free dotv scratch smaller than the largest partition");
 
 int dotv_nparts(int64_t n) { return dotv_nparts_for(n, sm_count()); }
 
@@ -416,8 +419,8 @@ extern "C" int gb_ddotv_noalloc_dev(gb_dim_t n, const double* x, gb_inc_t incx, 
         scratch = g_noalloc_ptr[dev];
         sms = g_noalloc_sms[dev];
     }
-    if (n > 0 && (x == nullptr || y == nullptr || incx == 0 || incy == 0))
-        return gb::set_error(GB_ERR_ARG, "gb_ddotv_noalloc_dev", "null vector or zero increment");
+    if (n > 0 && (x == nullptr || y == nullptr))
+        return gb::set_error(GB_ERR_ARG, "gb_ddotv_noalloc_dev", "null vector");
     if (rho == nullptr) return gb::set_error(GB_ERR_ARG, "gb_ddotv_noalloc_dev", "null rho");
     const int nparts = gb::dotv_nparts_for(n > 0 ? n : 1, sms);
     if (nparts > GB_DOTV_NOALLOC_MAX_PARTS) {

@@ -1948,6 +1948,7 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
 {
     if (r0 < 0 || rows <= 0 || r0 + rows > A->m || r0 % A->row_tile)
         return set_error(GB_ERR_ARG, "ozaki", "row block not aligned to the slice GEMM tile");
+    note_ozaki_slices(A->slices);
     if (A->out_tri && (r0 != 0 || rows != A->m || A->tri || A->out_rpc < 1))
         return set_error(GB_ERR_ARG, "ozaki", "a triangle of C is written from the whole of op(A) only");
     const int64_t m = rows, n = B->n, k = A->k, kpad = A->kpad, npad = B->npad;
@@ -2079,8 +2080,16 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
         // inside it in place, the diagonal block through scratch and a merge
         const int64_t rpc = A->out_rpc, W = 1024;
         const int64_t wmax = (n < W) ? n : W;
-        double* d = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(rpc * wmax * wmax), s));
-        if (!d) return bail(GB_ERR_NOMEM);
+        // the diagonal-block scratch reuses the level planes, which the recombination (ordered
+        // before it on s) has finished reading; a separate buffer only if they are too small
+        const size_t dbytes = sizeof(double) * (size_t)(rpc * wmax * wmax);
+        double* own = nullptr;
+        double* d = reinterpret_cast<double*>(planes);
+        if (dbytes > bytes_pl) {
+            own = static_cast<double*>(dev_alloc(dbytes, s));
+            if (!own) return bail(GB_ERR_NOMEM);
+            d = own;
+        }
         const bool lower = (A->out_tri == 1);
         for (int64_t j0 = 0; j0 < n && !rc; j0 += W) {
             const int64_t w = (n - j0 < W) ? n - j0 : W;
@@ -2102,7 +2111,7 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
                 }
             }
         }
-        dev_free(d, s);
+        if (own) dev_free(own, s);
     }
     dev_free(planes, s);
     return rc;

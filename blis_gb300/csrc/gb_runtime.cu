@@ -24,6 +24,8 @@ bool g_inited = false;
 int g_sms = 0;
 unsigned int* g_status = nullptr;  // device word, one per library instance
 std::atomic<int64_t> g_launches{0};
+std::atomic<unsigned long long> g_trsv_wait_ns{kWaitBudgetNs};
+std::atomic<int64_t> g_trsv_withhold{-1};
 std::atomic<int> g_timing{0};
 int g_dgemm_mode = GB_DGEMM_NATIVE;
 int g_ozaki_slices = 8;
@@ -117,18 +119,19 @@ cudaStream_t thread_copy_stream(int i)
     return t_copy[i & 1];
 }
 
-// A second compute stream per calling thread (work that forks from the
+// Two more compute streams per calling thread (work that forks from the
 // thread's stream and joins it again within one call).
-thread_local cudaStream_t t_aux = nullptr;
+thread_local cudaStream_t t_aux[2] = {nullptr, nullptr};
 thread_local int t_aux_dev = -1;
 
-cudaStream_t thread_aux_stream()
+cudaStream_t thread_aux_stream(int i)
 {
-    if (t_aux == nullptr || t_aux_dev != g_device) {
-        cudaStreamCreateWithFlags(&t_aux, cudaStreamNonBlocking);
+    if (t_aux_dev != g_device) {
+        t_aux[0] = t_aux[1] = nullptr;
         t_aux_dev = g_device;
     }
-    return t_aux;
+    if (t_aux[i & 1] == nullptr) cudaStreamCreateWithFlags(&t_aux[i & 1], cudaStreamNonBlocking);
+    return t_aux[i & 1];
 }
 
 void* dev_alloc(size_t bytes, cudaStream_t s)
@@ -184,6 +187,14 @@ ModeOverride::~ModeOverride()
     t_mode = mode_;
     t_slices = slices_;
 }
+
+unsigned long long trsv_wait_budget_ns() { return g_trsv_wait_ns.load(std::memory_order_relaxed); }
+int64_t trsv_withheld_block() { return g_trsv_withhold.load(std::memory_order_relaxed); }
+
+// Slice count of the calling thread's most recent Ozaki product (0 = the last
+// double-precision product of a gemm call ran on the native FP64 kernel).
+thread_local int t_last_slices = -1;
+void note_ozaki_slices(int slices) { t_last_slices = slices; }
 
 // ---------------------------------------------------------------- launches
 LaunchScope::LaunchScope(const char* name, cudaStream_t s) : name_(name), s_(s), timed_(false)
@@ -246,6 +257,17 @@ void gb_clear_last_error(void)
 }
 
 int64_t gb_launch_count(void) { return gb::g_launches.load(); }
+
+int gb_last_ozaki_slices(void) { return gb::t_last_slices; }
+
+int gb_test_trsv_wait_fault(int64_t withhold_block, int64_t wait_budget_ns)
+{
+    if (wait_budget_ns < 0 || (wait_budget_ns > 0 && wait_budget_ns < 100000) || wait_budget_ns > 10000000000ll)
+        return gb::set_error(GB_ERR_ARG, "gb_test_trsv_wait_fault", "budget outside [0.1 ms, 10 s]");
+    gb::g_trsv_withhold.store(withhold_block < 0 ? -1 : withhold_block);
+    gb::g_trsv_wait_ns.store(wait_budget_ns == 0 ? gb::kWaitBudgetNs : (unsigned long long)wait_budget_ns);
+    return GB_SUCCESS;
+}
 
 int gb_set_kernel_timing(int enable)
 {

@@ -6,15 +6,27 @@
 // when auto-selection is on: the configuration of least predicted time,
 // and in the Ozaki "auto" mode the proposed slice count, checked by the
 // error-bound verifier and raised if it fails.  Inference runs on the GPU
-// (one sample per new shape; results are cached per shape).  Without a
-// model, the small-problem rule of BLIS's sup thresholds applies
-// (frame/base/bli_cntx.h:186-193).
+// (one sample per new shape; results are cached per shape).
+//
+// By default the host entry points use the model committed next to the
+// library (tuning/selector_mlp.bin, loaded on first use unless the caller
+// loaded, unloaded or switched the selector off first, or GB_SELECTOR=rule).
+// Without a model, an occupancy rule stands in for BLIS's small-problem
+// thresholds (frame/base/bli_cntx.h:186-193): 128x128 tiles when they fill
+// the SMs, else the 64x64 engine with the least split of K that gives two
+// waves of CTAs (on the 13,334 FP64/FP32 autotuned shapes: mean regret 0.71 /
+// 0.20 against 3.19 / 2.21 for the threshold rule).
+#include <dlfcn.h>
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <mutex>
+#include <string>
 #include <unordered_map>
+#include <vector>
 
 #include "gb_internal.h"
 
@@ -27,6 +39,8 @@ float* g_params = nullptr;  // device copy of the MLP parameters
 float* g_io = nullptr;      // device scratch: 16 features + 8 outputs
 bool g_loaded = false;
 bool g_auto = false;
+bool g_user_configured = false;  // the caller loaded, unloaded or switched the selector itself
+std::once_flag g_default_once;
 std::unordered_map<uint64_t, uint64_t> g_cache;
 
 uint32_t crc32_bytes(const unsigned char* p, size_t n)
@@ -71,12 +85,82 @@ uint64_t key_of(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int 
 
 }  // namespace
 
-int selector_heuristic(int64_t m, int64_t n, int64_t k)
+namespace {
+// Reads a model file (magic, version, parameter count, CRC-32 of the parameters).
+bool read_model_file(const char* path, float* p)
 {
-    return ((m < n ? m : n) < 201 || k < 201) ? 1 : 0;
+    FILE* f = path ? fopen(path, "rb") : nullptr;
+    if (!f) return false;
+    char magic[8];
+    uint32_t hdr[3];
+    const bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "GBSELMLP", 8) == 0 &&
+                    fread(hdr, sizeof(uint32_t), 3, f) == 3 && hdr[0] == 1 && hdr[1] == GB_MLP_NPARAMS &&
+                    fread(p, sizeof(float), GB_MLP_NPARAMS, f) == GB_MLP_NPARAMS &&
+                    crc32_bytes(reinterpret_cast<const unsigned char*>(p), sizeof(float) * GB_MLP_NPARAMS) == hdr[2];
+    fclose(f);
+    return ok;
 }
 
-bool selector_auto() { return g_auto && g_loaded; }
+// Copies the parameters to the device.  A load the caller asked for (user) takes
+// charge of the selector; the default load switches auto-selection on unless the
+// caller already decided.
+int load_params(const float* params, bool user)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!user && g_user_configured) return GB_SUCCESS;
+    if (!g_params) {
+        GB_CUDA(cudaMalloc(&g_params, sizeof(float) * GB_MLP_NPARAMS));
+        GB_CUDA(cudaMalloc(&g_io, sizeof(float) * (GB_MLP_IN + GB_MLP_OUT)));
+    }
+    GB_CUDA(cudaMemcpy(g_params, params, sizeof(float) * GB_MLP_NPARAMS, cudaMemcpyHostToDevice));
+    g_cache.clear();
+    g_loaded = true;
+    if (user) g_user_configured = true;
+    else g_auto = true;
+    return GB_SUCCESS;
+}
+}  // namespace
+
+// The occupancy rule: config 0 (128x128 tiles) when its tiles cover the SMs,
+// else the 64x64 engine (configs 1..5 = K split 1, 2, 4, 8, 16) with the least
+// split that reaches two waves of CTAs or would leave fewer than 128 values of
+// k per part.
+int selector_heuristic(int64_t m, int64_t n, int64_t k)
+{
+    const int64_t sms = sm_count();
+    const int64_t t128 = ((m + 127) / 128) * ((n + 127) / 128);
+    if (t128 >= sms) return 0;
+    const int64_t t64 = ((m + 63) / 64) * ((n + 63) / 64);
+    for (int c = 1; c < GB_GEMM_NUM_CONFIGS; ++c) {
+        const int64_t split = int64_t(1) << (c - 1);
+        if (t64 * split >= 2 * sms || k / (2 * split) < 128) return c;
+    }
+    return GB_GEMM_NUM_CONFIGS - 1;
+}
+
+namespace {
+// tuning/selector_mlp.bin beside this library, when the caller has not taken charge
+void load_default_model()
+{
+    const char* env = getenv("GB_SELECTOR");
+    if (env && (strcmp(env, "rule") == 0 || strcmp(env, "off") == 0)) return;
+    Dl_info info;
+    if (!dladdr(reinterpret_cast<void*>(&load_default_model), &info) || !info.dli_fname) return;
+    std::string path(info.dli_fname);
+    const size_t slash = path.rfind('/');
+    path = (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/tuning/selector_mlp.bin";
+    if (access(path.c_str(), R_OK) != 0) return;
+    std::vector<float> p(GB_MLP_NPARAMS);
+    if (!read_model_file(path.c_str(), p.data())) return;
+    if (ensure_init() != GB_SUCCESS || load_params(p.data(), false) != GB_SUCCESS) gb_clear_last_error();
+}
+}  // namespace
+
+bool selector_auto()
+{
+    std::call_once(g_default_once, load_default_model);
+    return g_auto && g_loaded;
+}
 
 // Config (0..GB_GEMM_NUM_CONFIGS-1) and proposed Ozaki slice count for a shape.
 int selector_choose(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad, double sa, double sb,
@@ -149,38 +233,22 @@ int gb_selector_load(const float* params, int nparams)
     if (rc) return rc;
     if (!params || nparams != GB_MLP_NPARAMS)
         return set_error(GB_ERR_ARG, "gb_selector_load", "expected GB_MLP_NPARAMS parameters");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_params) {
-        GB_CUDA(cudaMalloc(&g_params, sizeof(float) * GB_MLP_NPARAMS));
-        GB_CUDA(cudaMalloc(&g_io, sizeof(float) * (GB_MLP_IN + GB_MLP_OUT)));
-    }
-    GB_CUDA(cudaMemcpy(g_params, params, sizeof(float) * GB_MLP_NPARAMS, cudaMemcpyHostToDevice));
-    g_cache.clear();
-    g_loaded = true;
-    return GB_SUCCESS;
+    return load_params(params, true);
 }
 
 int gb_selector_load_file(const char* path)
 {
-    FILE* f = path ? fopen(path, "rb") : nullptr;
-    if (!f) return set_error(GB_ERR_ARG, "gb_selector_load_file", "cannot open model file");
-    char magic[8];
-    uint32_t hdr[3];
-    float* p = new float[GB_MLP_NPARAMS];
-    const bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "GBSELMLP", 8) == 0 &&
-                    fread(hdr, sizeof(uint32_t), 3, f) == 3 && hdr[0] == 1 && hdr[1] == GB_MLP_NPARAMS &&
-                    fread(p, sizeof(float), GB_MLP_NPARAMS, f) == GB_MLP_NPARAMS &&
-                    crc32_bytes(reinterpret_cast<const unsigned char*>(p), sizeof(float) * GB_MLP_NPARAMS) == hdr[2];
-    fclose(f);
-    int rc = ok ? gb_selector_load(p, GB_MLP_NPARAMS)
-                : set_error(GB_ERR_ARG, "gb_selector_load_file", "bad magic, version, size or checksum");
-    delete[] p;
-    return rc;
+    std::vector<float> p(GB_MLP_NPARAMS);
+    if (!read_model_file(path, p.data()))
+        return set_error(GB_ERR_ARG, "gb_selector_load_file", "cannot open the model file, or bad magic, version, "
+                                                              "size or checksum");
+    return gb_selector_load(p.data(), GB_MLP_NPARAMS);
 }
 
 int gb_selector_unload(void)
 {
     std::lock_guard<std::mutex> lk(g_mu);
+    g_user_configured = true;
     g_loaded = false;
     g_cache.clear();
     return GB_SUCCESS;
@@ -188,6 +256,8 @@ int gb_selector_unload(void)
 
 int gb_set_gemm_autoselect(int on)
 {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_user_configured = true;
     g_auto = on != 0;
     return GB_SUCCESS;
 }

@@ -211,6 +211,8 @@ struct TrsvArgs {
     int* ticket;  // next solve position
     int* abort;   // set by a CTA that gave up
     unsigned int* status;
+    unsigned long long wait_ns;  // budget of each flag wait
+    int64_t withhold;            // block whose flag is never published (failure-detection test), -1 none
 };
 
 __device__ __forceinline__ int ld_acquire(const int* p)
@@ -279,7 +281,7 @@ __global__ void __launch_bounds__(SV_THREADS) trsv_flags_kernel(const TrsvArgs p
         if (tid == 0) {
             const uint64_t t0 = sv_clock();
             while (!ld_acquire(p.flags + j)) {
-                if (*(volatile int*)p.abort || sv_clock() - t0 > kWaitBudgetNs) {
+                if (*(volatile int*)p.abort || sv_clock() - t0 > p.wait_ns) {
                     atomicOr(p.status, DEV_WAIT_TIMEOUT);
                     atomicExch(p.abort, 1);
                     s_fail = 1;
@@ -357,7 +359,7 @@ __global__ void __launch_bounds__(SV_THREADS) trsv_flags_kernel(const TrsvArgs p
         if (rb < nb) p.x[(r0 + rb) * p.incx] = y1;
         __threadfence();
         __syncwarp();
-        if (lane == 0) st_release(p.flags + blk, 1);
+        if (lane == 0 && blk != p.withhold) st_release(p.flags + blk, 1);
     }
 }
 
@@ -384,6 +386,8 @@ int launch_trsv(bool lower, bool unit, int64_t m, double alpha, const double* a,
         p.ticket = ws + nblk;
         p.abort = ws + nblk + 1;
         p.status = device_status_word();
+        p.wait_ns = trsv_wait_budget_ns();
+        p.withhold = trsv_withheld_block();
         const bool rowmajor = (acs == 1 && ars != 1);
         LaunchScope ls("trsv_flags", s);
         if (lower)
@@ -551,30 +555,33 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     }
     int rc = check_cuda(cudaGetLastError(), "trsm_pack_diag");
     t.packed = packed;
-    if (!rc && slices > 0 && nn >= 2 * TRSM_SPLIT_MIN_COLS && mm > 4 * TRSM_NB) {
-        // the precision form's many small launches (split, slice GEMM,
-        // recombination per update) and the FP64-pipe diagonal solves of two
-        // column halves overlap on two streams
+    // the precision form's many small launches (split, slice GEMM, recombination
+    // per update) and the FP64-pipe diagonal solves of two column halves overlap
+    // on two streams, forked and joined by two events; if either event cannot be
+    // created the solve runs on one stream
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    const bool two = !rc && slices > 0 && nn >= 2 * TRSM_SPLIT_MIN_COLS && mm > 4 * TRSM_NB &&
+                     cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming) == cudaSuccess &&
+                     cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming) == cudaSuccess;
+    if (two) {
         TrsmCtx ts[2] = {t, t};
         const int64_t n1 = (nn / 2 + 7) / 8 * 8;
         ts[0].n = n1;
         ts[1].n = nn - n1;
         ts[1].b = b + n1 * bcs;
         ts[1].s = thread_aux_stream();
-        cudaEvent_t ev[2];
-        rc = check_cuda(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming), "trsm event");
-        if (!rc) rc = check_cuda(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming), "trsm event");
-        if (!rc) rc = check_cuda(cudaEventRecord(ev[0], s), "trsm fork");
+        rc = check_cuda(cudaEventRecord(ev[0], s), "trsm fork");
         if (!rc) rc = check_cuda(cudaStreamWaitEvent(ts[1].s, ev[0], 0), "trsm fork");
         if (!rc) rc = solve(ts, 2, 0, mm);
         // the join is recorded whatever happened, so s never runs ahead of the second stream's work
         cudaEventRecord(ev[1], ts[1].s);
         cudaStreamWaitEvent(s, ev[1], 0);
-        cudaEventDestroy(ev[0]);
-        cudaEventDestroy(ev[1]);
     } else if (!rc) {
+        cudaGetLastError();  // a failed event creation above is not this call's error
         rc = solve(&t, 1, 0, mm);
     }
+    for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
     dev_free(packed, s);
     return rc;
 }

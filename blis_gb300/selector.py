@@ -90,6 +90,20 @@ def heuristic_config(m, n, k):
     return 0 if min(m, n, k) >= 201 else 1
 
 
+def occupancy_config(m, n, k, sms=152):
+    """The library's rule without a model (gb_selector.cu selector_heuristic): 128x128
+    tiles when they cover the SMs, else the 64x64 engine with the least K split that
+    reaches two waves of CTAs or leaves fewer than 128 values of k per part."""
+    if ((m + 127) // 128) * ((n + 127) // 128) >= sms:
+        return 0
+    t64 = ((m + 63) // 64) * ((n + 63) // 64)
+    for c in range(1, NCONFIG):
+        split = 1 << (c - 1)
+        if t64 * split >= 2 * sms or k // (2 * split) < 128:
+            return c
+    return NCONFIG - 1
+
+
 # ------------------------------------------------------------------ shapes
 def sample_shapes(count, seed, dtypes=("fp64", "fp32", "bf16")):
     """m, n, k log-uniform integers in [1, 32768], random transposes and

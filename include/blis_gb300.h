@@ -66,6 +66,13 @@ typedef struct { double real, imag; } gb_dcomplex;
 #define GB_ERR_NOMEM (-4)
 #define GB_ERR_UNSUPPORTED (-5)
 
+/* Code compiled against BLIS's own blis.h (a gemm sandbox, the glue library
+   that registers kernels in BLIS's context) defines GB300_ADDON_ONLY before
+   including this header: the BLAS, CBLAS and typed bli_ declarations of
+   groups 1a-1c would clash with blis.h's, and that code calls the gb_ names
+   below, which cannot resolve back into libblis. */
+#ifndef GB300_ADDON_ONLY
+
 /* ===================================================================== */
 /* 1a. Fortran-77 BLAS compat layer                                        */
 /* ===================================================================== */
@@ -427,6 +434,8 @@ void bli_ddotv_ex(gb_conj_t conjx, gb_conj_t conjy, gb_dim_t n, const double* x,
                   gb_inc_t incx, const double* y, gb_inc_t incy, double* rho,
                   const void* cntx, const void* rntm);
 
+#endif /* GB300_ADDON_ONLY */
+
 /* Host-pointer entry points under the addon prefix, with the typed-API
    argument lists above.  A BLIS build that keeps its own bli_?gemm symbols
    (for instance a sandbox bli_gemm_ex that forwards to this library) calls
@@ -458,6 +467,10 @@ void gb_cgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_d
 void gb_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
               gb_dim_t m, gb_dim_t n, const double* alpha, const double* a,
               gb_inc_t rs_a, gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b);
+/* same as bli_ztrsm (frame/3/bli_l3_tapi_ex.c:533-586, complex instance) */
+void gb_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
+              gb_dim_t m, gb_dim_t n, const gb_dcomplex* alpha, const gb_dcomplex* a,
+              gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b);
 void gb_dgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n,
               const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
               const double* x, gb_inc_t incx, const double* beta, double* y, gb_inc_t incy);
@@ -774,6 +787,13 @@ void gb_clear_last_error(void);
 /* Number of kernels this library has launched since load. */
 int64_t gb_launch_count(void);
 
+/* Slice count of the calling thread's most recent Ozaki split product (so a
+   caller that let the library choose, slices = 0, can learn the count); 0 if
+   the last double-precision gemm in the Ozaki form ran on the native FP64
+   kernel instead (no slice count reached the error bound), -1 before any.
+   No reference counterpart. */
+int gb_last_ozaki_slices(void);
+
 /* Per-kernel device time (CUDA events on the launching stream), enabled by
    gb_set_kernel_timing(1).  gb_kernel_time_ms() synchronises the recorded
    events and returns the summed time and launch count of kernels whose name
@@ -783,6 +803,18 @@ double gb_kernel_time_ms(const char* prefix, int64_t* launches);
 
 /* Blocks until the calling thread's library stream is idle. */
 int gb_synchronize(void);
+
+/* Failure-detection test hook (no reference counterpart).  The one-launch
+   dtrsv (trsv_flags_kernel) hands each 64-row block of x from CTA to CTA
+   through flags with bounded waits.  With withhold_block >= 0 the CTA that
+   solves that block does not publish its flag, so the CTAs after it wait
+   until the budget runs out (wait_budget_ns, 0 = the default 2 s, else
+   0.1 ms .. 10 s), report DEV_WAIT_TIMEOUT in the device status word, stop
+   every other CTA through the grid's abort word and return; the call then
+   fails with GB_ERR_DEVICE and the context stays usable.  Nothing faults,
+   traps or waits without a bound.  (-1, 0) restores normal operation.
+   Process-wide; for tests only. */
+int gb_test_trsv_wait_fault(int64_t withhold_block, int64_t wait_budget_ns);
 
 #ifdef __cplusplus
 }

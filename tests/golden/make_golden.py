@@ -7,7 +7,7 @@ test inputs, read as text (nothing of the reference is compiled or run).
   blastest_params.json the N / ALPHA / BETA / K / INC values and the test-ratio
                       threshold of blastest/input/dblat2.in and dblat3.in
 
-Usage: python tests/golden/make_golden.py [path-to-reference-tree]
+Usage: python tests/golden/make_golden.py PATH-TO-REFERENCE-TREE
 """
 import json
 import os
@@ -82,7 +82,9 @@ def blastest_inputs(ref):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py PATH-TO-REFERENCE-TREE")
+    ref = sys.argv[1]
     with open(os.path.join(HERE, "dblat1_check2.json"), "w") as f:
         json.dump(dblat1(ref), f, indent=1)
     with open(os.path.join(HERE, "blastest_params.json"), "w") as f:

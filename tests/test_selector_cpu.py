@@ -88,3 +88,22 @@ def test_committed_model_regret_per_dtype_on_cpu():
         assert sel.sum() >= 600
         regret = 1.0 - np.mean(best[sel] / t_mlp[sel])
         assert regret < 0.05 and regret < 1.0 - np.mean(best[sel] / t_rule[sel])
+
+
+def test_occupancy_rule_between_threshold_rule_and_model():
+    """Without a model the library uses the occupancy rule; on the held-out FP64 and FP32
+    shapes it is better than BLIS's threshold rule and worse than the trained model."""
+    from oracle import mlp_ref as R
+    p, _ = S.load_model(os.path.join(TUNING, "selector_mlp.json"))
+    d = np.load(os.path.join(TUNING, "autotune_heldout.npz"))
+    pred = R.forward(p.astype(np.float64), d["X"].astype(np.float64))
+    T, sh = d["T"], d["shapes"]
+    best = T.min(1)
+    idx = np.arange(len(T))
+    t_mlp = T[idx, pred[:, :S.NCONFIG].argmin(1)]
+    t_occ = T[idx, [S.occupancy_config(int(r[0]), int(r[1]), int(r[2])) for r in sh]]
+    t_thr = T[idx, [S.heuristic_config(int(r[0]), int(r[1]), int(r[2])) for r in sh]]
+    for code in (0, 1):
+        sel = sh[:, 3] == code
+        r_mlp, r_occ, r_thr = (float(np.mean(t[sel] / best[sel])) - 1.0 for t in (t_mlp, t_occ, t_thr))
+        assert r_mlp < r_occ < r_thr, (code, r_mlp, r_occ, r_thr)

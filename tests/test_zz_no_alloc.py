@@ -24,6 +24,9 @@ def _dot_tol(x, y):
 
 
 def test_noalloc_dotv_matches_allocating_entry_point_twice(gblib):
+    """Both entry points partition the vectors the same way (the SM count of the current
+    device) and reduce the partial sums in the same order, so their results are the same
+    bits; the torch sum is a third opinion within the dot-product tolerance."""
     torch = pytest.importorskip("torch")
     L = _lib.load()
     L.gb_ddotv_noalloc_dev.restype = C.c_int
@@ -32,10 +35,13 @@ def test_noalloc_dotv_matches_allocating_entry_point_twice(gblib):
     torch.cuda.set_device(0)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream or 1)
     g = torch.Generator(device="cpu").manual_seed(11)
-    cases = [(1_000_003, 1), (300_001, 2)]  # different partitions, second one strided
+    # different partitions, a strided one, a zero increment (every element is x[0], y[0]), and
+    # an empty product (rho = 0, whatever the shared array holds from the calls before)
+    cases = [(1_000_003, 1), (300_001, 2), (5_000, 0), (0, 1)]
     for n, inc in cases:
-        x = (torch.rand(n * inc, generator=g, dtype=torch.float64) * 2 - 1).cuda()
-        y = (torch.rand(n * inc, generator=g, dtype=torch.float64) * 2 - 1).cuda()
+        size = max(1, n * inc)
+        x = (torch.rand(size, generator=g, dtype=torch.float64) * 2 - 1).cuda()
+        y = (torch.rand(size, generator=g, dtype=torch.float64) * 2 - 1).cuda()
         rho_new = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
         rho_old = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
         rc = L.gb_ddotv_noalloc_dev(n, x.data_ptr(), inc, y.data_ptr(), inc, rho_new.data_ptr(), stream)
@@ -43,9 +49,13 @@ def test_noalloc_dotv_matches_allocating_entry_point_twice(gblib):
         rc = L.gb_ddotv_dev(n, x.data_ptr(), inc, y.data_ptr(), inc, rho_old.data_ptr(), stream)
         assert rc == 0, _lib.last_error()
         torch.cuda.synchronize()
-        xs, ys = x[::inc][:n], y[::inc][:n]
-        tol = _dot_tol(xs, ys)
         a, b = float(rho_new.item()), float(rho_old.item())
-        assert abs(a - b) <= tol
+        if n == 0:
+            assert a == 0.0 and b == 0.0
+            continue
+        assert np.float64(a).tobytes() == np.float64(b).tobytes(), (n, inc, a, b)
+        xs = x[0].expand(n) if inc == 0 else x[::inc][:n]
+        ys = y[0].expand(n) if inc == 0 else y[::inc][:n]
+        tol = _dot_tol(xs, ys)
         ref = float((xs * ys).sum())
         assert abs(a - ref) <= tol
