@@ -6,12 +6,14 @@ C := A*B with m = n = k = 16384, column-major FP64, entries (1+u)*2^e with
 e uniform in [-20, 20] and random sign, generated on the device by the
 library's seeded generator.  A "step" is one full DGEMM.
 
-  value      Ozaki DGEMM (bf16 slices on tcgen05) in FP64-equivalent
-             TFLOP/s (2mnk per step), operands resident in HBM, CUDA events
-             on the launching stream, K steps after W warm-up steps.  The
-             slice count is the smallest of a 3..8 sweep whose max
-             componentwise error is at most native FP64 DGEMM's on the same
-             inputs (--slices fixes it instead).
+  value      emulated DGEMM on the bf16 tensor cores (tcgen05) in
+             FP64-equivalent TFLOP/s (2mnk per step), operands resident in
+             HBM, CUDA events on the launching stream, K steps after W
+             warm-up steps.  Two forms are swept: digit slices (s = 3..8,
+             s(s+1)/2 products) and CRT residues (N = 10..16 moduli, N
+             products); the value is the fastest whose max componentwise
+             error is at most native FP64 DGEMM's on the same inputs
+             (--slices or --moduli fixes the form instead).
   e2e        the same DGEMM through the BLAS entry point dgemm_ (C ABI) on
              pinned host buffers: H2D of A and B and D2H of C inside the
              timed region of every step.
@@ -65,6 +67,8 @@ def parse():
     p.add_argument("--slices", type=int, default=0,
                    help="slice count of the timed form; 0 = the smallest count of the 3..8 sweep whose "
                         "max componentwise error is at most native FP64's")
+    p.add_argument("--moduli", type=int, default=0,
+                   help="run the CRT form with this many moduli instead of the sweep's choice")
     p.add_argument("--e2e-steps", type=int, default=0, help="end-to-end steps (0: --steps)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     return p.parse_args()
@@ -322,25 +326,38 @@ def run_gpu(args):
     err_nat = dev.componentwise_error(Cn[ii, jj], hi, lo)
     del Cn
 
-    # ---------------- slice-count sweep: time and error of each form
-    sweep = []
-    chosen = None
-    for sl in range(3, 9):
-        dev.dgemm_ozaki(0, 0, 1.0, A, B, 0.0, Cz, sl)
-        ms_sl = timed(lambda: dev.dgemm_ozaki(0, 0, 1.0, A, B, 0.0, Cz, sl))
-        err_sl = dev.componentwise_error(Cz[ii, jj], hi, lo)
-        sweep.append({"slices": sl, "products": sl * (sl + 1) // 2, "ms": ms_sl,
-                      "tflops": flops / (ms_sl * 1e-3) / 1e12, "max_componentwise_err": err_sl})
-        if chosen is None and err_sl <= err_nat:
-            chosen = sl
-    if args.slices > 0:
-        s = args.slices
-    else:
-        s = chosen if chosen is not None else 8
+    # ---------------- sweep of both emulated forms: time and error of each count
+    # digit form: s slices, s(s+1)/2 products; CRT form: N moduli, N products
+    def run_form(form, cnt):
+        if form == "crt":
+            dev.dgemm_ozaki_crt(0, 0, 1.0, A, B, 0.0, Cz, cnt)
+        else:
+            dev.dgemm_ozaki(0, 0, 1.0, A, B, 0.0, Cz, cnt)
 
-    # ---------------- Ozaki form, device resident (value)
+    sweep = []
+    for form, counts in (("digits", range(3, 9)), ("crt", range(10, 17))):
+        for cnt in counts:
+            run_form(form, cnt)
+            ms_sl = timed(lambda: run_form(form, cnt))
+            err_sl = dev.componentwise_error(Cz[ii, jj], hi, lo)
+            prods = cnt * (cnt + 1) // 2 if form == "digits" else cnt
+            sweep.append({"form": form, "slices" if form == "digits" else "moduli": cnt, "products": prods,
+                          "ms": ms_sl, "tflops": flops / (ms_sl * 1e-3) / 1e12, "max_componentwise_err": err_sl})
+    ok = [r for r in sweep if r["max_componentwise_err"] <= err_nat]
+    if args.slices > 0:
+        form, s = "digits", args.slices
+    elif args.moduli > 0:
+        form, s = "crt", args.moduli
+    elif ok:
+        best = min(ok, key=lambda r: r["ms"])
+        form, s = best["form"], best.get("slices", best.get("moduli"))
+    else:
+        form, s = "digits", 8
+    npairs = s * (s + 1) // 2 if form == "digits" else s
+
+    # ---------------- the chosen emulated form, device resident (value)
     for _ in range(args.warmup):
-        dev.dgemm_ozaki(0, 0, 1.0, A, B, 0.0, Cz, s)
+        run_form(form, s)
     barrier()
     dev.set_kernel_timing(True)
     dev.kernel_time_ms("")  # drop earlier records
@@ -350,7 +367,7 @@ def run_gpu(args):
         barrier()
         ev0.record(stream)
         for _ in range(args.steps):
-            dev.dgemm_ozaki(0, 0, 1.0, A, B, 0.0, Cz, s)
+            run_form(form, s)
         ev1.record(stream)
         barrier()
     launches = int(L.gb_launch_count() - l0)
@@ -358,7 +375,7 @@ def run_gpu(args):
     ms = ev0.elapsed_time(ev1) / args.steps
     gemm_ms, gemm_n = dev.kernel_time_ms("ozaki_slice_gemm")
     stage_ms = {nm: dev.kernel_time_ms(nm)[0] / max(1, args.steps)
-                for nm in ("oz_rowmax", "oz_split", "oz_recombine", "dgemm_dmma_gated")}
+                for nm in ("oz_rowmax", "oz_split", "oz_recombine", "dgemm_dmma_gated")}  # oz_split: both forms
     split_ms = sum(stage_ms.values()) * max(1, args.steps)
     dev.kernel_time_ms("")
     err_oz = dev.componentwise_error(Cz[ii, jj], hi, lo)
@@ -368,7 +385,6 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = flops * ws / (ms * 1e-3) / 1e12
-    npairs = s * (s + 1) // 2
     kern_ms = gemm_ms / max(1, gemm_n)
     achieved = npairs * flops / (kern_ms * 1e-3) / 1e12
     peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
@@ -381,7 +397,7 @@ def run_gpu(args):
     Ah.copy_(A.t())  # Ah row-major storage of A^T == column-major A
     Bh.copy_(B.t())
     torch.cuda.synchronize()
-    blas.set_dgemm_mode(blas.DGEMM_OZAKI, s)
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI_CRT if form == "crt" else blas.DGEMM_OZAKI, s)
     an, bn, cn = Ah.numpy(), Bh.numpy(), Ch.numpy()
     blas.dgemm("N", "N", n, n, n, 1.0, an, n, bn, n, 0.0, cn, n)  # warm-up
     e2e_steps = args.e2e_steps if args.e2e_steps > 0 else args.steps
@@ -406,8 +422,8 @@ def run_gpu(args):
     del Ch2
 
     # ---------------- DRAM traffic of the dominant kernel: the ncu capture at 4096^3 above,
-    # scaled by the slice-product units of this size, (n/4096)^3, and by the slice-product
-    # count (traffic per product is the same tiling)
+    # scaled by the slice-product units of this size, (n/4096)^3, and by the product count
+    # (traffic per product is the same tiling; the planes written per product are the same)
     traffic = TRAFFIC_4096_BYTES * (n / 4096.0) ** 3 * npairs / (TRAFFIC_SLICES * (TRAFFIC_SLICES + 1) // 2)
 
     if rank != 0:
@@ -434,11 +450,15 @@ def run_gpu(args):
         "dtype": "f64",
         "data": "synthetic: (1+u)*2^e, e in [-20,20], random sign, seeded counter RNG on device",
         "config": {"workload": "ozaki_dgemm_%d" % n, "m": n, "n": n, "k": n, "layout": "column-major",
-                   "alpha": 1.0, "beta": 0.0, "form": "ozaki bf16 slices=%d (triangular, %d products)" % (s, npairs),
+                   "alpha": 1.0, "beta": 0.0,
+                   "form": ("ozaki bf16 slices=%d (triangular, %d products)" % (s, npairs)) if form == "digits"
+                   else ("ozaki CRT bf16 residues, %d moduli (%d products)" % (s, npairs)),
                    "l2": "inputs 2 GiB each, larger than the 126 MB L2", "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "forms": {
-            "ozaki": {"tflops": value / ws, "max_componentwise_err": err_oz, "slices": s,
-                      "slice_choice": "smallest of 3..8 with error <= native" if args.slices == 0 else "fixed"},
+            "ozaki": {"tflops": value / ws, "max_componentwise_err": err_oz, "form": form,
+                      "slices" if form == "digits" else "moduli": s, "products": npairs,
+                      "choice": "fastest of the sweep with error <= native"
+                      if args.slices == 0 and args.moduli == 0 else "fixed"},
             "slice_sweep": sweep,
             "native_fp64": {"tflops": native_tf, "ms": native_ms, "max_componentwise_err": err_nat,
                             "engine": os.environ.get("GB_DGEMM_ENGINE", "dmma")},

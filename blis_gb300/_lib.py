@@ -161,6 +161,7 @@ def load(path=None):
     dg = [C.c_int, C.c_int, _i64, _i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _d, _vp, _i64, _i64]
     _sig(L, "gb_dgemm_dev", C.c_int, dg + [_vp])
     _sig(L, "gb_dgemm_ozaki_dev", C.c_int, dg + [C.c_int, _vp])
+    _sig(L, "gb_dgemm_ozaki_crt_dev", C.c_int, dg + [C.c_int, _vp])
     sg = [C.c_int, C.c_int, _i64, _i64, _i64, _f, _vp, _i64, _i64, _vp, _i64, _i64, _f, _vp, _i64, _i64]
     _sig(L, "gb_sgemm_dev", C.c_int, sg + [_vp])
     _sig(L, "gb_dtrsm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _vp])

@@ -16,7 +16,7 @@ NO_CONJUGATE, CONJUGATE = 0x00, 0x10
 LOWER, UPPER = 0xC0, 0x60
 LEFT, RIGHT = 0, 1
 NONUNIT_DIAG, UNIT_DIAG = 0x000, 0x100
-DGEMM_NATIVE, DGEMM_OZAKI = 0, 1
+DGEMM_NATIVE, DGEMM_OZAKI, DGEMM_OZAKI_CRT = 0, 1, 2
 
 
 def _i(v):

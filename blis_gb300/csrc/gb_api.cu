@@ -389,6 +389,11 @@ int gemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, T alpha, 
                     return rc;
                 slices = checked;
                 native = checked > 12;  // no slice count reaches the bound: IEEE path
+                if (!native && ozaki_form() == 1) {
+                    // the CRT form at the precision of the verified digit count (8s - 1 bits)
+                    slices = ozaki_crt_moduli_for_bits(8 * checked - 1, k);
+                    native = slices < 0;
+                }
             }
             if (native) {
                 note_ozaki_slices(0);
@@ -1869,6 +1874,21 @@ int gb_dgemm_ozaki_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_
     const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
     return gb::dgemm_ozaki(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
                            tb ? rs_b : cs_b, beta, c, rs_c, cs_c, slices, pick_stream(stream));
+}
+
+int gb_dgemm_ozaki_crt_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                           double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                           gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c,
+                           gb_inc_t cs_c, int moduli, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_dgemm_ozaki_crt_dev", "negative dimension");
+    if (moduli < 2 || moduli > 16) return gb::set_error(GB_ERR_ARG, "gb_dgemm_ozaki_crt_dev", "moduli must be in [2, 16]");
+    gb::ModeOverride form(GB_DGEMM_OZAKI, moduli, 1);
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    return gb::dgemm_ozaki(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
+                           tb ? rs_b : cs_b, beta, c, rs_c, cs_c, moduli, pick_stream(stream));
 }
 
 int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,

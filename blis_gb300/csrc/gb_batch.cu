@@ -221,7 +221,8 @@ int batch_plan_create(const gb_gemm_problem_t* probs, int64_t count, int dtype, 
     *out = nullptr;
     if (dtype != GB_BATCH_FP64_OZAKI)
         return tune ? batch_plan_selected(probs, count, dtype, out) : batch_plan_policy(probs, count, dtype, 0, out);
-    int slices = ozaki_slices();
+    // the grouped batch runs the digit form (at the CRT form's precision when that form is set)
+    int slices = ozaki_digit_slices();
     if (slices < 2) slices = 8;  // automatic: the verifier is per problem; the batch uses 8
     std::vector<gb_gemm_problem_t> grouped, rest, singles;
     for (int64_t i = 0; i < count; ++i) {
@@ -357,8 +358,9 @@ int batch_loop(const gb_gemm_problem_t* probs, int64_t count, int dtype, cudaStr
         const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
         int rc;
         if (dtype == GB_BATCH_FP64_OZAKI) {
-            int slices = ozaki_slices();
+            int slices = ozaki_digit_slices();
             if (slices < 2) slices = 8;
+            ModeOverride digits(GB_DGEMM_OZAKI, slices, 0);
             rc = dgemm_ozaki(p.m, p.n, p.k, p.alpha, (const double*)p.a, ta ? p.lda : 1, ta ? 1 : p.lda,
                              (const double*)p.b, tb ? p.ldb : 1, tb ? 1 : p.ldb, p.beta, (double*)p.c, 1, p.ldc,
                              slices, s);

@@ -156,7 +156,9 @@ int chemm_dev(int side, int uplo, int herm, int conja, int transb, int64_t m, in
 // The Ozaki form in two phases (gb_ozaki.cu): op(A) split once, then any
 // number of products with column blocks of op(B) (bit-identical to one call).
 struct OzA {
-    int slices = 0;
+    int slices = 0;             // digit slices, or the CRT form's moduli count
+    int crt = 0;                // 1: the CRT form (residues mod `slices` moduli, crt_t-bit integers)
+    int crt_t = 0;
     bool pair_form = false;
     int64_t row_tile = 0;       // rows of one slice GEMM output tile (256 for CTA pairs, 128 else)
     int tri = 0;                // op(A) zero outside its lower (1) / upper (2) triangle: zero k blocks skipped
@@ -235,16 +237,25 @@ int dgemv_dev(int trans, int64_t m, int64_t n, double alpha, const double* a,
 int dgemm_mode();
 int ozaki_slices();
 // Scoped per-thread dgemm mode (restored on destruction).
+// Form of the Ozaki products (0: digit slices, 1: CRT residues), process-wide
+// (gb_set_dgemm_mode) with a per-thread override.
+int ozaki_form();
+// CRT form: integer bits t of the scaled operands for n moduli and depth k
+// (the largest t with k 2^(2t) <= 8 M / 17), or -1; the smallest n whose t
+// reaches `bits`, or -1; the digit count of equal precision (grouped batch).
+int ozaki_crt_bits(int n, int64_t k);
+int ozaki_crt_moduli_for_bits(int bits, int64_t k);
+int ozaki_digit_slices();
 // Records the slice count of an Ozaki product on the calling thread
 // (gb_last_ozaki_slices); 0 when a gemm's product ran on the native kernel.
 void note_ozaki_slices(int slices);
 class ModeOverride {
 public:
-    ModeOverride(int mode, int slices);
+    ModeOverride(int mode, int slices, int form = -1);
     ~ModeOverride();
 
 private:
-    int mode_, slices_;
+    int mode_, slices_, form_;
 };
 
 }  // namespace gb

@@ -57,6 +57,7 @@ constexpr uint32_t OZ_TMEM_COLS = 512;  // two 128x256 fp32 accumulators
 constexpr int OZ_SMEM_BYTES = OZ_STAGES * OZ_STAGE_BYTES + 1024 + 256;
 constexpr int OZ_CHUNK_KB = 16;  // 16 k-blocks of 64 = 1024 products per exact fp32 chunk
 constexpr int OZ_MAX_SLICES = 12;
+constexpr int OZ_MAX_LEVELS = 16;  // level tables: the digit form's s levels or the CRT form's moduli
 constexpr int OZ_GROUP_M = 16;
 
 struct OzLevel {
@@ -86,7 +87,7 @@ struct OzGemmParams {
     int out_tri = 0, tiles_valid = 0;
     const int* tile_cum = nullptr;
     const int* tile_first = nullptr;
-    OzLevel lv[OZ_MAX_SLICES];
+    OzLevel lv[OZ_MAX_LEVELS];
 };
 
 struct OzItem {
@@ -139,7 +140,7 @@ struct OzBatchParams {
     unsigned int* status;
     const int* skip;
     unsigned long long* counter;
-    OzLevel lv[OZ_MAX_SLICES];
+    OzLevel lv[OZ_MAX_LEVELS];
 };
 
 constexpr int OZ_IRING = 4;  // work-item ring depth (dynamic form)
@@ -1189,7 +1190,7 @@ struct OzRecombParams {
     int64_t rs_c, cs_c;
     const int* skip;
     int out_tri = 0, out_rpc = 1;  // only C's stored triangle is read and written (as OzA::out_tri)
-    OzLevel lv[OZ_MAX_SLICES];
+    OzLevel lv[OZ_MAX_LEVELS];
 };
 
 // Thread per 4 consecutive rows of one column: all S level planes are
@@ -1489,6 +1490,175 @@ __global__ void __launch_bounds__(256) oz_recombine_batch_kernel(const OzBatchPr
     }
 }
 
+// ---------------------------------------------------------------- CRT form
+// The second precision form (Ozaki, Uchino & Imamura, "Ozaki scheme II", 2025,
+// restated here with bf16 residues): every row of op(A) and of op(B)^T is
+// scaled to integers, X = RNE(|x| 2^(t+1-e)) with the sign of x (|X| <= 2^t,
+// e the row exponent of the digit form), so A'B' is an exact integer matrix
+// with |C'| <= k 2^(2t).  For N pairwise coprime moduli p_l <= 257 with
+// product M > 2 (17/16) k 2^(2t), the N products (A' mod p_l)(B' mod p_l)
+// (symmetric residues, |r| <= 128: exact in bf16, products <= 2^14 as for
+// the digits) determine C' by the Chinese remainder theorem.  N products
+// replace the digit form's s(s+1)/2: at k = 16384, N = 16 gives t = 55,
+// the representation error of s = 7 digits (28 products).
+//
+// Split: X's bytes b_q, s_l = sum_q b_q (2^(8q) mod p_l) < 2^19 (exact in
+// fp32), r_l = s_l - p_l rint(s_l / p_l) (exact: |s_l / p_l - half integer|
+// >= 1/514 dwarfs the fp32 error).  Recombination: the int32 products c_l
+// reduced to symmetric residues, C' = sum_l r_l W_l - Q M in 128-bit
+// two's-complement arithmetic (W_l the CRT weights, symmetric mod M), with
+// Q = rint(sum_l r_l (W_l / M)) in fp32 (error below 2^-9 while
+// |C'/M| < 0.471); then one RNE conversion of C' 2^(e_i + e_j - 2t - 2).
+constexpr int OZC_MAX = 16;
+
+struct OzCrtTab {
+    int n, t;
+    float p[OZC_MAX], invp[OZC_MAX], wm[OZC_MAX];
+    float pw[OZC_MAX][8];                           // 2^(8q) mod p_l
+    unsigned long long wlo[OZC_MAX], whi[OZC_MAX];  // W_l as a 128-bit two's-complement integer
+    unsigned long long mlo, mhi;                    // M
+};
+
+// |x| 2^(t+1-e), rounded to the nearest integer (ties to even), from the bits.
+__device__ __forceinline__ unsigned long long oz_crt_scaled(unsigned long long bits, int e, int t)
+{
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    const unsigned long long M = (bits & ((1ull << 52) - 1)) | (ex ? (1ull << 52) : 0ull);
+    if (M == 0) return 0ull;
+    const int E2 = ex ? ex - 1075 : -1074;
+    const int sh = E2 + t + 1 - e;
+    if (sh >= 0) return M << sh;  // |x| 2^(t+1-e) < 2^t
+    if (sh < -54) return 0ull;    // below half a unit
+    const int r = -sh;
+    const unsigned long long q = M >> r, rem = M & ((1ull << r) - 1), half = 1ull << (r - 1);
+    return (rem > half || (rem == half && (q & 1ull))) ? q + 1 : q;
+}
+
+// The N residues of x as floats (integers, |r| <= 128).
+template <int N>
+__device__ __forceinline__ void oz_crt_residues(double x, int e, const OzCrtTab& tab, float (&r)[N])
+{
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long X = oz_crt_scaled(bits & 0x7FFFFFFFFFFFFFFFull, e, tab.t);
+    float b[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)  // byte q of X as a float: its bits OR-ed into 2^23, minus 2^23
+        b[q] = __uint_as_float(0x4B000000u | (uint32_t)((X >> (8 * q)) & 255u)) - 8388608.0f;
+    const bool neg = (bits >> 63) != 0;
+#pragma unroll
+    for (int l = 0; l < N; ++l) {
+        float sl = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) sl = __fmaf_rn(b[q], tab.pw[l][q], sl);
+        const float rr = __fmaf_rn(-rintf(__fmul_rn(sl, tab.invp[l])), tab.p[l], sl);
+        r[l] = neg ? -rr : rr;
+    }
+}
+
+// Tile of 32 rows x 64 k per block (as oz_split_kernel); writes N bf16
+// residue planes, K-major, zero in the padding.
+template <int N>
+__global__ void __launch_bounds__(256) oz_crt_split_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
+                                                           int64_t sr, int64_t sl,
+                                                           const unsigned long long* __restrict__ maxbits,
+                                                           int64_t rpad, int64_t kpad, uint16_t* __restrict__ out,
+                                                           int32_t* __restrict__ exps, int* __restrict__ nonfinite,
+                                                           const __grid_constant__ OzCrtTab tab)
+{
+    __shared__ double tile[32][65];
+    const int64_t l0 = (int64_t)blockIdx.x * 64, r0 = (int64_t)blockIdx.y * 32;
+    const bool rows_fast = (sr == 1);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int e = threadIdx.x + 256 * q;
+        const int rr = rows_fast ? (e & 31) : (e >> 6);
+        const int ll = rows_fast ? (e >> 5) : (e & 63);
+        const int64_t r = r0 + rr, l = l0 + ll;
+        tile[rr][ll] = (r < rows && l < k) ? __ldcs(R + r * sr + l * sl) : 0.0;
+    }
+    __syncthreads();
+    const int rr = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 8;
+    const int64_t r = r0 + rr;
+    int e = 0;
+    if (r < rows) {
+        int nf = 0;
+        e = oz_row_exponent(maxbits[r], &nf);
+        if (nf) *nonfinite = 1;
+        if (blockIdx.x == 0 && (threadIdx.x & 7) == 0) exps[r] = e;
+    }
+    uint32_t packed[N][4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        float f0[N], f1[N];
+        oz_crt_residues<N>(r < rows ? tile[rr][c0 + 2 * h] : 0.0, e, tab, f0);
+        oz_crt_residues<N>(r < rows ? tile[rr][c0 + 2 * h + 1] : 0.0, e, tab, f1);
+#pragma unroll
+        for (int l = 0; l < N; ++l)
+            packed[l][h] = __byte_perm(__float_as_uint(f0[l]), __float_as_uint(f1[l]), 0x7632);
+    }
+#pragma unroll
+    for (int l = 0; l < N; ++l) {
+        uint4* dst = reinterpret_cast<uint4*>(out + ((int64_t)l * rpad + r) * kpad + l0 + c0);
+        *dst = make_uint4(packed[l][0], packed[l][1], packed[l][2], packed[l][3]);
+    }
+}
+
+// Thread per 4 consecutive rows of one column, as oz_recombine_kernel: the
+// N product planes (one part each), CRT into 128 bits, one rounding.
+template <int N>
+__global__ void __launch_bounds__(256, (N <= 12 ? 2 : 1)) oz_crt_recombine_kernel(const __grid_constant__ OzRecombParams p,
+                                                                  const __grid_constant__ OzCrtTab tab)
+{
+    if (*p.skip) return;
+    const int64_t mq = (p.m + 3) >> 2;
+    const int64_t total = mq * p.n;
+    const bool plain = (p.alpha == 1.0 && p.beta == 0.0);
+    const int64_t plane_stride = p.npad * p.mpad;
+    const unsigned __int128 Mm = ((unsigned __int128)tab.mhi << 64) | tab.mlo;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = e / mq, i0 = (e - j * mq) * 4;
+        const int64_t dlo = (int64_t)p.out_rpc * j, dhi = dlo + p.out_rpc - 1;
+        if (p.out_tri && (p.out_tri == 1 ? i0 + 3 < dlo : i0 > dhi)) continue;
+        const int64_t off = j * p.mpad + i0;
+        int4 v[N];
+#pragma unroll
+        for (int L = 0; L < N; ++L)
+            v[L] = __ldcs(reinterpret_cast<const int4*>(p.planes + (int64_t)p.lv[L].plane_base * plane_stride + off));
+        const int ebj = p.eb[j] - 2 * tab.t - 2;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int64_t i = i0 + r;
+            if (i >= p.m) break;
+            if (p.out_tri && (p.out_tri == 1 ? i < dlo : i > dhi)) continue;
+            unsigned __int128 acc = 0;
+            float qf = 0.0f;
+#pragma unroll
+            for (int L = 0; L < N; ++L) {
+                const int c = (r == 0) ? v[L].x : (r == 1) ? v[L].y : (r == 2) ? v[L].z : v[L].w;
+                const int pl = (int)tab.p[L];
+                // symmetric residue of c: an fp32 quotient is off by at most one
+                int rr = c - __float2int_rn(__fmul_rn((float)c, tab.invp[L])) * pl;
+                if (2 * rr > pl) rr -= pl;
+                else if (2 * rr < -pl) rr += pl;
+                const unsigned __int128 w = ((unsigned __int128)tab.whi[L] << 64) | tab.wlo[L];
+                acc += (unsigned __int128)(__int128)rr * w;
+                qf = __fmaf_rn((float)rr, tab.wm[L], qf);
+            }
+            const long long Q = __float2ll_rn(qf);
+            const __int128 C = (__int128)(acc - (unsigned __int128)((__int128)Q * (__int128)Mm));
+            const double ab = round_scaled(C, p.ea[i] + ebj);
+            double* cij = p.c + i * p.rs_c + j * p.cs_c;
+            if (plain) {
+                *cij = ab;
+            } else {
+                const double t = __dmul_rn(p.alpha, ab);
+                *cij = (p.beta == 0.0) ? t : __fma_rn(p.beta, *cij, t);
+            }
+        }
+    }
+}
+
 void launch_recombine(int slices, const OzRecombParams& r, unsigned blocks, cudaStream_t s)
 {
     switch (slices) {
@@ -1498,6 +1668,105 @@ void launch_recombine(int slices, const OzRecombParams& r, unsigned blocks, cuda
         GB_RECOMB_CASE(7) GB_RECOMB_CASE(8) GB_RECOMB_CASE(9) GB_RECOMB_CASE(10) GB_RECOMB_CASE(11)
         GB_RECOMB_CASE(12)
 #undef GB_RECOMB_CASE
+    default: break;
+    }
+}
+
+// Moduli of the CRT form, largest first: pairwise coprime (257, 251, 241, 239,
+// 233, 229, 227, 223, 211, 199, 197 prime; 256 = 2^8, 255 = 3 5 17,
+// 253 = 11 23, 247 = 13 19, 217 = 7 31), each at most 257 so that a
+// symmetric residue has |r| <= 128.
+constexpr int OZC_MODULI[OZC_MAX] = {257, 256, 255, 253, 251, 247, 241, 239, 233, 229, 227, 223, 217, 211, 199, 197};
+
+using u128 = unsigned __int128;
+
+u128 crt_modulus(int n)
+{
+    u128 M = 1;
+    for (int l = 0; l < n; ++l) M *= (u128)OZC_MODULI[l];
+    return M;
+}
+
+int modinv_small(int a, int p)
+{
+    // a^-1 mod p for gcd(a, p) = 1, extended Euclid on small integers
+    int t = 0, nt = 1, r = p, nr = a % p;
+    while (nr != 0) {
+        const int q = r / nr, tt = t - q * nt, tr = r - q * nr;
+        t = nt;
+        nt = tt;
+        r = nr;
+        nr = tr;
+    }
+    return t < 0 ? t + p : t;
+}
+
+void crt_table(int n, int t, OzCrtTab* tab)
+{
+    *tab = OzCrtTab();
+    tab->n = n;
+    tab->t = t;
+    const u128 M = crt_modulus(n);
+    for (int l = 0; l < n; ++l) {
+        const int pl = OZC_MODULI[l];
+        const u128 Ml = M / (u128)pl;
+        const int inv = modinv_small((int)(Ml % (u128)pl), pl);
+        u128 W = (Ml * (u128)inv) % M;  // W = 1 mod p_l, 0 mod the others
+        __int128 Ws = (W > M / 2) ? (__int128)W - (__int128)M : (__int128)W;
+        const u128 Wu = (u128)Ws;
+        tab->wlo[l] = (unsigned long long)Wu;
+        tab->whi[l] = (unsigned long long)(Wu >> 64);
+        tab->wm[l] = (float)((double)Ws / (double)M);
+        tab->p[l] = (float)pl;
+        tab->invp[l] = 1.0f / (float)pl;
+        int pw = 1 % pl;
+        for (int q = 0; q < 8; ++q) {
+            tab->pw[l][q] = (float)pw;
+            pw = (pw * 256) % pl;
+        }
+    }
+    tab->mlo = (unsigned long long)M;
+    tab->mhi = (unsigned long long)(M >> 64);
+}
+
+template <int N>
+void launch_crt_split(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl, const unsigned long long* mb,
+                      int64_t rpad, int64_t rcover, int64_t kpad, uint16_t* out, int32_t* ex, int* nonfinite,
+                      const OzCrtTab& tab, cudaStream_t s)
+{
+    LaunchScope ls("oz_split_crt", s);
+    oz_crt_split_kernel<N><<<dim3((unsigned)(kpad / 64), (unsigned)(rcover / 32)), 256, 0, s>>>(
+        rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, tab);
+}
+
+template <int N>
+void launch_crt_recombine(const OzRecombParams& r, const OzCrtTab& tab, unsigned blocks, cudaStream_t s)
+{
+    oz_crt_recombine_kernel<N><<<blocks, 256, 0, s>>>(r, tab);
+}
+
+#define GB_CRT_CASES(X) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16)
+
+void crt_split_dispatch(int n, int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl,
+                        const unsigned long long* mb, int64_t rpad, int64_t rcover, int64_t kpad, uint16_t* out,
+                        int32_t* ex, int* nonfinite, const OzCrtTab& tab, cudaStream_t s)
+{
+    switch (n) {
+#define GB_CRT_SPLIT(N) \
+    case N: launch_crt_split<N>(rows, k, R, sr, sl, mb, rpad, rcover, kpad, out, ex, nonfinite, tab, s); break;
+        GB_CRT_CASES(GB_CRT_SPLIT)
+#undef GB_CRT_SPLIT
+    default: break;
+    }
+}
+
+void crt_recombine_dispatch(int n, const OzRecombParams& r, const OzCrtTab& tab, unsigned blocks, cudaStream_t s)
+{
+    switch (n) {
+#define GB_CRT_RECOMB(N) \
+    case N: launch_crt_recombine<N>(r, tab, blocks, s); break;
+        GB_CRT_CASES(GB_CRT_RECOMB)
+#undef GB_CRT_RECOMB
     default: break;
     }
 }
@@ -1680,6 +1949,18 @@ void split_operand(int slices, int64_t rows, int64_t k, const double* R, int64_t
     split_dispatch(slices, rows, k, R, sr, sl, mb, rpad, rcover, kpad, out, ex, nonfinite, s);
 }
 
+// The CRT form's split of one row operand: row maxima, then the residues.
+void crt_split_operand(int n, int t, int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl,
+                       unsigned long long* mb, int64_t rpad, int64_t rcover, int64_t kpad, uint16_t* out, int32_t* ex,
+                       int* nonfinite, cudaStream_t s)
+{
+    OzCrtTab tab;
+    crt_table(n, t, &tab);
+    cudaMemsetAsync(mb, 0, sizeof(unsigned long long) * rows, s);
+    launch_rowmax(rows, k, R, sr, sl, mb, s);
+    crt_split_dispatch(n, rows, k, R, sr, sl, mb, rpad, rcover, kpad, out, ex, nonfinite, tab, s);
+}
+
 }  // namespace
 
 // Largest K of one part of a level with `npairs` slice products:
@@ -1774,14 +2055,47 @@ int slice_gemm_setup(int* max_pairs)
 // multiplications.  The Inf/NaN flag lives here and is shared by them.
 // ozaki_alloc_a sets up the arena; ozaki_split_a_rows splits a block of rows
 // (several blocks may be split as they arrive); ozaki_prepare_a does both.
+int ozaki_crt_bits(int n, int64_t k)
+{
+    if (n < 2 || n > OZC_MAX || k < 1) return -1;
+    const u128 M = crt_modulus(n);
+    const u128 lim = (M / 17) * 8 + ((M % 17) * 8) / 17;  // floor(8 M / 17): M > 2 (17/16) k 2^(2t)
+    int kb = 0;
+    while (kb < 63 && ((int64_t)1 << kb) < k) ++kb;  // k <= 2^kb
+    for (int t = 62; t >= 1; --t) {
+        if (2 * t + kb > 126) continue;
+        if (((u128)k << (2 * t)) <= lim) return t;
+    }
+    return -1;
+}
+
+int ozaki_crt_moduli_for_bits(int bits, int64_t k)
+{
+    for (int n = 2; n <= OZC_MAX; ++n)
+        if (ozaki_crt_bits(n, k) >= bits) return n;
+    return -1;
+}
+
 int ozaki_alloc_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t acs, int slices, cudaStream_t s,
                   OzA* A)
 {
     *A = OzA();
-    if (slices < 2 || slices > OZ_MAX_SLICES)
-        return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices must be in [2, 12]");
-    if (ozaki_t_bound_log2(slices, k) >= 126.0)
-        return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices and k exceed the 128-bit recombination range");
+    if (ozaki_form() == 1) {
+        // CRT form: `slices` moduli, one product (one int32 part) each
+        if (slices < 2 || slices > OZC_MAX)
+            return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "moduli must be in [2, 16]");
+        A->crt_t = ozaki_crt_bits(slices, k);
+        if (A->crt_t < 1)
+            return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "too few moduli for this k");
+        if (round_up(k, OZ_BK) > ozaki_kpart_limit(1))
+            return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "k beyond the CRT form's one-part limit");
+        A->crt = 1;
+    } else {
+        if (slices < 2 || slices > OZ_MAX_SLICES)
+            return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices must be in [2, 12]");
+        if (ozaki_t_bound_log2(slices, k) >= 126.0)
+            return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices and k exceed the 128-bit recombination range");
+    }
     A->pair_form = (ozaki_ctas_setting() == 2);
     A->row_tile = A->pair_form ? 2 * OZ2_ROWS : OZ_BM;
     A->slices = slices;
@@ -1813,8 +2127,12 @@ int ozaki_split_a_rows(const OzA* A, int64_t r0, int64_t r1, cudaStream_t s)
     if (r0 < 0 || r1 > A->m || r0 >= r1 || r0 % A->row_tile || (r1 != A->m && r1 % A->row_tile))
         return set_error(GB_ERR_ARG, "ozaki", "row block not aligned to the slice GEMM tile");
     const int64_t cover = (r1 == A->m ? A->mpad : r1) - r0;
-    split_operand(A->slices, r1 - r0, A->k, A->a + r0 * A->ars, A->ars, A->acs, A->maxa + r0, A->mpad, cover,
-                  A->kpad, A->sa + r0 * A->kpad, A->ea + r0, A->nonfinite, s);
+    if (A->crt)
+        crt_split_operand(A->slices, A->crt_t, r1 - r0, A->k, A->a + r0 * A->ars, A->ars, A->acs, A->maxa + r0,
+                          A->mpad, cover, A->kpad, A->sa + r0 * A->kpad, A->ea + r0, A->nonfinite, s);
+    else
+        split_operand(A->slices, r1 - r0, A->k, A->a + r0 * A->ars, A->ars, A->acs, A->maxa + r0, A->mpad, cover,
+                      A->kpad, A->sa + r0 * A->kpad, A->ea + r0, A->nonfinite, s);
     return check_cuda(cudaGetLastError(), "oz_split");
 }
 
@@ -1861,7 +2179,12 @@ int ozaki_prepare_b(const OzA* A, int64_t n, const double* b, int64_t brs, int64
     int rc = ozaki_alloc_b(A, n, b, brs, bcs, s, B);
     if (rc) return rc;
     // rows of op(B)^T: (j, l) = b[l*brs + j*bcs]
-    split_operand(A->slices, n, A->k, b, bcs, brs, B->maxb, B->npad, B->npad, A->kpad, B->sb, B->eb, A->nonfinite, s);
+    if (A->crt)
+        crt_split_operand(A->slices, A->crt_t, n, A->k, b, bcs, brs, B->maxb, B->npad, B->npad, A->kpad, B->sb,
+                          B->eb, A->nonfinite, s);
+    else
+        split_operand(A->slices, n, A->k, b, bcs, brs, B->maxb, B->npad, B->npad, A->kpad, B->sb, B->eb,
+                      A->nonfinite, s);
     rc = check_cuda(cudaGetLastError(), "oz_split");
     if (rc) ozaki_release_b(B, s);
     return rc;
@@ -1967,7 +2290,19 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
                                      : (int64_t)p.tiles_m * p.tiles_n;
     int planes_total = 0;
     int64_t items = 0;
-    for (int L = 0; L < slices; ++L) {  // heaviest level (most pairs) first
+    for (int L = 0; L < slices && A->crt; ++L) {  // CRT form: modulus L + 1 is A_(L+1) B_(L+1)^T alone
+        OzLevel& lv = p.lv[L];
+        lv.lev = 2 * (L + 1);
+        lv.pa_lo = L + 1;
+        lv.npairs = 1;
+        lv.nparts = 1;
+        lv.kb_per_part = kb_total;
+        lv.plane_base = planes_total;
+        lv.item_base = items;
+        planes_total += 1;
+        items += tiles;
+    }
+    for (int L = 0; L < slices && !A->crt; ++L) {  // heaviest level (most pairs) first
         OzLevel& lv = p.lv[L];
         lv.lev = slices + 1 - L;
         lv.pa_lo = (lv.lev - slices > 1) ? lv.lev - slices : 1;
@@ -2068,7 +2403,13 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
         int64_t blocks = (total + 255) / 256;
         if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
         LaunchScope ls("oz_recombine", s);
-        launch_recombine(slices, r, (unsigned)blocks, s);
+        if (A->crt) {
+            OzCrtTab tab;
+            crt_table(slices, A->crt_t, &tab);
+            crt_recombine_dispatch(slices, r, tab, (unsigned)blocks, s);
+        } else {
+            launch_recombine(slices, r, (unsigned)blocks, s);
+        }
     }
     if ((rc = check_cuda(cudaGetLastError(), "oz_recombine"))) return bail(rc);
     // IEEE path for non-finite operands: runs only when a split raised the flag
@@ -2152,7 +2493,7 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     if (alpha == 0.0 || k <= 0) return scal_matrix(m, n, beta, c, rs_c, cs_c, s);
     OzA A;
     int rc;
-    if (k > fused_split_max_k()) {
+    if (k > fused_split_max_k() || ozaki_form() == 1) {  // the CRT form always splits in two passes
         if ((rc = ozaki_prepare_a(m, k, a, ars, acs, slices, s, &A))) return rc;
         rc = ozaki_multiply(&A, n, b, brs, bcs, alpha, beta, c, rs_c, cs_c, s);
         ozaki_release_a(&A, s);

@@ -29,6 +29,7 @@ std::atomic<int64_t> g_trsv_withhold{-1};
 std::atomic<int> g_timing{0};
 int g_dgemm_mode = GB_DGEMM_NATIVE;
 int g_ozaki_slices = 8;
+int g_ozaki_form = 0;
 
 thread_local int t_err = GB_SUCCESS;
 thread_local char t_msg[512] = {0};
@@ -171,21 +172,33 @@ int read_and_clear_device_status(cudaStream_t s, const char* where)
 
 // A per-call form (gb_dgemm_ozaki) overrides the process-wide mode on the
 // calling thread for the duration of the call.
-thread_local int t_mode = -1, t_slices = -1;
+thread_local int t_mode = -1, t_slices = -1, t_form = -1;
 
 int dgemm_mode() { return t_mode >= 0 ? t_mode : g_dgemm_mode; }
 int ozaki_slices() { return t_slices >= 0 ? t_slices : g_ozaki_slices; }
+int ozaki_form() { return t_form >= 0 ? t_form : g_ozaki_form; }
 
-ModeOverride::ModeOverride(int mode, int slices) : mode_(t_mode), slices_(t_slices)
+int ozaki_digit_slices()
+{
+    const int sl = ozaki_slices();
+    if (ozaki_form() != 1 || sl < 2) return sl;
+    const int t = ozaki_crt_bits(sl, 16384);
+    int d = (t + 1) / 8;
+    return d < 2 ? 2 : (d > 12 ? 12 : d);
+}
+
+ModeOverride::ModeOverride(int mode, int slices, int form) : mode_(t_mode), slices_(t_slices), form_(t_form)
 {
     t_mode = mode;
     t_slices = slices;
+    if (form >= 0) t_form = form;
 }
 
 ModeOverride::~ModeOverride()
 {
     t_mode = mode_;
     t_slices = slices_;
+    t_form = form_;
 }
 
 unsigned long long trsv_wait_budget_ns() { return g_trsv_wait_ns.load(std::memory_order_relaxed); }
@@ -232,12 +245,18 @@ int gb_init(int device)
 
 int gb_set_dgemm_mode(int mode, int slices)
 {
-    if (mode != GB_DGEMM_NATIVE && mode != GB_DGEMM_OZAKI)
-        return gb::set_error(GB_ERR_ARG, "gb_set_dgemm_mode", "mode must be GB_DGEMM_NATIVE or GB_DGEMM_OZAKI");
+    if (mode != GB_DGEMM_NATIVE && mode != GB_DGEMM_OZAKI && mode != GB_DGEMM_OZAKI_CRT)
+        return gb::set_error(GB_ERR_ARG, "gb_set_dgemm_mode",
+                             "mode must be GB_DGEMM_NATIVE, GB_DGEMM_OZAKI or GB_DGEMM_OZAKI_CRT");
     if (mode == GB_DGEMM_OZAKI && slices != 0 && (slices < 2 || slices > 12))
         return gb::set_error(GB_ERR_ARG, "gb_set_dgemm_mode", "slices must be 0 (automatic) or in [2, 12]");
-    gb::g_dgemm_mode = mode;
-    if (mode == GB_DGEMM_OZAKI) gb::g_ozaki_slices = slices;
+    if (mode == GB_DGEMM_OZAKI_CRT && slices != 0 && (slices < 2 || slices > 16))
+        return gb::set_error(GB_ERR_ARG, "gb_set_dgemm_mode", "moduli must be 0 (automatic) or in [2, 16]");
+    gb::g_dgemm_mode = (mode == GB_DGEMM_NATIVE) ? GB_DGEMM_NATIVE : GB_DGEMM_OZAKI;
+    if (mode != GB_DGEMM_NATIVE) {
+        gb::g_ozaki_slices = slices;
+        gb::g_ozaki_form = (mode == GB_DGEMM_OZAKI_CRT) ? 1 : 0;
+    }
     return GB_SUCCESS;
 }
 

@@ -42,6 +42,15 @@ def dgemm_ozaki(transa, transb, alpha, a, b, beta, c, slices=8):
     return _lib.check(rc, "gb_dgemm_ozaki_dev")
 
 
+def dgemm_ozaki_crt(transa, transb, alpha, a, b, beta, c, moduli=16):
+    """The CRT form of the Ozaki product: `moduli` residue products."""
+    m, n = c.shape
+    rc = _lib.load().gb_dgemm_ozaki_crt_dev(transa, transb, m, n, _k(transa, a), alpha, a.data_ptr(),
+                                            *_rc(a), b.data_ptr(), *_rc(b), beta, c.data_ptr(), *_rc(c),
+                                            moduli, _stream())
+    return _lib.check(rc, "gb_dgemm_ozaki_crt_dev")
+
+
 def sgemm(transa, transb, alpha, a, b, beta, c):
     m, n = c.shape
     rc = _lib.load().gb_sgemm_dev(transa, transb, m, n, _k(transa, a), alpha, a.data_ptr(), *_rc(a),

@@ -501,6 +501,16 @@ int gb_dgemm_ozaki_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_
                        gb_inc_t cs_a, const double* b, gb_inc_t rs_b, gb_inc_t cs_b,
                        double beta, double* c, gb_inc_t rs_c, gb_inc_t cs_c, int slices,
                        void* stream);
+/* The CRT form of the Ozaki product (no reference counterpart): `moduli` bf16
+   residue products (2..16) instead of the digit form's s(s+1)/2; the operands
+   are scaled to t-bit integers, t = the largest with k 2^(2t) <= 8 M / 17 for
+   the product M of the moduli (t = 55 for 16 moduli at k = 16384), and the
+   result is the single rounding of their exact integer product.  k must be at
+   most 131072. */
+int gb_dgemm_ozaki_crt_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
+                           double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
+                           gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c,
+                           gb_inc_t cs_c, int moduli, void* stream);
 
 int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
                  float alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a,
@@ -774,6 +784,13 @@ int gb_init(int device);
    the error-bound verifier (the native kernel when no count reaches it). */
 #define GB_DGEMM_NATIVE 0
 #define GB_DGEMM_OZAKI 1
+/* The CRT form of the Ozaki products (no reference counterpart): `slices` is
+   the number of moduli N (2..16, or 0 for the count whose precision matches
+   the digit count the selector and verifier choose); N bf16 residue products
+   replace the digit form's s(s+1)/2 (N = 16 at k = 16384 carries the 55-bit
+   operands of s = 7 digits).  The grouped batch keeps the digit form at the
+   slice count of equal precision. */
+#define GB_DGEMM_OZAKI_CRT 2
 int gb_set_dgemm_mode(int mode, int slices);
 
 /* Engine of the Ozaki slice products: 1 = one CTA per 128x256 tile,

@@ -776,6 +776,127 @@ static void oz_task(void* p, int tid, int nt)
     }
 }
 
+/* ---------------------------------------------------------------------- */
+/* The CRT form of the Ozaki products, as a model of exact integers.       */
+/* Each row of op(A) and of op(B)^T is scaled to integers                  */
+/* X = RNE(|x| 2^(t+1-e)) with the sign of x (e = ilogb(row max) + 2, as   */
+/* the digit form), C' = sum_l A'(i,l) B'(l,j) exactly, and the result is  */
+/* RNE(C' 2^(e_i + e_j - 2t - 2)), then alpha and beta as in the digit     */
+/* form.  t is the largest integer with k 2^(2t) <= floor(8 M / 17) for    */
+/* the product M of the first n moduli (and 2t + ceil(log2 k) <= 126):     */
+/* the device computes C' from n residue products by the Chinese           */
+/* remainder theorem, which is exact under that bound, so the model needs  */
+/* no moduli beyond choosing t.                                            */
+static const int orc_crt_moduli[16] = {257, 256, 255, 253, 251, 247, 241, 239,
+                                       233, 229, 227, 223, 217, 211, 199, 197};
+
+int orc_ozaki_crt_bits(int n, int64_t k)
+{
+    if (n < 2 || n > 16 || k < 1) return -1;
+    u128 M = 1;
+    for (int l = 0; l < n; ++l) M *= (u128)orc_crt_moduli[l];
+    const u128 lim = (M / 17) * 8 + ((M % 17) * 8) / 17;
+    int kb = 0;
+    while (kb < 63 && ((int64_t)1 << kb) < k) ++kb;
+    for (int t = 62; t >= 1; --t) {
+        if (2 * t + kb > 126) continue;
+        if (((u128)k << (2 * t)) <= lim) return t;
+    }
+    return -1;
+}
+
+static int64_t crt_scaled(double x, int e, int t)
+{
+    uint64_t bits;
+    memcpy(&bits, &x, sizeof bits);
+    const int neg = (int)(bits >> 63);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    const uint64_t M = (bits & ((1ull << 52) - 1)) | (ex ? (1ull << 52) : 0ull);
+    if (M == 0) return 0;
+    const int E2 = ex ? ex - 1075 : -1074;
+    const int sh = E2 + t + 1 - e;
+    uint64_t X;
+    if (sh >= 0) {
+        X = M << sh;
+    } else if (sh < -54) {
+        X = 0;
+    } else {
+        const int r = -sh;
+        const uint64_t q = M >> r, rem = M & ((1ull << r) - 1), half = 1ull << (r - 1);
+        X = (rem > half || (rem == half && (q & 1ull))) ? q + 1 : q;
+    }
+    return neg ? -(int64_t)X : (int64_t)X;
+}
+
+static void crt_scale_rows(int64_t rows, int64_t k, const double* r, int64_t rs, int64_t cs, int t,
+                           int32_t* exps, int64_t* X)
+{
+    for (int64_t i = 0; i < rows; ++i) {
+        double mx = 0.0;
+        for (int64_t l = 0; l < k; ++l) { double v = fabs(r[i * rs + l * cs]); if (v > mx) mx = v; }
+        const int e = (mx == 0.0) ? 0 : ilogb(mx) + 2;
+        exps[i] = e;
+        for (int64_t l = 0; l < k; ++l) X[i * k + l] = crt_scaled(r[i * rs + l * cs], e, t);
+    }
+}
+
+typedef struct {
+    int64_t m, n, k; int t; const int64_t* xa; const int64_t* xb;
+    const int32_t* ea; const int32_t* eb; double alpha, beta;
+    double* c; int64_t rs_c, cs_c;
+} crt_args;
+
+static void crt_task(void* p, int tid, int nt)
+{
+    crt_args* g = (crt_args*)p;
+    for (int64_t i = tid; i < g->m; i += nt) {
+        for (int64_t j = 0; j < g->n; ++j) {
+            const int64_t* ra = g->xa + i * g->k;
+            const int64_t* rb = g->xb + j * g->k;
+            i128 T = 0;
+            for (int64_t l = 0; l < g->k; ++l) T += (i128)ra[l] * (i128)rb[l];
+            const double ab = oz_round_scaled(T, g->ea[i] + g->eb[j] - 2 * g->t - 2);
+            double* cij = g->c + i * g->rs_c + j * g->cs_c;
+            if (g->alpha == 1.0 && g->beta == 0.0) { *cij = ab; continue; }
+            const double tt = g->alpha * ab;
+            *cij = (g->beta == 0.0) ? tt : fma(g->beta, *cij, tt);
+        }
+    }
+}
+
+int orc_ozaki_crt_dgemm(int transa, int transb, int64_t m, int64_t n, int64_t k,
+                        double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+                        const double* b, int64_t rs_b, int64_t cs_b,
+                        double beta, double* c, int64_t rs_c, int64_t cs_c,
+                        int moduli, int nthreads)
+{
+    if (m <= 0 || n <= 0) return 0;
+    if (alpha == 0.0 || k <= 0) { d_scalm(m, n, beta, c, rs_c, cs_c); return 0; }
+    const int t = orc_ozaki_crt_bits(moduli, k);
+    if (t < 1) return -1;
+    const int64_t ars = ORC_TRANS(transa) ? cs_a : rs_a, acs = ORC_TRANS(transa) ? rs_a : cs_a;
+    const int64_t brs = ORC_TRANS(transb) ? cs_b : rs_b, bcs = ORC_TRANS(transb) ? rs_b : cs_b;
+    for (int64_t i = 0; i < m; ++i) for (int64_t l = 0; l < k; ++l)
+        if (!isfinite(a[i * ars + l * acs])) goto native;
+    for (int64_t l = 0; l < k; ++l) for (int64_t j = 0; j < n; ++j)
+        if (!isfinite(b[l * brs + j * bcs])) goto native;
+    {
+        int64_t* xa = (int64_t*)malloc(sizeof(int64_t) * (size_t)m * k);
+        int64_t* xb = (int64_t*)malloc(sizeof(int64_t) * (size_t)n * k);
+        int32_t* ea = (int32_t*)malloc(sizeof(int32_t) * m);
+        int32_t* eb = (int32_t*)malloc(sizeof(int32_t) * n);
+        crt_scale_rows(m, k, a, ars, acs, t, ea, xa);
+        crt_scale_rows(n, k, b, bcs, brs, t, eb, xb);
+        crt_args g = { m, n, k, t, xa, xb, ea, eb, alpha, beta, c, rs_c, cs_c };
+        orc_parallel(crt_task, &g, nthreads < 1 ? 1 : nthreads);
+        free(xa); free(xb); free(ea); free(eb);
+        return 0;
+    }
+native:
+    orc_dgemm(transa, transb, m, n, k, alpha, a, rs_a, cs_a, b, rs_b, cs_b, beta, c, rs_c, cs_c, nthreads);
+    return 1;
+}
+
 int orc_ozaki_dgemm(int transa, int transb, int64_t m, int64_t n, int64_t k,
                     double alpha, const double* a, int64_t rs_a, int64_t cs_a,
                     const double* b, int64_t rs_b, int64_t cs_b,

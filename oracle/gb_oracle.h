@@ -117,6 +117,13 @@ void orc_dd_dotv(int64_t n, const double* x, int64_t incx, const double* y,
 int64_t orc_ozaki_kpart_limit(int npairs);
 void orc_ozaki_split(int64_t rows, int64_t k, const double* r, int64_t rs, int64_t cs,
                      int slices, int32_t* exps, int16_t* digits);
+/* the CRT form (integer bits t for n moduli and depth k; the model) */
+int orc_ozaki_crt_bits(int n, int64_t k);
+int orc_ozaki_crt_dgemm(int transa, int transb, int64_t m, int64_t n, int64_t k,
+                        double alpha, const double* a, int64_t rs_a, int64_t cs_a,
+                        const double* b, int64_t rs_b, int64_t cs_b,
+                        double beta, double* c, int64_t rs_c, int64_t cs_c,
+                        int moduli, int nthreads);
 int orc_ozaki_dgemm(int transa, int transb, int64_t m, int64_t n, int64_t k,
                     double alpha, const double* a, int64_t rs_a, int64_t cs_a,
                     const double* b, int64_t rs_b, int64_t cs_b,

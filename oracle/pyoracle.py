@@ -81,6 +81,12 @@ def lib():
         L.orc_ozaki_kpart_limit.argtypes = [C.c_int]
         L.orc_ozaki_split.argtypes = [_i64, _i64, C.c_void_p, _i64, _i64, C.c_int, C.c_void_p,
                                       C.c_void_p]
+        L.orc_ozaki_crt_bits.restype = C.c_int
+        L.orc_ozaki_crt_bits.argtypes = [C.c_int, _i64]
+        L.orc_ozaki_crt_dgemm.restype = C.c_int
+        L.orc_ozaki_crt_dgemm.argtypes = g + [C.c_double, C.c_void_p, _i64, _i64, C.c_void_p, _i64,
+                                              _i64, C.c_double, C.c_void_p, _i64, _i64, C.c_int,
+                                              C.c_int]
         L.orc_ozaki_dgemm.restype = C.c_int
         L.orc_ozaki_dgemm.argtypes = g + [C.c_double, C.c_void_p, _i64, _i64, C.c_void_p, _i64,
                                           _i64, C.c_double, C.c_void_p, _i64, _i64, C.c_int,
@@ -333,6 +339,19 @@ def ozaki_dgemm(transa, transb, alpha, a, b, beta, c, slices, nthreads=None):
     return lib().orc_ozaki_dgemm(transa, transb, m, n, k, alpha, _p(a), *_strides(a), _p(b),
                                  *_strides(b), beta, _p(c), *_strides(c), slices,
                                  nthreads or nthreads_default())
+
+
+def ozaki_crt_bits(moduli, k):
+    return lib().orc_ozaki_crt_bits(moduli, k)
+
+
+def ozaki_crt_dgemm(transa, transb, alpha, a, b, beta, c, moduli, nthreads=None):
+    """The CRT form's model: exact integer product of the scaled operands, one rounding."""
+    m, n = c.shape
+    k = a.shape[0] if transa & TRANSPOSE else a.shape[1]
+    return lib().orc_ozaki_crt_dgemm(transa, transb, m, n, k, alpha, _p(a), *_strides(a), _p(b),
+                                     *_strides(b), beta, _p(c), *_strides(c), moduli,
+                                     nthreads or nthreads_default())
 
 
 def componentwise_error(c, hi, lo):

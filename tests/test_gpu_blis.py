@@ -115,12 +115,18 @@ def test_blas_tests_through_seams(integ, tmp_path, prog):
     _check_blat(prog, SEAM_ROUTINES[prog], rc, summary, err)
     rep = bp.parse_report(err)
     assert rep is not None and rep["kernel_launches"] > 0, err[-2000:]
-    assert rep["gemm_gpu"] > 0 and rep["gemm_cpu_forwarded"] == 0, rep
-    if prog[0] in "dz":
-        assert rep["trsm_gpu"] > 0 and rep["trsm_cpu_forwarded"] == 0, rep
+    assert rep["gemm_cpu_forwarded"] == 0, rep
+    if prog == "dblat1":
+        assert rep["axpyv_gpu"] > 0 and rep["dotv_gpu"] > 0, rep
+    elif prog == "dblat2":
+        assert rep["gemv_gpu"] > 0, rep
     else:
-        # single and single-complex trsm are not on the GPU path: BLIS's own code runs them
-        assert rep["trsm_gpu"] == 0, rep
+        assert rep["gemm_gpu"] > 0, rep
+        if prog[0] in "dz":
+            assert rep["trsm_gpu"] > 0 and rep["trsm_cpu_forwarded"] == 0, rep
+        else:
+            # single and single-complex trsm are not on the GPU path: BLIS's own code runs them
+            assert rep["trsm_gpu"] == 0, rep
 
 
 @pytest.mark.parametrize("prog", sorted(INTERPOSED_ROUTINES))
