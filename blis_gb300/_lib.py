@@ -194,6 +194,7 @@ def load(path=None):
     _sig(L, "gb_dd_gemm_entries_dev", C.c_int, [C.c_int, C.c_int, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64,
                                                  _d, _vp, _i64, _i64, _i64, _vp, _vp, _vp, _vp, _vp])
     _sig(L, "gb_set_ozaki_ctas", C.c_int, [C.c_int])
+    _sig(L, "gb_set_sgemm_mode", C.c_int, [C.c_int])
     _sig(L, "gb_selector_load", C.c_int, [_vp, C.c_int])
     _sig(L, "gb_selector_load_file", C.c_int, [_cp])
     _sig(L, "gb_selector_unload", C.c_int, [])

@@ -345,6 +345,13 @@ def bli_ddotv(x, y, n=None, incx=1, incy=1):
 
 
 # ------------------------------------------------------------ controls
+SGEMM_FMA, SGEMM_SPLIT, SGEMM_AUTO = 0, 1, 2
+
+
+def set_sgemm_mode(mode):
+    return _lib.check(_lib.load().gb_set_sgemm_mode(mode), "gb_set_sgemm_mode")
+
+
 def set_dgemm_mode(mode, slices=8):
     return _lib.check(_lib.load().gb_set_dgemm_mode(mode, slices), "gb_set_dgemm_mode")
 

@@ -404,6 +404,13 @@ int gemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, T alpha, 
                 rc = dgemm_ozaki(m, n, k, (double)alpha, ad, ars, acs, bd, brs, bcs, (double)beta, (double*)cd,
                                  C.rs, C.cs, slices, s);
         } else {
+            if (sizeof(T) == 4 && sgemm_use_split(m, n, k)) {
+                rc = sgemm_split_dev(m, n, k, (float)alpha, (const float*)A.origin, ars, acs,
+                                     (const float*)B.origin, brs, bcs, (float)beta, (float*)cd, C.rs, C.cs, s);
+                if (rc) return rc;
+                if ((rc = stage_out(c, m, n, rs_c, cs_c, esz, C, s))) return rc;
+                return finish(s, where);
+            }
             // the learned selector when it is on (by default: the committed model), else the
             // occupancy rule
             int cfg = selector_heuristic(m, n, k), unused = 0;
@@ -1900,6 +1907,9 @@ int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
     if (rc) return rc;
     if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_sgemm_dev", "negative dimension");
     const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    if (gb::sgemm_use_split(m, n, k))
+        return gb::sgemm_split_dev(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
+                                   tb ? rs_b : cs_b, beta, c, rs_c, cs_c, pick_stream(stream));
     return gb::sgemm_dev(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
                          tb ? rs_b : cs_b, beta, c, rs_c, cs_c, pick_stream(stream));
 }

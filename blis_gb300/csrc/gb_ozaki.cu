@@ -1514,10 +1514,17 @@ constexpr int OZC_MAX = 16;
 struct OzCrtTab {
     int n, t;
     float p[OZC_MAX], invp[OZC_MAX], wm[OZC_MAX];
-    float pw[OZC_MAX][8];                           // 2^(8q) mod p_l
-    unsigned long long wlo[OZC_MAX], whi[OZC_MAX];  // W_l as a 128-bit two's-complement integer
-    unsigned long long mlo, mhi;                    // M
+    float pw[OZC_MAX][8];  // 2^(8q) mod p_l
+    int wd[OZC_MAX][4];    // W_l = sum_q wd[l][q] 2^(32q), signed 32-bit digits
+    int md[4];             // M in the same digits
 };
+
+// The moduli as compile-time constants (the recombination reduces by them),
+// and for each the multiple of p_l at or above 2^31 that makes an int32 value
+// non-negative as a uint32 without changing its residue.
+__device__ constexpr int OZC_P[OZC_MAX] = {257, 256, 255, 253, 251, 247, 241, 239,
+                                           233, 229, 227, 223, 217, 211, 199, 197};
+__host__ __device__ constexpr unsigned ozc_offset(int p) { return (unsigned)(((2147483648ull + (unsigned)p - 1) / (unsigned)p) * (unsigned)p); }
 
 // |x| 2^(t+1-e), rounded to the nearest integer (ties to even), from the bits.
 __device__ __forceinline__ unsigned long long oz_crt_scaled(unsigned long long bits, int e, int t)
@@ -1550,7 +1557,9 @@ __device__ __forceinline__ void oz_crt_residues(double x, int e, const OzCrtTab&
         float sl = 0.0f;
 #pragma unroll
         for (int q = 0; q < 8; ++q) sl = __fmaf_rn(b[q], tab.pw[l][q], sl);
-        const float rr = __fmaf_rn(-rintf(__fmul_rn(sl, tab.invp[l])), tab.p[l], sl);
+        // rint(sl / p) by one fma onto 1.5 2^23 (unit in the last place 1): |sl / p| < 2^12
+        const float q = __fmaf_rn(sl, tab.invp[l], OZ_MAGIC) - OZ_MAGIC;
+        const float rr = __fmaf_rn(-q, tab.p[l], sl);
         r[l] = neg ? -rr : rr;
     }
 }
@@ -1606,7 +1615,7 @@ __global__ void __launch_bounds__(256) oz_crt_split_kernel(int64_t rows, int64_t
 // Thread per 4 consecutive rows of one column, as oz_recombine_kernel: the
 // N product planes (one part each), CRT into 128 bits, one rounding.
 template <int N>
-__global__ void __launch_bounds__(256, (N <= 12 ? 2 : 1)) oz_crt_recombine_kernel(const __grid_constant__ OzRecombParams p,
+__global__ void __launch_bounds__(256, 2) oz_crt_recombine_kernel(const __grid_constant__ OzRecombParams p,
                                                                   const __grid_constant__ OzCrtTab tab)
 {
     if (*p.skip) return;
@@ -1614,7 +1623,6 @@ __global__ void __launch_bounds__(256, (N <= 12 ? 2 : 1)) oz_crt_recombine_kerne
     const int64_t total = mq * p.n;
     const bool plain = (p.alpha == 1.0 && p.beta == 0.0);
     const int64_t plane_stride = p.npad * p.mpad;
-    const unsigned __int128 Mm = ((unsigned __int128)tab.mhi << 64) | tab.mlo;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = e / mq, i0 = (e - j * mq) * 4;
@@ -1631,22 +1639,35 @@ __global__ void __launch_bounds__(256, (N <= 12 ? 2 : 1)) oz_crt_recombine_kerne
             const int64_t i = i0 + r;
             if (i >= p.m) break;
             if (p.out_tri && (p.out_tri == 1 ? i < dlo : i > dhi)) continue;
-            unsigned __int128 acc = 0;
+            // sum_l r_l W_l - Q M in signed 32-bit digits: S_q = sum_l r_l wd[l][q] - Q md[q]
+            // (|r_l| <= 129, |S_q| < 2^45), then one 128-bit combination
+            long long S0 = 0, S1 = 0, S2 = 0, S3 = 0;
             float qf = 0.0f;
 #pragma unroll
             for (int L = 0; L < N; ++L) {
                 const int c = (r == 0) ? v[L].x : (r == 1) ? v[L].y : (r == 2) ? v[L].z : v[L].w;
-                const int pl = (int)tab.p[L];
-                // symmetric residue of c: an fp32 quotient is off by at most one
-                int rr = c - __float2int_rn(__fmul_rn((float)c, tab.invp[L])) * pl;
+                const int pl = OZC_P[L];
+                const unsigned cu = (unsigned)c + ozc_offset(OZC_P[L]);  // same residue, non-negative
+                int rr = (int)(cu % (unsigned)OZC_P[L]);
                 if (2 * rr > pl) rr -= pl;
-                else if (2 * rr < -pl) rr += pl;
-                const unsigned __int128 w = ((unsigned __int128)tab.whi[L] << 64) | tab.wlo[L];
-                acc += (unsigned __int128)(__int128)rr * w;
-                qf = __fmaf_rn((float)rr, tab.wm[L], qf);
+                S0 += (long long)rr * tab.wd[L][0];
+                S1 += (long long)rr * tab.wd[L][1];
+                S2 += (long long)rr * tab.wd[L][2];
+                S3 += (long long)rr * tab.wd[L][3];
+                // float(rr) from the bits of 1.5 2^23 + rr
+                qf = __fmaf_rn(__int_as_float(0x4B400000 + rr) - OZ_MAGIC, tab.wm[L], qf);
             }
-            const long long Q = __float2ll_rn(qf);
-            const __int128 C = (__int128)(acc - (unsigned __int128)((__int128)Q * (__int128)Mm));
+            const int Q = __float_as_int(qf + OZ_MAGIC) - 0x4B400000;  // rint(qf), |qf| < 2^12
+            S0 -= (long long)Q * tab.md[0];
+            S1 -= (long long)Q * tab.md[1];
+            S2 -= (long long)Q * tab.md[2];
+            S3 -= (long long)Q * tab.md[3];
+            // modulo 2^128 (the true |C'| is below 2^127)
+            const unsigned __int128 acc = (unsigned __int128)(__int128)S0 +
+                                          ((unsigned __int128)(__int128)S1 << 32) +
+                                          ((unsigned __int128)(__int128)S2 << 64) +
+                                          ((unsigned __int128)(__int128)S3 << 96);
+            const __int128 C = (__int128)acc;
             const double ab = round_scaled(C, p.ea[i] + ebj);
             double* cij = p.c + i * p.rs_c + j * p.cs_c;
             if (plain) {
@@ -1701,6 +1722,16 @@ int modinv_small(int a, int p)
     return t < 0 ? t + p : t;
 }
 
+// x = sum_q d[q] 2^(32q) with d[q] in [-2^31, 2^31) (|x| < 2^127)
+void signed_digits32(__int128 x, int (&d)[4])
+{
+    for (int q = 0; q < 4; ++q) {
+        const int dq = (int)(uint32_t)(u128)x;  // x mod 2^32, as a signed value
+        d[q] = dq;
+        x = (x - (__int128)dq) / ((__int128)1 << 32);  // exact
+    }
+}
+
 void crt_table(int n, int t, OzCrtTab* tab)
 {
     *tab = OzCrtTab();
@@ -1713,9 +1744,7 @@ void crt_table(int n, int t, OzCrtTab* tab)
         const int inv = modinv_small((int)(Ml % (u128)pl), pl);
         u128 W = (Ml * (u128)inv) % M;  // W = 1 mod p_l, 0 mod the others
         __int128 Ws = (W > M / 2) ? (__int128)W - (__int128)M : (__int128)W;
-        const u128 Wu = (u128)Ws;
-        tab->wlo[l] = (unsigned long long)Wu;
-        tab->whi[l] = (unsigned long long)(Wu >> 64);
+        signed_digits32(Ws, tab->wd[l]);
         tab->wm[l] = (float)((double)Ws / (double)M);
         tab->p[l] = (float)pl;
         tab->invp[l] = 1.0f / (float)pl;
@@ -1725,8 +1754,7 @@ void crt_table(int n, int t, OzCrtTab* tab)
             pw = (pw * 256) % pl;
         }
     }
-    tab->mlo = (unsigned long long)M;
-    tab->mhi = (unsigned long long)(M >> 64);
+    signed_digits32((__int128)M, tab->md);
 }
 
 template <int N>

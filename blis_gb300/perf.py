@@ -37,7 +37,7 @@ import os
 
 import numpy as np
 
-from . import _lib, dev
+from . import _lib, blas, dev
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SMALL = False  # --small: profiling sizes (inputs still larger than the 126 MB L2)
@@ -104,12 +104,26 @@ def run_gemm(out):
 
 
 def run_sgemm(out):
-    """SGEMM 8192^3 alone (the FP32 tile engine)."""
+    """SGEMM 8192^3 on both engines (FP32 FMA kernel, split form on the bf16 tensor cores):
+    time, and the max componentwise error of 4096 sampled entries against the double-double
+    product of the same FP32 operands, in units of the FP32 gauge u32 (|A||B|)_ij."""
     import torch
     n = 4096 if SMALL else 8192
     fa, fb, fc = (_mat(n, n, seed=s, dtype=torch.float32) for s in (7, 8, 9))
-    ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
-    out.append({"workload": "sgemm_%d" % n, "form": "ffma_fp32", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
+    g = torch.Generator(device="cpu").manual_seed(3)
+    ii = torch.randint(0, n, (4096,), generator=g).cuda()
+    jj = torch.randint(0, n, (4096,), generator=g).cuda()
+    da, db = fa.double(), fb.double()
+    hi, lo = dev.dd_gemm_entries(0, 0, 1.0, da, db, 0.0, None, ii, jj)
+    gauge = (da[ii, :].abs() * db[:, jj].abs().t()).sum(1)
+    u32 = 2.0 ** -24
+    for mode, name in ((blas.SGEMM_FMA, "ffma_fp32"), (blas.SGEMM_SPLIT, "split_bf16_s3")):
+        blas.set_sgemm_mode(mode)
+        ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
+        err = ((fc[ii, jj].double() - hi - lo).abs() / gauge).max().item() / u32
+        out.append({"workload": "sgemm_%d" % n, "form": name, "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9,
+                    "max_err_in_u32_gauge": err})
+    blas.set_sgemm_mode(blas.SGEMM_AUTO)
 
 
 def run_bgemm(out):
@@ -139,10 +153,10 @@ def run_trsm(out):
     L[d, d] = m + L[d, d].abs()
     b0 = _mat(m, n, seed=12)
     flops = float(m) * m * n
-    for mode, name in ((0, "native_fp64"), (1, "ozaki_s7_updates")):
+    for mode, cnt, name in ((0, 7, "native_fp64"), (1, 7, "ozaki_s7_updates"), (2, 16, "ozaki_crt16_updates")):
         if ("ozaki" if mode else "native") not in TRSM_FORMS:
             continue
-        _lib.load().gb_set_dgemm_mode(mode, 7)
+        _lib.load().gb_set_dgemm_mode(mode, cnt)
         x = b0.clone()
         ms = _timer(lambda: (x.copy_(b0), dev.dtrsm(0, 0xC0, 0, 0, 1.0, L, x)), reps=1, warmup=1)
         copy_ms = _timer(lambda: x.copy_(b0), reps=3, warmup=1)
@@ -169,10 +183,10 @@ def run_trsm_ozaki(out):
     jj = torch.randint(0, n, (4096,), generator=g).cuda()
     absL, absB = L.abs(), b0.abs()
     flops = float(m) * m * n
-    for mode, name in ((0, "native_fp64"), (1, "ozaki_s7_updates")):
+    for mode, cnt, name in ((0, 7, "native_fp64"), (1, 7, "ozaki_s7_updates"), (2, 16, "ozaki_crt16_updates")):
         if ("ozaki" if mode else "native") not in TRSM_FORMS:
             continue
-        _lib.load().gb_set_dgemm_mode(mode, 7)
+        _lib.load().gb_set_dgemm_mode(mode, cnt)
         x = b0.clone()
         reps = 1 if mode == 0 else 3
         ms = _timer(lambda: (x.copy_(b0), dev.dtrsm(0, 0xC0, 0, 0, 1.0, L, x)), reps=reps, warmup=1)

@@ -793,6 +793,18 @@ int gb_init(int device);
 #define GB_DGEMM_OZAKI_CRT 2
 int gb_set_dgemm_mode(int mode, int slices);
 
+/* SGEMM engine (no reference counterpart): GB_SGEMM_FMA the FP32 FMA kernel;
+   GB_SGEMM_SPLIT the split form on the bf16 tensor cores (op(A), op(B)
+   widened to FP64 and multiplied as the Ozaki digit form with 3 slices, six
+   bf16 products with exact integer accumulation, then C = RN32(alpha P +
+   beta C) from the FP64 product P); GB_SGEMM_AUTO (default) the split form
+   when m, n >= 1024 and k >= 512, the FMA kernel otherwise.  Host and device
+   sgemm entry points follow it. */
+#define GB_SGEMM_FMA 0
+#define GB_SGEMM_SPLIT 1
+#define GB_SGEMM_AUTO 2
+int gb_set_sgemm_mode(int mode);
+
 /* Engine of the Ozaki slice products: 1 = one CTA per 128x256 tile,
    2 = pairs of CTAs on two SMs per 256x256 tile (cta_group::2, default). */
 int gb_set_ozaki_ctas(int ctas);

@@ -1,0 +1,86 @@
+"""SGEMM's split form on the bf16 tensor cores (gb_sgemm_split.cu) against the FP64 product.
+
+The form widens op(A), op(B) to FP64, forms their product as the Ozaki digit form with three
+slices (exact integer accumulation) and rounds alpha P + beta C to FP32 once.  With beta = 0
+the model is exact: the oracle's digit-form product, times alpha in FP64, rounded to FP32.
+Otherwise the result is checked against an FP64 product within the form's bound:
+2^-(8s+1) (2^e_i |B_j|_1 + |A_i|_1 2^e_j) + 2^-(16s+2) k 2^(e_i+e_j) for the product (the
+digits' representation error, no accumulation error) plus one FP32 rounding.
+"""
+import numpy as np
+import pytest
+
+from blis_gb300 import blas
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+S = 3
+U32 = float(np.finfo(np.float32).eps) / 2
+
+
+@pytest.fixture(autouse=True)
+def split_mode(gblib):
+    blas.set_sgemm_mode(blas.SGEMM_SPLIT)
+    yield
+    blas.set_sgemm_mode(blas.SGEMM_AUTO)
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
+@pytest.mark.parametrize("m,n,k", [(300, 200, 1000), (33, 517, 64), (1024, 1024, 2048)])
+def test_split_sgemm_bit_exact_beta0(ta, tb, m, n, k):
+    a = po.uniform((k, m) if ta == "T" else (m, k), 1, dtype=np.float32)
+    b = po.uniform((n, k) if tb == "T" else (k, n), 2, dtype=np.float32)
+    c = np.zeros((m, n), dtype=np.float32, order="F")
+    blas.sgemm(ta, tb, m, n, k, 0.75, a, a.shape[0], b, b.shape[0], 0.0, c, m)
+    p = np.zeros((m, n), order="F")
+    po.ozaki_dgemm(8 if ta == "T" else 0, 8 if tb == "T" else 0, 1.0, np.asfortranarray(a, dtype=np.float64),
+                   np.asfortranarray(b, dtype=np.float64), 0.0, p, S)
+    ref = (np.float64(0.75) * p).astype(np.float32)
+    assert np.array_equal(c, ref)
+
+
+def test_split_sgemm_alpha_beta_within_bound():
+    m, n, k = 700, 650, 1500
+    a = po.uniform((m, k), 3, dtype=np.float32)
+    b = po.uniform((k, n), 4, dtype=np.float32)
+    c0 = po.uniform((m, n), 5, dtype=np.float32)
+    c = np.asfortranarray(c0.copy())
+    blas.sgemm("N", "N", m, n, k, -1.5, a, m, b, k, 0.5, c, m)
+    a64, b64 = a.astype(np.float64), b.astype(np.float64)
+    exact = -1.5 * (a64 @ b64) + 0.5 * c0.astype(np.float64)
+    ea = 2.0 ** (np.floor(np.log2(np.abs(a64).max(axis=1))) + 2)
+    eb = 2.0 ** (np.floor(np.log2(np.abs(b64).max(axis=0))) + 2)
+    pbound = 2.0 ** -(8 * S + 1) * (np.outer(ea, np.abs(b64).sum(0)) + np.outer(np.abs(a64).sum(1), eb)) \
+        + 2.0 ** -(16 * S + 2) * k * np.outer(ea, eb)
+    bound = 1.5 * pbound * (1 + 1e-12) + U32 * np.abs(exact) * (1 + 1e-6) + 1e-300
+    assert np.all(np.abs(c.astype(np.float64) - exact) <= bound)
+
+
+def test_split_sgemm_more_accurate_than_fma_at_large_k():
+    """The measurement behind the default: at k = 8192 the split form's error against an FP64
+    product is below the FP32 FMA kernel's."""
+    m, n, k = 1024, 1024, 8192
+    a = po.uniform((m, k), 6, dtype=np.float32)
+    b = po.uniform((k, n), 7, dtype=np.float32)
+    exact = a.astype(np.float64) @ b.astype(np.float64)
+    c_split = np.zeros((m, n), dtype=np.float32, order="F")
+    blas.sgemm("N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c_split, m)
+    blas.set_sgemm_mode(blas.SGEMM_FMA)
+    c_fma = np.zeros((m, n), dtype=np.float32, order="F")
+    blas.sgemm("N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c_fma, m)
+    e_split = np.abs(c_split - exact).max()
+    e_fma = np.abs(c_fma - exact).max()
+    assert e_split < e_fma, (e_split, e_fma)
+
+
+def test_split_sgemm_nonfinite_propagates():
+    m, n, k = 1024, 1024, 600
+    a = po.uniform((m, k), 8, dtype=np.float32)
+    b = po.uniform((k, n), 9, dtype=np.float32)
+    a[10, 20] = np.inf
+    b[30, 40] = np.nan
+    c = np.zeros((m, n), dtype=np.float32, order="F")
+    blas.sgemm("N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m)
+    ref = a.astype(np.float64) @ b.astype(np.float64)
+    assert np.array_equal(np.isnan(c), np.isnan(ref))
+    assert np.array_equal(np.isinf(c), np.isinf(ref))
