@@ -376,6 +376,11 @@ int gemm_host(int transa, int transb, int64_t m, int64_t n, int64_t k, T alpha, 
             const double* ad = reinterpret_cast<const double*>(A.origin);
             const double* bd = reinterpret_cast<const double*>(B.origin);
             int slices = ozaki_slices();
+            if (selector_auto()) {
+                // the selector's Ozaki engine for this shape, decided now (a host call waits anyway)
+                int eng = 0;
+                if ((rc = selector_ozaki_engine(m, n, k, &eng))) return rc;
+            }
             bool native = false;
             if (slices == 0) {
                 // auto: the selector's proposal, checked by the error-bound verifier
@@ -1866,8 +1871,12 @@ int gb_dgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
     if (rc) return rc;
     if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_dgemm_dev", "negative dimension");
     const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
-    return gb::dgemm_native(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
-                            tb ? rs_b : cs_b, beta, c, rs_c, cs_c, pick_stream(stream));
+    // a configuration the selector already decided for this shape, else the occupancy rule (a
+    // device entry point never waits for an inference)
+    int cfg = gb::selector_auto() ? gb::selector_cached_config(0, m, n, k, ta, tb, 0) : -1;
+    if (cfg < 0) cfg = gb::selector_heuristic(m, n, k);
+    return gb::gemm_config_dev(0, cfg, m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
+                               tb ? rs_b : cs_b, beta, c, rs_c, cs_c, pick_stream(stream));
 }
 
 int gb_dgemm_ozaki_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
@@ -1910,8 +1919,10 @@ int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
     if (gb::sgemm_use_split(m, n, k))
         return gb::sgemm_split_dev(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
                                    tb ? rs_b : cs_b, beta, c, rs_c, cs_c, pick_stream(stream));
-    return gb::sgemm_dev(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
-                         tb ? rs_b : cs_b, beta, c, rs_c, cs_c, pick_stream(stream));
+    int cfg = gb::selector_auto() ? gb::selector_cached_config(1, m, n, k, ta, tb, 0) : -1;
+    if (cfg < 0) cfg = gb::selector_heuristic(m, n, k);
+    return gb::gemm_config_dev(1, cfg, m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
+                               tb ? rs_b : cs_b, beta, c, rs_c, cs_c, pick_stream(stream));
 }
 
 int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,

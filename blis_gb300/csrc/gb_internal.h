@@ -89,6 +89,13 @@ int dgemm_native_gated(int64_t m, int64_t n, int64_t k, double alpha,
                        double* c, int64_t rs_c, int64_t cs_c, const int* gate, cudaStream_t s);
 double ozaki_t_bound_log2(int s, int64_t k);
 bool selector_auto();
+// Ozaki engine for an m x n x k product from the selector's engine output
+// (2 CTA pairs, 1 single CTAs), or *engine = 0 when the model has none.
+int selector_ozaki_engine(int64_t m, int64_t n, int64_t k, int* engine);
+int selector_cached_engine(int64_t m, int64_t n, int64_t k);
+int selector_cached_config(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad);
+int selector_choose_ex(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad, double sa, double sb,
+                       int* config, int* slices, int* engine);
 int selector_heuristic(int64_t m, int64_t n, int64_t k);
 int selector_choose(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad, double sa, double sb,
                     int* config, int* slices);

@@ -1514,7 +1514,7 @@ constexpr int OZC_MAX = 16;
 struct OzCrtTab {
     int n, t;
     float p[OZC_MAX], invp[OZC_MAX], wm[OZC_MAX];
-    float pw[OZC_MAX][8];  // 2^(8q) mod p_l
+    float pw[OZC_MAX][6];  // 2^(12q) mod p_l
     int wd[OZC_MAX][4];    // W_l = sum_q wd[l][q] 2^(32q), signed 32-bit digits
     int md[4];             // M in the same digits
 };
@@ -1541,23 +1541,27 @@ __device__ __forceinline__ unsigned long long oz_crt_scaled(unsigned long long b
     return (rem > half || (rem == half && (q & 1ull))) ? q + 1 : q;
 }
 
-// The N residues of x as floats (integers, |r| <= 128).
-template <int N>
+// The N residues of x as floats (integers, |r| <= 128), from NL 12-bit limbs of X
+// (NL = 5 for t <= 59, else 6): s_l = sum_q h_q (2^(12q) mod p_l) < 6 2^12 2^8 < 2^22.6
+// is exact in fp32, and rint(s_l / p_l) by one fma onto 1.5 2^23 (unit in the last place
+// 1) is exact: the fma rounds s_l invp_l, which differs from s_l / p_l by at most
+// s_l 2^-24 / p_l < 0.38 / p_l, while a non-integral s_l / p_l is at least 1 / (2 p_l) from
+// a half-integer.
+template <int N, int NL>
 __device__ __forceinline__ void oz_crt_residues(double x, int e, const OzCrtTab& tab, float (&r)[N])
 {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
     const unsigned long long X = oz_crt_scaled(bits & 0x7FFFFFFFFFFFFFFFull, e, tab.t);
-    float b[8];
+    float h[NL];
 #pragma unroll
-    for (int q = 0; q < 8; ++q)  // byte q of X as a float: its bits OR-ed into 2^23, minus 2^23
-        b[q] = __uint_as_float(0x4B000000u | (uint32_t)((X >> (8 * q)) & 255u)) - 8388608.0f;
+    for (int q = 0; q < NL; ++q)  // limb q of X as a float: its bits OR-ed into 2^23, minus 2^23
+        h[q] = __uint_as_float(0x4B000000u | (uint32_t)((X >> (12 * q)) & 4095u)) - 8388608.0f;
     const bool neg = (bits >> 63) != 0;
 #pragma unroll
     for (int l = 0; l < N; ++l) {
         float sl = 0.0f;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) sl = __fmaf_rn(b[q], tab.pw[l][q], sl);
-        // rint(sl / p) by one fma onto 1.5 2^23 (unit in the last place 1): |sl / p| < 2^12
+        for (int q = 0; q < NL; ++q) sl = __fmaf_rn(h[q], tab.pw[l][q], sl);
         const float q = __fmaf_rn(sl, tab.invp[l], OZ_MAGIC) - OZ_MAGIC;
         const float rr = __fmaf_rn(-q, tab.p[l], sl);
         r[l] = neg ? -rr : rr;
@@ -1566,7 +1570,7 @@ __device__ __forceinline__ void oz_crt_residues(double x, int e, const OzCrtTab&
 
 // Tile of 32 rows x 64 k per block (as oz_split_kernel); writes N bf16
 // residue planes, K-major, zero in the padding.
-template <int N>
+template <int N, int NL>
 __global__ void __launch_bounds__(256) oz_crt_split_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
                                                            int64_t sr, int64_t sl,
                                                            const unsigned long long* __restrict__ maxbits,
@@ -1599,8 +1603,8 @@ __global__ void __launch_bounds__(256) oz_crt_split_kernel(int64_t rows, int64_t
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
         float f0[N], f1[N];
-        oz_crt_residues<N>(r < rows ? tile[rr][c0 + 2 * h] : 0.0, e, tab, f0);
-        oz_crt_residues<N>(r < rows ? tile[rr][c0 + 2 * h + 1] : 0.0, e, tab, f1);
+        oz_crt_residues<N, NL>(r < rows ? tile[rr][c0 + 2 * h] : 0.0, e, tab, f0);
+        oz_crt_residues<N, NL>(r < rows ? tile[rr][c0 + 2 * h + 1] : 0.0, e, tab, f1);
 #pragma unroll
         for (int l = 0; l < N; ++l)
             packed[l][h] = __byte_perm(__float_as_uint(f0[l]), __float_as_uint(f1[l]), 0x7632);
@@ -1749,9 +1753,9 @@ void crt_table(int n, int t, OzCrtTab* tab)
         tab->p[l] = (float)pl;
         tab->invp[l] = 1.0f / (float)pl;
         int pw = 1 % pl;
-        for (int q = 0; q < 8; ++q) {
+        for (int q = 0; q < 6; ++q) {
             tab->pw[l][q] = (float)pw;
-            pw = (pw * 256) % pl;
+            pw = (pw * 4096) % pl;
         }
     }
     signed_digits32((__int128)M, tab->md);
@@ -1763,8 +1767,11 @@ void launch_crt_split(int64_t rows, int64_t k, const double* R, int64_t sr, int6
                       const OzCrtTab& tab, cudaStream_t s)
 {
     LaunchScope ls("oz_split_crt", s);
-    oz_crt_split_kernel<N><<<dim3((unsigned)(kpad / 64), (unsigned)(rcover / 32)), 256, 0, s>>>(
-        rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, tab);
+    const dim3 grid((unsigned)(kpad / 64), (unsigned)(rcover / 32));
+    if (tab.t <= 59)  // X < 2^60: five 12-bit limbs
+        oz_crt_split_kernel<N, 5><<<grid, 256, 0, s>>>(rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, tab);
+    else
+        oz_crt_split_kernel<N, 6><<<grid, 256, 0, s>>>(rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, tab);
 }
 
 template <int N>
@@ -1875,23 +1882,59 @@ int chunk_kb_setting()
 // Slice-GEMM engine: 1 = one CTA per 128x256 tile, 2 = CTA pairs per
 // 256x256 tile (cta_group::2).  gb_set_ozaki_ctas() or the environment
 // variable GB_OZAKI_CTAS select; the pair form is the default.
-static int g_ozaki_ctas = 0;
+static int g_ozaki_ctas = -1;
 
+// The engine setting: 1 or 2 forced (gb_set_ozaki_ctas, GB_OZAKI_CTAS), 0 chosen per
+// product (the selector's engine output, else the occupancy rule below).
 int ozaki_ctas_setting()
 {
-    if (g_ozaki_ctas == 0) {
+    if (g_ozaki_ctas < 0) {
         const char* e = getenv("GB_OZAKI_CTAS");
-        g_ozaki_ctas = (e && atoi(e) == 1) ? 1 : 2;
+        const int v = e ? atoi(e) : 0;
+        g_ozaki_ctas = (v == 1 || v == 2) ? v : 0;
     }
     return g_ozaki_ctas;
 }
 
 int set_ozaki_ctas(int ctas)
 {
-    if (ctas != 1 && ctas != 2) return set_error(GB_ERR_ARG, "gb_set_ozaki_ctas", "ctas must be 1 or 2");
+    if (ctas != 0 && ctas != 1 && ctas != 2)
+        return set_error(GB_ERR_ARG, "gb_set_ozaki_ctas", "ctas must be 0 (per product), 1 or 2");
     g_ozaki_ctas = ctas;
     return GB_SUCCESS;
 }
+
+thread_local int t_ozaki_ctas = 0;  // the engine of the product being prepared on this thread
+
+// The engine a product's operands are prepared for: the per-product choice,
+// else the forced setting, else CTA pairs.
+int ozaki_engine()
+{
+    if (t_ozaki_ctas) return t_ozaki_ctas;
+    const int v = ozaki_ctas_setting();
+    return v ? v : 2;
+}
+
+// Engine for an m x n x k product when the setting leaves the choice per product:
+// the selector's engine output for a shape it has decided (the host entry points
+// ask it before the product; device entry points never wait for an inference), else
+// CTA pairs for products of at least 2^30 FP64-equivalent flops and single CTAs
+// below (on the engine-tuned training shapes single CTAs won 70% of the time,
+// mostly the small ones; at 16384^3 the two are within 1%).
+int ozaki_engine_choice(int64_t m, int64_t n, int64_t k)
+{
+    const int v = ozaki_ctas_setting();
+    if (v) return v;
+    const int eng = selector_auto() ? selector_cached_engine(m, n, k) : 0;
+    if (eng) return eng;
+    return (2.0 * (double)m * (double)n * (double)k >= 1073741824.0) ? 2 : 1;
+}
+
+struct EngineScope {
+    int prev;
+    explicit EngineScope(int e) : prev(t_ozaki_ctas) { t_ozaki_ctas = e; }
+    ~EngineScope() { t_ozaki_ctas = prev; }
+};
 
 namespace {
 
@@ -2124,7 +2167,7 @@ int ozaki_alloc_a(int64_t m, int64_t k, const double* a, int64_t ars, int64_t ac
         if (ozaki_t_bound_log2(slices, k) >= 126.0)
             return set_error(GB_ERR_ARG, "gb_dgemm_ozaki", "slices and k exceed the 128-bit recombination range");
     }
-    A->pair_form = (ozaki_ctas_setting() == 2);
+    A->pair_form = (ozaki_engine() == 2);
     A->row_tile = A->pair_form ? 2 * OZ2_ROWS : OZ_BM;
     A->slices = slices;
     A->m = m;
@@ -2519,6 +2562,7 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
 {
     if (m <= 0 || n <= 0) return GB_SUCCESS;
     if (alpha == 0.0 || k <= 0) return scal_matrix(m, n, beta, c, rs_c, cs_c, s);
+    EngineScope engine(t_ozaki_ctas ? t_ozaki_ctas : ozaki_engine_choice(m, n, k));
     OzA A;
     int rc;
     if (k > fused_split_max_k() || ozaki_form() == 1) {  // the CRT form always splits in two passes

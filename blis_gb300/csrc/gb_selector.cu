@@ -38,6 +38,7 @@ std::mutex g_mu;
 float* g_params = nullptr;  // device copy of the MLP parameters
 float* g_io = nullptr;      // device scratch: 16 features + 8 outputs
 bool g_loaded = false;
+bool g_engine_output = false;  // the loaded model was trained with the Ozaki engine output (file version 2)
 bool g_auto = false;
 bool g_user_configured = false;  // the caller loaded, unloaded or switched the selector itself
 std::once_flag g_default_once;
@@ -87,27 +88,31 @@ uint64_t key_of(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int 
 
 namespace {
 // Reads a model file (magic, version, parameter count, CRC-32 of the parameters).
-bool read_model_file(const char* path, float* p)
+// Version 1: configuration times and slice count; version 2 adds the Ozaki engine output.
+bool read_model_file(const char* path, float* p, int* version)
 {
     FILE* f = path ? fopen(path, "rb") : nullptr;
     if (!f) return false;
     char magic[8];
     uint32_t hdr[3];
     const bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "GBSELMLP", 8) == 0 &&
-                    fread(hdr, sizeof(uint32_t), 3, f) == 3 && hdr[0] == 1 && hdr[1] == GB_MLP_NPARAMS &&
+                    fread(hdr, sizeof(uint32_t), 3, f) == 3 && (hdr[0] == 1 || hdr[0] == 2) &&
+                    hdr[1] == GB_MLP_NPARAMS &&
                     fread(p, sizeof(float), GB_MLP_NPARAMS, f) == GB_MLP_NPARAMS &&
                     crc32_bytes(reinterpret_cast<const unsigned char*>(p), sizeof(float) * GB_MLP_NPARAMS) == hdr[2];
     fclose(f);
+    if (ok && version) *version = (int)hdr[0];
     return ok;
 }
 
 // Copies the parameters to the device.  A load the caller asked for (user) takes
 // charge of the selector; the default load switches auto-selection on unless the
 // caller already decided.
-int load_params(const float* params, bool user)
+int load_params(const float* params, bool user, bool engine_output)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     if (!user && g_user_configured) return GB_SUCCESS;
+    g_engine_output = engine_output;
     if (!g_params) {
         GB_CUDA(cudaMalloc(&g_params, sizeof(float) * GB_MLP_NPARAMS));
         GB_CUDA(cudaMalloc(&g_io, sizeof(float) * (GB_MLP_IN + GB_MLP_OUT)));
@@ -151,8 +156,10 @@ void load_default_model()
     path = (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/tuning/selector_mlp.bin";
     if (access(path.c_str(), R_OK) != 0) return;
     std::vector<float> p(GB_MLP_NPARAMS);
-    if (!read_model_file(path.c_str(), p.data())) return;
-    if (ensure_init() != GB_SUCCESS || load_params(p.data(), false) != GB_SUCCESS) gb_clear_last_error();
+    int version = 0;
+    if (!read_model_file(path.c_str(), p.data(), &version)) return;
+    if (ensure_init() != GB_SUCCESS || load_params(p.data(), false, version >= 2) != GB_SUCCESS)
+        gb_clear_last_error();
 }
 }  // namespace
 
@@ -166,11 +173,20 @@ bool selector_auto()
 int selector_choose(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad, double sa, double sb,
                     int* config, int* slices)
 {
+    return selector_choose_ex(dtype, m, n, k, ta, tb, pad, sa, sb, config, slices, nullptr);
+}
+
+// Config, proposed slice count and (engine != nullptr) Ozaki engine for a shape.
+int selector_choose_ex(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad, double sa, double sb,
+                       int* config, int* slices, int* engine)
+{
     *config = selector_heuristic(m, n, k);
     *slices = 8;
+    if (engine) *engine = 0;
     if (!g_loaded) return GB_SUCCESS;
     if (2.0 * (double)m * (double)n * (double)k > kWorkCap) {
         *config = 0;
+        if (engine) *engine = 2;  // above the trained range: the pairs' large tiles
         return GB_SUCCESS;
     }
     const uint64_t key = key_of(dtype, m, n, k, ta, tb, pad, (int)lround(sa), (int)lround(sb));
@@ -178,7 +194,8 @@ int selector_choose(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, 
     auto it = g_cache.find(key);
     if (it != g_cache.end()) {
         *config = (int)(it->second & 0xFF);
-        *slices = (int)(it->second >> 8);
+        *slices = (int)((it->second >> 8) & 0xFF);
+        if (engine) *engine = (int)((it->second >> 16) & 0xFF);
         return GB_SUCCESS;
     }
     float host[GB_MLP_IN + GB_MLP_OUT];
@@ -196,10 +213,44 @@ int selector_choose(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, 
         if (out[c] < out[best]) best = c;
     int sl = (int)ceil(out[GB_GEMM_NUM_CONFIGS] * 12.0 - 0.25);
     sl = sl < 2 ? 2 : (sl > 12 ? 12 : sl);
+    // engine output: log2(t_one_cta / t_pair) / 10 for the Ozaki form, positive when the
+    // CTA pairs are faster (models trained before it carry a zero output: pairs)
+    const int eng = (out[GB_MLP_OUT - 1] >= 0.0f) ? 2 : 1;
     *config = best;
     *slices = sl;
-    g_cache[key] = (uint64_t)best | ((uint64_t)sl << 8);
+    if (engine) *engine = eng;
+    g_cache[key] = (uint64_t)best | ((uint64_t)sl << 8) | ((uint64_t)eng << 16);
     return GB_SUCCESS;
+}
+
+int selector_ozaki_engine(int64_t m, int64_t n, int64_t k, int* engine)
+{
+    *engine = 0;
+    if (!g_loaded || !g_engine_output) return GB_SUCCESS;
+    int cfg = 0, sl = 0;
+    return selector_choose_ex(0, m, n, k, 0, 0, 0, 0.0, 0.0, &cfg, &sl, engine);
+}
+
+// The configuration of an already decided shape (no inference, no synchronization), or -1.
+int selector_cached_config(int dtype, int64_t m, int64_t n, int64_t k, int ta, int tb, int pad)
+{
+    if (!g_loaded) return -1;
+    if (2.0 * (double)m * (double)n * (double)k > kWorkCap) return 0;
+    const uint64_t key = key_of(dtype, m, n, k, ta, tb, pad, 0, 0);
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_cache.find(key);
+    return (it == g_cache.end()) ? -1 : (int)(it->second & 0xFF);
+}
+
+// The engine of an already decided shape (no inference, no synchronization), or 0.
+int selector_cached_engine(int64_t m, int64_t n, int64_t k)
+{
+    if (!g_loaded || !g_engine_output) return 0;
+    if (2.0 * (double)m * (double)n * (double)k > kWorkCap) return 2;
+    const uint64_t key = key_of(0, m, n, k, 0, 0, 0, 0, 0);
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_cache.find(key);
+    return (it == g_cache.end()) ? 0 : (int)((it->second >> 16) & 0xFF);
 }
 
 // Binary exponent half-range over a strided sample of a host matrix, the
@@ -233,16 +284,19 @@ int gb_selector_load(const float* params, int nparams)
     if (rc) return rc;
     if (!params || nparams != GB_MLP_NPARAMS)
         return set_error(GB_ERR_ARG, "gb_selector_load", "expected GB_MLP_NPARAMS parameters");
-    return load_params(params, true);
+    return load_params(params, true, false);
 }
 
 int gb_selector_load_file(const char* path)
 {
     std::vector<float> p(GB_MLP_NPARAMS);
-    if (!read_model_file(path, p.data()))
+    int version = 0;
+    if (!read_model_file(path, p.data(), &version))
         return set_error(GB_ERR_ARG, "gb_selector_load_file", "cannot open the model file, or bad magic, version, "
                                                               "size or checksum");
-    return gb_selector_load(p.data(), GB_MLP_NPARAMS);
+    int rc = ensure_init();
+    if (rc) return rc;
+    return load_params(p.data(), true, version >= 2);
 }
 
 int gb_selector_unload(void)

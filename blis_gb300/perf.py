@@ -490,7 +490,27 @@ def run_hermitian(out):
     L.gb_set_dgemm_mode(0, 8)
 
 
-SUITES = {"gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
+def run_crt(out):
+    """The CRT form of the Ozaki product alone, 16 moduli, exponent-spread operands (the
+    benchmark's inputs) at 16384^3, or 4096^3 with --small (the profiling case: each of the
+    split, slice GEMM and recombination kernels launches once per product, three products)."""
+    n = 4096 if SMALL else 16384
+    a = _mat(n, n, kind=dev.RAND_EXPSPREAD, seed=61, p0=-20, p1=20)
+    b = _mat(n, n, kind=dev.RAND_EXPSPREAD, seed=62, p0=-20, p1=20)
+    c = _mat(n, n, seed=63)
+    ms = _timer(lambda: dev.dgemm_ozaki_crt(0, 0, 1.0, a, b, 0.0, c, 16), reps=3, warmup=1)
+    dev.set_kernel_timing(True)
+    dev.kernel_time_ms("")
+    for _ in range(3):
+        dev.dgemm_ozaki_crt(0, 0, 1.0, a, b, 0.0, c, 16)
+    stages = {pre: dev.kernel_time_ms(pre)[0] / 3 for pre in ("oz_rowmax", "oz_split_crt", "ozaki_slice_gemm",
+                                                              "oz_recombine")}
+    dev.set_kernel_timing(False)
+    out.append({"workload": "dgemm_%d_crt16_expspread" % n, "ms": ms, "tflops": 2.0 * n ** 3 / ms / 1e9,
+                "stage_ms": stages})
+
+
+SUITES = {"crt": run_crt, "gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
           "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm, "bgemm": run_bgemm,
           "level3x": run_level3x, "level12x": run_level12x, "complex": run_complex, "hermitian": run_hermitian}
 

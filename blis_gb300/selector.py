@@ -44,6 +44,7 @@ NPARAMS = 9928
 CONFIG_NAMES = ["tile128", "tile64", "tile64_k2", "tile64_k4", "tile64_k8", "tile64_k16"]
 NCONFIG = len(CONFIG_NAMES)
 OUT_SLICES = 6
+OUT_ENGINE = 7  # log2(t_one_cta / t_pair) / TIME_SCALE of the Ozaki form: CTA pairs when >= 0
 DTYPES = {"fp64": 0, "fp32": 1, "bf16": 2}  # bf16: A, B bf16, C and arithmetic fp32
 PADS = (0, 8, 64)
 SCHEMA = "gb300-selector-mlp/1"
@@ -231,6 +232,70 @@ def build_dataset(shapes, log_every=0):
                                 for s in shapes], np.int64)}
 
 
+def ozaki_engine_rule(m, n, k):
+    """The library's engine rule without a model (gb_ozaki.cu ozaki_engine_choice): CTA pairs
+    for products of at least 2^30 FP64-equivalent flops, single CTAs below (measured: on the
+    6,668 engine-tuned training shapes single CTAs win 70% of the time, mostly small ones)."""
+    return 2 if 2.0 * m * n * k >= 2.0 ** 30 else 1
+
+
+def tune_engines(data, log_every=0):
+    """Times the Ozaki form of every FP64 shape of a tuning set on both slice-GEMM engines
+    (single CTAs, CTA pairs) at the shape's label slice count, with CUDA events; returns the
+    set with TE (times, [one, pair]) and the engine target in Y / M."""
+    tuner = Autotuner()
+    torch = tuner.torch
+    L = tuner.L
+    L.gb_dgemm_ozaki_dev.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_void_p,
+                                     C.c_int64, C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_double,
+                                     C.c_void_p, C.c_int64, C.c_int64, C.c_int, C.c_void_p]
+    a, b, c = tuner.buf[0]
+    out = {key: np.array(data[key]) for key in data.files}
+    sh = out["shapes"]
+    TE = np.zeros((len(sh), 2), np.float64)
+    t0 = time.time()
+    rows = np.nonzero(sh[:, 3] == 0)[0]
+
+    def call(i):
+        m, n, k, ta, tb, pad = (int(v) for v in sh[i, [0, 1, 2, 4, 5, 6]])
+        ra, rb = (k if ta else m), (n if tb else k)
+        rc = L.gb_dgemm_ozaki_dev(8 if ta else 0, 8 if tb else 0, m, n, k, 1.0, a.data_ptr(), 1, ra + pad,
+                                  b.data_ptr(), 1, rb + pad, 0.0, c.data_ptr(), 1, m + pad,
+                                  int(out["S"][i]), tuner.stream)
+        if rc != 0:
+            raise RuntimeError("gb_dgemm_ozaki_dev: %s" % (_lib.last_error(),))
+
+    try:
+        for nrow, i in enumerate(rows):
+            if not 2 <= int(out["S"][i]) <= 12:
+                continue
+            for col, ctas in ((0, 1), (1, 2)):
+                _lib.check(L.gb_set_ozaki_ctas(ctas), "gb_set_ozaki_ctas")
+                call(i)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                call(i)
+                e1.record()
+                e1.synchronize()
+                t = e0.elapsed_time(e1) * 1e3
+                if t < 20000.0:
+                    e0.record()
+                    for _ in range(3):
+                        call(i)
+                    e1.record()
+                    e1.synchronize()
+                    t = e0.elapsed_time(e1) * 1e3 / 3
+                TE[i, col] = t
+            out["Y"][i, OUT_ENGINE] = np.log2(TE[i, 0] / TE[i, 1]) / TIME_SCALE
+            out["M"][i, OUT_ENGINE] = 1.0
+            if log_every and (nrow + 1) % log_every == 0:
+                print("engine-tuned %d/%d FP64 shapes in %.1f s" % (nrow + 1, len(rows), time.time() - t0), flush=True)
+    finally:
+        L.gb_set_ozaki_ctas(0)
+    out["TE"] = TE
+    return out
+
+
 # ------------------------------------------------------------------ model
 def init_params(seed=0):
     rng = np.random.default_rng(seed)
@@ -345,6 +410,23 @@ def evaluate(params, data):
             res["per_dtype"][name] = {"n": int(sel.sum()),
                                       "mlp_mean_throughput_regret": float(1.0 - np.mean(best[sel] / t_mlp[sel])),
                                       "rule_mean_throughput_regret": float(1.0 - np.mean(best[sel] / t_heur[sel]))}
+    if "TE" in data.files:
+        TE = data["TE"]
+        tuned = TE[:, 1] > 0
+        if tuned.any():
+            te = TE[tuned]
+            best_e = te.min(1)
+            pick = np.where(pred[tuned, OUT_ENGINE] >= 0.0, 1, 0)
+            rule = np.array([ozaki_engine_rule(int(r[0]), int(r[1]), int(r[2])) for r in sh[tuned]]) - 1
+            rows = np.arange(len(te))
+            res["ozaki_engine"] = {
+                "n": int(tuned.sum()),
+                "mlp_mean_time_over_best": float(np.mean(te[rows, pick] / best_e)),
+                "rule_mean_time_over_best": float(np.mean(te[rows, rule] / best_e)),
+                "always_pair_mean_time_over_best": float(np.mean(te[:, 1] / best_e)),
+                "always_one_cta_mean_time_over_best": float(np.mean(te[:, 0] / best_e)),
+                "mlp_exact_choice_rate": float(np.mean(te[rows, pick] == best_e)),
+                "pair_best_fraction": float(np.mean(te[:, 1] <= te[:, 0]))}
     fp64 = sh[:, 3] == 0
     if fp64.any():
         s_true = data["S"][fp64]
@@ -427,15 +509,16 @@ def save_model(path, params, meta):
 BIN_MAGIC = b"GBSELMLP"
 
 
-def save_model_bin(path, params):
-    """The binary form read by gb_selector_load_file: magic, version 1,
-    parameter count, CRC-32 of the float32 parameters, parameters."""
+def save_model_bin(path, params, version=2):
+    """The binary form read by gb_selector_load_file: magic, version (2: the Ozaki engine
+    output is trained; 1: it is not), parameter count, CRC-32 of the float32 parameters,
+    parameters."""
     import struct
     import zlib
     p = np.asarray(params, "<f4")
     blob = p.tobytes()
     with open(path, "wb") as f:
-        f.write(BIN_MAGIC + struct.pack("<III", 1, p.size, zlib.crc32(blob) & 0xFFFFFFFF) + blob)
+        f.write(BIN_MAGIC + struct.pack("<III", version, p.size, zlib.crc32(blob) & 0xFFFFFFFF) + blob)
 
 
 DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning", "selector_mlp.bin")
@@ -488,7 +571,7 @@ class Selector:
 
 def _main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["tune", "train", "eval"])
+    ap.add_argument("cmd", choices=["tune", "tune-engines", "train", "eval"])
     ap.add_argument("--count", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out")
@@ -501,13 +584,19 @@ def _main():
     if a.cmd == "tune":
         d = build_dataset(sample_shapes(a.count, a.seed), log_every=500)
         np.savez_compressed(a.out, **d)
+    elif a.cmd == "tune-engines":
+        # adds the Ozaki engine timings to a tuning file (--data in, --out written)
+        np.savez_compressed(a.out, **tune_engines(np.load(a.data), log_every=500))
     elif a.cmd == "train":
         # --data may name several tuning files (comma separated); they are concatenated
         parts = [np.load(p) for p in a.data.split(",")]
         X, Y, M = (np.concatenate([d[key] for d in parts]) for key in ("X", "Y", "M"))
         p, curve = train(X, Y, M, epochs=a.epochs, log=print)
-        save_model(a.out, p, {"train_samples": int(X.shape[0]), "final_loss": curve[-1]})
-        save_model_bin(os.path.splitext(a.out)[0] + ".bin", p)
+        engine = bool(M[:, OUT_ENGINE].any())
+        save_model(a.out, p, {"train_samples": int(X.shape[0]), "final_loss": curve[-1],
+                              "engine_output": engine,
+                              "engine_samples": int(M[:, OUT_ENGINE].sum())})
+        save_model_bin(os.path.splitext(a.out)[0] + ".bin", p, version=2 if engine else 1)
     else:
         p, _ = load_model(a.model)
         d = np.load(a.data)

@@ -806,7 +806,11 @@ int gb_set_dgemm_mode(int mode, int slices);
 int gb_set_sgemm_mode(int mode);
 
 /* Engine of the Ozaki slice products: 1 = one CTA per 128x256 tile,
-   2 = pairs of CTAs on two SMs per 256x256 tile (cta_group::2, default). */
+   2 = pairs of CTAs on two SMs per 256x256 tile (cta_group::2, a cluster of
+   two), 0 = chosen per product (default): the learned selector's engine
+   output for shapes a host entry point has asked it about, else CTA pairs
+   for products of at least 2^30 flops and single CTAs below.  The
+   GB_OZAKI_CTAS environment variable (1 or 2) forces one engine. */
 int gb_set_ozaki_ctas(int ctas);
 
 /* Last error of the calling thread (GB_SUCCESS if none), with its message. */

@@ -21,7 +21,7 @@ def engine(gblib, request):
     """Every test runs on both slice-GEMM engines (CTA pairs and single CTAs)."""
     assert gblib.gb_set_ozaki_ctas(request.param) == 0
     yield request.param
-    gblib.gb_set_ozaki_ctas(2)
+    gblib.gb_set_ozaki_ctas(0)
     blas.set_dgemm_mode(blas.DGEMM_NATIVE)
 
 

@@ -22,7 +22,7 @@ N, T = blas.NO_TRANSPOSE, blas.TRANSPOSE
 def engine(gblib, request):
     assert gblib.gb_set_ozaki_ctas(request.param) == 0
     yield request.param
-    gblib.gb_set_ozaki_ctas(2)
+    gblib.gb_set_ozaki_ctas(0)
     blas.set_dgemm_mode(blas.DGEMM_NATIVE)
 
 

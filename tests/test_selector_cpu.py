@@ -107,3 +107,29 @@ def test_occupancy_rule_between_threshold_rule_and_model():
         sel = sh[:, 3] == code
         r_mlp, r_occ, r_thr = (float(np.mean(t[sel] / best[sel])) - 1.0 for t in (t_mlp, t_occ, t_thr))
         assert r_mlp < r_occ < r_thr, (code, r_mlp, r_occ, r_thr)
+
+
+def test_engine_output_beats_rules_on_heldout():
+    """The Ozaki engine output (CTA pairs or single CTAs per shape) of the committed model,
+    recomputed on the CPU: on the engine-tuned held-out FP64 shapes its mean time over the
+    exhaustive best is below always-pairs, always-single-CTA and the library's size rule."""
+    from oracle import mlp_ref as R
+    p, doc = S.load_model(os.path.join(TUNING, "selector_mlp.json"))
+    assert doc["meta"].get("engine_output")
+    raw = open(os.path.join(TUNING, "selector_mlp.bin"), "rb").read()
+    assert int(np.frombuffer(raw[8:12], "<u4")[0]) == 2  # file version 2: the engine output is trained
+    d = np.load(os.path.join(TUNING, "autotune_heldout.npz"))
+    TE, sh = d["TE"], d["shapes"]
+    tuned = TE[:, 1] > 0
+    assert tuned.sum() >= 600
+    pred = R.forward(p.astype(np.float64), d["X"][tuned].astype(np.float64))
+    te = TE[tuned]
+    best = te.min(1)
+    rows = np.arange(len(te))
+    t_mlp = te[rows, np.where(pred[:, S.OUT_ENGINE] >= 0.0, 1, 0)]
+    t_rule = te[rows, [S.ozaki_engine_rule(int(r[0]), int(r[1]), int(r[2])) - 1 for r in sh[tuned]]]
+    r_mlp, r_rule = np.mean(t_mlp / best), np.mean(t_rule / best)
+    r_pair, r_one = np.mean(te[:, 1] / best), np.mean(te[:, 0] / best)
+    assert r_mlp < r_rule < r_pair and r_mlp < r_one, (r_mlp, r_rule, r_pair, r_one)
+    ev = json.load(open(os.path.join(TUNING, "selector_eval_heldout.json")))
+    assert abs(ev["ozaki_engine"]["mlp_mean_time_over_best"] - r_mlp) < 1e-3
