@@ -410,7 +410,7 @@ def evaluate(params, data):
             res["per_dtype"][name] = {"n": int(sel.sum()),
                                       "mlp_mean_throughput_regret": float(1.0 - np.mean(best[sel] / t_mlp[sel])),
                                       "rule_mean_throughput_regret": float(1.0 - np.mean(best[sel] / t_heur[sel]))}
-    if "TE" in data.files:
+    if "TE" in (data.files if hasattr(data, "files") else data):
         TE = data["TE"]
         tuned = TE[:, 1] > 0
         if tuned.any():
