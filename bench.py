@@ -51,10 +51,11 @@ SIZE = 16384
 SLICES = 8
 EMIN, EMAX = -20, 20
 SEED_A, SEED_B = 20261204, 20261205
-# DRAM read + write bytes of one ozaki_slice_gemm_pair_kernel launch at 4096^3, 7 slices, from
-# one ncu --set full capture (dram__bytes_read.sum + dram__bytes_write.sum)
-TRAFFIC_4096_BYTES = 7136346112 + 473230848
-TRAFFIC_SLICES = 7
+# DRAM bytes read and written by one ozaki_slice_gemm_pair_kernel launch at 4096^3 from ncu --set
+# full captures (dram__bytes_read.sum, dram__bytes_write.sum), with the products and int32 planes
+# of that launch: the digit form at 7 slices (28 products, 7 level planes) and the CRT form at 16
+# moduli (16 products, 16 planes)
+TRAFFIC_4096 = {"digits": (7136346112, 473230848, 28, 7), "crt": (1717197000, 1061339000, 16, 16)}
 
 
 def parse():
@@ -403,8 +404,11 @@ def run_gpu(args):
     e2e_steps = args.e2e_steps if args.e2e_steps > 0 else args.steps
     barrier()
     t0 = time.perf_counter()
+    call_ms = []
     for _ in range(e2e_steps):
-        blas.dgemm("N", "N", n, n, n, 1.0, an, n, bn, n, 0.0, cn, n)
+        t1 = time.perf_counter()
+        blas.dgemm("N", "N", n, n, n, 1.0, an, n, bn, n, 0.0, cn, n)  # returns after C is on the host
+        call_ms.append((time.perf_counter() - t1) * 1e3)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     blas.set_dgemm_mode(blas.DGEMM_NATIVE)
     if ws > 1:
@@ -421,10 +425,12 @@ def run_gpu(args):
     e2e_ok = bool(np.array_equal(cn, Ch2.numpy()))
     del Ch2
 
-    # ---------------- DRAM traffic of the dominant kernel: the ncu capture at 4096^3 above,
-    # scaled by the slice-product units of this size, (n/4096)^3, and by the product count
-    # (traffic per product is the same tiling; the planes written per product are the same)
-    traffic = TRAFFIC_4096_BYTES * (n / 4096.0) ** 3 * npairs / (TRAFFIC_SLICES * (TRAFFIC_SLICES + 1) // 2)
+    # ---------------- DRAM traffic of the dominant kernel from the ncu captures at 4096^3 above:
+    # reads scale with the slice-product units, (n/4096)^3 per product (each tile reads its rows
+    # and columns over all of k, in the same tiling), writes with the int32 planes, (n/4096)^2 per
+    # plane
+    rd, wr, prods, planes = TRAFFIC_4096[form]
+    traffic = rd * (n / 4096.0) ** 3 * npairs / prods + wr * (n / 4096.0) ** 2 * (npairs if form == "crt" else s) / planes
 
     if rank != 0:
         if ws > 1:
@@ -472,7 +478,8 @@ def run_gpu(args):
                 "matches_device_result": e2e_ok, "compared": "all of C, bit for bit",
                 "host_link_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs},
                 "copy_ms_if_serial": (2 * 8 * n * n / (h2d_gbs * 1e9) + 8 * n * n / (d2h_gbs * 1e9)) * 1e3,
-                "exposed_ms": e2e_ms - ms},
+                "exposed_ms": e2e_ms - ms,
+                "per_call_ms": {"min": min(call_ms), "median": float(np.median(call_ms)), "max": max(call_ms)}},
         "roofline": {"bound": "tensor", "kernel": "ozaki_slice_gemm", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "%s bf16_tflops_sustained" % peak_kind,

@@ -210,6 +210,7 @@ def load(path=None):
     _sig(L, "gb_launch_count", _i64, [])
     _sig(L, "gb_set_kernel_timing", C.c_int, [C.c_int])
     _sig(L, "gb_kernel_time_ms", _d, [_cp, C.POINTER(_i64)])
+    _sig(L, "gb_kernel_trace", _i64, [C.c_void_p, _i64])
     _sig(L, "gb_synchronize", C.c_int, [])
     _lib = L
     return L

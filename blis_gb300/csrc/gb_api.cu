@@ -256,6 +256,7 @@ int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double 
         cudaStreamWaitEvent(ss, ev_alloc, 0);
         auto copy_a = [&](int i) {
             const int64_t r0 = rb[i], rows = rb[i + 1] - rb[i];
+            LaunchScope ls("copy_h2d_a", cin, false);
             if (!rc)
                 rc = ta ? check_cuda(cudaMemcpy2DAsync(ad + r0 * k, k * sizeof(double), a + r0 * lda,
                                                        lda * sizeof(double), k * sizeof(double), rows,
@@ -266,6 +267,7 @@ int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double 
         };
         auto copy_b = [&](int j) {
             const int64_t j0 = col0(j), nj = col0(j + 1) - j0;
+            LaunchScope ls("copy_h2d_b", cin, false);
             if (!rc)
                 rc = check_cuda(cudaMemcpy2DAsync(bd + j0 * k, k * sizeof(double), b + j0 * ldb, ldb * sizeof(double),
                                                   k * sizeof(double), nj, cudaMemcpyDefault, cin), "B block");
@@ -300,6 +302,7 @@ int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double 
             if (!rc) rc = ozaki_multiply_rows(&prep, r0, rows, &pb[(size_t)j], alpha, beta, cd + j0 * m + r0, 1, m, ps);
             cudaEventRecord(ev_c[i * nch + j], ps);
             cudaStreamWaitEvent(cout, ev_c[i * nch + j], 0);
+            LaunchScope ls("copy_d2h_c", cout, false);
             if (!rc)
                 rc = check_cuda(cudaMemcpy2DAsync(c + j0 * ldc + r0, ldc * sizeof(double), cd + j0 * m + r0,
                                                   m * sizeof(double), rows * sizeof(double), nj, cudaMemcpyDefault,

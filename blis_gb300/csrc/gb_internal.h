@@ -54,10 +54,11 @@ enum : unsigned int {
 };
 
 // Wrap every kernel launch: counts it and, when per-kernel timing is on,
-// brackets it with CUDA events recorded on the launching stream.
+// brackets it with CUDA events recorded on the launching stream.  A copy
+// wrapped for the timeline passes is_kernel = false (recorded, not counted).
 class LaunchScope {
   public:
-    LaunchScope(const char* name, cudaStream_t s);
+    LaunchScope(const char* name, cudaStream_t s, bool is_kernel = true);
     ~LaunchScope();
 
   private:
@@ -252,6 +253,12 @@ int ozaki_form();
 // reaches `bits`, or -1; the digit count of equal precision (grouped batch).
 int ozaki_crt_bits(int n, int64_t k);
 int ozaki_crt_moduli_for_bits(int bits, int64_t k);
+// B := B - A X in the digit form at `slices` slices, one launch (R <= 128 rows,
+// k <= 128): bit-identical to dgemm_ozaki(rows, n, k, -1, A, X, 1, B) with
+// the same slices.
+bool trsm_update_fused_fits(int slices, int64_t rows, int64_t k, int64_t n);
+int trsm_update_fused(int slices, int64_t rows, int64_t k, int64_t n, const double* a, int64_t ars, int64_t acs,
+                      const double* x, int64_t xrs, int64_t xcs, double* b, int64_t brs, int64_t bcs, cudaStream_t s);
 int ozaki_digit_slices();
 // SGEMM split form (gb_sgemm_split.cu): the digit form with this many slices on
 // FP64-widened operands; whether a shape takes it (gb_set_sgemm_mode).

@@ -88,6 +88,10 @@ struct OzGemmParams {
     const int* tile_cum = nullptr;
     const int* tile_first = nullptr;
     OzLevel lv[OZ_MAX_LEVELS];
+    // CRT form: planes hold int16 residues of the product sums modulo plane L's modulus
+    // crt_p[L] (with 1 / p and 2^16 mod p, symmetric, for the reduction); else int32 level sums
+    int crt = 0;
+    float crt_p[OZ_MAX_LEVELS], crt_invp[OZ_MAX_LEVELS], crt_w16[OZ_MAX_LEVELS];
 };
 
 struct OzItem {
@@ -317,16 +321,38 @@ __device__ __forceinline__ void oz_load_stage(const OzBatchParams& p, const CUte
     tma_load_3d(sb, mb, bar, 0, 0, (int)zb);
 }
 
-// Level sums of one epilogue thread (row quad*32 + lane, columns half*128 ..
-// +127 of the tile) into the level plane.
-__device__ __forceinline__ void oz_store_sums(const OzGemmParams& p, const OzItem& w, int quad, int half,
-                                              int lane, const int32_t (&acc)[128])
+// A CRT product sum v reduced to its symmetric residue modulo the plane's
+// modulus p (|r| <= p/2 <= 128, stored as int16).  With v = hi 2^16 + lo,
+// lo in [0, 2^16), and w = 2^16 mod p in [-p/2, p/2]: s = hi w + lo has
+// |s| < 2^22 + 2^16, an integer exact in fp32 (the fma rounds nothing) with
+// v's residue; rint(s / p) by one fma onto 1.5 2^23 is exact as in the split
+// (s invp is within |s| 2^-24 / p < 0.27 / p of s / p, and a non-integral
+// s / p is at least 1 / (2p) from a half-integer; for p = 256, invp is exact
+// and a tie rounds to even, either sign being the same residue).
+__device__ __forceinline__ int16_t oz_crt_reduce(int32_t v, float p, float invp, float w16)
 {
-    const int64_t i = (int64_t)w.tm * OZ_BM + quad * 32 + lane;
-    const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
-    if (i >= p.m) return;
-    int32_t* dst = p.planes + ((int64_t)w.plane * p.npad + j0) * p.mpad + i;
+    const float sv = __fmaf_rn((float)(v >> 16), w16, (float)(v & 0xFFFF));
+    const float q = __fmaf_rn(sv, invp, 12582912.0f) - 12582912.0f;  // 1.5 2^23
+    return (int16_t)__float2int_rn(__fmaf_rn(-q, p, sv));
+}
+
+// The product sums of one epilogue thread (row i of C, columns j0 .. j0 + 127)
+// into plane w.plane: int32 level sums, or int16 residues in the CRT form.
+__device__ __forceinline__ void oz_store_plane(const OzGemmParams& p, const OzItem& w, int64_t i, int64_t j0,
+                                               const int32_t (&acc)[128])
+{
+    if (i >= p.m) return;  // level sums of padding rows and columns are not stored
     const int64_t jn = p.n - j0;  // columns of this half that exist
+    const int64_t at = ((int64_t)w.plane * p.npad + j0) * p.mpad + i;
+    if (p.crt) {
+        int16_t* dst = reinterpret_cast<int16_t*>(p.planes) + at;
+        const float pm = p.crt_p[w.plane], ip = p.crt_invp[w.plane], w16 = p.crt_w16[w.plane];
+#pragma unroll
+        for (int c = 0; c < 128; ++c)
+            if (jn >= 128 || c < jn) dst[(int64_t)c * p.mpad] = oz_crt_reduce(acc[c], pm, ip, w16);
+        return;
+    }
+    int32_t* dst = p.planes + at;
     if (jn >= 128) {
 #pragma unroll
         for (int c = 0; c < 128; ++c) dst[(int64_t)c * p.mpad] = acc[c];
@@ -335,6 +361,14 @@ __device__ __forceinline__ void oz_store_sums(const OzGemmParams& p, const OzIte
         for (int c = 0; c < 128; ++c)
             if (c < jn) dst[(int64_t)c * p.mpad] = acc[c];
     }
+}
+
+// Level sums of one epilogue thread (row quad*32 + lane, columns half*128 ..
+// +127 of the tile) into the level plane.
+__device__ __forceinline__ void oz_store_sums(const OzGemmParams& p, const OzItem& w, int quad, int half,
+                                              int lane, const int32_t (&acc)[128])
+{
+    oz_store_plane(p, w, (int64_t)w.tm * OZ_BM + quad * 32 + lane, (int64_t)w.tn * OZ_BN + half * 128, acc);
 }
 
 __device__ __forceinline__ void oz_store_sums(const OzBatchParams& p, const OzItem& w, int quad, int half,
@@ -869,20 +903,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 ++chunk_ctr;
             }
             if (!ok) break;
-            const int64_t i = (int64_t)w.tm * (2 * OZ2_ROWS) + (int64_t)rank * OZ2_ROWS + quad * 32 + lane;
-            const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
-            if (i < p.m) {  // level sums of padding rows and columns are not stored
-                int32_t* dst = p.planes + ((int64_t)w.plane * p.npad + j0) * p.mpad + i;
-                const int64_t jn = p.n - j0;
-                if (jn >= 128) {
-#pragma unroll
-                    for (int c = 0; c < 128; ++c) dst[(int64_t)c * p.mpad] = acc[c];
-                } else {
-#pragma unroll
-                    for (int c = 0; c < 128; ++c)
-                        if (c < jn) dst[(int64_t)c * p.mpad] = acc[c];
-                }
-            }
+            oz_store_plane(p, w, (int64_t)w.tm * (2 * OZ2_ROWS) + (int64_t)rank * OZ2_ROWS + quad * 32 + lane,
+                           (int64_t)w.tn * OZ_BN + half * 128, acc);
         }
     }
 
@@ -1542,36 +1564,39 @@ __device__ __forceinline__ unsigned long long oz_crt_scaled(unsigned long long b
 }
 
 // The N residues of x as floats (integers, |r| <= 128), from NL 12-bit limbs of X
-// (NL = 5 for t <= 59, else 6): s_l = sum_q h_q (2^(12q) mod p_l) < 6 2^12 2^8 < 2^22.6
-// is exact in fp32, and rint(s_l / p_l) by one fma onto 1.5 2^23 (unit in the last place
-// 1) is exact: the fma rounds s_l invp_l, which differs from s_l / p_l by at most
-// s_l 2^-24 / p_l < 0.38 / p_l, while a non-integral s_l / p_l is at least 1 / (2 p_l) from
-// a half-integer.
+// (NL = 5 for t <= 59, else 6) carrying x's sign: s_l = sum_q h_q (2^(12q) mod p_l),
+// |s_l| < 6 2^12 2^8 < 2^22.6, is exact in fp32, and rint(s_l / p_l) by one fma onto
+// 1.5 2^23 (unit in the last place 1) is exact: the fma rounds s_l invp_l, which differs
+// from s_l / p_l by at most |s_l| 2^-24 / p_l < 0.38 / p_l, while a non-integral s_l / p_l
+// is at least 1 / (2 p_l) from a half-integer.  s_l - rint(s_l / p_l) p_l is then the
+// symmetric residue of the signed value.
 template <int N, int NL>
 __device__ __forceinline__ void oz_crt_residues(double x, int e, const OzCrtTab& tab, float (&r)[N])
 {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
     const unsigned long long X = oz_crt_scaled(bits & 0x7FFFFFFFFFFFFFFFull, e, tab.t);
+    // limb q of X as a float with x's sign: the limb's bits OR-ed into +-2^23, minus +-2^23
+    const uint32_t sgn = (uint32_t)(bits >> 32) & 0x80000000u;
+    const float off = sgn ? 8388608.0f : -8388608.0f;
     float h[NL];
 #pragma unroll
-    for (int q = 0; q < NL; ++q)  // limb q of X as a float: its bits OR-ed into 2^23, minus 2^23
-        h[q] = __uint_as_float(0x4B000000u | (uint32_t)((X >> (12 * q)) & 4095u)) - 8388608.0f;
-    const bool neg = (bits >> 63) != 0;
+    for (int q = 0; q < NL; ++q) h[q] = __uint_as_float(sgn | 0x4B000000u | (uint32_t)((X >> (12 * q)) & 4095u)) + off;
 #pragma unroll
     for (int l = 0; l < N; ++l) {
         float sl = 0.0f;
 #pragma unroll
         for (int q = 0; q < NL; ++q) sl = __fmaf_rn(h[q], tab.pw[l][q], sl);
         const float q = __fmaf_rn(sl, tab.invp[l], OZ_MAGIC) - OZ_MAGIC;
-        const float rr = __fmaf_rn(-q, tab.p[l], sl);
-        r[l] = neg ? -rr : rr;
+        r[l] = __fmaf_rn(-q, tab.p[l], sl);
     }
 }
 
 // Tile of 32 rows x 64 k per block (as oz_split_kernel); writes N bf16
-// residue planes, K-major, zero in the padding.
+// residue planes, K-major, zero in the padding.  Warp w converts rows 4w ..
+// 4w + 3 in turn, lane c elements 2c and 2c + 1 of the row: every plane store
+// of a warp is one contiguous 128-byte line.
 template <int N, int NL>
-__global__ void __launch_bounds__(256) oz_crt_split_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
+__global__ void __launch_bounds__(256, 4) oz_crt_split_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
                                                            int64_t sr, int64_t sl,
                                                            const unsigned long long* __restrict__ maxbits,
                                                            int64_t rpad, int64_t kpad, uint16_t* __restrict__ out,
@@ -1590,29 +1615,27 @@ __global__ void __launch_bounds__(256) oz_crt_split_kernel(int64_t rows, int64_t
         tile[rr][ll] = (r < rows && l < k) ? __ldcs(R + r * sr + l * sl) : 0.0;
     }
     __syncthreads();
-    const int rr = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 8;
-    const int64_t r = r0 + rr;
-    int e = 0;
-    if (r < rows) {
-        int nf = 0;
-        e = oz_row_exponent(maxbits[r], &nf);
-        if (nf) *nonfinite = 1;
-        if (blockIdx.x == 0 && (threadIdx.x & 7) == 0) exps[r] = e;
-    }
-    uint32_t packed[N][4];
-#pragma unroll
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t plane_words = rpad * kpad / 2;  // one residue plane in 32-bit words
+#pragma unroll 1
     for (int h = 0; h < 4; ++h) {
+        const int rr = warp * 4 + h;
+        const int64_t r = r0 + rr;
+        int e = 0;
+        if (r < rows) {
+            int nf = 0;
+            e = oz_row_exponent(maxbits[r], &nf);
+            if (nf) *nonfinite = 1;
+            if (blockIdx.x == 0 && lane == 0) exps[r] = e;
+        }
         float f0[N], f1[N];
-        oz_crt_residues<N, NL>(r < rows ? tile[rr][c0 + 2 * h] : 0.0, e, tab, f0);
-        oz_crt_residues<N, NL>(r < rows ? tile[rr][c0 + 2 * h + 1] : 0.0, e, tab, f1);
+        oz_crt_residues<N, NL>(r < rows ? tile[rr][2 * lane] : 0.0, e, tab, f0);
+        oz_crt_residues<N, NL>(r < rows ? tile[rr][2 * lane + 1] : 0.0, e, tab, f1);
+        // kpad and l0 are multiples of 64: the pair's 4 bytes are aligned
+        uint32_t* dst = reinterpret_cast<uint32_t*>(out + r * kpad + l0) + lane;
 #pragma unroll
         for (int l = 0; l < N; ++l)
-            packed[l][h] = __byte_perm(__float_as_uint(f0[l]), __float_as_uint(f1[l]), 0x7632);
-    }
-#pragma unroll
-    for (int l = 0; l < N; ++l) {
-        uint4* dst = reinterpret_cast<uint4*>(out + ((int64_t)l * rpad + r) * kpad + l0 + c0);
-        *dst = make_uint4(packed[l][0], packed[l][1], packed[l][2], packed[l][3]);
+            dst[(int64_t)l * plane_words] = __byte_perm(__float_as_uint(f0[l]), __float_as_uint(f1[l]), 0x7632);
     }
 }
 
@@ -1633,10 +1656,17 @@ __global__ void __launch_bounds__(256, 2) oz_crt_recombine_kernel(const __grid_c
         const int64_t dlo = (int64_t)p.out_rpc * j, dhi = dlo + p.out_rpc - 1;
         if (p.out_tri && (p.out_tri == 1 ? i0 + 3 < dlo : i0 > dhi)) continue;
         const int64_t off = j * p.mpad + i0;
+        // four int16 residues of consecutive rows per plane (8-byte aligned: mpad and i0 are
+        // multiples of 4), sign-extended
+        const int16_t* planes16 = reinterpret_cast<const int16_t*>(p.planes);
         int4 v[N];
 #pragma unroll
-        for (int L = 0; L < N; ++L)
-            v[L] = __ldcs(reinterpret_cast<const int4*>(p.planes + (int64_t)p.lv[L].plane_base * plane_stride + off));
+        for (int L = 0; L < N; ++L) {
+            const uint2 raw =
+                __ldcs(reinterpret_cast<const uint2*>(planes16 + (int64_t)p.lv[L].plane_base * plane_stride + off));
+            v[L] = make_int4((int)(int16_t)(raw.x & 0xFFFFu), (int)raw.x >> 16, (int)(int16_t)(raw.y & 0xFFFFu),
+                             (int)raw.y >> 16);
+        }
         const int ebj = p.eb[j] - 2 * tab.t - 2;
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
@@ -2398,7 +2428,20 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
     p.tri_rows = (int)A->row_tile;
     p.tri_row0 = r0;
 
-    const size_t bytes_pl = (size_t)planes_total * npad * mpad * 4;
+    if (A->crt) {
+        OzCrtTab tab;
+        crt_table(slices, A->crt_t, &tab);
+        p.crt = 1;
+        for (int L = 0; L < slices; ++L) {
+            const int pm = (int)tab.p[L];
+            const int w = 65536 % pm;
+            p.crt_p[L] = tab.p[L];
+            p.crt_invp[L] = tab.invp[L];
+            p.crt_w16[L] = (float)(2 * w > pm ? w - pm : w);
+        }
+    }
+    // CRT planes hold int16 residues, the digit form's int32 level sums
+    const size_t bytes_pl = (size_t)planes_total * npad * mpad * (A->crt ? 2 : 4);
     const size_t bytes_tab = A->out_tri ? sizeof(int) * (size_t)(2 * p.tiles_m + 1) : 0;
     int32_t* planes = static_cast<int32_t*>(dev_alloc(bytes_pl + 1024 + bytes_tab, s));
     if (!planes) return GB_ERR_NOMEM;
@@ -3023,6 +3066,282 @@ int bgemm_tc(int64_t m, int64_t n, int64_t k, float alpha, const uint16_t* a, in
     dev_free(own_a, s);
     dev_free(own_b, s);
     return rc;
+}
+
+namespace {
+
+// ---------------------------------------------------------------- fused TRSM update
+// B := B - A X for one of the small updates at the bottom of the TRSM
+// recursion (R <= 128 rows, depth K <= 128, any n columns), the digit form
+// at S <= 7 slices in one launch instead of four (split, slice GEMM,
+// recombination, gated IEEE fallback).  CTA j owns columns [32j, 32j + 32)
+// of X and B.  It takes the row exponents of A and the column exponents of
+// its X columns as the split kernels do, writes the digits of each 64-deep
+// k chunk of both operands into shared memory in the 128-byte-swizzled
+// K-major layout that TMA gives the slice GEMM, and issues the S(S+1)/2
+// digit products of the chunk as M=128 N=32 K=16 tcgen05 MMAs (one thread)
+// into S level accumulators in TMEM.  fp32 holds the level sums exactly:
+// |sum| <= K P 128^2 <= 2^24 for K <= 128 and P <= 8 products per level.
+// The epilogue reads the level sums back and recombines each entry as
+// oz_recombine_kernel does (exact weighted sum, one rounding, B - AB rounded
+// once), so the update is bit-identical to the four-launch form.  A tile
+// with an Inf or NaN in A or in its X columns takes FP64 FMAs instead.
+constexpr int TU_THREADS = 256;
+constexpr int TU_N = 32;                      // columns of X and B per CTA
+constexpr int TU_ROWS = 128;                  // MMA rows (zero beyond R)
+constexpr int TU_KC = 64;                     // k of one chunk
+constexpr int TU_MAXS = 8;                    // slices (TMEM: 8 levels x 32 columns)
+constexpr int TU_A_PLANE = TU_ROWS * 128;     // one digit plane of a chunk of A: 16 KB
+constexpr int TU_B_PLANE = TU_N * 128;        // one of X^T: 4 KB
+constexpr int TU_SMEM_BYTES = TU_MAXS * (TU_A_PLANE + TU_B_PLANE) + 1024 + 64;
+constexpr uint32_t TU_TMEM_COLS = 256;
+
+struct TuArgs {
+    int R, K;
+    int64_t n;
+    const double* a;  // A(i, l) = a[i*ars + l*acs]
+    int64_t ars, acs;
+    const double* x;  // X(l, j) = x[l*xrs + j*xcs]
+    int64_t xrs, xcs;
+    double* b;  // B(i, j) = b[i*brs + j*bcs]
+    int64_t brs, bcs;
+    unsigned int* status;
+};
+
+// byte offset of element (row, k) of a 128-byte-swizzled K-major plane of bf16 (k < 64)
+__device__ __forceinline__ uint32_t tu_swz(int row, int k)
+{
+    return (uint32_t)(row * 128 + ((((k >> 3) ^ (row & 7))) << 4) + (k & 7) * 2);
+}
+
+template <int S>
+__global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const TuArgs p)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* sa = smem;                          // S planes of 16 KB
+    uint8_t* sb = smem + TU_MAXS * TU_A_PLANE;   // S planes of 4 KB
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + TU_MAXS * (TU_A_PLANE + TU_B_PLANE));
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+    __shared__ int er[TU_ROWS], ec[TU_N];
+    __shared__ int s_nf, s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t c0 = (int64_t)blockIdx.x * TU_N;
+    const int ncols = (p.n - c0 < TU_N) ? (int)(p.n - c0) : TU_N;
+    const int R = p.R, K = p.K;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_barrier_init();
+        s_nf = 0;
+        s_fail = 0;
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_slot, TU_TMEM_COLS);
+        tmem_relinquish();
+    }
+    __syncthreads();
+    // exponents: thread per row of A; warp w for columns 4w .. 4w + 3 of X
+    if (tid < TU_ROWS) {
+        unsigned long long mx = 0;
+        if (tid < R)
+            for (int l = 0; l < K; ++l) {
+                const unsigned long long v = abs_bits(p.a[(int64_t)tid * p.ars + (int64_t)l * p.acs]);
+                mx = v > mx ? v : mx;
+            }
+        int nf = 0;
+        er[tid] = oz_row_exponent(mx, &nf);
+        if (nf) s_nf = 1;
+    }
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+        const int c = warp * 4 + cc;
+        unsigned long long mx = 0;
+        if (c < ncols)
+            for (int l = lane; l < K; l += 32) {
+                const unsigned long long v = abs_bits(p.x[(int64_t)l * p.xrs + (c0 + c) * p.xcs]);
+                mx = v > mx ? v : mx;
+            }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
+            mx = v > mx ? v : mx;
+        }
+        if (lane == 0) {
+            int nf = 0;
+            ec[c] = oz_row_exponent(mx, &nf);
+            if (nf) s_nf = 1;
+        }
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    if (s_nf) {
+        // IEEE path for this tile: B - A X by FP64 FMAs
+        for (int e = tid; e < R * ncols; e += TU_THREADS) {
+            const int i = e % R, j = e / R;
+            double t = 0.0;
+            for (int l = 0; l < K; ++l)
+                t = fma(p.a[(int64_t)i * p.ars + (int64_t)l * p.acs], p.x[(int64_t)l * p.xrs + (c0 + j) * p.xcs], t);
+            double* bij = p.b + (int64_t)i * p.brs + (c0 + j) * p.bcs;
+            *bij = *bij - t;
+        }
+    } else {
+        uint32_t phase = 0;
+        for (int k0 = 0; k0 < K; k0 += TU_KC) {
+            // digits of A (rows beyond R and k beyond K are zero), two k per 32-bit word;
+            // consecutive threads take consecutive rows (column-major A reads coalesce)
+            for (int e = tid; e < TU_ROWS * (TU_KC / 2); e += TU_THREADS) {
+                const int row = e & (TU_ROWS - 1), kp = e >> 7;
+                const int l = k0 + 2 * kp;
+                const double* ar = p.a + (int64_t)row * p.ars;
+                const double v0 = (row < R && l < K) ? ar[(int64_t)l * p.acs] : 0.0;
+                const double v1 = (row < R && l + 1 < K) ? ar[(int64_t)(l + 1) * p.acs] : 0.0;
+                uint32_t w[S];
+                oz_digits_bf16x2<S>(v0, v1, er[row], w);
+                const uint32_t off = tu_swz(row, 2 * kp);
+#pragma unroll
+                for (int q = 0; q < S; ++q) *reinterpret_cast<uint32_t*>(sa + q * TU_A_PLANE + off) = w[q];
+            }
+            // digits of X^T (columns beyond n are zero); lanes run along k
+            for (int e = tid; e < TU_N * (TU_KC / 2); e += TU_THREADS) {
+                const int kp = e & 31, c = e >> 5;
+                const int l = k0 + 2 * kp;
+                const double* xc = p.x + (c0 + c) * p.xcs;
+                const double v0 = (c < ncols && l < K) ? xc[(int64_t)l * p.xrs] : 0.0;
+                const double v1 = (c < ncols && l + 1 < K) ? xc[(int64_t)(l + 1) * p.xrs] : 0.0;
+                uint32_t w[S];
+                oz_digits_bf16x2<S>(v0, v1, ec[c], w);
+                const uint32_t off = tu_swz(c, 2 * kp);
+#pragma unroll
+                for (int q = 0; q < S; ++q) *reinterpret_cast<uint32_t*>(sb + q * TU_B_PLANE + off) = w[q];
+            }
+            fence_proxy_async();  // the digits, written by threads, become visible to the MMAs
+            __syncthreads();
+            if (tid == 0) {
+                tc_fence_after();
+                constexpr uint32_t idesc = idesc_bf16_f32(TU_ROWS, TU_N);
+                for (int L = 2; L <= S + 1; ++L) {
+                    const uint32_t d_tmem = tmem + (uint32_t)((L - 2) * TU_N);
+                    bool first = (k0 == 0);
+                    const int pa_lo = (L - S > 1) ? L - S : 1, pa_hi = (L - 1 < S) ? L - 1 : S;
+                    for (int pa = pa_lo; pa <= pa_hi; ++pa) {
+                        const uint64_t ad = sdesc_kmajor_sw128(smem_addr(sa + (pa - 1) * TU_A_PLANE));
+                        const uint64_t bd = sdesc_kmajor_sw128(smem_addr(sb + (L - pa - 1) * TU_B_PLANE));
+#pragma unroll
+                        for (int j = 0; j < TU_KC / 16; ++j)
+                            mma_bf16_ss(d_tmem, ad + 2 * j, bd + 2 * j, idesc, (first && j == 0) ? 0u : 1u);
+                        first = false;
+                    }
+                }
+                mma_commit(bar);
+            }
+            __syncwarp();
+            int ok = 1;
+            if (lane == 0) ok = mbar_wait_bounded(bar, phase, kWaitBudgetNs) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok && lane == 0) {
+                atomicOr(p.status, DEV_WAIT_TIMEOUT);
+                s_fail = 1;
+            }
+            phase ^= 1u;
+            __syncthreads();  // the next chunk overwrites the digits only after the MMAs read them
+            tc_fence_after();
+            if (s_fail) break;
+        }
+        if (!s_fail) {
+            // warp w reads TMEM lanes 32 (w % 4) .. (rows) and columns 16 (w / 4) .. + 15
+            const int qd = warp & 3, half = warp >> 2;
+            const int row = qd * 32 + lane;
+#pragma unroll 1
+            for (int g = 0; g < 2; ++g) {
+                const int cb = half * 16 + g * 8;
+                int32_t lv[S][8];
+#pragma unroll
+                for (int li = 0; li < S; ++li) {
+                    uint32_t r8[8];
+                    tmem_ld_32x32b_x8(tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(li * TU_N + cb), r8);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) lv[li][c] = __float2int_rn(__uint_as_float(r8[c]));
+                }
+                if (row < R) {
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        const int col = cb + c;
+                        if (col >= ncols) break;
+                        int a[S];  // a[t] is level S + 1 - t, weight 2^(8t)
+#pragma unroll
+                        for (int li = 0; li < S; ++li) a[S - 1 - li] = lv[li][c];
+                        const __int128 T = oz_weighted_sum<S>(a);
+                        const double ab = round_scaled(T, er[row] + ec[col] - 8 * (S + 1));
+                        double* bij = p.b + (int64_t)row * p.brs + (c0 + col) * p.bcs;
+                        *bij = __fma_rn(1.0, *bij, -ab);
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, TU_TMEM_COLS);
+}
+
+template <int S>
+int launch_trsm_update_fused(const TuArgs& a, cudaStream_t s)
+{
+    static bool attr = false;
+    if (!attr) {
+        const int rc = check_cuda(cudaFuncSetAttribute(trsm_update_fused_kernel<S>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, TU_SMEM_BYTES),
+                                  "trsm update smem attr");
+        if (rc) return rc;
+        attr = true;
+    }
+    const int64_t grid = (a.n + TU_N - 1) / TU_N;
+    LaunchScope ls("trsm_update_fused", s);
+    trsm_update_fused_kernel<S><<<(unsigned)grid, TU_THREADS, TU_SMEM_BYTES, s>>>(a);
+    return check_cuda(cudaGetLastError(), "trsm_update_fused");
+}
+
+}  // namespace
+
+bool trsm_update_fused_fits(int slices, int64_t rows, int64_t k, int64_t n)
+{
+    return slices >= 2 && slices <= TU_MAXS && rows >= 1 && rows <= TU_ROWS && k >= 1 && k <= 2 * TU_KC && n >= 1 &&
+           (n + TU_N - 1) / TU_N <= INT32_MAX;
+}
+
+int trsm_update_fused(int slices, int64_t rows, int64_t k, int64_t n, const double* a, int64_t ars, int64_t acs,
+                      const double* x, int64_t xrs, int64_t xcs, double* b, int64_t brs, int64_t bcs, cudaStream_t s)
+{
+    if (!trsm_update_fused_fits(slices, rows, k, n))
+        return set_error(GB_ERR_ARG, "trsm_update_fused", "update outside the fused kernel's shape");
+    TuArgs t;
+    t.R = (int)rows;
+    t.K = (int)k;
+    t.n = n;
+    t.a = a;
+    t.ars = ars;
+    t.acs = acs;
+    t.x = x;
+    t.xrs = xrs;
+    t.xcs = xcs;
+    t.b = b;
+    t.brs = brs;
+    t.bcs = bcs;
+    t.status = device_status_word();
+    note_ozaki_slices(slices);
+    switch (slices) {
+    case 2: return launch_trsm_update_fused<2>(t, s);
+    case 3: return launch_trsm_update_fused<3>(t, s);
+    case 4: return launch_trsm_update_fused<4>(t, s);
+    case 5: return launch_trsm_update_fused<5>(t, s);
+    case 6: return launch_trsm_update_fused<6>(t, s);
+    case 7: return launch_trsm_update_fused<7>(t, s);
+    default: return launch_trsm_update_fused<8>(t, s);
+    }
 }
 
 }  // namespace gb

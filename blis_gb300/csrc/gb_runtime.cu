@@ -210,9 +210,9 @@ thread_local int t_last_slices = -1;
 void note_ozaki_slices(int slices) { t_last_slices = slices; }
 
 // ---------------------------------------------------------------- launches
-LaunchScope::LaunchScope(const char* name, cudaStream_t s) : name_(name), s_(s), timed_(false)
+LaunchScope::LaunchScope(const char* name, cudaStream_t s, bool is_kernel) : name_(name), s_(s), timed_(false)
 {
-    g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (is_kernel) g_launches.fetch_add(1, std::memory_order_relaxed);
     if (g_timing.load(std::memory_order_relaxed)) {
         timed_ = true;
         cudaEventCreate(&start_);
@@ -317,6 +317,35 @@ double gb_kernel_time_ms(const char* prefix, int64_t* launches)
     gb::g_timed.swap(keep);
     if (launches) *launches = cnt;
     return total;
+}
+
+int64_t gb_kernel_trace(gb_trace_entry_t* out, int64_t max_entries)
+{
+    std::lock_guard<std::mutex> lk(gb::g_timing_mu);
+    const int64_t n = (int64_t)gb::g_timed.size();
+    if (n == 0) return 0;
+    cudaEvent_t origin = gb::g_timed[0].start;
+    for (auto& t : gb::g_timed) cudaEventSynchronize(t.stop);
+    int64_t w = 0;
+    for (auto& t : gb::g_timed) {
+        if (out && w < max_entries) {
+            float t0 = 0.f, t1 = 0.f;
+            cudaEventElapsedTime(&t0, origin, t.start);
+            cudaEventElapsedTime(&t1, origin, t.stop);
+            gb_trace_entry_t& e = out[w];
+            strncpy(e.name, t.name.c_str(), sizeof(e.name) - 1);
+            e.name[sizeof(e.name) - 1] = 0;
+            e.start_ms = t0;
+            e.end_ms = t1;
+            ++w;
+        }
+    }
+    for (auto& t : gb::g_timed) {
+        cudaEventDestroy(t.start);
+        cudaEventDestroy(t.stop);
+    }
+    gb::g_timed.clear();
+    return w;
 }
 
 int gb_synchronize(void)

@@ -402,15 +402,44 @@ int launch_trsv(bool lower, bool unit, int64_t m, double alpha, const double* a,
     return rc;
 }
 
+// Depth (k) from which a precision-form TRSM update runs in the CRT form, at the
+// moduli that carry the digit form's precision (GB_TRSM_CRT_MIN_K; 0 never): its
+// 16 or so products against the digit form's s(s+1)/2 pay for the wider split and
+// recombination only on the deep updates at the top of the recursion.
+int64_t trsm_crt_min_k()
+{
+    static int64_t v = -1;
+    if (v < 0) {
+        const char* e = getenv("GB_TRSM_CRT_MIN_K");
+        v = e ? atoll(e) : 2048;
+        if (v < 0) v = 0;
+    }
+    return v;
+}
+
 int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t ccount)
 {
     // B[r0:r0+rcount, :] -= op(A)[r0:.., c0:c0+ccount] * X[c0:c0+ccount, :]
     const double* ap = t.a + r0 * t.ars + c0 * t.acs;
     const double* xp = t.b + c0 * t.brs;
     double* bp = t.b + r0 * t.brs;
-    if (t.slices > 0 && (double)rcount * (double)ccount * (double)t.n >= trsm_ozaki_min_fma())
+    if (t.slices > 0 && (double)rcount * (double)ccount * (double)t.n >= trsm_ozaki_min_fma()) {
+        // the small updates at the bottom of the recursion: one fused launch
+        // (GB_TRSM_FUSED=0 turns it off; read per call)
+        const char* fz = getenv("GB_TRSM_FUSED");
+        if (!(fz && fz[0] == '0') && trsm_update_fused_fits(t.slices, rcount, ccount, t.n))
+            return trsm_update_fused(t.slices, rcount, ccount, t.n, ap, t.ars, t.acs, xp, t.brs, t.bcs, bp, t.brs,
+                                     t.bcs, t.s);
+        const int64_t kc = trsm_crt_min_k();
+        const int moduli = (kc > 0 && ccount >= kc) ? ozaki_crt_moduli_for_bits(8 * t.slices - 1, ccount) : -1;
+        if (moduli > 0) {
+            ModeOverride crt(GB_DGEMM_OZAKI, moduli, 1);
+            return dgemm_ozaki(rcount, t.n, ccount, -1.0, ap, t.ars, t.acs, xp, t.brs, t.bcs, 1.0, bp, t.brs,
+                               t.bcs, moduli, t.s);
+        }
         return dgemm_ozaki(rcount, t.n, ccount, -1.0, ap, t.ars, t.acs, xp, t.brs, t.bcs, 1.0, bp,
                            t.brs, t.bcs, t.slices, t.s);
+    }
     return dgemm_native(rcount, t.n, ccount, -1.0, ap, t.ars, t.acs, xp, t.brs, t.bcs, 1.0, bp,
                         t.brs, t.bcs, t.s);
 }
@@ -511,9 +540,10 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
               int slices, cudaStream_t s)
 {
     if (m <= 0 || n <= 0) return GB_SUCCESS;
-    // the updates keep the digit form: measured on GB300, the CRT form's sixteen residue planes
-    // cost more to split and recombine than its fewer products save on updates of this depth
-    // (8192 x 4096: 13.8 ms with 7 digit slices, 19.5 ms with 16 moduli)
+    // the updates take the digit form, the deep ones the CRT form at the same precision
+    // (update): measured on GB300, the CRT form's residue planes cost more to split and
+    // recombine than its fewer products save on shallow updates (8192 x 4096: 13.8 ms with
+    // every update in 7 digit slices, 19.5 ms with every update in 16 moduli)
     if (slices > 0 && ozaki_form() == 1) slices = ozaki_digit_slices();
     ModeOverride digits(dgemm_mode(), slices, 0);
     int64_t brs = rs_b, bcs = cs_b, mm = m, nn = n;

@@ -211,5 +211,17 @@ def kernel_time_ms(prefix):
     return ms, int(n.value)
 
 
+class _TraceEntry(C.Structure):
+    _fields_ = [("name", C.c_char * 40), ("start_ms", C.c_double), ("end_ms", C.c_double)]
+
+
+def kernel_trace(max_entries=1 << 16):
+    """The recorded launches (and the host pipeline's copies) as a timeline:
+    [(name, start_ms, end_ms)] from the first record's start; forgets them."""
+    buf = (_TraceEntry * max_entries)()
+    n = _lib.load().gb_kernel_trace(C.cast(buf, C.c_void_p), max_entries)
+    return [(buf[i].name.decode(), buf[i].start_ms, buf[i].end_ms) for i in range(n)]
+
+
 def synchronize():
     return _lib.check(_lib.load().gb_synchronize(), "gb_synchronize")

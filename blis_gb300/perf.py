@@ -100,7 +100,7 @@ def run_gemm(out):
     del a, b, c
     fa, fb, fc = (_mat(n, n, seed=s, dtype=torch.float32) for s in (7, 8, 9))
     ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
-    out.append({"workload": "sgemm_%d" % n, "form": "ffma_fp32", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
+    out.append({"workload": "sgemm_%d" % n, "form": "default_dispatch", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9})
 
 
 def run_sgemm(out):

@@ -834,6 +834,18 @@ int gb_last_ozaki_slices(void);
 int gb_set_kernel_timing(int enable);
 double gb_kernel_time_ms(const char* prefix, int64_t* launches);
 
+/* The recorded launches as a timeline, in the order they were issued: name,
+   start and end in milliseconds from the first record's start (CUDA events on
+   each launch's stream, so launches on different streams show their overlap;
+   the host pipeline of dgemm_ also records its copies, as "copy_*").  Writes
+   at most max_entries, returns how many it wrote, and forgets every record.
+   No reference counterpart (the profiling aid of a box without nsys). */
+typedef struct {
+    char name[40];
+    double start_ms, end_ms;
+} gb_trace_entry_t;
+int64_t gb_kernel_trace(gb_trace_entry_t* out, int64_t max_entries);
+
 /* Blocks until the calling thread's library stream is idle. */
 int gb_synchronize(void);
 
