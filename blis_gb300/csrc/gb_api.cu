@@ -1890,6 +1890,9 @@ int gb_dgemm_ozaki_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_
     int rc = gb::ensure_init();
     if (rc) return rc;
     if (m < 0 || n < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_dgemm_ozaki_dev", "negative dimension");
+    // the digit form at `slices` slices whatever form gb_set_dgemm_mode chose for the host entry
+    // points (the CRT form has its own entry point)
+    gb::ModeOverride form(GB_DGEMM_OZAKI, slices, 0);
     const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
     return gb::dgemm_ozaki(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
                            tb ? rs_b : cs_b, beta, c, rs_c, cs_c, slices, pick_stream(stream));

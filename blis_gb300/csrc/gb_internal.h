@@ -7,6 +7,9 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <unordered_map>
+#include <utility>
+
 #include "../../include/blis_gb300.h"
 
 // BLIS bit encodings (frame/include/bli_type_defs.h:395-427).
@@ -256,9 +259,24 @@ int ozaki_crt_moduli_for_bits(int bits, int64_t k);
 // B := B - A X in the digit form at `slices` slices, one launch (R <= 128 rows,
 // k <= 128): bit-identical to dgemm_ozaki(rows, n, k, -1, A, X, 1, B) with
 // the same slices.
+// aimg/aexp: A's digit image from trsm_images_build (null: the kernel splits A).
 bool trsm_update_fused_fits(int slices, int64_t rows, int64_t k, int64_t n);
 int trsm_update_fused(int slices, int64_t rows, int64_t k, int64_t n, const double* a, int64_t ars, int64_t acs,
-                      const double* x, int64_t xrs, int64_t xcs, double* b, int64_t brs, int64_t bcs, cudaStream_t s);
+                      const double* x, int64_t xrs, int64_t xcs, double* b, int64_t brs, int64_t bcs, cudaStream_t s,
+                      const uint8_t* aimg = nullptr, const int* aexp = nullptr);
+// Digit images of the A blocks of a solve's fused updates, built by one launch:
+// block (r0, c0) of op(A) (rows x k) -> (image, exponents).
+struct TrsmImgSpec {
+    int64_t r0, c0, rows, k;
+};
+struct TrsmImages {
+    uint8_t* arena = nullptr;
+    int slices = 0;
+    std::unordered_map<uint64_t, std::pair<const uint8_t*, const int*>> index;
+};
+int trsm_images_build(int slices, const double* a, int64_t ars, int64_t acs, const TrsmImgSpec* specs, int nspecs,
+                      TrsmImages* out, cudaStream_t s);
+void trsm_images_release(TrsmImages* im, cudaStream_t s);
 int ozaki_digit_slices();
 // SGEMM split form (gb_sgemm_split.cu): the digit form with this many slices on
 // FP64-widened operands; whether a shape takes it (gb_set_sgemm_mode).

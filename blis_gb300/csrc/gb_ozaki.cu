@@ -1541,12 +1541,6 @@ struct OzCrtTab {
     int md[4];             // M in the same digits
 };
 
-// The moduli as compile-time constants (the recombination reduces by them),
-// and for each the multiple of p_l at or above 2^31 that makes an int32 value
-// non-negative as a uint32 without changing its residue.
-__device__ constexpr int OZC_P[OZC_MAX] = {257, 256, 255, 253, 251, 247, 241, 239,
-                                           233, 229, 227, 223, 217, 211, 199, 197};
-__host__ __device__ constexpr unsigned ozc_offset(int p) { return (unsigned)(((2147483648ull + (unsigned)p - 1) / (unsigned)p) * (unsigned)p); }
 
 // |x| 2^(t+1-e), rounded to the nearest integer (ties to even), from the bits.
 __device__ __forceinline__ unsigned long long oz_crt_scaled(unsigned long long bits, int e, int t)
@@ -1679,11 +1673,8 @@ __global__ void __launch_bounds__(256, 2) oz_crt_recombine_kernel(const __grid_c
             float qf = 0.0f;
 #pragma unroll
             for (int L = 0; L < N; ++L) {
-                const int c = (r == 0) ? v[L].x : (r == 1) ? v[L].y : (r == 2) ? v[L].z : v[L].w;
-                const int pl = OZC_P[L];
-                const unsigned cu = (unsigned)c + ozc_offset(OZC_P[L]);  // same residue, non-negative
-                int rr = (int)(cu % (unsigned)OZC_P[L]);
-                if (2 * rr > pl) rr -= pl;
+                // the slice GEMM stored the symmetric residue (|rr| <= p_l / 2 <= 128)
+                const int rr = (r == 0) ? v[L].x : (r == 1) ? v[L].y : (r == 2) ? v[L].z : v[L].w;
                 S0 += (long long)rr * tab.wd[L][0];
                 S1 += (long long)rr * tab.wd[L][1];
                 S2 += (long long)rr * tab.wd[L][2];
@@ -3106,12 +3097,45 @@ struct TuArgs {
     double* b;  // B(i, j) = b[i*brs + j*bcs]
     int64_t brs, bcs;
     unsigned int* status;
+    // A's digits prepared once per solve by trsm_image_kernel (null: the CTA splits A itself):
+    // chunk c, slice q at aimg + (c S + q) 16 KB; row exponents aexp[0..127], aexp[128] = 1 if
+    // the block holds an Inf or NaN
+    const uint8_t* aimg;
+    const int* aexp;
+};
+
+// A block of op(A) whose digit image trsm_image_kernel writes.
+struct TuImgBlock {
+    int64_t r0, c0;  // first row and column in op(A)
+    int R, K;
+    int64_t img_off, exp_off;  // bytes into the image arena, ints into the exponent arena
 };
 
 // byte offset of element (row, k) of a 128-byte-swizzled K-major plane of bf16 (k < 64)
 __device__ __forceinline__ uint32_t tu_swz(int row, int k)
 {
     return (uint32_t)(row * 128 + ((((k >> 3) ^ (row & 7))) << 4) + (k & 7) * 2);
+}
+
+// RNE(T 2^E) for T = sum_t a[t] 2^(8t), |a[t]| <= 2^24 (the fused kernel's level
+// sums), equal to round_scaled(oz_weighted_sum(a), E).  T = hi 2^(8P) + lo with
+// P = max(S - 4, 0): each part spans at most four levels, so |hi|, |lo| < 2^48.01
+// are exact doubles; for E in [-1000, 900] hi 2^(E+8P) is exact, and one fma adds
+// lo 2^E to it exactly before its single rounding (gradual underflow included).
+// Outside that range the integer path rounds.
+template <int S>
+__device__ __forceinline__ double tu_round_levels(const int (&a)[S], int E)
+{
+    if (E < -1000 || E > 900) return round_scaled(oz_weighted_sum<S>(a), E);
+    constexpr int P = S > 4 ? S - 4 : 0;
+    long long hi = 0, lo = 0;
+#pragma unroll
+    for (int t = S - 1; t >= P; --t) hi = hi * 256 + a[t];
+#pragma unroll
+    for (int t = P - 1; t >= 0; --t) lo = lo * 256 + a[t];
+    const double sh = __longlong_as_double((long long)(E + 8 * P + 1023) << 52);  // 2^(E+8P), normal
+    const double sl = __longlong_as_double((long long)(E + 1023) << 52);          // 2^E, normal
+    return __fma_rn((double)lo, sl, (double)hi * sh);
 }
 
 template <int S>
@@ -3122,7 +3146,7 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
     uint8_t* sa = smem;                          // S planes of 16 KB
     uint8_t* sb = smem + TU_MAXS * TU_A_PLANE;   // S planes of 4 KB
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + TU_MAXS * (TU_A_PLANE + TU_B_PLANE));
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
     __shared__ int er[TU_ROWS], ec[TU_N];
     __shared__ int s_nf, s_fail;
 
@@ -3131,7 +3155,8 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
     const int ncols = (p.n - c0 < TU_N) ? (int)(p.n - c0) : TU_N;
     const int R = p.R, K = p.K;
     if (tid == 0) {
-        mbar_init(bar, 1);
+        mbar_init(bar, 1);      // MMA completion of a chunk
+        mbar_init(bar + 1, 1);  // A's image planes of a chunk
         fence_barrier_init();
         s_nf = 0;
         s_fail = 0;
@@ -3141,8 +3166,11 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
         tmem_relinquish();
     }
     __syncthreads();
-    // exponents: thread per row of A; warp w for columns 4w .. 4w + 3 of X
-    if (tid < TU_ROWS) {
+    // exponents: thread per row of A (or the image's); warp w for columns 4w .. 4w + 3 of X
+    if (p.aimg) {
+        if (tid < TU_ROWS) er[tid] = p.aexp[tid];
+        if (tid == 0 && p.aexp[TU_ROWS]) s_nf = 1;
+    } else if (tid < TU_ROWS) {
         unsigned long long mx = 0;
         if (tid < R)
             for (int l = 0; l < K; ++l) {
@@ -3189,6 +3217,15 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
     } else {
         uint32_t phase = 0;
         for (int k0 = 0; k0 < K; k0 += TU_KC) {
+            if (p.aimg) {
+                // the chunk's S digit planes of A, prepared once per solve, by bulk copy
+                if (tid == 0) {
+                    mbar_arrive_expect_tx(bar + 1, (uint32_t)(S * TU_A_PLANE));
+                    const uint8_t* src = p.aimg + (int64_t)(k0 / TU_KC) * S * TU_A_PLANE;
+#pragma unroll
+                    for (int q = 0; q < S; ++q) bulk_load(sa + q * TU_A_PLANE, src + q * TU_A_PLANE, TU_A_PLANE, bar + 1);
+                }
+            } else
             // digits of A (rows beyond R and k beyond K are zero), two k per 32-bit word;
             // consecutive threads take consecutive rows (column-major A reads coalesce)
             for (int e = tid; e < TU_ROWS * (TU_KC / 2); e += TU_THREADS) {
@@ -3217,7 +3254,12 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
                 for (int q = 0; q < S; ++q) *reinterpret_cast<uint32_t*>(sb + q * TU_B_PLANE + off) = w[q];
             }
             fence_proxy_async();  // the digits, written by threads, become visible to the MMAs
+            if (p.aimg && tid == 0 && !mbar_wait_bounded(bar + 1, phase, kWaitBudgetNs)) {
+                atomicOr(p.status, DEV_WAIT_TIMEOUT);
+                s_fail = 1;
+            }
             __syncthreads();
+            if (s_fail) break;  // no MMA was issued for this chunk
             if (tid == 0) {
                 tc_fence_after();
                 constexpr uint32_t idesc = idesc_bf16_f32(TU_ROWS, TU_N);
@@ -3256,15 +3298,11 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
 #pragma unroll 1
             for (int g = 0; g < 2; ++g) {
                 const int cb = half * 16 + g * 8;
-                int32_t lv[S][8];
+                uint32_t r8[S][8];
 #pragma unroll
-                for (int li = 0; li < S; ++li) {
-                    uint32_t r8[8];
-                    tmem_ld_32x32b_x8(tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(li * TU_N + cb), r8);
-                    tmem_ld_wait();
-#pragma unroll
-                    for (int c = 0; c < 8; ++c) lv[li][c] = __float2int_rn(__uint_as_float(r8[c]));
-                }
+                for (int li = 0; li < S; ++li)
+                    tmem_ld_32x32b_x8(tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(li * TU_N + cb), r8[li]);
+                tmem_ld_wait();
                 if (row < R) {
 #pragma unroll
                     for (int c = 0; c < 8; ++c) {
@@ -3272,9 +3310,8 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
                         if (col >= ncols) break;
                         int a[S];  // a[t] is level S + 1 - t, weight 2^(8t)
 #pragma unroll
-                        for (int li = 0; li < S; ++li) a[S - 1 - li] = lv[li][c];
-                        const __int128 T = oz_weighted_sum<S>(a);
-                        const double ab = round_scaled(T, er[row] + ec[col] - 8 * (S + 1));
+                        for (int li = 0; li < S; ++li) a[S - 1 - li] = __float2int_rn(__uint_as_float(r8[li][c]));
+                        const double ab = tu_round_levels<S>(a, er[row] + ec[col] - 8 * (S + 1));
                         double* bij = p.b + (int64_t)row * p.brs + (c0 + col) * p.bcs;
                         *bij = __fma_rn(1.0, *bij, -ab);
                     }
@@ -3286,6 +3323,75 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
     __syncthreads();
     tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, TU_TMEM_COLS);
+}
+
+// The digit images of the A blocks of a solve's small updates, once per solve:
+// CTA b writes block b's row exponents (the split kernels' rule over the
+// block's columns), its Inf/NaN flag and, per 64-deep k chunk, S planes of
+// 128 rows in the fused kernel's shared-memory layout (zero beyond R and K).
+// Thread items are (row, 8 consecutive k): one 16-byte store per plane.
+template <int S>
+__global__ void __launch_bounds__(TU_THREADS) trsm_image_kernel(const double* __restrict__ a, int64_t ars,
+                                                                int64_t acs, const TuImgBlock* __restrict__ blocks,
+                                                                uint8_t* __restrict__ img, int* __restrict__ exps)
+{
+    const TuImgBlock blk = blocks[blockIdx.x];
+    const double* ab = a + blk.r0 * ars + blk.c0 * acs;
+    __shared__ unsigned long long part[2][TU_ROWS];
+    __shared__ int er[TU_ROWS];
+    __shared__ int s_nf;
+    const int tid = threadIdx.x;
+    if (tid == 0) s_nf = 0;
+    {
+        const int row = tid & (TU_ROWS - 1), h = tid >> 7;
+        unsigned long long mx = 0;
+        if (row < blk.R)
+            for (int l = h; l < blk.K; l += 2) {
+                const unsigned long long v = abs_bits(ab[(int64_t)row * ars + (int64_t)l * acs]);
+                mx = v > mx ? v : mx;
+            }
+        part[h][row] = mx;
+    }
+    __syncthreads();
+    if (tid < TU_ROWS) {
+        const unsigned long long m0 = part[0][tid], m1 = part[1][tid];
+        int nf = 0;
+        er[tid] = oz_row_exponent(m0 > m1 ? m0 : m1, &nf);
+        if (nf) s_nf = 1;
+        exps[blk.exp_off + tid] = er[tid];
+    }
+    __syncthreads();
+    if (tid == 0) exps[blk.exp_off + TU_ROWS] = s_nf;
+    const int nch = (blk.K + TU_KC - 1) / TU_KC;
+    for (int e = tid; e < nch * TU_ROWS * (TU_KC / 8); e += TU_THREADS) {
+        const int row = e & (TU_ROWS - 1), k8 = (e >> 7) % (TU_KC / 8), c = (e >> 7) / (TU_KC / 8);
+        const int l0 = c * TU_KC + k8 * 8;
+        uint32_t w[S][4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const int l = l0 + 2 * h;
+            const double* ar = ab + (int64_t)row * ars;
+            const double v0 = (row < blk.R && l < blk.K) ? ar[(int64_t)l * acs] : 0.0;
+            const double v1 = (row < blk.R && l + 1 < blk.K) ? ar[(int64_t)(l + 1) * acs] : 0.0;
+            uint32_t ww[S];
+            oz_digits_bf16x2<S>(v0, v1, er[row], ww);
+#pragma unroll
+            for (int q = 0; q < S; ++q) w[q][h] = ww[q];
+        }
+        uint8_t* base = img + blk.img_off + (int64_t)c * S * TU_A_PLANE + tu_swz(row, k8 * 8);
+#pragma unroll
+        for (int q = 0; q < S; ++q)
+            *reinterpret_cast<uint4*>(base + q * TU_A_PLANE) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
+    }
+}
+
+template <int S>
+int launch_trsm_image(const double* a, int64_t ars, int64_t acs, const TuImgBlock* blocks, int nblocks, uint8_t* img,
+                      int* exps, cudaStream_t s)
+{
+    LaunchScope ls("trsm_image", s);
+    trsm_image_kernel<S><<<(unsigned)nblocks, TU_THREADS, 0, s>>>(a, ars, acs, blocks, img, exps);
+    return check_cuda(cudaGetLastError(), "trsm_image");
 }
 
 template <int S>
@@ -3313,8 +3419,74 @@ bool trsm_update_fused_fits(int slices, int64_t rows, int64_t k, int64_t n)
            (n + TU_N - 1) / TU_N <= INT32_MAX;
 }
 
+// Digit images of the A blocks (rows R <= 128, depth K <= 128) that fused updates of
+// one solve will read: arena layout by the host, one launch for all blocks.
+int trsm_images_build(int slices, const double* a, int64_t ars, int64_t acs, const TrsmImgSpec* specs, int nspecs,
+                      TrsmImages* out, cudaStream_t s)
+{
+    *out = TrsmImages();
+    if (nspecs <= 0) return GB_SUCCESS;
+    if (slices < 2 || slices > TU_MAXS) return set_error(GB_ERR_ARG, "trsm_images_build", "slices outside 2..8");
+    std::vector<TuImgBlock> blocks((size_t)nspecs);
+    int64_t img_bytes = 0, exp_ints = 0;
+    for (int i = 0; i < nspecs; ++i) {
+        const TrsmImgSpec& q = specs[i];
+        if (q.rows < 1 || q.rows > TU_ROWS || q.k < 1 || q.k > 2 * TU_KC)
+            return set_error(GB_ERR_ARG, "trsm_images_build", "block outside the fused kernel's shape");
+        TuImgBlock& b = blocks[(size_t)i];
+        b.r0 = q.r0;
+        b.c0 = q.c0;
+        b.R = (int)q.rows;
+        b.K = (int)q.k;
+        b.img_off = img_bytes;
+        b.exp_off = exp_ints;
+        img_bytes += (int64_t)((q.k + TU_KC - 1) / TU_KC) * slices * TU_A_PLANE;
+        exp_ints += TU_ROWS + 4;  // exponents, flag, padding to 16 bytes
+    }
+    const size_t bytes_tab = sizeof(TuImgBlock) * (size_t)nspecs;
+    const size_t total = (size_t)img_bytes + sizeof(int) * (size_t)exp_ints + bytes_tab + 256;
+    uint8_t* arena = static_cast<uint8_t*>(dev_alloc(total, s));
+    if (!arena) return GB_ERR_NOMEM;
+    int* exps = reinterpret_cast<int*>(arena + img_bytes);
+    TuImgBlock* d_blocks = reinterpret_cast<TuImgBlock*>(arena + img_bytes + sizeof(int) * (size_t)exp_ints);
+    int rc = check_cuda(cudaMemcpyAsync(d_blocks, blocks.data(), bytes_tab, cudaMemcpyHostToDevice, s), "trsm images");
+    if (!rc) {
+        switch (slices) {
+        case 2: rc = launch_trsm_image<2>(a, ars, acs, d_blocks, nspecs, arena, exps, s); break;
+        case 3: rc = launch_trsm_image<3>(a, ars, acs, d_blocks, nspecs, arena, exps, s); break;
+        case 4: rc = launch_trsm_image<4>(a, ars, acs, d_blocks, nspecs, arena, exps, s); break;
+        case 5: rc = launch_trsm_image<5>(a, ars, acs, d_blocks, nspecs, arena, exps, s); break;
+        case 6: rc = launch_trsm_image<6>(a, ars, acs, d_blocks, nspecs, arena, exps, s); break;
+        case 7: rc = launch_trsm_image<7>(a, ars, acs, d_blocks, nspecs, arena, exps, s); break;
+        default: rc = launch_trsm_image<8>(a, ars, acs, d_blocks, nspecs, arena, exps, s); break;
+        }
+    }
+    // the host table is only read by the copy above, which the stream orders before any use
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "trsm images");
+    if (rc) {
+        dev_free(arena, s);
+        return rc;
+    }
+    out->arena = arena;
+    out->slices = slices;
+    for (int i = 0; i < nspecs; ++i) {
+        const TuImgBlock& b = blocks[(size_t)i];
+        out->index[((uint64_t)b.r0 << 32) | (uint64_t)b.c0] =
+            std::make_pair(static_cast<const uint8_t*>(arena + b.img_off), static_cast<const int*>(exps + b.exp_off));
+    }
+    return GB_SUCCESS;
+}
+
+void trsm_images_release(TrsmImages* im, cudaStream_t s)
+{
+    dev_free(im->arena, s);
+    im->arena = nullptr;
+    im->index.clear();
+}
+
 int trsm_update_fused(int slices, int64_t rows, int64_t k, int64_t n, const double* a, int64_t ars, int64_t acs,
-                      const double* x, int64_t xrs, int64_t xcs, double* b, int64_t brs, int64_t bcs, cudaStream_t s)
+                      const double* x, int64_t xrs, int64_t xcs, double* b, int64_t brs, int64_t bcs, cudaStream_t s,
+                      const uint8_t* aimg, const int* aexp)
 {
     if (!trsm_update_fused_fits(slices, rows, k, n))
         return set_error(GB_ERR_ARG, "trsm_update_fused", "update outside the fused kernel's shape");
@@ -3332,6 +3504,8 @@ int trsm_update_fused(int slices, int64_t rows, int64_t k, int64_t n, const doub
     t.brs = brs;
     t.bcs = bcs;
     t.status = device_status_word();
+    t.aimg = aimg;
+    t.aexp = aexp;
     note_ozaki_slices(slices);
     switch (slices) {
     case 2: return launch_trsm_update_fused<2>(t, s);

@@ -20,6 +20,8 @@
 // of the recursion.
 #include <stdlib.h>
 
+#include <vector>
+
 #include "gb_internal.h"
 
 namespace gb {
@@ -184,7 +186,15 @@ struct TrsmCtx {
     int64_t brs, bcs;
     int64_t n;
     cudaStream_t s;
+    const TrsmImages* img = nullptr;  // digit images of the fused updates' A blocks
 };
+
+bool trsm_fused_enabled()
+{
+    // GB_TRSM_FUSED=0 turns the fused small updates off (read per call)
+    const char* fz = getenv("GB_TRSM_FUSED");
+    return !(fz && fz[0] == '0');
+}
 
 // ---------------------------------------------------------------- trsv
 // One right-hand side in ONE launch.  CTA i (in the order of an atomic
@@ -424,12 +434,21 @@ int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t cco
     const double* xp = t.b + c0 * t.brs;
     double* bp = t.b + r0 * t.brs;
     if (t.slices > 0 && (double)rcount * (double)ccount * (double)t.n >= trsm_ozaki_min_fma()) {
-        // the small updates at the bottom of the recursion: one fused launch
-        // (GB_TRSM_FUSED=0 turns it off; read per call)
-        const char* fz = getenv("GB_TRSM_FUSED");
-        if (!(fz && fz[0] == '0') && trsm_update_fused_fits(t.slices, rcount, ccount, t.n))
+        // the small updates at the bottom of the recursion: one fused launch, reading the
+        // digit image of the A block built for the solve when there is one
+        if (trsm_fused_enabled() && trsm_update_fused_fits(t.slices, rcount, ccount, t.n)) {
+            const uint8_t* aimg = nullptr;
+            const int* aexp = nullptr;
+            if (t.img && t.img->slices == t.slices) {
+                auto it = t.img->index.find(((uint64_t)r0 << 32) | (uint64_t)c0);
+                if (it != t.img->index.end()) {
+                    aimg = it->second.first;
+                    aexp = it->second.second;
+                }
+            }
             return trsm_update_fused(t.slices, rcount, ccount, t.n, ap, t.ars, t.acs, xp, t.brs, t.bcs, bp, t.brs,
-                                     t.bcs, t.s);
+                                     t.bcs, t.s, aimg, aexp);
+        }
         const int64_t kc = trsm_crt_min_k();
         const int moduli = (kc > 0 && ccount >= kc) ? ozaki_crt_moduli_for_bits(8 * t.slices - 1, ccount) : -1;
         if (moduli > 0) {
@@ -492,6 +511,20 @@ int solve(const TrsmCtx* ts, int nt, int64_t r0, int64_t mm)
     for (int g = 0; g < nt; ++g)
         if ((rc = update(ts[g], r0, m1, r0 + m1, m2))) return rc;
     return solve(ts, nt, r0, m1);
+}
+
+// The updates of the recursion (solve's splitting rule) whose A block the fused
+// kernel takes: (r0, c0, rows, k) of op(A).
+void fused_update_blocks(bool lower, int64_t r0, int64_t mm, int slices, int64_t n, std::vector<TrsmImgSpec>& out)
+{
+    if (mm <= TRSM_NB) return;
+    int64_t m1 = ((mm / 2 + TRSM_NB - 1) / TRSM_NB) * TRSM_NB;
+    if (m1 >= mm) m1 = mm - TRSM_NB;
+    const int64_t m2 = mm - m1;
+    const TrsmImgSpec u = lower ? TrsmImgSpec{r0 + m1, r0, m2, m1} : TrsmImgSpec{r0, r0 + m1, m1, m2};
+    fused_update_blocks(lower, lower ? r0 : r0 + m1, lower ? m1 : m2, slices, n, out);
+    if (trsm_update_fused_fits(slices, u.rows, u.k, n)) out.push_back(u);
+    fused_update_blocks(lower, lower ? r0 + m1 : r0, lower ? m2 : m1, slices, n, out);
 }
 
 }  // namespace
@@ -590,12 +623,25 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     }
     int rc = check_cuda(cudaGetLastError(), "trsm_pack_diag");
     t.packed = packed;
+    // the fused updates' A blocks split once for the solve (both column groups read them)
+    TrsmImages images;
+    const char* gi = getenv("GB_TRSM_IMAGES");  // 0: each fused update splits its A block itself
+    if (!rc && slices > 0 && trsm_fused_enabled() && !(gi && gi[0] == '0') && trsm_ozaki_min_fma() == 0.0) {
+        std::vector<TrsmImgSpec> specs;
+        fused_update_blocks(t.lower != 0, 0, mm, slices, nn, specs);
+        if (!specs.empty() &&
+            trsm_images_build(slices, a, t.ars, t.acs, specs.data(), (int)specs.size(), &images, s) == GB_SUCCESS)
+            t.img = &images;
+        else
+            cudaGetLastError();  // without images each fused update splits its A block itself
+    }
     // the precision form's many small launches (split, slice GEMM, recombination
     // per update) and the FP64-pipe diagonal solves of two column halves overlap
     // on two streams, forked and joined by two events; if either event cannot be
     // created the solve runs on one stream
     cudaEvent_t ev[2] = {nullptr, nullptr};
-    const bool two = !rc && slices > 0 && nn >= 2 * TRSM_SPLIT_MIN_COLS && mm > 4 * TRSM_NB &&
+    const char* gs = getenv("GB_TRSM_STREAMS");  // 1: the column halves stay on one stream
+    const bool two = !rc && slices > 0 && nn >= 2 * TRSM_SPLIT_MIN_COLS && mm > 4 * TRSM_NB && !(gs && gs[0] == '1') &&
                      cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming) == cudaSuccess &&
                      cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming) == cudaSuccess;
     if (two) {
@@ -617,6 +663,7 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     }
     for (cudaEvent_t e : ev)
         if (e) cudaEventDestroy(e);
+    trsm_images_release(&images, s);
     dev_free(packed, s);
     return rc;
 }

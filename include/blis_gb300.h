@@ -495,7 +495,9 @@ int gb_dgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
 
 /* Ozaki split-product DGEMM: FP64 operands cut into `slices` bf16 digit
    slices, products on the tcgen05 tensor cores, exact integer level sums,
-   FP64 recombination.  No reference counterpart (precision form). */
+   FP64 recombination.  Always the digit form, whatever form
+   gb_set_dgemm_mode chose for the host entry points (the CRT form is
+   gb_dgemm_ozaki_crt_dev).  No reference counterpart (precision form). */
 int gb_dgemm_ozaki_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
                        gb_dim_t k, double alpha, const double* a, gb_inc_t rs_a,
                        gb_inc_t cs_a, const double* b, gb_inc_t rs_b, gb_inc_t cs_b,
