@@ -3182,23 +3182,36 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
         if (nf) s_nf = 1;
     }
 #pragma unroll
-    for (int cc = 0; cc < 4; ++cc) {
-        const int c = warp * 4 + cc;
-        unsigned long long mx = 0;
-        if (c < ncols)
-            for (int l = lane; l < K; l += 32) {
-                const unsigned long long v = abs_bits(p.x[(int64_t)l * p.xrs + (c0 + c) * p.xcs]);
+    {
+        // all 16 loads of a lane (4 columns x k = lane + 32 i, K <= 128) in flight at once
+        double xv[4][2 * TU_KC / 32];
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            const int c = warp * 4 + cc;
+#pragma unroll
+            for (int i = 0; i < 2 * TU_KC / 32; ++i) {
+                const int l = lane + 32 * i;
+                xv[cc][i] = (c < ncols && l < K) ? p.x[(int64_t)l * p.xrs + (c0 + c) * p.xcs] : 0.0;
+            }
+        }
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+            unsigned long long mx = 0;
+#pragma unroll
+            for (int i = 0; i < 2 * TU_KC / 32; ++i) {
+                const unsigned long long v = abs_bits(xv[cc][i]);
                 mx = v > mx ? v : mx;
             }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
-            mx = v > mx ? v : mx;
-        }
-        if (lane == 0) {
-            int nf = 0;
-            ec[c] = oz_row_exponent(mx, &nf);
-            if (nf) s_nf = 1;
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
+                mx = v > mx ? v : mx;
+            }
+            if (lane == 0) {
+                int nf = 0;
+                ec[warp * 4 + cc] = oz_row_exponent(mx, &nf);
+                if (nf) s_nf = 1;
+            }
         }
     }
     __syncthreads();
@@ -3240,18 +3253,28 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
 #pragma unroll
                 for (int q = 0; q < S; ++q) *reinterpret_cast<uint32_t*>(sa + q * TU_A_PLANE + off) = w[q];
             }
-            // digits of X^T (columns beyond n are zero); lanes run along k
-            for (int e = tid; e < TU_N * (TU_KC / 2); e += TU_THREADS) {
-                const int kp = e & 31, c = e >> 5;
-                const int l = k0 + 2 * kp;
-                const double* xc = p.x + (c0 + c) * p.xcs;
-                const double v0 = (c < ncols && l < K) ? xc[(int64_t)l * p.xrs] : 0.0;
-                const double v1 = (c < ncols && l + 1 < K) ? xc[(int64_t)(l + 1) * p.xrs] : 0.0;
-                uint32_t w[S];
-                oz_digits_bf16x2<S>(v0, v1, ec[c], w);
-                const uint32_t off = tu_swz(c, 2 * kp);
+            // digits of X^T (columns beyond n are zero); lanes run along k, the loads of all
+            // of a thread's items first
+            {
+                constexpr int IT = TU_N * (TU_KC / 2) / TU_THREADS;
+                double xv[IT][2];
 #pragma unroll
-                for (int q = 0; q < S; ++q) *reinterpret_cast<uint32_t*>(sb + q * TU_B_PLANE + off) = w[q];
+                for (int it = 0; it < IT; ++it) {
+                    const int e = tid + it * TU_THREADS, kp = e & 31, c = e >> 5;
+                    const int l = k0 + 2 * kp;
+                    const double* xc = p.x + (c0 + c) * p.xcs;
+                    xv[it][0] = (c < ncols && l < K) ? xc[(int64_t)l * p.xrs] : 0.0;
+                    xv[it][1] = (c < ncols && l + 1 < K) ? xc[(int64_t)(l + 1) * p.xrs] : 0.0;
+                }
+#pragma unroll
+                for (int it = 0; it < IT; ++it) {
+                    const int e = tid + it * TU_THREADS, kp = e & 31, c = e >> 5;
+                    uint32_t w[S];
+                    oz_digits_bf16x2<S>(xv[it][0], xv[it][1], ec[c], w);
+                    const uint32_t off = tu_swz(c, 2 * kp);
+#pragma unroll
+                    for (int q = 0; q < S; ++q) *reinterpret_cast<uint32_t*>(sb + q * TU_B_PLANE + off) = w[q];
+                }
             }
             fence_proxy_async();  // the digits, written by threads, become visible to the MMAs
             if (p.aimg && tid == 0 && !mbar_wait_bounded(bar + 1, phase, kWaitBudgetNs)) {
@@ -3304,17 +3327,21 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
                     tmem_ld_32x32b_x8(tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(li * TU_N + cb), r8[li]);
                 tmem_ld_wait();
                 if (row < R) {
+                    // the 8 entries of B first (loads in flight together), then the updates
+                    double* brow = p.b + (int64_t)row * p.brs + (c0 + cb) * p.bcs;
+                    double bv[8];
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) bv[c] = (cb + c < ncols) ? brow[(int64_t)c * p.bcs] : 0.0;
 #pragma unroll
                     for (int c = 0; c < 8; ++c) {
-                        const int col = cb + c;
-                        if (col >= ncols) break;
                         int a[S];  // a[t] is level S + 1 - t, weight 2^(8t)
 #pragma unroll
                         for (int li = 0; li < S; ++li) a[S - 1 - li] = __float2int_rn(__uint_as_float(r8[li][c]));
-                        const double ab = tu_round_levels<S>(a, er[row] + ec[col] - 8 * (S + 1));
-                        double* bij = p.b + (int64_t)row * p.brs + (c0 + col) * p.bcs;
-                        *bij = __fma_rn(1.0, *bij, -ab);
+                        bv[c] = __fma_rn(1.0, bv[c], -tu_round_levels<S>(a, er[row] + ec[cb + c] - 8 * (S + 1)));
                     }
+#pragma unroll
+                    for (int c = 0; c < 8; ++c)
+                        if (cb + c < ncols) brow[(int64_t)c * p.bcs] = bv[c];
                 }
             }
         }

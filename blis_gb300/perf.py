@@ -23,6 +23,10 @@ L2 where the workload allows:
                   transposes: grouped launches (captured graph) vs a
                   per-problem launch loop, FP64 native, FP64 Ozaki (7
                   slices) and FP32
+  e2e             dgemm_ 16384^3 (4096^3 with --small) in the CRT form (16
+                  moduli) on pinned host buffers, per call: host time and
+                  the timeline of its launches and copies (gb_kernel_trace)
+                  for the fastest and the slowest of the calls
 
 Usage: python -m blis_gb300.perf [--only name,...] [--json out.jsonl] [--batch-count N] [--small]
                                 [--trsm-forms native,ozaki] [--forms native,ozaki]
@@ -510,7 +514,41 @@ def run_crt(out):
                 "stage_ms": stages})
 
 
-SUITES = {"crt": run_crt, "gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
+def run_e2e(out, calls=8):
+    """dgemm_ on pinned host buffers through the C ABI (the pipelined host path): the host
+    time of each call, and the launch/copy timeline of the fastest and the slowest call."""
+    import time
+    import torch
+    n = 4096 if SMALL else 16384
+    hs = [torch.empty((n, n), dtype=torch.float64, pin_memory=True) for _ in range(3)]
+    for i, h in enumerate(hs[:2]):
+        d = _mat(n, n, kind=dev.RAND_EXPSPREAD, seed=71 + i, p0=-20, p1=20)
+        h.copy_(d.t())  # row-major storage of the transpose: column-major d
+        del d
+    torch.cuda.synchronize()
+    an, bn, cn = (h.numpy() for h in hs)
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI_CRT, 16)
+    try:
+        blas.dgemm("N", "N", n, n, n, 1.0, an, n, bn, n, 0.0, cn, n)
+        dev.set_kernel_timing(True)
+        dev.kernel_trace()
+        runs = []
+        for _ in range(calls):
+            t0 = time.perf_counter()
+            blas.dgemm("N", "N", n, n, n, 1.0, an, n, bn, n, 0.0, cn, n)
+            runs.append(((time.perf_counter() - t0) * 1e3, dev.kernel_trace()))
+    finally:
+        dev.set_kernel_timing(False)
+        blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+    ms = sorted(r[0] for r in runs)
+    rec = {"workload": "dgemm_%d_e2e_crt16" % n, "calls": calls, "ms": [r[0] for r in runs],
+           "tflops_median": 2.0 * n ** 3 / ms[len(ms) // 2] / 1e9, "tflops_best": 2.0 * n ** 3 / ms[0] / 1e9}
+    for label, (t, tr) in (("fastest", min(runs, key=lambda r: r[0])), ("slowest", max(runs, key=lambda r: r[0]))):
+        rec[label] = {"ms": t, "timeline": [(nm, round(a, 3), round(b, 3)) for nm, a, b in sorted(tr, key=lambda x: x[1])]}
+    out.append(rec)
+
+
+SUITES = {"crt": run_crt, "e2e": run_e2e, "gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
           "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm, "bgemm": run_bgemm,
           "level3x": run_level3x, "level12x": run_level12x, "complex": run_complex, "hermitian": run_hermitian}
 
