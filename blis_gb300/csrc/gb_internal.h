@@ -260,10 +260,13 @@ int ozaki_crt_moduli_for_bits(int bits, int64_t k);
 // k <= 128): bit-identical to dgemm_ozaki(rows, n, k, -1, A, X, 1, B) with
 // the same slices.
 // aimg/aexp: A's digit image from trsm_images_build (null: the kernel splits A).
+// packed_diag: the packed 64 x 64 diagonal block of the updated rows (rows <= 64), which the
+// kernel then solves in place (lower or upper substitution), as trsm_diag_kernel would.
 bool trsm_update_fused_fits(int slices, int64_t rows, int64_t k, int64_t n);
 int trsm_update_fused(int slices, int64_t rows, int64_t k, int64_t n, const double* a, int64_t ars, int64_t acs,
                       const double* x, int64_t xrs, int64_t xcs, double* b, int64_t brs, int64_t bcs, cudaStream_t s,
-                      const uint8_t* aimg = nullptr, const int* aexp = nullptr);
+                      const uint8_t* aimg = nullptr, const int* aexp = nullptr, const double* packed_diag = nullptr,
+                      int diag_lower = 0);
 // Digit images of the A blocks of a solve's fused updates, built by one launch:
 // block (r0, c0) of op(A) (rows x k) -> (image, exponents).
 struct TrsmImgSpec {

@@ -3102,7 +3102,44 @@ struct TuArgs {
     // the block holds an Inf or NaN
     const uint8_t* aimg;
     const int* aexp;
+    // gemmtrsm shape: after the update, the R <= 64 rows solve their diagonal block in place
+    // from its packed form (64 x 64 row-major, inverted diagonal, the trsm solves' layout);
+    // null: update only
+    const double* pk;
+    int diag_lower;
 };
+
+// In-place substitution of one packed 64 x 64 diagonal block for 32 columns,
+// 8 lanes per column, 8 rows per lane: the arithmetic of trsm_diag_kernel<8>
+// (same FMAs in the same order), on Ls = P [64][65] and Xs = X [64][33] in
+// shared memory.
+template <bool LOWER>
+__device__ __forceinline__ void tu_diag_solve(const double* Ls, double* Xs, int tid)
+{
+    const int c = tid >> 3, g = tid & 7;
+    const int src0 = (tid & 31) - g;
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = Xs[(q * 8 + g) * 33 + c];
+#pragma unroll
+    for (int step = 0; step < 64; ++step) {
+        const int i = LOWER ? step : 63 - step;
+        const int qi = i >> 3, gi = i & 7;
+        const double v = __shfl_sync(0xffffffffu, x[qi], src0 + gi);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            if (LOWER ? (q * 8 + 7 > i) : (q * 8 < i)) {
+                const int r = q * 8 + g;
+                if (LOWER ? (r > i) : (r < i)) x[q] = fma(-Ls[r * 65 + i], v, x[q]);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int r = q * 8 + g;
+        Xs[r * 33 + c] = x[q] * Ls[r * 65 + r];
+    }
+}
 
 // A block of op(A) whose digit image trsm_image_kernel writes.
 struct TuImgBlock {
@@ -3346,6 +3383,26 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
             }
         }
     }
+    if (p.pk && !s_fail) {
+        // the diagonal block of the updated rows (the reference's gemmtrsm shape): the digit
+        // planes' shared memory is free once the MMAs have completed
+        __syncthreads();  // the updated rows of B are in global memory
+        double* Ls = reinterpret_cast<double*>(sa);  // [64][65]
+        double* Xs = reinterpret_cast<double*>(sb);  // [64][33]
+        for (int e = tid; e < 64 * 64; e += TU_THREADS) Ls[(e >> 6) * 65 + (e & 63)] = p.pk[e];
+        for (int e = tid; e < 64 * TU_N; e += TU_THREADS) {
+            const int i = e & 63, c = e >> 6;  // B column-major: consecutive threads, consecutive rows
+            Xs[i * 33 + c] = (c < ncols && i < R) ? p.b[(int64_t)i * p.brs + (c0 + c) * p.bcs] : 0.0;
+        }
+        __syncthreads();
+        if (p.diag_lower) tu_diag_solve<true>(Ls, Xs, tid);
+        else tu_diag_solve<false>(Ls, Xs, tid);
+        __syncthreads();
+        for (int e = tid; e < 64 * TU_N; e += TU_THREADS) {
+            const int i = e & 63, c = e >> 6;
+            if (c < ncols && i < R) p.b[(int64_t)i * p.brs + (c0 + c) * p.bcs] = Xs[i * 33 + c];
+        }
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -3513,9 +3570,9 @@ void trsm_images_release(TrsmImages* im, cudaStream_t s)
 
 int trsm_update_fused(int slices, int64_t rows, int64_t k, int64_t n, const double* a, int64_t ars, int64_t acs,
                       const double* x, int64_t xrs, int64_t xcs, double* b, int64_t brs, int64_t bcs, cudaStream_t s,
-                      const uint8_t* aimg, const int* aexp)
+                      const uint8_t* aimg, const int* aexp, const double* packed_diag, int diag_lower)
 {
-    if (!trsm_update_fused_fits(slices, rows, k, n))
+    if (!trsm_update_fused_fits(slices, rows, k, n) || (packed_diag && rows > 64))
         return set_error(GB_ERR_ARG, "trsm_update_fused", "update outside the fused kernel's shape");
     TuArgs t;
     t.R = (int)rows;
@@ -3533,6 +3590,8 @@ int trsm_update_fused(int slices, int64_t rows, int64_t k, int64_t n, const doub
     t.status = device_status_word();
     t.aimg = aimg;
     t.aexp = aexp;
+    t.pk = packed_diag;
+    t.diag_lower = diag_lower;
     note_ozaki_slices(slices);
     switch (slices) {
     case 2: return launch_trsm_update_fused<2>(t, s);

@@ -463,6 +463,38 @@ int update(const TrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t cco
                         t.brs, t.bcs, t.s);
 }
 
+// Whether the update of `rows` rows at depth k and the diagonal solve of those rows run as one
+// fused launch (the precision form's fused updates; GB_TRSM_GEMMTRSM=0 keeps them apart).
+bool gemmtrsm_applies(const TrsmCtx& t, int64_t rows, int64_t k)
+{
+    const char* e = getenv("GB_TRSM_GEMMTRSM");
+    return !(e && e[0] == '0') && t.slices > 0 && trsm_fused_enabled() && rows <= TRSM_NB &&
+           (double)rows * (double)k * (double)t.n >= trsm_ozaki_min_fma() &&
+           trsm_update_fused_fits(t.slices, rows, k, t.n);
+}
+
+// B[r0:r0+rows] := solve(diagonal block at r0, B[r0:r0+rows] - op(A)[r0.., c0..c0+k] X[c0..c0+k]):
+// the fused update followed, in the same launch, by the diagonal block's substitution.
+int gemmtrsm(const TrsmCtx& t, int64_t r0, int64_t rows, int64_t c0, int64_t k)
+{
+    const double* ap = t.a + r0 * t.ars + c0 * t.acs;
+    const double* xp = t.b + c0 * t.brs;
+    double* bp = t.b + r0 * t.brs;
+    const uint8_t* aimg = nullptr;
+    const int* aexp = nullptr;
+    if (t.img && t.img->slices == t.slices) {
+        auto it = t.img->index.find(((uint64_t)r0 << 32) | (uint64_t)c0);
+        if (it != t.img->index.end()) {
+            aimg = it->second.first;
+            aexp = it->second.second;
+        }
+    }
+    // r0 is a multiple of the block size: the split in solve keeps it so
+    const double* pk = t.packed + (r0 / TRSM_NB) * TRSM_NB * TRSM_NB;
+    return trsm_update_fused(t.slices, rows, k, t.n, ap, t.ars, t.acs, xp, t.brs, t.bcs, bp, t.brs, t.bcs, t.s, aimg,
+                             aexp, pk, t.lower);
+}
+
 int diag_solve(const TrsmCtx& t, int64_t r0, int64_t mm)
 {
     // r0 is a multiple of the block size: the split in solve keeps it so
@@ -503,11 +535,22 @@ int solve(const TrsmCtx* ts, int nt, int64_t r0, int64_t mm)
     const int64_t m2 = mm - m1;
     if (ts[0].lower) {
         if ((rc = solve(ts, nt, r0, m1))) return rc;
+        // the last diagonal block and the update before it in one fused launch
+        if (m2 <= TRSM_NB && gemmtrsm_applies(ts[0], m2, m1)) {
+            for (int g = 0; g < nt; ++g)
+                if ((rc = gemmtrsm(ts[g], r0 + m1, m2, r0, m1))) return rc;
+            return GB_SUCCESS;
+        }
         for (int g = 0; g < nt; ++g)
             if ((rc = update(ts[g], r0 + m1, m2, r0, m1))) return rc;
         return solve(ts, nt, r0 + m1, m2);
     }
     if ((rc = solve(ts, nt, r0 + m1, m2))) return rc;
+    if (m1 <= TRSM_NB && gemmtrsm_applies(ts[0], m1, m2)) {
+        for (int g = 0; g < nt; ++g)
+            if ((rc = gemmtrsm(ts[g], r0, m1, r0 + m1, m2))) return rc;
+        return GB_SUCCESS;
+    }
     for (int g = 0; g < nt; ++g)
         if ((rc = update(ts[g], r0, m1, r0 + m1, m2))) return rc;
     return solve(ts, nt, r0, m1);

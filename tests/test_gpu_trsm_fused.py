@@ -2,10 +2,13 @@
 gb_ozaki.cu): the updates of at most 128 rows and depth 128 at the bottom of the
 recursion run as one launch that splits both operands into digits (A's from the digit
 images trsm_image_kernel builds once per solve, or by the CTA itself with
-GB_TRSM_IMAGES=0), multiplies them on the tensor cores and recombines in place.  It must
-give the same bits as the four-launch form (split, slice GEMM, recombination, gated IEEE
-fallback) that GB_TRSM_FUSED=0 selects, on every side / triangle / transposition, ragged
-sizes, one and two column groups, and every slice count the kernel takes."""
+GB_TRSM_IMAGES=0), multiplies them on the tensor cores and recombines in place; where the
+updated rows are a whole diagonal block, the same launch then solves that block (the
+gemmtrsm shape; GB_TRSM_GEMMTRSM=0 keeps the separate diagonal solve).  It must give the
+same bits as the four-launch form (split, slice GEMM, recombination, gated IEEE fallback)
+and separate diagonal solves that GB_TRSM_FUSED=0 selects, on every side / triangle /
+transposition, ragged sizes, one and two column groups, and every slice count the kernel
+takes."""
 import os
 
 import numpy as np
@@ -23,6 +26,7 @@ def restore(gblib):
     yield
     os.environ.pop("GB_TRSM_FUSED", None)
     os.environ.pop("GB_TRSM_IMAGES", None)
+    os.environ.pop("GB_TRSM_GEMMTRSM", None)
     blas.set_dgemm_mode(blas.DGEMM_NATIVE, 8)
 
 
@@ -66,6 +70,17 @@ def test_fused_updates_every_slice_count(slices):
     a, b0 = _problem("L", m, n, 41, spread=True)
     ref = _solve("L", "L", "N", "U", m, n, 1.0, a, b0, slices, False)
     got = _solve("L", "L", "N", "U", m, n, 1.0, a, b0, slices, True)
+    assert np.array_equal(got, ref), float(np.max(np.abs(got - ref)))
+
+
+@pytest.mark.parametrize("side,uplo,trans", [("L", "L", "N"), ("L", "U", "N"), ("R", "U", "T")])
+def test_fused_updates_without_gemmtrsm(side, uplo, trans):
+    # fused updates, diagonal blocks solved by their own launches: the same bits
+    m, n = 330, 140
+    a, b0 = _problem(side, m, n, 81, spread=True)
+    ref = _solve(side, uplo, trans, "N", m, n, 1.0, a, b0, 7, False)
+    os.environ["GB_TRSM_GEMMTRSM"] = "0"
+    got = _solve(side, uplo, trans, "N", m, n, 1.0, a, b0, 7, True)
     assert np.array_equal(got, ref), float(np.max(np.abs(got - ref)))
 
 
