@@ -55,7 +55,7 @@ SEED_A, SEED_B = 20261204, 20261205
 # full captures (dram__bytes_read.sum, dram__bytes_write.sum), with the products and int32 planes
 # of that launch: the digit form at 7 slices (28 products, 7 level planes) and the CRT form at 16
 # moduli (16 products, 16 planes)
-TRAFFIC_4096 = {"digits": (7136346112, 473230848, 28, 7), "crt": (1717197000, 1061339000, 16, 16)}
+TRAFFIC_4096 = {"digits": (7136346112, 473230848, 28, 7), "crt": (1368333000, 532505600, 16, 16)}
 
 
 def parse():

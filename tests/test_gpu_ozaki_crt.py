@@ -141,3 +141,21 @@ def test_crt_device_api_and_pipelined_host_path():
     finally:
         blas.set_dgemm_mode(blas.DGEMM_NATIVE)
     assert np.array_equal(c, ref)
+
+
+
+@pytest.mark.parametrize("moduli", list(range(2, 17)))
+def test_crt_every_moduli_count(moduli):
+    # the model's bits at every moduli count (the int16 residue planes and the recombination's
+    # weight tables), a partial tile of rows, op(B) transposed for odd counts
+    m, n, k = 300, 70, 120
+    a = po.expspread((m, k), 11)
+    b = po.expspread((k, n), 12)
+    tb = T if moduli % 2 else N
+    bb = b.T.copy(order="F") if moduli % 2 else b
+    c0 = po.uniform((m, n), 13)
+    ref = np.asfortranarray(c0.copy())
+    assert po.ozaki_crt_dgemm(N, tb, 0.5, a, bb, -1.0, ref, moduli) == 0
+    c = np.asfortranarray(c0.copy())
+    _run_gpu(N, tb, 0.5, a, bb, -1.0, c, moduli)
+    assert np.array_equal(c, ref), moduli
