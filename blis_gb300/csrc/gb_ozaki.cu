@@ -1537,6 +1537,7 @@ struct OzCrtTab {
     int n, t;
     float p[OZC_MAX], invp[OZC_MAX], wm[OZC_MAX];
     float pw[OZC_MAX][6];  // 2^(12q) mod p_l
+    float pw14[OZC_MAX][4];  // 2^(14q) mod p_l, symmetric (|.| <= p_l / 2)
     int wd[OZC_MAX][4];    // W_l = sum_q wd[l][q] 2^(32q), signed 32-bit digits
     int md[4];             // M in the same digits
 };
@@ -1557,14 +1558,16 @@ __device__ __forceinline__ unsigned long long oz_crt_scaled(unsigned long long b
     return (rem > half || (rem == half && (q & 1ull))) ? q + 1 : q;
 }
 
-// The N residues of x as floats (integers, |r| <= 128), from NL 12-bit limbs of X
-// (NL = 5 for t <= 59, else 6) carrying x's sign: s_l = sum_q h_q (2^(12q) mod p_l),
-// |s_l| < 6 2^12 2^8 < 2^22.6, is exact in fp32, and rint(s_l / p_l) by one fma onto
-// 1.5 2^23 (unit in the last place 1) is exact: the fma rounds s_l invp_l, which differs
-// from s_l / p_l by at most |s_l| 2^-24 / p_l < 0.38 / p_l, while a non-integral s_l / p_l
-// is at least 1 / (2 p_l) from a half-integer.  s_l - rint(s_l / p_l) p_l is then the
-// symmetric residue of the signed value.
-template <int N, int NL>
+// The N residues of x as floats (integers, |r| <= 128), from NL limbs of LB bits of X
+// carrying x's sign: s_l = sum_q h_q (2^(LB q) mod p_l).  Four 14-bit limbs with the
+// symmetric table (t <= 55: X <= 2^55 < 2^56) give |s_l| < 4 2^14 2^7 = 2^23; five or six
+// 12-bit limbs with the non-negative one (t <= 59, else t <= 71) give |s_l| < 6 2^12 2^8 <
+// 2^22.6.  Either is exact in fp32, and rint(s_l / p_l) by one fma onto 1.5 2^23 (unit in
+// the last place 1) is exact: the fma rounds s_l invp_l, which differs from s_l / p_l by at
+// most |s_l| 2^-24 / p_l < 1 / (2 p_l), while a non-integral s_l / p_l is at least
+// 1 / (2 p_l) from a half-integer.  s_l - rint(s_l / p_l) p_l is then the symmetric residue
+// of the signed value.
+template <int N, int NL, int LB>
 __device__ __forceinline__ void oz_crt_residues(double x, int e, const OzCrtTab& tab, float (&r)[N])
 {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
@@ -1574,12 +1577,13 @@ __device__ __forceinline__ void oz_crt_residues(double x, int e, const OzCrtTab&
     const float off = sgn ? 8388608.0f : -8388608.0f;
     float h[NL];
 #pragma unroll
-    for (int q = 0; q < NL; ++q) h[q] = __uint_as_float(sgn | 0x4B000000u | (uint32_t)((X >> (12 * q)) & 4095u)) + off;
+    for (int q = 0; q < NL; ++q)
+        h[q] = __uint_as_float(sgn | 0x4B000000u | (uint32_t)((X >> (LB * q)) & ((1u << LB) - 1u))) + off;
 #pragma unroll
     for (int l = 0; l < N; ++l) {
         float sl = 0.0f;
 #pragma unroll
-        for (int q = 0; q < NL; ++q) sl = __fmaf_rn(h[q], tab.pw[l][q], sl);
+        for (int q = 0; q < NL; ++q) sl = __fmaf_rn(h[q], LB == 14 ? tab.pw14[l][q] : tab.pw[l][q], sl);
         const float q = __fmaf_rn(sl, tab.invp[l], OZ_MAGIC) - OZ_MAGIC;
         r[l] = __fmaf_rn(-q, tab.p[l], sl);
     }
@@ -1589,7 +1593,7 @@ __device__ __forceinline__ void oz_crt_residues(double x, int e, const OzCrtTab&
 // residue planes, K-major, zero in the padding.  Warp w converts rows 4w ..
 // 4w + 3 in turn, lane c elements 2c and 2c + 1 of the row: every plane store
 // of a warp is one contiguous 128-byte line.
-template <int N, int NL>
+template <int N, int NL, int LB>
 __global__ void __launch_bounds__(256, 4) oz_crt_split_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
                                                            int64_t sr, int64_t sl,
                                                            const unsigned long long* __restrict__ maxbits,
@@ -1623,8 +1627,8 @@ __global__ void __launch_bounds__(256, 4) oz_crt_split_kernel(int64_t rows, int6
             if (blockIdx.x == 0 && lane == 0) exps[r] = e;
         }
         float f0[N], f1[N];
-        oz_crt_residues<N, NL>(r < rows ? tile[rr][2 * lane] : 0.0, e, tab, f0);
-        oz_crt_residues<N, NL>(r < rows ? tile[rr][2 * lane + 1] : 0.0, e, tab, f1);
+        oz_crt_residues<N, NL, LB>(r < rows ? tile[rr][2 * lane] : 0.0, e, tab, f0);
+        oz_crt_residues<N, NL, LB>(r < rows ? tile[rr][2 * lane + 1] : 0.0, e, tab, f1);
         // kpad and l0 are multiples of 64: the pair's 4 bytes are aligned
         uint32_t* dst = reinterpret_cast<uint32_t*>(out + r * kpad + l0) + lane;
 #pragma unroll
@@ -1778,6 +1782,11 @@ void crt_table(int n, int t, OzCrtTab* tab)
             tab->pw[l][q] = (float)pw;
             pw = (pw * 4096) % pl;
         }
+        pw = 1 % pl;
+        for (int q = 0; q < 4; ++q) {
+            tab->pw14[l][q] = (float)(2 * pw > pl ? pw - pl : pw);
+            pw = (pw * 16384) % pl;
+        }
     }
     signed_digits32((__int128)M, tab->md);
 }
@@ -1789,10 +1798,12 @@ void launch_crt_split(int64_t rows, int64_t k, const double* R, int64_t sr, int6
 {
     LaunchScope ls("oz_split_crt", s);
     const dim3 grid((unsigned)(kpad / 64), (unsigned)(rcover / 32));
-    if (tab.t <= 59)  // X < 2^60: five 12-bit limbs
-        oz_crt_split_kernel<N, 5><<<grid, 256, 0, s>>>(rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, tab);
+    if (tab.t <= 55)  // X <= 2^55: four 14-bit limbs
+        oz_crt_split_kernel<N, 4, 14><<<grid, 256, 0, s>>>(rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, tab);
+    else if (tab.t <= 59)  // X <= 2^59: five 12-bit limbs
+        oz_crt_split_kernel<N, 5, 12><<<grid, 256, 0, s>>>(rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, tab);
     else
-        oz_crt_split_kernel<N, 6><<<grid, 256, 0, s>>>(rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, tab);
+        oz_crt_split_kernel<N, 6, 12><<<grid, 256, 0, s>>>(rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite, tab);
 }
 
 template <int N>
