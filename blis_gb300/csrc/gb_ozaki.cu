@@ -3229,7 +3229,6 @@ __global__ void __launch_bounds__(TU_THREADS, 1) trsm_update_fused_kernel(const 
         er[tid] = oz_row_exponent(mx, &nf);
         if (nf) s_nf = 1;
     }
-#pragma unroll
     {
         // all 16 loads of a lane (4 columns x k = lane + 32 i, K <= 128) in flight at once
         double xv[4][2 * TU_KC / 32];

@@ -117,5 +117,8 @@ def test_fused_updates_nonfinite_tile():
     ref = _solve("L", "L", "N", "N", m, n, 1.0, a, b0, 7, False)
     got = _solve("L", "L", "N", "N", m, n, 1.0, a, b0, 7, True)
     assert np.array_equal(np.isfinite(got), np.isfinite(ref))
+    # the fused path sends only the 32-column tiles that meet the Inf to FP64 FMAs, the
+    # four-launch path the whole update to the IEEE kernel: the other columns differ by the
+    # Ozaki form's rounding against the native kernel's, normwise
     fin = np.isfinite(ref)
-    assert np.allclose(got[fin], ref[fin], rtol=1e-13, atol=0.0)
+    assert np.max(np.abs(got[fin] - ref[fin])) <= 1e-13 * np.max(np.abs(ref[fin]))
