@@ -1235,7 +1235,9 @@ __global__ void __launch_bounds__(256, (S <= 7 ? 3 : 2)) oz_recombine_kernel(con
     const int64_t plane_stride = p.npad * p.mpad;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = e / mq, i0 = (e - j * mq) * 4;
+        // 32-bit division while the index fits (the 64-bit one costs several times more)
+        const int64_t j = (total <= 0xFFFFFFFFll) ? (int64_t)((uint32_t)e / (uint32_t)mq) : e / mq;
+        const int64_t i0 = (e - j * mq) * 4;
         // rows of column j's diagonal element: lower keeps rows >= dlo, upper rows <= dhi
         const int64_t dlo = (int64_t)p.out_rpc * j, dhi = dlo + p.out_rpc - 1;
         if (p.out_tri && (p.out_tri == 1 ? i0 + 3 < dlo : i0 > dhi)) continue;
@@ -1650,7 +1652,9 @@ __global__ void __launch_bounds__(256, 2) oz_crt_recombine_kernel(const __grid_c
     const int64_t plane_stride = p.npad * p.mpad;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = e / mq, i0 = (e - j * mq) * 4;
+        // 32-bit division while the index fits (the 64-bit one costs several times more)
+        const int64_t j = (total <= 0xFFFFFFFFll) ? (int64_t)((uint32_t)e / (uint32_t)mq) : e / mq;
+        const int64_t i0 = (e - j * mq) * 4;
         const int64_t dlo = (int64_t)p.out_rpc * j, dhi = dlo + p.out_rpc - 1;
         if (p.out_tri && (p.out_tri == 1 ? i0 + 3 < dlo : i0 > dhi)) continue;
         const int64_t off = j * p.mpad + i0;

@@ -23,7 +23,9 @@ __global__ void f32_to_f64_kernel(int64_t rows, int64_t cols, const float* __res
     const int64_t total = rows * cols;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = e / rows, i = e - j * rows;
+        // 32-bit division while the index fits (the 64-bit one costs several times more)
+        const int64_t j = (total <= 0xFFFFFFFFll) ? (int64_t)((uint32_t)e / (uint32_t)rows) : e / rows;
+        const int64_t i = e - j * rows;
         dst[e] = (double)src[i * rs + j * cs];
     }
 }
@@ -35,7 +37,8 @@ __global__ void sgemm_split_epilogue_kernel(int64_t m, int64_t n, const double* 
     const int64_t total = m * n;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = e / m, i = e - j * m;
+        const int64_t j = (total <= 0xFFFFFFFFll) ? (int64_t)((uint32_t)e / (uint32_t)m) : e / m;
+        const int64_t i = e - j * m;
         float* cij = c + i * rs_c + j * cs_c;
         const double t = alpha * P[e];
         *cij = (float)(beta == 0.0 ? t : fma(beta, (double)*cij, t));

@@ -101,6 +101,9 @@ def run_gemm(out):
     ms = _timer(lambda: dev.dgemm_ozaki(0, 0, 1.0, a, b, 0.0, c, 7), reps=3)
     out.append({"workload": "dgemm_%d" % n, "form": "ozaki_s7", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9,
                 "bf16_frac_of_measured_peak": 28 * 2 * n ** 3 / ms / 1e9 / pk.get("bf16_tflops", 1900.0)})
+    ms = _timer(lambda: dev.dgemm_ozaki_crt(0, 0, 1.0, a, b, 0.0, c, 16), reps=3)
+    out.append({"workload": "dgemm_%d" % n, "form": "ozaki_crt16", "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9,
+                "bf16_frac_of_measured_peak": 16 * 2 * n ** 3 / ms / 1e9 / pk.get("bf16_tflops", 1900.0)})
     del a, b, c
     fa, fb, fc = (_mat(n, n, seed=s, dtype=torch.float32) for s in (7, 8, 9))
     ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
