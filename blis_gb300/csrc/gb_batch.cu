@@ -66,6 +66,67 @@ __global__ void __launch_bounds__(NT) grouped_gemm_kernel(const BatchDesc* __res
     }
 }
 
+// FP32 problems through SGEMM's split form (plan policy 3): one grouped launch
+// widens every stored op(A) and op(B) into FP64 arenas (exact), the FP64
+// products P = op(A) op(B) run as one grouped Ozaki plan at 3 slices, and one
+// grouped launch rounds alpha P + beta C to FP32 once.  A job is one matrix;
+// its elements go in blocks of 1024 (4 per thread), block b of the launch
+// finding its job by binary search over the jobs' first blocks.
+struct SplitJob {
+    const void* src;  // widen: the FP32 matrix; round: P
+    void* dst;        // widen: the FP64 arena copy; round: C
+    int64_t rows, cols, ld;  // widen: stored shape and ld of src; round: m, n and ldc of C
+    double alpha, beta;
+    int64_t block0;
+};
+
+__device__ __forceinline__ int split_job_of(const SplitJob* __restrict__ jobs, int njobs, int64_t b)
+{
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].block0 <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) split_widen_kernel(const SplitJob* __restrict__ jobs, int njobs)
+{
+    const SplitJob& q = jobs[split_job_of(jobs, njobs, blockIdx.x)];
+    const float* src = static_cast<const float*>(q.src);
+    double* dst = static_cast<double*>(q.dst);
+    const int64_t total = q.rows * q.cols;
+    const int64_t e0 = ((int64_t)blockIdx.x - q.block0) * 1024 + threadIdx.x;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int64_t e = e0 + 256 * u;
+        if (e < total) {
+            const int64_t j = (int64_t)((uint32_t)e / (uint32_t)q.rows), i = e - j * q.rows;  // total < 2^32
+            dst[e] = (double)src[i + j * q.ld];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) split_round_kernel(const SplitJob* __restrict__ jobs, int njobs)
+{
+    const SplitJob& q = jobs[split_job_of(jobs, njobs, blockIdx.x)];
+    const double* P = static_cast<const double*>(q.src);
+    float* c = static_cast<float*>(q.dst);
+    const int64_t total = q.rows * q.cols;
+    const int64_t e0 = ((int64_t)blockIdx.x - q.block0) * 1024 + threadIdx.x;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int64_t e = e0 + 256 * u;
+        if (e < total) {
+            const int64_t j = (int64_t)((uint32_t)e / (uint32_t)q.rows), i = e - j * q.rows;
+            float* cij = c + i + j * q.ld;
+            const double t = (q.alpha == 0.0) ? 0.0 : q.alpha * P[e];  // alpha = 0: P is not read
+            *cij = (float)(q.beta == 0.0 ? t : fma(q.beta, (double)*cij, t));
+        }
+    }
+}
+
 }  // namespace
 
 // A resident batch: descriptor table in HBM, tile counter, optional graph.
@@ -90,11 +151,31 @@ struct BatchPlan {
     BatchPlan* rest = nullptr;
     std::vector<gb_gemm_problem_t> singles;
     int slices = 0;
+    // policy 3 (FP32 through the split form): arenas, job tables, the inner FP64 Ozaki plan
+    double* split_arena = nullptr;
+    SplitJob* d_jobs = nullptr;  // widen jobs, then round jobs
+    int wjobs = 0, rjobs = 0;
+    int64_t wblocks = 0, rblocks = 0;
+    BatchPlan* inner = nullptr;
 };
 
 static int launch_plan(BatchPlan* pl, cudaStream_t s)
 {
     int rc;
+    if (pl->inner) {
+        if (pl->wblocks > 0) {
+            LaunchScope ls("batch_split_widen", s);
+            split_widen_kernel<<<(unsigned)pl->wblocks, 256, 0, s>>>(pl->d_jobs, pl->wjobs);
+            if ((rc = check_cuda(cudaGetLastError(), "batch split widen"))) return rc;
+        }
+        if ((rc = launch_plan(pl->inner, s))) return rc;
+        if (pl->rblocks > 0) {
+            LaunchScope ls("batch_split_round", s);
+            split_round_kernel<<<(unsigned)pl->rblocks, 256, 0, s>>>(pl->d_jobs + pl->wjobs, pl->rjobs);
+            if ((rc = check_cuda(cudaGetLastError(), "batch split round"))) return rc;
+        }
+        return GB_SUCCESS;
+    }
     if (pl->oz && (rc = ozaki_batch_launch(pl->oz, s))) return rc;
     if (pl->rest && (rc = launch_plan(pl->rest, s))) return rc;
     for (const gb_gemm_problem_t& p : pl->singles) {
@@ -125,12 +206,115 @@ void batch_plan_destroy(BatchPlan* pl);
 int batch_plan_run(BatchPlan* pl, cudaStream_t s, bool use_graph);
 static int batch_plan_build(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out);
 
+int batch_plan_create(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out, bool tune);
+
+// Policy 3, FP32 only: the split form (see SplitJob).
+static int batch_plan_split(const gb_gemm_problem_t* probs, int64_t count, BatchPlan** out)
+{
+    *out = nullptr;
+    std::vector<gb_gemm_problem_t> p64;
+    std::vector<SplitJob> widen, round;
+    int64_t elems = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        const gb_gemm_problem_t& p = probs[i];
+        if (p.m < 0 || p.n < 0 || p.k < 0) return set_error(GB_ERR_ARG, "gb_batch", "negative dimension");
+        if (p.m == 0 || p.n == 0) continue;
+        const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
+        const int64_t ar = ta ? p.k : p.m, ac = ta ? p.m : p.k, br = tb ? p.n : p.k, bc = tb ? p.k : p.n;
+        if (ar * ac >= 0xFFFFFFFFll || br * bc >= 0xFFFFFFFFll || p.m * p.n >= 0xFFFFFFFFll)
+            return set_error(GB_ERR_UNSUPPORTED, "gb_batch", "a problem too large for the split plan");
+        elems += ar * ac + br * bc + p.m * p.n;
+    }
+    BatchPlan* pl = new BatchPlan();
+    pl->dtype = GB_BATCH_FP32;
+    pl->nprob = 0;
+    pl->total_tiles = 0;
+    pl->d_desc = nullptr;
+    pl->d_counter = nullptr;
+    pl->graph = nullptr;
+    pl->graph_stream = nullptr;
+    cudaStream_t s = thread_stream();
+    pl->split_arena = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(elems + 1), s));
+    if (!pl->split_arena) {
+        delete pl;
+        return GB_ERR_NOMEM;
+    }
+    int64_t off = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        const gb_gemm_problem_t& p = probs[i];
+        if (p.m == 0 || p.n == 0) continue;
+        const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
+        const int64_t ar = ta ? p.k : p.m, ac = ta ? p.m : p.k, br = tb ? p.n : p.k, bc = tb ? p.k : p.n;
+        double* a64 = pl->split_arena + off;
+        off += ar * ac;
+        double* b64 = pl->split_arena + off;
+        off += br * bc;
+        double* c64 = pl->split_arena + off;
+        off += p.m * p.n;
+        if (ar * ac > 0) widen.push_back(SplitJob{p.a, a64, ar, ac, p.lda, 0.0, 0.0, 0});
+        if (br * bc > 0) widen.push_back(SplitJob{p.b, b64, br, bc, p.ldb, 0.0, 0.0, 0});
+        gb_gemm_problem_t q = p;
+        q.a = a64;
+        q.lda = ar > 0 ? ar : 1;
+        q.b = b64;
+        q.ldb = br > 0 ? br : 1;
+        q.c = c64;
+        q.ldc = p.m;
+        q.alpha = (p.alpha == 0.0) ? 0.0 : 1.0;  // P = op(A) op(B), or 0
+        q.beta = 0.0;
+        p64.push_back(q);
+        round.push_back(SplitJob{c64, p.c, p.m, p.n, p.ldc, p.alpha, p.beta, 0});
+    }
+    auto number = [](std::vector<SplitJob>& v) {
+        int64_t b = 0;
+        for (auto& j : v) {
+            j.block0 = b;
+            b += (j.rows * j.cols + 1023) / 1024;
+        }
+        return b;
+    };
+    pl->wblocks = number(widen);
+    pl->rblocks = number(round);
+    pl->wjobs = (int)widen.size();
+    pl->rjobs = (int)round.size();
+    int rc = GB_SUCCESS;
+    if (pl->wblocks > INT32_MAX || pl->rblocks > INT32_MAX)
+        rc = set_error(GB_ERR_UNSUPPORTED, "gb_batch", "batch too large for the split plan");
+    if (!rc) {
+        std::vector<SplitJob> all(widen);
+        all.insert(all.end(), round.begin(), round.end());
+        pl->d_jobs = static_cast<SplitJob*>(dev_alloc(sizeof(SplitJob) * (all.size() + 1), s));
+        if (!pl->d_jobs) rc = GB_ERR_NOMEM;
+        if (!rc && !all.empty())
+            rc = check_cuda(cudaMemcpyAsync(pl->d_jobs, all.data(), sizeof(SplitJob) * all.size(),
+                                            cudaMemcpyHostToDevice, s),
+                            "batch split jobs");
+        if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "batch split jobs");
+    }
+    if (!rc) {
+        // the FP64 products: the grouped Ozaki plan in the digit form at the split form's slices
+        ModeOverride digits(GB_DGEMM_OZAKI, GB_SGEMM_SPLIT_SLICES, 0);
+        rc = batch_plan_create(p64.data(), (int64_t)p64.size(), GB_BATCH_FP64_OZAKI, &pl->inner, false);
+    }
+    if (rc) {
+        batch_plan_destroy(pl);
+        return rc;
+    }
+    pl->policy = 3;
+    *out = pl;
+    return GB_SUCCESS;
+}
+
 // Native FP64/FP32 batch with one configuration policy: 0 = every problem
 // on the 128 x 128 engine; 1 = the 64 x 64 engine for the problems whose
 // selected configuration is 1..5, without split-K (a batch already has
 // parallelism); 2 = the selected configuration including its split-K.
 int batch_plan_policy(const gb_gemm_problem_t* probs, int64_t count, int dtype, int policy, BatchPlan** out)
 {
+    if (policy == 3) {
+        if (dtype != GB_BATCH_FP32) return set_error(GB_ERR_ARG, "gb_batch", "policy 3 (split form) is FP32 only");
+        return batch_plan_split(probs, count, out);
+    }
     std::vector<gb_gemm_problem_t> big, small;
     std::vector<int> cfgs;
     for (int64_t i = 0; i < count; ++i) {
@@ -161,14 +345,18 @@ int batch_plan_policy(const gb_gemm_problem_t* probs, int64_t count, int dtype, 
     return GB_SUCCESS;
 }
 
-// Native FP64/FP32 plan.  Without a selector model (gb_selector_load_file +
-// gb_set_gemm_autoselect) every problem takes the 128 x 128 engine.  With
-// one, the plan is autotuned when it is created: each policy runs twice on
-// the batch's own shapes with scratch outputs (the caller's C is not
-// touched), timed with CUDA events, and the fastest is kept.
+// Native FP64/FP32 plan, autotuned when it is created: each candidate policy
+// runs twice on the batch's own shapes with scratch outputs (the caller's C
+// is not touched), timed with CUDA events, and the fastest is kept.  The
+// candidates: policy 0 always; 1 and 2 with a selector model loaded
+// (gb_selector_load_file + gb_set_gemm_autoselect); 3 for FP32 unless
+// gb_set_sgemm_mode pinned SGEMM to the FP32 pipe.
 static int batch_plan_selected(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out)
 {
-    if (!selector_auto()) return batch_plan_policy(probs, count, dtype, 0, out);
+    std::vector<int> cands{0};
+    if (selector_auto()) cands.insert(cands.end(), {1, 2});
+    if (dtype == GB_BATCH_FP32 && sgemm_mode_setting != GB_SGEMM_FMA) cands.push_back(3);
+    if (cands.size() == 1) return batch_plan_policy(probs, count, dtype, 0, out);
     cudaStream_t s = thread_stream();
     const size_t esz = dtype == GB_BATCH_FP32 ? 4 : 8;
     std::vector<gb_gemm_problem_t> tune(probs, probs + count);
@@ -189,7 +377,8 @@ static int batch_plan_selected(const gb_gemm_problem_t* probs, int64_t count, in
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int policy = 0; policy < 3 && !rc; ++policy) {
+    for (size_t ci = 0; ci < cands.size() && !rc; ++ci) {
+        const int policy = cands[ci];
         BatchPlan* t = nullptr;
         if ((rc = batch_plan_policy(tune.data(), count, dtype, policy, &t))) break;
         rc = batch_plan_run(t, s, false);  // warm-up
@@ -313,7 +502,7 @@ static int batch_plan_build(const gb_gemm_problem_t* probs, int64_t count, int d
 int batch_plan_run(BatchPlan* pl, cudaStream_t s, bool use_graph)
 {
     // problems run one by one through the Ozaki form allocate workspace per call: no graph
-    if (!use_graph || !pl->singles.empty()) return launch_plan(pl, s);
+    if (!use_graph || !pl->singles.empty() || (pl->inner && !pl->inner->singles.empty())) return launch_plan(pl, s);
     if (!pl->graph) {
         cudaStream_t cap;
         GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -345,8 +534,11 @@ void batch_plan_destroy(BatchPlan* pl)
     dev_free(pl->d_counter, s);
     ozaki_batch_destroy(pl->oz, s);
     sup_group_destroy(pl->sup, s);
+    dev_free(pl->split_arena, s);
+    dev_free(pl->d_jobs, s);
     cudaStreamSynchronize(s);
     batch_plan_destroy(pl->rest);
+    batch_plan_destroy(pl->inner);
     delete pl;
 }
 
@@ -615,8 +807,9 @@ extern "C" int gb_batch_plan_create_ex(const gb_gemm_problem_t* probs, gb_dim_t 
     *plan = nullptr;
     if (dtype != GB_BATCH_FP64 && dtype != GB_BATCH_FP32)
         return gb::set_error(GB_ERR_ARG, "gb_batch_plan_create_ex", "dtype must be GB_BATCH_FP64 or FP32");
-    if (policy < -1 || policy > 2) return gb::set_error(GB_ERR_ARG, "gb_batch_plan_create_ex", "policy in -1..2");
-    if (policy > 0 && !gb::selector_auto())
+    if (policy < -1 || policy > 3 || (policy == 3 && dtype != GB_BATCH_FP32))
+        return gb::set_error(GB_ERR_ARG, "gb_batch_plan_create_ex", "policy in -1..2, or 3 for FP32");
+    if ((policy == 1 || policy == 2) && !gb::selector_auto())
         return gb::set_error(GB_ERR_ARG, "gb_batch_plan_create_ex", "policies 1 and 2 need a loaded selector");
     gb::BatchPlan* pl = nullptr;
     rc = (policy < 0) ? gb::batch_plan_create(probs, count, dtype, &pl, true)

@@ -284,6 +284,7 @@ int ozaki_digit_slices();
 // SGEMM split form (gb_sgemm_split.cu): the digit form with this many slices on
 // FP64-widened operands; whether a shape takes it (gb_set_sgemm_mode).
 constexpr int GB_SGEMM_SPLIT_SLICES = 3;
+extern int sgemm_mode_setting;  // GB_SGEMM_FMA, _SPLIT or _AUTO (gb_set_sgemm_mode)
 bool sgemm_use_split(int64_t m, int64_t n, int64_t k);
 int sgemm_split_dev(int64_t m, int64_t n, int64_t k, float alpha, const float* a, int64_t ars, int64_t acs,
                     const float* b, int64_t brs, int64_t bcs, float beta, float* c, int64_t rs_c, int64_t cs_c,

@@ -334,7 +334,8 @@ def run_batch(out):
             S.load_into_library()
             try:
                 pol = {}
-                for policy in (1, 2, -1):  # fixed policies, then the plan's own autotuning
+                # fixed policies (3: FP32 through the split form), then the plan's own autotuning
+                for policy in ((1, 2, 3, -1) if dtype == 1 else (1, 2, -1)):
                     plan2 = C.c_void_p()
                     _lib.check(L.gb_batch_plan_create_ex(C.addressof(probs), 4096, dtype, policy, C.byref(plan2)),
                                "plan")
@@ -347,9 +348,32 @@ def run_batch(out):
             rec.update({"policy1_selected_tiles_ms": pol[1][0], "policy2_selected_tiles_splitk_ms": pol[2][0],
                         "autotuned_plan_ms": pol[-1][0], "autotuned_policy": pol[-1][1],
                         "autotuned_tflops": flops / pol[-1][0] / 1e9})
+            if dtype == 1:
+                rec["policy3_split_form_ms"] = pol[3][0]
         out.append(rec)
         L.gb_set_dgemm_mode(0, 8)
         del keep
+
+
+def run_batch_large_fp32(out):
+    """FP32 gemm_batch of 64 problems with m, n, k log-uniform in [1024, 4096]:
+    the FP32-pipe grouped plan (policy 0) against the split form (policy 3:
+    widen, grouped Ozaki at 3 slices, round), and the plan's autotuned pick."""
+    L = _lib.load()
+    probs, keep, flops = batch_problems(64, 5, 1, lo=1024, hi=4096)
+    st = _stream()
+    rec = {"workload": "batch_64_fp32_1024_4096", "flops": flops}
+    for policy, key in ((0, "policy0_ffma"), (3, "policy3_split_form"), (-1, "autotuned")):
+        plan = C.c_void_p()
+        _lib.check(L.gb_batch_plan_create_ex(C.addressof(probs), 64, 1, policy, C.byref(plan)), "plan")
+        ms = _timer(lambda: _lib.check(L.gb_batch_plan_run(plan, 1, st), "run"), reps=3, warmup=1)
+        rec[key + "_ms"] = ms
+        rec[key + "_tflops"] = flops / ms / 1e9
+        if policy < 0:
+            rec["autotuned_policy"] = L.gb_batch_plan_policy(plan)
+        L.gb_batch_plan_destroy(plan)
+    out.append(rec)
+    del keep
 
 
 def run_level3x(out):
@@ -552,7 +576,8 @@ def run_e2e(out, calls=8):
 
 
 SUITES = {"crt": run_crt, "e2e": run_e2e, "gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
-          "batch": run_batch, "batch_ozaki": run_batch_ozaki, "sgemm": run_sgemm, "bgemm": run_bgemm,
+          "batch": run_batch, "batch_fp32_large": run_batch_large_fp32, "batch_ozaki": run_batch_ozaki,
+          "sgemm": run_sgemm, "bgemm": run_bgemm,
           "level3x": run_level3x, "level12x": run_level12x, "complex": run_complex, "hermitian": run_hermitian}
 
 

@@ -692,11 +692,16 @@ int gb_batch_plan_destroy(void* plan);
    the 128x128 engine; 1 = the 64x64 engine for the problems the selector
    assigns to configs 1..5, without split-K; 2 = the selected configuration
    including split-K (those problems run in a second grouped launch and a
-   grouped fold, in the same graph).  gb_batch_plan_create autotunes it when
-   a selector model is loaded and auto-selection is on: each policy runs on
-   the batch's shapes with scratch outputs and the fastest is kept (without a
-   model: policy 0).  One-shot gb_gemm_batch_dev / dgemm_batch_ calls use
-   policy 0.  gb_batch_plan_create_ex fixes the policy (-1 = autotune). */
+   grouped fold, in the same graph); 3 (FP32 only) = SGEMM's split form for
+   the whole batch: one grouped launch widens op(A) and op(B) to FP64, the
+   products run as one grouped Ozaki plan at 3 slices on the bf16 tensor
+   cores, one grouped launch rounds alpha P + beta C to FP32 once.
+   gb_batch_plan_create autotunes it: each candidate runs on the batch's
+   shapes with scratch outputs and the fastest is kept.  Candidates: 0; 1 and
+   2 when a selector model is loaded and auto-selection is on; 3 for FP32
+   unless gb_set_sgemm_mode(GB_SGEMM_FMA).  One-shot gb_gemm_batch_dev /
+   dgemm_batch_ calls use policy 0.  gb_batch_plan_create_ex fixes the policy
+   (-1 = autotune). */
 int gb_batch_plan_create_ex(const gb_gemm_problem_t* probs, gb_dim_t count, int dtype, int policy, void** plan);
 int gb_batch_plan_policy(const void* plan);
 

@@ -142,6 +142,82 @@ def test_grouped_equals_loop_and_graph_replay(gblib):
         assert np.allclose(g.cpu().numpy().T, ref, rtol=1e-12, atol=1e-12)
 
 
+def test_fp32_plan_split_form_edge_cases(gblib):
+    """FP32 plans through the split form (policy 3): larger problems, beta != 0,
+    alpha = 0 over NaN operands, k = 0, m = 0, an Inf in op(A); the autotuned plan
+    (no selector loaded) picks between policies 0 and 3, and pinning SGEMM to the
+    FP32 pipe leaves policy 0 alone."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(31)
+    shapes = [(1100, 900, 1300, 1.0, 0.0), (700, 1024, 1500, -0.75, 0.5), (64, 48, 0, 1.0, 0.5),
+              (0, 40, 30, 1.0, 0.0), (200, 100, 300, 0.0, 0.5), (300, 200, 250, 1.0, 0.0),
+              (33, 17, 1000, 2.0, -1.0)]
+    probs = []
+    for i, (m, n, k, alpha, beta) in enumerate(shapes):
+        ta, tb = int(rng.integers(0, 2)), int(rng.integers(0, 2))
+        a = po.uniform((k, m) if ta else (m, k), 300 + i, dtype=np.float32)
+        b = po.uniform((n, k) if tb else (k, n), 400 + i, dtype=np.float32)
+        c = po.uniform((m, n), 500 + i, dtype=np.float32)
+        if alpha == 0.0:
+            a[:] = np.nan  # not read when alpha = 0
+        if i == 5:
+            a[3, 7] = np.inf
+        probs.append((ta, tb, m, n, k, alpha, beta, a, b, c))
+    L = _lib.load()
+    L.gb_batch_plan_create_ex.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+    L.gb_batch_plan_run.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    L.gb_batch_plan_destroy.argtypes = [C.c_void_p]
+    L.gb_batch_plan_policy.argtypes = [C.c_void_p]
+
+    def run(policy):
+        descs = (_lib_problem * len(probs))()
+        keep, outs = [], []
+        for i, (ta, tb, m, n, k, alpha, beta, a, b, c) in enumerate(probs):
+            A = torch.from_numpy(np.asfortranarray(a).T.copy()).cuda()
+            B = torch.from_numpy(np.asfortranarray(b).T.copy()).cuda()
+            Cg = torch.from_numpy(np.asfortranarray(c).T.copy()).cuda()
+            keep += [A, B]
+            outs.append(Cg)
+            descs[i] = _lib_problem(8 * ta, 8 * tb, m, n, k, alpha, beta, A.data_ptr(), max(a.shape[0], 1),
+                                    B.data_ptr(), max(b.shape[0], 1), Cg.data_ptr(), max(m, 1))
+        torch.cuda.synchronize()
+        plan = C.c_void_p()
+        assert L.gb_batch_plan_create_ex(C.addressof(descs), len(probs), 1, policy, C.byref(plan)) == 0
+        got_policy = L.gb_batch_plan_policy(plan)
+        assert L.gb_batch_plan_run(plan, 1, None) == 0
+        assert L.gb_synchronize() == 0
+        L.gb_batch_plan_destroy(plan)
+        return got_policy, [o.cpu().numpy().T for o in outs]
+
+    pol3, res3 = run(3)
+    assert pol3 == 3
+    polt, rest = run(-1)
+    assert polt in (0, 3)
+    assert gblib.gb_set_sgemm_mode(0) == 0  # GB_SGEMM_FMA
+    try:
+        pol0, res0 = run(-1)
+    finally:
+        assert gblib.gb_set_sgemm_mode(2) == 0  # GB_SGEMM_AUTO
+    assert pol0 == 0
+    u = 2.0 ** -24
+    for (ta, tb, m, n, k, alpha, beta, a, b, c), g3, gt, g0 in zip(probs, res3, rest, res0):
+        A = (a.T if ta else a).astype(np.float64)
+        B = (b.T if tb else b).astype(np.float64)
+        c64 = c.astype(np.float64)
+        if alpha == 0.0:
+            ref, bound = beta * c64, np.abs(beta * c64) * u
+        else:
+            with np.errstate(invalid="ignore"):
+                ref = alpha * (A @ B) + beta * c64
+                bound = 2 * (k + 2) * u * (abs(alpha) * (np.abs(A) @ np.abs(B)) + abs(beta) * np.abs(c64))
+        fin = np.isfinite(ref)
+        for g in (g3, gt, g0):
+            g = g.astype(np.float64)
+            assert np.array_equal(np.isnan(g), np.isnan(ref)) and np.array_equal(np.isinf(g), np.isinf(ref))
+            assert np.array_equal(g[~fin & ~np.isnan(ref)], ref[~fin & ~np.isnan(ref)])
+            assert np.all(np.abs(g[fin] - ref[fin]) <= bound[fin])
+
+
 class _lib_problem(C.Structure):
     _fields_ = [("transa", C.c_int), ("transb", C.c_int), ("m", C.c_int64), ("n", C.c_int64),
                 ("k", C.c_int64), ("alpha", C.c_double), ("beta", C.c_double), ("a", C.c_void_p),
@@ -193,10 +269,13 @@ def test_batch_with_selected_configs(gblib, dtype):
         assert any(v >= 1 for v in cfgs)  # the grouped 64 x 64 launch is exercised
         c0 = [o.clone() for o in outs]
         results = {}
-        for policy in (1, 2, -1):  # fixed policies, then the plan's own autotuning
+        # fixed policies (3: FP32 through SGEMM's split form), then the plan's own autotuning
+        policies = (1, 2, 3, -1) if code == 1 else (1, 2, -1)
+        for policy in policies:
             plan = C.c_void_p()
             assert L.gb_batch_plan_create_ex(C.addressof(descs), len(probs), code, policy, C.byref(plan)) == 0
-            assert L.gb_batch_plan_policy(plan) in ((0, 1, 2) if policy < 0 else (policy,))
+            assert L.gb_batch_plan_policy(plan) in (((0, 1, 2, 3) if code == 1 else (0, 1, 2)) if policy < 0
+                                                    else (policy,))
             first = None
             for rep in range(3):
                 for o, z in zip(outs, c0):
@@ -218,13 +297,14 @@ def test_batch_with_selected_configs(gblib, dtype):
     # componentwise: |C - C_ref| <= 2 k u (|alpha| |A| |B| + |beta| |C0|) (operands are not
     # normalized as in the testsuite, so its absolute residual does not apply)
     u = 2.0 ** -53 if dtype == np.float64 else 2.0 ** -24
-    for (ta, tb, m, n, k, a, b, c), g1, g2 in zip(probs, results[1], results[2]):
+    checked = [results[1], results[2]] + ([results[3]] if code == 1 else [])
+    for idx, (ta, tb, m, n, k, a, b, c) in enumerate(probs):
         A = H.op(a, 8 if ta == "T" else 0).astype(np.float64)
         B = H.op(b, 8 if tb == "T" else 0).astype(np.float64)
         ref = 1.25 * (A @ B) - 0.5 * c.astype(np.float64)
         bound = 2 * (k + 2) * u * (1.25 * (np.abs(A) @ np.abs(B)) + 0.5 * np.abs(c.astype(np.float64)))
-        for g in (g1, g2):
-            assert np.all(np.abs(g.cpu().numpy().T.astype(np.float64) - ref) <= bound)
+        for res in checked:
+            assert np.all(np.abs(res[idx].cpu().numpy().T.astype(np.float64) - ref) <= bound)
 
 
 @pytest.mark.parametrize("n", [300, 20000, 40000, 120000])
