@@ -66,73 +66,12 @@ __global__ void __launch_bounds__(NT) grouped_gemm_kernel(const BatchDesc* __res
     }
 }
 
-// FP32 problems through SGEMM's split form (plan policy 3): one grouped launch
-// widens every stored op(A) and op(B) into FP64 arenas (exact), the FP64
-// products P = op(A) op(B) run as one grouped Ozaki plan at 3 slices, and one
-// grouped launch rounds alpha P + beta C to FP32 once.  A job is one matrix;
-// its elements go in blocks of 1024 (4 per thread), block b of the launch
-// finding its job by binary search over the jobs' first blocks.
-struct SplitJob {
-    const void* src;  // widen: the FP32 matrix; round: P
-    void* dst;        // widen: the FP64 arena copy; round: C
-    int64_t rows, cols, ld;  // widen: stored shape and ld of src; round: m, n and ldc of C
-    double alpha, beta;
-    int64_t block0;
-};
-
-__device__ __forceinline__ int split_job_of(const SplitJob* __restrict__ jobs, int njobs, int64_t b)
-{
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (jobs[mid].block0 <= b) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-__global__ void __launch_bounds__(256) split_widen_kernel(const SplitJob* __restrict__ jobs, int njobs)
-{
-    const SplitJob& q = jobs[split_job_of(jobs, njobs, blockIdx.x)];
-    const float* src = static_cast<const float*>(q.src);
-    double* dst = static_cast<double*>(q.dst);
-    const int64_t total = q.rows * q.cols;
-    const int64_t e0 = ((int64_t)blockIdx.x - q.block0) * 1024 + threadIdx.x;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const int64_t e = e0 + 256 * u;
-        if (e < total) {
-            const int64_t j = (int64_t)((uint32_t)e / (uint32_t)q.rows), i = e - j * q.rows;  // total < 2^32
-            dst[e] = (double)src[i + j * q.ld];
-        }
-    }
-}
-
-__global__ void __launch_bounds__(256) split_round_kernel(const SplitJob* __restrict__ jobs, int njobs)
-{
-    const SplitJob& q = jobs[split_job_of(jobs, njobs, blockIdx.x)];
-    const double* P = static_cast<const double*>(q.src);
-    float* c = static_cast<float*>(q.dst);
-    const int64_t total = q.rows * q.cols;
-    const int64_t e0 = ((int64_t)blockIdx.x - q.block0) * 1024 + threadIdx.x;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const int64_t e = e0 + 256 * u;
-        if (e < total) {
-            const int64_t j = (int64_t)((uint32_t)e / (uint32_t)q.rows), i = e - j * q.rows;
-            float* cij = c + i + j * q.ld;
-            const double t = (q.alpha == 0.0) ? 0.0 : q.alpha * P[e];  // alpha = 0: P is not read
-            *cij = (float)(q.beta == 0.0 ? t : fma(q.beta, (double)*cij, t));
-        }
-    }
-}
-
 }  // namespace
 
 // A resident batch: descriptor table in HBM, tile counter, optional graph.
-// The Ozaki form (GB_BATCH_FP64_OZAKI) adds the grouped Ozaki tables and
-// arenas; this plan's own table then holds the same problems for the native
-// launch gated on the Ozaki form's Inf/NaN flag, `rest` the problems with
+// The Ozaki form (GB_BATCH_FP64_OZAKI, and FP32 policy 3) adds the grouped
+// Ozaki tables and arenas; this plan's own table then holds the same problems
+// for the native launch gated on the Ozaki form's Inf/NaN flag, `rest` the problems with
 // k == 0 or alpha == 0 (C := beta C) and `singles` those with a k too long
 // for the grouped form.
 struct BatchPlan {
@@ -151,35 +90,22 @@ struct BatchPlan {
     BatchPlan* rest = nullptr;
     std::vector<gb_gemm_problem_t> singles;
     int slices = 0;
-    // policy 3 (FP32 through the split form): arenas, job tables, the inner FP64 Ozaki plan
-    double* split_arena = nullptr;
-    SplitJob* d_jobs = nullptr;  // widen jobs, then round jobs
-    int wjobs = 0, rjobs = 0;
-    int64_t wblocks = 0, rblocks = 0;
-    BatchPlan* inner = nullptr;
 };
 
 static int launch_plan(BatchPlan* pl, cudaStream_t s)
 {
     int rc;
-    if (pl->inner) {
-        if (pl->wblocks > 0) {
-            LaunchScope ls("batch_split_widen", s);
-            split_widen_kernel<<<(unsigned)pl->wblocks, 256, 0, s>>>(pl->d_jobs, pl->wjobs);
-            if ((rc = check_cuda(cudaGetLastError(), "batch split widen"))) return rc;
-        }
-        if ((rc = launch_plan(pl->inner, s))) return rc;
-        if (pl->rblocks > 0) {
-            LaunchScope ls("batch_split_round", s);
-            split_round_kernel<<<(unsigned)pl->rblocks, 256, 0, s>>>(pl->d_jobs + pl->wjobs, pl->rjobs);
-            if ((rc = check_cuda(cudaGetLastError(), "batch split round"))) return rc;
-        }
-        return GB_SUCCESS;
-    }
     if (pl->oz && (rc = ozaki_batch_launch(pl->oz, s))) return rc;
     if (pl->rest && (rc = launch_plan(pl->rest, s))) return rc;
     for (const gb_gemm_problem_t& p : pl->singles) {
         const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
+        if (pl->dtype == GB_BATCH_FP32) {  // policy 3: k past the grouped form's range
+            rc = sgemm_split_dev(p.m, p.n, p.k, (float)p.alpha, (const float*)p.a, ta ? p.lda : 1, ta ? 1 : p.lda,
+                                 (const float*)p.b, tb ? p.ldb : 1, tb ? 1 : p.ldb, (float)p.beta, (float*)p.c, 1,
+                                 p.ldc, s);
+            if (rc) return rc;
+            continue;
+        }
         rc = dgemm_ozaki(p.m, p.n, p.k, p.alpha, (const double*)p.a, ta ? p.lda : 1, ta ? 1 : p.lda,
                          (const double*)p.b, tb ? p.ldb : 1, tb ? 1 : p.ldb, p.beta, (double*)p.c, 1, p.ldc,
                          pl->slices, s);
@@ -191,14 +117,14 @@ static int launch_plan(BatchPlan* pl, cudaStream_t s)
     const int sms = sm_count() > 0 ? sm_count() : 148;
     int64_t grid = (int64_t)sms * 2;  // 2 resident CTAs of 256 threads per SM (DMMA: 240 regs)
     if (grid > pl->total_tiles) grid = pl->total_tiles;
-    LaunchScope ls(pl->dtype == 1 ? "batch_grouped_ffma" : (pl->gate ? "batch_grouped_dmma_gated"
-                                                                      : "batch_grouped_dmma"), s);
+    LaunchScope ls(pl->dtype == 1 ? (pl->gate ? "batch_grouped_ffma_gated" : "batch_grouped_ffma")
+                                  : (pl->gate ? "batch_grouped_dmma_gated" : "batch_grouped_dmma"), s);
     if (pl->dtype != 1)
         grouped_gemm_kernel<double, true><<<(unsigned)grid, NT, 0, s>>>(pl->d_desc, pl->nprob,
                                                                        pl->total_tiles, pl->d_counter, pl->gate);
     else
         grouped_gemm_kernel<float, false><<<(unsigned)grid, NT, 0, s>>>(pl->d_desc, pl->nprob,
-                                                                       pl->total_tiles, pl->d_counter, nullptr);
+                                                                       pl->total_tiles, pl->d_counter, pl->gate);
     return check_cuda(cudaGetLastError(), "grouped_gemm");
 }
 
@@ -206,100 +132,40 @@ void batch_plan_destroy(BatchPlan* pl);
 int batch_plan_run(BatchPlan* pl, cudaStream_t s, bool use_graph);
 static int batch_plan_build(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out);
 
-int batch_plan_create(const gb_gemm_problem_t* probs, int64_t count, int dtype, BatchPlan** out, bool tune);
-
-// Policy 3, FP32 only: the split form (see SplitJob).
+// Policy 3, FP32 only: SGEMM's split form for the whole batch, the grouped
+// Ozaki form on the FP32 operands themselves at GB_SGEMM_SPLIT_SLICES
+// (every element widened exactly as it is split, C = RN32(alpha P + beta C)
+// in the recombination), bit-identical per problem to the single-problem
+// split form.  Problems with k = 0 or alpha = 0 (C := beta C) take the FP32
+// grouped launch; a k past the grouped form's range runs alone through the
+// single-problem split form; Inf/NaN in any operand raises the grouped
+// form's flag, and the FP32 grouped launch gated on it recomputes every
+// grouped problem.
 static int batch_plan_split(const gb_gemm_problem_t* probs, int64_t count, BatchPlan** out)
 {
     *out = nullptr;
-    std::vector<gb_gemm_problem_t> p64;
-    std::vector<SplitJob> widen, round;
-    int64_t elems = 0;
+    const int slices = GB_SGEMM_SPLIT_SLICES;
+    std::vector<gb_gemm_problem_t> grouped, rest, singles;
     for (int64_t i = 0; i < count; ++i) {
         const gb_gemm_problem_t& p = probs[i];
         if (p.m < 0 || p.n < 0 || p.k < 0) return set_error(GB_ERR_ARG, "gb_batch", "negative dimension");
         if (p.m == 0 || p.n == 0) continue;
-        const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
-        const int64_t ar = ta ? p.k : p.m, ac = ta ? p.m : p.k, br = tb ? p.n : p.k, bc = tb ? p.k : p.n;
-        if (ar * ac >= 0xFFFFFFFFll || br * bc >= 0xFFFFFFFFll || p.m * p.n >= 0xFFFFFFFFll)
-            return set_error(GB_ERR_UNSUPPORTED, "gb_batch", "a problem too large for the split plan");
-        elems += ar * ac + br * bc + p.m * p.n;
+        if (p.k == 0 || p.alpha == 0.0) rest.push_back(p);
+        else if (ozaki_batch_accepts(p.k, slices)) grouped.push_back(p);
+        else singles.push_back(p);
     }
-    BatchPlan* pl = new BatchPlan();
-    pl->dtype = GB_BATCH_FP32;
-    pl->nprob = 0;
-    pl->total_tiles = 0;
-    pl->d_desc = nullptr;
-    pl->d_counter = nullptr;
-    pl->graph = nullptr;
-    pl->graph_stream = nullptr;
+    BatchPlan* pl = nullptr;
+    int rc = batch_plan_build(grouped.data(), (int64_t)grouped.size(), GB_BATCH_FP32, &pl);
+    if (rc) return rc;
+    pl->slices = slices;
+    pl->singles = singles;
     cudaStream_t s = thread_stream();
-    pl->split_arena = static_cast<double*>(dev_alloc(sizeof(double) * (size_t)(elems + 1), s));
-    if (!pl->split_arena) {
-        delete pl;
-        return GB_ERR_NOMEM;
-    }
-    int64_t off = 0;
-    for (int64_t i = 0; i < count; ++i) {
-        const gb_gemm_problem_t& p = probs[i];
-        if (p.m == 0 || p.n == 0) continue;
-        const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
-        const int64_t ar = ta ? p.k : p.m, ac = ta ? p.m : p.k, br = tb ? p.n : p.k, bc = tb ? p.k : p.n;
-        double* a64 = pl->split_arena + off;
-        off += ar * ac;
-        double* b64 = pl->split_arena + off;
-        off += br * bc;
-        double* c64 = pl->split_arena + off;
-        off += p.m * p.n;
-        if (ar * ac > 0) widen.push_back(SplitJob{p.a, a64, ar, ac, p.lda, 0.0, 0.0, 0});
-        if (br * bc > 0) widen.push_back(SplitJob{p.b, b64, br, bc, p.ldb, 0.0, 0.0, 0});
-        gb_gemm_problem_t q = p;
-        q.a = a64;
-        q.lda = ar > 0 ? ar : 1;
-        q.b = b64;
-        q.ldb = br > 0 ? br : 1;
-        q.c = c64;
-        q.ldc = p.m;
-        q.alpha = (p.alpha == 0.0) ? 0.0 : 1.0;  // P = op(A) op(B), or 0
-        q.beta = 0.0;
-        p64.push_back(q);
-        round.push_back(SplitJob{c64, p.c, p.m, p.n, p.ldc, p.alpha, p.beta, 0});
-    }
-    auto number = [](std::vector<SplitJob>& v) {
-        int64_t b = 0;
-        for (auto& j : v) {
-            j.block0 = b;
-            b += (j.rows * j.cols + 1023) / 1024;
-        }
-        return b;
-    };
-    pl->wblocks = number(widen);
-    pl->rblocks = number(round);
-    pl->wjobs = (int)widen.size();
-    pl->rjobs = (int)round.size();
-    int rc = GB_SUCCESS;
-    if (pl->wblocks > INT32_MAX || pl->rblocks > INT32_MAX)
-        rc = set_error(GB_ERR_UNSUPPORTED, "gb_batch", "batch too large for the split plan");
-    if (!rc) {
-        std::vector<SplitJob> all(widen);
-        all.insert(all.end(), round.begin(), round.end());
-        pl->d_jobs = static_cast<SplitJob*>(dev_alloc(sizeof(SplitJob) * (all.size() + 1), s));
-        if (!pl->d_jobs) rc = GB_ERR_NOMEM;
-        if (!rc && !all.empty())
-            rc = check_cuda(cudaMemcpyAsync(pl->d_jobs, all.data(), sizeof(SplitJob) * all.size(),
-                                            cudaMemcpyHostToDevice, s),
-                            "batch split jobs");
-        if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "batch split jobs");
-    }
-    if (!rc) {
-        // the FP64 products: the grouped Ozaki plan in the digit form at the split form's slices
-        ModeOverride digits(GB_DGEMM_OZAKI, GB_SGEMM_SPLIT_SLICES, 0);
-        rc = batch_plan_create(p64.data(), (int64_t)p64.size(), GB_BATCH_FP64_OZAKI, &pl->inner, false);
-    }
-    if (rc) {
+    if ((rc = ozaki_batch_create(grouped.data(), (int64_t)grouped.size(), slices, s, &pl->oz, true)) ||
+        (!rest.empty() && (rc = batch_plan_build(rest.data(), (int64_t)rest.size(), GB_BATCH_FP32, &pl->rest)))) {
         batch_plan_destroy(pl);
         return rc;
     }
+    pl->gate = ozaki_batch_flag(pl->oz);
     pl->policy = 3;
     *out = pl;
     return GB_SUCCESS;
@@ -502,7 +368,7 @@ static int batch_plan_build(const gb_gemm_problem_t* probs, int64_t count, int d
 int batch_plan_run(BatchPlan* pl, cudaStream_t s, bool use_graph)
 {
     // problems run one by one through the Ozaki form allocate workspace per call: no graph
-    if (!use_graph || !pl->singles.empty() || (pl->inner && !pl->inner->singles.empty())) return launch_plan(pl, s);
+    if (!use_graph || !pl->singles.empty()) return launch_plan(pl, s);
     if (!pl->graph) {
         cudaStream_t cap;
         GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -534,11 +400,8 @@ void batch_plan_destroy(BatchPlan* pl)
     dev_free(pl->d_counter, s);
     ozaki_batch_destroy(pl->oz, s);
     sup_group_destroy(pl->sup, s);
-    dev_free(pl->split_arena, s);
-    dev_free(pl->d_jobs, s);
     cudaStreamSynchronize(s);
     batch_plan_destroy(pl->rest);
-    batch_plan_destroy(pl->inner);
     delete pl;
 }
 

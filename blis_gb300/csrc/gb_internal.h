@@ -215,10 +215,12 @@ int bgemm_tc(int64_t m, int64_t n, int64_t k, float alpha, const uint16_t* a, in
 // (m, n, k > 0, alpha != 0, ozaki_batch_accepts) in three launches.  The
 // flag is raised when an operand holds Inf/NaN; the launches then do
 // nothing and a native grouped launch gated on the flag must follow.
+// f32: FP32 operands and C (SGEMM's split form at GB_SGEMM_SPLIT_SLICES),
+// each element widened exactly as it is split, C rounded once.
 struct OzBatch;
 bool ozaki_batch_accepts(int64_t k, int slices);
 int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices, cudaStream_t s,
-                       OzBatch** out);
+                       OzBatch** out, bool f32 = false);
 int ozaki_batch_launch(OzBatch* ob, cudaStream_t s);
 const int* ozaki_batch_flag(const OzBatch* ob);
 void ozaki_batch_destroy(OzBatch* ob, cudaStream_t s);

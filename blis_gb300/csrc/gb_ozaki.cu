@@ -35,6 +35,7 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "gb_internal.h"
@@ -111,11 +112,11 @@ struct OzItem {
 // C's own orientation, so the recombination reads and writes as for any
 // other problem.  The digit products are the same either way: bit-identical.
 struct OzBatchProb {
-    const double* a;
+    const void* a;     // FP64, or FP32 in the SGEMM form of the batch (OzBatch::f32)
     int64_t ars, acs;  // rows of op(A): (i, l) at a[i*ars + l*acs]
-    const double* b;
+    const void* b;
     int64_t brs, bcs;  // rows of op(B)^T: (j, l) at b[j*brs + l*bcs]
-    double* c;
+    void* c;
     int64_t rs_c, cs_c;
     double alpha, beta;
     int64_t m, n, k;
@@ -1304,8 +1305,28 @@ __global__ void __launch_bounds__(256, (S <= 7 ? 3 : 2)) oz_recombine_kernel(con
 // registers while one is cut, and hands each thread's 8 bf16 digits of a
 // slice to store(p, kb, rr, c0, v) (slice p, k block kb, tile row rr,
 // columns c0 .. c0 + 7).  Rows past `rows` and k past `k` give zero digits.
-template <int S, typename Store>
-__device__ __forceinline__ void oz_split_unit(const double* __restrict__ R, int64_t rows, int64_t sr, int64_t sl,
+// T is double, or float for FP32 operands (each element widened exactly on
+// load; the row maxima compare the FP32 bits, and only the maximum is
+// widened to the FP64 bits oz_row_exponent reads).
+template <typename T>
+using OzKey = std::conditional_t<sizeof(T) == 4, uint32_t, unsigned long long>;
+
+template <typename T>
+__device__ __forceinline__ OzKey<T> oz_abs_key(T x)
+{
+    if constexpr (sizeof(T) == 4) return __float_as_uint(x) & 0x7fffffffu;
+    else return abs_bits(x);
+}
+
+template <typename T>
+__device__ __forceinline__ unsigned long long oz_key_f64(unsigned long long key)
+{
+    if constexpr (sizeof(T) == 4) return (unsigned long long)__double_as_longlong((double)__uint_as_float((uint32_t)key));
+    else return key;
+}
+
+template <int S, typename T, typename Store>
+__device__ __forceinline__ void oz_split_unit(const T* __restrict__ R, int64_t rows, int64_t sr, int64_t sl,
                                               int64_t k, int nkb, int64_t r0, int32_t* __restrict__ exps,
                                               int* __restrict__ nonfinite, Store store)
 {
@@ -1320,13 +1341,13 @@ __device__ __forceinline__ void oz_split_unit(const double* __restrict__ R, int6
         const int rr = rows_fast ? (t & 31) : (t >> 3);
         const int l0 = rows_fast ? (t >> 5) : (t & 7);
         const int64_t r = r0 + rr;
-        unsigned long long mx = 0, my = 0;
+        OzKey<T> mx = 0, my = 0;
         if (r < rows) {
             int64_t l = l0;
             for (; l + 8 * 7 < k; l += 8 * 8) {  // eight loads in flight per thread
-                unsigned long long b[8];
+                OzKey<T> b[8];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) b[u] = abs_bits(__ldg(R + r * sr + (l + 8 * u) * sl));
+                for (int u = 0; u < 8; ++u) b[u] = oz_abs_key(__ldg(R + r * sr + (l + 8 * u) * sl));
 #pragma unroll
                 for (int u = 0; u < 8; u += 2) {
                     mx = b[u] > mx ? b[u] : mx;
@@ -1334,7 +1355,7 @@ __device__ __forceinline__ void oz_split_unit(const double* __restrict__ R, int6
                 }
             }
             for (; l < k; l += 8) {
-                const unsigned long long b = abs_bits(__ldg(R + r * sr + l * sl));
+                const OzKey<T> b = oz_abs_key(__ldg(R + r * sr + l * sl));
                 mx = b > mx ? b : mx;
             }
         }
@@ -1349,7 +1370,7 @@ __device__ __forceinline__ void oz_split_unit(const double* __restrict__ R, int6
         const int64_t r = r0 + t;
         if (r < rows) {
             int nf = 0;
-            e = oz_row_exponent(mx, &nf);
+            e = oz_row_exponent(oz_key_f64<T>(mx), &nf);
             if (nf) *nonfinite = 1;
             exps[r] = e;
         }
@@ -1361,7 +1382,7 @@ __device__ __forceinline__ void oz_split_unit(const double* __restrict__ R, int6
     const int rr = t >> 3, c0 = (t & 7) * 8;
     const int e = rowe[rr];
     const bool live = (r0 + rr < rows);
-    double nxt[8];
+    T nxt[8];
     auto fetch = [&](int kb) {
         const int64_t l0 = (int64_t)kb * 64;
 #pragma unroll
@@ -1370,7 +1391,7 @@ __device__ __forceinline__ void oz_split_unit(const double* __restrict__ R, int6
             const int tr = rows_fast ? (idx & 31) : (idx >> 6);
             const int tl = rows_fast ? (idx >> 5) : (idx & 63);
             const int64_t r = r0 + tr, l = l0 + tl;
-            nxt[g] = (r < rows && l < k) ? __ldg(R + r * sr + l * sl) : 0.0;
+            nxt[g] = (r < rows && l < k) ? __ldg(R + r * sr + l * sl) : T(0);
         }
     };
     fetch(0);
@@ -1443,8 +1464,8 @@ __global__ void __launch_bounds__(256, 2) oz_split_two_kernel(OzSplitOperand a, 
 // run; their rows past m (n) and k past k_i up to the block width are
 // written as zeros, and the remaining padding rows of a box stay as the
 // plan's one-time zero fill left them.
-template <int S>
-__global__ void __launch_bounds__(256, 2) oz_split_batch_kernel(const OzBatchProb* __restrict__ probs,
+template <int S, typename T>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4) ? 4 : 2) oz_split_batch_kernel(const OzBatchProb* __restrict__ probs,
                                                              const int32_t* __restrict__ unit_prob,
                                                              const int64_t* __restrict__ unit_base,
                                                              int64_t boxes_a, int64_t boxes_b,
@@ -1462,7 +1483,7 @@ __global__ void __launch_bounds__(256, 2) oz_split_batch_kernel(const OzBatchPro
     const int64_t boxes = isb ? boxes_b : boxes_a;
     const int64_t box0 = (isb ? q.bbox : q.abox) + (r0 / box_rows) * q.kb;
     const int64_t rb = (r0 % box_rows);
-    oz_split_unit<S>(isb ? q.b : q.a, isb ? q.n : q.m, isb ? q.brs : q.ars, isb ? q.bcs : q.acs, q.k, q.kb, r0,
+    oz_split_unit<S>(static_cast<const T*>(isb ? q.b : q.a), isb ? q.n : q.m, isb ? q.brs : q.ars, isb ? q.bcs : q.acs, q.k, q.kb, r0,
                      isb ? q.eb : q.ea, nonfinite, [&](int p, int kb, int rr, int c0, uint4 v) {
                          const int64_t z = (int64_t)p * boxes + box0 + kb;
                          *reinterpret_cast<uint4*>(out + (z * box_rows + rb + rr) * 64 + c0) = v;
@@ -1471,7 +1492,9 @@ __global__ void __launch_bounds__(256, 2) oz_split_batch_kernel(const OzBatchPro
 
 // Recombination for every problem of a batch in one launch: blocks are
 // assigned to problems by a table, each thread takes 4 rows of one column.
-template <int S>
+// CT is C's type: for FP32, C = RN32(alpha P + beta C) from the FP64 product
+// P, as the single-problem SGEMM split form rounds it.
+template <int S, typename CT>
 __global__ void __launch_bounds__(256) oz_recombine_batch_kernel(const OzBatchProb* __restrict__ probs,
                                                                  const int32_t* __restrict__ block_prob,
                                                                  const int64_t* __restrict__ block_base,
@@ -1504,12 +1527,12 @@ __global__ void __launch_bounds__(256) oz_recombine_batch_kernel(const OzBatchPr
         for (int L = 0; L < S; ++L) a[L] = (r == 0) ? v[L].x : (r == 1) ? v[L].y : (r == 2) ? v[L].z : v[L].w;
         const __int128 T = oz_weighted_sum<S>(a);
         const double ab = round_scaled(T, ea[i] + ebj);
-        double* cij = q.c + i * q.rs_c + j * q.cs_c;
+        CT* cij = static_cast<CT*>(q.c) + i * q.rs_c + j * q.cs_c;
         if (plain) {
-            *cij = ab;
+            *cij = (CT)ab;
         } else {
             const double tt = __dmul_rn(q.alpha, ab);
-            *cij = (q.beta == 0.0) ? tt : __fma_rn(q.beta, *cij, tt);
+            *cij = (CT)((q.beta == 0.0) ? tt : __fma_rn(q.beta, (double)*cij, tt));
         }
     }
 }
@@ -2654,6 +2677,7 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
 // a plan can replay the launches (or a graph of them).
 struct OzBatch {
     int slices = 0;
+    bool f32 = false;  // FP32 operands and C (the batch's SGEMM form, GB_SGEMM_SPLIT_SLICES only)
     int nprob = 0;
     int64_t items = 0, units = 0, rblocks = 0, boxes_a = 0, boxes_b = 0;
     uint8_t* arena = nullptr;  // slices, planes, exponents, tables, flag
@@ -2693,15 +2717,30 @@ int make_box_map(CUtensorMap* map, const void* base, int box_rows, int64_t nboxe
 template <int S>
 void launch_split_batch(const OzBatch& ob, cudaStream_t s)
 {
-    oz_split_batch_kernel<S><<<(unsigned)ob.units, 256, 0, s>>>(ob.d_probs, ob.d_unit_prob, ob.d_unit_base,
-                                                                 ob.boxes_a, ob.boxes_b, ob.sa, ob.sb, ob.d_flag);
+    if constexpr (S == GB_SGEMM_SPLIT_SLICES) {
+        if (ob.f32) {
+            oz_split_batch_kernel<S, float><<<(unsigned)ob.units, 256, 0, s>>>(
+                ob.d_probs, ob.d_unit_prob, ob.d_unit_base, ob.boxes_a, ob.boxes_b, ob.sa, ob.sb, ob.d_flag);
+            return;
+        }
+    }
+    oz_split_batch_kernel<S, double><<<(unsigned)ob.units, 256, 0, s>>>(ob.d_probs, ob.d_unit_prob, ob.d_unit_base,
+                                                                         ob.boxes_a, ob.boxes_b, ob.sa, ob.sb,
+                                                                         ob.d_flag);
 }
 
 template <int S>
 void launch_recombine_batch(const OzBatch& ob, cudaStream_t s)
 {
-    oz_recombine_batch_kernel<S><<<(unsigned)ob.rblocks, 256, 0, s>>>(ob.d_probs, ob.d_rblock_prob,
-                                                                       ob.d_rblock_base, ob.d_flag);
+    if constexpr (S == GB_SGEMM_SPLIT_SLICES) {
+        if (ob.f32) {
+            oz_recombine_batch_kernel<S, float><<<(unsigned)ob.rblocks, 256, 0, s>>>(ob.d_probs, ob.d_rblock_prob,
+                                                                                     ob.d_rblock_base, ob.d_flag);
+            return;
+        }
+    }
+    oz_recombine_batch_kernel<S, double><<<(unsigned)ob.rblocks, 256, 0, s>>>(ob.d_probs, ob.d_rblock_prob,
+                                                                               ob.d_rblock_base, ob.d_flag);
 }
 
 }  // namespace
@@ -2715,11 +2754,13 @@ bool ozaki_batch_accepts(int64_t k, int slices)
 }
 
 int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices, cudaStream_t s,
-                       OzBatch** out)
+                       OzBatch** out, bool f32)
 {
     *out = nullptr;
     if (slices < 2 || slices > OZ_MAX_SLICES)
         return set_error(GB_ERR_ARG, "ozaki batch", "slices must be in [2, 12]");
+    if (f32 && slices != GB_SGEMM_SPLIT_SLICES)
+        return set_error(GB_ERR_ARG, "ozaki batch", "the FP32 form runs at the SGEMM split form's slice count");
     std::vector<OzBatchProb> h;
     h.reserve((size_t)count);
     for (int64_t i = 0; i < count; ++i) {
@@ -2728,9 +2769,9 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
             return set_error(GB_ERR_ARG, "ozaki batch", "problem not eligible for the grouped form");
         const bool ta = GB_IS_TRANS(p.transa), tb = GB_IS_TRANS(p.transb);
         OzBatchProb q = {};
-        const double* pa = static_cast<const double*>(p.a);
+        const void* pa = p.a;
         const int64_t ars = ta ? p.lda : 1, acs = ta ? 1 : p.lda;
-        const double* pb = static_cast<const double*>(p.b);
+        const void* pb = p.b;
         const int64_t brs = tb ? 1 : p.ldb, bcs = tb ? p.ldb : 1;  // rows of op(B)^T are columns of op(B)
         // tiles covered as C and as C^T; the transposed form when it needs fewer
         const int64_t cover = ((p.m + OZ_BM - 1) / OZ_BM) * ((p.n + OZ_BN - 1) / OZ_BN);
@@ -2742,7 +2783,7 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
         q.b = q.swap ? pa : pb;
         q.brs = q.swap ? ars : brs;
         q.bcs = q.swap ? acs : bcs;
-        q.c = static_cast<double*>(p.c);
+        q.c = p.c;
         q.rs_c = 1;
         q.cs_c = p.ldc;
         q.alpha = p.alpha;
@@ -2762,6 +2803,7 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
 
     OzBatch* ob = new OzBatch();
     ob->slices = slices;
+    ob->f32 = f32;
     ob->nprob = (int)h.size();
     OzBatchParams& gp = ob->gp;
     gp.slices = slices;
