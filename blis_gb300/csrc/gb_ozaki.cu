@@ -97,8 +97,7 @@ struct OzGemmParams {
 
 struct OzItem {
     int lev, npairs, pa_lo, tm, tn, kb0, kbn, plane;
-    int prob;       // grouped form only: index into the problem table
-    int bn = OZ_BN;  // the tile's width (MMA N): 64 or 128 for narrow problems of the grouped form
+    int prob;  // grouped form only: index into the problem table
 };
 
 // Grouped form (gemm_batch): every problem's slices live in one arena of
@@ -122,7 +121,6 @@ struct OzBatchProb {
     double alpha, beta;
     int64_t m, n, k;
     int32_t tiles_m, tiles_n, kb, swap;
-    int32_t bn, bn_unused;  // tile width: 256, or 64 / 128 when n fits (boxes keep 256-row strides)
     int32_t* ea;  // row exponents of op(A), op(B)^T
     int32_t* eb;
     int64_t abox, bbox;  // first box of this problem in one slice plane
@@ -139,7 +137,6 @@ struct OzBatchProb {
 struct OzBatchParams {
     static constexpr bool kDynamic = true;
     static constexpr bool kRawAcc = false;
-    CUtensorMap map_b64;  // B boxes in 64-row pieces, for tiles narrower than 256
     int slices, nlevels, chunk_kb, nprob;
     int64_t items, boxes_a, boxes_b;  // work items; boxes per slice plane
     const OzBatchProb* probs;
@@ -301,7 +298,6 @@ __device__ __forceinline__ OzItem oz_decode(const OzBatchParams& p, int64_t it)
     w.kbn = q.kb;
     w.plane = L;
     w.prob = pi;
-    w.bn = q.bn;
     return w;
 }
 
@@ -323,13 +319,7 @@ __device__ __forceinline__ void oz_load_stage(const OzBatchParams& p, const CUte
     const int64_t za = (int64_t)(pa - 1) * p.boxes_a + q.abox + (int64_t)w.tm * q.kb + kb;
     const int64_t zb = (int64_t)(pb - 1) * p.boxes_b + q.bbox + (int64_t)w.tn * q.kb + kb;
     tma_load_3d(sa, ma, bar, 0, 0, (int)za);
-    if (w.bn == OZ_BN) {
-        tma_load_3d(sb, mb, bar, 0, 0, (int)zb);
-    } else {
-        // the first bn rows of the box in 64-row pieces: 8 KB each, stacked in the
-        // 128-byte-swizzled layout one 256-row box would have
-        for (int y = 0; y < w.bn; y += 64) tma_load_3d(sb + y * OZ_BK * 2, &p.map_b64, bar, 0, y, (int)zb);
-    }
+    tma_load_3d(sb, mb, bar, 0, 0, (int)zb);
 }
 
 // A CRT product sum v reduced to its symmetric residue modulo the plane's
@@ -387,10 +377,9 @@ __device__ __forceinline__ void oz_store_sums(const OzBatchParams& p, const OzIt
 {
     const OzBatchProb& q = p.probs[w.prob];
     const int64_t i = (int64_t)w.tm * OZ_BM + quad * 32 + lane;
-    const int64_t j0 = (int64_t)w.tn * w.bn + half * 128;
-    if (i >= q.m || half * 128 >= w.bn) return;
-    int64_t jn = q.n - j0;  // columns of this half that exist (and lie in the tile)
-    if (jn > w.bn - half * 128) jn = w.bn - half * 128;
+    const int64_t j0 = (int64_t)w.tn * OZ_BN + half * 128;
+    if (i >= q.m) return;
+    const int64_t jn = q.n - j0;  // columns of this half that exist
     if (!q.swap) {
         int32_t* dst = q.planes + ((int64_t)w.plane * q.n + j0) * q.ld + i;
 #pragma unroll
@@ -400,15 +389,14 @@ __device__ __forceinline__ void oz_store_sums(const OzBatchParams& p, const OzIt
         // row i of the product is column i of C: the thread's 128 sums are contiguous in the
         // plane (j0 and ld are multiples of 4, so 16-byte stores)
         int32_t* dst = q.planes + ((int64_t)w.plane * q.m + i) * q.ld + j0;
+        if (jn >= 128) {
 #pragma unroll
-        for (int c = 0; c < 128; c += 4) {
-            if (c + 4 <= jn) {
+            for (int c = 0; c < 128; c += 4)
                 *reinterpret_cast<int4*>(dst + c) = make_int4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
-            } else {
+        } else {
 #pragma unroll
-                for (int r = 0; r < 4; ++r)
-                    if (c + r < jn) dst[c + r] = acc[c + r];
-            }
+            for (int c = 0; c < 128; ++c)
+                if (c < jn) dst[c] = acc[c];
         }
     }
 }
@@ -564,7 +552,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                         }
                         uint8_t* sa = smem + stage * OZ_STAGE_BYTES;
                         uint8_t* sb = sa + OZ_A_BYTES;
-                        mbar_arrive_expect_tx(&full[stage], OZ_A_BYTES + w.bn * OZ_BK * 2);
+                        mbar_arrive_expect_tx(&full[stage], OZ_STAGE_BYTES);
                         oz_load_stage(p, &map_a, &map_b, sa, sb, &full[stage], w, pa, pb, kb);
                         issued_mask |= 1u << stage;
                         last_phase = (last_phase & ~(1u << stage)) | (phase << stage);
@@ -584,6 +572,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         }
     } else if (warp == OZ_MMA_WARP) {
         if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16_f32(OZ_BM, OZ_BN);
             int stage = 0;
             uint32_t phase = 0;
             uint32_t chunk_ctr = 0;
@@ -597,9 +586,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 }
                 if (it < 0) break;
                 const OzItem w = oz_decode(p, it);
-                const uint32_t idesc = (w.bn == 64)    ? idesc_bf16_f32(OZ_BM, 64)
-                                       : (w.bn == 128) ? idesc_bf16_f32(OZ_BM, 128)
-                                                       : idesc_bf16_f32(OZ_BM, OZ_BN);
                 const int total = w.npairs * w.kbn;
                 for (int t0 = 0; t0 < total && ok; t0 += p.chunk_kb) {
                     const int nkb = (total - t0 < p.chunk_kb) ? total - t0 : p.chunk_kb;
@@ -685,7 +671,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 const uint32_t taddr = tmem_base + ((uint32_t)(quad * 32) << 16) + buf * OZ_BN + half * 128;
 #pragma unroll
                 for (int g = 0; g < 4; ++g) {
-                    if (half * 128 + g * 32 >= w.bn) break;  // past a narrow tile: nothing accumulated
                     uint32_t r[32];
                     tmem_ld_32x32b_x32(taddr + g * 32, r);
                     tmem_ld_wait();
@@ -1492,13 +1477,12 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4) ? 4 : 2) oz_split_batch_
     int64_t u = (int64_t)blockIdx.x - unit_base[pi];
     const bool isb = (u >= q.units_a);
     if (isb) u -= q.units_a;
-    const int box_rows = isb ? OZ_BN : OZ_BM;    // the arena's row stride of a box
-    const int tile_rows = isb ? q.bn : OZ_BM;    // rows of a box that hold this problem's rows
+    const int box_rows = isb ? OZ_BN : OZ_BM;
     const int64_t r0 = u * 32;
     uint16_t* out = isb ? sb : sa;
     const int64_t boxes = isb ? boxes_b : boxes_a;
-    const int64_t box0 = (isb ? q.bbox : q.abox) + (r0 / tile_rows) * q.kb;
-    const int64_t rb = (r0 % tile_rows);
+    const int64_t box0 = (isb ? q.bbox : q.abox) + (r0 / box_rows) * q.kb;
+    const int64_t rb = (r0 % box_rows);
     oz_split_unit<S>(static_cast<const T*>(isb ? q.b : q.a), isb ? q.n : q.m, isb ? q.brs : q.ars, isb ? q.bcs : q.acs, q.k, q.kb, r0,
                      isb ? q.eb : q.ea, nonfinite, [&](int p, int kb, int rr, int c0, uint4 v) {
                          const int64_t z = (int64_t)p * boxes + box0 + kb;
@@ -1939,24 +1923,6 @@ int ozaki_batch_orient_setting()
         v = e ? (atoi(e) != 0) : 1;
     }
     return v;
-}
-
-// Tile width of a grouped-form product with n columns: the narrowest of 64,
-// 128 and 256 that holds n (GB_OZAKI_BATCH_NARROW=0: always 256).  A narrow
-// tile loads and multiplies only its own columns of B instead of zero
-// padding.  The grouped slice GEMM is bound by the bytes its tiles pull
-// through L2 (about 12 TB/s on the 4096-problem batch of m, n, k in
-// [16, 1024]), and there the large problems, whose tiles are full, move most
-// of them: narrow tiles cut 3% of the bytes and 1% of the time.
-int ozaki_batch_tile_n(int64_t n)
-{
-    static int narrow = -1;
-    if (narrow < 0) {
-        const char* e = getenv("GB_OZAKI_BATCH_NARROW");
-        narrow = e ? (atoi(e) != 0) : 1;
-    }
-    if (!narrow) return OZ_BN;
-    return n <= 64 ? 64 : (n <= 128 ? 128 : OZ_BN);
 }
 
 int chunk_kb_setting()
@@ -2732,15 +2698,14 @@ struct OzBatch {
 
 namespace {
 
-int make_box_map(CUtensorMap* map, const void* base, int box_rows, int64_t nboxes, int load_rows = 0)
+int make_box_map(CUtensorMap* map, const void* base, int box_rows, int64_t nboxes)
 {
-    if (load_rows <= 0) load_rows = box_rows;  // rows one load copies (a piece of a box)
     auto fn = encode_fn();
     if (!fn) return set_error(GB_ERR_CUDA, "ozaki", "cuTensorMapEncodeTiled unavailable");
     if (nboxes > INT32_MAX) return set_error(GB_ERR_ARG, "ozaki batch", "too many k blocks for TMA coordinates");
     cuuint64_t dims[3] = {(cuuint64_t)OZ_BK, (cuuint64_t)box_rows, (cuuint64_t)nboxes};
     cuuint64_t strides[2] = {(cuuint64_t)(OZ_BK * 2), (cuuint64_t)box_rows * OZ_BK * 2};
-    cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)load_rows, 1};
+    cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -2808,9 +2773,7 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
         const int64_t ars = ta ? p.lda : 1, acs = ta ? 1 : p.lda;
         const void* pb = p.b;
         const int64_t brs = tb ? 1 : p.ldb, bcs = tb ? p.ldb : 1;  // rows of op(B)^T are columns of op(B)
-        // 128 x 256 tiles covered as C and as C^T; the transposed form when it needs fewer
-        // (counting each form's narrow tiles by their bytes instead chose more, smaller items
-        // and ran 8% slower on the 4096-problem batch)
+        // tiles covered as C and as C^T; the transposed form when it needs fewer
         const int64_t cover = ((p.m + OZ_BM - 1) / OZ_BM) * ((p.n + OZ_BN - 1) / OZ_BN);
         const int64_t cover_t = ((p.n + OZ_BM - 1) / OZ_BM) * ((p.m + OZ_BN - 1) / OZ_BN);
         q.swap = (cover_t < cover && ozaki_batch_orient_setting()) ? 1 : 0;
@@ -2829,9 +2792,8 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
         q.n = q.swap ? p.m : p.n;
         q.k = p.k;
         q.kb = (int32_t)((p.k + OZ_BK - 1) / OZ_BK);
-        q.bn = ozaki_batch_tile_n(q.n);
         q.tiles_m = (int32_t)((q.m + OZ_BM - 1) / OZ_BM);
-        q.tiles_n = (int32_t)((q.n + q.bn - 1) / q.bn);
+        q.tiles_n = (int32_t)((q.n + OZ_BN - 1) / OZ_BN);
         q.units_a = (q.m + 31) / 32;  // 32-row blocks holding rows of op(A); the padding is zeroed once
         q.ld = round_up(p.m, 4);      // rows of C
         h.push_back(q);
@@ -2942,8 +2904,6 @@ int ozaki_batch_create(const gb_gemm_problem_t* probs, int64_t count, int slices
     if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "batch tables");  // host vectors go out of scope
     if (!rc && ob->nprob > 0) rc = make_box_map(&ob->map_a, ob->sa, OZ_BM, (int64_t)slices * ob->boxes_a);
     if (!rc && ob->nprob > 0) rc = make_box_map(&ob->map_b, ob->sb, OZ_BN, (int64_t)slices * ob->boxes_b);
-    if (!rc && ob->nprob > 0)
-        rc = make_box_map(&ob->gp.map_b64, ob->sb, OZ_BN, (int64_t)slices * ob->boxes_b, 64);
     if (!rc && ob->nprob > 0) {
         static bool attr = false;
         if (!attr) {

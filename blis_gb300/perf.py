@@ -128,8 +128,21 @@ def run_sgemm(out):
         blas.set_sgemm_mode(mode)
         ms = _timer(lambda: dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc), reps=3)
         err = ((fc[ii, jj].double() - hi - lo).abs() / gauge).max().item() / u32
-        out.append({"workload": "sgemm_%d" % n, "form": name, "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9,
-                    "max_err_in_u32_gauge": err})
+        rec = {"workload": "sgemm_%d" % n, "form": name, "ms": ms, "tflops": 2 * n ** 3 / ms / 1e9,
+               "max_err_in_u32_gauge": err}
+        if mode == blas.SGEMM_SPLIT:
+            # device time of each stage (the library's own events), mean of three calls
+            dev.set_kernel_timing(True)
+            dev.kernel_trace()
+            for _ in range(3):
+                dev.sgemm(0, 0, 1.0, fa, fb, 0.0, fc)
+            dev.synchronize()
+            stages = {}
+            for nm, t0, t1 in dev.kernel_trace():
+                stages[nm] = stages.get(nm, 0.0) + (t1 - t0) / 3
+            dev.set_kernel_timing(False)
+            rec["stage_ms"] = {k: round(v, 4) for k, v in stages.items()}
+        out.append(rec)
     blas.set_sgemm_mode(blas.SGEMM_AUTO)
 
 
