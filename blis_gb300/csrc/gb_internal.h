@@ -35,7 +35,7 @@ int check_cuda(cudaError_t e, const char* where);
 // blocks cached.
 cudaStream_t thread_stream();
 cudaStream_t thread_copy_stream(int i);  // i = 0, 1: copy streams of the calling thread
-cudaStream_t thread_aux_stream(int i = 0);  // i = 0, 1: more compute streams of the calling thread
+cudaStream_t thread_aux_stream(int i = 0);  // i = 0, 1, 2: more compute streams of the calling thread
 int ensure_init();
 int sm_count();
 

@@ -120,19 +120,20 @@ cudaStream_t thread_copy_stream(int i)
     return t_copy[i & 1];
 }
 
-// Two more compute streams per calling thread (work that forks from the
+// Three more compute streams per calling thread (work that forks from the
 // thread's stream and joins it again within one call).
-thread_local cudaStream_t t_aux[2] = {nullptr, nullptr};
+thread_local cudaStream_t t_aux[3] = {nullptr, nullptr, nullptr};
 thread_local int t_aux_dev = -1;
 
 cudaStream_t thread_aux_stream(int i)
 {
     if (t_aux_dev != g_device) {
-        t_aux[0] = t_aux[1] = nullptr;
+        t_aux[0] = t_aux[1] = t_aux[2] = nullptr;
         t_aux_dev = g_device;
     }
-    if (t_aux[i & 1] == nullptr) cudaStreamCreateWithFlags(&t_aux[i & 1], cudaStreamNonBlocking);
-    return t_aux[i & 1];
+    i = (i < 0 || i > 2) ? 0 : i;
+    if (t_aux[i] == nullptr) cudaStreamCreateWithFlags(&t_aux[i], cudaStreamNonBlocking);
+    return t_aux[i];
 }
 
 void* dev_alloc(size_t bytes, cudaStream_t s)

@@ -679,27 +679,35 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
             cudaGetLastError();  // without images each fused update splits its A block itself
     }
     // the precision form's many small launches (split, slice GEMM, recombination
-    // per update) and the FP64-pipe diagonal solves of two column halves overlap
-    // on two streams, forked and joined by two events; if either event cannot be
-    // created the solve runs on one stream
-    cudaEvent_t ev[2] = {nullptr, nullptr};
-    const char* gs = getenv("GB_TRSM_STREAMS");  // 1: the column halves stay on one stream
-    const bool two = !rc && slices > 0 && nn >= 2 * TRSM_SPLIT_MIN_COLS && mm > 4 * TRSM_NB && !(gs && gs[0] == '1') &&
-                     cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming) == cudaSuccess &&
-                     cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming) == cudaSuccess;
-    if (two) {
-        TrsmCtx ts[2] = {t, t};
-        const int64_t n1 = (nn / 2 + 7) / 8 * 8;
-        ts[0].n = n1;
-        ts[1].n = nn - n1;
-        ts[1].b = b + n1 * bcs;
-        ts[1].s = thread_aux_stream();
+    // per update) and the FP64-pipe diagonal solves of G column groups overlap
+    // on G streams (the caller's and G - 1 more of this thread), forked and
+    // joined by events; if an event cannot be created the solve runs on one stream
+    const char* gs = getenv("GB_TRSM_STREAMS");  // column groups: 1 .. 4 (default 2)
+    int groups = gs ? atoi(gs) : 2;
+    groups = groups < 1 ? 1 : (groups > 4 ? 4 : groups);
+    while (groups > 1 && nn < (int64_t)groups * TRSM_SPLIT_MIN_COLS) --groups;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // fork, then the joins of groups 1..
+    bool multi = !rc && slices > 0 && groups > 1 && mm > 4 * TRSM_NB;
+    for (int g = 0; multi && g < groups; ++g)
+        multi = cudaEventCreateWithFlags(&ev[g], cudaEventDisableTiming) == cudaSuccess;
+    if (multi) {
+        TrsmCtx ts[4] = {t, t, t, t};
+        int64_t c0 = 0;
+        for (int g = 0; g < groups; ++g) {
+            const int64_t c1 = (g + 1 == groups) ? nn : ((nn * (g + 1) / groups) + 7) / 8 * 8;
+            ts[g].n = c1 - c0;
+            ts[g].b = b + c0 * bcs;
+            if (g > 0) ts[g].s = thread_aux_stream(g - 1);
+            c0 = c1;
+        }
         rc = check_cuda(cudaEventRecord(ev[0], s), "trsm fork");
-        if (!rc) rc = check_cuda(cudaStreamWaitEvent(ts[1].s, ev[0], 0), "trsm fork");
-        if (!rc) rc = solve(ts, 2, 0, mm);
-        // the join is recorded whatever happened, so s never runs ahead of the second stream's work
-        cudaEventRecord(ev[1], ts[1].s);
-        cudaStreamWaitEvent(s, ev[1], 0);
+        for (int g = 1; g < groups && !rc; ++g) rc = check_cuda(cudaStreamWaitEvent(ts[g].s, ev[0], 0), "trsm fork");
+        if (!rc) rc = solve(ts, groups, 0, mm);
+        // the joins are recorded whatever happened, so s never runs ahead of the other streams' work
+        for (int g = 1; g < groups; ++g) {
+            cudaEventRecord(ev[g], ts[g].s);
+            cudaStreamWaitEvent(s, ev[g], 0);
+        }
     } else if (!rc) {
         cudaGetLastError();  // a failed event creation above is not this call's error
         rc = solve(&t, 1, 0, mm);
