@@ -135,6 +135,21 @@ int dgemm_native_gated(int64_t m, int64_t n, int64_t k, double alpha,
     return check_cuda(cudaGetLastError(), "dgemm_native");
 }
 
+// FP32 C := alpha op(A) op(B) + beta C on the FP32 FMA pipe, only when *gate is
+// nonzero: the IEEE fallback of the SGEMM split form for Inf/NaN operands.
+int sgemm_native_gated(int64_t m, int64_t n, int64_t k, float alpha, const float* a, int64_t ars, int64_t acs,
+                       const float* b, int64_t brs, int64_t bcs, float beta, float* c, int64_t rs_c, int64_t cs_c,
+                       const int* gate, cudaStream_t s)
+{
+    if (m <= 0 || n <= 0 || alpha == 0.0f || k <= 0) return GB_SUCCESS;  // the split form handled these
+    const int64_t gx = (n + BN - 1) / BN, gy = (m + BM - 1) / BM;
+    if (gy > 65535) return set_error(GB_ERR_ARG, "gb_sgemm", "m too large for one launch");
+    GArgs<float> p{m, n, k, alpha, beta, a, ars, acs, b, brs, bcs, c, rs_c, cs_c};
+    LaunchScope ls("sgemm_ffma_gated", s);
+    gemm_simt_kernel<float><<<dim3((unsigned)gx, (unsigned)gy), NT, 0, s>>>(p, gate);
+    return check_cuda(cudaGetLastError(), "sgemm_native_gated");
+}
+
 int dgemm_native(int64_t m, int64_t n, int64_t k, double alpha,
                  const double* a, int64_t ars, int64_t acs,
                  const double* b, int64_t brs, int64_t bcs, double beta,

@@ -928,9 +928,30 @@ __device__ __forceinline__ unsigned long long abs_bits(double x)
     return ((unsigned long long)hi << 32) | lo;
 }
 
+// Row-maximum keys of FP64 or FP32 elements: the IEEE bits of |x| (monotone
+// in |x|), and the FP64 bits of a maximum for oz_row_exponent.  FP32 keys
+// stay 32 bits; only the maximum is widened (exactly).
+template <typename T>
+using OzKey = std::conditional_t<sizeof(T) == 4, uint32_t, unsigned long long>;
+
+template <typename T>
+__device__ __forceinline__ OzKey<T> oz_abs_key(T x)
+{
+    if constexpr (sizeof(T) == 4) return __float_as_uint(x) & 0x7fffffffu;
+    else return abs_bits(x);
+}
+
+template <typename T>
+__device__ __forceinline__ unsigned long long oz_key_f64(unsigned long long key)
+{
+    if constexpr (sizeof(T) == 4) return (unsigned long long)__double_as_longlong((double)__uint_as_float((uint32_t)key));
+    else return key;
+}
+
 // Rows contiguous (sr == 1, e.g. column-major op(A)): thread per row, the
 // grid's y dimension splits k.
-__global__ void oz_rowmax_rows_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
+template <typename T>
+__global__ void oz_rowmax_rows_kernel(int64_t rows, int64_t k, const T* __restrict__ R,
                                       int64_t sl, int64_t kchunk, unsigned long long* __restrict__ maxbits)
 {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -938,26 +959,27 @@ __global__ void oz_rowmax_rows_kernel(int64_t rows, int64_t k, const double* __r
     const int64_t l0 = (int64_t)blockIdx.y * kchunk;
     const int64_t l1 = (l0 + kchunk < k) ? l0 + kchunk : k;
     // eight loads in flight per thread (one HBM round trip hides behind about 40 KB per SM)
-    unsigned long long mq[4] = {0, 0, 0, 0};
+    OzKey<T> mq[4] = {0, 0, 0, 0};
     int64_t l = l0;
     for (; l + 7 < l1; l += 8) {
-        unsigned long long b[8];
+        OzKey<T> b[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) b[u] = abs_bits(__ldcs(R + r + (l + u) * sl));
+        for (int u = 0; u < 8; ++u) b[u] = oz_abs_key(__ldcs(R + r + (l + u) * sl));
 #pragma unroll
         for (int u = 0; u < 8; ++u) mq[u & 3] = b[u] > mq[u & 3] ? b[u] : mq[u & 3];
     }
     for (; l < l1; ++l) {
-        const unsigned long long b0 = abs_bits(__ldcs(R + r + l * sl));
+        const OzKey<T> b0 = oz_abs_key(__ldcs(R + r + l * sl));
         mq[0] = b0 > mq[0] ? b0 : mq[0];
     }
-    const unsigned long long m01 = mq[0] > mq[1] ? mq[0] : mq[1], m23 = mq[2] > mq[3] ? mq[2] : mq[3];
-    const unsigned long long mx = m01 > m23 ? m01 : m23;
-    if (mx) atomicMax(maxbits + r, mx);
+    const OzKey<T> m01 = mq[0] > mq[1] ? mq[0] : mq[1], m23 = mq[2] > mq[3] ? mq[2] : mq[3];
+    const OzKey<T> mx = m01 > m23 ? m01 : m23;
+    if (mx) atomicMax(maxbits + r, oz_key_f64<T>(mx));
 }
 
 // Any other layout: warp per row, lanes stride along k.
-__global__ void oz_rowmax_warp_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
+template <typename T>
+__global__ void oz_rowmax_warp_kernel(int64_t rows, int64_t k, const T* __restrict__ R,
                                       int64_t sr, int64_t sl, int64_t kchunk,
                                       unsigned long long* __restrict__ maxbits)
 {
@@ -966,12 +988,12 @@ __global__ void oz_rowmax_warp_kernel(int64_t rows, int64_t k, const double* __r
     if (r >= rows) return;
     const int64_t l0 = (int64_t)blockIdx.y * kchunk;
     const int64_t l1 = (l0 + kchunk < k) ? l0 + kchunk : k;
-    unsigned long long mx = 0, my = 0;
+    OzKey<T> mx = 0, my = 0;
     int64_t l = l0 + lane;
     for (; l + 32 * 7 < l1; l += 32 * 8) {  // eight loads in flight per lane
-        unsigned long long b[8];
+        OzKey<T> b[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) b[u] = abs_bits(__ldcs(R + r * sr + (l + 32 * u) * sl));
+        for (int u = 0; u < 8; ++u) b[u] = oz_abs_key(__ldcs(R + r * sr + (l + 32 * u) * sl));
 #pragma unroll
         for (int u = 0; u < 8; u += 2) {
             mx = b[u] > mx ? b[u] : mx;
@@ -979,16 +1001,16 @@ __global__ void oz_rowmax_warp_kernel(int64_t rows, int64_t k, const double* __r
         }
     }
     for (; l < l1; l += 32) {
-        const unsigned long long b = abs_bits(__ldcs(R + r * sr + l * sl));
+        const OzKey<T> b = oz_abs_key(__ldcs(R + r * sr + l * sl));
         mx = b > mx ? b : mx;
     }
     mx = my > mx ? my : mx;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
+        const OzKey<T> o = __shfl_xor_sync(0xffffffffu, mx, off);
         mx = o > mx ? o : mx;
     }
-    if (lane == 0 && mx) atomicMax(maxbits + r, mx);
+    if (lane == 0 && mx) atomicMax(maxbits + r, oz_key_f64<T>(mx));
 }
 
 __device__ __forceinline__ int clz128(unsigned __int128 u)
@@ -1084,8 +1106,8 @@ __device__ __forceinline__ int oz_row_exponent(unsigned long long bits, int* non
 
 // Tile of 32 rows x 64 k per block; writes S bf16 digit planes, K-major,
 // zero in the padding.
-template <int S>
-__global__ void __launch_bounds__(256) oz_split_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
+template <int S, typename T = double>
+__global__ void __launch_bounds__(256) oz_split_kernel(int64_t rows, int64_t k, const T* __restrict__ R,
                                                        int64_t sr, int64_t sl,
                                                        const unsigned long long* __restrict__ maxbits,
                                                        int64_t rpad, int64_t kpad,
@@ -1101,7 +1123,7 @@ __global__ void __launch_bounds__(256) oz_split_kernel(int64_t rows, int64_t k, 
         const int rr = rows_fast ? (e & 31) : (e >> 6);
         const int ll = rows_fast ? (e >> 5) : (e & 63);
         const int64_t r = r0 + rr, l = l0 + ll;
-        tile[rr][ll] = (r < rows && l < k) ? __ldcs(R + r * sr + l * sl) : 0.0;
+        tile[rr][ll] = (r < rows && l < k) ? (double)__ldcs(R + r * sr + l * sl) : 0.0;
     }
     __syncthreads();
     const int rr = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 8;
@@ -1210,6 +1232,7 @@ struct OzRecombParams {
     const int32_t* eb;
     double alpha, beta;
     double* c;
+    float* cf = nullptr;  // FP32 C instead (SGEMM's split form): RN32(alpha P + beta C) from the FP64 P
     int64_t rs_c, cs_c;
     const int* skip;
     int out_tri = 0, out_rpc = 1;  // only C's stored triangle is read and written (as OzA::out_tri)
@@ -1285,6 +1308,16 @@ __global__ void __launch_bounds__(256, (S <= 7 ? 3 : 2)) oz_recombine_kernel(con
                 for (int L = S - 1; L >= 0; --L) T = (__int128)((unsigned __int128)T << 8) + (__int128)acc[L][r];
             }
             const double ab = round_scaled(T, p.ea[i] + ebj);
+            if (p.cf) {
+                float* cij = p.cf + i * p.rs_c + j * p.cs_c;
+                if (plain) {
+                    *cij = (float)ab;
+                } else {
+                    const double t = __dmul_rn(p.alpha, ab);
+                    *cij = (float)((p.beta == 0.0) ? t : __fma_rn(p.beta, (double)*cij, t));
+                }
+                continue;
+            }
             double* cij = p.c + i * p.rs_c + j * p.cs_c;
             if (plain) {
                 *cij = ab;
@@ -1308,23 +1341,6 @@ __global__ void __launch_bounds__(256, (S <= 7 ? 3 : 2)) oz_recombine_kernel(con
 // T is double, or float for FP32 operands (each element widened exactly on
 // load; the row maxima compare the FP32 bits, and only the maximum is
 // widened to the FP64 bits oz_row_exponent reads).
-template <typename T>
-using OzKey = std::conditional_t<sizeof(T) == 4, uint32_t, unsigned long long>;
-
-template <typename T>
-__device__ __forceinline__ OzKey<T> oz_abs_key(T x)
-{
-    if constexpr (sizeof(T) == 4) return __float_as_uint(x) & 0x7fffffffu;
-    else return abs_bits(x);
-}
-
-template <typename T>
-__device__ __forceinline__ unsigned long long oz_key_f64(unsigned long long key)
-{
-    if constexpr (sizeof(T) == 4) return (unsigned long long)__double_as_longlong((double)__uint_as_float((uint32_t)key));
-    else return key;
-}
-
 template <int S, typename T, typename Store>
 __device__ __forceinline__ void oz_split_unit(const T* __restrict__ R, int64_t rows, int64_t sr, int64_t sl,
                                               int64_t k, int nkb, int64_t r0, int32_t* __restrict__ exps,
@@ -1421,8 +1437,8 @@ __device__ __forceinline__ void oz_split_unit(const T* __restrict__ R, int64_t r
 // launch (oz_split_unit): block u owns rows 32u .. 32u + 31 of the padded
 // row range, so the padding rows up to rpad and the k padding up to kpad
 // are written as zeros, in the slice planes' layout of oz_split_kernel.
-template <int S>
-__global__ void __launch_bounds__(256, 2) oz_split_rows_kernel(int64_t rows, int64_t k, const double* __restrict__ R,
+template <int S, typename T = double>
+__global__ void __launch_bounds__(256, 2) oz_split_rows_kernel(int64_t rows, int64_t k, const T* __restrict__ R,
                                                             int64_t sr, int64_t sl, int64_t rpad, int64_t kpad,
                                                             uint16_t* __restrict__ out, int32_t* __restrict__ exps,
                                                             int* __restrict__ nonfinite)
@@ -2000,13 +2016,13 @@ namespace {
 // The split launchers take the slice planes' row stride (rpad) apart from
 // the rows they cover (rcover, a multiple of 32): a block of rows r0.. of a
 // larger operand is split by passing R, mb, out and ex offset to row r0.
-template <int S>
-void launch_split(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl,
+template <int S, typename T>
+void launch_split(int64_t rows, int64_t k, const T* R, int64_t sr, int64_t sl,
                   const unsigned long long* mb, int64_t rpad, int64_t rcover, int64_t kpad, uint16_t* out,
                   int32_t* ex, int* nonfinite, cudaStream_t s)
 {
     LaunchScope ls("oz_split", s);
-    oz_split_kernel<S><<<dim3((unsigned)(kpad / 64), (unsigned)(rcover / 32)), 256, 0, s>>>(
+    oz_split_kernel<S, T><<<dim3((unsigned)(kpad / 64), (unsigned)(rcover / 32)), 256, 0, s>>>(
         rows, k, R, sr, sl, mb, rpad, kpad, out, ex, nonfinite);
 }
 
@@ -2042,16 +2058,17 @@ int64_t fused_split_max_k()
     return v;
 }
 
-template <int S>
-void launch_split_rows(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl, int64_t rpad,
+template <int S, typename T>
+void launch_split_rows(int64_t rows, int64_t k, const T* R, int64_t sr, int64_t sl, int64_t rpad,
                        int64_t rcover, int64_t kpad, uint16_t* out, int32_t* ex, int* nonfinite, cudaStream_t s)
 {
     LaunchScope ls("oz_split_rows", s);
-    oz_split_rows_kernel<S><<<(unsigned)(rcover / 32), 256, 0, s>>>(rows, k, R, sr, sl, rpad, kpad, out, ex,
-                                                                     nonfinite);
+    oz_split_rows_kernel<S, T><<<(unsigned)(rcover / 32), 256, 0, s>>>(rows, k, R, sr, sl, rpad, kpad, out, ex,
+                                                                        nonfinite);
 }
 
-void launch_rowmax(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl, unsigned long long* mb,
+template <typename T>
+void launch_rowmax(int64_t rows, int64_t k, const T* R, int64_t sr, int64_t sl, unsigned long long* mb,
                    cudaStream_t s);
 
 // Row maxima and digit slices of one row operand (or of rows r0.. of one,
@@ -2077,6 +2094,22 @@ void split_operand(int slices, int64_t rows, int64_t k, const double* R, int64_t
     cudaMemsetAsync(mb, 0, sizeof(unsigned long long) * rows, s);
     launch_rowmax(rows, k, R, sr, sl, mb, s);
     split_dispatch(slices, rows, k, R, sr, sl, mb, rpad, rcover, kpad, out, ex, nonfinite, s);
+}
+
+// split_operand for FP32 rows at the SGEMM split form's slice count: the
+// same launches reading 4-byte elements (each widened exactly as it loads).
+void split_operand_f32(int64_t rows, int64_t k, const float* R, int64_t sr, int64_t sl, unsigned long long* mb,
+                       int64_t rpad, int64_t rcover, int64_t kpad, uint16_t* out, int32_t* ex, int* nonfinite,
+                       cudaStream_t s)
+{
+    constexpr int S = GB_SGEMM_SPLIT_SLICES;
+    if (k <= fused_split_max_k() && rcover / 32 <= INT32_MAX) {
+        launch_split_rows<S>(rows, k, R, sr, sl, rpad, rcover, kpad, out, ex, nonfinite, s);
+        return;
+    }
+    cudaMemsetAsync(mb, 0, sizeof(unsigned long long) * rows, s);
+    launch_rowmax(rows, k, R, sr, sl, mb, s);
+    launch_split<S>(rows, k, R, sr, sl, mb, rpad, rcover, kpad, out, ex, nonfinite, s);
 }
 
 // The CRT form's split of one row operand: row maxima, then the residues.
@@ -2115,7 +2148,8 @@ double ozaki_t_bound_log2(int s, int64_t k)
 
 namespace {
 
-void launch_rowmax(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t sl, unsigned long long* mb,
+template <typename T>
+void launch_rowmax(int64_t rows, int64_t k, const T* R, int64_t sr, int64_t sl, unsigned long long* mb,
                    cudaStream_t s)
 {
     const int sms = sm_count() > 0 ? sm_count() : 148;
@@ -2127,7 +2161,7 @@ void launch_rowmax(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t
         const int64_t kchunk = (k + gy - 1) / gy;
         gy = (k + kchunk - 1) / kchunk;
         LaunchScope ls("oz_rowmax", s);
-        oz_rowmax_rows_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sl, kchunk, mb);
+        oz_rowmax_rows_kernel<T><<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sl, kchunk, mb);
     } else {
         const int64_t gx = (rows * 32 + 255) / 256;
         int64_t gy = ((int64_t)sms * 8 + gx - 1) / gx;
@@ -2137,7 +2171,7 @@ void launch_rowmax(int64_t rows, int64_t k, const double* R, int64_t sr, int64_t
         const int64_t kchunk = (k + gy - 1) / gy;
         gy = (k + kchunk - 1) / kchunk;
         LaunchScope ls("oz_rowmax", s);
-        oz_rowmax_warp_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sr, sl, kchunk, mb);
+        oz_rowmax_warp_kernel<T><<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(rows, k, R, sr, sl, kchunk, mb);
     }
 }
 
@@ -2396,11 +2430,36 @@ __global__ void __launch_bounds__(256) oz_tri_merge_gated_kernel(int64_t rows, i
 // prepared op(A) (r0 a multiple of the row tile) and a prepared op(B); C is
 // that rows x n block; the slice GEMM, the recombination and the gated IEEE
 // fallback.
+namespace {
+
+// FP32 operands and C of SGEMM's split form (multiply_rows_impl): C is written
+// in FP32 by the recombination, and the IEEE fallback reads these operands.
+struct OzF32 {
+    const float* a;
+    const float* b;
+    float* c;
+};
+
+int multiply_rows_impl(const OzA* A, int64_t r0, int64_t rows, const OzB* B, double alpha, double beta, double* c,
+                       int64_t rs_c, int64_t cs_c, const OzF32* f32, cudaStream_t s);
+
+}  // namespace
+
 int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, double alpha, double beta, double* c,
                         int64_t rs_c, int64_t cs_c, cudaStream_t s)
 {
+    return multiply_rows_impl(A, r0, rows, B, alpha, beta, c, rs_c, cs_c, nullptr, s);
+}
+
+namespace {
+
+int multiply_rows_impl(const OzA* A, int64_t r0, int64_t rows, const OzB* B, double alpha, double beta, double* c,
+                       int64_t rs_c, int64_t cs_c, const OzF32* f32, cudaStream_t s)
+{
     if (r0 < 0 || rows <= 0 || r0 + rows > A->m || r0 % A->row_tile)
         return set_error(GB_ERR_ARG, "ozaki", "row block not aligned to the slice GEMM tile");
+    if (f32 && (A->out_tri || A->crt))
+        return set_error(GB_ERR_ARG, "ozaki", "the FP32 form writes a whole C from the digit form");
     note_ozaki_slices(A->slices);
     if (A->out_tri && (r0 != 0 || rows != A->m || A->tri || A->out_rpc < 1))
         return set_error(GB_ERR_ARG, "ozaki", "a triangle of C is written from the whole of op(A) only");
@@ -2536,6 +2595,7 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
         r.alpha = alpha;
         r.beta = beta;
         r.c = c;
+        r.cf = f32 ? f32->c : nullptr;
         r.rs_c = rs_c;
         r.cs_c = cs_c;
         r.skip = A->nonfinite;
@@ -2556,7 +2616,10 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
     }
     if ((rc = check_cuda(cudaGetLastError(), "oz_recombine"))) return bail(rc);
     // IEEE path for non-finite operands: runs only when a split raised the flag
-    if (!A->out_tri) {
+    if (f32) {
+        rc = sgemm_native_gated(m, n, k, (float)alpha, f32->a + r0 * A->ars, A->ars, A->acs, f32->b, B->brs, B->bcs,
+                                (float)beta, f32->c, rs_c, cs_c, A->nonfinite, s);
+    } else if (!A->out_tri) {
         rc = dgemm_native_gated(m, n, k, alpha, A->a + r0 * A->ars, A->ars, A->acs, B->b, B->brs, B->bcs, beta, c,
                                 rs_c, cs_c, A->nonfinite, s);
     } else {
@@ -2600,6 +2663,8 @@ int ozaki_multiply_rows(const OzA* A, int64_t r0, int64_t rows, const OzB* B, do
     dev_free(planes, s);
     return rc;
 }
+
+}  // namespace
 
 // Phases 2 and 3 for all rows of op(A).
 int ozaki_multiply(const OzA* A, int64_t n, const double* b, int64_t brs, int64_t bcs, double alpha, double beta,
@@ -2665,6 +2730,40 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
         rc = check_cuda(cudaGetLastError(), "oz_split");
     }
     if (!rc) rc = ozaki_multiply_rows(&A, 0, m, &B, alpha, beta, c, rs_c, cs_c, s);
+    ozaki_release_b(&B, s);
+    ozaki_release_a(&A, s);
+    return rc;
+}
+
+// SGEMM's split form on the FP32 operands themselves: the digit form at
+// GB_SGEMM_SPLIT_SLICES slices splits op(A) and op(B) straight from FP32
+// (each element widened exactly as it loads), the slice GEMM runs as for
+// dgemm_ozaki, and the recombination writes C = RN32(alpha P + beta C) from
+// the FP64 product P, the rounding of the form through FP64 copies; Inf/NaN
+// operands raise the flag and an FP32 kernel gated on it computes C instead.
+int sgemm_ozaki(int64_t m, int64_t n, int64_t k, float alpha, const float* a, int64_t ars, int64_t acs,
+                const float* b, int64_t brs, int64_t bcs, float beta, float* c, int64_t rs_c, int64_t cs_c,
+                cudaStream_t s)
+{
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    if (alpha == 0.0f || k <= 0) return scal_matrix_f(m, n, beta, c, rs_c, cs_c, s);
+    constexpr int S = GB_SGEMM_SPLIT_SLICES;
+    ModeOverride digits(GB_DGEMM_OZAKI, S, 0);
+    EngineScope engine(t_ozaki_ctas ? t_ozaki_ctas : ozaki_engine_choice(m, n, k));
+    OzA A;
+    int rc = ozaki_alloc_a(m, k, nullptr, ars, acs, S, s, &A);
+    if (rc) return rc;
+    OzB B;
+    if ((rc = ozaki_alloc_b(&A, n, nullptr, brs, bcs, s, &B))) {
+        ozaki_release_a(&A, s);
+        return rc;
+    }
+    split_operand_f32(m, k, a, ars, acs, A.maxa, A.mpad, A.mpad, A.kpad, A.sa, A.ea, A.nonfinite, s);
+    // rows of op(B)^T: (j, l) = b[l*brs + j*bcs]
+    split_operand_f32(n, k, b, bcs, brs, B.maxb, B.npad, B.npad, A.kpad, B.sb, B.eb, A.nonfinite, s);
+    rc = check_cuda(cudaGetLastError(), "oz_split");
+    const OzF32 f32{a, b, c};
+    if (!rc) rc = multiply_rows_impl(&A, 0, m, &B, (double)alpha, (double)beta, nullptr, rs_c, cs_c, &f32, s);
     ozaki_release_b(&B, s);
     ozaki_release_a(&A, s);
     return rc;

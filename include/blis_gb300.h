@@ -693,9 +693,9 @@ int gb_batch_plan_destroy(void* plan);
    assigns to configs 1..5, without split-K; 2 = the selected configuration
    including split-K (those problems run in a second grouped launch and a
    grouped fold, in the same graph); 3 (FP32 only) = SGEMM's split form for
-   the whole batch: one grouped launch widens op(A) and op(B) to FP64, the
-   products run as one grouped Ozaki plan at 3 slices on the bf16 tensor
-   cores, one grouped launch rounds alpha P + beta C to FP32 once.
+   the whole batch: the grouped Ozaki form at 3 slices on the bf16 tensor
+   cores, its split reading op(A) and op(B) in FP32 (each element widened
+   exactly), its recombination rounding alpha P + beta C to FP32 once.
    gb_batch_plan_create autotunes it: each candidate runs on the batch's
    shapes with scratch outputs and the fastest is kept.  Candidates: 0; 1 and
    2 when a selector model is loaded and auto-selection is on; 3 for FP32
@@ -802,9 +802,9 @@ int gb_set_dgemm_mode(int mode, int slices);
 
 /* SGEMM engine (no reference counterpart): GB_SGEMM_FMA the FP32 FMA kernel;
    GB_SGEMM_SPLIT the split form on the bf16 tensor cores (op(A), op(B)
-   widened to FP64 and multiplied as the Ozaki digit form with 3 slices, six
-   bf16 products with exact integer accumulation, then C = RN32(alpha P +
-   beta C) from the FP64 product P); GB_SGEMM_AUTO (default) the split form
+   split from FP32, each element widened exactly, and multiplied as the Ozaki
+   digit form with 3 slices, six bf16 products with exact integer
+   accumulation, then C = RN32(alpha P + beta C) from the FP64 product P); GB_SGEMM_AUTO (default) the split form
    when m, n >= 1024 and k >= 512, the FMA kernel otherwise.  Host and device
    sgemm entry points follow it. */
 #define GB_SGEMM_FMA 0

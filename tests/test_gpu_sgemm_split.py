@@ -1,7 +1,8 @@
 """SGEMM's split form on the bf16 tensor cores (gb_sgemm_split.cu) against the FP64 product.
 
-The form widens op(A), op(B) to FP64, forms their product as the Ozaki digit form with three
-slices (exact integer accumulation) and rounds alpha P + beta C to FP32 once.  With beta = 0
+The form splits op(A), op(B) straight from FP32 (each element widened exactly to FP64 as it
+loads), forms their product as the Ozaki digit form with three slices (exact integer
+accumulation) and rounds alpha P + beta C to FP32 once in the recombination.  With beta = 0
 the model is exact: the oracle's digit-form product, times alpha in FP64, rounded to FP32.
 Otherwise the result is checked against an FP64 product within the form's bound:
 2^-(8s+1) (2^e_i |B_j|_1 + |A_i|_1 2^e_j) + 2^-(16s+2) k 2^(e_i+e_j) for the product (the
@@ -26,10 +27,17 @@ def split_mode(gblib):
 
 
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
-@pytest.mark.parametrize("m,n,k", [(300, 200, 1000), (33, 517, 64), (1024, 1024, 2048)])
-def test_split_sgemm_bit_exact_beta0(ta, tb, m, n, k):
-    a = po.uniform((k, m) if ta == "T" else (m, k), 1, dtype=np.float32)
-    b = po.uniform((n, k) if tb == "T" else (k, n), 2, dtype=np.float32)
+@pytest.mark.parametrize("m,n,k,spread", [(300, 200, 1000, False), (33, 517, 64, False), (1024, 1024, 2048, False),
+                                          (200, 300, 5000, False), (260, 150, 700, True), (130, 270, 5000, True)])
+def test_split_sgemm_bit_exact_beta0(ta, tb, m, n, k, spread):
+    # k = 5000 takes the row-maximum kernel and the tiled split (k past the fused split's 4096);
+    # spread: entries (1 + u) 2^e, e in [-30, 30], so rows lose their small entries' low bits
+    if spread:
+        a = po.expspread((k, m) if ta == "T" else (m, k), 1, -30, 30).astype(np.float32)
+        b = po.expspread((n, k) if tb == "T" else (k, n), 2, -30, 30).astype(np.float32)
+    else:
+        a = po.uniform((k, m) if ta == "T" else (m, k), 1, dtype=np.float32)
+        b = po.uniform((n, k) if tb == "T" else (k, n), 2, dtype=np.float32)
     c = np.zeros((m, n), dtype=np.float32, order="F")
     blas.sgemm(ta, tb, m, n, k, 0.75, a, a.shape[0], b, b.shape[0], 0.0, c, m)
     p = np.zeros((m, n), order="F")
