@@ -1224,6 +1224,37 @@ __device__ __forceinline__ double round_scaled(__int128 T, int E)
     return __longlong_as_double((long long)bits);
 }
 
+// round_scaled for a T that fits 64 bits (the digit form at S <= 4 slices:
+// one group of oz_weighted_sum): the same RNE on 64-bit integers where the
+// result is a normal number, the 128-bit routine otherwise.
+__device__ __forceinline__ double round_scaled64(long long T, int E)
+{
+    if (T == 0) return 0.0;
+    const bool neg = T < 0;
+    const unsigned long long u = neg ? 0ull - (unsigned long long)T : (unsigned long long)T;
+    const int msb = 63 - __clzll((long long)u);
+    const int lead = msb + E;
+    if (lead < -1022 || lead > 1023) return round_scaled((__int128)T, E);
+    const unsigned long long top = u << (63 - msb);  // every bit of u is kept: no sticky bits below
+    unsigned long long q = top >> 11;
+    const unsigned long long rb = top & 0x7FFull;
+    if (rb > 0x400ull || (rb == 0x400ull && (q & 1ull))) q += 1;
+    unsigned long long bits = ((unsigned long long)(lead + 1022) << 52) + q;  // q in [2^52, 2^53]
+    if (bits >= 0x7FF0000000000000ull) bits = 0x7FF0000000000000ull;
+    if (neg) bits |= 0x8000000000000000ull;
+    return __longlong_as_double((long long)bits);
+}
+
+template <int S, typename A>
+__device__ __forceinline__ long long oz_weighted_sum64(const A (&a)[S])
+{
+    static_assert(S <= 4, "one 64-bit group");
+    long long v = 0;
+#pragma unroll
+    for (int t = 0; t < S; ++t) v += (long long)a[t] * (1ll << (8 * t));
+    return v;
+}
+
 struct OzRecombParams {
     int slices, nlevels;
     int64_t m, n, mpad, npad;
@@ -1292,22 +1323,36 @@ __global__ void __launch_bounds__(256, (S <= 7 ? 3 : 2)) oz_recombine_kernel(con
             const int64_t i = i0 + r;
             if (i >= p.m) break;
             if (p.out_tri && (p.out_tri == 1 ? i < dlo : i > dhi)) continue;
-            __int128 T = 0;
-            if (one_part) {
-                int a[S];
+            double ab;
+            bool done = false;
+            if constexpr (S <= 4) {
+                if (few_parts) {  // |sum| < 2^63 (oz_weighted_sum): the 64-bit rounding
+                    long long a[S];
 #pragma unroll
-                for (int L = 0; L < S; ++L) a[L] = (int)acc[L][r];
-                T = oz_weighted_sum<S>(a);
-            } else if (few_parts) {
-                long long a[S];
-#pragma unroll
-                for (int L = 0; L < S; ++L) a[L] = acc[L][r];
-                T = oz_weighted_sum<S>(a);
-            } else {
-#pragma unroll
-                for (int L = S - 1; L >= 0; --L) T = (__int128)((unsigned __int128)T << 8) + (__int128)acc[L][r];
+                    for (int L = 0; L < S; ++L) a[L] = acc[L][r];
+                    ab = round_scaled64(oz_weighted_sum64<S>(a), p.ea[i] + ebj);
+                    done = true;
+                }
             }
-            const double ab = round_scaled(T, p.ea[i] + ebj);
+            if (!done) {
+                __int128 T = 0;
+                if (one_part) {
+                    int a[S];
+#pragma unroll
+                    for (int L = 0; L < S; ++L) a[L] = (int)acc[L][r];
+                    T = oz_weighted_sum<S>(a);
+                } else if (few_parts) {
+                    long long a[S];
+#pragma unroll
+                    for (int L = 0; L < S; ++L) a[L] = acc[L][r];
+                    T = oz_weighted_sum<S>(a);
+                } else {
+#pragma unroll
+                    for (int L = S - 1; L >= 0; --L)
+                        T = (__int128)((unsigned __int128)T << 8) + (__int128)acc[L][r];
+                }
+                ab = round_scaled(T, p.ea[i] + ebj);
+            }
             if (p.cf) {
                 float* cij = p.cf + i * p.rs_c + j * p.cs_c;
                 if (plain) {
@@ -1541,8 +1586,9 @@ __global__ void __launch_bounds__(256) oz_recombine_batch_kernel(const OzBatchPr
         int a[S];
 #pragma unroll
         for (int L = 0; L < S; ++L) a[L] = (r == 0) ? v[L].x : (r == 1) ? v[L].y : (r == 2) ? v[L].z : v[L].w;
-        const __int128 T = oz_weighted_sum<S>(a);
-        const double ab = round_scaled(T, ea[i] + ebj);
+        double ab;
+        if constexpr (S <= 4) ab = round_scaled64(oz_weighted_sum64<S>(a), ea[i] + ebj);
+        else ab = round_scaled(oz_weighted_sum<S>(a), ea[i] + ebj);
         CT* cij = static_cast<CT*>(q.c) + i * q.rs_c + j * q.cs_c;
         if (plain) {
             *cij = (CT)ab;
