@@ -1076,10 +1076,33 @@ __device__ __forceinline__ void oz_digit_floats(double x, int e, float (&f)[S])
     }
 }
 
+// The same digits of an FP32 element in 32-bit integers (S <= 3: Y < 2^(8S+3)
+// fits 32 bits).  X = floor(|x| 2^(F-e)) does not depend on the format x is
+// held in, so the digits equal those of x widened to FP64 (subnormal inputs
+// included); Inf/NaN (whose row raised the flag) give unused digits.
+template <int S>
+__device__ __forceinline__ void oz_digit_floats(float x, int e, float (&f)[S])
+{
+    static_assert(8 * S + 3 <= 32, "the 32-bit digit form holds at most 3 slices");
+    const uint32_t bits = __float_as_uint(x);
+    const uint32_t m = (uint32_t)((int32_t)bits >> 31);
+    const uint32_t c = m ? OZ_MAGIC_BITS + 129u : OZ_MAGIC_BITS - 128u;
+    const int ex = (int)((bits >> 23) & 0xFFu);
+    const uint32_t M = (bits & 0x7FFFFFu) | (ex ? 0x800000u : 0u);
+    const int E2 = ex ? ex - 150 : -149;
+    constexpr int F = 8 * S + 2;
+    const int sh = E2 - e + F;  // U 2^F = M 2^sh < 2^(F-1)
+    const uint32_t X = (sh >= 0) ? (sh < 32 ? M << sh : 0u) : (sh > -32 ? M >> (-sh) : 0u);
+    const uint32_t Y = X + oz_bias<uint32_t>(S);
+    f[0] = __uint_as_float(((Y >> (F - 8)) ^ m) + c) - OZ_MAGIC;
+#pragma unroll
+    for (int p = 2; p <= S; ++p) f[p - 1] = __uint_as_float((((Y >> (F - 8 * p)) & 255u) ^ m) + c) - OZ_MAGIC;
+}
+
 // Digits of two elements, slice by slice as bf16 pairs (x0 in the low half):
 // one byte permute takes the upper halves of both fp32 images.
-template <int S>
-__device__ __forceinline__ void oz_digits_bf16x2(double x0, double x1, int e, uint32_t (&w)[S])
+template <int S, typename T>
+__device__ __forceinline__ void oz_digits_bf16x2(T x0, T x1, int e, uint32_t (&w)[S])
 {
     float f0[S], f1[S];
     oz_digit_floats<S>(x0, e, f0);
@@ -1114,7 +1137,7 @@ __global__ void __launch_bounds__(256) oz_split_kernel(int64_t rows, int64_t k, 
                                                        uint16_t* __restrict__ out, int32_t* __restrict__ exps,
                                                        int* __restrict__ nonfinite)
 {
-    __shared__ double tile[32][65];
+    __shared__ T tile[32][65];
     const int64_t l0 = (int64_t)blockIdx.x * 64, r0 = (int64_t)blockIdx.y * 32;
     const bool rows_fast = (sr == 1);
 #pragma unroll
@@ -1123,7 +1146,7 @@ __global__ void __launch_bounds__(256) oz_split_kernel(int64_t rows, int64_t k, 
         const int rr = rows_fast ? (e & 31) : (e >> 6);
         const int ll = rows_fast ? (e >> 5) : (e & 63);
         const int64_t r = r0 + rr, l = l0 + ll;
-        tile[rr][ll] = (r < rows && l < k) ? (double)__ldcs(R + r * sr + l * sl) : 0.0;
+        tile[rr][ll] = (r < rows && l < k) ? __ldcs(R + r * sr + l * sl) : T(0);
     }
     __syncthreads();
     const int rr = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 8;
@@ -1139,7 +1162,7 @@ __global__ void __launch_bounds__(256) oz_split_kernel(int64_t rows, int64_t k, 
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
         uint32_t w[S];
-        oz_digits_bf16x2<S>(r < rows ? tile[rr][c0 + 2 * h] : 0.0, r < rows ? tile[rr][c0 + 2 * h + 1] : 0.0, e, w);
+        oz_digits_bf16x2<S>(r < rows ? tile[rr][c0 + 2 * h] : T(0), r < rows ? tile[rr][c0 + 2 * h + 1] : T(0), e, w);
 #pragma unroll
         for (int p = 0; p < S; ++p) packed[p][h] = w[p];
     }
@@ -1391,7 +1414,7 @@ __device__ __forceinline__ void oz_split_unit(const T* __restrict__ R, int64_t r
                                               int64_t k, int nkb, int64_t r0, int32_t* __restrict__ exps,
                                               int* __restrict__ nonfinite, Store store)
 {
-    __shared__ double tile[32][65];
+    __shared__ T tile[32][65];
     __shared__ unsigned long long red[8][32];
     __shared__ int rowe[32];
     const bool rows_fast = (sr == 1);
@@ -1468,7 +1491,7 @@ __device__ __forceinline__ void oz_split_unit(const T* __restrict__ R, int64_t r
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
             uint32_t w[S];
-            oz_digits_bf16x2<S>(live ? tile[rr][c0 + 2 * h] : 0.0, live ? tile[rr][c0 + 2 * h + 1] : 0.0, e, w);
+            oz_digits_bf16x2<S>(live ? tile[rr][c0 + 2 * h] : T(0), live ? tile[rr][c0 + 2 * h + 1] : T(0), e, w);
 #pragma unroll
             for (int p = 0; p < S; ++p) packed[p][h] = w[p];
         }
