@@ -41,6 +41,33 @@ __global__ void __launch_bounds__(NT) gemm_simt_kernel(GArgs<T> p, const int* ga
     simt_tile<T>(p, (int64_t)blockIdx.y * BM, (int64_t)blockIdx.x * BN, As, Bs);
 }
 
+// The gated IEEE fallbacks (Inf/NaN operands of the Ozaki and split forms):
+// at most two CTAs per SM, each walking tiles (tile t: row block t / gx,
+// column block t % gx), so that a launch whose flag is clear, the common
+// case, retires a few hundred CTAs instead of one per tile.
+__global__ void __launch_bounds__(NT) dgemm_dmma_gated_kernel(DArgs p, const int* gate, int64_t gx, int64_t tiles)
+{
+    if (*gate == 0) return;
+    __shared__ double As[BK * LDS];
+    __shared__ double Bs[BK * LDS];
+    for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) dmma_tile(p, (t / gx) * BM, (t % gx) * BN, As, Bs);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) gemm_simt_gated_kernel(GArgs<T> p, const int* gate, int64_t gx, int64_t tiles)
+{
+    if (*gate == 0) return;
+    __shared__ T As[BK * LDS];
+    __shared__ T Bs[BK * LDS];
+    for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) simt_tile<T>(p, (t / gx) * BM, (t % gx) * BN, As, Bs);
+}
+
+unsigned gated_grid(int64_t tiles)
+{
+    const int64_t cap = 2 * (int64_t)(sm_count() > 0 ? sm_count() : 148);
+    return (unsigned)(tiles < cap ? tiles : cap);
+}
+
 template <bool VEC, bool A_RC, bool B_RC>
 __global__ void __launch_bounds__(NT, 2) sgemm_kernel(GArgs<float> p)  // two CTAs (16 warps) per SM
 {
@@ -125,6 +152,16 @@ int dgemm_native_gated(int64_t m, int64_t n, int64_t k, double alpha,
     if (gy > 65535) return set_error(GB_ERR_ARG, "gb_dgemm", "m too large for one launch");
     DArgs p{m, n, k, alpha, beta, a, ars, acs, b, brs, bcs, c, rs_c, cs_c};
     dim3 grid((unsigned)gx, (unsigned)gy);
+    if (gate) {
+        if (use_dfma()) {
+            LaunchScope ls("dgemm_dfma_gated", s);
+            gemm_simt_gated_kernel<double><<<gated_grid(gx * gy), NT, 0, s>>>(p, gate, gx, gx * gy);
+        } else {
+            LaunchScope ls("dgemm_dmma_gated", s);
+            dgemm_dmma_gated_kernel<<<gated_grid(gx * gy), NT, 0, s>>>(p, gate, gx, gx * gy);
+        }
+        return check_cuda(cudaGetLastError(), "dgemm_native_gated");
+    }
     if (use_dfma()) {
         LaunchScope ls("dgemm_dfma", s);
         gemm_simt_kernel<double><<<grid, NT, 0, s>>>(p, gate);
@@ -146,7 +183,7 @@ int sgemm_native_gated(int64_t m, int64_t n, int64_t k, float alpha, const float
     if (gy > 65535) return set_error(GB_ERR_ARG, "gb_sgemm", "m too large for one launch");
     GArgs<float> p{m, n, k, alpha, beta, a, ars, acs, b, brs, bcs, c, rs_c, cs_c};
     LaunchScope ls("sgemm_ffma_gated", s);
-    gemm_simt_kernel<float><<<dim3((unsigned)gx, (unsigned)gy), NT, 0, s>>>(p, gate);
+    gemm_simt_gated_kernel<float><<<gated_grid(gx * gy), NT, 0, s>>>(p, gate, gx, gx * gy);
     return check_cuda(cudaGetLastError(), "sgemm_native_gated");
 }
 
