@@ -1562,11 +1562,13 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4) ? 4 : 2) oz_split_batch_
     const bool isb = (u >= q.units_a);
     if (isb) u -= q.units_a;
     const int box_rows = isb ? OZ_BN : OZ_BM;
+    const int box_shift = isb ? 8 : 7;  // log2 of box_rows: shifts, not a 64-bit division
+    static_assert(OZ_BN == 256 && OZ_BM == 128, "box heights");
     const int64_t r0 = u * 32;
     uint16_t* out = isb ? sb : sa;
     const int64_t boxes = isb ? boxes_b : boxes_a;
-    const int64_t box0 = (isb ? q.bbox : q.abox) + (r0 / box_rows) * q.kb;
-    const int64_t rb = (r0 % box_rows);
+    const int64_t box0 = (isb ? q.bbox : q.abox) + (r0 >> box_shift) * q.kb;
+    const int64_t rb = r0 & (box_rows - 1);
     oz_split_unit<S>(static_cast<const T*>(isb ? q.b : q.a), isb ? q.n : q.m, isb ? q.brs : q.ars, isb ? q.bcs : q.acs, q.k, q.kb, r0,
                      isb ? q.eb : q.ea, nonfinite, [&](int p, int kb, int rr, int c0, uint4 v) {
                          const int64_t z = (int64_t)p * boxes + box0 + kb;
@@ -1594,7 +1596,9 @@ __global__ void __launch_bounds__(256) oz_recombine_batch_kernel(const OzBatchPr
     const int64_t mq = (m + 3) >> 2;
     const int64_t e = ((int64_t)blockIdx.x - block_base[pi]) * 256 + threadIdx.x;
     if (e >= mq * n) return;
-    const int64_t j = e / mq, i0 = (e - j * mq) * 4;
+    // 32-bit division while the index fits (the 64-bit one is a library call)
+    const int64_t j = (mq * n <= 0xFFFFFFFFll) ? (int64_t)((uint32_t)e / (uint32_t)mq) : e / mq;
+    const int64_t i0 = (e - j * mq) * 4;
     const int64_t plane_stride = n * q.ld;
     const int32_t* src = q.planes + j * q.ld + i0;  // ld is a multiple of 4: 16-byte aligned
     int4 v[S];
