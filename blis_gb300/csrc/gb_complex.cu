@@ -97,6 +97,8 @@ int real_gemm<double>(int64_t m, int64_t n, int64_t k, const double* a, const do
 template <>
 int real_gemm<float>(int64_t m, int64_t n, int64_t k, const float* a, const float* b, float* c, int, cudaStream_t s)
 {
+    // the engine sgemm itself would take for this shape (gb_set_sgemm_mode)
+    if (sgemm_use_split(m, n, k)) return sgemm_split_dev(m, n, k, 1.0f, a, 1, m, b, 1, k, 0.0f, c, 1, m, s);
     return sgemm_dev(m, n, k, 1.0f, a, 1, m, b, 1, k, 0.0f, c, 1, m, s);
 }
 

@@ -159,6 +159,8 @@ template <>
 int real_gemm_cm<float>(int64_t m, int64_t n, int64_t k, float alpha, const float* a, int64_t lda, const float* b,
                         int64_t ldb, float beta, float* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
 {
+    // the engine sgemm itself would take for this shape (gb_set_sgemm_mode)
+    if (sgemm_use_split(m, n, k)) return sgemm_split_dev(m, n, k, alpha, a, 1, lda, b, 1, ldb, beta, c, rs_c, cs_c, s);
     return sgemm_dev(m, n, k, alpha, a, 1, lda, b, 1, ldb, beta, c, rs_c, cs_c, s);
 }
 

@@ -467,7 +467,7 @@ def run_complex(out):
         b = torch.complex(_mat(n, n, seed=73, dtype=torch.float64), _mat(n, n, seed=74, dtype=torch.float64)).to(dt)
         a, b = a.t().contiguous().t(), b.t().contiguous().t()
         c = torch.zeros((n, n), dtype=dt, device="cuda").t()
-        forms = _forms(((0, "native_fp64"), (1, "ozaki_s7")) if dt == torch.complex128 else ((0, "native_fp32"),))
+        forms = _forms(((0, "native_fp64"), (1, "ozaki_s7")) if dt == torch.complex128 else ((0, "fp32_default_dispatch"),))
         for mode, form in forms:
             L.gb_set_dgemm_mode(mode, 7)
             if dt == torch.complex128:
