@@ -92,3 +92,35 @@ def test_split_sgemm_nonfinite_propagates():
     ref = a.astype(np.float64) @ b.astype(np.float64)
     assert np.array_equal(np.isnan(c), np.isnan(ref))
     assert np.array_equal(np.isinf(c), np.isinf(ref))
+
+
+@pytest.mark.parametrize("ta,tb", [(0, 0), (8, 8)])
+def test_split_sgemm_general_strides_bit_exact(gblib, ta, tb):
+    """The splits read op(A) and op(B) in the caller's memory: element strides other than one
+    on both dimensions (a general-stride A, B and C), against the model."""
+    torch = pytest.importorskip("torch")
+    from blis_gb300 import _lib
+    m, n, k = 300, 170, 700
+    a = po.uniform((k, m) if ta else (m, k), 21, dtype=np.float32)
+    b = po.uniform((n, k) if tb else (k, n), 22, dtype=np.float32)
+    c0 = po.uniform((m, n), 23, dtype=np.float32)
+
+    def strided(x, rs, cs):
+        # x(i, j) at buf[i*rs + j*cs] of a device buffer
+        buf = torch.zeros((x.shape[0] - 1) * rs + (x.shape[1] - 1) * cs + 1, dtype=torch.float32)
+        idx = (np.arange(x.shape[0])[:, None] * rs + np.arange(x.shape[1])[None, :] * cs).ravel()
+        buf[torch.from_numpy(idx)] = torch.from_numpy(np.ascontiguousarray(x).ravel())
+        return buf.cuda(), idx
+
+    A, _ = strided(a, 3, 3 * a.shape[0] + 5)
+    B, _ = strided(b, 2 * b.shape[1] + 1, 2)
+    C, cidx = strided(c0, 2, 2 * m + 3)
+    L = _lib.load()
+    assert L.gb_sgemm_dev(ta, tb, m, n, k, 1.5, A.data_ptr(), 3, 3 * a.shape[0] + 5, B.data_ptr(),
+                          2 * b.shape[1] + 1, 2, 0.0, C.data_ptr(), 2, 2 * m + 3, None) == 0
+    assert L.gb_synchronize() == 0
+    got = C.cpu().numpy()[cidx].reshape(m, n)
+    p = np.zeros((m, n), order="F")
+    po.ozaki_dgemm(ta, tb, 1.0, np.asfortranarray(a, dtype=np.float64), np.asfortranarray(b, dtype=np.float64),
+                   0.0, p, S)
+    assert np.array_equal(got, (np.float64(1.5) * p).astype(np.float32))
