@@ -124,3 +124,32 @@ def test_split_sgemm_general_strides_bit_exact(gblib, ta, tb):
     po.ozaki_dgemm(ta, tb, 1.0, np.asfortranarray(a, dtype=np.float64), np.asfortranarray(b, dtype=np.float64),
                    0.0, p, S)
     assert np.array_equal(got, (np.float64(1.5) * p).astype(np.float32))
+
+
+def test_split_sgemm_k_beyond_one_part_bit_exact():
+    """k = 50000 exceeds one exact k part at 3 slices (43648): the levels are summed over two
+    parts and the recombination still rounds once, bit-exact against the model."""
+    m, n, k = 70, 90, 50000
+    a = po.uniform((m, k), 31, dtype=np.float32)
+    b = po.uniform((k, n), 32, dtype=np.float32)
+    assert k > po.ozaki_kpart_limit(S)
+    c = np.zeros((m, n), dtype=np.float32, order="F")
+    blas.sgemm("N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m)
+    p = np.zeros((m, n), order="F")
+    po.ozaki_dgemm(0, 0, 1.0, np.asfortranarray(a, dtype=np.float64), np.asfortranarray(b, dtype=np.float64), 0.0,
+                   p, S)
+    assert np.array_equal(c, p.astype(np.float32))
+
+
+def test_split_sgemm_alpha_zero_and_k_zero():
+    """alpha = 0 (A and B not read: NaN there changes nothing) and k = 0 scale C by beta."""
+    m, n, k = 40, 30, 20
+    a = np.full((m, k), np.nan, dtype=np.float32, order="F")
+    b = np.full((k, n), np.nan, dtype=np.float32, order="F")
+    c0 = po.uniform((m, n), 33, dtype=np.float32)
+    c = np.asfortranarray(c0.copy())
+    blas.sgemm("N", "N", m, n, k, 0.0, a, m, b, k, 0.5, c, m)
+    assert np.array_equal(c, (np.float32(0.5) * c0).astype(np.float32))
+    c = np.asfortranarray(c0.copy())
+    blas.sgemm("N", "N", m, n, 0, 2.0, a, m, b, 1, -1.0, c, m)
+    assert np.array_equal(c, -c0)
