@@ -386,8 +386,13 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = flops * ws / (ms * 1e-3) / 1e12
+    # the product runs as one slice GEMM launch, or as one per block of C (the device entry
+    # points' blocked form at large sizes): the algorithmic flops of a launch are the step's
+    # divided by the launches per step
     kern_ms = gemm_ms / max(1, gemm_n)
-    achieved = npairs * flops / (kern_ms * 1e-3) / 1e12
+    launches_per_step = max(1.0, gemm_n / max(1, args.steps))
+    flops_per_launch = npairs * flops / launches_per_step
+    achieved = flops_per_launch / (kern_ms * 1e-3) / 1e12
     peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
 
     # ---------------- end to end through dgemm_ with pinned host buffers
@@ -430,7 +435,9 @@ def run_gpu(args):
     # and columns over all of k, in the same tiling), writes with the int32 planes, (n/4096)^2 per
     # plane
     rd, wr, prods, planes = TRAFFIC_4096[form]
+    # (per step; a block product moves its share of it: the same tiling over its rows and columns)
     traffic = rd * (n / 4096.0) ** 3 * npairs / prods + wr * (n / 4096.0) ** 2 * (npairs if form == "crt" else s) / planes
+    traffic /= launches_per_step
 
     if rank != 0:
         if ws > 1:
@@ -483,9 +490,14 @@ def run_gpu(args):
         "roofline": {"bound": "tensor", "kernel": "ozaki_slice_gemm", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "%s bf16_tflops_sustained" % peak_kind,
-                     "kernel_ms": kern_ms, "algorithmic_flops_per_launch": npairs * flops,
+                     "kernel_ms": kern_ms, "algorithmic_flops_per_launch": flops_per_launch,
+                     "launches_per_step": launches_per_step,
                      "split_recombine_ms_per_step": (split_ms / max(1, args.steps)),
-                     "stage_ms_per_step": stage_ms},
+                     "stage_ms_per_step": stage_ms,
+                     "timing_note": "CUDA-event span of each launch on its own stream; with the product in "
+                                    "blocks on two compute streams the spans overlap one another, so kernel_ms "
+                                    "and the stage times are upper bounds and achieved a lower bound"
+                                    if launches_per_step > 1 else "CUDA-event span of each launch"},
         "cpu_baseline": {"value": cpu_tf, "unit": "TFLOP/s", "cores": threads, "kind": cpu_kind,
                          "sample": cpu_sample},
         "cpu_baseline_port": {"value": port_tf, "unit": "TFLOP/s", "cores": threads, "kind": "port",

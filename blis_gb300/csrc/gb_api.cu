@@ -208,7 +208,11 @@ int ozaki_host_pipelined(int transa, int64_t m, int64_t n, int64_t k, double alp
 // SMs with the next block's first (a 4096 x 4096 block is 256 tiles of
 // 256 x 256, 3.4 waves of 76 CTA pairs); the splits run on a third stream as
 // the blocks land, and each product waits only for the splits it reads.
-// Rows and columns are split independently: bit-identical to one call.
+// Rows and columns are split independently: with finite operands the result
+// is bit-identical to one call.  Each block product is gated on the Inf/NaN
+// flags of its own row and column blocks (ozaki_flag_or): a flag shared by
+// all blocks could be raised by a later block's split between one product's
+// recombination and its gated fallback, applying beta twice.
 int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double alpha, const double* a,
                             int64_t lda, const double* b, int64_t ldb, double beta, double* c, int64_t ldc,
                             int slices, int nch, const char* where)
@@ -233,6 +237,16 @@ int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double 
     }
     rb.push_back(m);
     const int na = (int)rb.size() - 1;
+    // Inf/NaN flags: one per row block, per column block and per block product
+    int* flags = rc ? nullptr : static_cast<int*>(dev_alloc(sizeof(int) * (size_t)(na + nch + na * nch), s));
+    if (!rc && !flags) rc = GB_ERR_NOMEM;
+    if (!rc) rc = check_cuda(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(na + nch + na * nch), s), "flags");
+    int *fa = flags, *fb = flags + na, *fab = flags + na + nch;
+    auto with_flag = [&](int* f) {
+        OzA x = prep;
+        x.nonfinite = f;
+        return x;
+    };
     // events: A blocks in, B blocks in, A blocks split, B blocks split, C blocks done, then
     // the allocation, the two copy streams' ends, the second compute stream's end and the
     // split stream's end
@@ -283,13 +297,15 @@ int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double 
         // splits on their own stream, in arrival order: A0, B0, the other A blocks, the other B blocks
         auto split_a = [&](int i) {
             cudaStreamWaitEvent(ss, ev_a[i], 0);
-            if (!rc) rc = ozaki_split_a_rows(&prep, rb[i], rb[i + 1], ss);
+            const OzA ai = with_flag(fa + i);
+            if (!rc) rc = ozaki_split_a_rows(&ai, rb[i], rb[i + 1], ss);
             cudaEventRecord(ev_sa[i], ss);
         };
         auto split_b = [&](int j) {
             const int64_t j0 = col0(j), nj = col0(j + 1) - j0;
             cudaStreamWaitEvent(ss, ev_b[j], 0);
-            if (!rc) rc = ozaki_prepare_b(&prep, nj, bd + j0 * k, 1, k, ss, &pb[(size_t)j]);
+            const OzA aj = with_flag(fb + j);
+            if (!rc) rc = ozaki_prepare_b(&aj, nj, bd + j0 * k, 1, k, ss, &pb[(size_t)j]);
             cudaEventRecord(ev_sb[j], ss);
         };
         int q = 0;  // product stream of the next block
@@ -299,7 +315,10 @@ int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double 
             q ^= 1;
             cudaStreamWaitEvent(ps, ev_sa[i], 0);
             cudaStreamWaitEvent(ps, ev_sb[j], 0);
-            if (!rc) rc = ozaki_multiply_rows(&prep, r0, rows, &pb[(size_t)j], alpha, beta, cd + j0 * m + r0, 1, m, ps);
+            int* f = fab + i * nch + j;
+            if (!rc) rc = ozaki_flag_or(fa + i, fb + j, f, ps);
+            const OzA aij = with_flag(f);
+            if (!rc) rc = ozaki_multiply_rows(&aij, r0, rows, &pb[(size_t)j], alpha, beta, cd + j0 * m + r0, 1, m, ps);
             cudaEventRecord(ev_c[i * nch + j], ps);
             cudaStreamWaitEvent(cout, ev_c[i * nch + j], 0);
             LaunchScope ls("copy_d2h_c", cout, false);
@@ -326,6 +345,7 @@ int ozaki_host_pipelined_2d(int transa, int64_t m, int64_t n, int64_t k, double 
     }
     for (auto& x : pb) ozaki_release_b(&x, s);
     ozaki_release_a(&prep, s);
+    dev_free(flags, s);
     dev_free(ad, s);
     dev_free(bd, s);
     dev_free(cd, s);
@@ -1894,8 +1914,8 @@ int gb_dgemm_ozaki_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_
     // points (the CRT form has its own entry point)
     gb::ModeOverride form(GB_DGEMM_OZAKI, slices, 0);
     const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
-    return gb::dgemm_ozaki(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
-                           tb ? rs_b : cs_b, beta, c, rs_c, cs_c, slices, pick_stream(stream));
+    return gb::dgemm_ozaki_blocks(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
+                                  tb ? rs_b : cs_b, beta, c, rs_c, cs_c, slices, pick_stream(stream));
 }
 
 int gb_dgemm_ozaki_crt_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
@@ -1909,8 +1929,8 @@ int gb_dgemm_ozaki_crt_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_
     if (moduli < 2 || moduli > 16) return gb::set_error(GB_ERR_ARG, "gb_dgemm_ozaki_crt_dev", "moduli must be in [2, 16]");
     gb::ModeOverride form(GB_DGEMM_OZAKI, moduli, 1);
     const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
-    return gb::dgemm_ozaki(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
-                           tb ? rs_b : cs_b, beta, c, rs_c, cs_c, moduli, pick_stream(stream));
+    return gb::dgemm_ozaki_blocks(m, n, k, alpha, a, ta ? cs_a : rs_a, ta ? rs_a : cs_a, b, tb ? cs_b : rs_b,
+                                  tb ? rs_b : cs_b, beta, c, rs_c, cs_c, moduli, pick_stream(stream));
 }
 
 int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,

@@ -291,6 +291,10 @@ int ozaki_digit_slices();
 constexpr int GB_SGEMM_SPLIT_SLICES = 3;
 extern int sgemm_mode_setting;  // GB_SGEMM_FMA, _SPLIT or _AUTO (gb_set_sgemm_mode)
 bool sgemm_use_split(int64_t m, int64_t n, int64_t k);
+int ozaki_flag_or(const int* fa, const int* fb, int* out, cudaStream_t s);  // out = *fa | *fb, on s
+int dgemm_ozaki_blocks(int64_t m, int64_t n, int64_t k, double alpha, const double* a, int64_t ars, int64_t acs,
+                       const double* b, int64_t brs, int64_t bcs, double beta, double* c, int64_t rs_c, int64_t cs_c,
+                       int slices, cudaStream_t s);  // gb_ozaki.cu: dgemm_ozaki in blocks on three streams
 int sgemm_ozaki(int64_t m, int64_t n, int64_t k, float alpha, const float* a, int64_t ars, int64_t acs,
                 const float* b, int64_t brs, int64_t bcs, float beta, float* c, int64_t rs_c, int64_t cs_c,
                 cudaStream_t s);  // gb_ozaki.cu

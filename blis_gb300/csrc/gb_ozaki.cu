@@ -2812,6 +2812,132 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
     return rc;
 }
 
+namespace {
+
+__global__ void oz_flag_or_kernel(const int* __restrict__ fa, const int* __restrict__ fb, int* __restrict__ out)
+{
+    *out = (*fa | *fb) ? 1 : 0;
+}
+
+}  // namespace
+
+// out = fa | fb on s: the Inf/NaN flag of one block product of a blocked
+// Ozaki product, from the flags of the row block and the column block it
+// reads (each raised by that block's own split, complete before the product).
+// A flag shared by all blocks could be raised by a later block's split
+// between one product's recombination and its gated fallback.
+int ozaki_flag_or(const int* fa, const int* fb, int* out, cudaStream_t s)
+{
+    oz_flag_or_kernel<<<1, 1, 0, s>>>(fa, fb, out);
+    return check_cuda(cudaGetLastError(), "ozaki flag");
+}
+
+// The Ozaki form of dgemm_ozaki on device buffers in blocks, for the device
+// entry points' large products: op(A) in row blocks and op(B) in column
+// blocks, split on a stream of their own, every (row block, column block) of C
+// one slice GEMM with its recombination and gated fallback, the block
+// products alternating between the caller's stream and a second compute
+// stream.  One block's recombination and the later blocks' splits then run
+// beside another block's product instead of before and after the whole one
+// (the host entry points' pipeline, without the copies).  Rows and columns
+// are split independently, so with finite operands the result is
+// bit-identical to dgemm_ozaki; a block whose row or column block holds an
+// Inf or NaN is computed by the native kernel (ozaki_flag_or), the others
+// stay in the Ozaki form.  Stream-ordered on s: nothing here waits for the device.
+int dgemm_ozaki_blocks(int64_t m, int64_t n, int64_t k, double alpha, const double* a, int64_t ars, int64_t acs,
+                       const double* b, int64_t brs, int64_t bcs, double beta, double* c, int64_t rs_c, int64_t cs_c,
+                       int slices, cudaStream_t s)
+{
+    const int nch = (n >= 8192) ? 4 : ((n >= 4096) ? 2 : 1);
+    if (m <= 0 || n <= 0 || alpha == 0.0 || k <= 0 || nch < 2 || m < 2048)
+        return dgemm_ozaki(m, n, k, alpha, a, ars, acs, b, brs, bcs, beta, c, rs_c, cs_c, slices, s);
+    EngineScope engine(t_ozaki_ctas ? t_ozaki_ctas : ozaki_engine_choice(m / 4, n / nch, k));
+    cudaStream_t sp[2] = {s, thread_aux_stream(0)}, ss = thread_aux_stream(1);
+    OzA prep;
+    int rc = ozaki_alloc_a(m, k, a, ars, acs, slices, s, &prep);
+    if (rc) return rc;
+    // row blocks on the slice GEMM's row tile
+    const int nra = (m >= 8 * prep.row_tile) ? 4 : ((m >= 2 * prep.row_tile) ? 2 : 1);
+    std::vector<int64_t> rb(1, 0);
+    for (int i = 1; i < nra; ++i) {
+        const int64_t r = (m * i / nra + prep.row_tile - 1) / prep.row_tile * prep.row_tile;
+        if (r > rb.back() && r < m) rb.push_back(r);
+    }
+    rb.push_back(m);
+    const int na = (int)rb.size() - 1;
+    // Inf/NaN flags: one per row block, per column block and per block product
+    int* flags = static_cast<int*>(dev_alloc(sizeof(int) * (size_t)(na + nch + na * nch), s));
+    if (!flags) {
+        ozaki_release_a(&prep, s);
+        return GB_ERR_NOMEM;
+    }
+    rc = check_cuda(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(na + nch + na * nch), s), "memset flags");
+    int *fa = flags, *fb = flags + na, *fab = flags + na + nch;
+    auto with_flag = [&](int* f) {
+        OzA x = prep;
+        x.nonfinite = f;
+        return x;
+    };
+    // events: the fork, A blocks split, B blocks split, the second compute stream's and the
+    // split stream's ends
+    std::vector<cudaEvent_t> ev((size_t)(1 + na + nch + 2), nullptr);
+    for (auto& e : ev)
+        if (!rc) rc = check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "ozaki blocks events");
+    cudaEvent_t ev_fork = ev[0], *ev_sa = ev.data() + 1, *ev_sb = ev_sa + na, ev_aux_done = ev_sb[nch],
+                ev_split_done = ev_sb[nch + 1];
+    auto col0 = [&](int j) { return n * j / nch; };
+    std::vector<OzB> pb((size_t)nch);
+    if (!rc) {
+        // the other streams start after the caller's work so far and prep's allocation
+        cudaEventRecord(ev_fork, s);
+        cudaStreamWaitEvent(sp[1], ev_fork, 0);
+        cudaStreamWaitEvent(ss, ev_fork, 0);
+        for (int i = 0; i < na && !rc; ++i) {
+            const OzA ai = with_flag(fa + i);
+            rc = ozaki_split_a_rows(&ai, rb[i], rb[i + 1], ss);
+            cudaEventRecord(ev_sa[i], ss);
+            if (i == 0) {  // op(B)'s first block right after A's first: the first product needs only these
+                const int64_t nj = col0(1);
+                const OzA a0 = with_flag(fb);
+                if (!rc) rc = ozaki_prepare_b(&a0, nj, b, brs, bcs, ss, &pb[0]);
+                cudaEventRecord(ev_sb[0], ss);
+            }
+        }
+        for (int j = 1; j < nch && !rc; ++j) {
+            const int64_t j0 = col0(j), nj = col0(j + 1) - j0;
+            const OzA aj = with_flag(fb + j);
+            rc = ozaki_prepare_b(&aj, nj, b + j0 * bcs, brs, bcs, ss, &pb[(size_t)j]);
+            cudaEventRecord(ev_sb[j], ss);
+        }
+        int q = 0;
+        for (int j = 0; j < nch && !rc; ++j)
+            for (int i = 0; i < na && !rc; ++i) {
+                const int64_t j0 = col0(j), r0 = rb[i], rows = rb[i + 1] - rb[i];
+                cudaStream_t ps = sp[q];
+                q ^= 1;
+                cudaStreamWaitEvent(ps, ev_sa[i], 0);
+                cudaStreamWaitEvent(ps, ev_sb[j], 0);
+                int* f = fab + i * nch + j;
+                rc = ozaki_flag_or(fa + i, fb + j, f, ps);
+                const OzA aij = with_flag(f);
+                if (!rc)
+                    rc = ozaki_multiply_rows(&aij, r0, rows, &pb[(size_t)j], alpha, beta, c + r0 * rs_c + j0 * cs_c,
+                                             rs_c, cs_c, ps);
+            }
+        // the join is recorded whatever happened, so s never runs ahead of the other streams
+        cudaEventRecord(ev_aux_done, sp[1]);
+        cudaEventRecord(ev_split_done, ss);
+        cudaStreamWaitEvent(s, ev_aux_done, 0);
+        cudaStreamWaitEvent(s, ev_split_done, 0);
+    }
+    for (auto& x : pb) ozaki_release_b(&x, s);
+    ozaki_release_a(&prep, s);
+    dev_free(flags, s);
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    return rc;
+}
+
 // SGEMM's split form on the FP32 operands themselves: the digit form at
 // GB_SGEMM_SPLIT_SLICES slices splits op(A) and op(B) straight from FP32
 // (each element widened exactly as it loads), the slice GEMM runs as for
