@@ -2848,8 +2848,25 @@ int dgemm_ozaki_blocks(int64_t m, int64_t n, int64_t k, double alpha, const doub
                        const double* b, int64_t brs, int64_t bcs, double beta, double* c, int64_t rs_c, int64_t cs_c,
                        int slices, cudaStream_t s)
 {
-    const int nch = (n >= 8192) ? 4 : ((n >= 4096) ? 2 : 1);
-    if (m <= 0 || n <= 0 || alpha == 0.0 || k <= 0 || nch < 2 || m < 2048)
+    // GB_OZAKI_DEV_BLOCKS=RxC fixes the row and column block counts (1x1: one product); read
+    // per call (one getenv against a large product)
+    int fix_r = 0, fix_c = 0;
+    {
+        const char* e = getenv("GB_OZAKI_DEV_BLOCKS");
+        int r = 0, cc = 0;
+        if (e && sscanf(e, "%dx%d", &r, &cc) == 2 && r >= 1 && r <= 8 && cc >= 1 && cc <= 8) {
+            fix_r = r;
+            fix_c = cc;
+        }
+    }
+    // 8 row blocks x 4 column blocks where they measured faster than one product on GB300
+    // (ms, 8192^3 / 16384^3: digit form s = 7 19.9 -> 18.7 at 8192; CRT form, 16 moduli, 94.6 ->
+    // 87.1 at 16384 but 12.7 -> 13.6 at 8192, where the blocks' smaller products lose more than
+    // the overlap saves); one product otherwise
+    const int big = (ozaki_form() == 1) ? 16384 : 8192;
+    int nch = (m >= big && n >= big) ? 4 : 1;
+    if (fix_c) nch = (int)((fix_c < n) ? fix_c : 1);
+    if (m <= 0 || n <= 0 || alpha == 0.0 || k <= 0 || nch < 2 || m < 2048 || (fix_r == 1 && fix_c == 1))
         return dgemm_ozaki(m, n, k, alpha, a, ars, acs, b, brs, bcs, beta, c, rs_c, cs_c, slices, s);
     EngineScope engine(t_ozaki_ctas ? t_ozaki_ctas : ozaki_engine_choice(m / 4, n / nch, k));
     cudaStream_t sp[2] = {s, thread_aux_stream(0)}, ss = thread_aux_stream(1);
@@ -2857,7 +2874,7 @@ int dgemm_ozaki_blocks(int64_t m, int64_t n, int64_t k, double alpha, const doub
     int rc = ozaki_alloc_a(m, k, a, ars, acs, slices, s, &prep);
     if (rc) return rc;
     // row blocks on the slice GEMM's row tile
-    const int nra = (m >= 8 * prep.row_tile) ? 4 : ((m >= 2 * prep.row_tile) ? 2 : 1);
+    const int nra = fix_r ? fix_r : 8;  // m >= 8192: row blocks of at least 1024 rows
     std::vector<int64_t> rb(1, 0);
     for (int i = 1; i < nra; ++i) {
         const int64_t r = (m * i / nra + prep.row_tile - 1) / prep.row_tile * prep.row_tile;

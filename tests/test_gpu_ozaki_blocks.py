@@ -17,9 +17,16 @@ from oracle import pyoracle as po
 
 pytestmark = pytest.mark.gpu
 
-# m >= 2048 and n >= 4096 take the blocked form; m is not a multiple of the 256-row tile and n
-# splits unevenly, so the last row and column blocks are ragged
+# The default takes blocks from 8192 (digit form) or 16384 (CRT form); GB_OZAKI_DEV_BLOCKS fixes
+# the grid here at a size the CPU models finish quickly.  m is not a multiple of the 256-row tile
+# and n splits unevenly, so the last row and column blocks are ragged.
 M, NN, K = 2600, 4100, 300
+
+
+@pytest.fixture(autouse=True, params=["4x2", "8x3"])
+def blocks(request, monkeypatch):
+    monkeypatch.setenv("GB_OZAKI_DEV_BLOCKS", request.param)
+    yield request.param
 
 
 def _dev(x):
