@@ -2854,7 +2854,7 @@ int dgemm_ozaki_blocks(int64_t m, int64_t n, int64_t k, double alpha, const doub
     {
         const char* e = getenv("GB_OZAKI_DEV_BLOCKS");
         int r = 0, cc = 0;
-        if (e && sscanf(e, "%dx%d", &r, &cc) == 2 && r >= 1 && r <= 8 && cc >= 1 && cc <= 8) {
+        if (e && sscanf(e, "%dx%d", &r, &cc) == 2 && r >= 1 && r <= 16 && cc >= 1 && cc <= 16) {
             fix_r = r;
             fix_c = cc;
         }
