@@ -371,7 +371,7 @@ def run_batch(out):
 def run_batch_large_fp32(out):
     """FP32 gemm_batch of 64 problems with m, n, k log-uniform in [1024, 4096]:
     the FP32-pipe grouped plan (policy 0) against the split form (policy 3:
-    widen, grouped Ozaki at 3 slices, round), and the plan's autotuned pick."""
+    the grouped Ozaki form at 3 slices on the FP32 operands), and the plan's autotuned pick."""
     L = _lib.load()
     probs, keep, flops = batch_problems(64, 5, 1, lo=1024, hi=4096)
     st = _stream()

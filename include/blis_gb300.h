@@ -497,7 +497,12 @@ int gb_dgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
    slices, products on the tcgen05 tensor cores, exact integer level sums,
    FP64 recombination.  Always the digit form, whatever form
    gb_set_dgemm_mode chose for the host entry points (the CRT form is
-   gb_dgemm_ozaki_crt_dev).  No reference counterpart (precision form). */
+   gb_dgemm_ozaki_crt_dev).  From m, n >= 8192 (CRT form: 16384) the product
+   runs in 8 x 4 blocks of C on the calling thread's stream and two more of
+   its streams, forked from and joined to `stream` (GB_OZAKI_DEV_BLOCKS fixes
+   the grid): the same bits on finite operands; a block whose rows of op(A) or
+   columns of op(B) hold an Inf or NaN is computed by the native kernel, the
+   others stay in the Ozaki form.  No reference counterpart (precision form). */
 int gb_dgemm_ozaki_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n,
                        gb_dim_t k, double alpha, const double* a, gb_inc_t rs_a,
                        gb_inc_t cs_a, const double* b, gb_inc_t rs_b, gb_inc_t cs_b,
@@ -508,7 +513,7 @@ int gb_dgemm_ozaki_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_
    are scaled to t-bit integers, t = the largest with k 2^(2t) <= 8 M / 17 for
    the product M of the moduli (t = 55 for 16 moduli at k = 16384), and the
    result is the single rounding of their exact integer product.  k must be at
-   most 131072. */
+   most 131072.  Large products run in blocks as for gb_dgemm_ozaki_dev. */
 int gb_dgemm_ozaki_crt_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k,
                            double alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* b,
                            gb_inc_t rs_b, gb_inc_t cs_b, double beta, double* c, gb_inc_t rs_c,
