@@ -90,7 +90,7 @@ template <>
 int real_gemm<double>(int64_t m, int64_t n, int64_t k, const double* a, const double* b, double* c, int slices,
                       cudaStream_t s)
 {
-    if (slices > 0) return dgemm_ozaki(m, n, k, 1.0, a, 1, m, b, 1, k, 0.0, c, 1, m, slices, s);
+    if (slices > 0) return dgemm_ozaki_blocks(m, n, k, 1.0, a, 1, m, b, 1, k, 0.0, c, 1, m, slices, s);
     return dgemm_native(m, n, k, 1.0, a, 1, m, b, 1, k, 0.0, c, 1, m, s);
 }
 

@@ -2859,12 +2859,14 @@ int dgemm_ozaki_blocks(int64_t m, int64_t n, int64_t k, double alpha, const doub
             fix_c = cc;
         }
     }
-    // 8 row blocks x 4 column blocks where they measured faster than one product on GB300
-    // (ms, 8192^3 / 16384^3: digit form s = 7 19.9 -> 18.7 at 8192; CRT form, 16 moduli, 94.6 ->
-    // 87.1 at 16384 but 12.7 -> 13.6 at 8192, where the blocks' smaller products lose more than
-    // the overlap saves); one product otherwise
-    const int big = (ozaki_form() == 1) ? 16384 : 8192;
-    int nch = (m >= big && n >= big) ? 4 : 1;
+    // 8 row blocks x up to 4 column blocks where they measured faster than one product on GB300
+    // (ms: digit form s = 7 at 8192^3 19.9 -> 18.7 in 8 x 4, ZGEMM 4096^3's real 8192 x 4096 x
+    // 8192 product 9.40 -> 9.16 in 8 x 2; CRT form, 16 moduli, 94.6 -> 87.1 at 16384^3 but
+    // 12.7 -> 13.6 at 8192^3, where the blocks' smaller products lose more than the overlap
+    // saves); one product otherwise
+    const bool crt = (ozaki_form() == 1);
+    int nch = crt ? ((m >= 16384 && n >= 16384) ? 4 : 1)
+                  : ((m >= 8192 && n >= 4096) ? (int)std::min<int64_t>(4, n / 2048) : 1);
     if (fix_c) nch = (int)((fix_c < n) ? fix_c : 1);
     if (m <= 0 || n <= 0 || alpha == 0.0 || k <= 0 || nch < 2 || m < 2048 || (fix_r == 1 && fix_c == 1))
         return dgemm_ozaki(m, n, k, alpha, a, ars, acs, b, brs, bcs, beta, c, rs_c, cs_c, slices, s);
