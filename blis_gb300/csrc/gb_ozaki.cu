@@ -2832,6 +2832,20 @@ int ozaki_flag_or(const int* fa, const int* fb, int* out, cudaStream_t s)
     return check_cuda(cudaGetLastError(), "ozaki flag");
 }
 
+// GB_OZAKI_DEV_BLOCKS=RxC fixes the row and column block counts of the
+// blocked forms (1x1: one product); read per call (one getenv against a
+// large product).  Unset or malformed: *r = *c = 0.
+void ozaki_fixed_blocks(int* r, int* c)
+{
+    *r = *c = 0;
+    const char* e = getenv("GB_OZAKI_DEV_BLOCKS");
+    int rr = 0, cc = 0;
+    if (e && sscanf(e, "%dx%d", &rr, &cc) == 2 && rr >= 1 && rr <= 16 && cc >= 1 && cc <= 16) {
+        *r = rr;
+        *c = cc;
+    }
+}
+
 // The Ozaki form of dgemm_ozaki on device buffers in blocks, for the device
 // entry points' large products: op(A) in row blocks and op(B) in column
 // blocks, split on a stream of their own, every (row block, column block) of C
@@ -2848,17 +2862,8 @@ int dgemm_ozaki_blocks(int64_t m, int64_t n, int64_t k, double alpha, const doub
                        const double* b, int64_t brs, int64_t bcs, double beta, double* c, int64_t rs_c, int64_t cs_c,
                        int slices, cudaStream_t s)
 {
-    // GB_OZAKI_DEV_BLOCKS=RxC fixes the row and column block counts (1x1: one product); read
-    // per call (one getenv against a large product)
     int fix_r = 0, fix_c = 0;
-    {
-        const char* e = getenv("GB_OZAKI_DEV_BLOCKS");
-        int r = 0, cc = 0;
-        if (e && sscanf(e, "%dx%d", &r, &cc) == 2 && r >= 1 && r <= 16 && cc >= 1 && cc <= 16) {
-            fix_r = r;
-            fix_c = cc;
-        }
-    }
+    ozaki_fixed_blocks(&fix_r, &fix_c);
     // 8 row blocks x up to 4 column blocks where they measured faster than one product on GB300
     // (ms: digit form s = 7 at 8192^3 19.9 -> 18.7 in 8 x 4, ZGEMM 4096^3's real 8192 x 4096 x
     // 8192 product 9.40 -> 9.16 in 8 x 2; CRT form, 16 moduli, 94.6 -> 87.1 at 16384^3 but
@@ -2963,6 +2968,98 @@ int dgemm_ozaki_blocks(int64_t m, int64_t n, int64_t k, double alpha, const doub
 // dgemm_ozaki, and the recombination writes C = RN32(alpha P + beta C) from
 // the FP64 product P, the rounding of the form through FP64 copies; Inf/NaN
 // operands raise the flag and an FP32 kernel gated on it computes C instead.
+namespace {
+
+// sgemm_ozaki in blocks, as dgemm_ozaki_blocks: op(A)'s row blocks and
+// op(B)'s column blocks split from FP32 on a stream of their own, one slice
+// GEMM with its FP32 recombination per block of C on two compute streams,
+// each block gated on its own row and column blocks' Inf/NaN flags.
+int sgemm_ozaki_blocks(int na_req, int nch, int64_t m, int64_t n, int64_t k, float alpha, const float* a, int64_t ars,
+                       int64_t acs, const float* b, int64_t brs, int64_t bcs, float beta, float* c, int64_t rs_c,
+                       int64_t cs_c, cudaStream_t s)
+{
+    constexpr int S = GB_SGEMM_SPLIT_SLICES;
+    cudaStream_t sp[2] = {s, thread_aux_stream(0)}, ss = thread_aux_stream(1);
+    OzA A;
+    int rc = ozaki_alloc_a(m, k, nullptr, ars, acs, S, s, &A);
+    if (rc) return rc;
+    std::vector<int64_t> rb(1, 0);
+    for (int i = 1; i < na_req; ++i) {
+        const int64_t r = (m * i / na_req + A.row_tile - 1) / A.row_tile * A.row_tile;
+        if (r > rb.back() && r < m) rb.push_back(r);
+    }
+    rb.push_back(m);
+    const int na = (int)rb.size() - 1;
+    int* flags = static_cast<int*>(dev_alloc(sizeof(int) * (size_t)(na + nch + na * nch), s));
+    if (!flags) {
+        ozaki_release_a(&A, s);
+        return GB_ERR_NOMEM;
+    }
+    rc = check_cuda(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(na + nch + na * nch), s), "memset flags");
+    int *fa = flags, *fb = flags + na, *fab = flags + na + nch;
+    std::vector<cudaEvent_t> ev((size_t)(1 + na + nch + 2), nullptr);
+    for (auto& e : ev)
+        if (!rc) rc = check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "sgemm blocks events");
+    cudaEvent_t ev_fork = ev[0], *ev_sa = ev.data() + 1, *ev_sb = ev_sa + na, ev_aux_done = ev_sb[nch],
+                ev_split_done = ev_sb[nch + 1];
+    auto col0 = [&](int j) { return n * j / nch; };
+    std::vector<OzB> pb((size_t)nch);
+    if (!rc) {
+        cudaEventRecord(ev_fork, s);
+        cudaStreamWaitEvent(sp[1], ev_fork, 0);
+        cudaStreamWaitEvent(ss, ev_fork, 0);
+        auto split_b = [&](int j) {
+            const int64_t j0 = col0(j), nj = col0(j + 1) - j0;
+            if (!rc) rc = ozaki_alloc_b(&A, nj, nullptr, brs, bcs, ss, &pb[(size_t)j]);
+            if (!rc) {  // rows of op(B)^T: (j, l) = b[l*brs + j*bcs]
+                OzB& B = pb[(size_t)j];
+                split_operand_f32(nj, k, b + j0 * bcs, bcs, brs, B.maxb, B.npad, B.npad, A.kpad, B.sb, B.eb, fb + j, ss);
+                rc = check_cuda(cudaGetLastError(), "oz_split");
+            }
+            cudaEventRecord(ev_sb[j], ss);
+        };
+        for (int i = 0; i < na && !rc; ++i) {
+            const int64_t r0 = rb[i], r1 = rb[i + 1];
+            const int64_t cover = (r1 == m ? A.mpad : r1) - r0;
+            split_operand_f32(r1 - r0, k, a + r0 * ars, ars, acs, A.maxa + r0, A.mpad, cover, A.kpad,
+                              A.sa + r0 * A.kpad, A.ea + r0, fa + i, ss);
+            rc = check_cuda(cudaGetLastError(), "oz_split");
+            cudaEventRecord(ev_sa[i], ss);
+            if (i == 0) split_b(0);  // the first product needs only A's and op(B)'s first blocks
+        }
+        for (int j = 1; j < nch && !rc; ++j) split_b(j);
+        int q = 0;
+        for (int j = 0; j < nch && !rc; ++j)
+            for (int i = 0; i < na && !rc; ++i) {
+                const int64_t j0 = col0(j), r0 = rb[i], rows = rb[i + 1] - rb[i];
+                cudaStream_t ps = sp[q];
+                q ^= 1;
+                cudaStreamWaitEvent(ps, ev_sa[i], 0);
+                cudaStreamWaitEvent(ps, ev_sb[j], 0);
+                int* f = fab + i * nch + j;
+                rc = ozaki_flag_or(fa + i, fb + j, f, ps);
+                OzA aij = A;
+                aij.nonfinite = f;
+                const OzF32 f32{a, b + j0 * bcs, c + r0 * rs_c + j0 * cs_c};
+                if (!rc)
+                    rc = multiply_rows_impl(&aij, r0, rows, &pb[(size_t)j], (double)alpha, (double)beta, nullptr, rs_c,
+                                            cs_c, &f32, ps);
+            }
+        cudaEventRecord(ev_aux_done, sp[1]);
+        cudaEventRecord(ev_split_done, ss);
+        cudaStreamWaitEvent(s, ev_aux_done, 0);
+        cudaStreamWaitEvent(s, ev_split_done, 0);
+    }
+    for (auto& x : pb) ozaki_release_b(&x, s);
+    ozaki_release_a(&A, s);
+    dev_free(flags, s);
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    return rc;
+}
+
+}  // namespace
+
 int sgemm_ozaki(int64_t m, int64_t n, int64_t k, float alpha, const float* a, int64_t ars, int64_t acs,
                 const float* b, int64_t brs, int64_t bcs, float beta, float* c, int64_t rs_c, int64_t cs_c,
                 cudaStream_t s)
@@ -2971,6 +3068,20 @@ int sgemm_ozaki(int64_t m, int64_t n, int64_t k, float alpha, const float* a, in
     if (alpha == 0.0f || k <= 0) return scal_matrix_f(m, n, beta, c, rs_c, cs_c, s);
     constexpr int S = GB_SGEMM_SPLIT_SLICES;
     ModeOverride digits(GB_DGEMM_OZAKI, S, 0);
+    int br = 0, bc = 0;
+    ozaki_fixed_blocks(&br, &bc);
+    if (!br) {
+        // 4 x 2 blocks from 8192: 4.29-4.35 -> 4.22 ms at 8192^3 (2 x 2, 2 x 4, 4 x 4 no better,
+        // 8 x 4 worse: six products per block leave less to overlap than the FP64 forms' 16-28)
+        const bool big = (m >= 8192 && n >= 8192);
+        br = big ? 4 : 1;
+        bc = big ? 2 : 1;
+    }
+    if (bc > n) bc = 1;
+    if (br * bc > 1 && m >= 2048) {
+        EngineScope engine(t_ozaki_ctas ? t_ozaki_ctas : ozaki_engine_choice(m / br, n / bc, k));
+        return sgemm_ozaki_blocks(br, bc, m, n, k, alpha, a, ars, acs, b, brs, bcs, beta, c, rs_c, cs_c, s);
+    }
     EngineScope engine(t_ozaki_ctas ? t_ozaki_ctas : ozaki_engine_choice(m, n, k));
     OzA A;
     int rc = ozaki_alloc_a(m, k, nullptr, ars, acs, S, s, &A);

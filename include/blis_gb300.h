@@ -811,7 +811,8 @@ int gb_set_dgemm_mode(int mode, int slices);
    digit form with 3 slices, six bf16 products with exact integer
    accumulation, then C = RN32(alpha P + beta C) from the FP64 product P); GB_SGEMM_AUTO (default) the split form
    when m, n >= 1024 and k >= 512, the FMA kernel otherwise.  Host and device
-   sgemm entry points follow it. */
+   sgemm entry points follow it; from m, n >= 8192 the split form runs in 4 x 2
+   blocks of C on three streams, as gb_dgemm_ozaki_dev's blocked form. */
 #define GB_SGEMM_FMA 0
 #define GB_SGEMM_SPLIT 1
 #define GB_SGEMM_AUTO 2

@@ -153,3 +153,41 @@ def test_split_sgemm_alpha_zero_and_k_zero():
     c = np.asfortranarray(c0.copy())
     blas.sgemm("N", "N", m, n, 0, 2.0, a, m, b, 1, -1.0, c, m)
     assert np.array_equal(c, -c0)
+
+
+@pytest.mark.parametrize("grid", ["4x2", "3x3"])
+def test_split_sgemm_blocked_bit_exact(grid, monkeypatch):
+    """The blocked form (row blocks of op(A), column blocks of op(B), two compute streams),
+    forced at a size the model finishes quickly, with ragged last blocks: the same bits."""
+    monkeypatch.setenv("GB_OZAKI_DEV_BLOCKS", grid)
+    m, n, k = 2600, 1100, 700
+    a = po.expspread((m, k), 51, -12, 12).astype(np.float32)
+    b = po.uniform((k, n), 52, dtype=np.float32)
+    c0 = po.uniform((m, n), 53, dtype=np.float32)
+    c = np.asfortranarray(c0.copy())
+    blas.sgemm("N", "N", m, n, k, 1.0, a, m, b, k, 0.0, c, m)
+    p = np.zeros((m, n), order="F")
+    po.ozaki_dgemm(0, 0, 1.0, np.asfortranarray(a, dtype=np.float64), np.asfortranarray(b, dtype=np.float64), 0.0,
+                   p, S)
+    assert np.array_equal(c, p.astype(np.float32))
+
+
+def test_split_sgemm_blocked_nonfinite_with_beta(monkeypatch):
+    """Blocks whose rows of op(A) or columns of op(B) hold an Inf or NaN take the FP32 pipe, the
+    others the split form, and beta enters once everywhere."""
+    monkeypatch.setenv("GB_OZAKI_DEV_BLOCKS", "4x2")
+    m, n, k = 2600, 1100, 300
+    a = po.uniform((m, k), 54, dtype=np.float32)
+    b = po.uniform((k, n), 55, dtype=np.float32)
+    c0 = po.uniform((m, n), 56, dtype=np.float32)
+    a[m - 3, 5] = np.inf
+    b[7, n - 2] = np.nan
+    c = np.asfortranarray(c0.copy())
+    blas.sgemm("N", "N", m, n, k, 1.0, a, m, b, k, 0.5, c, m)
+    ref = a.astype(np.float64) @ b.astype(np.float64) + 0.5 * c0.astype(np.float64)
+    assert np.array_equal(np.isnan(c), np.isnan(ref)) and np.array_equal(np.isinf(c), np.isinf(ref))
+    fin = np.isfinite(ref)
+    af = np.where(np.isfinite(a), np.abs(a), 0).astype(np.float64)
+    bf = np.where(np.isfinite(b), np.abs(b), 0).astype(np.float64)
+    gauge = af @ bf + 0.5 * np.abs(c0.astype(np.float64))
+    assert np.all(np.abs(c[fin].astype(np.float64) - ref[fin]) <= 2 * (k + 2) * U32 * gauge[fin])
