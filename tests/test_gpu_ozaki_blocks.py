@@ -34,7 +34,7 @@ def _dev(x):
     return torch.from_numpy(np.asfortranarray(x).T.copy()).cuda()  # column-major storage
 
 
-def _run(crt, count, ta, a, b, alpha, beta, c0):
+def _run(crt, count, ta, a, b, alpha, beta, c0, tb=False):
     torch = pytest.importorskip("torch")
     L = _lib.load()
     A, B, Cd = _dev(a), _dev(b), _dev(c0)
@@ -46,23 +46,24 @@ def _run(crt, count, ta, a, b, alpha, beta, c0):
                    C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.c_void_p, C.c_int64, C.c_int64,
                    C.c_int, C.c_void_p]
     torch.cuda.synchronize()
-    assert fn(8 if ta else 0, 0, m, n, k, alpha, A.data_ptr(), 1, a.shape[0], B.data_ptr(), 1, b.shape[0], beta,
-              Cd.data_ptr(), 1, m, count, None) == 0
+    assert fn(8 if ta else 0, 8 if tb else 0, m, n, k, alpha, A.data_ptr(), 1, a.shape[0], B.data_ptr(), 1,
+              b.shape[0], beta, Cd.data_ptr(), 1, m, count, None) == 0
     assert L.gb_synchronize() == 0
     return Cd.cpu().numpy().T
 
 
-@pytest.mark.parametrize("crt,count,ta", [(False, 5, False), (True, 12, False), (True, 16, True)])
-def test_blocked_form_bit_exact_vs_model(gblib, crt, count, ta):
+@pytest.mark.parametrize("crt,count,ta,tb", [(False, 5, False, False), (True, 12, False, True), (True, 16, True, False),
+                                             (False, 7, True, True)])
+def test_blocked_form_bit_exact_vs_model(gblib, crt, count, ta, tb):
     a = po.expspread((K, M) if ta else (M, K), 41)
-    b = po.expspread((K, NN), 42)
+    b = po.expspread((NN, K) if tb else (K, NN), 42)
     c0 = po.uniform((M, NN), 43)
-    got = _run(crt, count, ta, a, b, 1.25, -0.5, c0)
+    got = _run(crt, count, ta, a, b, 1.25, -0.5, c0, tb)
     ref = np.asfortranarray(c0.copy())
     if crt:
-        po.ozaki_crt_dgemm(8 if ta else 0, 0, 1.25, a, b, -0.5, ref, count)
+        po.ozaki_crt_dgemm(8 if ta else 0, 8 if tb else 0, 1.25, a, b, -0.5, ref, count)
     else:
-        po.ozaki_dgemm(8 if ta else 0, 0, 1.25, a, b, -0.5, ref, count)
+        po.ozaki_dgemm(8 if ta else 0, 8 if tb else 0, 1.25, a, b, -0.5, ref, count)
     assert np.array_equal(got, ref)
 
 
