@@ -56,6 +56,10 @@ SEED_A, SEED_B = 20261204, 20261205
 # of that launch: the digit form at 7 slices (28 products, 7 level planes) and the CRT form at 16
 # moduli (16 products, 16 planes)
 TRAFFIC_4096 = {"digits": (7136346112, 473230848, 28, 7), "crt": (1368333000, 532505600, 16, 16)}
+# One block product of the CRT form's blocked layout (2048 x 4096 x 8192, 16 moduli) moved 2.75 GB
+# from DRAM (ncu, SpeedOfLight + MemoryWorkloadAnalysis: dram__bytes.sum.per_second x duration);
+# a block launch of another size is scaled by its units m_b n_b k
+TRAFFIC_CRT_BLOCK = (2.752e9, 2048 * 4096 * 8192, 16)
 
 
 def parse():
@@ -438,6 +442,10 @@ def run_gpu(args):
     # (per step; a block product moves its share of it: the same tiling over its rows and columns)
     traffic = rd * (n / 4096.0) ** 3 * npairs / prods + wr * (n / 4096.0) ** 2 * (npairs if form == "crt" else s) / planes
     traffic /= launches_per_step
+    if form == "crt" and launches_per_step > 1:
+        # the blocked form's launch, from the capture of one block product scaled by its units
+        tb, units, mod = TRAFFIC_CRT_BLOCK
+        traffic = tb * (float(n) ** 3 / launches_per_step) / units * npairs / mod
 
     if rank != 0:
         if ws > 1:
