@@ -56,10 +56,10 @@ SEED_A, SEED_B = 20261204, 20261205
 # of that launch: the digit form at 7 slices (28 products, 7 level planes) and the CRT form at 16
 # moduli (16 products, 16 planes)
 TRAFFIC_4096 = {"digits": (7136346112, 473230848, 28, 7), "crt": (1368333000, 532505600, 16, 16)}
-# One block product of the CRT form's blocked layout (2048 x 4096 x 8192, 16 moduli) moved 2.75 GB
+# One block product of the CRT form's blocked layout (2048 x 4096 x 8192, 16 moduli) moved 2.78 GB
 # from DRAM (ncu, SpeedOfLight + MemoryWorkloadAnalysis: dram__bytes.sum.per_second x duration);
 # a block launch of another size is scaled by its units m_b n_b k
-TRAFFIC_CRT_BLOCK = (2.752e9, 2048 * 4096 * 8192, 16)
+TRAFFIC_CRT_BLOCK = (2.782e9, 2048 * 4096 * 8192, 16)
 
 
 def parse():

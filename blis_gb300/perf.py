@@ -47,6 +47,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SMALL = False  # --small: profiling sizes (inputs still larger than the 126 MB L2)
 TRSM_FORMS = ("native", "ozaki")  # --trsm-forms: which DTRSM forms the trsm suites time
 FORMS = ("native", "ozaki")  # --forms: which forms the level3x, hermitian and complex suites time
+CRT_N = 0  # --crt-n: size of the crt suite's product (0: 16384, or 4096 with --small)
 
 
 def _forms(pairs):
@@ -538,7 +539,7 @@ def run_crt(out):
     """The CRT form of the Ozaki product alone, 16 moduli, exponent-spread operands (the
     benchmark's inputs) at 16384^3, or 4096^3 with --small (the profiling case: each of the
     split, slice GEMM and recombination kernels launches once per product, three products)."""
-    n = 4096 if SMALL else 16384
+    n = CRT_N or (4096 if SMALL else 16384)
     a = _mat(n, n, kind=dev.RAND_EXPSPREAD, seed=61, p0=-20, p1=20)
     b = _mat(n, n, kind=dev.RAND_EXPSPREAD, seed=62, p0=-20, p1=20)
     c = _mat(n, n, seed=63)
@@ -601,11 +602,13 @@ def main():
     ap.add_argument("--json")
     ap.add_argument("--batch-count", type=int, default=4096, help="problems of the batch_ozaki suite")
     ap.add_argument("--small", action="store_true", help="profiling sizes (workload names keep the full size)")
+    ap.add_argument("--crt-n", type=int, default=0, help="size of the crt suite's product (0: 16384, 4096 with --small)")
     ap.add_argument("--trsm-forms", default="native,ozaki", help="DTRSM forms of the trsm suites")
     ap.add_argument("--forms", default="native,ozaki", help="forms of the level3x, hermitian and complex suites")
     a = ap.parse_args()
-    global BATCH_COUNT, SMALL, TRSM_FORMS, FORMS
+    global BATCH_COUNT, SMALL, TRSM_FORMS, FORMS, CRT_N
     BATCH_COUNT = a.batch_count
+    CRT_N = a.crt_n
     SMALL = a.small
     TRSM_FORMS = tuple(f for f in a.trsm_forms.split(",") if f)
     FORMS = tuple(f for f in a.forms.split(",") if f)
