@@ -2616,6 +2616,7 @@ int multiply_rows_impl(const OzA* A, int64_t r0, int64_t rows, const OzB* B, dou
         p.tiles_valid = (int)tiles;
         p.tile_cum = tab;
         p.tile_first = tab + p.tiles_m + 1;
+        LaunchScope ls("oz_tri_tiles", s);
         oz_tri_tiles_kernel<<<1, 1, 0, s>>>(p.tiles_m, p.tiles_n, A->row_tile, m, A->out_rpc, A->out_tri, tab,
                                             tab + p.tiles_m + 1);
     }
@@ -2729,6 +2730,7 @@ int multiply_rows_impl(const OzA* A, int64_t r0, int64_t rows, const OzB* B, dou
                 if (!rc) {
                     int64_t blocks = (dr * w + 255) / 256;
                     if (blocks > 4096) blocks = 4096;
+                    LaunchScope ls("oz_tri_merge_gated", s);
                     oz_tri_merge_gated_kernel<<<(unsigned)blocks, 256, 0, s>>>(dr, w, d0, j0, lower ? 1 : 0, (int)rpc,
                                                                                d, beta, c, rs_c, cs_c, A->nonfinite);
                     rc = check_cuda(cudaGetLastError(), "ozaki triangle fallback");
@@ -2828,6 +2830,7 @@ __global__ void oz_flag_or_kernel(const int* __restrict__ fa, const int* __restr
 // between one product's recombination and its gated fallback.
 int ozaki_flag_or(const int* fa, const int* fb, int* out, cudaStream_t s)
 {
+    LaunchScope ls("oz_flag_or", s);
     oz_flag_or_kernel<<<1, 1, 0, s>>>(fa, fb, out);
     return check_cuda(cudaGetLastError(), "ozaki flag");
 }
