@@ -2872,9 +2872,12 @@ int dgemm_ozaki_blocks(int64_t m, int64_t n, int64_t k, double alpha, const doub
     // 8192 product 9.40 -> 9.16 in 8 x 2; CRT form, 16 moduli, 94.6 -> 87.1 at 16384^3 but
     // 12.7 -> 13.6 at 8192^3, where the blocks' smaller products lose more than the overlap
     // saves); one product otherwise
+    // (every grid measured had k >= 8192; below k = 2048 the blocks' launches would outweigh
+    // the overlap, so one product)
     const bool crt = (ozaki_form() == 1);
-    int nch = crt ? ((m >= 16384 && n >= 16384) ? 4 : 1)
-                  : ((m >= 8192 && n >= 4096) ? (int)std::min<int64_t>(4, n / 2048) : 1);
+    int nch = (k < 2048) ? 1
+                         : crt ? ((m >= 16384 && n >= 16384) ? 4 : 1)
+                               : ((m >= 8192 && n >= 4096) ? (int)std::min<int64_t>(4, n / 2048) : 1);
     if (fix_c) nch = (int)((fix_c < n) ? fix_c : 1);
     if (m <= 0 || n <= 0 || alpha == 0.0 || k <= 0 || nch < 2 || m < 2048 || (fix_r == 1 && fix_c == 1))
         return dgemm_ozaki(m, n, k, alpha, a, ars, acs, b, brs, bcs, beta, c, rs_c, cs_c, slices, s);
@@ -3076,7 +3079,7 @@ int sgemm_ozaki(int64_t m, int64_t n, int64_t k, float alpha, const float* a, in
     if (!br) {
         // 4 x 2 blocks from 8192: 4.29-4.35 -> 4.22 ms at 8192^3 (2 x 2, 2 x 4, 4 x 4 no better,
         // 8 x 4 worse: six products per block leave less to overlap than the FP64 forms' 16-28)
-        const bool big = (m >= 8192 && n >= 8192);
+        const bool big = (m >= 8192 && n >= 8192 && k >= 2048);
         br = big ? 4 : 1;
         bc = big ? 2 : 1;
     }

@@ -497,8 +497,8 @@ int gb_dgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
    slices, products on the tcgen05 tensor cores, exact integer level sums,
    FP64 recombination.  Always the digit form, whatever form
    gb_set_dgemm_mode chose for the host entry points (the CRT form is
-   gb_dgemm_ozaki_crt_dev).  From m >= 8192 and n >= 4096 (CRT form: both
-   16384) the product runs in 8 x 2..4 blocks of C on `stream` and two more of
+   gb_dgemm_ozaki_crt_dev).  From m >= 8192, n >= 4096 and k >= 2048 (CRT
+   form: m, n >= 16384) the product runs in 8 x 2..4 blocks of C on `stream` and two more of
    the calling thread's streams, forked from and joined to it (GB_OZAKI_DEV_BLOCKS fixes
    the grid): the same bits on finite operands; a block whose rows of op(A) or
    columns of op(B) hold an Inf or NaN is computed by the native kernel, the
