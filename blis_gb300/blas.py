@@ -55,6 +55,11 @@ def dtrsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
                        C.byref(C.c_double(alpha)), _p(a), _i(lda), _p(b), _i(ldb))
 
 
+def strsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
+    _lib.load().strsm_(_c(side), _c(uplo), _c(transa), _c(diag), _i(m), _i(n),
+                       C.byref(C.c_float(alpha)), _p(a), _i(lda), _p(b), _i(ldb))
+
+
 def _cscalar(v, dtype):
     return np.array([v], dtype=dtype)
 

@@ -553,6 +553,27 @@ int trsm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     return finish(s, "trsm");
 }
 
+// strsm on host buffers: the operands staged into HBM, strsm_dev (native FP32 recursion)
+int strsm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, float alpha, const float* a,
+               int64_t rs_a, int64_t cs_a, float* b, int64_t rs_b, int64_t cs_b, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const int64_t na = (side == GB_LEFT) ? m : n;
+    Staged& B = bufs.next();
+    if ((rc = stage_in(b, m, n, rs_b, cs_b, 4, alpha != 0.0f, &B, s))) return rc;
+    Staged& A = bufs.next();
+    if (alpha != 0.0f && (rc = stage_in(a, na, na, rs_a, cs_a, 4, true, &A, s))) return rc;
+    if ((rc = strsm_dev(side, uplo, transa, diag, m, n, alpha, reinterpret_cast<const float*>(A.origin), A.rs,
+                        A.cs, reinterpret_cast<float*>(B.origin), B.rs, B.cs, s)))
+        return rc;
+    if ((rc = stage_out(b, m, n, rs_b, cs_b, 4, B, s))) return rc;
+    return finish(s, where);
+}
+
 int level3_slices() { return (dgemm_mode() == GB_DGEMM_OZAKI) ? ozaki_slices() : 0; }
 
 int trmm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, double alpha, const double* a,
@@ -1119,6 +1140,33 @@ void dtrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char
               unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, *n, *alpha, a, 1, *lda, b, 1, *ldb);
 }
 
+void strsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const float* alpha,
+            const float* a, const gb_f77_int* lda, float* b, const gb_f77_int* ldb)
+{
+    // the argument checks of dtrsm_ (frame/compat/check/bla_trmm_check.h:37-86)
+    const bool left = lsame(*side, 'L'), right = lsame(*side, 'R');
+    const bool lower = lsame(*uploa, 'L'), upper = lsame(*uploa, 'U');
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T'), conja = lsame(*transa, 'C');
+    const bool unita = lsame(*diaga, 'U'), nonua = lsame(*diaga, 'N');
+    const int nrowa = left ? *m : *n;
+    int info = 0;
+    if (!left && !right) info = 1;
+    else if (!lower && !upper) info = 2;
+    else if (!nota && !ta && !conja) info = 3;
+    else if (!unita && !nonua) info = 4;
+    else if (*m < 0) info = 5;
+    else if (*n < 0) info = 6;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 9;
+    else if (*ldb < (*m > 1 ? *m : 1)) info = 11;
+    if (info) {
+        call_xerbla("STRSM ", info);
+        return;
+    }
+    strsm_host(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, map_trans(*transa),
+               unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, *n, *alpha, a, 1, *lda, b, 1, *ldb, "strsm_");
+}
+
 void zgemm_(const gb_f77_char* transa, const gb_f77_char* transb, const gb_f77_int* m, const gb_f77_int* n,
             const gb_f77_int* k, const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda,
             const gb_dcomplex* b, const gb_f77_int* ldb, const gb_dcomplex* beta, gb_dcomplex* c,
@@ -1575,6 +1623,13 @@ void bli_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t dia
     trsm_host(side, uploa, transa, diaga, m, n, *alpha, a, rs_a, cs_a, b, rs_b, cs_b);
 }
 
+void bli_strsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+               gb_dim_t n, const float* alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a,
+               float* b, gb_inc_t rs_b, gb_inc_t cs_b)
+{
+    strsm_host(side, uploa, transa, diaga, m, n, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, "bli_strsm");
+}
+
 void bli_dtrsm_ex(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
                   gb_dim_t n, const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
                   double* b, gb_inc_t rs_b, gb_inc_t cs_b, const void* cntx, const void* rntm)
@@ -1850,6 +1905,13 @@ void gb_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diag
     trsm_host(side, uploa, transa, diaga, m, n, *alpha, a, rs_a, cs_a, b, rs_b, cs_b);
 }
 
+void gb_strsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+              gb_dim_t n, const float* alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a,
+              float* b, gb_inc_t rs_b, gb_inc_t cs_b)
+{
+    strsm_host(side, uploa, transa, diaga, m, n, *alpha, a, rs_a, cs_a, b, rs_b, cs_b, "gb_strsm");
+}
+
 void gb_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
               const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b,
               gb_inc_t rs_b, gb_inc_t cs_b)
@@ -1963,6 +2025,16 @@ int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
     const int slices = (gb::dgemm_mode() == GB_DGEMM_OZAKI) ? gb::ozaki_slices() : 0;
     return gb::dtrsm_dev(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, slices,
                          pick_stream(stream));
+}
+
+int gb_strsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+                 gb_dim_t n, float alpha, const float* a, gb_inc_t rs_a, gb_inc_t cs_a, float* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_strsm_dev", "negative dimension");
+    return gb::strsm_dev(side, uploa, transa, diaga, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, pick_stream(stream));
 }
 
 int gb_zgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_dim_t k, gb_dcomplex alpha,

@@ -121,6 +121,8 @@ int dgemm_ozaki(int64_t m, int64_t n, int64_t k, double alpha,
 int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, double alpha,
               const double* a, int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b,
               int64_t cs_b, int slices, cudaStream_t s);
+int strsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, float alpha, const float* a,
+              int64_t rs_a, int64_t cs_a, float* b, int64_t rs_b, int64_t cs_b, cudaStream_t s);  // gb_trsm.cu
 int64_t ozaki_kpart_limit(int slices);
 // Lanes per right-hand side (1, 2, 4, 8) for the 64-row diagonal-block
 // kernels of trsm and trmm, from the FP64-instruction cost model (gb_trsm.cu).

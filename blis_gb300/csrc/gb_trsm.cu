@@ -36,33 +36,34 @@ constexpr int64_t TRSM_SPLIT_MIN_COLS = 1024;  // columns per half for the two-s
 // the identity rows that pad a short last block), P[r][i] = a_ri inv(a_ii)
 // inside the strict triangle and 0 elsewhere.  The scaling lets the solve
 // work on y = D X (D = diag(a)) with a unit triangle; see trsm_diag_kernel.
-template <bool LOWER>
-__global__ void __launch_bounds__(256) trsm_pack_diag_kernel(int64_t m, int unit, const double* __restrict__ a,
-                                                             int64_t ars, int64_t acs, double* __restrict__ packed)
+// E is double, or float for strsm.
+template <typename E, bool LOWER>
+__global__ void __launch_bounds__(256) trsm_pack_diag_kernel(int64_t m, int unit, const E* __restrict__ a,
+                                                             int64_t ars, int64_t acs, E* __restrict__ packed)
 {
-    __shared__ double T[TRSM_NB][TRSM_NB + 1];
-    __shared__ double dinv[TRSM_NB];
+    __shared__ E Tb[TRSM_NB][TRSM_NB + 1];
+    __shared__ E dinv[TRSM_NB];
     const int64_t r0 = (int64_t)blockIdx.x * TRSM_NB;
     const int nb = (m - r0 < TRSM_NB) ? (int)(m - r0) : TRSM_NB;
-    const double* blk = a + r0 * ars + r0 * acs;
+    const E* blk = a + r0 * ars + r0 * acs;
     const bool rows_fast = (ars == 1);
     for (int e = threadIdx.x; e < TRSM_NB * TRSM_NB; e += 256) {
         const int i = rows_fast ? e % TRSM_NB : e / TRSM_NB, l = rows_fast ? e / TRSM_NB : e % TRSM_NB;
         const bool keep = (i < nb && l < nb) && (LOWER ? (l <= i) : (l >= i));
-        T[i][l] = keep ? blk[i * ars + l * acs] : 0.0;
+        Tb[i][l] = keep ? blk[i * ars + l * acs] : E(0);
     }
     __syncthreads();
     if (threadIdx.x < TRSM_NB) {
         const int i = threadIdx.x;
-        dinv[i] = (unit || i >= nb) ? 1.0 : 1.0 / T[i][i];
+        dinv[i] = (unit || i >= nb) ? E(1) : E(1) / Tb[i][i];
     }
     __syncthreads();
-    double* out = packed + (int64_t)blockIdx.x * TRSM_NB * TRSM_NB;
+    E* out = packed + (int64_t)blockIdx.x * TRSM_NB * TRSM_NB;
     for (int e = threadIdx.x; e < TRSM_NB * TRSM_NB; e += 256) {
         const int r = e / TRSM_NB, i = e % TRSM_NB;
-        double v = 0.0;
+        E v = E(0);
         if (r == i) v = dinv[r];
-        else if (LOWER ? (i < r) : (i > r)) v = T[r][i] * dinv[i];
+        else if (LOWER ? (i < r) : (i > r)) v = Tb[r][i] * dinv[i];
         out[e] = v;
     }
 }
@@ -86,15 +87,15 @@ __global__ void __launch_bounds__(256) trsm_pack_diag_kernel(int64_t m, int unit
 // loops are unrolled, so every register index is a constant.
 constexpr int TRSM_THREADS = 128;
 
-template <int LANES, bool LOWER>
-__global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, const double* __restrict__ pk,
-                                                                 double* __restrict__ b, int64_t brs, int64_t bcs,
+template <typename E, int LANES, bool LOWER>
+__global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, const E* __restrict__ pk,
+                                                                 E* __restrict__ b, int64_t brs, int64_t bcs,
                                                                  int64_t ncols)
 {
     constexpr int COLS = TRSM_THREADS / LANES, R = TRSM_NB / LANES, LL = TRSM_NB + 1, LX = COLS + 1;
-    extern __shared__ double trsm_smem[];
-    double* L = trsm_smem;                 // [TRSM_NB][LL]
-    double* X = L + TRSM_NB * LL;          // [TRSM_NB][LX]
+    extern __shared__ __align__(16) unsigned char trsm_smem[];
+    E* L = reinterpret_cast<E*>(trsm_smem);  // [TRSM_NB][LL]
+    E* X = L + TRSM_NB * LL;                 // [TRSM_NB][LX]
     const int t = threadIdx.x;
     const int64_t j0 = (int64_t)blockIdx.x * COLS;
     const int cols = (ncols - j0 < COLS) ? (int)(ncols - j0) : COLS;
@@ -104,19 +105,19 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, const d
 #pragma unroll 8
     for (int e = t; e < TRSM_NB * COLS; e += TRSM_THREADS) {
         const int i = rows_fast ? e % TRSM_NB : e / COLS, c = rows_fast ? e / TRSM_NB : e % COLS;
-        X[i * LX + c] = (c < cols && i < nb) ? b[i * brs + (j0 + c) * bcs] : 0.0;
+        X[i * LX + c] = (c < cols && i < nb) ? b[i * brs + (j0 + c) * bcs] : E(0);
     }
     __syncthreads();
     const int c = t / LANES, g = t % LANES;  // the lanes of a column share a warp
     const int src0 = (t % 32) - g;           // the column's first lane within the warp
-    double x[R];
+    E x[R];
 #pragma unroll
     for (int q = 0; q < R; ++q) x[q] = X[(q * LANES + g) * LX + c];
 #pragma unroll
     for (int step = 0; step < TRSM_NB; ++step) {
         const int i = LOWER ? step : TRSM_NB - 1 - step;
         const int qi = i / LANES, gi = i % LANES;
-        double v = x[qi];
+        E v = x[qi];
         if constexpr (LANES > 1) v = __shfl_sync(0xffffffffu, v, src0 + gi);
 #pragma unroll
         for (int q = 0; q < R; ++q) {
@@ -140,25 +141,26 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_diag_kernel(int nb, const d
     }
 }
 
+template <typename E>
 constexpr size_t trsm_smem_bytes(int lanes)
 {
-    return sizeof(double) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB * (TRSM_THREADS / lanes + 1));
+    return sizeof(E) * (TRSM_NB * (TRSM_NB + 1) + TRSM_NB * (TRSM_THREADS / lanes + 1));
 }
 
-template <int LANES, bool LOWER>
-int launch_trsm_diag(int nb, const double* pk, double* b, int64_t brs, int64_t bcs, int64_t ncols, cudaStream_t s)
+template <typename E, int LANES, bool LOWER>
+int launch_trsm_diag(int nb, const E* pk, E* b, int64_t brs, int64_t bcs, int64_t ncols, cudaStream_t s)
 {
     static bool attr = false;
     if (!attr) {
-        const int rc = check_cuda(cudaFuncSetAttribute(trsm_diag_kernel<LANES, LOWER>,
+        const int rc = check_cuda(cudaFuncSetAttribute(trsm_diag_kernel<E, LANES, LOWER>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                       (int)trsm_smem_bytes(LANES)), "trsm smem attr");
+                                                       (int)trsm_smem_bytes<E>(LANES)), "trsm smem attr");
         if (rc) return rc;
         attr = true;
     }
     const int64_t blocks = (ncols + TRSM_THREADS / LANES - 1) / (TRSM_THREADS / LANES);
-    if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "dtrsm", "too many right-hand sides");
-    trsm_diag_kernel<LANES, LOWER><<<(unsigned)blocks, TRSM_THREADS, trsm_smem_bytes(LANES), s>>>(
+    if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "trsm", "too many right-hand sides");
+    trsm_diag_kernel<E, LANES, LOWER><<<(unsigned)blocks, TRSM_THREADS, trsm_smem_bytes<E>(LANES), s>>>(
         nb, pk, b, brs, bcs, ncols);
     return check_cuda(cudaGetLastError(), "trsm_diag");
 }
@@ -504,17 +506,17 @@ int diag_solve(const TrsmCtx& t, int64_t r0, int64_t mm)
     LaunchScope ls("trsm_diag", t.s);
     switch (diag_block_lanes(t.n)) {
     case 1:
-        return t.lower ? launch_trsm_diag<1, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                       : launch_trsm_diag<1, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+        return t.lower ? launch_trsm_diag<double, 1, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<double, 1, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
     case 2:
-        return t.lower ? launch_trsm_diag<2, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                       : launch_trsm_diag<2, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+        return t.lower ? launch_trsm_diag<double, 2, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<double, 2, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
     case 4:
-        return t.lower ? launch_trsm_diag<4, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                       : launch_trsm_diag<4, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+        return t.lower ? launch_trsm_diag<double, 4, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<double, 4, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
     default:
-        return t.lower ? launch_trsm_diag<8, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                       : launch_trsm_diag<8, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+        return t.lower ? launch_trsm_diag<double, 8, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<double, 8, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
     }
 }
 
@@ -660,9 +662,9 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     {
         LaunchScope ls("trsm_pack_diag", s);
         if (t.lower)
-            trsm_pack_diag_kernel<true><<<(unsigned)nblk, 256, 0, s>>>(mm, t.unit, a, t.ars, t.acs, packed);
+            trsm_pack_diag_kernel<double, true><<<(unsigned)nblk, 256, 0, s>>>(mm, t.unit, a, t.ars, t.acs, packed);
         else
-            trsm_pack_diag_kernel<false><<<(unsigned)nblk, 256, 0, s>>>(mm, t.unit, a, t.ars, t.acs, packed);
+            trsm_pack_diag_kernel<double, false><<<(unsigned)nblk, 256, 0, s>>>(mm, t.unit, a, t.ars, t.acs, packed);
     }
     int rc = check_cuda(cudaGetLastError(), "trsm_pack_diag");
     t.packed = packed;
@@ -715,6 +717,119 @@ int dtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, do
     for (cudaEvent_t e : ev)
         if (e) cudaEventDestroy(e);
     trsm_images_release(&images, s);
+    dev_free(packed, s);
+    return rc;
+}
+
+// STRSM on the GPU (the native form only): the recursion of dtrsm_dev at FP32
+// with the same packed diagonal blocks and diagonal-solve kernel, the updates
+// B2 -= op(A21) X1 through sgemm's own engine choice (gb_set_sgemm_mode: the
+// split form on the bf16 tensor cores for large updates, the FP32 FMA kernel
+// below), on the caller's stream.
+namespace {
+
+struct STrsmCtx {
+    const float* packed;
+    const float* a;
+    int64_t ars, acs;
+    float* b;
+    int64_t brs, bcs, n;
+    bool lower;
+    cudaStream_t s;
+};
+
+int s_diag_solve(const STrsmCtx& t, int64_t r0, int64_t mm)
+{
+    const float* pk = t.packed + (r0 / TRSM_NB) * TRSM_NB * TRSM_NB;
+    float* b1 = t.b + r0 * t.brs;
+    const int nb = (int)mm;
+    LaunchScope ls("trsm_diag", t.s);
+    switch (diag_block_lanes(t.n)) {
+    case 1:
+        return t.lower ? launch_trsm_diag<float, 1, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<float, 1, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+    case 2:
+        return t.lower ? launch_trsm_diag<float, 2, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<float, 2, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+    case 4:
+        return t.lower ? launch_trsm_diag<float, 4, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<float, 4, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+    default:
+        return t.lower ? launch_trsm_diag<float, 8, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                       : launch_trsm_diag<float, 8, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+    }
+}
+
+int s_update(const STrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t ccount)
+{
+    // B[r0:r0+rcount, :] -= op(A)[r0:.., c0:c0+ccount] * X[c0:c0+ccount, :]
+    const float* ap = t.a + r0 * t.ars + c0 * t.acs;
+    const float* xp = t.b + c0 * t.brs;
+    float* bp = t.b + r0 * t.brs;
+    if (sgemm_use_split(rcount, t.n, ccount))
+        return sgemm_split_dev(rcount, t.n, ccount, -1.0f, ap, t.ars, t.acs, xp, t.brs, t.bcs, 1.0f, bp, t.brs,
+                               t.bcs, t.s);
+    return sgemm_dev(rcount, t.n, ccount, -1.0f, ap, t.ars, t.acs, xp, t.brs, t.bcs, 1.0f, bp, t.brs, t.bcs, t.s);
+}
+
+int s_solve(const STrsmCtx& t, int64_t r0, int64_t mm)
+{
+    if (mm <= TRSM_NB) return s_diag_solve(t, r0, mm);
+    int64_t m1 = ((mm / 2 + TRSM_NB - 1) / TRSM_NB) * TRSM_NB;
+    if (m1 >= mm) m1 = mm - TRSM_NB;
+    const int64_t m2 = mm - m1;
+    int rc;
+    if (t.lower) {
+        if ((rc = s_solve(t, r0, m1)) || (rc = s_update(t, r0 + m1, m2, r0, m1))) return rc;
+        return s_solve(t, r0 + m1, m2);
+    }
+    if ((rc = s_solve(t, r0 + m1, m2)) || (rc = s_update(t, r0, m1, r0 + m1, m2))) return rc;
+    return s_solve(t, r0, m1);
+}
+
+}  // namespace
+
+int strsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, float alpha, const float* a,
+              int64_t rs_a, int64_t cs_a, float* b, int64_t rs_b, int64_t cs_b, cudaStream_t s)
+{
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    int64_t brs = rs_b, bcs = cs_b, mm = m, nn = n;
+    bool trans = GB_IS_TRANS(transa);
+    if (side == GB_RIGHT) {  // X op(A) = B  <=>  op(A)^T X^T = B^T
+        brs = cs_b;
+        bcs = rs_b;
+        mm = n;
+        nn = m;
+        trans = !trans;
+    }
+    if (alpha == 0.0f) return scal_matrix_f(mm, nn, 0.0f, b, brs, bcs, s);
+    int rc;
+    if (alpha != 1.0f && (rc = scal_matrix_f(mm, nn, alpha, b, brs, bcs, s))) return rc;
+    STrsmCtx t;
+    t.ars = trans ? cs_a : rs_a;
+    t.acs = trans ? rs_a : cs_a;
+    t.lower = (uplo == GB_LOWER) != trans;
+    t.a = a;
+    t.b = b;
+    t.brs = brs;
+    t.bcs = bcs;
+    t.n = nn;
+    t.s = s;
+    const int64_t nblk = (mm + TRSM_NB - 1) / TRSM_NB;
+    if (nblk > INT32_MAX) return set_error(GB_ERR_ARG, "strsm", "too many diagonal blocks");
+    float* packed = static_cast<float*>(dev_alloc(sizeof(float) * nblk * TRSM_NB * TRSM_NB, s));
+    if (!packed) return GB_ERR_NOMEM;
+    {
+        LaunchScope ls("trsm_pack_diag", s);
+        const int unit = (diag == GB_UNIT_DIAG) ? 1 : 0;
+        if (t.lower)
+            trsm_pack_diag_kernel<float, true><<<(unsigned)nblk, 256, 0, s>>>(mm, unit, a, t.ars, t.acs, packed);
+        else
+            trsm_pack_diag_kernel<float, false><<<(unsigned)nblk, 256, 0, s>>>(mm, unit, a, t.ars, t.acs, packed);
+    }
+    rc = check_cuda(cudaGetLastError(), "trsm_pack_diag");
+    t.packed = packed;
+    if (!rc) rc = s_solve(t, 0, mm);
     dev_free(packed, s);
     return rc;
 }

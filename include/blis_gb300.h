@@ -96,6 +96,11 @@ void dtrsm_(const gb_f77_char* side, const gb_f77_char* uploa,
             const gb_f77_char* transa, const gb_f77_char* diaga,
             const gb_f77_int* m, const gb_f77_int* n, const double* alpha,
             const double* a, const gb_f77_int* lda, double* b, const gb_f77_int* ldb);
+/* replaces strsm_ (the same macro instance of frame/compat/bla_trsm.c:121-219) */
+void strsm_(const gb_f77_char* side, const gb_f77_char* uploa,
+            const gb_f77_char* transa, const gb_f77_char* diaga,
+            const gb_f77_int* m, const gb_f77_int* n, const float* alpha,
+            const float* a, const gb_f77_int* lda, float* b, const gb_f77_int* ldb);
 
 /* replaces dtrmm_, frame/compat/bla_trmm.c:45-121 (checks
    frame/compat/check/bla_trmm_check.h:37-86): B := alpha op(A) B or alpha B op(A) */
@@ -406,6 +411,10 @@ void bli_dgemmt(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t 
 void bli_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
                gb_dim_t m, gb_dim_t n, const double* alpha, const double* a,
                gb_inc_t rs_a, gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b);
+/* replaces bli_strsm (frame/3/bli_l3_tapi_ex.c:533-586, float instance) */
+void bli_strsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
+               gb_dim_t m, gb_dim_t n, const float* alpha, const float* a,
+               gb_inc_t rs_a, gb_inc_t cs_a, float* b, gb_inc_t rs_b, gb_inc_t cs_b);
 void bli_dtrsm_ex(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
                   gb_dim_t m, gb_dim_t n, const double* alpha, const double* a,
                   gb_inc_t rs_a, gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b,
@@ -467,6 +476,9 @@ void gb_cgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_d
 void gb_dtrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
               gb_dim_t m, gb_dim_t n, const double* alpha, const double* a,
               gb_inc_t rs_a, gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b);
+void gb_strsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
+              gb_dim_t m, gb_dim_t n, const float* alpha, const float* a,
+              gb_inc_t rs_a, gb_inc_t cs_a, float* b, gb_inc_t rs_b, gb_inc_t cs_b);
 /* same as bli_ztrsm (frame/3/bli_l3_tapi_ex.c:533-586, complex instance) */
 void gb_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
               gb_dim_t m, gb_dim_t n, const gb_dcomplex* alpha, const gb_dcomplex* a,
@@ -528,6 +540,11 @@ int gb_sgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
 int gb_dtrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
                  gb_dim_t m, gb_dim_t n, double alpha, const double* a, gb_inc_t rs_a,
                  gb_inc_t cs_a, double* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
+/* The float instance (native form: FP32 diagonal solves of 64-row blocks,
+   updates through sgemm's engine choice, gb_set_sgemm_mode). */
+int gb_strsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
+                 gb_dim_t m, gb_dim_t n, float alpha, const float* a, gb_inc_t rs_a,
+                 gb_inc_t cs_a, float* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
 
 /* Device-pointer complex gemm (zgemm: native FP64 or the Ozaki form by
    gb_set_dgemm_mode with a fixed slice count; cgemm: FP32). */
