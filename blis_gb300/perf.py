@@ -186,6 +186,35 @@ def run_trsm(out):
     _lib.load().gb_set_dgemm_mode(0, 8)
 
 
+def run_strsm(out):
+    """STRSM L/L/N/N 8192 x 4096 in FP32 (m^2 n flop): the FP32 recursion, its updates through
+    sgemm's engine choice (the split form at size), against the same solve with every update on
+    the FP32 FMA kernel."""
+    import torch
+    m, n = (2048, 10240) if SMALL else (8192, 4096)
+    L = _mat(m, m, seed=11, dtype=torch.float32)
+    L.copy_(torch.tril(L))
+    d = torch.arange(m, device="cuda")
+    L[d, d] = m + L[d, d].abs()
+    b0 = _mat(m, n, seed=12, dtype=torch.float32)
+    flops = float(m) * m * n
+    lib = _lib.load()
+    for mode, name in ((blas.SGEMM_AUTO, "updates_default_dispatch"), (blas.SGEMM_FMA, "updates_ffma")):
+        blas.set_sgemm_mode(mode)
+        x = b0.clone()
+        st = _stream()
+
+        def call():
+            x.copy_(b0)
+            _lib.check(lib.gb_strsm_dev(0, 0xC0, 0, 0, m, n, 1.0, L.data_ptr(), 1, m, x.data_ptr(), 1, m, st),
+                       "gb_strsm_dev")
+        ms = _timer(call, reps=3, warmup=1)
+        copy_ms = _timer(lambda: x.copy_(b0), reps=3, warmup=1)
+        out.append({"workload": "strsm_%dx%d" % (m, n), "form": name, "ms": ms - copy_ms,
+                    "tflops": flops / (ms - copy_ms) / 1e9})
+    blas.set_sgemm_mode(blas.SGEMM_AUTO)
+
+
 def run_trsm_ozaki(out):
     """DTRSM L/L/N/N m = n = 16384: L as above (diagonal 16384+|u|), B with
     entries (1+u) 2^e, e in [-20, 20].  Native FP64 and Ozaki off-diagonal
@@ -589,7 +618,7 @@ def run_e2e(out, calls=8):
     out.append(rec)
 
 
-SUITES = {"crt": run_crt, "e2e": run_e2e, "gemm": run_gemm, "trsm": run_trsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
+SUITES = {"crt": run_crt, "e2e": run_e2e, "gemm": run_gemm, "trsm": run_trsm, "strsm": run_strsm, "trsm_ozaki": run_trsm_ozaki, "level12": run_level12,
           "batch": run_batch, "batch_fp32_large": run_batch_large_fp32, "batch_ozaki": run_batch_ozaki,
           "sgemm": run_sgemm, "bgemm": run_bgemm,
           "level3x": run_level3x, "level12x": run_level12x, "complex": run_complex, "hermitian": run_hermitian}
