@@ -84,9 +84,13 @@ def bli_zgemm(transa, transb, alpha, a, b, beta, c):
 
 
 def ztrsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
-    al = _cscalar(alpha, np.complex128)
-    _lib.load().ztrsm_(_c(side), _c(uplo), _c(transa), _c(diag), _i(m), _i(n), _p(al), _p(a), _i(lda), _p(b),
-                       _i(ldb))
+    """Complex trsm on complex128 (ztrsm_) or complex64 (ctrsm_) Fortran-order arrays, by b's dtype."""
+    fn = _lib.load().ztrsm_ if b.dtype == np.complex128 else _lib.load().ctrsm_
+    al = _cscalar(alpha, b.dtype)
+    fn(_c(side), _c(uplo), _c(transa), _c(diag), _i(m), _i(n), _p(al), _p(a), _i(lda), _p(b), _i(ldb))
+
+
+ctrsm = ztrsm
 
 
 def _real_dtype(c):

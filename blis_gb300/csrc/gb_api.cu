@@ -795,6 +795,27 @@ int ztrsm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, c
     return finish(s, where);
 }
 
+int ctrsm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const float* alpha, const float* a,
+               int64_t rs_a, int64_t cs_a, float* b, int64_t rs_b, int64_t cs_b, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const int64_t na = (side == GB_LEFT) ? m : n;
+    const bool nz = !(alpha[0] == 0.0f && alpha[1] == 0.0f);
+    Staged& B = bufs.next();
+    if ((rc = stage_in(b, m, n, rs_b, cs_b, 8, nz, &B, s))) return rc;
+    Staged& A = bufs.next();
+    if (nz && (rc = stage_in(a, na, na, rs_a, cs_a, 8, true, &A, s))) return rc;
+    if ((rc = ctrsm_dev(side, uplo, transa, diag, m, n, alpha, reinterpret_cast<const float*>(A.origin), A.rs, A.cs,
+                        reinterpret_cast<float*>(B.origin), B.rs, B.cs, s)))
+        return rc;
+    if ((rc = stage_out(b, m, n, rs_b, cs_b, 8, B, s))) return rc;
+    return finish(s, where);
+}
+
 // herk / her2k: the whole of C goes up and comes back, so the untouched
 // triangle round-trips unchanged
 template <typename T>
@@ -1222,6 +1243,34 @@ void ztrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char
     ztrsm_host(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, map_trans(*transa),
                unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, *n, &alpha->real, &a->real, 1, *lda, &b->real, 1, *ldb,
                "ZTRSM");
+}
+
+void ctrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const gb_scomplex* alpha,
+            const gb_scomplex* a, const gb_f77_int* lda, gb_scomplex* b, const gb_f77_int* ldb)
+{
+    // the argument checks of ztrsm_ (frame/compat/check/bla_trmm_check.h:37-86)
+    const bool left = lsame(*side, 'L'), right = lsame(*side, 'R');
+    const bool lower = lsame(*uploa, 'L'), upper = lsame(*uploa, 'U');
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T'), conja = lsame(*transa, 'C');
+    const bool unita = lsame(*diaga, 'U'), nonua = lsame(*diaga, 'N');
+    const int nrowa = left ? *m : *n;
+    int info = 0;
+    if (!left && !right) info = 1;
+    else if (!lower && !upper) info = 2;
+    else if (!nota && !ta && !conja) info = 3;
+    else if (!unita && !nonua) info = 4;
+    else if (*m < 0) info = 5;
+    else if (*n < 0) info = 6;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 9;
+    else if (*ldb < (*m > 1 ? *m : 1)) info = 11;
+    if (info) {
+        call_xerbla("CTRSM ", info);
+        return;
+    }
+    ctrsm_host(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, map_trans(*transa),
+               unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, *n, &alpha->real, &a->real, 1, *lda, &b->real, 1, *ldb,
+               "CTRSM");
 }
 
 void zherk_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
@@ -1663,6 +1712,14 @@ void bli_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t dia
                "bli_ztrsm");
 }
 
+void bli_ctrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+               const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_scomplex* b,
+               gb_inc_t rs_b, gb_inc_t cs_b)
+{
+    ctrsm_host(side, uploa, transa, diaga, m, n, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+               "bli_ctrsm");
+}
+
 // frame/3/bli_l3_tapi_ex.c herk / her2k / hemm / symm / syr2k (prototypes
 // frame/3/bli_l3_tapi_ex.h:62-168)
 void bli_zherk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const double* alpha, const gb_dcomplex* a,
@@ -1920,6 +1977,14 @@ void gb_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diag
                "gb_ztrsm");
 }
 
+void gb_ctrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+              const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_scomplex* b,
+              gb_inc_t rs_b, gb_inc_t cs_b)
+{
+    ctrsm_host(side, uploa, transa, diaga, m, n, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+               "gb_ctrsm");
+}
+
 void gb_dgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, const double* alpha,
               const double* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* x, gb_inc_t incx,
               const double* beta, double* y, gb_inc_t incy)
@@ -2068,6 +2133,17 @@ int gb_ztrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
     if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_ztrsm_dev", "negative dimension");
     return gb::ztrsm_dev(side, uploa, transa, diaga, m, n, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
                          gb::level3_slices(), pick_stream(stream));
+}
+
+int gb_ctrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+                 gb_scomplex alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_scomplex* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_ctrsm_dev", "negative dimension");
+    return gb::ctrsm_dev(side, uploa, transa, diaga, m, n, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                         pick_stream(stream));
 }
 
 int gb_zherk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, double alpha, const gb_dcomplex* a,

@@ -172,64 +172,82 @@ namespace {
 constexpr int ZNB = 64;
 constexpr int ZTHREADS = 128;
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+// The complex element of a real type R: double2 for ztrsm, float2 for ctrsm.
+template <typename R> struct Cx;
+template <> struct Cx<double> {
+    using T = double2;
+    __device__ __forceinline__ static T make(double x, double y) { return make_double2(x, y); }
+};
+template <> struct Cx<float> {
+    using T = float2;
+    __device__ __forceinline__ static T make(float x, float y) { return make_float2(x, y); }
+};
+
+template <typename C2>
+__device__ __forceinline__ C2 cmul(C2 a, C2 b)
 {
-    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+    C2 r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
 }
 
-__device__ __forceinline__ double2 cinv(double2 a)
+template <typename R>
+__device__ __forceinline__ typename Cx<R>::T cinv(typename Cx<R>::T a)
 {
     // 1 / a with the larger component scaled out (Smith's method)
     if (fabs(a.x) >= fabs(a.y)) {
-        const double r = a.y / a.x, d = a.x + a.y * r;
-        return make_double2(1.0 / d, -r / d);
+        const R r = a.y / a.x, d = a.x + a.y * r;
+        return Cx<R>::make(R(1) / d, -r / d);
     }
-    const double r = a.x / a.y, d = a.x * r + a.y;
-    return make_double2(r / d, -1.0 / d);
+    const R r = a.x / a.y, d = a.x * r + a.y;
+    return Cx<R>::make(r / d, R(-1) / d);
 }
 
-template <bool LOWER>
+template <typename R, bool LOWER>
 __global__ void __launch_bounds__(256) ztrsm_pack_diag_kernel(int64_t m, int unit, int conj,
-                                                              const double2* __restrict__ a, int64_t ars,
-                                                              int64_t acs, double2* __restrict__ packed)
+                                                              const typename Cx<R>::T* __restrict__ a, int64_t ars,
+                                                              int64_t acs, typename Cx<R>::T* __restrict__ packed)
 {
-    __shared__ double2 T[ZNB][ZNB + 1];
-    __shared__ double2 dinv[ZNB];
+    using C2 = typename Cx<R>::T;
+    __shared__ C2 Tb[ZNB][ZNB + 1];
+    __shared__ C2 dinv[ZNB];
     const int64_t r0 = (int64_t)blockIdx.x * ZNB;
     const int nb = (m - r0 < ZNB) ? (int)(m - r0) : ZNB;
-    const double2* blk = a + r0 * ars + r0 * acs;
+    const C2* blk = a + r0 * ars + r0 * acs;
     for (int e = threadIdx.x; e < ZNB * ZNB; e += 256) {
         const int i = e % ZNB, l = e / ZNB;
         const bool keep = (i < nb && l < nb) && (LOWER ? (l <= i) : (l >= i));
-        double2 v = keep ? blk[i * ars + l * acs] : make_double2(0.0, 0.0);
+        C2 v = keep ? blk[i * ars + l * acs] : Cx<R>::make(R(0), R(0));
         if (conj) v.y = -v.y;
-        T[i][l] = v;
+        Tb[i][l] = v;
     }
     __syncthreads();
     if (threadIdx.x < ZNB) {
         const int i = threadIdx.x;
-        dinv[i] = (unit || i >= nb) ? make_double2(1.0, 0.0) : cinv(T[i][i]);
+        dinv[i] = (unit || i >= nb) ? Cx<R>::make(R(1), R(0)) : cinv<R>(Tb[i][i]);
     }
     __syncthreads();
-    double2* out = packed + (int64_t)blockIdx.x * ZNB * ZNB;
+    C2* out = packed + (int64_t)blockIdx.x * ZNB * ZNB;
     for (int e = threadIdx.x; e < ZNB * ZNB; e += 256) {
         const int r = e / ZNB, i = e % ZNB;
-        double2 v = make_double2(0.0, 0.0);
+        C2 v = Cx<R>::make(R(0), R(0));
         if (r == i) v = dinv[r];
-        else if (LOWER ? (i < r) : (i > r)) v = cmul(T[r][i], dinv[i]);
+        else if (LOWER ? (i < r) : (i > r)) v = cmul(Tb[r][i], dinv[i]);
         out[e] = v;
     }
 }
 
-template <int LANES, bool LOWER>
-__global__ void __launch_bounds__(ZTHREADS) ztrsm_diag_kernel(int nb, const double2* __restrict__ pk,
-                                                              double2* __restrict__ b, int64_t brs, int64_t bcs,
-                                                              int64_t ncols)
+template <typename R, int LANES, bool LOWER>
+__global__ void __launch_bounds__(ZTHREADS) ztrsm_diag_kernel(int nb, const typename Cx<R>::T* __restrict__ pk,
+                                                              typename Cx<R>::T* __restrict__ b, int64_t brs,
+                                                              int64_t bcs, int64_t ncols)
 {
-    constexpr int COLS = ZTHREADS / LANES, R = ZNB / LANES, LL = ZNB + 1, LX = COLS + 1;
-    extern __shared__ double2 ztrsm_smem[];
-    double2* L = ztrsm_smem;       // [ZNB][LL]
-    double2* X = L + ZNB * LL;     // [ZNB][LX]
+    using C2 = typename Cx<R>::T;
+    constexpr int COLS = ZTHREADS / LANES, RR = ZNB / LANES, LL = ZNB + 1, LX = COLS + 1;
+    extern __shared__ __align__(16) unsigned char ztrsm_smem[];
+    C2* L = reinterpret_cast<C2*>(ztrsm_smem);  // [ZNB][LL]
+    C2* X = L + ZNB * LL;                       // [ZNB][LX]
     const int t = threadIdx.x;
     const int64_t j0 = (int64_t)blockIdx.x * COLS;
     const int cols = (ncols - j0 < COLS) ? (int)(ncols - j0) : COLS;
@@ -237,29 +255,29 @@ __global__ void __launch_bounds__(ZTHREADS) ztrsm_diag_kernel(int nb, const doub
     const bool rows_fast = (brs == 1);
     for (int e = t; e < ZNB * COLS; e += ZTHREADS) {
         const int i = rows_fast ? e % ZNB : e / COLS, c = rows_fast ? e / ZNB : e % COLS;
-        X[i * LX + c] = (c < cols && i < nb) ? b[i * brs + (j0 + c) * bcs] : make_double2(0.0, 0.0);
+        X[i * LX + c] = (c < cols && i < nb) ? b[i * brs + (j0 + c) * bcs] : Cx<R>::make(R(0), R(0));
     }
     __syncthreads();
     const int c = t / LANES, g = t % LANES;
     const int src0 = (t % 32) - g;
-    double2 x[R];
+    C2 x[RR];
 #pragma unroll
-    for (int q = 0; q < R; ++q) x[q] = X[(q * LANES + g) * LX + c];
+    for (int q = 0; q < RR; ++q) x[q] = X[(q * LANES + g) * LX + c];
 #pragma unroll
     for (int step = 0; step < ZNB; ++step) {
         const int i = LOWER ? step : ZNB - 1 - step;
         const int qi = i / LANES, gi = i % LANES;
-        double2 v = x[qi];
+        C2 v = x[qi];
         if constexpr (LANES > 1) {
             v.x = __shfl_sync(0xffffffffu, v.x, src0 + gi);
             v.y = __shfl_sync(0xffffffffu, v.y, src0 + gi);
         }
 #pragma unroll
-        for (int q = 0; q < R; ++q) {
+        for (int q = 0; q < RR; ++q) {
             if (LOWER ? (q * LANES + LANES - 1 > i) : (q * LANES < i)) {
                 const int r = q * LANES + g;
                 if (LOWER ? (r > i) : (r < i)) {
-                    const double2 p = L[r * LL + i];
+                    const C2 p = L[r * LL + i];
                     x[q].x = fma(-p.x, v.x, fma(p.y, v.y, x[q].x));
                     x[q].y = fma(-p.x, v.y, fma(-p.y, v.x, x[q].y));
                 }
@@ -267,7 +285,7 @@ __global__ void __launch_bounds__(ZTHREADS) ztrsm_diag_kernel(int nb, const doub
         }
     }
 #pragma unroll
-    for (int q = 0; q < R; ++q) {
+    for (int q = 0; q < RR; ++q) {
         const int r = q * LANES + g;
         X[r * LX + c] = cmul(x[q], L[r * LL + r]);
     }
@@ -278,79 +296,85 @@ __global__ void __launch_bounds__(ZTHREADS) ztrsm_diag_kernel(int nb, const doub
     }
 }
 
+template <typename R>
 constexpr size_t ztrsm_smem_bytes(int lanes)
 {
-    return sizeof(double2) * (ZNB * (ZNB + 1) + ZNB * (ZTHREADS / lanes + 1));
+    return 2 * sizeof(R) * (ZNB * (ZNB + 1) + ZNB * (ZTHREADS / lanes + 1));
 }
 
-template <int LANES, bool LOWER>
-int launch_ztrsm_diag(int nb, const double2* pk, double2* b, int64_t brs, int64_t bcs, int64_t ncols, cudaStream_t s)
+template <typename R, int LANES, bool LOWER>
+int launch_ztrsm_diag(int nb, const typename Cx<R>::T* pk, typename Cx<R>::T* b, int64_t brs, int64_t bcs,
+                      int64_t ncols, cudaStream_t s)
 {
     static bool attr = false;
     if (!attr) {
-        const int rc = check_cuda(cudaFuncSetAttribute(ztrsm_diag_kernel<LANES, LOWER>,
+        const int rc = check_cuda(cudaFuncSetAttribute(ztrsm_diag_kernel<R, LANES, LOWER>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                       (int)ztrsm_smem_bytes(LANES)), "ztrsm smem attr");
+                                                       (int)ztrsm_smem_bytes<R>(LANES)), "ztrsm smem attr");
         if (rc) return rc;
         attr = true;
     }
     const int64_t blocks = (ncols + ZTHREADS / LANES - 1) / (ZTHREADS / LANES);
-    if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "ztrsm", "too many right-hand sides");
-    ztrsm_diag_kernel<LANES, LOWER><<<(unsigned)blocks, ZTHREADS, ztrsm_smem_bytes(LANES), s>>>(nb, pk, b, brs, bcs,
-                                                                                               ncols);
+    if (blocks > INT32_MAX) return set_error(GB_ERR_ARG, "complex trsm", "too many right-hand sides");
+    ztrsm_diag_kernel<R, LANES, LOWER><<<(unsigned)blocks, ZTHREADS, ztrsm_smem_bytes<R>(LANES), s>>>(
+        nb, pk, b, brs, bcs, ncols);
     return check_cuda(cudaGetLastError(), "ztrsm_diag");
 }
 
-__global__ void __launch_bounds__(NT) zscal_kernel(int64_t m, int64_t n, double ar, double ai, double2* __restrict__ b,
+template <typename R>
+__global__ void __launch_bounds__(NT) zscal_kernel(int64_t m, int64_t n, R ar, R ai, typename Cx<R>::T* __restrict__ b,
                                                    int64_t brs, int64_t bcs)
 {
     const int64_t total = m * n;
     for (int64_t e = (int64_t)blockIdx.x * NT + threadIdx.x; e < total; e += (int64_t)gridDim.x * NT) {
         const int64_t j = e / m, i = e - j * m;
-        double2* p = b + i * brs + j * bcs;
-        *p = (ar == 0.0 && ai == 0.0) ? make_double2(0.0, 0.0) : cmul(make_double2(ar, ai), *p);
+        typename Cx<R>::T* p = b + i * brs + j * bcs;
+        *p = (ar == R(0) && ai == R(0)) ? Cx<R>::make(R(0), R(0)) : cmul(Cx<R>::make(ar, ai), *p);
     }
 }
 
+template <typename R>
 struct ZtrsmCtx {
     int lower, conj, slices;
-    const double2* packed;
-    const double2* a;
+    const typename Cx<R>::T* packed;
+    const typename Cx<R>::T* a;
     int64_t ars, acs;
-    double2* b;
+    typename Cx<R>::T* b;
     int64_t brs, bcs, n;
     cudaStream_t s;
 };
 
-int ztrsm_update(const ZtrsmCtx& t, int64_t r0, int64_t rcount, int64_t c0, int64_t ccount)
+template <typename R>
+int ztrsm_update(const ZtrsmCtx<R>& t, int64_t r0, int64_t rcount, int64_t c0, int64_t ccount)
 {
     // B[r0..] -= op(A)[r0.., c0..] X[c0..]; op(A) by the folded strides, conjugated when t.conj
-    const double minus_one[2] = {-1.0, 0.0}, one[2] = {1.0, 0.0};
-    return cgemm_dev<double>(t.conj ? 0x10 : 0x00, 0x00, rcount, t.n, ccount, minus_one,
-                             reinterpret_cast<const double*>(t.a + r0 * t.ars + c0 * t.acs), t.ars, t.acs,
-                             reinterpret_cast<const double*>(t.b + c0 * t.brs), t.brs, t.bcs, one,
-                             reinterpret_cast<double*>(t.b + r0 * t.brs), t.brs, t.bcs, t.slices, t.s);
+    const R minus_one[2] = {R(-1), R(0)}, one[2] = {R(1), R(0)};
+    return cgemm_dev<R>(t.conj ? 0x10 : 0x00, 0x00, rcount, t.n, ccount, minus_one,
+                        reinterpret_cast<const R*>(t.a + r0 * t.ars + c0 * t.acs), t.ars, t.acs,
+                        reinterpret_cast<const R*>(t.b + c0 * t.brs), t.brs, t.bcs, one,
+                        reinterpret_cast<R*>(t.b + r0 * t.brs), t.brs, t.bcs, t.slices, t.s);
 }
 
-int ztrsm_solve(const ZtrsmCtx& t, int64_t r0, int64_t mm)
+template <typename R>
+int ztrsm_solve(const ZtrsmCtx<R>& t, int64_t r0, int64_t mm)
 {
     if (mm <= ZNB) {
-        const double2* pk = t.packed + (r0 / ZNB) * ZNB * ZNB;
-        double2* b1 = t.b + r0 * t.brs;
+        const typename Cx<R>::T* pk = t.packed + (r0 / ZNB) * ZNB * ZNB;
+        typename Cx<R>::T* b1 = t.b + r0 * t.brs;
         const int nb = (int)mm;
         int lanes = diag_block_lanes(t.n);
         if (lanes < 2) lanes = 2;  // 64 complex rows per lane would not fit the registers
         LaunchScope ls("ztrsm_diag", t.s);
         switch (lanes) {
         case 2:
-            return t.lower ? launch_ztrsm_diag<2, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_ztrsm_diag<2, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+            return t.lower ? launch_ztrsm_diag<R, 2, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_ztrsm_diag<R, 2, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
         case 4:
-            return t.lower ? launch_ztrsm_diag<4, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_ztrsm_diag<4, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+            return t.lower ? launch_ztrsm_diag<R, 4, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_ztrsm_diag<R, 4, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
         default:
-            return t.lower ? launch_ztrsm_diag<8, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
-                           : launch_ztrsm_diag<8, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
+            return t.lower ? launch_ztrsm_diag<R, 8, true>(nb, pk, b1, t.brs, t.bcs, t.n, t.s)
+                           : launch_ztrsm_diag<R, 8, false>(nb, pk, b1, t.brs, t.bcs, t.n, t.s);
         }
     }
     int64_t m1 = ((mm / 2 + ZNB - 1) / ZNB) * ZNB;
@@ -367,13 +391,14 @@ int ztrsm_solve(const ZtrsmCtx& t, int64_t r0, int64_t mm)
     return ztrsm_solve(t, r0, m1);
 }
 
-}  // namespace
-
-// op(A) X = alpha B (left) or X op(A) = alpha B (right), dcomplex, in place;
-// transa may be N, T or C (conjugate transpose: the 0x10 bit).
-int ztrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const double* alpha, const double* a,
-              int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b, int slices, cudaStream_t s)
+// op(A) X = alpha B (left) or X op(A) = alpha B (right) in place for complex R
+// (dcomplex: R = double, scomplex: R = float); transa may be N, T or C
+// (conjugate transpose: the 0x10 bit).
+template <typename R>
+int xtrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const R* alpha, const R* a,
+              int64_t rs_a, int64_t cs_a, R* b, int64_t rs_b, int64_t cs_b, int slices, cudaStream_t s)
 {
+    using C2 = typename Cx<R>::T;
     if (m <= 0 || n <= 0) return GB_SUCCESS;
     int64_t brs = rs_b, bcs = cs_b, mm = m, nn = n;
     bool trans = GB_IS_TRANS(transa);
@@ -386,43 +411,58 @@ int ztrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, co
         nn = m;
         trans = !trans;
     }
-    double2* bz = reinterpret_cast<double2*>(b);
-    if (!(alpha[0] == 1.0 && alpha[1] == 0.0)) {
+    C2* bz = reinterpret_cast<C2*>(b);
+    if (!(alpha[0] == R(1) && alpha[1] == R(0))) {
         LaunchScope ls("zscal", s);
-        zscal_kernel<<<grid_of(mm * nn), NT, 0, s>>>(mm, nn, alpha[0], alpha[1], bz, brs, bcs);
+        zscal_kernel<R><<<grid_of(mm * nn), NT, 0, s>>>(mm, nn, alpha[0], alpha[1], bz, brs, bcs);
         int rc = check_cuda(cudaGetLastError(), "zscal");
-        if (rc || (alpha[0] == 0.0 && alpha[1] == 0.0)) return rc;
+        if (rc || (alpha[0] == R(0) && alpha[1] == R(0))) return rc;
     }
-    ZtrsmCtx t;
+    ZtrsmCtx<R> t;
     t.ars = trans ? cs_a : rs_a;
     t.acs = trans ? rs_a : cs_a;
     t.lower = ((uplo == GB_LOWER) != trans) ? 1 : 0;
     t.conj = conj;
     t.slices = slices;
-    t.a = reinterpret_cast<const double2*>(a);
+    t.a = reinterpret_cast<const C2*>(a);
     t.b = bz;
     t.brs = brs;
     t.bcs = bcs;
     t.n = nn;
     t.s = s;
     const int64_t nblk = (mm + ZNB - 1) / ZNB;
-    if (nblk > INT32_MAX) return set_error(GB_ERR_ARG, "ztrsm", "too many diagonal blocks");
-    double2* packed = static_cast<double2*>(dev_alloc(sizeof(double2) * nblk * ZNB * ZNB, s));
+    if (nblk > INT32_MAX) return set_error(GB_ERR_ARG, "complex trsm", "too many diagonal blocks");
+    C2* packed = static_cast<C2*>(dev_alloc(sizeof(C2) * nblk * ZNB * ZNB, s));
     if (!packed) return GB_ERR_NOMEM;
     {
         LaunchScope ls("ztrsm_pack_diag", s);
         if (t.lower)
-            ztrsm_pack_diag_kernel<true><<<(unsigned)nblk, 256, 0, s>>>(mm, diag == GB_UNIT_DIAG, conj, t.a, t.ars,
-                                                                        t.acs, packed);
+            ztrsm_pack_diag_kernel<R, true><<<(unsigned)nblk, 256, 0, s>>>(mm, diag == GB_UNIT_DIAG, conj, t.a, t.ars,
+                                                                           t.acs, packed);
         else
-            ztrsm_pack_diag_kernel<false><<<(unsigned)nblk, 256, 0, s>>>(mm, diag == GB_UNIT_DIAG, conj, t.a, t.ars,
-                                                                         t.acs, packed);
+            ztrsm_pack_diag_kernel<R, false><<<(unsigned)nblk, 256, 0, s>>>(mm, diag == GB_UNIT_DIAG, conj, t.a,
+                                                                            t.ars, t.acs, packed);
     }
     int rc = check_cuda(cudaGetLastError(), "ztrsm_pack_diag");
     t.packed = packed;
     if (!rc) rc = ztrsm_solve(t, 0, mm);
     dev_free(packed, s);
     return rc;
+}
+
+}  // namespace
+
+int ztrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const double* alpha, const double* a,
+              int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b, int slices, cudaStream_t s)
+{
+    return xtrsm_dev<double>(side, uplo, transa, diag, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, slices, s);
+}
+
+// scomplex: the FP32 solve with the updates through cgemm's FP32 real product (sgemm's engine choice)
+int ctrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const float* alpha, const float* a,
+              int64_t rs_a, int64_t cs_a, float* b, int64_t rs_b, int64_t cs_b, cudaStream_t s)
+{
+    return xtrsm_dev<float>(side, uplo, transa, diag, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, 0, s);
 }
 
 }  // namespace gb

@@ -136,6 +136,8 @@ int cgemm_dev(int transa, int transb, int64_t m, int64_t n, int64_t k, const T* 
               int slices, cudaStream_t s);
 int ztrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const double* alpha, const double* a,
               int64_t rs_a, int64_t cs_a, double* b, int64_t rs_b, int64_t cs_b, int slices, cudaStream_t s);
+int ctrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const float* alpha, const float* a,
+              int64_t rs_a, int64_t cs_a, float* b, int64_t rs_b, int64_t cs_b, cudaStream_t s);  // gb_complex.cu
 int dscalv_dev(int64_t n, double alpha, double* x, int64_t incx, cudaStream_t s);
 int dcopyv_dev(int64_t n, const double* x, int64_t incx, double* y, int64_t incy, cudaStream_t s);
 int damaxv_dev(int64_t n, const double* x, int64_t incx, int64_t* index_dev, cudaStream_t s);

@@ -158,6 +158,11 @@ void ztrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char
             const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n,
             const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, gb_dcomplex* b,
             const gb_f77_int* ldb);
+/* replaces ctrsm_ (the scomplex instance of frame/compat/bla_trsm.c:121-219) */
+void ctrsm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n,
+            const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, gb_scomplex* b,
+            const gb_f77_int* ldb);
 
 /* replace zherk_ / cherk_ (frame/compat/bla_herk.c:45-130, checks
    frame/compat/check/bla_herk_check.h:37-77; trans N or C; the BLAS early
@@ -329,6 +334,10 @@ void bli_cgemm(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, gb_
 void bli_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
                gb_dim_t n, const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a,
                gb_inc_t cs_a, gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b);
+/* replaces bli_ctrsm (the same, for scomplex) */
+void bli_ctrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+               gb_dim_t n, const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a,
+               gb_inc_t cs_a, gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b);
 
 /* replace bli_zherk / bli_cherk, bli_zher2k / bli_cher2k, bli_zhemm /
    bli_chemm, bli_zsymm / bli_csymm and bli_dsyr2k (frame/3/bli_l3_tapi_ex.c;
@@ -483,6 +492,9 @@ void gb_strsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diag
 void gb_ztrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
               gb_dim_t m, gb_dim_t n, const gb_dcomplex* alpha, const gb_dcomplex* a,
               gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b);
+void gb_ctrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga,
+              gb_dim_t m, gb_dim_t n, const gb_scomplex* alpha, const gb_scomplex* a,
+              gb_inc_t rs_a, gb_inc_t cs_a, gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b);
 void gb_dgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n,
               const double* alpha, const double* a, gb_inc_t rs_a, gb_inc_t cs_a,
               const double* x, gb_inc_t incx, const double* beta, double* y, gb_inc_t incy);
@@ -560,6 +572,10 @@ int gb_cgemm_dev(gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t n, g
 int gb_ztrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
                  gb_dim_t n, gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
                  gb_dcomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
+/* The scomplex instance: FP32 diagonal solves, updates through cgemm's FP32 real product. */
+int gb_ctrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m,
+                 gb_dim_t n, gb_scomplex alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a,
+                 gb_scomplex* b, gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
 
 /* Device-pointer forms of zherk, zher2k, zhemm, zsymm, dtrmm3 and dsyr2k
    (asynchronous on the stream). */

@@ -21,8 +21,8 @@
  *          docs/PluginHowTo.md): the typed level-1v API calls the context
  *          kernel once per vector (frame/1/bli_l1v_tapi.c:155-232)
  *
- * Datatypes the GPU library does not cover (trsm in single complex, gemv
- * other than double) keep BLIS's own code: trsm is
+ * Datatypes the GPU library does not cover (gemv other than double) keep
+ * BLIS's own code: trsm (all four datatypes on the GPU) is
  * forwarded to the next bli_trsm_ex in the link order (libblis's), gemv is
  * simply not interposed for them.  Forwarded calls are counted, and with
  * GB300_BLIS_REPORT set the library prints the counts of GPU and forwarded
@@ -110,7 +110,8 @@ void bli_trsm_ex( side_t side, const obj_t* alpha, const obj_t* a, const obj_t* 
 	// On the GPU: A and B of one datatype the library covers, A square and conformal,
 	// A's diagonal through its first element, B without a transposition bit.  Anything
 	// else (including the operands that bli_trsm_check rejects) goes to BLIS.
-	const bool gpu_dt = ( dt == BLIS_DOUBLE || dt == BLIS_FLOAT || dt == BLIS_DCOMPLEX ) && bli_obj_dt( a ) == dt;
+	const bool gpu_dt = ( dt == BLIS_DOUBLE || dt == BLIS_FLOAT || dt == BLIS_DCOMPLEX || dt == BLIS_SCOMPLEX ) &&
+	                    bli_obj_dt( a ) == dt;
 	if ( !gpu_dt ||
 	     bli_obj_length( a ) != bli_obj_width( a ) || bli_obj_length( a ) != na ||
 	     bli_obj_diag_offset( a ) != 0 || bli_obj_has_trans( b ) || bli_obj_has_conj( b ) ||
@@ -145,10 +146,14 @@ void bli_trsm_ex( side_t side, const obj_t* alpha, const obj_t* a, const obj_t* 
 		gb_strsm( sd == BLIS_LEFT ? GB_LEFT : GB_RIGHT, uplo, ta, diag, m, n,
 		          ( const float* )bli_obj_buffer( &alpha_cast ), ( const float* )pa, rsa, csa,
 		          ( float* )pb, rsb, csb );
-	else
+	else if ( dt == BLIS_DCOMPLEX )
 		gb_ztrsm( sd == BLIS_LEFT ? GB_LEFT : GB_RIGHT, uplo, ta, diag, m, n,
 		          ( const gb_dcomplex* )bli_obj_buffer( &alpha_cast ), ( const gb_dcomplex* )pa, rsa, csa,
 		          ( gb_dcomplex* )pb, rsb, csb );
+	else
+		gb_ctrsm( sd == BLIS_LEFT ? GB_LEFT : GB_RIGHT, uplo, ta, diag, m, n,
+		          ( const gb_scomplex* )bli_obj_buffer( &alpha_cast ), ( const gb_scomplex* )pa, rsa, csa,
+		          ( gb_scomplex* )pb, rsb, csb );
 }
 
 // ------------------------------------------------------------------ gemv

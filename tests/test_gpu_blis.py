@@ -83,7 +83,7 @@ def test_blis_testsuite_through_seams(integ, tmp_path, name, ops, dts, rand):
 # routines whose calls reach the GPU in each link order
 SEAM_ROUTINES = {
     "dblat1": ["DDOT", "DAXPY"], "dblat2": ["DGEMV"], "dblat3": ["DGEMM", "DTRSM"],
-    "sblat3": ["SGEMM", "STRSM"], "zblat3": ["ZGEMM", "ZTRSM"], "cblat3": ["CGEMM"],
+    "sblat3": ["SGEMM", "STRSM"], "zblat3": ["ZGEMM", "ZTRSM"], "cblat3": ["CGEMM", "CTRSM"],
 }
 INTERPOSED_ROUTINES = {
     "dblat1": ["DDOT", "DAXPY", "DCOPY", "DSCAL", "IDAMAX"],
@@ -91,7 +91,7 @@ INTERPOSED_ROUTINES = {
     "dblat3": ["DGEMM", "DSYMM", "DTRMM", "DTRSM", "DSYRK", "DSYR2K"],
     "sblat3": ["SGEMM", "STRSM"],
     "zblat3": ["ZGEMM", "ZHEMM", "ZSYMM", "ZTRSM", "ZHERK", "ZHER2K"],
-    "cblat3": ["CGEMM", "CHEMM", "CSYMM", "CHERK", "CHER2K"],
+    "cblat3": ["CGEMM", "CHEMM", "CSYMM", "CTRSM", "CHERK", "CHER2K"],
 }
 
 
@@ -122,11 +122,7 @@ def test_blas_tests_through_seams(integ, tmp_path, prog):
         assert rep["gemv_gpu"] > 0, rep
     else:
         assert rep["gemm_gpu"] > 0, rep
-        if prog[0] in "dzs":
-            assert rep["trsm_gpu"] > 0 and rep["trsm_cpu_forwarded"] == 0, rep
-        else:
-            # single-complex trsm is not on the GPU path: BLIS's own code runs it
-            assert rep["trsm_gpu"] == 0, rep
+        assert rep["trsm_gpu"] > 0 and rep["trsm_cpu_forwarded"] == 0, rep
 
 
 @pytest.mark.parametrize("prog", sorted(INTERPOSED_ROUTINES))

@@ -182,3 +182,51 @@ def test_ztrsm_ozaki_updates_and_alpha_zero():
     x[:] = np.nan  # alpha = 0: B := 0 without reading it
     blas.ztrsm("L", "L", "C", "N", m, n, 0.0, a, m, x, m)
     assert (x == 0).all()
+
+
+@pytest.mark.parametrize("side", ["L", "R"])
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("trans", ["N", "T", "C"])
+@pytest.mark.parametrize("diag", ["N", "U"])
+@pytest.mark.parametrize("m,n", [(150, 90), (65, 1), (1, 7), (300, 260)])
+def test_ctrsm_residual(side, uplo, trans, diag, m, n):
+    # single complex: FP32 diagonal solves and cgemm updates, residual against FP32's epsilon
+    na = m if side == "L" else n
+    a = np.asfortranarray(_cplx((na, na), 34, np.complex64) / na + 2.0 * np.eye(na, dtype=np.complex64))
+    b0 = _cplx((m, n), 35, np.complex64)
+    x = b0.copy(order="F")
+    alpha = np.complex64(0.5 + 1.5j)
+    blas.ctrsm(side, uplo, trans, diag, m, n, alpha, a, na, x, m)
+    t = _op(_ztri(a.astype(np.complex128), uplo, diag), trans)
+    xd = x.astype(np.complex128)
+    lhs = t @ xd if side == "L" else xd @ t
+    rhs = complex(alpha) * b0.astype(np.complex128)
+    assert np.linalg.norm(lhs - rhs) <= 64 * max(m, n) * U32 * np.linalg.norm(rhs)
+
+
+def test_ctrsm_general_strides_and_alpha_zero():
+    """gb_ctrsm_dev on a row-major A and a B with a leading dimension larger than m; then alpha =
+    0 sets B to zero without reading it (NaN there stays out)."""
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    m, n, ldb = 520, 130, 530
+    a = _cplx((m, m), 36, np.complex64) / m + 2.0 * np.eye(m, dtype=np.complex64)
+    a_rm = np.ascontiguousarray(a)  # row-major: rs = m, cs = 1
+    b0 = _cplx((m, n), 37, np.complex64)
+    bbuf = np.zeros((ldb, n), dtype=np.complex64, order="F")
+    bbuf[:m] = b0
+    A = torch.from_numpy(a_rm.view(np.float32)).cuda()
+    B = torch.from_numpy(np.ascontiguousarray(bbuf.T).view(np.float32)).cuda()
+    one = _lib.SComplex(1.0, 0.0)
+    assert L.gb_ctrsm_dev(0, 0xC0, 0x18, 0x100, m, n, one, A.data_ptr(), m, 1, B.data_ptr(), 1, ldb, None) == 0
+    assert L.gb_synchronize() == 0
+    x = B.cpu().numpy().view(np.complex64).T[:m].astype(np.complex128)
+    t = np.conj(_ztri(a.astype(np.complex128), "L", "U")).T
+    assert np.linalg.norm(t @ x - b0) <= 64 * m * U32 * np.linalg.norm(b0)
+    assert (B.cpu().numpy().view(np.complex64).T[m:] == 0).all()  # rows past m untouched
+    B.fill_(float("nan"))
+    zero = _lib.SComplex(0.0, 0.0)
+    assert L.gb_ctrsm_dev(0, 0xC0, 0, 0, m, n, zero, A.data_ptr(), m, 1, B.data_ptr(), 1, ldb, None) == 0
+    assert L.gb_synchronize() == 0
+    bz = B.cpu().numpy().view(np.complex64).T
+    assert (bz[:m] == 0).all() and np.isnan(bz[m:]).all()
