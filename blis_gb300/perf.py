@@ -15,7 +15,7 @@ L2 where the workload allows:
   dtrsm_16384     L/L/N/N, B entries (1+u) 2^e, e in [-20,20]: native and
                   Ozaki updates, sampled componentwise backward error
   level12x        dscal / dcopy / idamax at 2^28, dger 32768^2, dtrsv 16384
-  complex         zgemm 4096^3 native / Ozaki, cgemm 4096^3 (8 mnk flop), ztrsm 4096^2
+  complex         zgemm 4096^3 native / Ozaki, cgemm 4096^3 (8 mnk flop), ztrsm / ctrsm 4096^2
                   native / Ozaki updates (4 m^2 n flop)
   level3x         dtrmm 8192x4096 (m^2 n), dsyrk n=k=8192 (n^2 k), dsymm
                   8192x4096 (2 m^2 n): native FP64 and Ozaki (7 slices)
@@ -527,6 +527,17 @@ def run_complex(out):
         out.append({"workload": "ztrsm_%dx%d" % (n, n), "form": form, "ms": ms - copy_ms,
                     "tflops": 4.0 * n ** 3 / (ms - copy_ms) / 1e9})
     L.gb_set_dgemm_mode(0, 8)
+    # ctrsm, the same solve in single complex: FP32 diagonal solves, cgemm updates
+    ac = a.to(torch.complex64).t().contiguous().t()
+    bc = b0.to(torch.complex64).t().contiguous().t()
+    xc = bc.clone()
+    onec = _lib.SComplex(1.0, 0.0)
+    fn = lambda: (xc.copy_(bc), _lib.check(L.gb_ctrsm_dev(0, 0xC0, 0, 0, n, n, onec, ac.data_ptr(), 1, n,
+                                                          xc.data_ptr(), 1, n, _stream()), "ctrsm"))
+    ms = _timer(fn, reps=3, warmup=1)
+    copy_ms = _timer(lambda: xc.copy_(bc), reps=3, warmup=1)
+    out.append({"workload": "ctrsm_%dx%d" % (n, n), "form": "fp32_default_dispatch", "ms": ms - copy_ms,
+                "tflops": 4.0 * n ** 3 / (ms - copy_ms) / 1e9})
 
 
 def run_hermitian(out):
