@@ -166,6 +166,14 @@ def load(path=None):
     _sig(L, "gb_sgemm_dev", C.c_int, sg + [_vp])
     _sig(L, "gb_dtrsm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _vp])
     _sig(L, "gb_strsm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, _f, _vp, _i64, _i64, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_zsyrk_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, DComplex, _vp, _i64, _i64, DComplex, _vp, _i64,
+                                      _i64, _vp])
+    _sig(L, "gb_csyrk_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, SComplex, _vp, _i64, _i64, SComplex, _vp, _i64,
+                                      _i64, _vp])
+    _sig(L, "gb_zsyr2k_dev", C.c_int, [C.c_int, C.c_int, C.c_int, _i64, _i64, DComplex, _vp, _i64, _i64, _vp, _i64,
+                                       _i64, DComplex, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_csyr2k_dev", C.c_int, [C.c_int, C.c_int, C.c_int, _i64, _i64, SComplex, _vp, _i64, _i64, _vp, _i64,
+                                       _i64, SComplex, _vp, _i64, _i64, _vp])
     _sig(L, "gb_ctrsm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, SComplex, _vp, _i64, _i64, _vp, _i64, _i64,
                                                       _vp])
     _sig(L, "gb_dscalv_dev", C.c_int, [_i64, _d, _vp, _i64, _vp])

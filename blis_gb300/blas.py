@@ -120,6 +120,28 @@ def zher2k(uplo, trans, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
 cher2k = zher2k
 
 
+def zsyrk(uplo, trans, n, k, alpha, a, lda, beta, c, ldc):
+    """zsyrk_ / csyrk_ by c's dtype (alpha, beta complex; trans 'N' or 'T')."""
+    L = _lib.load()
+    fn = L.zsyrk_ if c.dtype == np.complex128 else L.csyrk_
+    al, be = _cscalar(alpha, c.dtype), _cscalar(beta, c.dtype)
+    fn(_c(uplo), _c(trans), _i(n), _i(k), _p(al), _p(a), _i(lda), _p(be), _p(c), _i(ldc))
+
+
+csyrk = zsyrk
+
+
+def zsyr2k(uplo, trans, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+    """zsyr2k_ / csyr2k_ by c's dtype (alpha, beta complex; trans 'N' or 'T')."""
+    L = _lib.load()
+    fn = L.zsyr2k_ if c.dtype == np.complex128 else L.csyr2k_
+    al, be = _cscalar(alpha, c.dtype), _cscalar(beta, c.dtype)
+    fn(_c(uplo), _c(trans), _i(n), _i(k), _p(al), _p(a), _i(lda), _p(b), _i(ldb), _p(be), _p(c), _i(ldc))
+
+
+csyr2k = zsyr2k
+
+
 def zhemm(side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc, herm=True):
     """zhemm_ / chemm_ (herm) or zsymm_ / csymm_ by c's dtype."""
     L = _lib.load()

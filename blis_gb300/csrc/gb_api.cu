@@ -870,6 +870,36 @@ int cher2k_host(int uplo, int transa, int transb, int64_t m, int64_t k, const T*
     return finish(s, where);
 }
 
+// complex syrk (b null) / syr2k, the same staging as herk / her2k
+template <typename T>
+int csyr2k_host(int uplo, int transa, int transb, int64_t m, int64_t k, const T* alpha, const T* a, int64_t rs_a,
+                int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, const T* beta, T* c, int64_t rs_c,
+                int64_t cs_c, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const size_t esz = 2 * sizeof(T);
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    Staged& C = bufs.next();
+    if ((rc = stage_in(c, m, m, rs_c, cs_c, esz, true, &C, s))) return rc;
+    Staged& A = bufs.next();
+    Staged& B = bufs.next();
+    if (!(alpha[0] == T(0) && alpha[1] == T(0)) && k > 0) {
+        if ((rc = stage_in(a, ta ? k : m, ta ? m : k, rs_a, cs_a, esz, true, &A, s))) return rc;
+        if (b && (rc = stage_in(b, tb ? k : m, tb ? m : k, rs_b, cs_b, esz, true, &B, s))) return rc;
+    }
+    const int slices = (sizeof(T) == 8) ? level3_slices() : 0;
+    if ((rc = csyr2k_dev<T>(uplo, transa, transb, m, k, alpha, reinterpret_cast<const T*>(A.origin), A.rs, A.cs,
+                            b ? reinterpret_cast<const T*>(B.origin) : nullptr, B.rs, B.cs, beta,
+                            reinterpret_cast<T*>(C.origin), C.rs, C.cs, slices, s)))
+        return rc;
+    if ((rc = stage_out(c, m, m, rs_c, cs_c, esz, C, s))) return rc;
+    return finish(s, where);
+}
+
 template <typename T>
 int chemm_host(int side, int uplo, int herm, int conja, int transb, int64_t m, int64_t n, const T* alpha, const T* a, int64_t rs_a,
                int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, const T* beta, T* c, int64_t rs_c, int64_t cs_c,
@@ -1072,6 +1102,38 @@ void her2k_blas(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77
     const int t = map_trans(*trans);
     cher2k_host<T>(lsame(*uploc, 'L') ? GB_LOWER : GB_UPPER, t, t, *m, *k, &alpha->real, &a->real, 1, *lda,
                    &b->real, 1, *ldb, *beta, &c->real, 1, *ldc, name);
+}
+
+// complex syrk / syr2k (frame/compat/bla_syrk.c:45-121, bla_syr2k.c:45-128;
+// checks frame/compat/check/bla_syrk_check.h:37-84, bla_syr2k_check.h:37-84):
+// trans N or T only in the complex domain
+template <typename T, typename C>
+void csyr2k_blas(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+                 const C* alpha, const C* a, const gb_f77_int* lda, const C* b, const gb_f77_int* ldb,
+                 const C* beta, C* c, const gb_f77_int* ldc, const char* xname, const char* name)
+{
+    const bool two = (b != nullptr);
+    const bool lower = lsame(*uploc, 'L'), upper = lsame(*uploc, 'U');
+    const bool nota = lsame(*trans, 'N'), ta = lsame(*trans, 'T');
+    const int nrowa = nota ? *m : *k;
+    int info = 0;
+    if (!lower && !upper) info = 1;
+    else if (!nota && !ta) info = 2;
+    else if (*m < 0) info = 3;
+    else if (*k < 0) info = 4;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 7;
+    else if (two && *ldb < (nrowa > 1 ? nrowa : 1)) info = 9;
+    else if (*ldc < (*m > 1 ? *m : 1)) info = two ? 12 : 10;
+    if (info) {
+        call_xerbla(xname, info);
+        return;
+    }
+    if (*m == 0 || (((alpha->real == T(0) && alpha->imag == T(0)) || *k == 0) && beta->real == T(1) &&
+                    beta->imag == T(0)))
+        return;
+    const int t = nota ? GB_NO_TRANSPOSE : GB_TRANSPOSE;
+    csyr2k_host<T>(lower ? GB_LOWER : GB_UPPER, t, t, *m, *k, &alpha->real, &a->real, 1, *lda,
+                   two ? &b->real : nullptr, 1, two ? *ldb : 1, &beta->real, &c->real, 1, *ldc, name);
 }
 
 template <typename T, typename C>
@@ -1292,6 +1354,36 @@ void zher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_in
              const gb_f77_int* ldb, const double* beta, gb_dcomplex* c, const gb_f77_int* ldc)
 {
     her2k_blas<double, gb_dcomplex>(uploc, trans, m, k, alpha, a, lda, b, ldb, beta, c, ldc, "ZHER2K");
+}
+
+void zsyrk_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+            const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* beta,
+            gb_dcomplex* c, const gb_f77_int* ldc)
+{
+    csyr2k_blas<double, gb_dcomplex>(uploc, trans, m, k, alpha, a, lda, nullptr, nullptr, beta, c, ldc, "ZSYRK ",
+                                     "ZSYRK");
+}
+
+void csyrk_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+            const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* beta,
+            gb_scomplex* c, const gb_f77_int* ldc)
+{
+    csyr2k_blas<float, gb_scomplex>(uploc, trans, m, k, alpha, a, lda, nullptr, nullptr, beta, c, ldc, "CSYRK ",
+                                    "CSYRK");
+}
+
+void zsyr2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+             const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* b,
+             const gb_f77_int* ldb, const gb_dcomplex* beta, gb_dcomplex* c, const gb_f77_int* ldc)
+{
+    csyr2k_blas<double, gb_dcomplex>(uploc, trans, m, k, alpha, a, lda, b, ldb, beta, c, ldc, "ZSYR2K", "ZSYR2K");
+}
+
+void csyr2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+             const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
+             const gb_f77_int* ldb, const gb_scomplex* beta, gb_scomplex* c, const gb_f77_int* ldc)
+{
+    csyr2k_blas<float, gb_scomplex>(uploc, trans, m, k, alpha, a, lda, b, ldb, beta, c, ldc, "CSYR2K", "CSYR2K");
 }
 
 void cher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
@@ -1722,6 +1814,38 @@ void bli_ctrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t dia
 
 // frame/3/bli_l3_tapi_ex.c herk / her2k / hemm / symm / syr2k (prototypes
 // frame/3/bli_l3_tapi_ex.h:62-168)
+void bli_zsyrk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const gb_dcomplex* alpha,
+               const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* beta, gb_dcomplex* c,
+               gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    csyr2k_host<double>(uploc, transa, transa, m, k, &alpha->real, &a->real, rs_a, cs_a, nullptr, 1, 1, &beta->real,
+                        &c->real, rs_c, cs_c, "bli_zsyrk");
+}
+
+void bli_csyrk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const gb_scomplex* alpha,
+               const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* beta, gb_scomplex* c,
+               gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    csyr2k_host<float>(uploc, transa, transa, m, k, &alpha->real, &a->real, rs_a, cs_a, nullptr, 1, 1, &beta->real,
+                       &c->real, rs_c, cs_c, "bli_csyrk");
+}
+
+void bli_zsyr2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b,
+                gb_inc_t rs_b, gb_inc_t cs_b, const gb_dcomplex* beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    csyr2k_host<double>(uploc, transa, transb, m, k, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                        &beta->real, &c->real, rs_c, cs_c, "bli_zsyr2k");
+}
+
+void bli_csyr2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* b,
+                gb_inc_t rs_b, gb_inc_t cs_b, const gb_scomplex* beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
+{
+    csyr2k_host<float>(uploc, transa, transb, m, k, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                       &beta->real, &c->real, rs_c, cs_c, "bli_csyr2k");
+}
+
 void bli_zherk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const double* alpha, const gb_dcomplex* a,
                gb_inc_t rs_a, gb_inc_t cs_a, const double* beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c)
 {
@@ -2144,6 +2268,50 @@ int gb_ctrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
     if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_ctrsm_dev", "negative dimension");
     return gb::ctrsm_dev(side, uploa, transa, diaga, m, n, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
                          pick_stream(stream));
+}
+
+int gb_zsyrk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, gb_dcomplex alpha, const gb_dcomplex* a,
+                 gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c,
+                 void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_zsyrk_dev", "negative dimension");
+    return gb::csyr2k_dev<double>(uploc, transa, transa, m, k, &alpha.real, &a->real, rs_a, cs_a, nullptr, 1, 1,
+                                  &beta.real, &c->real, rs_c, cs_c, gb::level3_slices(), pick_stream(stream));
+}
+
+int gb_csyrk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, gb_scomplex alpha, const gb_scomplex* a,
+                 gb_inc_t rs_a, gb_inc_t cs_a, gb_scomplex beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c,
+                 void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_csyrk_dev", "negative dimension");
+    return gb::csyr2k_dev<float>(uploc, transa, transa, m, k, &alpha.real, &a->real, rs_a, cs_a, nullptr, 1, 1,
+                                 &beta.real, &c->real, rs_c, cs_c, 0, pick_stream(stream));
+}
+
+int gb_zsyr2k_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k, gb_dcomplex alpha,
+                  const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b, gb_inc_t rs_b,
+                  gb_inc_t cs_b, gb_dcomplex beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_zsyr2k_dev", "negative dimension");
+    return gb::csyr2k_dev<double>(uploc, transa, transb, m, k, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b,
+                                  cs_b, &beta.real, &c->real, rs_c, cs_c, gb::level3_slices(), pick_stream(stream));
+}
+
+int gb_csyr2k_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k, gb_scomplex alpha,
+                  const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* b, gb_inc_t rs_b,
+                  gb_inc_t cs_b, gb_scomplex beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || k < 0) return gb::set_error(GB_ERR_ARG, "gb_csyr2k_dev", "negative dimension");
+    return gb::csyr2k_dev<float>(uploc, transa, transb, m, k, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                                 &beta.real, &c->real, rs_c, cs_c, 0, pick_stream(stream));
 }
 
 int gb_zherk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, double alpha, const gb_dcomplex* a,

@@ -100,11 +100,11 @@ __global__ void __launch_bounds__(NT) pack_conj_trans_kernel(int64_t m, int64_t 
 // (r0, c0); P is the block's real view (rows 2i and 2i+1 the real and
 // imaginary parts of row i, leading dimension ldp), or zero when p is null.
 // beta == 0 writes without reading C.  The imaginary parts on C's diagonal
-// are set to zero.
+// are set to zero when herm (herk, her2k; not the complex syrk forms).
 template <typename T>
 __global__ void __launch_bounds__(NT) herk_merge_kernel(int64_t rows, int64_t cols, int64_t r0, int64_t c0,
-                                                        int lower, const T* __restrict__ p, int64_t ldp, T beta,
-                                                        T* __restrict__ c, int64_t rs_c, int64_t cs_c)
+                                                        int lower, int herm, const T* __restrict__ p, int64_t ldp,
+                                                        T beta, T* __restrict__ c, int64_t rs_c, int64_t cs_c)
 {
     const int64_t total = rows * cols;
     for (int64_t e = (int64_t)blockIdx.x * NT + threadIdx.x; e < total; e += (int64_t)gridDim.x * NT) {
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(NT) herk_merge_kernel(int64_t rows, int64_t co
             im += beta * cij[1];
         }
         cij[0] = re;
-        cij[1] = (gi == gj) ? T(0) : im;
+        cij[1] = (herm && gi == gj) ? T(0) : im;
     }
 }
 
@@ -166,11 +166,11 @@ int real_gemm_cm<float>(int64_t m, int64_t n, int64_t k, float alpha, const floa
 
 template <typename T>
 int launch_merge(int64_t rows, int64_t cols, int64_t r0, int64_t c0, bool lower, const T* p, int64_t ldp, T beta,
-                 T* c, int64_t rs_c, int64_t cs_c, cudaStream_t s)
+                 T* c, int64_t rs_c, int64_t cs_c, cudaStream_t s, bool herm = true)
 {
     LaunchScope ls("herk_merge", s);
-    herk_merge_kernel<T><<<grid_of(rows * cols), NT, 0, s>>>(rows, cols, r0, c0, lower ? 1 : 0, p, ldp, beta, c,
-                                                             rs_c, cs_c);
+    herk_merge_kernel<T><<<grid_of(rows * cols), NT, 0, s>>>(rows, cols, r0, c0, lower ? 1 : 0, herm ? 1 : 0, p, ldp,
+                                                             beta, c, rs_c, cs_c);
     return check_cuda(cudaGetLastError(), "herk merge");
 }
 
@@ -181,6 +181,28 @@ int launch_merge(int64_t rows, int64_t cols, int64_t r0, int64_t c0, bool lower,
 // scratch block and the merge; the panel beside it straight into C when C is
 // column-stored, else through the scratch panel and the merge.
 // the imaginary parts of C's diagonal set to zero
+// the stored triangle of the m x m complex C times (br + i bi); beta = 0
+// writes zeros without reading C
+template <typename T>
+__global__ void __launch_bounds__(NT) tri_scale_kernel(int64_t m, int lower, T br, T bi, T* __restrict__ c,
+                                                       int64_t rs_c, int64_t cs_c)
+{
+    const int64_t total = m * m;
+    for (int64_t e = (int64_t)blockIdx.x * NT + threadIdx.x; e < total; e += (int64_t)gridDim.x * NT) {
+        const int64_t j = e / m, i = e - j * m;
+        if (lower ? (i < j) : (i > j)) continue;
+        T* cij = c + 2 * (i * rs_c + j * cs_c);
+        if (br == T(0) && bi == T(0)) {
+            cij[0] = T(0);
+            cij[1] = T(0);
+        } else {
+            const T re = cij[0], im = cij[1];
+            cij[0] = br * re - bi * im;
+            cij[1] = br * im + bi * re;
+        }
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NT) zero_diag_imag_kernel(int64_t m, T* __restrict__ c, int64_t rs_c, int64_t cs_c)
 {
@@ -190,7 +212,7 @@ __global__ void __launch_bounds__(NT) zero_diag_imag_kernel(int64_t m, T* __rest
 
 template <typename T>
 int herk_blocks(bool lower, int64_t m, int64_t kk, T alpha, const T* xb, const T* yb, T beta, T* c, int64_t rs_c,
-                int64_t cs_c, int slices, cudaStream_t s)
+                int64_t cs_c, int slices, cudaStream_t s, bool herm = true)
 {
     const bool direct = (rs_c == 1);
     if constexpr (sizeof(T) == 8) {
@@ -205,7 +227,7 @@ int herk_blocks(bool lower, int64_t m, int64_t kk, T alpha, const T* xb, const T
             prep.out_rpc = 2;
             rc = ozaki_multiply(&prep, m, yb, 1, 2 * kk, alpha, beta, c, 1, 2 * cs_c, s);
             ozaki_release_a(&prep, s);
-            if (rc) return rc;
+            if (rc || !herm) return rc;
             LaunchScope ls("herk_zero_diag", s);
             zero_diag_imag_kernel<T><<<grid_of(m), NT, 0, s>>>(m, c, rs_c, cs_c);
             return check_cuda(cudaGetLastError(), "herk zero diagonal");
@@ -235,7 +257,7 @@ int herk_blocks(bool lower, int64_t m, int64_t kk, T alpha, const T* xb, const T
             if (oz) rc = ozaki_multiply_rows(&prep, 2 * j0, 2 * w, &pb, alpha, 0.0, scratch, 1, 2 * w, s);
         }
         if (!oz) rc = real_gemm_cm<T>(2 * w, w, 2 * kk, alpha, xb + 2 * j0, 2 * m, yj, 2 * kk, T(0), scratch, 1, 2 * w, s);
-        if (!rc) rc = launch_merge<T>(w, w, j0, j0, lower, scratch, 2 * w, beta, c, rs_c, cs_c, s);
+        if (!rc) rc = launch_merge<T>(w, w, j0, j0, lower, scratch, 2 * w, beta, c, rs_c, cs_c, s, herm);
         if (!rc && prows > 0) {
             // panel: in place on C's real view (rows 2i, 2i+1; column stride 2 cs_c), or scratch + merge
             T* dst = direct ? c + 2 * (pr0 + j0 * cs_c) : scratch;
@@ -247,7 +269,8 @@ int herk_blocks(bool lower, int64_t m, int64_t kk, T alpha, const T* xb, const T
             if (!oz)
                 rc = real_gemm_cm<T>(2 * prows, w, 2 * kk, alpha, xb + 2 * pr0, 2 * m, yj, 2 * kk, dbeta, dst, 1, dcs,
                                      s);
-            if (!rc && !direct) rc = launch_merge<T>(prows, w, pr0, j0, lower, scratch, 2 * prows, beta, c, rs_c, cs_c, s);
+            if (!rc && !direct)
+                rc = launch_merge<T>(prows, w, pr0, j0, lower, scratch, 2 * prows, beta, c, rs_c, cs_c, s, herm);
         }
         if constexpr (sizeof(T) == 8) {
             if (oz) ozaki_release_b(&pb, s);
@@ -372,6 +395,56 @@ int chemm_dev(int side, int uplo, int herm, int conja, int transb, int64_t m, in
     return rc;
 }
 
+// complex syrk (b null) / syr2k: the stored triangle of C := alpha op(A)
+// op(A)^T + beta C, or alpha op(A) op(B)^T + alpha op(B) op(A)^T + beta C,
+// alpha and beta complex, no conjugate transposes (trans_t's 0x10 bit
+// conjugates its operand); the diagonal keeps its imaginary parts.  A beta
+// with an imaginary part scales the triangle first, and the products then
+// add to it.
+template <typename T>
+int csyr2k_dev(int uplo, int transa, int transb, int64_t m, int64_t k, const T* alpha, const T* a, int64_t rs_a,
+               int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, const T* beta, T* c, int64_t rs_c,
+               int64_t cs_c, int slices, cudaStream_t s)
+{
+    if (m <= 0) return GB_SUCCESS;
+    const bool lower = (uplo == GB_LOWER);
+    const bool nothing = (alpha[0] == T(0) && alpha[1] == T(0)) || k <= 0;
+    T rbeta = beta[0];
+    if (beta[1] != T(0) || nothing) {
+        LaunchScope ls("syrk_scale", s);
+        tri_scale_kernel<T><<<grid_of(m * m), NT, 0, s>>>(m, lower ? 1 : 0, beta[0], beta[1], c, rs_c, cs_c);
+        int rc = check_cuda(cudaGetLastError(), "syrk scale");
+        if (rc || nothing) return rc;
+        rbeta = T(1);
+    }
+    const bool two = (b != nullptr);
+    const bool ta = GB_IS_TRANS(transa), tb = GB_IS_TRANS(transb);
+    const int ca = (transa & 0x10) ? 1 : 0, cb = (transb & 0x10) ? 1 : 0;
+    const int64_t ars = ta ? cs_a : rs_a, acs = ta ? rs_a : cs_a;
+    const int64_t brs = tb ? cs_b : rs_b, bcs = tb ? rs_b : cs_b;
+    const int64_t kk = two ? 2 * k : k;
+    const size_t nx = (size_t)(4 * m * kk), ny = (size_t)(2 * kk * m);
+    T* ws = static_cast<T*>(dev_alloc(sizeof(T) * (nx + ny) + 256, s));
+    if (!ws) return GB_ERR_NOMEM;
+    T* xb = ws;
+    T* yb = ws + nx;
+    // X = alpha [op(A) | op(B)], Y = [op(B) | op(A)]^T: the packing of Y is a
+    // conjugate transpose, so it takes the operand's conjugation flipped
+    int rc = launch_pack_x<T>(m, k, a, ars, acs, ca, alpha, kk, 0, xb, s);
+    if (!rc && two) rc = launch_pack_x<T>(m, k, b, brs, bcs, cb, alpha, kk, k, xb, s);
+    if (!rc && two) rc = launch_pack_y<T>(m, k, b, brs, bcs, 1 - cb, kk, 0, yb, s);
+    if (!rc) rc = launch_pack_y<T>(m, k, a, ars, acs, 1 - ca, kk, two ? k : 0, yb, s);
+    if (!rc) rc = herk_blocks<T>(lower, m, kk, T(1), xb, yb, rbeta, c, rs_c, cs_c, slices, s, false);
+    dev_free(ws, s);
+    return rc;
+}
+
+template int csyr2k_dev<double>(int, int, int, int64_t, int64_t, const double*, const double*, int64_t, int64_t,
+                                const double*, int64_t, int64_t, const double*, double*, int64_t, int64_t, int,
+                                cudaStream_t);
+template int csyr2k_dev<float>(int, int, int, int64_t, int64_t, const float*, const float*, int64_t, int64_t,
+                               const float*, int64_t, int64_t, const float*, float*, int64_t, int64_t, int,
+                               cudaStream_t);
 template int cherk_dev<double>(int, int, int64_t, int64_t, double, const double*, int64_t, int64_t, double, double*,
                                int64_t, int64_t, int, cudaStream_t);
 template int cherk_dev<float>(int, int, int64_t, int64_t, float, const float*, int64_t, int64_t, float, float*,

@@ -164,6 +164,10 @@ template <typename T>
 int cherk_dev(int uplo, int transa, int64_t m, int64_t k, T alpha, const T* a, int64_t rs_a, int64_t cs_a, T beta,
               T* c, int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s);
 template <typename T>
+int csyr2k_dev(int uplo, int transa, int transb, int64_t m, int64_t k, const T* alpha, const T* a, int64_t rs_a,
+               int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, const T* beta, T* c, int64_t rs_c,
+               int64_t cs_c, int slices, cudaStream_t s);
+template <typename T>
 int cher2k_dev(int uplo, int transa, int transb, int64_t m, int64_t k, const T* alpha, const T* a, int64_t rs_a,
                int64_t cs_a, const T* b, int64_t rs_b, int64_t cs_b, T beta, T* c, int64_t rs_c, int64_t cs_c,
                int slices, cudaStream_t s);

@@ -187,6 +187,23 @@ void zher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_in
 void cher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
              const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
              const gb_f77_int* ldb, const float* beta, gb_scomplex* c, const gb_f77_int* ldc);
+/* replace zsyrk_ / csyrk_ (frame/compat/bla_syrk.c:45-121) and zsyr2k_ /
+   csyr2k_ (frame/compat/bla_syr2k.c:45-128); checks
+   frame/compat/check/bla_syrk_check.h:37-84 and bla_syr2k_check.h:37-84
+   (complex: trans N or T, 'C' is info 2); the BLAS early return when nothing
+   is added and beta == 1 */
+void zsyrk_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+            const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* beta,
+            gb_dcomplex* c, const gb_f77_int* ldc);
+void csyrk_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+            const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* beta,
+            gb_scomplex* c, const gb_f77_int* ldc);
+void zsyr2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+             const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* b,
+             const gb_f77_int* ldb, const gb_dcomplex* beta, gb_dcomplex* c, const gb_f77_int* ldc);
+void csyr2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
+             const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
+             const gb_f77_int* ldb, const gb_scomplex* beta, gb_scomplex* c, const gb_f77_int* ldc);
 void zhemm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_int* m, const gb_f77_int* n,
             const gb_dcomplex* alpha, const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* b,
             const gb_f77_int* ldb, const gb_dcomplex* beta, gb_dcomplex* c, const gb_f77_int* ldc);
@@ -343,6 +360,20 @@ void bli_ctrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t dia
    bli_chemm, bli_zsymm / bli_csymm and bli_dsyr2k (frame/3/bli_l3_tapi_ex.c;
    prototypes frame/3/bli_l3_tapi_ex.h:62-168): herk takes real alpha and
    beta, her2k a real beta; hemm / symm take conja (conjugates A) and transb */
+/* replace bli_zsyrk / bli_csyrk and bli_zsyr2k / bli_csyr2k (the same
+   files): complex alpha and beta, C's stored triangle only */
+void bli_zsyrk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const gb_dcomplex* alpha,
+               const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* beta, gb_dcomplex* c,
+               gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_csyrk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const gb_scomplex* alpha,
+               const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* beta, gb_scomplex* c,
+               gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_zsyr2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b,
+                gb_inc_t rs_b, gb_inc_t cs_b, const gb_dcomplex* beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c);
+void bli_csyr2k(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* b,
+                gb_inc_t rs_b, gb_inc_t cs_b, const gb_scomplex* beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c);
 void bli_zherk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const double* alpha,
                const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const double* beta, gb_dcomplex* c,
                gb_inc_t rs_c, gb_inc_t cs_c);
@@ -579,6 +610,22 @@ int gb_ctrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
 
 /* Device-pointer forms of zherk, zher2k, zhemm, zsymm, dtrmm3 and dsyr2k
    (asynchronous on the stream). */
+/* complex syrk / syr2k on device pointers: the products on herk's block-real
+   form (Ozaki for double complex when the library's level-3 mode selects it) */
+int gb_zsyrk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, gb_dcomplex alpha,
+                 const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex beta, gb_dcomplex* c,
+                 gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+int gb_csyrk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, gb_scomplex alpha,
+                 const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_scomplex beta, gb_scomplex* c,
+                 gb_inc_t rs_c, gb_inc_t cs_c, void* stream);
+int gb_zsyr2k_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                  gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* b,
+                  gb_inc_t rs_b, gb_inc_t cs_b, gb_dcomplex beta, gb_dcomplex* c, gb_inc_t rs_c, gb_inc_t cs_c,
+                  void* stream);
+int gb_csyr2k_dev(gb_uplo_t uploc, gb_trans_t transa, gb_trans_t transb, gb_dim_t m, gb_dim_t k,
+                  gb_scomplex alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* b,
+                  gb_inc_t rs_b, gb_inc_t cs_b, gb_scomplex beta, gb_scomplex* c, gb_inc_t rs_c, gb_inc_t cs_c,
+                  void* stream);
 int gb_zherk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, double alpha,
                  const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, double beta, gb_dcomplex* c,
                  gb_inc_t rs_c, gb_inc_t cs_c, void* stream);

@@ -1,4 +1,5 @@
-"""zherk / cherk, zher2k / cher2k, zhemm / chemm, zsymm / csymm and dsyr2k on
+"""zherk / cherk, zher2k / cher2k, zsyrk / csyrk, zsyr2k / csyr2k, zhemm /
+chemm, zsymm / csymm and dsyr2k on
 the GPU (gb_hermitian.cu, gb_level3x.cu) against the CPU oracle: the stored
 triangle within the componentwise bound of the products, the other triangle
 bit-for-bit untouched, the imaginary parts of C's diagonal zero after herk /
@@ -330,3 +331,93 @@ def test_zherk_ozaki_nonfinite_keeps_other_triangle():
     bound = 8 * (k + 4) * U64 * ((oa @ oa.T) + np.abs(c0))
     d = np.abs(c - ref)[sub][t[sub]]
     assert np.all(d <= bound[sub][t[sub]])
+
+
+@pytest.mark.parametrize("dt", [np.complex128, np.complex64])
+@pytest.mark.parametrize("two", [False, True])
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("trans", ["N", "T"])
+@pytest.mark.parametrize("m,k", [(130, 90), (1, 17), (1100, 40)])
+def test_complex_syrk_syr2k_vs_numpy(dt, two, uplo, trans, m, k):
+    """C := alpha op(A) op(B)^T (+ alpha op(B) op(A)^T) + beta C on the stored triangle: complex
+    alpha and beta, no conjugation anywhere, the diagonal keeps its imaginary parts."""
+    a = _cplx((k, m) if trans == "T" else (m, k), 11, dt)
+    b = _cplx(a.shape, 12, dt)
+    c0 = _cplx((m, m), 13, dt)
+    alpha, beta = 0.75 - 0.5j, -1.25 + 0.25j
+    c = c0.copy(order="F")
+    if two:
+        blas.zsyr2k(uplo, trans, m, k, alpha, a, a.shape[0], b, b.shape[0], beta, c, m)
+    else:
+        blas.zsyrk(uplo, trans, m, k, alpha, a, a.shape[0], beta, c, m)
+    A, B, C0 = (x.astype(np.complex128) for x in (a, b, c0))
+    oa, ob = (A.T, B.T) if trans == "T" else (A, B)
+    if two:
+        ref = alpha * (oa @ ob.T) + alpha * (ob @ oa.T) + beta * C0
+        g = 2 * abs(alpha) * (np.abs(oa) @ np.abs(ob).T) + abs(beta) * np.abs(C0)
+    else:
+        ref = alpha * (oa @ oa.T) + beta * C0
+        g = abs(alpha) * (np.abs(oa) @ np.abs(oa).T) + abs(beta) * np.abs(C0)
+    eps = U64 if dt == np.complex128 else U32
+    _check_triangle(c.astype(np.complex128), ref, C0, 8 * (2 * k + 4) * eps * g + 1e-300, uplo == "L")
+    if m > 1:
+        assert np.any(c.diagonal().imag != 0)
+
+
+def test_zsyrk_beta_forms_early_return_and_error_exit():
+    m, k = 200, 50
+    a = _cplx((m, k), 14)
+    c0 = _cplx((m, m), 15)
+    low = _tri(True, m)
+    # beta = 0 with NaN in C: the stored triangle is written without reading it
+    c = c0.copy(order="F")
+    c[low] = np.nan
+    blas.zsyrk("L", "N", m, k, 1.0, a, m, 0.0, c, m)
+    assert np.all(np.isfinite(c[low]))
+    ref = a @ a.T
+    g = np.abs(a) @ np.abs(a).T
+    assert np.all(np.abs(c - ref)[low] <= 8 * (k + 4) * U64 * g[low])
+    # alpha = 0, beta = 1: the BLAS early return leaves C as it is
+    c = c0.copy(order="F")
+    blas.zsyrk("U", "T", m, k, 0.0, a, k, 1.0, c, m)
+    assert np.array_equal(c, c0)
+    # alpha = 0, complex beta: the triangle scaled, the rest untouched
+    c = c0.copy(order="F")
+    blas.zsyrk("U", "N", m, k, 0.0, a, m, 0.5 + 2.0j, c, m)
+    up = _tri(False, m)
+    assert np.allclose(c[up], (0.5 + 2.0j) * c0[up], rtol=4 * U64, atol=0)
+    assert np.array_equal(c[~up], c0[~up])
+
+
+def test_zsyr2k_ozaki_and_device_strides():
+    """The precision form (double complex under the Ozaki mode) and gb_csyr2k_dev on a row-major
+    C with transposed operands."""
+    torch = pytest.importorskip("torch")
+    m, k = 700, 300
+    a = _cplx((m, k), 16)
+    b = _cplx((m, k), 17)
+    c0 = _cplx((m, m), 18)
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 8)
+    c = c0.copy(order="F")
+    blas.zsyr2k("L", "N", m, k, 1.0 + 1.0j, a, m, b, m, 2.0 - 1.0j, c, m)
+    ref = (1.0 + 1.0j) * (a @ b.T + b @ a.T) + (2.0 - 1.0j) * c0
+    g = 2 * np.sqrt(2) * (np.abs(a) @ np.abs(b).T) + np.sqrt(5) * np.abs(c0)
+    _check_triangle(c, ref, c0, 64 * U64 * g + 1e-300, True)
+    blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+    L = _lib.load()
+    n, kk = 260, 70
+    at = _cplx((kk, n), 19, np.complex64)  # op(A) = A^T, A stored k x n column-major
+    bt = _cplx((kk, n), 20, np.complex64)
+    cr = _cplx((n, n), 21, np.complex64)
+    A = torch.from_numpy(np.ascontiguousarray(at.T).view(np.float32)).cuda()  # column-major at: rs 1, cs kk
+    B = torch.from_numpy(np.ascontiguousarray(bt.T).view(np.float32)).cuda()
+    Cd = torch.from_numpy(np.ascontiguousarray(cr).view(np.float32)).cuda()  # row-major C: rs n, cs 1
+    al, be = _lib.SComplex(0.5, 0.25), _lib.SComplex(-1.0, 0.0)
+    assert L.gb_csyr2k_dev(0x60, 0x08, 0x08, n, kk, al, A.data_ptr(), 1, kk, B.data_ptr(), 1, kk, be,
+                           Cd.data_ptr(), n, 1, None) == 0
+    assert L.gb_synchronize() == 0
+    got = Cd.cpu().numpy().view(np.complex64).astype(np.complex128)
+    AT, BT, C0 = at.T.astype(np.complex128), bt.T.astype(np.complex128), cr.astype(np.complex128)
+    ref = (0.5 + 0.25j) * (AT @ BT.T + BT @ AT.T) - C0
+    g = 2 * (np.abs(AT) @ np.abs(BT).T) + np.abs(C0)
+    _check_triangle(got, ref, C0, 8 * (2 * kk + 4) * U32 * g, False)
