@@ -93,6 +93,16 @@ def ztrsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
 ctrsm = ztrsm
 
 
+def ztrmm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
+    """Complex trmm on complex128 (ztrmm_) or complex64 (ctrmm_) Fortran-order arrays, by b's dtype."""
+    fn = _lib.load().ztrmm_ if b.dtype == np.complex128 else _lib.load().ctrmm_
+    al = _cscalar(alpha, b.dtype)
+    fn(_c(side), _c(uplo), _c(transa), _c(diag), _i(m), _i(n), _p(al), _p(a), _i(lda), _p(b), _i(ldb))
+
+
+ctrmm = ztrmm
+
+
 def _real_dtype(c):
     return np.float64 if c.dtype == np.complex128 else np.float32
 

@@ -870,6 +870,31 @@ int cher2k_host(int uplo, int transa, int transb, int64_t m, int64_t k, const T*
     return finish(s, where);
 }
 
+// complex trmm: B up (read unless alpha == 0) and back, A up
+template <typename T>
+int ctrmm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const T* alpha, const T* a,
+               int64_t rs_a, int64_t cs_a, T* b, int64_t rs_b, int64_t cs_b, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const size_t esz = 2 * sizeof(T);
+    const int64_t na = (side == GB_LEFT) ? m : n;
+    const bool nz = !(alpha[0] == T(0) && alpha[1] == T(0));
+    Staged& B = bufs.next();
+    if ((rc = stage_in(b, m, n, rs_b, cs_b, esz, nz, &B, s))) return rc;
+    Staged& A = bufs.next();
+    if (nz && (rc = stage_in(a, na, na, rs_a, cs_a, esz, true, &A, s))) return rc;
+    const int slices = (sizeof(T) == 8) ? level3_slices() : 0;
+    if ((rc = ctrmm_dev<T>(side, uplo, transa, diag, m, n, alpha, reinterpret_cast<const T*>(A.origin), A.rs, A.cs,
+                           reinterpret_cast<T*>(B.origin), B.rs, B.cs, slices, s)))
+        return rc;
+    if ((rc = stage_out(b, m, n, rs_b, cs_b, esz, B, s))) return rc;
+    return finish(s, where);
+}
+
 // complex syrk (b null) / syr2k, the same staging as herk / her2k
 template <typename T>
 int csyr2k_host(int uplo, int transa, int transb, int64_t m, int64_t k, const T* alpha, const T* a, int64_t rs_a,
@@ -1102,6 +1127,36 @@ void her2k_blas(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77
     const int t = map_trans(*trans);
     cher2k_host<T>(lsame(*uploc, 'L') ? GB_LOWER : GB_UPPER, t, t, *m, *k, &alpha->real, &a->real, 1, *lda,
                    &b->real, 1, *ldb, *beta, &c->real, 1, *ldc, name);
+}
+
+// complex trmm (frame/compat/bla_trmm.c:45-121, checks
+// frame/compat/check/bla_trmm_check.h:37-86)
+template <typename T, typename C>
+void ctrmm_blas(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+                const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const C* alpha, const C* a,
+                const gb_f77_int* lda, C* b, const gb_f77_int* ldb, const char* xname, const char* name)
+{
+    const bool left = lsame(*side, 'L'), right = lsame(*side, 'R');
+    const bool lower = lsame(*uploa, 'L'), upper = lsame(*uploa, 'U');
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T'), conja = lsame(*transa, 'C');
+    const bool unita = lsame(*diaga, 'U'), nonua = lsame(*diaga, 'N');
+    const int nrowa = left ? *m : *n;
+    int info = 0;
+    if (!left && !right) info = 1;
+    else if (!lower && !upper) info = 2;
+    else if (!nota && !ta && !conja) info = 3;
+    else if (!unita && !nonua) info = 4;
+    else if (*m < 0) info = 5;
+    else if (*n < 0) info = 6;
+    else if (*lda < (nrowa > 1 ? nrowa : 1)) info = 9;
+    else if (*ldb < (*m > 1 ? *m : 1)) info = 11;
+    if (info) {
+        call_xerbla(xname, info);
+        return;
+    }
+    ctrmm_host<T>(left ? GB_LEFT : GB_RIGHT, lower ? GB_LOWER : GB_UPPER, map_trans(*transa),
+                  unita ? GB_UNIT_DIAG : GB_NONUNIT_DIAG, *m, *n, &alpha->real, &a->real, 1, *lda, &b->real, 1, *ldb,
+                  name);
 }
 
 // complex syrk / syr2k (frame/compat/bla_syrk.c:45-121, bla_syr2k.c:45-128;
@@ -1354,6 +1409,20 @@ void zher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_in
              const gb_f77_int* ldb, const double* beta, gb_dcomplex* c, const gb_f77_int* ldc)
 {
     her2k_blas<double, gb_dcomplex>(uploc, trans, m, k, alpha, a, lda, b, ldb, beta, c, ldc, "ZHER2K");
+}
+
+void ztrmm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const gb_dcomplex* alpha,
+            const gb_dcomplex* a, const gb_f77_int* lda, gb_dcomplex* b, const gb_f77_int* ldb)
+{
+    ctrmm_blas<double, gb_dcomplex>(side, uploa, transa, diaga, m, n, alpha, a, lda, b, ldb, "ZTRMM ", "ZTRMM");
+}
+
+void ctrmm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const gb_scomplex* alpha,
+            const gb_scomplex* a, const gb_f77_int* lda, gb_scomplex* b, const gb_f77_int* ldb)
+{
+    ctrmm_blas<float, gb_scomplex>(side, uploa, transa, diaga, m, n, alpha, a, lda, b, ldb, "CTRMM ", "CTRMM");
 }
 
 void zsyrk_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
@@ -1814,6 +1883,22 @@ void bli_ctrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t dia
 
 // frame/3/bli_l3_tapi_ex.c herk / her2k / hemm / symm / syr2k (prototypes
 // frame/3/bli_l3_tapi_ex.h:62-168)
+void bli_ztrmm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+               const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b,
+               gb_inc_t rs_b, gb_inc_t cs_b)
+{
+    ctrmm_host<double>(side, uploa, transa, diaga, m, n, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                       "bli_ztrmm");
+}
+
+void bli_ctrmm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+               const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_scomplex* b,
+               gb_inc_t rs_b, gb_inc_t cs_b)
+{
+    ctrmm_host<float>(side, uploa, transa, diaga, m, n, &alpha->real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
+                      "bli_ctrmm");
+}
+
 void bli_zsyrk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const gb_dcomplex* alpha,
                const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* beta, gb_dcomplex* c,
                gb_inc_t rs_c, gb_inc_t cs_c)
@@ -2268,6 +2353,28 @@ int gb_ctrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
     if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_ctrsm_dev", "negative dimension");
     return gb::ctrsm_dev(side, uploa, transa, diaga, m, n, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
                          pick_stream(stream));
+}
+
+int gb_ztrmm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+                 gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b, gb_inc_t rs_b,
+                 gb_inc_t cs_b, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_ztrmm_dev", "negative dimension");
+    return gb::ctrmm_dev<double>(side, uploa, transa, diaga, m, n, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b,
+                                 cs_b, gb::level3_slices(), pick_stream(stream));
+}
+
+int gb_ctrmm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+                 gb_scomplex alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_scomplex* b, gb_inc_t rs_b,
+                 gb_inc_t cs_b, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_ctrmm_dev", "negative dimension");
+    return gb::ctrmm_dev<float>(side, uploa, transa, diaga, m, n, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b,
+                                cs_b, 0, pick_stream(stream));
 }
 
 int gb_zsyrk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, gb_dcomplex alpha, const gb_dcomplex* a,

@@ -465,4 +465,92 @@ int ctrsm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, co
     return xtrsm_dev<float>(side, uplo, transa, diag, m, n, alpha, a, rs_a, cs_a, b, rs_b, cs_b, 0, s);
 }
 
+namespace {
+
+// the na x na uplo triangle of A (strides in complex elements; the unit
+// diagonal when unit) as a full column-major complex matrix, zeros outside it
+template <typename R>
+__global__ void __launch_bounds__(NT) ctri_full_kernel(int64_t na, int lower, int unit, const R* __restrict__ a,
+                                                      int64_t rs, int64_t cs, R* __restrict__ out)
+{
+    const int64_t total = na * na;
+    for (int64_t e = (int64_t)blockIdx.x * NT + threadIdx.x; e < total; e += (int64_t)gridDim.x * NT) {
+        const int64_t j = e / na, i = e - j * na;
+        R re = R(0), im = R(0);
+        if (i == j && unit) {
+            re = R(1);
+        } else if (lower ? (i >= j) : (i <= j)) {
+            const R* p = a + 2 * (i * rs + j * cs);
+            re = p[0];
+            im = p[1];
+        }
+        out[2 * e] = re;
+        out[2 * e + 1] = im;
+    }
+}
+
+// the packed column-major m x n complex matrix into B (strides rs, cs)
+template <typename R>
+__global__ void __launch_bounds__(NT) cscatter_kernel(int64_t m, int64_t n, const R* __restrict__ in,
+                                                     R* __restrict__ b, int64_t rs, int64_t cs)
+{
+    const int64_t total = m * n;
+    for (int64_t e = (int64_t)blockIdx.x * NT + threadIdx.x; e < total; e += (int64_t)gridDim.x * NT) {
+        const int64_t j = e / m, i = e - j * m;
+        R* p = b + 2 * (i * rs + j * cs);
+        p[0] = in[2 * e];
+        p[1] = in[2 * e + 1];
+    }
+}
+
+}  // namespace
+
+// complex trmm: B := alpha op(A) B (left, A m x m) or alpha B op(A) (right,
+// A n x n), A triangular in its uplo triangle, op N, T, C or conjugate-only.
+// The triangle goes into a full matrix, one complex gemm (the block-real
+// product, Ozaki for double complex when slices > 0) writes a scratch, and
+// the scratch is scattered back into B.
+template <typename R>
+int ctrmm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const R* alpha, const R* a,
+              int64_t rs_a, int64_t cs_a, R* b, int64_t rs_b, int64_t cs_b, int slices, cudaStream_t s)
+{
+    if (m <= 0 || n <= 0) return GB_SUCCESS;
+    if (alpha[0] == R(0) && alpha[1] == R(0)) {
+        LaunchScope ls("ztrmm_zero", s);
+        zscal_kernel<R><<<grid_of(m * n), NT, 0, s>>>(m, n, R(0), R(0), reinterpret_cast<typename Cx<R>::T*>(b),
+                                                      rs_b, cs_b);
+        return check_cuda(cudaGetLastError(), "ztrmm zero");
+    }
+    const bool left = (side == GB_LEFT);
+    const int64_t na = left ? m : n;
+    R* full = static_cast<R*>(dev_alloc(sizeof(R) * (size_t)(2 * na * na + 2 * m * n), s));
+    if (!full) return GB_ERR_NOMEM;
+    R* tmp = full + 2 * na * na;
+    int rc;
+    {
+        LaunchScope ls("ztrmm_tri_full", s);
+        ctri_full_kernel<R><<<grid_of(na * na), NT, 0, s>>>(na, uplo == GB_LOWER ? 1 : 0, diag == GB_UNIT_DIAG ? 1 : 0,
+                                                             a, rs_a, cs_a, full);
+        rc = check_cuda(cudaGetLastError(), "ztrmm tri full");
+    }
+    const R zero[2] = {R(0), R(0)};
+    if (!rc)
+        rc = left ? cgemm_dev<R>(transa, GB_NO_TRANSPOSE, m, n, m, alpha, full, 1, na, b, rs_b, cs_b, zero, tmp, 1, m,
+                                 slices, s)
+                  : cgemm_dev<R>(GB_NO_TRANSPOSE, transa, m, n, n, alpha, b, rs_b, cs_b, full, 1, na, zero, tmp, 1, m,
+                                 slices, s);
+    if (!rc) {
+        LaunchScope ls("ztrmm_scatter", s);
+        cscatter_kernel<R><<<grid_of(m * n), NT, 0, s>>>(m, n, tmp, b, rs_b, cs_b);
+        rc = check_cuda(cudaGetLastError(), "ztrmm scatter");
+    }
+    dev_free(full, s);
+    return rc;
+}
+
+template int ctrmm_dev<double>(int, int, int, int, int64_t, int64_t, const double*, const double*, int64_t, int64_t,
+                               double*, int64_t, int64_t, int, cudaStream_t);
+template int ctrmm_dev<float>(int, int, int, int, int64_t, int64_t, const float*, const float*, int64_t, int64_t,
+                              float*, int64_t, int64_t, int, cudaStream_t);
+
 }  // namespace gb

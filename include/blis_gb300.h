@@ -187,6 +187,14 @@ void zher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_in
 void cher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
              const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
              const gb_f77_int* ldb, const float* beta, gb_scomplex* c, const gb_f77_int* ldc);
+/* replace ztrmm_ / ctrmm_ (frame/compat/bla_trmm.c:45-121, checks
+   frame/compat/check/bla_trmm_check.h:37-86) */
+void ztrmm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const gb_dcomplex* alpha,
+            const gb_dcomplex* a, const gb_f77_int* lda, gb_dcomplex* b, const gb_f77_int* ldb);
+void ctrmm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
+            const gb_f77_char* diaga, const gb_f77_int* m, const gb_f77_int* n, const gb_scomplex* alpha,
+            const gb_scomplex* a, const gb_f77_int* lda, gb_scomplex* b, const gb_f77_int* ldb);
 /* replace zsyrk_ / csyrk_ (frame/compat/bla_syrk.c:45-121) and zsyr2k_ /
    csyr2k_ (frame/compat/bla_syr2k.c:45-128); checks
    frame/compat/check/bla_syrk_check.h:37-84 and bla_syr2k_check.h:37-84
@@ -360,6 +368,14 @@ void bli_ctrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t dia
    bli_chemm, bli_zsymm / bli_csymm and bli_dsyr2k (frame/3/bli_l3_tapi_ex.c;
    prototypes frame/3/bli_l3_tapi_ex.h:62-168): herk takes real alpha and
    beta, her2k a real beta; hemm / symm take conja (conjugates A) and transb */
+/* replace bli_ztrmm / bli_ctrmm (frame/3/bli_l3_tapi_ex.c; trans_t may carry
+   the conjugation bit 0x10) */
+void bli_ztrmm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+               const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b,
+               gb_inc_t rs_b, gb_inc_t cs_b);
+void bli_ctrmm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+               const gb_scomplex* alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_scomplex* b,
+               gb_inc_t rs_b, gb_inc_t cs_b);
 /* replace bli_zsyrk / bli_csyrk and bli_zsyr2k / bli_csyr2k (the same
    files): complex alpha and beta, C's stored triangle only */
 void bli_zsyrk(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, const gb_dcomplex* alpha,
@@ -610,6 +626,14 @@ int gb_ctrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
 
 /* Device-pointer forms of zherk, zher2k, zhemm, zsymm, dtrmm3 and dsyr2k
    (asynchronous on the stream). */
+/* complex trmm on device pointers: the triangle as a full matrix, one complex
+   gemm into a scratch, scattered back into B */
+int gb_ztrmm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+                 gb_dcomplex alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
+int gb_ctrmm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
+                 gb_scomplex alpha, const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_scomplex* b,
+                 gb_inc_t rs_b, gb_inc_t cs_b, void* stream);
 /* complex syrk / syr2k on device pointers: the products on herk's block-real
    form (Ozaki for double complex when the library's level-3 mode selects it) */
 int gb_zsyrk_dev(gb_uplo_t uploc, gb_trans_t transa, gb_dim_t m, gb_dim_t k, gb_dcomplex alpha,

@@ -90,8 +90,8 @@ INTERPOSED_ROUTINES = {
     "dblat2": ["DGEMV", "DGER", "DTRSV"],
     "dblat3": ["DGEMM", "DSYMM", "DTRMM", "DTRSM", "DSYRK", "DSYR2K"],
     "sblat3": ["SGEMM", "STRSM"],
-    "zblat3": ["ZGEMM", "ZHEMM", "ZSYMM", "ZTRSM", "ZHERK", "ZSYRK", "ZHER2K", "ZSYR2K"],
-    "cblat3": ["CGEMM", "CHEMM", "CSYMM", "CTRSM", "CHERK", "CSYRK", "CHER2K", "CSYR2K"],
+    "zblat3": ["ZGEMM", "ZHEMM", "ZSYMM", "ZTRMM", "ZTRSM", "ZHERK", "ZSYRK", "ZHER2K", "ZSYR2K"],
+    "cblat3": ["CGEMM", "CHEMM", "CSYMM", "CTRMM", "CTRSM", "CHERK", "CSYRK", "CHER2K", "CSYR2K"],
 }
 
 

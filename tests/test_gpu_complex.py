@@ -230,3 +230,58 @@ def test_ctrsm_general_strides_and_alpha_zero():
     assert L.gb_synchronize() == 0
     bz = B.cpu().numpy().view(np.complex64).T
     assert (bz[:m] == 0).all() and np.isnan(bz[m:]).all()
+
+
+@pytest.mark.parametrize("dt", [np.complex128, np.complex64])
+@pytest.mark.parametrize("side", ["L", "R"])
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("trans", ["N", "T", "C"])
+@pytest.mark.parametrize("diag", ["N", "U"])
+def test_complex_trmm_vs_numpy(dt, side, uplo, trans, diag):
+    """ztrmm_ / ctrmm_: B := alpha op(tri(A)) B or alpha B op(tri(A)); the other triangle of A
+    (NaN here) and, with a unit diagonal, A's diagonal are not read."""
+    m, n = 150, 70
+    na = m if side == "L" else n
+    a = _cplx((na, na), 40, dt)
+    other = np.triu(np.ones((na, na), bool), 1) if uplo == "L" else np.tril(np.ones((na, na), bool), -1)
+    a[other] = np.nan
+    if diag == "U":
+        np.fill_diagonal(a, np.nan)
+    b0 = _cplx((m, n), 41, dt)
+    x = b0.copy(order="F")
+    alpha = 0.5 - 1.25j
+    blas.ztrmm(side, uplo, trans, diag, m, n, alpha, a, na, x, m)
+    t = _op(_ztri(np.where(np.isnan(a), 0, a).astype(np.complex128), uplo, diag), trans)
+    B0 = b0.astype(np.complex128)
+    ref = alpha * (t @ B0 if side == "L" else B0 @ t)
+    g = abs(alpha) * ((np.abs(t) @ np.abs(B0)) if side == "L" else (np.abs(B0) @ np.abs(t)))
+    eps = U64 if dt == np.complex128 else U32
+    assert np.all(np.abs(x.astype(np.complex128) - ref) <= 8 * (na + 4) * eps * g + 1e-300)
+
+
+def test_complex_trmm_alpha_zero_ozaki_and_device_strides():
+    torch = pytest.importorskip("torch")
+    m, n = 300, 120
+    a = _cplx((m, m), 42) + 2.0 * np.eye(m)
+    x = np.full((m, n), np.nan, dtype=np.complex128, order="F")
+    blas.ztrmm("L", "U", "N", "N", m, n, 0.0, a, m, x, m)  # alpha = 0: B := 0 without reading it
+    assert (x == 0).all()
+    b0 = _cplx((m, n), 43)
+    blas.set_dgemm_mode(blas.DGEMM_OZAKI, 8)
+    x = b0.copy(order="F")
+    blas.ztrmm("L", "L", "C", "N", m, n, 1.0, a, m, x, m)
+    t = np.conj(np.tril(a)).T
+    assert np.all(np.abs(x - t @ b0) <= 64 * U64 * (np.abs(t) @ np.abs(b0)))
+    blas.set_dgemm_mode(blas.DGEMM_NATIVE)
+    L = _lib.load()
+    ac = _cplx((n, n), 44, np.complex64)
+    bc = _cplx((m, n), 45, np.complex64)
+    A = torch.from_numpy(np.ascontiguousarray(ac.T).view(np.float32)).cuda()  # column-major A: rs 1, cs n
+    B = torch.from_numpy(np.ascontiguousarray(bc).view(np.float32)).cuda()  # row-major B: rs n, cs 1
+    al = _lib.SComplex(2.0, 0.0)
+    assert L.gb_ctrmm_dev(1, 0x60, 0x08, 0x100, m, n, al, A.data_ptr(), 1, n, B.data_ptr(), n, 1, None) == 0
+    assert L.gb_synchronize() == 0
+    got = B.cpu().numpy().view(np.complex64).astype(np.complex128)
+    t = _ztri(ac.astype(np.complex128), "U", "U").T
+    ref = 2.0 * (bc.astype(np.complex128) @ t)
+    assert np.all(np.abs(got - ref) <= 8 * (n + 4) * U32 * 2.0 * (np.abs(bc.astype(np.complex128)) @ np.abs(t)))
