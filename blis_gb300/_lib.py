@@ -166,6 +166,10 @@ def load(path=None):
     _sig(L, "gb_sgemm_dev", C.c_int, sg + [_vp])
     _sig(L, "gb_dtrsm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, _d, _vp, _i64, _i64, _vp, _i64, _i64, _vp])
     _sig(L, "gb_strsm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, _f, _vp, _i64, _i64, _vp, _i64, _i64, _vp])
+    _sig(L, "gb_zgemv_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, DComplex, _vp, _i64, _i64, _vp, _i64, DComplex,
+                                      _vp, _i64, _vp])
+    _sig(L, "gb_cgemv_dev", C.c_int, [C.c_int, C.c_int, _i64, _i64, SComplex, _vp, _i64, _i64, _vp, _i64, SComplex,
+                                      _vp, _i64, _vp])
     _sig(L, "gb_ztrmm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, DComplex, _vp, _i64, _i64, _vp, _i64, _i64,
                                                       _vp])
     _sig(L, "gb_ctrmm_dev", C.c_int, [C.c_int] * 4 + [_i64, _i64, SComplex, _vp, _i64, _i64, _vp, _i64, _i64,

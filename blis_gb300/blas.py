@@ -103,6 +103,16 @@ def ztrmm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
 ctrmm = ztrmm
 
 
+def zgemv(trans, m, n, alpha, a, lda, x, incx, beta, y, incy):
+    """zgemv_ / cgemv_ by y's dtype."""
+    fn = _lib.load().zgemv_ if y.dtype == np.complex128 else _lib.load().cgemv_
+    al, be = _cscalar(alpha, y.dtype), _cscalar(beta, y.dtype)
+    fn(_c(trans), _i(m), _i(n), _p(al), _p(a), _i(lda), _p(x), _i(incx), _p(be), _p(y), _i(incy))
+
+
+cgemv = zgemv
+
+
 def _real_dtype(c):
     return np.float64 if c.dtype == np.complex128 else np.float32
 

@@ -870,6 +870,43 @@ int cher2k_host(int uplo, int transa, int transb, int64_t m, int64_t k, const T*
     return finish(s, where);
 }
 
+// complex gemv: y up (read unless beta == 0) and back, A and x up when
+// something is added
+template <typename T>
+int cgemv_host(int transa, int conjx, int64_t m, int64_t n, const T* alpha, const T* a, int64_t rs_a, int64_t cs_a,
+               const T* x, int64_t incx, const T* beta, T* y, int64_t incy, const char* where)
+{
+    int rc = ensure_init();
+    if (rc) return rc;
+    const bool tr = GB_IS_TRANS(transa);
+    const int64_t my = tr ? n : m, nx = tr ? m : n;
+    if (my <= 0) return GB_SUCCESS;
+    cudaStream_t s = thread_stream();
+    Bufs bufs(s);
+    const size_t esz = 2 * sizeof(T);
+    Staged& Y = bufs.next();
+    if ((rc = stage_in(y, my, 1, incy, my, esz, !(beta[0] == T(0) && beta[1] == T(0)), &Y, s))) return rc;
+    const T* ad = nullptr;
+    const T* xd = nullptr;
+    int64_t ars = rs_a, acs = cs_a, xinc = incx;
+    if (nx > 0 && !(alpha[0] == T(0) && alpha[1] == T(0))) {
+        Staged& A = bufs.next();
+        Staged& X = bufs.next();
+        if ((rc = stage_in(a, m, n, rs_a, cs_a, esz, true, &A, s))) return rc;
+        if ((rc = stage_in(x, nx, 1, incx, nx, esz, true, &X, s))) return rc;
+        ad = reinterpret_cast<const T*>(A.origin);
+        xd = reinterpret_cast<const T*>(X.origin);
+        ars = A.rs;
+        acs = A.cs;
+        xinc = X.rs;
+    }
+    if ((rc = cgemv_dev<T>(transa, conjx, m, n, alpha, ad, ars, acs, xd, xinc, beta, reinterpret_cast<T*>(Y.origin),
+                           Y.rs, s)))
+        return rc;
+    if ((rc = stage_out(y, my, 1, incy, my, esz, Y, s))) return rc;
+    return finish(s, where);
+}
+
 // complex trmm: B up (read unless alpha == 0) and back, A up
 template <typename T>
 int ctrmm_host(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const T* alpha, const T* a,
@@ -1127,6 +1164,33 @@ void her2k_blas(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77
     const int t = map_trans(*trans);
     cher2k_host<T>(lsame(*uploc, 'L') ? GB_LOWER : GB_UPPER, t, t, *m, *k, &alpha->real, &a->real, 1, *lda,
                    &b->real, 1, *ldb, *beta, &c->real, 1, *ldc, name);
+}
+
+// complex gemv (frame/compat/bla_gemv.c:45-143, checks
+// frame/compat/check/bla_gemv_check.h:37-75)
+template <typename T, typename C>
+void cgemv_blas(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n, const C* alpha, const C* a,
+                const gb_f77_int* lda, const C* x, const gb_f77_int* incx, const C* beta, C* y,
+                const gb_f77_int* incy, const char* xname, const char* name)
+{
+    const bool nota = lsame(*transa, 'N'), ta = lsame(*transa, 'T'), conja = lsame(*transa, 'C');
+    int info = 0;
+    if (!nota && !ta && !conja) info = 1;
+    else if (*m < 0) info = 2;
+    else if (*n < 0) info = 3;
+    else if (*lda < (*m > 1 ? *m : 1)) info = 6;
+    else if (*incx == 0) info = 8;
+    else if (*incy == 0) info = 11;
+    if (info) {
+        call_xerbla(xname, info);
+        return;
+    }
+    const int t = map_trans(*transa);
+    const int64_t m0 = *m, n0 = *n;
+    const int64_t m_y = GB_IS_TRANS(t) ? n0 : m0, n_x = GB_IS_TRANS(t) ? m0 : n0;
+    if (m_y > 0 && n_x == 0) return;  // netlib quirk kept by frame/compat/bla_gemv.c:88-106
+    cgemv_host<T>(t, 0, m0, n0, &alpha->real, &a->real, 1, *lda, &blas_vec<C>(x, n_x, *incx)->real, *incx,
+                  &beta->real, const_cast<T*>(&blas_vec<C>(y, m_y, *incy)->real), *incy, name);
 }
 
 // complex trmm (frame/compat/bla_trmm.c:45-121, checks
@@ -1409,6 +1473,20 @@ void zher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_in
              const gb_f77_int* ldb, const double* beta, gb_dcomplex* c, const gb_f77_int* ldc)
 {
     her2k_blas<double, gb_dcomplex>(uploc, trans, m, k, alpha, a, lda, b, ldb, beta, c, ldc, "ZHER2K");
+}
+
+void zgemv_(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n, const gb_dcomplex* alpha,
+            const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* x, const gb_f77_int* incx,
+            const gb_dcomplex* beta, gb_dcomplex* y, const gb_f77_int* incy)
+{
+    cgemv_blas<double, gb_dcomplex>(transa, m, n, alpha, a, lda, x, incx, beta, y, incy, "ZGEMV ", "ZGEMV");
+}
+
+void cgemv_(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n, const gb_scomplex* alpha,
+            const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* x, const gb_f77_int* incx,
+            const gb_scomplex* beta, gb_scomplex* y, const gb_f77_int* incy)
+{
+    cgemv_blas<float, gb_scomplex>(transa, m, n, alpha, a, lda, x, incx, beta, y, incy, "CGEMV ", "CGEMV");
 }
 
 void ztrmm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
@@ -1883,6 +1961,22 @@ void bli_ctrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t dia
 
 // frame/3/bli_l3_tapi_ex.c herk / her2k / hemm / symm / syr2k (prototypes
 // frame/3/bli_l3_tapi_ex.h:62-168)
+void bli_zgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, const gb_dcomplex* alpha,
+               const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* x, gb_inc_t incx,
+               const gb_dcomplex* beta, gb_dcomplex* y, gb_inc_t incy)
+{
+    cgemv_host<double>(transa, conjx == GB_CONJUGATE, m, n, &alpha->real, &a->real, rs_a, cs_a, &x->real, incx,
+                       &beta->real, &y->real, incy, "bli_zgemv");
+}
+
+void bli_cgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, const gb_scomplex* alpha,
+               const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* x, gb_inc_t incx,
+               const gb_scomplex* beta, gb_scomplex* y, gb_inc_t incy)
+{
+    cgemv_host<float>(transa, conjx == GB_CONJUGATE, m, n, &alpha->real, &a->real, rs_a, cs_a, &x->real, incx,
+                      &beta->real, &y->real, incy, "bli_cgemv");
+}
+
 void bli_ztrmm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
                const gb_dcomplex* alpha, const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, gb_dcomplex* b,
                gb_inc_t rs_b, gb_inc_t cs_b)
@@ -2353,6 +2447,28 @@ int gb_ctrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
     if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_ctrsm_dev", "negative dimension");
     return gb::ctrsm_dev(side, uploa, transa, diaga, m, n, &alpha.real, &a->real, rs_a, cs_a, &b->real, rs_b, cs_b,
                          pick_stream(stream));
+}
+
+int gb_zgemv_dev(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, gb_dcomplex alpha, const gb_dcomplex* a,
+                 gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* x, gb_inc_t incx, gb_dcomplex beta, gb_dcomplex* y,
+                 gb_inc_t incy, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_zgemv_dev", "negative dimension");
+    return gb::cgemv_dev<double>(transa, conjx == GB_CONJUGATE, m, n, &alpha.real, &a->real, rs_a, cs_a, &x->real,
+                                 incx, &beta.real, &y->real, incy, pick_stream(stream));
+}
+
+int gb_cgemv_dev(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, gb_scomplex alpha, const gb_scomplex* a,
+                 gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* x, gb_inc_t incx, gb_scomplex beta, gb_scomplex* y,
+                 gb_inc_t incy, void* stream)
+{
+    int rc = gb::ensure_init();
+    if (rc) return rc;
+    if (m < 0 || n < 0) return gb::set_error(GB_ERR_ARG, "gb_cgemv_dev", "negative dimension");
+    return gb::cgemv_dev<float>(transa, conjx == GB_CONJUGATE, m, n, &alpha.real, &a->real, rs_a, cs_a, &x->real,
+                                incx, &beta.real, &y->real, incy, pick_stream(stream));
 }
 
 int gb_ztrmm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,

@@ -548,6 +548,128 @@ int ctrmm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, co
     return rc;
 }
 
+namespace {
+
+constexpr int GV_WARP_ROWS = NT / 32;  // output rows of a warp-per-row block
+
+// Partial sums of y' = op(A) x' over the column split blockIdx.y (columns
+// l0 .. l0 + chunk of op(A)): part[2 (s ly + i) + {0, 1}].  op(A)(i, l) =
+// A[i ers + l ecs] (conjugated when ca), x'(l) = x[l incx] (conjugated when
+// cx).  ROWS: one thread per output row, for op(A)'s rows contiguous in
+// memory (ers == 1: a warp reads 32 consecutive elements of one column);
+// otherwise one warp per output row with the lanes striding over l.
+template <typename R, bool ROWS>
+__global__ void __launch_bounds__(NT) cgemv_partial_kernel(int64_t ly, int64_t lx, int64_t chunk,
+                                                          const R* __restrict__ a, int64_t ers, int64_t ecs, int ca,
+                                                          const R* __restrict__ x, int64_t incx, int cx,
+                                                          R* __restrict__ part)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t i = ROWS ? (int64_t)blockIdx.x * NT + threadIdx.x
+                           : (int64_t)blockIdx.x * GV_WARP_ROWS + (threadIdx.x >> 5);
+    if (i >= ly) return;
+    const int64_t l0 = (int64_t)blockIdx.y * chunk;
+    const int64_t l1 = (l0 + chunk < lx) ? l0 + chunk : lx;
+    const R sa = ca ? R(-1) : R(1), sx = cx ? R(-1) : R(1);
+    R sr = R(0), si = R(0);
+    for (int64_t l = l0 + (ROWS ? 0 : lane); l < l1; l += (ROWS ? 1 : 32)) {
+        const R* p = a + 2 * (i * ers + l * ecs);
+        const R* q = x + 2 * (l * incx);
+        const R ar = p[0], ai = sa * p[1], xr = q[0], xi = sx * q[1];
+        sr += ar * xr - ai * xi;
+        si += ar * xi + ai * xr;
+    }
+    if (!ROWS) {
+        for (int off = 16; off > 0; off >>= 1) {
+            sr += __shfl_down_sync(0xffffffffu, sr, off);
+            si += __shfl_down_sync(0xffffffffu, si, off);
+        }
+        if (lane != 0) return;
+    }
+    R* o = part + 2 * ((int64_t)blockIdx.y * ly + i);
+    o[0] = sr;
+    o[1] = si;
+}
+
+// y(i) := alpha sum_s part(s, i) + beta y(i); beta = 0 does not read y, and
+// splits = 0 (nothing to add) leaves beta y
+template <typename R>
+__global__ void __launch_bounds__(NT) cgemv_combine_kernel(int64_t ly, int splits, const R* __restrict__ part,
+                                                          R alr, R ali, R ber, R bei, R* __restrict__ y, int64_t incy)
+{
+    for (int64_t i = (int64_t)blockIdx.x * NT + threadIdx.x; i < ly; i += (int64_t)gridDim.x * NT) {
+        R sr = R(0), si = R(0);
+        for (int sp = 0; sp < splits; ++sp) {
+            sr += part[2 * (sp * ly + i)];
+            si += part[2 * (sp * ly + i) + 1];
+        }
+        R* py = y + 2 * (i * incy);
+        R yr = alr * sr - ali * si, yi = alr * si + ali * sr;
+        if (!(ber == R(0) && bei == R(0))) {
+            const R cr = py[0], ci = py[1];
+            yr += ber * cr - bei * ci;
+            yi += ber * ci + bei * cr;
+        }
+        py[0] = yr;
+        py[1] = yi;
+    }
+}
+
+}  // namespace
+
+// complex gemv: y := alpha op(A) x' + beta y, op N, T, C or conjugate-only
+// (trans_t's bits 0x08, 0x10), x' = conj(x) when conjx; A m x n, strides in
+// complex elements.  Bandwidth-bound: op(A)'s columns split so that the grid
+// holds about four blocks per SM, partial sums in a scratch, one combine.
+template <typename R>
+int cgemv_dev(int transa, int conjx, int64_t m, int64_t n, const R* alpha, const R* a, int64_t rs_a, int64_t cs_a,
+              const R* x, int64_t incx, const R* beta, R* y, int64_t incy, cudaStream_t s)
+{
+    const bool tr = GB_IS_TRANS(transa);
+    const int64_t ly = tr ? n : m, lx = tr ? m : n;
+    if (ly <= 0) return GB_SUCCESS;
+    const bool nothing = lx <= 0 || (alpha[0] == R(0) && alpha[1] == R(0));
+    const int64_t ers = tr ? cs_a : rs_a, ecs = tr ? rs_a : cs_a;
+    const bool rows = (ers == 1);
+    int splits = 0;
+    R* part = nullptr;
+    int rc = GB_SUCCESS;
+    if (!nothing) {
+        const int sms = sm_count() > 0 ? sm_count() : 148;
+        const int64_t rb = rows ? (ly + NT - 1) / NT : (ly + GV_WARP_ROWS - 1) / GV_WARP_ROWS;
+        int64_t sp = (4 * (int64_t)sms + rb - 1) / rb;
+        const int64_t maxsp = (lx + 63) / 64;
+        if (sp > maxsp) sp = maxsp;
+        if (sp > 1024) sp = 1024;
+        if (sp < 1) sp = 1;
+        const int64_t chunk = (lx + sp - 1) / sp;
+        splits = (int)((lx + chunk - 1) / chunk);
+        part = static_cast<R*>(dev_alloc(sizeof(R) * (size_t)(2 * splits * ly), s));
+        if (!part) return GB_ERR_NOMEM;
+        LaunchScope ls("cgemv_partial", s);
+        const dim3 grid((unsigned)rb, (unsigned)splits);
+        const int ca = (transa & 0x10) ? 1 : 0;
+        if (rows)
+            cgemv_partial_kernel<R, true><<<grid, NT, 0, s>>>(ly, lx, chunk, a, ers, ecs, ca, x, incx, conjx, part);
+        else
+            cgemv_partial_kernel<R, false><<<grid, NT, 0, s>>>(ly, lx, chunk, a, ers, ecs, ca, x, incx, conjx, part);
+        rc = check_cuda(cudaGetLastError(), "cgemv partial");
+    }
+    if (!rc) {
+        LaunchScope ls("cgemv_combine", s);
+        cgemv_combine_kernel<R><<<grid_of(ly), NT, 0, s>>>(ly, splits, part, alpha[0], alpha[1], beta[0], beta[1], y,
+                                                          incy);
+        rc = check_cuda(cudaGetLastError(), "cgemv combine");
+    }
+    if (part) dev_free(part, s);
+    return rc;
+}
+
+template int cgemv_dev<double>(int, int, int64_t, int64_t, const double*, const double*, int64_t, int64_t,
+                               const double*, int64_t, const double*, double*, int64_t, cudaStream_t);
+template int cgemv_dev<float>(int, int, int64_t, int64_t, const float*, const float*, int64_t, int64_t, const float*,
+                              int64_t, const float*, float*, int64_t, cudaStream_t);
+
 template int ctrmm_dev<double>(int, int, int, int, int64_t, int64_t, const double*, const double*, int64_t, int64_t,
                                double*, int64_t, int64_t, int, cudaStream_t);
 template int ctrmm_dev<float>(int, int, int, int, int64_t, int64_t, const float*, const float*, int64_t, int64_t,

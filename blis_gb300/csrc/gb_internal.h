@@ -164,6 +164,9 @@ template <typename T>
 int cherk_dev(int uplo, int transa, int64_t m, int64_t k, T alpha, const T* a, int64_t rs_a, int64_t cs_a, T beta,
               T* c, int64_t rs_c, int64_t cs_c, int slices, cudaStream_t s);
 template <typename R>
+int cgemv_dev(int transa, int conjx, int64_t m, int64_t n, const R* alpha, const R* a, int64_t rs_a, int64_t cs_a,
+              const R* x, int64_t incx, const R* beta, R* y, int64_t incy, cudaStream_t s);
+template <typename R>
 int ctrmm_dev(int side, int uplo, int transa, int diag, int64_t m, int64_t n, const R* alpha, const R* a,
               int64_t rs_a, int64_t cs_a, R* b, int64_t rs_b, int64_t cs_b, int slices, cudaStream_t s);
 template <typename T>

@@ -15,7 +15,8 @@ L2 where the workload allows:
   dtrsm_16384     L/L/N/N, B entries (1+u) 2^e, e in [-20,20]: native and
                   Ozaki updates, sampled componentwise backward error
   level12x        dscal / dcopy / idamax at 2^28, dger 32768^2, dtrsv 16384
-  complex         zgemm 4096^3 native / Ozaki, cgemm 4096^3 (8 mnk flop), ztrsm / ctrsm 4096^2
+  complex         zgemm 4096^3 native / Ozaki, cgemm 4096^3 (8 mnk flop), ztrsm / ctrsm 4096^2,
+                  zgemv / cgemv 16384^2
                   native / Ozaki updates (4 m^2 n flop)
   level3x         dtrmm 8192x4096 (m^2 n), dsyrk n=k=8192 (n^2 k), dsymm
                   8192x4096 (2 m^2 n): native FP64 and Ozaki (7 slices)
@@ -538,6 +539,22 @@ def run_complex(out):
     copy_ms = _timer(lambda: xc.copy_(bc), reps=3, warmup=1)
     out.append({"workload": "ctrsm_%dx%d" % (n, n), "form": "fp32_default_dispatch", "ms": ms - copy_ms,
                 "tflops": 4.0 * n ** 3 / (ms - copy_ms) / 1e9})
+    # zgemv / cgemv N and T on a 16384 x 16384 column-major A (8192 when small): HBM-bound, the
+    # algorithmic bytes are A's once
+    g = 8192 if SMALL else 16384
+    for dt, name, fn_name, S in ((torch.complex128, "zgemv", "gb_zgemv_dev", _lib.DComplex),
+                                 (torch.complex64, "cgemv", "gb_cgemv_dev", _lib.SComplex)):
+        ag = torch.complex(_mat(g, g, seed=79), _mat(g, g, seed=80)).to(dt)
+        xg = torch.complex(_mat(g, 1, seed=81), _mat(g, 1, seed=82)).to(dt).view(-1)
+        yg = torch.zeros(g, dtype=dt, device="cuda")
+        fn_dev = getattr(L, fn_name)
+        for tr, tname in ((0, "N"), (8, "T")):
+            fn = lambda: _lib.check(fn_dev(tr, 0, g, g, S(1.0, 0.5), ag.data_ptr(), 1, g, xg.data_ptr(), 1,
+                                           S(0.0, 0.0), yg.data_ptr(), 1, _stream()), name)
+            ms = _timer(fn, reps=5, warmup=2)
+            out.append({"workload": "%s_%s_%d" % (name, tname, g), "ms": ms,
+                        "gbs": ag.element_size() * g * g / ms / 1e6})
+        del ag
 
 
 def run_hermitian(out):

@@ -187,6 +187,15 @@ void zher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_in
 void cher2k_(const gb_f77_char* uploc, const gb_f77_char* trans, const gb_f77_int* m, const gb_f77_int* k,
              const gb_scomplex* alpha, const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* b,
              const gb_f77_int* ldb, const float* beta, gb_scomplex* c, const gb_f77_int* ldc);
+/* replace zgemv_ / cgemv_ (frame/compat/bla_gemv.c:45-143, checks
+   frame/compat/check/bla_gemv_check.h:37-75; negative increments address
+   the vectors from their far end) */
+void zgemv_(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n, const gb_dcomplex* alpha,
+            const gb_dcomplex* a, const gb_f77_int* lda, const gb_dcomplex* x, const gb_f77_int* incx,
+            const gb_dcomplex* beta, gb_dcomplex* y, const gb_f77_int* incy);
+void cgemv_(const gb_f77_char* transa, const gb_f77_int* m, const gb_f77_int* n, const gb_scomplex* alpha,
+            const gb_scomplex* a, const gb_f77_int* lda, const gb_scomplex* x, const gb_f77_int* incx,
+            const gb_scomplex* beta, gb_scomplex* y, const gb_f77_int* incy);
 /* replace ztrmm_ / ctrmm_ (frame/compat/bla_trmm.c:45-121, checks
    frame/compat/check/bla_trmm_check.h:37-86) */
 void ztrmm_(const gb_f77_char* side, const gb_f77_char* uploa, const gb_f77_char* transa,
@@ -368,6 +377,14 @@ void bli_ctrsm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t dia
    bli_chemm, bli_zsymm / bli_csymm and bli_dsyr2k (frame/3/bli_l3_tapi_ex.c;
    prototypes frame/3/bli_l3_tapi_ex.h:62-168): herk takes real alpha and
    beta, her2k a real beta; hemm / symm take conja (conjugates A) and transb */
+/* replace bli_zgemv / bli_cgemv (frame/2/bli_l2_tapi.c:43-127): trans_t may
+   carry the conjugation bit 0x10, conjx conjugates x */
+void bli_zgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, const gb_dcomplex* alpha,
+               const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* x, gb_inc_t incx,
+               const gb_dcomplex* beta, gb_dcomplex* y, gb_inc_t incy);
+void bli_cgemv(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, const gb_scomplex* alpha,
+               const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* x, gb_inc_t incx,
+               const gb_scomplex* beta, gb_scomplex* y, gb_inc_t incy);
 /* replace bli_ztrmm / bli_ctrmm (frame/3/bli_l3_tapi_ex.c; trans_t may carry
    the conjugation bit 0x10) */
 void bli_ztrmm(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,
@@ -626,6 +643,14 @@ int gb_ctrsm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t d
 
 /* Device-pointer forms of zherk, zher2k, zhemm, zsymm, dtrmm3 and dsyr2k
    (asynchronous on the stream). */
+/* complex gemv on device pointers: op(A)'s columns split over the grid,
+   partial sums in a scratch, one combine with alpha and beta */
+int gb_zgemv_dev(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, gb_dcomplex alpha,
+                 const gb_dcomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_dcomplex* x, gb_inc_t incx,
+                 gb_dcomplex beta, gb_dcomplex* y, gb_inc_t incy, void* stream);
+int gb_cgemv_dev(gb_trans_t transa, gb_conj_t conjx, gb_dim_t m, gb_dim_t n, gb_scomplex alpha,
+                 const gb_scomplex* a, gb_inc_t rs_a, gb_inc_t cs_a, const gb_scomplex* x, gb_inc_t incx,
+                 gb_scomplex beta, gb_scomplex* y, gb_inc_t incy, void* stream);
 /* complex trmm on device pointers: the triangle as a full matrix, one complex
    gemm into a scratch, scattered back into B */
 int gb_ztrmm_dev(gb_side_t side, gb_uplo_t uploa, gb_trans_t transa, gb_diag_t diaga, gb_dim_t m, gb_dim_t n,

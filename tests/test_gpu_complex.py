@@ -285,3 +285,72 @@ def test_complex_trmm_alpha_zero_ozaki_and_device_strides():
     t = _ztri(ac.astype(np.complex128), "U", "U").T
     ref = 2.0 * (bc.astype(np.complex128) @ t)
     assert np.all(np.abs(got - ref) <= 8 * (n + 4) * U32 * 2.0 * (np.abs(bc.astype(np.complex128)) @ np.abs(t)))
+
+
+def _strided(v, inc, dt):
+    """v laid out with increment inc (BLAS convention: a negative inc stores v from the far end)."""
+    n = len(v)
+    buf = np.full(1 + (n - 1) * abs(inc), np.nan, dtype=dt) if n else np.zeros(1, dt)
+    idx = np.arange(n) * abs(inc)
+    buf[idx if inc > 0 else idx[::-1]] = v
+    return buf
+
+
+def _unstrided(buf, n, inc):
+    idx = np.arange(n) * abs(inc)
+    return buf[idx if inc > 0 else idx[::-1]]
+
+
+@pytest.mark.parametrize("dt", [np.complex128, np.complex64])
+@pytest.mark.parametrize("trans", ["N", "T", "C"])
+@pytest.mark.parametrize("m,n", [(300, 200), (3, 5000), (5000, 3), (1, 1)])
+@pytest.mark.parametrize("incx,incy", [(1, 1), (-2, 3)])
+def test_complex_gemv_vs_numpy(dt, trans, m, n, incx, incy):
+    a = _cplx((m, n), 50, dt)
+    ly, lx = (n, m) if trans != "N" else (m, n)
+    xv = _cplx((lx,), 51, dt)
+    y0 = _cplx((ly,), 52, dt)
+    alpha, beta = 1.5 - 0.5j, -0.25 + 2.0j
+    xb, yb = _strided(xv, incx, dt), _strided(y0, incy, dt)
+    blas.zgemv(trans, m, n, alpha, a, m, xb, incx, beta, yb, incy)
+    got = _unstrided(yb, ly, incy).astype(np.complex128)
+    A, X, Y0 = a.astype(np.complex128), xv.astype(np.complex128), y0.astype(np.complex128)
+    op = _op(A, trans)
+    ref = alpha * (op @ X) + beta * Y0
+    g = abs(alpha) * (np.abs(op) @ np.abs(X)) + abs(beta) * np.abs(Y0)
+    eps = U64 if dt == np.complex128 else U32
+    assert np.all(np.abs(got - ref) <= 8 * (lx + 4) * eps * g)
+    if abs(incy) > 1:  # the gaps between y's elements are not written
+        gaps = np.ones(len(yb), bool)
+        gaps[np.arange(ly) * abs(incy)] = False
+        assert np.all(np.isnan(yb[gaps]))
+
+
+def test_complex_gemv_beta_zero_quirk_and_device_conj():
+    torch = pytest.importorskip("torch")
+    m, n = 400, 250
+    a = _cplx((m, n), 53)
+    xv = _cplx((n,), 54)
+    y = np.full(m, np.nan, dtype=np.complex128)
+    blas.zgemv("N", m, n, 1.0, a, m, xv, 1, 0.0, y, 1)  # beta = 0: y is not read
+    assert np.all(np.abs(y - a @ xv) <= 8 * (n + 4) * U64 * (np.abs(a) @ np.abs(xv)))
+    y0 = _cplx((m,), 55)
+    y = y0.copy()
+    blas.zgemv("N", m, 0, 1.0, a, m, xv, 1, 3.0, y, 1)  # nothing to add: y left as it is (netlib)
+    assert np.array_equal(y, y0)
+    # gb_cgemv_dev, A row-major (the warp-per-row kernel for op = N), conjugated x, conjugate-only A
+    L = _lib.load()
+    ac = _cplx((m, n), 56, np.complex64)
+    xc = _cplx((n,), 57, np.complex64)
+    yc = _cplx((m,), 58, np.complex64)
+    A = torch.from_numpy(np.ascontiguousarray(ac).view(np.float32)).cuda()
+    X = torch.from_numpy(xc.view(np.float32).copy()).cuda()
+    Y = torch.from_numpy(yc.view(np.float32).copy()).cuda()
+    assert L.gb_cgemv_dev(0x10, 0x10, m, n, _lib.SComplex(1.0, 1.0), A.data_ptr(), n, 1, X.data_ptr(), 1,
+                          _lib.SComplex(0.5, 0.0), Y.data_ptr(), 1, None) == 0
+    assert L.gb_synchronize() == 0
+    got = Y.cpu().numpy().view(np.complex64).astype(np.complex128)
+    A2, X2 = np.conj(ac.astype(np.complex128)), np.conj(xc.astype(np.complex128))
+    ref = (1.0 + 1.0j) * (A2 @ X2) + 0.5 * yc.astype(np.complex128)
+    g = np.sqrt(2) * (np.abs(A2) @ np.abs(X2)) + 0.5 * np.abs(yc)
+    assert np.all(np.abs(got - ref) <= 8 * (n + 4) * U32 * g)
