@@ -576,8 +576,11 @@ __global__ void __launch_bounds__(NT) cgemv_partial_kernel(int64_t ly, int64_t l
         const R* p = a + 2 * (i * ers + l * ecs);
         const R* q = x + 2 * (l * incx);
         const R ar = p[0], ai = sa * p[1], xr = q[0], xi = sx * q[1];
-        sr += ar * xr - ai * xi;
-        si += ar * xi + ai * xr;
+        // four fused multiply-adds per element (FP64 gemv is bound by the FP64 pipe)
+        sr = fma(ar, xr, sr);
+        sr = fma(-ai, xi, sr);
+        si = fma(ar, xi, si);
+        si = fma(ai, xr, si);
     }
     if (!ROWS) {
         for (int off = 16; off > 0; off >>= 1) {
